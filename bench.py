@@ -1,0 +1,304 @@
+"""Benchmark of the per-sample path-tracing hot path on one GB300.
+
+A step is one progressive frame (Renderer::render, render/renderer.rs:224)
+of the workload at its full resolution and samples per pixel. Default
+workload: the triangle-mesh scene (displaced icosphere of 1,310,720
+triangles in a 12-triangle Cornell box, 1024x1024, 64 spp, depth 8).
+
+Prints one JSON line:
+  value   Msamples/s over K frames, inputs resident in HBM, device time
+          (CUDA events around each frame on the renderer's stream; the L2 is
+          flushed with a 512 MB write between frames, outside the events)
+  e2e     the same metric through the public API (Renderer.render -> C ABI
+          rg_render) with the image copied back to host memory every frame
+  roofline, cpu_baseline, clocks, gpu_launches as described in the README of
+          the JSON keys below.
+
+--impl reference times the CPU restatement of the reference renderer (the
+reference crate cannot be built: no Rust toolchain) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "mesh": "triangle-mesh Cornell box: displaced icosphere 1,310,720 tris + 12 box tris, 1024x1024, 64 spp, depth 8",
+    "spheres": "random spheres (488 spheres), 400x225, 32 spp, depth 50",
+    "sdf": "Mandelbulb + torus SDFs, 2 media, 100 spheres, 1280x720, 128 spp, depth 16",
+}
+
+
+def load_workload(name: str):
+    from rayna_gb300 import presets
+    if name == "mesh":
+        return presets.cornell_mesh(level=8, seed=0)
+    if name == "spheres":
+        return presets.random_spheres(seed=0)
+    if name == "sdf":
+        return presets.sdf_volumes(seed=0)
+    raise ValueError(name)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]) if parts[3] not in ("[N/A]", "N/A") else 0.0,
+                             parts[5], parts[6], parts[7], parts[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [r[0] for r in rows]
+        busy = [r for r in rows if r[2] > 200.0] or rows
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, v in zip(names, r[3:]):
+                if v.lower().startswith("active"):
+                    reasons.add(k)
+        return {"sm_mhz": statistics.median(r[0] for r in busy), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "sm_mhz_min": min(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(name: str, threads: int, target_s: float = 15.0):
+    """Times the f64 CPU restatement of the reference renderer on a bounded
+    sample of the workload (same scene, camera, depth and spp; reduced
+    resolution), scaled to about `target_s` seconds of work."""
+    from oracle import binding as ob
+    from rayna_gb300.scene import RenderOpts, flatten
+    scene, cam, opts = load_workload(name)
+    flat = flatten(scene)
+    probe = RenderOpts(width=16, height=16, samples=opts.samples, ray_depth=opts.ray_depth)
+    st, _, _, secs = ob.render(flat, cam, probe, seed=1, frames=1, policy=ob.POLICY_REF_F64, threads=threads)
+    per_px = max(secs, 1e-3) / (16 * 16)
+    npx = int(max(256, min(opts.width * opts.height, target_s / per_px)))
+    side_w = max(16, int(round((npx * opts.width / opts.height) ** 0.5)))
+    side_h = max(16, int(round(npx / side_w)))
+    sample = RenderOpts(width=side_w, height=side_h, samples=opts.samples, ray_depth=opts.ray_depth)
+    st, _, _, secs = ob.render(flat, cam, sample, seed=2, frames=1, policy=ob.POLICY_REF_F64, threads=threads)
+    ns = side_w * side_h * opts.samples
+    return {"value": ns / secs / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"{side_w}x{side_h} px x {opts.samples} spp of the same scene and camera "
+                      f"({ns / 1e6:.2f} M samples, {secs:.1f} s), f64 oracle, {threads} threads"}, secs
+
+
+def run_reference(args, rank, world):
+    from oracle import binding as ob
+    name = args.workload
+    threads = ob.hardware_threads()
+    if rank != 0:
+        return
+    results = []
+    for i in range(args.warmup + args.steps):
+        res, secs = cpu_baseline(name, threads, target_s=args.ref_seconds)
+        if i >= args.warmup:
+            results.append(res)
+    v = statistics.median(r["value"] for r in results)
+    line = {
+        "impl": "reference", "metric": "Msamples/s", "value": v, "unit": "Msamples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[name]},
+        "cpu_baseline": {"value": v, "unit": "Msamples/s", "cores": threads, "kind": "port",
+                         "sample": results[-1]["sample"]},
+        "e2e": {"value": v, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference crate unbuildable here (no Rust toolchain); timed arm is its f64 C++ restatement",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world):
+    import ctypes as C
+
+    import torch
+
+    from rayna_gb300 import Renderer
+    from rayna_gb300 import _abi as A
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    scene, cam, opts = load_workload(args.workload)
+    stream = torch.cuda.current_stream()
+    forms = ["megakernel", "wavefront"] if args.form == "best" else [args.form]
+    results = {}
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    t_setup = time.perf_counter()
+    for form in forms:
+        try:
+            r = Renderer.new_from(scene, cam, opts, 0, form=form, stream=stream.cuda_stream, seed=1000 + rank)
+        except A.RaynaError as e:
+            results[form] = {"error": str(e)}
+            continue
+        # counting frame: algorithmic work per frame (node visits, primitive tests)
+        rc = Renderer.new_from(scene, cam, opts, 0, form=form, stream=stream.cuda_stream, seed=99, counters=True)
+        cst = rc.render().stats
+        rc.close()
+        lib, h = r._lib, r.handle
+        st = A.rg_render_stats()
+        for i in range(args.warmup):
+            A.check(lib, h, lib.rg_render_async(h, r.next_seed(), None, C.byref(st)))
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        rays = 0
+        torch.cuda.synchronize()
+        with ClockSampler(dev) as clk:
+            w0 = time.perf_counter()
+            for k in range(args.steps):
+                flush.fill_(float(k))
+                starts[k].record(stream)
+                A.check(lib, h, lib.rg_render_async(h, r.next_seed(), None, C.byref(st)))
+                ends[k].record(stream)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - w0
+        A.check(lib, h, lib.rg_sync_stats(h, C.byref(st)))
+        if dist:
+            dist.barrier()
+        ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        dev_s = sum(ms) / 1e3
+        if dist:
+            t = torch.tensor([dev_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dev_s = float(t.item())
+        samples = opts.width * opts.height * opts.samples
+        # end-to-end: the public call with the image read back to host memory every frame
+        r.clear_accumulation()
+        for _ in range(2):
+            r.render()
+        e0 = time.perf_counter()
+        for _ in range(args.steps):
+            out = r.render()
+        e2e_s = time.perf_counter() - e0
+        assert out.stats.error_flags == 0, out.stats.error_flags
+        results[form] = {
+            "msamples_s": samples * args.steps * world / dev_s / 1e6,
+            "ms_per_step": dev_s * 1e3 / args.steps,
+            "e2e_msamples_s": samples * args.steps * world / e2e_s / 1e6,
+            "mrays_s": cst.rays * args.steps * world / dev_s / 1e6,
+            "rays_per_frame": cst.rays, "node_visits": cst.node_visits, "prim_tests": cst.prim_tests,
+            "sdf_steps": cst.sdf_steps, "wall_s": wall, "clocks": clk.summary(),
+        }
+        r.close()
+    if rank != 0:
+        return
+    ok = {f: v for f, v in results.items() if "error" not in v}
+    best = max(ok, key=lambda f: ok[f]["msamples_s"])
+    b = ok[best]
+    hbm, peak_kind = measured_peaks()
+    npx = opts.width * opts.height
+    alg_bytes = 64 * b["node_visits"] + 48 * b["prim_tests"] + 32 * b["rays_per_frame"] + 12 * npx
+    achieved = alg_bytes / (b["ms_per_step"] / 1e3) / 1e9
+    line = {
+        "metric": "Msamples/s", "value": b["msamples_s"], "unit": "Msamples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "form": best, "l2": "flushed (512 MB write) between frames",
+                   "parallelism": f"replicas{world}"},
+        "e2e": {"value": b["e2e_msamples_s"], "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": npx * 12},
+        "mrays_s": b["mrays_s"],
+        "forms": {f: {k: v[k] for k in ("msamples_s", "mrays_s", "e2e_msamples_s", "ms_per_step")} if "error" not in v
+                  else v for f, v in results.items()},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_frame": alg_bytes},
+        "gpu_launches": args.steps,
+        "clocks": b["clocks"],
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        from oracle import binding as ob
+        cb, _ = cpu_baseline(args.workload, ob.hardware_threads(), target_s=args.ref_seconds)
+        line["cpu_baseline"] = cb
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=list(WORKLOADS), default="mesh")
+    ap.add_argument("--form", choices=["best", "megakernel", "wavefront"], default="best")
+    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        import __graft_entry__ as g
+        g.ensure_built()
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

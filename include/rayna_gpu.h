@@ -1,0 +1,309 @@
+/*
+ * rayna_gpu.h — C ABI of the GB300 (sm_103a) path-tracing library.
+ *
+ * This is the drop-in boundary for rayna_engine's CPU render call. Every entry
+ * point below replaces one method of `Renderer<Obj, Sky, Rng>`
+ * (rayna_engine/src/render/renderer.rs) or a piece of state it owns; the
+ * comment on each names the reference interface it stands in for.
+ *
+ * Conventions
+ *   - Every function returns rg_status; nothing unwinds across the boundary.
+ *     rg_last_error() gives a human-readable message for the last failure on
+ *     a handle (or the last handle-less failure when h == NULL).
+ *   - A handle is not thread-safe: calls on one handle must be serialised by
+ *     the caller, exactly as `&mut self` serialises them in the reference.
+ *     Separate handles may be used from separate threads.
+ *   - All scene arrays are host pointers owned by the caller; the library
+ *     copies what it needs during the call.
+ *   - Geometry and radiance are FP32 on the device. The camera is given in
+ *     f64 (the reference's `Number`) and its viewport is computed on the host
+ *     in f64 exactly like Camera::calculate_viewport, then rounded to f32.
+ *   - Images are laid out [x][y][rgb] (x-major), which is the memory order of
+ *     the reference's `Image` (an ndarray of shape (width, height),
+ *     rayna_engine/src/core/image.rs:24-25): pixel (x, y) starts at float
+ *     offset 3 * (x * height + y).
+ */
+#ifndef RAYNA_GPU_H
+#define RAYNA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RG_ABI_VERSION 1u
+
+/* Status codes. 0 is success. */
+typedef enum rg_status {
+    RG_OK = 0,
+    RG_INVALID_ARG = 1,          /* malformed descriptor, NaN/Inf parameter, bad size */
+    RG_UNSUPPORTED_VARIANT = 2,  /* a reference variant this library does not run (e.g. RenderMode other than PBR) */
+    RG_INVALID_CAMERA = 3,       /* Camera::calculate_viewport returned Err (scene/camera.rs:114-167) */
+    RG_OOM = 4,                  /* device or host allocation failed */
+    RG_CUDA_ERROR = 5,           /* a CUDA runtime call failed; see rg_last_error */
+    RG_QUEUE_OVERFLOW = 6,       /* a device queue or traversal stack ran out of space */
+    RG_STEP_LIMIT = 7,           /* a device loop hit its iteration budget */
+    RG_TIMEOUT = 8,              /* a bounded wait ran out */
+    RG_NO_DEVICE = 9,            /* no CUDA device is visible */
+    RG_NOT_READY = 10            /* call order violated (e.g. render before set_scene) */
+} rg_status;
+
+typedef struct rg_renderer* rg_handle;
+
+/* ------------------------------------------------------------------------ */
+/* Scene description (flattened StandardScene)                               */
+/* ------------------------------------------------------------------------ */
+
+/* Material kinds: MaterialInstance variants with a SolidTexture
+ * (rayna_engine/src/material/mod.rs:168-175, texture/solid.rs:28-30). */
+enum {
+    RG_MAT_LAMBERTIAN = 0,  /* LambertianMaterial { albedo }                      material/lambertian.rs */
+    RG_MAT_METAL = 1,       /* MetalMaterial { albedo, fuzz }                      material/metal.rs */
+    RG_MAT_DIELECTRIC = 2,  /* DielectricMaterial { albedo, refractive_index, density } material/dielectric.rs */
+    RG_MAT_ISOTROPIC = 3,   /* IsotropicMaterial { albedo, density }               material/isotropic.rs */
+    RG_MAT_LIGHT = 4        /* LightMaterial { emissive } (colour in `albedo`)     material/light.rs */
+};
+
+/* 32 bytes; the device material table holds these verbatim. */
+typedef struct rg_material {
+    uint32_t kind;
+    float albedo[3];          /* albedo, or emissive radiance for RG_MAT_LIGHT */
+    float fuzz;               /* metal */
+    float refractive_index;   /* dielectric */
+    float density;            /* dielectric / isotropic Beer term (material density) */
+    uint32_t reserved;        /* must be 0 */
+} rg_material;
+
+/* Skybox variants (rayna_engine/src/skybox/mod.rs:28-43). */
+enum {
+    RG_SKY_SIMPLE = 0,  /* SimpleSkybox: lerp(white, (0.5,0.7,1), 0.5*dir.y+0.5) */
+    RG_SKY_WHITE = 1,   /* WhiteSkybox */
+    RG_SKY_NONE = 2     /* NoSkybox (black) */
+};
+
+/* Constant-density medium: VolumetricObject (rayna_engine/src/object/volumetric.rs). */
+enum { RG_BOUNDARY_SPHERE = 0, RG_BOUNDARY_BOX = 1 };
+typedef struct rg_volume {
+    uint32_t boundary;  /* RG_BOUNDARY_SPHERE: a = centre, b[0] = radius; RG_BOUNDARY_BOX: a, b = two corners */
+    float a[3];
+    float b[3];
+    float density;      /* medium density (VolumetricObject::density) */
+    uint32_t material;  /* index into the material table */
+} rg_volume;
+
+/* Signed-distance functions that can cross the C ABI. The reference takes an
+ * arbitrary closure (mesh/isosurface/mod.rs:7-9); closures cannot cross an FFI,
+ * so RaymarchedIsosurfaceMesh is described by one of these kinds. */
+enum {
+    RG_SDF_SPHERE = 0,      /* params[0] = radius */
+    RG_SDF_TORUS = 1,       /* params[0] = major radius R, params[1] = minor radius r; axis = +y */
+    RG_SDF_MANDELBULB = 2   /* params[0] = power, params[1] = iterations, params[2] = scale (world units per unit bulb) */
+};
+typedef struct rg_sdf {
+    uint32_t kind;
+    float centre[3];
+    float params[4];
+    uint32_t max_iterations;  /* RaymarchedIsosurfaceMesh::max_iterations */
+    float epsilon;            /* RaymarchedIsosurfaceMesh::epsilon */
+    uint32_t material;
+} rg_sdf;
+
+/* A flattened scene. Object order (which decides exact-distance ties and the
+ * order of unbounded objects) is: spheres, standalone triangles, triangle
+ * meshes (by mesh id), boxes, volumes, SDFs. Global primitive ids, as
+ * reported by rg_query_rays, number the same arrays in the same order:
+ * spheres [0, ns), triangles [ns, ns+nt), boxes, volumes, SDFs. */
+typedef struct rg_scene_desc {
+    uint32_t n_spheres;
+    const float* spheres;            /* n x 4: centre xyz, radius */
+    const uint32_t* sphere_material; /* n */
+
+    uint32_t n_triangles;
+    const float* tri_vertices;       /* n x 3 x 3 */
+    const float* tri_normals;        /* n x 3 x 3, unit length (Triangle::new asserts it) */
+    const uint32_t* tri_material;    /* n */
+    const int32_t* tri_mesh;         /* n: BvhMesh id, or -1 for a standalone Triangle object; NULL = all standalone */
+
+    uint32_t n_boxes;
+    const float* boxes;              /* n x 6: corner a xyz, corner b xyz (AxisBoxMesh::new) */
+    const uint32_t* box_material;    /* n */
+
+    uint32_t n_volumes;
+    const rg_volume* volumes;
+
+    uint32_t n_sdfs;
+    const rg_sdf* sdfs;
+
+    uint32_t n_materials;
+    const rg_material* materials;
+
+    uint32_t skybox;                 /* RG_SKY_* */
+} rg_scene_desc;
+
+/* Camera (rayna_engine/src/scene/camera.rs:10-25), angles in radians. */
+typedef struct rg_camera {
+    double pos[3];
+    double fwd[3];
+    double v_fov;
+    double focus_dist;
+    double defocus_angle;
+} rg_camera;
+
+/* RenderMode (rayna_engine/src/render/render_opts.rs:34-52). */
+enum {
+    RG_MODE_PBR = 0,
+    RG_MODE_RAY_NORMAL = 1,
+    RG_MODE_OUTWARD_NORMAL = 2,
+    RG_MODE_SCATTER = 3,
+    RG_MODE_FRONT_FACE = 4,
+    RG_MODE_DISTANCE = 5,
+    RG_MODE_UV = 6,
+    RG_MODE_SIDE = 7
+};
+
+/* RenderOpts (render_opts.rs:8-29). width/height/samples/ray_branching are
+ * NonZeroUsize in the reference: 0 is rejected with RG_INVALID_ARG. */
+typedef struct rg_render_opts {
+    uint32_t width;
+    uint32_t height;
+    uint32_t samples;
+    uint32_t mode;
+    uint32_t ray_depth;
+    uint32_t ray_branching;
+} rg_render_opts;
+
+/* Which kernel form renders a frame. Both forms run the same estimator and
+ * produce the same image for the same seed. */
+enum { RG_FORM_MEGAKERNEL = 0, RG_FORM_WAVEFRONT = 1 };
+
+typedef struct rg_device_opts {
+    int32_t device;        /* CUDA ordinal */
+    void* stream;          /* cudaStream_t to run on, or NULL for a library-owned stream */
+    uint32_t form;         /* RG_FORM_* */
+    uint32_t flags;        /* RG_FLAG_* */
+} rg_device_opts;
+
+enum { RG_FLAG_COUNTERS = 1u };  /* maintain device work counters (node visits, tests) for the roofline */
+
+/* RenderStats (render/render.rs:4-15) plus device figures. */
+typedef struct rg_render_stats {
+    double duration_ms;       /* wall time of the call */
+    double kernel_ms;         /* device time of this frame's kernels (CUDA events on the handle's stream) */
+    uint64_t samples;         /* path samples traced this frame */
+    uint64_t rays;            /* extend queries (ray segments) this frame */
+    uint64_t node_visits;     /* BVH node pairs fetched (RG_FLAG_COUNTERS only, else 0) */
+    uint64_t prim_tests;      /* primitive tests (RG_FLAG_COUNTERS only, else 0) */
+    uint64_t sdf_steps;       /* SDF evaluations (RG_FLAG_COUNTERS only, else 0) */
+    uint32_t accum_frames;    /* AccumulationBuffer::frame_count */
+    uint32_t img_width;       /* dimensions of the image written to out_rgb */
+    uint32_t img_height;
+    uint32_t num_threads;     /* 0: the device renders */
+    uint32_t error_flags;     /* device-side error bits seen this frame (0 = none) */
+    uint32_t reserved;
+} rg_render_stats;
+
+/* Hit record of rg_query_rays. */
+typedef struct rg_hit {
+    uint32_t hit;        /* 0 or 1 */
+    uint32_t prim;       /* global primitive id (see rg_scene_desc) */
+    float t;             /* Intersection::dist */
+    float normal[3];     /* Intersection::normal (outward) */
+    float ray_normal[3]; /* Intersection::ray_normal (against the ray) */
+    uint32_t front_face;
+    uint32_t material;
+    uint32_t side;       /* Intersection::side */
+} rg_hit;  /* 48 bytes */
+
+/* Host-side summary of a scene as the library would build it. */
+typedef struct rg_scene_info {
+    uint32_t n_prims;        /* bounded primitives in the BVH */
+    uint32_t n_unbounded;    /* SDFs */
+    uint32_t n_nodes;        /* 64-byte node pairs */
+    uint32_t max_depth;      /* deepest node pair (traversal stack bound) */
+    uint32_t n_leaves;
+    uint32_t max_leaf_size;
+    double sah_cost;         /* sum over node pairs of child area x prims / root area */
+    uint64_t device_bytes;   /* bytes the scene occupies in device memory */
+} rg_scene_info;
+
+/* ------------------------------------------------------------------------ */
+/* Renderer lifecycle                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* ABI version of the loaded library (RG_ABI_VERSION). */
+uint32_t rg_abi_version(void);
+
+/* Replaces Renderer::new_from / new_default (renderer.rs:66-107). Creates the
+ * handle and its stream; scene, camera and options are set separately. */
+rg_status rg_create(const rg_device_opts* opts, rg_handle* out);
+
+/* Drop for Renderer. Frees every device buffer of the handle. */
+rg_status rg_destroy(rg_handle h);
+
+/* Last error message for `h` (or the thread's last handle-less error when h is NULL). */
+rg_status rg_last_error(rg_handle h, char* buf, size_t len);
+
+/* Validates a scene and builds its BVH on the host only, without a device
+ * (no reference counterpart: the preflight half of Renderer::set_scene,
+ * renderer.rs:165-168, so callers can reject a scene before creating a
+ * handle). Fails exactly where rg_set_scene would fail validation. */
+rg_status rg_inspect_scene(const rg_scene_desc* scene, rg_scene_info* out);
+
+/* Renderer::set_scene (renderer.rs:165-168): copies the scene to the device,
+ * builds the BVH and clears the accumulation buffer. */
+rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene);
+
+/* Renderer::set_camera (renderer.rs:158-161): also clears accumulation. An
+ * invalid camera is accepted here, as in the reference; render reports it. */
+rg_status rg_set_camera(rg_handle h, const rg_camera* camera);
+
+/* Renderer::set_options (renderer.rs:173-176): also clears accumulation. */
+rg_status rg_set_options(rg_handle h, const rg_render_opts* opts);
+
+/* Renderer::clear_accumulation (renderer.rs:153). */
+rg_status rg_clear_accumulation(rg_handle h);
+
+/* Renderer::render (renderer.rs:224-264). Adds one frame of `samples`
+ * samples per pixel to the accumulation buffer and writes the running mean to
+ * `out_rgb` (host memory, width*height*3 floats, [x][y][rgb]) when it is not
+ * NULL. `seed` keys the counter-based random streams of this frame.
+ * With an invalid camera the call returns RG_INVALID_CAMERA and writes the
+ * reference's fallback checker image (renderer.rs:269-292), whose dimensions
+ * are ilog2(width) x ilog2(height), reported in out_stats. */
+rg_status rg_render(rg_handle h, uint64_t seed, float* out_rgb, rg_render_stats* out_stats);
+
+/* Same frame as rg_render, but the running mean is written to device memory
+ * `d_out_rgb` (or not written when NULL) and the call does not wait for the
+ * device: it returns once the frame's kernels are queued on the stream.
+ * Stats other than `samples` are filled by rg_sync_stats. */
+rg_status rg_render_async(rg_handle h, uint64_t seed, float* d_out_rgb, rg_render_stats* out_stats);
+
+/* Waits for the handle's stream and fills device timings and counters of the
+ * last queued frame. */
+rg_status rg_sync_stats(rg_handle h, rg_render_stats* out_stats);
+
+/* Checkpoint/resume of the AccumulationBuffer (accum_buffer.rs:9-78):
+ * `sum` is width*height*3 floats in [x][y][rgb] order, `frames` the count. */
+rg_status rg_get_accumulation(rg_handle h, float* sum, uint32_t* frames);
+rg_status rg_set_accumulation(rg_handle h, const float* sum, uint32_t frames);
+
+/* Per-pixel sample statistics of the last frame: mean and unbiased sample
+ * variance over the frame's `samples` samples, [x][y][rgb] each. Used to state
+ * Monte Carlo standard errors. */
+rg_status rg_frame_moments(rg_handle h, float* mean, float* variance);
+
+/* Ray-query entry (no reference counterpart as a public call: it exposes
+ * ObjectInstance::full_intersect, object/mod.rs:59-71, for parity tests).
+ * Rays are traced against the current scene with interval [tmin[i], tmax[i]].
+ * `volume_u`, if not NULL, is n x n_volumes uniforms in (0,1] used for the
+ * free-flight draw of each medium instead of the counter-based stream. */
+rg_status rg_query_rays(rg_handle h, uint32_t n, const float* origins, const float* dirs,
+                        const float* tmin, const float* tmax, const float* volume_u, rg_hit* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAYNA_GPU_H */

@@ -1,0 +1,93 @@
+"""ctypes binding of the CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as
+the checker. The rayna_gb300 package never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from rayna_gb300 import _abi as A
+from rayna_gb300.renderer import HIT_DTYPE
+
+from . import build as _build
+
+POLICY_REF_F64 = 0
+POLICY_GPU_F32 = 1
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        fp, dp, up = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_uint32)
+        L.orc_philox.argtypes = [up, up, up]
+        L.orc_viewport.argtypes = [C.POINTER(A.rg_camera), dp]
+        L.orc_viewport.restype = C.c_int
+        L.orc_query.argtypes = [C.POINTER(A.rg_scene_desc), C.c_int, C.c_int, C.c_uint32, fp, fp, fp, fp, fp,
+                                C.POINTER(A.rg_hit), dp, dp]
+        L.orc_query.restype = C.c_int
+        L.orc_render.argtypes = [C.POINTER(A.rg_scene_desc), C.POINTER(A.rg_camera), C.POINTER(A.rg_render_opts),
+                                 C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_int, dp, dp, dp]
+        L.orc_render.restype = C.c_int
+        L.orc_hardware_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().orc_philox(c, k, o)
+    return list(o)
+
+
+def viewport(camera):
+    out = (C.c_double * 18)()
+    st = lib().orc_viewport(C.byref(camera.to_c()), out)
+    return st, np.array(out).reshape(6, 3)
+
+
+def query(flat, origins, dirs, tmin=1e-3, tmax=3.4028235e38, volume_u=None, policy=POLICY_GPU_F32, pretest=True):
+    """Closest hits from the oracle. Returns (hits structured array, t64, n64)."""
+    o = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    n = o.shape[0]
+    t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(tmin, np.float32), (n,)))
+    t1 = np.ascontiguousarray(np.broadcast_to(np.asarray(tmax, np.float32), (n,)))
+    out = (A.rg_hit * max(n, 1))()
+    t64 = np.zeros(n)
+    n64 = np.zeros((n, 3))
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    vu = None
+    if volume_u is not None:
+        vu_arr = np.ascontiguousarray(volume_u, np.float32)
+        vu = fp(vu_arr)
+    st = lib().orc_query(C.byref(flat.desc), policy, 1 if pretest else 0, n, fp(o), fp(d), fp(t0), fp(t1), vu, out,
+                         t64.ctypes.data_as(C.POINTER(C.c_double)), n64.ctypes.data_as(C.POINTER(C.c_double)))
+    assert st == 0
+    hits = np.frombuffer(out, dtype=HIT_DTYPE, count=n).copy()
+    return hits, t64, n64
+
+
+def render(flat, camera, opts, seed=0, frames=1, policy=POLICY_REF_F64, gpu_sampling=False, threads=0):
+    """Renders with the oracle. Returns (status, mean (w,h,3), var (w,h,3), seconds)."""
+    w, h = opts.width, opts.height
+    mean = np.zeros((w, h, 3))
+    var = np.zeros((w, h, 3))
+    secs = C.c_double(0.0)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    st = lib().orc_render(C.byref(flat.desc), C.byref(camera.to_c()), C.byref(opts.to_c()), int(seed), int(frames),
+                          int(policy), 1 if gpu_sampling else 0, int(threads), dp(mean), dp(var), C.byref(secs))
+    return st, mean, var, secs.value
+
+
+def hardware_threads() -> int:
+    return int(lib().orc_hardware_threads())

@@ -1,0 +1,1166 @@
+// rayna_oracle.hpp — TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of rayna_engine's per-sample path-tracing path (the
+// reference is the Rust crate rayna_engine of v0x0g/rayna). Only tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg use this code, as
+// the checker; the GPU library never links it.
+//
+// Parity status: PARTIALLY PINNED. The reference cannot be compiled in this
+// environment (no Rust toolchain, no crate registry, git-over-ssh patched
+// dependencies), so no reference output can be generated. The only known
+// answers the reference's own tests hold for this path are the four pixel
+// class checks of rayna_engine/tests/simple_renders.rs:22-142; tests/
+// pins this oracle against them and against closed-form cases (furnace
+// identities, analytic sphere/triangle hits). Everything else — including
+// the glam vector arithmetic (dot, cross, normalize/try_normalize) and the
+// `rand` streams, which are entropy-seeded in the reference — is unpinned:
+// the restatement follows the documented behaviour of those crates.
+//
+// Two arithmetic policies:
+//   RefF64 — f64 with the reference's operation order (glam scalar
+//            formulas, no fused multiply-add). Faithful to the reference.
+//   GpuF32 — f32 with the operation order and explicit fused multiply-adds
+//            of the CUDA kernels, so closed-form intersections (sphere,
+//            triangle, box, slab) are bit-identical to the device.
+// Two sampler modes:
+//   kRefSampling — the reference's rejection samplers on a sequential
+//                  per-path stream (rng.rs:64-142).
+//   kGpuSampling — the device's inverse-CDF samplers and its counter
+//                  assignment, so paths can be compared one by one.
+// Compile with -ffp-contract=off: every fused multiply-add is explicit.
+#pragma once
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <memory>
+#include <thread>
+#include <vector>
+
+#include "../include/rayna_gpu.h"
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// Counter-based random numbers: Philox4x32-10 (Salmon, Moraes, Dror, Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11).
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t v[4]; };
+
+inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)M0 * c.v[0];
+    uint64_t p1 = (uint64_t)M1 * c.v[2];
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    U4 n;
+    n.v[0] = hi1 ^ c.v[1] ^ k0;
+    n.v[1] = lo1;
+    n.v[2] = hi0 ^ c.v[3] ^ k1;
+    n.v[3] = lo0;
+    c = n;
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// [0,1) and (0,1] floats from the top 24 bits (the device uses the same maps).
+inline float u01f(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+inline float u01f_open0(uint32_t x) { return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f); }
+inline double u01d(uint32_t a, uint32_t b) {
+  return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+// Counter purposes of the device's random-number assignment.
+enum : uint32_t { kPurposeCamera = 0, kPurposeScatter = 1, kPurposeVolume0 = 2 };
+
+// Sequential stream used in the reference-sampling mode: one Philox block of
+// four words per refill, counter (a, b, c, k++).
+struct SeqRng {
+  uint32_t k0, k1, a, b, c, k = 0;
+  U4 buf{};
+  int left = 0;
+  SeqRng(uint64_t seed, uint32_t a_, uint32_t b_, uint32_t c_)
+      : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), a(a_), b(b_), c(c_) {}
+  uint32_t next_u32() {
+    if (left == 0) {
+      buf = philox4x32_10(U4{{a, b, c, k++}}, k0, k1);
+      left = 4;
+    }
+    return buf.v[4 - (left--)];
+  }
+  double gen() { uint32_t x = next_u32(); uint32_t y = next_u32(); return u01d(x, y); }  // rng.gen::<f64>() in [0,1)
+  double range_incl(double lo, double hi) { return lo + (hi - lo) * gen(); }           // gen_range(lo..=hi)
+};
+
+// ---------------------------------------------------------------------------
+// Arithmetic policies.
+// ---------------------------------------------------------------------------
+struct RefF64 { using T = double; static constexpr bool gpu = false; };
+struct GpuF32 { using T = float; static constexpr bool gpu = true; };
+
+template <class T> struct V3 { T x, y, z; };
+template <class T> inline V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class T> inline V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> inline V3<T> operator*(V3<T> a, V3<T> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+template <class T> inline V3<T> operator*(V3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class T> inline V3<T> operator/(V3<T> a, T s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class T> inline V3<T> operator-(V3<T> a) { return {-a.x, -a.y, -a.z}; }
+template <class T> inline T comp(V3<T> v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+
+template <class P> struct Math {
+  using T = typename P::T;
+  using V = V3<T>;
+  // glam: (x*x') + (y*y') + (z*z'); device: fma(x,x', fma(y,y', z*z')).
+  static T dot(V a, V b) {
+    if constexpr (P::gpu) return std::fma(a.x, b.x, std::fma(a.y, b.y, a.z * b.z));
+    else return a.x * b.x + a.y * b.y + a.z * b.z;
+  }
+  static V cross(V a, V b) {
+    if constexpr (P::gpu)
+      return {std::fma(a.y, b.z, -(a.z * b.y)), std::fma(a.z, b.x, -(a.x * b.z)), std::fma(a.x, b.y, -(a.y * b.x))};
+    else
+      return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+  }
+  // Ray::at: pos + dir * t
+  static V at(V o, V d, T t) {
+    if constexpr (P::gpu) return {std::fma(d.x, t, o.x), std::fma(d.y, t, o.y), std::fma(d.z, t, o.z)};
+    else return o + d * t;
+  }
+  static T length(V v) { return std::sqrt(dot(v, v)); }
+  // glam normalize: self * (1 / length)
+  static V normalize(V v) { T r = T(1) / length(v); return v * r; }
+  // glam try_normalize: Some(self * rcp) if rcp is finite and > 0
+  static bool try_normalize(V v, V& out) {
+    T r = T(1) / length(v);
+    if (std::isfinite(r) && r > T(0)) { out = v * r; return true; }
+    return false;
+  }
+  static T signum(T x) { return std::isnan(x) ? x : std::copysign(T(1), x); }
+};
+
+// ---------------------------------------------------------------------------
+// Ray, Interval, Aabb (shared/ray.rs, shared/interval.rs, shared/aabb.rs)
+// ---------------------------------------------------------------------------
+template <class P> struct Ray {
+  using T = typename P::T;
+  V3<T> pos, dir, inv;
+  // Ray::new (ray.rs:15-23): normalise the direction and store its reciprocal.
+  static Ray make(V3<T> p, V3<T> d) {
+    Ray r;
+    r.pos = p;
+    r.dir = Math<P>::normalize(d);
+    r.inv = {T(1) / r.dir.x, T(1) / r.dir.y, T(1) / r.dir.z};
+    return r;
+  }
+};
+
+template <class T> struct Interval {
+  bool has_start = false, has_end = false;
+  T start = 0, end = 0;
+  static Interval full() { return Interval{}; }
+  static Interval range(T s, T e) { Interval i; i.has_start = i.has_end = true; i.start = s; i.end = e; return i; }
+  static Interval from(T s) { Interval i; i.has_start = true; i.start = s; return i; }
+  // interval.rs:108-124
+  bool contains(T x) const {
+    if (has_start && has_end) return start <= x && x <= end;
+    if (has_start) return start <= x;
+    if (has_end) return x <= end;
+    return true;
+  }
+  // interval.rs:67-93
+  bool range_overlaps(T mn, T mx) const {
+    if (!has_start && !has_end) return true;
+    if (has_start && has_end) {
+      T low = mn > start ? mn : start;
+      T high = mx < end ? mx : end;
+      return low <= high;
+    }
+    if (has_end) { T high = mx < end ? mx : end; return mn <= high; }
+    T low = mn > start ? mn : start;
+    return low <= mx;
+  }
+  Interval with_end(T e) const { Interval i = *this; i.has_end = true; i.end = e; return i; }
+};
+
+template <class T> struct Aabb {
+  V3<T> mn{0, 0, 0}, mx{0, 0, 0};  // Default: a zero box at the origin (aabb.rs:16, derive(Default))
+  static Aabb make(V3<T> a, V3<T> b) {
+    Aabb r;
+    r.mn = {std::fmin(a.x, b.x), std::fmin(a.y, b.y), std::fmin(a.z, b.z)};
+    r.mx = {std::fmax(a.x, b.x), std::fmax(a.y, b.y), std::fmax(a.z, b.z)};
+    return r;
+  }
+  static Aabb encompass(const Aabb& a, const Aabb& b) { return make(V3<T>{std::fmin(a.mn.x, b.mn.x), std::fmin(a.mn.y, b.mn.y), std::fmin(a.mn.z, b.mn.z)}, V3<T>{std::fmax(a.mx.x, b.mx.x), std::fmax(a.mx.y, b.mx.y), std::fmax(a.mx.z, b.mx.z)}); }
+  // aabb.rs:37-38: ((sx*sy) + (sy*sz) + (sz*sx)) * 2
+  double area() const {
+    double sx = (double)mx.x - (double)mn.x, sy = (double)mx.y - (double)mn.y, sz = (double)mx.z - (double)mn.z;
+    return ((sx * sy) + (sy * sz) + (sz * sx)) * 2.0;
+  }
+};
+
+// Aabb::hit (aabb.rs:117-153). The device computes each slab distance as
+// fma(bound, inv, -(pos*inv)); the reference as (bound - pos) * inv.
+template <class P> inline bool aabb_hit(const Aabb<typename P::T>& b, const Ray<P>& r, const Interval<typename P::T>& iv) {
+  using T = typename P::T;
+  T t1[3], t2[3];
+  for (int a = 0; a < 3; ++a) {
+    T lo = comp(b.mn, a), hi = comp(b.mx, a), o = comp(r.pos, a), inv = comp(r.inv, a);
+    if constexpr (P::gpu) {
+      T oi = o * inv;
+      t1[a] = std::fma(lo, inv, -oi);
+      t2[a] = std::fma(hi, inv, -oi);
+    } else {
+      t1[a] = (lo - o) * inv;
+      t2[a] = (hi - o) * inv;
+    }
+  }
+  T tmin = std::fmin(t1[0], t2[0]);
+  T tmax = std::fmax(t1[0], t2[0]);
+  tmin = std::fmax(tmin, std::fmin(t1[1], t2[1]));
+  tmax = std::fmin(tmax, std::fmax(t1[1], t2[1]));
+  tmin = std::fmax(tmin, std::fmin(t1[2], t2[2]));
+  tmax = std::fmin(tmax, std::fmax(t1[2], t2[2]));
+  return iv.range_overlaps(tmin, tmax);
+}
+
+// Intersection (shared/intersect.rs:8-43) plus the material and primitive.
+template <class T> struct Hit {
+  T dist = 0;
+  V3<T> pos_w{0, 0, 0}, normal{0, 0, 0}, ray_normal{0, 0, 0};
+  bool front_face = false;
+  T u = 0, v = 0;
+  uint32_t side = 0;
+  uint32_t prim = 0;
+  uint32_t material = 0;
+};
+
+// ---------------------------------------------------------------------------
+// Meshes
+// ---------------------------------------------------------------------------
+template <class P> struct Sphere {
+  using T = typename P::T;
+  V3<T> c; T r, r2;
+  Aabb<T> aabb() const { V3<T> s{r, r, r}; return Aabb<T>::make(c - s, c + s); }  // sphere.rs:34
+  // SphereMesh::intersect (sphere.rs:44-99)
+  bool intersect(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
+    V3<T> oc = ray.pos - c;
+    T half_b, cc, disc;
+    if constexpr (P::gpu) {
+      half_b = Math<P>::dot(oc, ray.dir);
+      cc = std::fma(oc.x, oc.x, std::fma(oc.y, oc.y, std::fma(oc.z, oc.z, -r2)));
+      disc = std::fma(half_b, half_b, -cc);
+    } else {
+      half_b = Math<P>::dot(oc, ray.dir);
+      cc = Math<P>::dot(oc, oc) - r2;
+      disc = (half_b * half_b) - cc;
+    }
+    if (disc < T(0)) return false;
+    T sq = std::sqrt(disc);
+    T root = -half_b - sq;
+    if (!iv.contains(root)) {
+      root = -half_b + sq;
+      if (!iv.contains(root)) return false;
+    }
+    h.dist = root;
+    h.pos_w = Math<P>::at(ray.pos, ray.dir, root);
+    V3<T> local = (h.pos_w - c) / r;
+    h.normal = local;
+    bool inside = Math<P>::dot(ray.dir, local) > T(0);
+    h.ray_normal = inside ? -local : local;
+    h.front_face = !inside;
+    // sphere_uv (sphere.rs:114-121)
+    T theta = std::acos(-local.y);
+    T phi = std::atan2(-local.z, local.x) + T(M_PI);
+    h.u = phi / T(2 * M_PI);
+    h.v = theta / T(M_PI);
+    h.side = 0;
+    return true;
+  }
+};
+
+template <class P> struct Triangle {
+  using T = typename P::T;
+  V3<T> v0, v1, v2, n0, n1, n2;
+  Aabb<T> aabb() const {  // Aabb::encompass_points (aabb.rs:70-80)
+    V3<T> mn{std::fmin(std::fmin(v0.x, v1.x), v2.x), std::fmin(std::fmin(v0.y, v1.y), v2.y), std::fmin(std::fmin(v0.z, v1.z), v2.z)};
+    V3<T> mx{std::fmax(std::fmax(v0.x, v1.x), v2.x), std::fmax(std::fmax(v0.y, v1.y), v2.y), std::fmax(std::fmax(v0.z, v1.z), v2.z)};
+    return Aabb<T>::make(mn, mx);
+  }
+  V3<T> centre() const { return (v0 + v1 + v2) / T(3); }
+  // Triangle::intersect (triangle.rs:53-109), Moller-Trumbore.
+  bool intersect(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
+    using M = Math<P>;
+    V3<T> e1 = v1 - v0, e2 = v2 - v0;
+    V3<T> pvec = M::cross(ray.dir, e2);
+    T det = M::dot(e1, pvec);
+    if (det == T(0)) return false;
+    T inv_det = T(1) / det;
+    V3<T> tvec = ray.pos - v0;
+    T u = M::dot(tvec, pvec) * inv_det;
+    if (u < T(0) || u > T(1)) return false;
+    V3<T> qvec = M::cross(tvec, e1);
+    T v = M::dot(ray.dir, qvec) * inv_det;
+    if (v < T(0) || u + v > T(1)) return false;
+    T t = M::dot(e2, qvec) * inv_det;
+    if (!iv.contains(t)) return false;
+    T b0 = (T(1) - u) - v;
+    // interpolate_normals (triangle.rs:114-119): fold from zero, then try_normalize
+    V3<T> n;
+    if constexpr (P::gpu) {
+      n = {std::fma(n2.x, v, std::fma(n1.x, u, n0.x * b0)), std::fma(n2.y, v, std::fma(n1.y, u, n0.y * b0)),
+           std::fma(n2.z, v, std::fma(n1.z, u, n0.z * b0))};
+    } else {
+      n = (n0 * b0 + n1 * u) + n2 * v;
+    }
+    V3<T> nn;
+    if (!M::try_normalize(n, nn)) return false;  // opposing vertex normals: a miss
+    h.dist = t;
+    h.pos_w = M::at(ray.pos, ray.dir, t);
+    h.front_face = std::signbit(det);
+    h.u = u;
+    h.v = v;
+    h.side = 0;
+    h.normal = nn;
+    h.ray_normal = nn * (-M::signum(det));
+    return true;
+  }
+};
+
+template <class P> struct AxisBox {
+  using T = typename P::T;
+  V3<T> centre, radius, inv_radius;
+  Aabb<T> box;
+  static AxisBox make(V3<T> a, V3<T> b) {  // axis_box.rs:29-37
+    AxisBox r;
+    r.box = Aabb<T>::make(a, b);
+    r.centre = (r.box.mn + r.box.mx) / T(2);
+    V3<T> size = r.box.mx - r.box.mn;
+    r.radius = size / T(2);
+    r.inv_radius = {T(1) / r.radius.x, T(1) / r.radius.y, T(1) / r.radius.z};
+    return r;
+  }
+  Aabb<T> aabb() const { return box; }
+  // AxisBoxMesh::intersect (axis_box.rs:64-145), Majercik et al. 2018.
+  bool intersect(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
+    using M = Math<P>;
+    V3<T> ro = ray.pos - centre;
+    V3<T> rd = ray.dir;
+    V3<T> q = {std::fabs(ro.x) * inv_radius.x, std::fabs(ro.y) * inv_radius.y, std::fabs(ro.z) * inv_radius.z};
+    T winding = M::signum(std::fmax(q.x, std::fmax(q.y, q.z)) - T(1));
+    V3<T> sgn = {-M::signum(rd.x), -M::signum(rd.y), -M::signum(rd.z)};
+    V3<T> pd = {((radius.x * winding) * sgn.x - ro.x) * ray.inv.x, ((radius.y * winding) * sgn.y - ro.y) * ray.inv.y,
+                ((radius.z * winding) * sgn.z - ro.z) * ray.inv.z};
+    for (int ax = 0; ax < 3; ++ax) {
+      T dist = comp(pd, ax);
+      if (!iv.contains(dist)) continue;
+      int a1 = ax == 0 ? 1 : (ax == 1 ? 2 : 0);  // x: yz, y: zx, z: xy
+      int a2 = ax == 0 ? 2 : (ax == 1 ? 0 : 1);
+      T u0, u1;
+      if constexpr (P::gpu) {
+        u0 = std::fma(comp(rd, a1), dist, comp(ro, a1));
+        u1 = std::fma(comp(rd, a2), dist, comp(ro, a2));
+      } else {
+        u0 = comp(ro, a1) + comp(rd, a1) * dist;
+        u1 = comp(ro, a2) + comp(rd, a2) * dist;
+      }
+      T r1 = comp(radius, a1), r2 = comp(radius, a2);
+      if (std::fabs(u0) < r1 && std::fabs(u1) < r2) {
+        T s = comp(sgn, ax);
+        V3<T> rn{0, 0, 0};
+        if (ax == 0) rn.x = s; else if (ax == 1) rn.y = s; else rn.z = s;
+        h.dist = dist;
+        h.pos_w = M::at(ray.pos, ray.dir, dist);
+        h.ray_normal = rn;
+        h.normal = rn * winding;
+        h.front_face = !std::signbit(winding);
+        h.u = (u0 / r1 + T(1)) / T(2);
+        h.v = (u1 / r2 + T(1)) / T(2);
+        h.side = (uint32_t)ax * 2u + (s > T(0) ? 1u : 0u);
+        return true;
+      }
+    }
+    return false;
+  }
+};
+
+// Signed distance functions evaluated in world space.
+template <class P> struct Sdf {
+  using T = typename P::T;
+  uint32_t kind;
+  V3<T> c;
+  T p[4];
+  uint32_t max_iter;
+  T eps;
+  // Bounding radius outside of which the function is replaced by the
+  // distance to an enclosing sphere (a valid lower bound of the distance).
+  static constexpr double kBulbInner = 1.2, kBulbOuter = 1.5;
+  T eval(V3<T> x) const {
+    V3<T> q = x - c;
+    if (kind == RG_SDF_SPHERE) return Math<P>::length(q) - p[0];
+    if (kind == RG_SDF_TORUS) {
+      T a = std::sqrt(q.x * q.x + q.z * q.z) - p[0];
+      return std::sqrt(a * a + q.y * q.y) - p[1];
+    }
+    // Mandelbulb distance estimator (spherical-coordinate power map with the
+    // running derivative; Hart et al. 1989 / the standard escape-time DE).
+    T s = p[2];
+    V3<T> z0 = q / s;
+    T rq = Math<P>::length(z0);
+    if (rq > T(kBulbOuter)) return (rq - T(kBulbInner)) * s;
+    T power = p[0];
+    int iters = (int)p[1];
+    V3<T> z = z0;
+    T dr = T(1), r = T(0);
+    for (int i = 0; i < iters; ++i) {
+      r = Math<P>::length(z);
+      if (r > T(2)) break;
+      T theta = std::acos(z.z / r);
+      T phi = std::atan2(z.y, z.x);
+      dr = std::pow(r, power - T(1)) * power * dr + T(1);
+      T zr = std::pow(r, power);
+      theta = theta * power;
+      phi = phi * power;
+      T st = std::sin(theta);
+      z = V3<T>{zr * (st * std::cos(phi)), zr * (std::sin(phi) * st), zr * std::cos(theta)} + z0;
+    }
+    return (T(0.5) * std::log(r) * r / dr) * s;
+  }
+  // RaymarchedIsosurfaceMesh::intersect (raymarched.rs:73-122)
+  bool intersect(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
+    T total = iv.has_start ? iv.start : T(0);
+    V3<T> point = Math<P>::at(ray.pos, ray.dir, total);
+    uint32_t i = 0;
+    for (;;) {
+      T d = eval(point);
+      total = total + std::fabs(d);
+      point = Math<P>::at(ray.pos, ray.dir, total);
+      if (std::fabs(d) < eps && iv.contains(total)) {
+        V3<T> pp = point;
+        V3<T> g{eval(V3<T>{pp.x + eps, pp.y, pp.z}) - eval(V3<T>{pp.x - eps, pp.y, pp.z}),
+                eval(V3<T>{pp.x, pp.y + eps, pp.z}) - eval(V3<T>{pp.x, pp.y - eps, pp.z}),
+                eval(V3<T>{pp.x, pp.y, pp.z + eps}) - eval(V3<T>{pp.x, pp.y, pp.z - eps})};
+        V3<T> n = Math<P>::normalize(g);
+        h.dist = total;
+        h.pos_w = pp;
+        h.normal = n;
+        h.ray_normal = n;
+        h.front_face = !std::signbit(d);
+        h.u = h.v = 0;
+        h.side = i;
+        return true;
+      }
+      if (i > max_iter) return false;
+      ++i;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Sampling
+// ---------------------------------------------------------------------------
+// Per-path random source. In kGpuSampling mode it reproduces the device's
+// counter assignment: block (pixel, sample, depth, purpose).
+struct PathRng {
+  bool gpu;
+  uint64_t seed;
+  uint32_t pixel, sample;
+  SeqRng seq;
+  const float* injected_volume_u = nullptr;  // query mode: per-volume uniforms
+  PathRng(bool g, uint64_t s, uint32_t px, uint32_t smp)
+      : gpu(g), seed(s), pixel(px), sample(smp), seq(s, px, smp, 0x52u) {}
+  U4 block(uint32_t depth, uint32_t purpose) const {
+    return philox4x32_10(U4{{pixel, sample, depth, purpose}}, (uint32_t)seed, (uint32_t)(seed >> 32));
+  }
+};
+
+template <class T> inline V3<T> unit_sphere_from(T r1, T r2) {
+  // normal_on_unit_sphere (rng.rs:75-87)
+  T two_pi = T(2 * M_PI);
+  T s = T(2) * std::sqrt(r2 * (T(1) - r2));
+  return {std::cos(two_pi * r1) * s, std::sin(two_pi * r1) * s, T(1) - T(2) * r2};
+}
+
+// ---------------------------------------------------------------------------
+// Scene
+// ---------------------------------------------------------------------------
+enum ObjKind : uint32_t { OBJ_SPHERE, OBJ_TRIANGLE, OBJ_MESH, OBJ_BOX, OBJ_VOLUME, OBJ_SDF };
+
+template <class P> struct Scene;
+
+// GenericBvh node (shared/generic_bvh.rs:30-36): Nested(aabb) with children,
+// or Object(item).
+template <class T> struct BvhNode {
+  bool is_item = false;
+  uint32_t item = 0;
+  Aabb<T> box;
+  std::vector<uint32_t> children;
+};
+
+template <class T> struct Bvh {
+  std::vector<BvhNode<T>> nodes;
+  int root = -1;
+};
+
+// Exhaustive SAH builder of GenericBvh::generate_nodes_sah (generic_bvh.rs:
+// 97-290): two binary splits per node (up to four children), leaves of at most
+// 8 items, costs from boxes folded from the origin-anchored default box. The
+// per-split box folds are computed by prefix/suffix sweeps (the same boxes as
+// the reference's per-split Aabb::encompass_iter, in O(n) per axis).
+template <class T> struct RefBvhBuilder {
+  const std::vector<Aabb<T>>& boxes;
+  Bvh<T>& out;
+  explicit RefBvhBuilder(const std::vector<Aabb<T>>& b, Bvh<T>& o) : boxes(b), out(o) {}
+
+  Aabb<T> fold(const uint32_t* it, size_t n) const {
+    Aabb<T> a;  // default: zero box at the origin
+    for (size_t i = 0; i < n; ++i) a = Aabb<T>::encompass(a, boxes[it[i]]);
+    return a;
+  }
+  void sort_axis(std::vector<uint32_t>& v, int ax) const {
+    std::stable_sort(v.begin(), v.end(), [&](uint32_t a, uint32_t b) { return comp(boxes[a].mn, ax) < comp(boxes[b].mn, ax); });
+  }
+  // calculate_optimal_split::<1, 2> (generic_bvh.rs:173-290)
+  bool split(std::vector<uint32_t>& v, int& best_axis, size_t& best_left) const {
+    size_t n = v.size();
+    if (n <= 2) return false;
+    bool have = false;
+    double best = 0;
+    std::vector<Aabb<T>> pre(n + 1), suf(n + 1);
+    for (int ax = 0; ax < 3; ++ax) {
+      sort_axis(v, ax);
+      pre[0] = Aabb<T>();
+      for (size_t i = 0; i < n; ++i) pre[i + 1] = Aabb<T>::encompass(pre[i], boxes[v[i]]);
+      suf[n] = Aabb<T>();
+      for (size_t i = n; i-- > 0;) suf[i] = Aabb<T>::encompass(suf[i + 1], boxes[v[i]]);
+      for (size_t p = 1; p + 2 <= n; ++p) {  // split positions 1 ..= n-2
+        double cost = (double)p * pre[p].area() + (double)(n - p) * suf[p].area();
+        if (!have || cost < best) { have = true; best = cost; best_axis = ax; best_left = p; }
+      }
+    }
+    return have;
+  }
+  uint32_t leaf(uint32_t item) {
+    BvhNode<T> nd; nd.is_item = true; nd.item = item; nd.box = boxes[item];
+    out.nodes.push_back(nd);
+    return (uint32_t)out.nodes.size() - 1;
+  }
+  uint32_t build(std::vector<uint32_t> v) {
+    if (v.size() == 1) return leaf(v[0]);
+    uint32_t me = (uint32_t)out.nodes.size();
+    out.nodes.push_back(BvhNode<T>{});
+    out.nodes[me].box = fold(v.data(), v.size());
+    if (v.size() <= 8) {
+      for (uint32_t it : v) { uint32_t c = leaf(it); out.nodes[me].children.push_back(c); }
+      return me;
+    }
+    int ax; size_t p;
+    split(v, ax, p);
+    sort_axis(v, ax);
+    std::vector<uint32_t> parts[2] = {std::vector<uint32_t>(v.begin(), v.begin() + p), std::vector<uint32_t>(v.begin() + p, v.end())};
+    for (auto& part : parts) {
+      int ax2; size_t p2;
+      if (split(part, ax2, p2)) {
+        sort_axis(part, ax2);
+        std::vector<uint32_t> a(part.begin(), part.begin() + p2), b(part.begin() + p2, part.end());
+        uint32_t ca = build(std::move(a)); out.nodes[me].children.push_back(ca);
+        uint32_t cb = build(std::move(b)); out.nodes[me].children.push_back(cb);
+      } else {
+        uint32_t c = build(std::move(part)); out.nodes[me].children.push_back(c);
+      }
+    }
+    return me;
+  }
+};
+
+// Binned SAH builder (16 bins, leaves of at most 4 items) for inputs too large
+// for the reference's exhaustive builder. Deviation from the reference, used
+// only for the tree shape: traversal results are independent of it except for
+// exact-distance ties.
+template <class T> struct BinnedBvhBuilder {
+  const std::vector<Aabb<T>>& boxes;
+  std::vector<V3<double>> cent;
+  Bvh<T>& out;
+  BinnedBvhBuilder(const std::vector<Aabb<T>>& b, Bvh<T>& o) : boxes(b), out(o) {
+    cent.resize(b.size());
+    for (size_t i = 0; i < b.size(); ++i)
+      cent[i] = {0.5 * ((double)b[i].mn.x + b[i].mx.x), 0.5 * ((double)b[i].mn.y + b[i].mx.y), 0.5 * ((double)b[i].mn.z + b[i].mx.z)};
+  }
+  uint32_t build(uint32_t* it, size_t n) {
+    uint32_t me = (uint32_t)out.nodes.size();
+    out.nodes.push_back(BvhNode<T>{});
+    Aabb<T> bb = boxes[it[0]];
+    for (size_t i = 1; i < n; ++i) bb = Aabb<T>::encompass(bb, boxes[it[i]]);
+    out.nodes[me].box = bb;
+    auto make_leaf = [&]() {
+      for (size_t i = 0; i < n; ++i) {
+        BvhNode<T> nd; nd.is_item = true; nd.item = it[i]; nd.box = boxes[it[i]];
+        out.nodes.push_back(nd);
+        out.nodes[me].children.push_back((uint32_t)out.nodes.size() - 1);
+      }
+      return me;
+    };
+    if (n <= 4) return make_leaf();
+    double cmin[3] = {1e300, 1e300, 1e300}, cmax[3] = {-1e300, -1e300, -1e300};
+    for (size_t i = 0; i < n; ++i) for (int a = 0; a < 3; ++a) { double c = comp(cent[it[i]], a); cmin[a] = std::min(cmin[a], c); cmax[a] = std::max(cmax[a], c); }
+    const int B = 16;
+    double best = 1e300; int bax = -1, bsplit = -1;
+    for (int a = 0; a < 3; ++a) {
+      double ext = cmax[a] - cmin[a];
+      if (!(ext > 0)) continue;
+      Aabb<T> bin[B]; int cnt[B] = {0}; bool init[B] = {false};
+      for (size_t i = 0; i < n; ++i) {
+        int k = std::min(B - 1, (int)((comp(cent[it[i]], a) - cmin[a]) / ext * B));
+        bin[k] = init[k] ? Aabb<T>::encompass(bin[k], boxes[it[i]]) : boxes[it[i]]; init[k] = true; cnt[k]++;
+      }
+      double la[B], ra[B]; int lc[B], rc[B];
+      Aabb<T> acc; bool ai = false; int c = 0;
+      for (int k = 0; k < B; ++k) { if (init[k]) { acc = ai ? Aabb<T>::encompass(acc, bin[k]) : bin[k]; ai = true; } c += cnt[k]; la[k] = ai ? acc.area() : 0; lc[k] = c; }
+      ai = false; c = 0;
+      for (int k = B - 1; k >= 0; --k) { if (init[k]) { acc = ai ? Aabb<T>::encompass(acc, bin[k]) : bin[k]; ai = true; } c += cnt[k]; ra[k] = ai ? acc.area() : 0; rc[k] = c; }
+      for (int k = 0; k + 1 < B; ++k) {
+        if (lc[k] == 0 || rc[k + 1] == 0) continue;
+        double cost = lc[k] * la[k] + rc[k + 1] * ra[k + 1];
+        if (cost < best) { best = cost; bax = a; bsplit = k; }
+      }
+    }
+    size_t mid;
+    if (bax < 0) {
+      mid = n / 2;  // all centroids coincide: median split
+    } else {
+      double ext = cmax[bax] - cmin[bax];
+      uint32_t* m = std::partition(it, it + n, [&](uint32_t i) { return std::min(B - 1, (int)((comp(cent[i], bax) - cmin[bax]) / ext * B)) <= bsplit; });
+      mid = (size_t)(m - it);
+      if (mid == 0 || mid == n) mid = n / 2;
+    }
+    uint32_t l = build(it, mid);
+    out.nodes[me].children.push_back(l);
+    uint32_t r = build(it + mid, n - mid);
+    out.nodes[me].children.push_back(r);
+    return me;
+  }
+};
+
+template <class T> inline void build_bvh(const std::vector<Aabb<T>>& boxes, Bvh<T>& out, size_t exact_limit) {
+  out.nodes.clear();
+  out.root = -1;
+  if (boxes.empty()) return;
+  std::vector<uint32_t> idx(boxes.size());
+  for (size_t i = 0; i < idx.size(); ++i) idx[i] = (uint32_t)i;
+  if (boxes.size() <= exact_limit) {
+    RefBvhBuilder<T> b(boxes, out);
+    out.root = (int)b.build(std::move(idx));
+  } else {
+    BinnedBvhBuilder<T> b(boxes, out);
+    out.root = (int)b.build(idx.data(), idx.size());
+  }
+}
+
+struct Options {
+  bool prim_pretest = true;    // test each leaf object's own Aabb first (object/bvh.rs:100-106)
+  size_t exact_bvh_limit = 200000;
+};
+
+template <class P> struct Scene {
+  using T = typename P::T;
+  std::vector<Sphere<P>> spheres;
+  std::vector<Triangle<P>> tris;
+  std::vector<AxisBox<P>> boxes;
+  struct Volume { uint32_t boundary; Sphere<P> s; AxisBox<P> b; T density, neg_inv_density; uint32_t material; };
+  std::vector<Volume> volumes;
+  std::vector<Sdf<P>> sdfs;
+  std::vector<uint32_t> sphere_mat, tri_mat, box_mat;
+  std::vector<rg_material> materials;
+  uint32_t skybox = RG_SKY_SIMPLE;
+  uint32_t ns = 0, nt = 0, nb = 0, nv = 0, nsdf = 0;
+
+  struct Mesh { std::vector<uint32_t> tris; Bvh<T> bvh; uint32_t material; Aabb<T> box; };
+  std::vector<Mesh> meshes;
+  struct Object { uint32_t kind, index; Aabb<T> box; };
+  std::vector<Object> bounded;    // ObjectList::bvh items, in list order
+  std::vector<uint32_t> unbounded; // SDF indices, in list order
+  Bvh<T> top;
+  Options opt;
+
+  uint32_t prim_sphere(uint32_t i) const { return i; }
+  uint32_t prim_tri(uint32_t i) const { return ns + i; }
+  uint32_t prim_box(uint32_t i) const { return ns + nt + i; }
+  uint32_t prim_vol(uint32_t i) const { return ns + nt + nb + i; }
+  uint32_t prim_sdf(uint32_t i) const { return ns + nt + nb + nv + i; }
+
+  void load(const rg_scene_desc& d, const Options& o) {
+    opt = o;
+    ns = d.n_spheres; nt = d.n_triangles; nb = d.n_boxes; nv = d.n_volumes; nsdf = d.n_sdfs;
+    skybox = d.skybox;
+    materials.assign(d.materials, d.materials + d.n_materials);
+    for (uint32_t i = 0; i < ns; ++i) {
+      Sphere<P> s;
+      s.c = {(T)d.spheres[4 * i], (T)d.spheres[4 * i + 1], (T)d.spheres[4 * i + 2]};
+      s.r = (T)d.spheres[4 * i + 3];
+      s.r2 = s.r * s.r;
+      spheres.push_back(s);
+      sphere_mat.push_back(d.sphere_material[i]);
+    }
+    for (uint32_t i = 0; i < nt; ++i) {
+      const float* v = d.tri_vertices + 9 * i;
+      const float* n = d.tri_normals + 9 * i;
+      Triangle<P> t;
+      t.v0 = {(T)v[0], (T)v[1], (T)v[2]}; t.v1 = {(T)v[3], (T)v[4], (T)v[5]}; t.v2 = {(T)v[6], (T)v[7], (T)v[8]};
+      t.n0 = {(T)n[0], (T)n[1], (T)n[2]}; t.n1 = {(T)n[3], (T)n[4], (T)n[5]}; t.n2 = {(T)n[6], (T)n[7], (T)n[8]};
+      tris.push_back(t);
+      tri_mat.push_back(d.tri_material[i]);
+    }
+    for (uint32_t i = 0; i < nb; ++i) {
+      const float* b = d.boxes + 6 * i;
+      boxes.push_back(AxisBox<P>::make({(T)b[0], (T)b[1], (T)b[2]}, {(T)b[3], (T)b[4], (T)b[5]}));
+      box_mat.push_back(d.box_material[i]);
+    }
+    for (uint32_t i = 0; i < nv; ++i) {
+      const rg_volume& v = d.volumes[i];
+      Volume vol{};
+      vol.boundary = v.boundary;
+      if (v.boundary == RG_BOUNDARY_SPHERE) {
+        vol.s.c = {(T)v.a[0], (T)v.a[1], (T)v.a[2]}; vol.s.r = (T)v.b[0]; vol.s.r2 = vol.s.r * vol.s.r;
+      } else {
+        vol.b = AxisBox<P>::make({(T)v.a[0], (T)v.a[1], (T)v.a[2]}, {(T)v.b[0], (T)v.b[1], (T)v.b[2]});
+      }
+      vol.density = (T)v.density;
+      vol.neg_inv_density = T(-1) / vol.density;
+      vol.material = v.material;
+      volumes.push_back(vol);
+    }
+    for (uint32_t i = 0; i < nsdf; ++i) {
+      const rg_sdf& s = d.sdfs[i];
+      sdf_material.push_back(s.material);
+      Sdf<P> f;
+      f.kind = s.kind; f.c = {(T)s.centre[0], (T)s.centre[1], (T)s.centre[2]};
+      for (int k = 0; k < 4; ++k) f.p[k] = (T)s.params[k];
+      f.max_iter = s.max_iterations; f.eps = (T)s.epsilon;
+      sdfs.push_back(f);
+    }
+    // Objects in list order: spheres, standalone triangles, meshes, boxes, volumes; SDFs unbounded.
+    for (uint32_t i = 0; i < ns; ++i) bounded.push_back({OBJ_SPHERE, i, spheres[i].aabb()});
+    std::vector<int32_t> mesh_ids;
+    for (uint32_t i = 0; i < nt; ++i) {
+      int32_t g = d.tri_mesh ? d.tri_mesh[i] : -1;
+      if (g < 0) { bounded.push_back({OBJ_TRIANGLE, i, tris[i].aabb()}); continue; }
+      size_t k = std::find(mesh_ids.begin(), mesh_ids.end(), g) - mesh_ids.begin();
+      if (k == mesh_ids.size()) { mesh_ids.push_back(g); meshes.push_back(Mesh{}); meshes.back().material = tri_mat[i]; }
+      meshes[k].tris.push_back(i);
+    }
+    std::vector<size_t> order(meshes.size());
+    for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return mesh_ids[a] < mesh_ids[b]; });
+    for (size_t k : order) {
+      Mesh& m = meshes[k];
+      std::vector<Aabb<T>> bx;
+      for (uint32_t t : m.tris) bx.push_back(tris[t].aabb());
+      build_bvh(bx, m.bvh, opt.exact_bvh_limit);
+      m.box = m.bvh.nodes[m.bvh.root].box;  // BvhMesh::aabb: the root's box (mesh/advanced/bvh.rs:117-131)
+      bounded.push_back({OBJ_MESH, (uint32_t)k, m.box});
+    }
+    for (uint32_t i = 0; i < nb; ++i) bounded.push_back({OBJ_BOX, i, boxes[i].aabb()});
+    for (uint32_t i = 0; i < nv; ++i)
+      bounded.push_back({OBJ_VOLUME, i, volumes[i].boundary == RG_BOUNDARY_SPHERE ? volumes[i].s.aabb() : volumes[i].b.aabb()});
+    for (uint32_t i = 0; i < nsdf; ++i) unbounded.push_back(i);
+    std::vector<Aabb<T>> bx;
+    for (auto& o : bounded) bx.push_back(o.box);
+    build_bvh(bx, top, opt.exact_bvh_limit);
+  }
+
+  bool boundary_hit(const Volume& v, const Ray<P>& r, const Interval<T>& iv, Hit<T>& h) const {
+    return v.boundary == RG_BOUNDARY_SPHERE ? v.s.intersect(r, iv, h) : v.b.intersect(r, iv, h);
+  }
+
+  // VolumetricObject::full_intersect (object/volumetric.rs:86-160). `u` is the
+  // uniform of the free-flight draw; the arbitrary normals are drawn after a hit.
+  bool volume_intersect(uint32_t vi, const Ray<P>& ray, const Interval<T>& iv, PathRng& rng, uint32_t depth, Hit<T>& h) const {
+    const Volume& v = volumes[vi];
+    Hit<T> tmp;
+    if (!boundary_hit(v, ray, Interval<T>::full(), tmp)) return false;
+    T enter = tmp.dist;
+    if (iv.has_start) enter = std::fmax(enter, iv.start);
+    if (!boundary_hit(v, ray, Interval<T>::from(enter + T(0.001)), tmp)) return false;
+    T exitd = tmp.dist;
+    if (iv.has_end) exitd = std::fmin(exitd, iv.end);
+    T inside = exitd - enter;
+    T u;
+    U4 blk{};
+    if (rng.injected_volume_u) u = (T)rng.injected_volume_u[vi];
+    else if (rng.gpu) { blk = rng.block(depth, kPurposeVolume0 + vi); u = (T)u01f_open0(blk.v[0]); }
+    else u = (T)rng.seq.gen();
+    T hit_dist = v.neg_inv_density * std::log(u);
+    T dist = enter + hit_dist;
+    if (hit_dist > inside) return false;
+    h.dist = dist;
+    h.pos_w = Math<P>::at(ray.pos, ray.dir, dist);
+    if (rng.gpu || rng.injected_volume_u) {
+      if (!rng.injected_volume_u) blk = rng.block(depth, kPurposeVolume0 + vi);
+      h.normal = unit_sphere_from<T>((T)u01f(blk.v[1]), (T)u01f(blk.v[2]));
+      h.ray_normal = h.normal;
+      h.u = (T)u01f(blk.v[3]); h.v = h.u;
+    } else {
+      h.normal = unit_sphere_from<T>((T)rng.seq.gen(), (T)rng.seq.gen());
+      h.ray_normal = unit_sphere_from<T>((T)rng.seq.gen(), (T)rng.seq.gen());
+      h.u = (T)rng.seq.gen(); h.v = (T)rng.seq.gen();
+    }
+    h.front_face = true;
+    h.side = 0;
+    h.material = v.material;
+    h.prim = prim_vol(vi);
+    return true;
+  }
+
+  bool object_intersect(const Object& o, const Ray<P>& ray, const Interval<T>& iv, PathRng& rng, uint32_t depth, Hit<T>& h) const {
+    switch (o.kind) {
+      case OBJ_SPHERE:
+        if (!spheres[o.index].intersect(ray, iv, h)) return false;
+        h.material = sphere_mat[o.index]; h.prim = prim_sphere(o.index); return true;
+      case OBJ_TRIANGLE:
+        if (!tris[o.index].intersect(ray, iv, h)) return false;
+        h.material = tri_mat[o.index]; h.prim = prim_tri(o.index); return true;
+      case OBJ_MESH: {
+        const Mesh& m = meshes[o.index];
+        if (!mesh_node(m, m.bvh.root, ray, iv, h)) return false;
+        h.material = m.material; return true;
+      }
+      case OBJ_BOX:
+        if (!boxes[o.index].intersect(ray, iv, h)) return false;
+        h.material = box_mat[o.index]; h.prim = prim_box(o.index); return true;
+      case OBJ_VOLUME:
+        return volume_intersect(o.index, ray, iv, rng, depth, h);
+    }
+    return false;
+  }
+
+  // BvhMesh::bvh_node_intersect (mesh/advanced/bvh.rs:63-103)
+  bool mesh_node(const Mesh& m, int node, const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
+    const BvhNode<T>& n = m.bvh.nodes[node];
+    if (n.is_item) {
+      const Triangle<P>& t = tris[m.tris[n.item]];
+      if (opt.prim_pretest && !aabb_hit<P>(n.box, ray, iv)) return false;
+      if (!t.intersect(ray, iv, h)) return false;
+      h.prim = prim_tri(m.tris[n.item]);
+      return true;
+    }
+    if (!aabb_hit<P>(n.box, ray, iv)) return false;
+    Interval<T> sh = iv;
+    bool any = false;
+    for (uint32_t c : n.children) {
+      Hit<T> hc;
+      if (!mesh_node(m, (int)c, ray, sh, hc)) continue;
+      sh = sh.with_end(hc.dist);
+      h = hc;
+      any = true;
+    }
+    return any;
+  }
+
+  // BvhObject::bvh_node_intersect (object/bvh.rs:70-108)
+  bool top_node(int node, const Ray<P>& ray, const Interval<T>& iv, PathRng& rng, uint32_t depth, Hit<T>& h) const {
+    const BvhNode<T>& n = top.nodes[node];
+    if (n.is_item) {
+      if (opt.prim_pretest && !aabb_hit<P>(n.box, ray, iv)) return false;
+      return object_intersect(bounded[n.item], ray, iv, rng, depth, h);
+    }
+    if (!aabb_hit<P>(n.box, ray, iv)) return false;
+    Interval<T> sh = iv;
+    bool any = false;
+    for (uint32_t c : n.children) {
+      Hit<T> hc;
+      if (!top_node((int)c, ray, sh, rng, depth, hc)) continue;
+      sh = sh.with_end(hc.dist);
+      h = hc;
+      any = true;
+    }
+    return any;
+  }
+
+  // ObjectList::full_intersect (object/list.rs:112-129): the BVH result, then
+  // every unbounded object with the original interval; the first minimum wins.
+  bool intersect(const Ray<P>& ray, const Interval<T>& iv, PathRng& rng, uint32_t depth, Hit<T>& h) const {
+    bool any = false;
+    if (top.root >= 0) any = top_node(top.root, ray, iv, rng, depth, h);
+    for (uint32_t si : unbounded) {
+      Hit<T> hs;
+      if (!sdfs[si].intersect(ray, iv, hs)) continue;
+      if (!any || hs.dist < h.dist) {
+        h = hs;
+        h.prim = prim_sdf(si);
+        h.material = sdf_material[si];
+        any = true;
+      }
+    }
+    return any;
+  }
+  std::vector<uint32_t> sdf_material;
+};
+
+// ---------------------------------------------------------------------------
+// Camera (scene/camera.rs:114-213), in f64 on the host.
+// ---------------------------------------------------------------------------
+struct Viewport {
+  double pos[3], pixel_center[3], viewport_u[3], viewport_v[3], defocus_u[3], defocus_v[3];
+};
+
+// Camera::calculate_viewport. Returns false for the Err cases.
+inline bool calculate_viewport(const rg_camera& c, Viewport& vp) {
+  using M = Math<RefF64>;
+  using V = V3<double>;
+  double focal = c.focus_dist;
+  if (c.v_fov == 0.0) return false;
+  if (focal == 0.0) return false;
+  V fwd{c.fwd[0], c.fwd[1], c.fwd[2]};
+  V wn;
+  if (!M::try_normalize(fwd, wn)) return false;
+  V w = -wn;
+  V uu;
+  if (!M::try_normalize(M::cross(V{0, 1, 0}, w), uu)) return false;
+  V v = M::cross(w, uu);
+  V pos{c.pos[0], c.pos[1], c.pos[2]};
+  V pc = pos - (w * focal);
+  double rad = focal * std::tan(c.defocus_angle / 2.0);
+  V du = uu * rad, dv = v * rad;
+  double h = std::tan(c.v_fov / 2.0);
+  double size = 2.0 * h * focal;
+  V vu = uu * size;
+  V vv = (-v) * size;
+  auto put = [](double* o, V x) { o[0] = x.x; o[1] = x.y; o[2] = x.z; };
+  put(vp.pos, pos); put(vp.pixel_center, pc); put(vp.viewport_u, vu); put(vp.viewport_v, vv);
+  put(vp.defocus_u, du); put(vp.defocus_v, dv);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Colour arithmetic is f32 (Channel), as in the reference.
+// ---------------------------------------------------------------------------
+struct C3 { float r, g, b; };
+inline C3 operator+(C3 a, C3 b) { return {a.r + b.r, a.g + b.g, a.b + b.b}; }
+inline C3 operator*(C3 a, C3 b) { return {a.r * b.r, a.g * b.g, a.b * b.b}; }
+inline C3 operator*(C3 a, float s) { return {a.r * s, a.g * s, a.b * s}; }
+
+template <class P> inline C3 sky_colour(uint32_t sky, const Ray<P>& r) {
+  if (sky == RG_SKY_WHITE) return {1, 1, 1};
+  if (sky == RG_SKY_NONE) return {0, 0, 0};
+  // SimpleSkybox (skybox/simple.rs:13-21): white + (blue - white) * a
+  float a;
+  if constexpr (P::gpu) a = 0.5f * r.dir.y + 0.5f;
+  else a = (float)((0.5 * r.dir.y) + 0.5);
+  return {1.0f + (0.5f - 1.0f) * a, 1.0f + (0.7f - 1.0f) * a, 1.0f + (1.0f - 1.0f) * a};
+}
+
+// Material::scatter for each variant. Returns false for None.
+template <class P>
+inline bool scatter(const rg_material& m, const Ray<P>& ray, const Hit<typename P::T>& h, PathRng& rng, uint32_t depth,
+                    V3<typename P::T>& out) {
+  using T = typename P::T;
+  using M = Math<P>;
+  using V = V3<T>;
+  U4 blk{};
+  if (rng.gpu) blk = rng.block(depth, kPurposeScatter);
+  switch (m.kind) {
+    case RG_MAT_LAMBERTIAN: {  // lambertian.rs:29-37
+      V rnd;
+      if (rng.gpu) {
+        T z = T(1) - T(2) * (T)u01f(blk.v[0]);
+        T phi = T(2 * M_PI) * (T)u01f(blk.v[1]);
+        T s = std::sqrt(std::fmax(T(0), T(1) - z * z));
+        T rad = std::cbrt((T)u01f(blk.v[2]));
+        rnd = {s * std::cos(phi) * rad, s * std::sin(phi) * rad, z * rad};
+      } else {
+        for (;;) {  // vector_in_unit_sphere (rng.rs:64-72)
+          rnd = {(T)rng.seq.range_incl(-1, 1), (T)rng.seq.range_incl(-1, 1), (T)rng.seq.range_incl(-1, 1)};
+          if (M::dot(rnd, rnd) <= T(1)) break;
+        }
+      }
+      V vec = h.ray_normal + rnd;
+      if (!M::try_normalize(vec, out)) out = h.ray_normal;
+      return true;
+    }
+    case RG_MAT_METAL: {  // metal.rs:17-34
+      V d = ray.dir;
+      V refl = d - h.ray_normal * (T(2) * M::dot(d, h.ray_normal));
+      V rnd;
+      if (rng.gpu) rnd = unit_sphere_from<T>((T)u01f(blk.v[0]), (T)u01f(blk.v[1]));
+      else { T r1 = (T)rng.seq.range_incl(0, 1); T r2 = (T)rng.seq.range_incl(0, 1); rnd = unit_sphere_from<T>(r1, r2); }
+      V vec = refl + rnd * (T)m.fuzz;
+      if (!(M::dot(vec, h.ray_normal) > T(0))) return false;
+      out = M::normalize(vec);
+      return true;
+    }
+    case RG_MAT_DIELECTRIC: {  // dielectric.rs:19-37
+      T ior = (T)m.refractive_index;
+      T ratio = h.front_face ? T(1) / ior : ior;
+      V d = ray.dir;
+      T cos_t = std::fmin(M::dot(-d, h.ray_normal), T(1));
+      T sin_t = std::sqrt(T(1) - cos_t * cos_t);
+      bool tir = ratio * sin_t > T(1);
+      T r0 = (T(1) - ratio) / (T(1) + ratio);
+      T r02 = r0 * r0;
+      T x = T(1) - cos_t;
+      T x2 = x * x;
+      T x5 = (x2 * x2) * x;
+      T refl_p = r02 + (T(1) - r02) * x5;
+      T u = rng.gpu ? (T)u01f(blk.v[0]) : (T)rng.seq.gen();
+      bool schlick = refl_p > u;
+      if (tir || schlick) {
+        out = d - h.ray_normal * (T(2) * M::dot(d, h.ray_normal));
+      } else {  // math::refract (shared/math.rs:20-25)
+        T c2 = std::fmin(M::dot(-d, h.ray_normal), T(1));
+        V perp = (d + h.ray_normal * c2) * ratio;
+        V par = h.ray_normal * (-std::sqrt(std::fabs(T(1) - M::dot(perp, perp))));
+        out = perp + par;
+      }
+      return true;
+    }
+    case RG_MAT_ISOTROPIC: {  // isotropic.rs:29-31
+      if (rng.gpu) out = unit_sphere_from<T>((T)u01f(blk.v[0]), (T)u01f(blk.v[1]));
+      else { T r1 = (T)rng.seq.range_incl(0, 1); T r2 = (T)rng.seq.range_incl(0, 1); out = unit_sphere_from<T>(r1, r2); }
+      return true;
+    }
+    default:  // LightMaterial: no scatter (light.rs:17)
+      return false;
+  }
+}
+
+// Material::reflected_light factor: the colour multiplying future_col.
+template <class P> inline C3 attenuation(const rg_material& m, const Ray<P>& ray, const Hit<typename P::T>& h) {
+  C3 alb{m.albedo[0], m.albedo[1], m.albedo[2]};
+  switch (m.kind) {
+    case RG_MAT_LAMBERTIAN:
+    case RG_MAT_METAL:
+      return alb;
+    case RG_MAT_DIELECTRIC:
+      if (h.front_face) return {1, 1, 1};  // entering: future_col unchanged (dielectric.rs:63-65)
+      [[fallthrough]];
+    case RG_MAT_ISOTROPIC: {
+      double dist = (double)Math<P>::length(h.pos_w - ray.pos);
+      float tr = (float)(-(double)m.density * dist);
+      if constexpr (P::gpu) tr = -m.density * (float)dist;
+      float e = std::exp(tr);
+      return alb * e;
+    }
+    default:
+      return {0, 0, 0};
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Integrator
+// ---------------------------------------------------------------------------
+struct RenderParams {
+  uint32_t width, height, spp, ray_depth;
+  uint64_t seed;
+};
+
+template <class P> struct Renderer {
+  using T = typename P::T;
+  using V = V3<T>;
+  const Scene<P>& sc;
+  Viewport vp;
+  RenderParams rp;
+  Renderer(const Scene<P>& s, const Viewport& v, const RenderParams& r) : sc(s), vp(v), rp(r) {}
+
+  // ray_colour_recursive (renderer.rs:508-572), branching 1.
+  C3 colour_recursive(const Ray<P>& ray, uint32_t depth, PathRng& rng) const {
+    if (depth > rp.ray_depth) return {0, 0, 0};
+    Hit<T> h;
+    Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
+    if (!sc.intersect(ray, iv, rng, depth, h)) return sky_colour<P>(sc.skybox, ray);
+    const rg_material& m = sc.materials[h.material];
+    C3 emitted = m.kind == RG_MAT_LIGHT ? C3{m.albedo[0], m.albedo[1], m.albedo[2]} : C3{0, 0, 0};
+    V dir;
+    if (!scatter<P>(m, ray, h, rng, depth, dir)) return emitted + C3{0, 0, 0} * (1.0f / 1.0f);
+    Ray<P> next = Ray<P>::make(h.pos_w, dir);
+    C3 fut = colour_recursive(next, depth + 1, rng);
+    C3 scattered = m.kind == RG_MAT_LIGHT ? C3{0, 0, 0} : fut * attenuation<P>(m, ray, h);
+    return emitted + scattered;
+  }
+
+  // The device integrator: the same recursion evaluated front to back.
+  C3 colour_iterative(Ray<P> ray, PathRng& rng) const {
+    C3 L{0, 0, 0}, beta{1, 1, 1};
+    for (uint32_t depth = 0; depth <= rp.ray_depth; ++depth) {
+      Hit<T> h;
+      Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
+      if (!sc.intersect(ray, iv, rng, depth, h)) {
+        C3 s = sky_colour<P>(sc.skybox, ray);
+        L = L + beta * s;
+        break;
+      }
+      const rg_material& m = sc.materials[h.material];
+      if (m.kind == RG_MAT_LIGHT) {
+        L = L + beta * C3{m.albedo[0], m.albedo[1], m.albedo[2]};
+        break;
+      }
+      V dir;
+      if (!scatter<P>(m, ray, h, rng, depth, dir)) break;
+      beta = beta * attenuation<P>(m, ray, h);
+      ray = Ray<P>::make(h.pos_w, dir);
+    }
+    return L;
+  }
+
+  // Viewport::calc_ray (camera.rs:191-213) for sub-pixel coordinates (fx, fy).
+  Ray<P> camera_ray(T fx, T fy, T lx, T ly) const {
+    T w = (T)rp.width, hh = (T)rp.height;
+    T u = (fx - (w / T(2))) / hh;
+    T v = (fy - (hh / T(2))) / hh;
+    V pc{(T)vp.pixel_center[0], (T)vp.pixel_center[1], (T)vp.pixel_center[2]};
+    V vu{(T)vp.viewport_u[0], (T)vp.viewport_u[1], (T)vp.viewport_u[2]};
+    V vv{(T)vp.viewport_v[0], (T)vp.viewport_v[1], (T)vp.viewport_v[2]};
+    V pos{(T)vp.pos[0], (T)vp.pos[1], (T)vp.pos[2]};
+    V du{(T)vp.defocus_u[0], (T)vp.defocus_u[1], (T)vp.defocus_u[2]};
+    V dv{(T)vp.defocus_v[0], (T)vp.defocus_v[1], (T)vp.defocus_v[2]};
+    V ps = (pc + vu * u) + vv * v;
+    V rpos = (pos + du * lx) + dv * ly;
+    return Ray<P>::make(rpos, ps - rpos);
+  }
+
+  // One sample of pixel (x, y); sample index s of spp.
+  C3 sample(uint32_t x, uint32_t y, uint32_t s, bool gpu_sampling, SeqRng* msaa) const {
+    uint32_t d = (uint32_t)std::sqrt((double)rp.spp);
+    while ((d + 1) * (d + 1) <= rp.spp) ++d;
+    while (d * d > rp.spp) --d;
+    uint32_t pix = y * rp.width + x;
+    PathRng rng(gpu_sampling, rp.seed, pix, s);
+    T jx, jy, lx = 0, ly = 0;
+    if (gpu_sampling) {
+      U4 b = rng.block(0xFFFFFFFFu, kPurposeCamera);
+      jx = (T)u01f(b.v[0]) - T(0.5);
+      jy = (T)u01f(b.v[1]) - T(0.5);
+      T r = std::sqrt((T)u01f(b.v[2]));
+      T ph = T(2 * M_PI) * (T)u01f(b.v[3]);
+      lx = r * std::cos(ph);
+      ly = r * std::sin(ph);
+    } else {
+      jx = (T)msaa->range_incl(-0.5, 0.5);
+      jy = (T)msaa->range_incl(-0.5, 0.5);
+      for (;;) {  // vector_in_unit_circle (rng.rs:134-142)
+        lx = (T)rng.seq.range_incl(-1, 1);
+        ly = (T)rng.seq.range_incl(-1, 1);
+        if (lx * lx + ly * ly <= T(1)) break;
+      }
+    }
+    T fx, fy;
+    if (s < d * d) {  // render_px_msaa (renderer.rs:370-384): index i + d*j
+      T dinv = T(1) / (T)d;
+      uint32_t i = s % d, j = s / d;
+      fx = ((T)x + jx * dinv) + (T)i * dinv;
+      fy = ((T)y + jy * dinv) + (T)j * dinv;
+    } else {
+      fx = (T)x + jx;
+      fy = (T)y + jy;
+    }
+    Ray<P> ray = camera_ray(fx, fy, lx, ly);
+    return gpu_sampling ? colour_iterative(ray, rng) : colour_recursive(ray, 0, rng);
+  }
+};
+
+}  // namespace orc

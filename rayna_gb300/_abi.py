@@ -1,0 +1,166 @@
+"""ctypes mirror of include/rayna_gpu.h and the loader of the native library.
+
+The library is built in-tree (``rayna_gb300/_lib/librayna_gpu.so``) by
+``__graft_entry__.build()``. Loading fails loudly when it is missing: there is
+no CPU fallback behind this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "librayna_gpu.so")
+
+RG_OK = 0
+RG_INVALID_ARG = 1
+RG_UNSUPPORTED_VARIANT = 2
+RG_INVALID_CAMERA = 3
+RG_OOM = 4
+RG_CUDA_ERROR = 5
+RG_QUEUE_OVERFLOW = 6
+RG_STEP_LIMIT = 7
+RG_TIMEOUT = 8
+RG_NO_DEVICE = 9
+RG_NOT_READY = 10
+
+STATUS_NAMES = {
+    0: "RG_OK", 1: "RG_INVALID_ARG", 2: "RG_UNSUPPORTED_VARIANT", 3: "RG_INVALID_CAMERA",
+    4: "RG_OOM", 5: "RG_CUDA_ERROR", 6: "RG_QUEUE_OVERFLOW", 7: "RG_STEP_LIMIT",
+    8: "RG_TIMEOUT", 9: "RG_NO_DEVICE", 10: "RG_NOT_READY",
+}
+
+RG_MAT_LAMBERTIAN, RG_MAT_METAL, RG_MAT_DIELECTRIC, RG_MAT_ISOTROPIC, RG_MAT_LIGHT = range(5)
+RG_SKY_SIMPLE, RG_SKY_WHITE, RG_SKY_NONE = range(3)
+RG_BOUNDARY_SPHERE, RG_BOUNDARY_BOX = range(2)
+RG_SDF_SPHERE, RG_SDF_TORUS, RG_SDF_MANDELBULB = range(3)
+RG_FORM_MEGAKERNEL, RG_FORM_WAVEFRONT = range(2)
+RG_FLAG_COUNTERS = 1
+
+
+class rg_material(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("albedo", C.c_float * 3), ("fuzz", C.c_float),
+                ("refractive_index", C.c_float), ("density", C.c_float), ("reserved", C.c_uint32)]
+
+
+class rg_volume(C.Structure):
+    _fields_ = [("boundary", C.c_uint32), ("a", C.c_float * 3), ("b", C.c_float * 3),
+                ("density", C.c_float), ("material", C.c_uint32)]
+
+
+class rg_sdf(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("centre", C.c_float * 3), ("params", C.c_float * 4),
+                ("max_iterations", C.c_uint32), ("epsilon", C.c_float), ("material", C.c_uint32)]
+
+
+class rg_scene_desc(C.Structure):
+    _fields_ = [
+        ("n_spheres", C.c_uint32), ("spheres", C.POINTER(C.c_float)), ("sphere_material", C.POINTER(C.c_uint32)),
+        ("n_triangles", C.c_uint32), ("tri_vertices", C.POINTER(C.c_float)), ("tri_normals", C.POINTER(C.c_float)),
+        ("tri_material", C.POINTER(C.c_uint32)), ("tri_mesh", C.POINTER(C.c_int32)),
+        ("n_boxes", C.c_uint32), ("boxes", C.POINTER(C.c_float)), ("box_material", C.POINTER(C.c_uint32)),
+        ("n_volumes", C.c_uint32), ("volumes", C.POINTER(rg_volume)),
+        ("n_sdfs", C.c_uint32), ("sdfs", C.POINTER(rg_sdf)),
+        ("n_materials", C.c_uint32), ("materials", C.POINTER(rg_material)),
+        ("skybox", C.c_uint32),
+    ]
+
+
+class rg_camera(C.Structure):
+    _fields_ = [("pos", C.c_double * 3), ("fwd", C.c_double * 3), ("v_fov", C.c_double),
+                ("focus_dist", C.c_double), ("defocus_angle", C.c_double)]
+
+
+class rg_render_opts(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("samples", C.c_uint32),
+                ("mode", C.c_uint32), ("ray_depth", C.c_uint32), ("ray_branching", C.c_uint32)]
+
+
+class rg_device_opts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("stream", C.c_void_p), ("form", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class rg_render_stats(C.Structure):
+    _fields_ = [("duration_ms", C.c_double), ("kernel_ms", C.c_double), ("samples", C.c_uint64),
+                ("rays", C.c_uint64), ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64),
+                ("sdf_steps", C.c_uint64), ("accum_frames", C.c_uint32), ("img_width", C.c_uint32),
+                ("img_height", C.c_uint32), ("num_threads", C.c_uint32), ("error_flags", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class rg_scene_info(C.Structure):
+    _fields_ = [("n_prims", C.c_uint32), ("n_unbounded", C.c_uint32), ("n_nodes", C.c_uint32),
+                ("max_depth", C.c_uint32), ("n_leaves", C.c_uint32), ("max_leaf_size", C.c_uint32),
+                ("sah_cost", C.c_double), ("device_bytes", C.c_uint64)]
+
+
+class rg_hit(C.Structure):
+    _fields_ = [("hit", C.c_uint32), ("prim", C.c_uint32), ("t", C.c_float), ("normal", C.c_float * 3),
+                ("ray_normal", C.c_float * 3), ("front_face", C.c_uint32), ("material", C.c_uint32),
+                ("side", C.c_uint32)]
+
+
+assert C.sizeof(rg_material) == 32
+assert C.sizeof(rg_hit) == 48
+
+# Every entry point declared in include/rayna_gpu.h, with its ctypes signature.
+_P = C.c_void_p
+_F = C.POINTER(C.c_float)
+SIGNATURES = {
+    "rg_abi_version": (C.c_uint32, []),
+    "rg_create": (C.c_int, [C.POINTER(rg_device_opts), C.POINTER(_P)]),
+    "rg_destroy": (C.c_int, [_P]),
+    "rg_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
+    "rg_inspect_scene": (C.c_int, [C.POINTER(rg_scene_desc), C.POINTER(rg_scene_info)]),
+    "rg_set_scene": (C.c_int, [_P, C.POINTER(rg_scene_desc)]),
+    "rg_set_camera": (C.c_int, [_P, C.POINTER(rg_camera)]),
+    "rg_set_options": (C.c_int, [_P, C.POINTER(rg_render_opts)]),
+    "rg_clear_accumulation": (C.c_int, [_P]),
+    "rg_render": (C.c_int, [_P, C.c_uint64, _F, C.POINTER(rg_render_stats)]),
+    "rg_render_async": (C.c_int, [_P, C.c_uint64, _P, C.POINTER(rg_render_stats)]),
+    "rg_sync_stats": (C.c_int, [_P, C.POINTER(rg_render_stats)]),
+    "rg_get_accumulation": (C.c_int, [_P, _F, C.POINTER(C.c_uint32)]),
+    "rg_set_accumulation": (C.c_int, [_P, _F, C.c_uint32]),
+    "rg_frame_moments": (C.c_int, [_P, _F, _F]),
+    "rg_query_rays": (C.c_int, [_P, C.c_uint32, _F, _F, _F, _F, _F, C.POINTER(rg_hit)]),
+}
+
+_lib = None
+
+
+class RaynaError(RuntimeError):
+    """A non-zero rg_status from the native library."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads librayna_gpu.so and binds every declared signature."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"native library {p} is missing; build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def last_error(lib, handle) -> str:
+    buf = C.create_string_buffer(1024)
+    lib.rg_last_error(handle, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(lib, handle, status: int) -> None:
+    if status != RG_OK:
+        raise RaynaError(status, last_error(lib, handle))

@@ -1,0 +1,706 @@
+// renderer.cpp — the C ABI (include/rayna_gpu.h): the GPU stand-in for
+// rayna_engine's Renderer (render/renderer.rs).
+//
+// A handle owns one CUDA stream (or borrows the caller's), the scene's device
+// buffers, the accumulation buffer and the frame counters. Every entry point
+// returns a status; exceptions never cross the boundary.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/rayna_gpu.h"
+#include "bvh_build.h"
+#include "gpu_scene.h"
+#include "kernels.h"
+#include "renderer_state.h"
+
+using namespace rg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+rg_status fail(rg_renderer* h, rg_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  else g_last_error = buf;
+  return st;
+}
+
+rg_status cuda_fail(rg_renderer* h, cudaError_t e, const char* what) {
+  cudaGetLastError();  // clear a sticky launch error so the next call can report its own
+  if (e == cudaErrorMemoryAllocation) return fail(h, RG_OOM, "%s: %s", what, cudaGetErrorString(e));
+  return fail(h, RG_CUDA_ERROR, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define RG_CUDA(h, call, what)                   \
+  do {                                           \
+    cudaError_t e__ = (call);                    \
+    if (e__ != cudaSuccess) return cuda_fail(h, e__, what); \
+  } while (0)
+
+template <class T> void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+// Camera::calculate_viewport (scene/camera.rs:114-167), in f64.
+struct D3 { double x, y, z; };
+D3 sub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+D3 scl(D3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+D3 neg(D3 a) { return {-a.x, -a.y, -a.z}; }
+D3 crs(D3 a, D3 b) { return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+bool try_norm(D3 v, D3& out) {
+  double r = 1.0 / std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+  if (std::isfinite(r) && r > 0.0) { out = scl(v, r); return true; }
+  return false;
+}
+
+bool compute_viewport(const rg_camera& c, HostViewport& vp) {
+  double focal = c.focus_dist;
+  if (c.v_fov == 0.0 || focal == 0.0) return false;
+  D3 w;
+  if (!try_norm(D3{c.fwd[0], c.fwd[1], c.fwd[2]}, w)) return false;
+  w = neg(w);
+  D3 u;
+  if (!try_norm(crs(D3{0, 1, 0}, w), u)) return false;
+  D3 v = crs(w, u);
+  D3 pos{c.pos[0], c.pos[1], c.pos[2]};
+  D3 pc = sub(pos, scl(w, focal));
+  double rad = focal * std::tan(c.defocus_angle / 2.0);
+  double size = 2.0 * std::tan(c.v_fov / 2.0) * focal;
+  auto put = [](double* o, D3 x) { o[0] = x.x; o[1] = x.y; o[2] = x.z; };
+  put(vp.pos, pos);
+  put(vp.pixel_center, pc);
+  put(vp.viewport_u, scl(u, size));
+  put(vp.viewport_v, scl(neg(v), size));
+  put(vp.defocus_u, scl(u, rad));
+  put(vp.defocus_v, scl(v, rad));
+  for (int i = 0; i < 3; ++i)
+    if (!std::isfinite(vp.pixel_center[i]) || !std::isfinite(vp.viewport_u[i]) || !std::isfinite(vp.viewport_v[i]) ||
+        !std::isfinite(vp.defocus_u[i]) || !std::isfinite(vp.defocus_v[i]) || !std::isfinite(vp.pos[i]))
+      return false;
+  return true;
+}
+
+uint32_t float_bits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+float bits_float(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+
+uint32_t ilog2(uint32_t v) { uint32_t r = 0; while (v >>= 1) ++r; return r; }
+
+rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
+  auto need = [&](uint32_t n, const void* p, const char* what) -> bool {
+    if (n > 0 && p == nullptr) { fail(h, RG_INVALID_ARG, "%s is NULL but its count is %u", what, n); return false; }
+    return true;
+  };
+  if (!need(d.n_spheres, d.spheres, "spheres") || !need(d.n_spheres, d.sphere_material, "sphere_material") ||
+      !need(d.n_triangles, d.tri_vertices, "tri_vertices") || !need(d.n_triangles, d.tri_normals, "tri_normals") ||
+      !need(d.n_triangles, d.tri_material, "tri_material") || !need(d.n_boxes, d.boxes, "boxes") ||
+      !need(d.n_boxes, d.box_material, "box_material") || !need(d.n_volumes, d.volumes, "volumes") ||
+      !need(d.n_sdfs, d.sdfs, "sdfs") || !need(d.n_materials, d.materials, "materials"))
+    return RG_INVALID_ARG;
+  uint64_t total = (uint64_t)d.n_spheres + d.n_triangles + d.n_boxes + d.n_volumes + d.n_sdfs;
+  if (total >= (1ull << 31)) return fail(h, RG_INVALID_ARG, "too many primitives (%llu)", (unsigned long long)total);
+  if (d.n_materials > kMaterialMask) return fail(h, RG_INVALID_ARG, "too many materials");
+  if (d.skybox > RG_SKY_NONE) return fail(h, RG_UNSUPPORTED_VARIANT, "skybox kind %u", d.skybox);
+  for (uint32_t i = 0; i < d.n_materials; ++i) {
+    const rg_material& m = d.materials[i];
+    if (m.kind > RG_MAT_LIGHT) return fail(h, RG_UNSUPPORTED_VARIANT, "material %u has kind %u", i, m.kind);
+    if (!finite3(m.albedo) || !std::isfinite(m.fuzz) || !std::isfinite(m.refractive_index) || !std::isfinite(m.density))
+      return fail(h, RG_INVALID_ARG, "material %u has a non-finite parameter", i);
+    if (m.reserved != 0) return fail(h, RG_INVALID_ARG, "material %u: reserved field must be 0", i);
+  }
+  auto mat_ok = [&](uint32_t m, const char* what, uint32_t i) -> bool {
+    if (m >= d.n_materials) { fail(h, RG_INVALID_ARG, "%s %u uses material %u of %u", what, i, m, d.n_materials); return false; }
+    return true;
+  };
+  for (uint32_t i = 0; i < d.n_spheres; ++i) {
+    if (!finite3(d.spheres + 4 * i) || !std::isfinite(d.spheres[4 * i + 3]))
+      return fail(h, RG_INVALID_ARG, "sphere %u is not finite", i);
+    if (!mat_ok(d.sphere_material[i], "sphere", i)) return RG_INVALID_ARG;
+  }
+  for (uint32_t i = 0; i < d.n_triangles; ++i) {
+    const float* v = d.tri_vertices + 9ull * i;
+    const float* n = d.tri_normals + 9ull * i;
+    for (int k = 0; k < 3; ++k) {
+      if (!finite3(v + 3 * k) || !finite3(n + 3 * k)) return fail(h, RG_INVALID_ARG, "triangle %u is not finite", i);
+      double l2 = (double)n[3 * k] * n[3 * k] + (double)n[3 * k + 1] * n[3 * k + 1] + (double)n[3 * k + 2] * n[3 * k + 2];
+      if (std::fabs(l2 - 1.0) > 2e-3) return fail(h, RG_INVALID_ARG, "triangle %u: normals must be normalised", i);
+    }
+    auto same = [&](int a, int b) { return v[3 * a] == v[3 * b] && v[3 * a + 1] == v[3 * b + 1] && v[3 * a + 2] == v[3 * b + 2]; };
+    if (same(0, 1) || same(1, 2) || same(2, 0)) return fail(h, RG_INVALID_ARG, "triangle %u has duplicate vertices", i);
+    if (!mat_ok(d.tri_material[i], "triangle", i)) return RG_INVALID_ARG;
+  }
+  for (uint32_t i = 0; i < d.n_boxes; ++i) {
+    if (!finite3(d.boxes + 6 * i) || !finite3(d.boxes + 6 * i + 3)) return fail(h, RG_INVALID_ARG, "box %u is not finite", i);
+    if (!mat_ok(d.box_material[i], "box", i)) return RG_INVALID_ARG;
+  }
+  for (uint32_t i = 0; i < d.n_volumes; ++i) {
+    const rg_volume& v = d.volumes[i];
+    if (v.boundary > RG_BOUNDARY_BOX) return fail(h, RG_UNSUPPORTED_VARIANT, "volume %u boundary kind %u", i, v.boundary);
+    if (!finite3(v.a) || !finite3(v.b) || !std::isfinite(v.density) || v.density < 0.0f)
+      return fail(h, RG_INVALID_ARG, "volume %u has an invalid parameter", i);
+    if (!mat_ok(v.material, "volume", i)) return RG_INVALID_ARG;
+  }
+  for (uint32_t i = 0; i < d.n_sdfs; ++i) {
+    const rg_sdf& s = d.sdfs[i];
+    if (s.kind > RG_SDF_MANDELBULB) return fail(h, RG_UNSUPPORTED_VARIANT, "sdf %u kind %u", i, s.kind);
+    if (!finite3(s.centre) || !std::isfinite(s.epsilon) || !(s.epsilon > 0.0f))
+      return fail(h, RG_INVALID_ARG, "sdf %u has an invalid parameter", i);
+    for (int k = 0; k < 4; ++k) if (!std::isfinite(s.params[k])) return fail(h, RG_INVALID_ARG, "sdf %u params", i);
+    if (s.kind == RG_SDF_MANDELBULB && (!(s.params[2] > 0.0f) || s.params[1] < 1.0f || s.params[1] > 64.0f))
+      return fail(h, RG_INVALID_ARG, "sdf %u: mandelbulb needs scale > 0 and 1..64 iterations", i);
+    if (s.max_iterations > (1u << 20)) return fail(h, RG_INVALID_ARG, "sdf %u: max_iterations too large", i);
+    if (!mat_ok(s.material, "sdf", i)) return RG_INVALID_ARG;
+  }
+  return RG_OK;
+}
+
+template <class T>
+rg_status upload(rg_renderer* h, T*& dst, const T* src, size_t n, const char* what) {
+  dfree(dst);
+  if (n == 0) return RG_OK;
+  RG_CUDA(h, cudaMalloc((void**)&dst, n * sizeof(T)), what);
+  RG_CUDA(h, cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, h->stream), what);
+  return RG_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Scene building (shared with other translation units through renderer_state.h)
+// ---------------------------------------------------------------------------
+namespace rg {
+
+rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs) {
+  rg_status st = validate_scene(h, d);
+  if (st != RG_OK) return st;
+  hs = HostScene{};
+  hs.ns = d.n_spheres; hs.nt = d.n_triangles; hs.nb = d.n_boxes; hs.nv = d.n_volumes; hs.nsdf = d.n_sdfs;
+  hs.sky = d.skybox;
+  hs.materials.assign(d.materials, d.materials + d.n_materials);
+  hs.volumes.assign(d.volumes, d.volumes + d.n_volumes);
+  const uint32_t nbounded = hs.ns + hs.nt + hs.nb + hs.nv;
+  std::vector<GpuPrim> prims(nbounded);
+  std::vector<float> lo(3ull * nbounded), hi(3ull * nbounded);
+  auto bits = [](uint32_t kind, uint32_t mat) { return bits_float((kind << kKindShift) | mat); };
+  auto setbox = [&](uint32_t i, float lx, float ly, float lz, float hx, float hy, float hz) {
+    lo[3ull * i] = std::fmin(lx, hx); lo[3ull * i + 1] = std::fmin(ly, hy); lo[3ull * i + 2] = std::fmin(lz, hz);
+    hi[3ull * i] = std::fmax(lx, hx); hi[3ull * i + 1] = std::fmax(ly, hy); hi[3ull * i + 2] = std::fmax(lz, hz);
+  };
+  uint32_t id = 0;
+  for (uint32_t i = 0; i < hs.ns; ++i, ++id) {
+    const float* s = d.spheres + 4ull * i;
+    float r = s[3];
+    GpuPrim& p = prims[id];
+    p.a = {s[0], s[1], s[2], bits(PK_SPHERE, d.sphere_material[i])};
+    p.b = {r, r * r, 0.0f, bits_float(id)};
+    p.c = {0, 0, 0, 0};
+    setbox(id, s[0] - r, s[1] - r, s[2] - r, s[0] + r, s[1] + r, s[2] + r);
+  }
+  hs.tri_normals.assign(d.tri_normals, d.tri_normals + 9ull * hs.nt);
+  for (uint32_t i = 0; i < hs.nt; ++i, ++id) {
+    const float* v = d.tri_vertices + 9ull * i;
+    const float* n = d.tri_normals + 9ull * i;
+    uint32_t flags = 0;
+    // If every pair of vertex normals has a positive dot product, any convex
+    // combination has length >= 1/sqrt(3): the interpolated normal always
+    // normalises. Otherwise flag the triangle for the in-traversal check.
+    for (int a = 0; a < 3; ++a)
+      for (int b = a + 1; b < 3; ++b)
+        if ((double)n[3 * a] * n[3 * b] + (double)n[3 * a + 1] * n[3 * b + 1] + (double)n[3 * a + 2] * n[3 * b + 2] <= 0.0)
+          flags |= kTriCheckNormals;
+    GpuPrim& p = prims[id];
+    p.a = {v[0], v[1], v[2], bits(PK_TRIANGLE, d.tri_material[i])};
+    p.b = {v[3] - v[0], v[4] - v[1], v[5] - v[2], bits_float(id)};
+    p.c = {v[6] - v[0], v[7] - v[1], v[8] - v[2], bits_float(flags)};
+    setbox(id, std::fmin(std::fmin(v[0], v[3]), v[6]), std::fmin(std::fmin(v[1], v[4]), v[7]),
+           std::fmin(std::fmin(v[2], v[5]), v[8]), std::fmax(std::fmax(v[0], v[3]), v[6]),
+           std::fmax(std::fmax(v[1], v[4]), v[7]), std::fmax(std::fmax(v[2], v[5]), v[8]));
+  }
+  // AxisBoxMesh::new (axis_box.rs:29-37): centre, radius = size/2, inv_radius.
+  auto axis_box = [](const float* a, const float* b, float* centre, float* radius, float* inv, float* mn, float* mx) {
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = std::fmin(a[k], b[k]);
+      mx[k] = std::fmax(a[k], b[k]);
+      centre[k] = (mn[k] + mx[k]) / 2.0f;
+      radius[k] = (mx[k] - mn[k]) / 2.0f;
+      inv[k] = 1.0f / radius[k];
+    }
+  };
+  for (uint32_t i = 0; i < hs.nb; ++i, ++id) {
+    float c[3], r[3], iv[3], mn[3], mx[3];
+    axis_box(d.boxes + 6ull * i, d.boxes + 6ull * i + 3, c, r, iv, mn, mx);
+    GpuPrim& p = prims[id];
+    p.a = {c[0], c[1], c[2], bits(PK_BOX, d.box_material[i])};
+    p.b = {r[0], r[1], r[2], bits_float(id)};
+    p.c = {iv[0], iv[1], iv[2], 0.0f};
+    setbox(id, mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]);
+  }
+  hs.vol_base = id;
+  for (uint32_t i = 0; i < hs.nv; ++i, ++id) {
+    const rg_volume& v = d.volumes[i];
+    float nid = -1.0f / v.density;
+    GpuPrim& p = prims[id];
+    if (v.boundary == RG_BOUNDARY_SPHERE) {
+      float r = v.b[0];
+      p.a = {v.a[0], v.a[1], v.a[2], bits(PK_VOL_SPHERE, v.material)};
+      p.b = {r, r * r, nid, bits_float(id)};
+      p.c = {0, 0, 0, 0};
+      setbox(id, v.a[0] - r, v.a[1] - r, v.a[2] - r, v.a[0] + r, v.a[1] + r, v.a[2] + r);
+    } else {
+      float c[3], r[3], iv[3], mn[3], mx[3];
+      axis_box(v.a, v.b, c, r, iv, mn, mx);
+      p.a = {c[0], c[1], c[2], bits(PK_VOL_BOX, v.material)};
+      p.b = {r[0], r[1], r[2], bits_float(id)};
+      p.c = {iv[0], iv[1], iv[2], nid};
+      setbox(id, mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]);
+    }
+  }
+  for (uint32_t i = 0; i < hs.nsdf; ++i, ++id) {
+    const rg_sdf& s = d.sdfs[i];
+    GpuSdf g{};
+    g.kind = s.kind;
+    g.cx = s.centre[0]; g.cy = s.centre[1]; g.cz = s.centre[2];
+    g.p0 = s.params[0]; g.p1 = s.params[1]; g.p2 = s.params[2]; g.p3 = s.params[3];
+    g.max_iter = s.max_iterations;
+    g.eps = s.epsilon;
+    g.material = s.material;
+    g.prim_id = id;
+    // Beyond bound_radius the function exceeds epsilon by a wide margin.
+    double r0;
+    if (s.kind == RG_SDF_SPHERE) r0 = std::fabs(s.params[0]);
+    else if (s.kind == RG_SDF_TORUS) r0 = std::fabs(s.params[0]) + std::fabs(s.params[1]);
+    else r0 = 1.5 * s.params[2];
+    double margin = std::max(1e-3 * std::max(r0, 1.0), 16.0 * (double)s.epsilon);
+    g.bound_radius = (float)((r0 + margin) * (1.0 + 1e-4));
+    hs.sdfs.push_back(g);
+  }
+  BvhBuildResult bvh = build_bvh(lo.data(), hi.data(), nbounded, 4, 16, 40);
+  hs.nodes = std::move(bvh.nodes);
+  hs.max_depth = bvh.max_depth;
+  hs.prims.resize(nbounded);
+  for (uint32_t i = 0; i < nbounded; ++i) hs.prims[i] = prims[bvh.order[i]];
+  if (hs.max_depth >= kMaxBuildDepth)
+    return fail(h, RG_INVALID_ARG, "BVH depth %d exceeds the traversal stack", hs.max_depth);
+  return RG_OK;
+}
+
+rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
+  DeviceScene& ds = h->dev;
+  rg_status st;
+  if ((st = upload(h, ds.nodes, hs.nodes.data(), hs.nodes.size(), "upload nodes")) != RG_OK) return st;
+  if ((st = upload(h, ds.prims, hs.prims.data(), hs.prims.size(), "upload prims")) != RG_OK) return st;
+  if ((st = upload(h, ds.tri_normals, hs.tri_normals.data(), hs.tri_normals.size(), "upload normals")) != RG_OK) return st;
+  if ((st = upload(h, ds.materials, hs.materials.data(), hs.materials.size(), "upload materials")) != RG_OK) return st;
+  if ((st = upload(h, ds.sdfs, hs.sdfs.data(), hs.sdfs.size(), "upload sdfs")) != RG_OK) return st;
+  RG_CUDA(h, cudaStreamSynchronize(h->stream), "upload scene");
+  GpuScene& g = h->gs;
+  g.nodes = ds.nodes;
+  g.prims = ds.prims;
+  g.tri_normals = ds.tri_normals;
+  g.materials = ds.materials;
+  g.sdfs = ds.sdfs;
+  g.n_nodes = (uint32_t)hs.nodes.size();
+  g.n_prims = (uint32_t)hs.prims.size();
+  g.n_sdfs = hs.nsdf;
+  g.n_volumes = hs.nv;
+  g.sky = hs.sky;
+  g.tri_base = hs.ns;
+  g.vol_base = hs.vol_base;
+  g.n_tris = hs.nt;
+  return RG_OK;
+}
+
+void free_scene(DeviceScene& ds) {
+  dfree(ds.nodes); dfree(ds.prims); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
+}
+
+rg_status set_error(rg_renderer* h, rg_status st, const char* msg) { return fail(h, st, "%s", msg); }
+
+rg_status ensure_frame_buffers(rg_renderer* h) {
+  const uint32_t w = h->opts.width, hh = h->opts.height;
+  if (h->acc_w == w && h->acc_h == hh && h->d_accum) return RG_OK;
+  dfree(h->d_accum); dfree(h->d_out); dfree(h->d_fmean); dfree(h->d_fvar);
+  size_t n = (size_t)w * hh * 3;
+  RG_CUDA(h, cudaMalloc((void**)&h->d_accum, n * sizeof(float)), "alloc accumulation");
+  RG_CUDA(h, cudaMalloc((void**)&h->d_out, n * sizeof(float)), "alloc output");
+  RG_CUDA(h, cudaMalloc((void**)&h->d_fmean, n * sizeof(float)), "alloc frame mean");
+  RG_CUDA(h, cudaMalloc((void**)&h->d_fvar, n * sizeof(float)), "alloc frame variance");
+  RG_CUDA(h, cudaMemsetAsync(h->d_accum, 0, n * sizeof(float), h->stream), "clear accumulation");
+  h->acc_w = w;
+  h->acc_h = hh;
+  h->pixel_accum = 0;  // AccumulationBuffer::new_frame: a resize starts from a blank image
+  return RG_OK;
+}
+
+void fill_frame_params(rg_renderer* h, uint64_t seed, FrameParams& fp) {
+  std::memset(&fp, 0, sizeof(fp));
+  fp.width = h->opts.width;
+  fp.height = h->opts.height;
+  fp.spp = h->opts.samples;
+  fp.ray_depth = h->opts.ray_depth;
+  uint32_t d = (uint32_t)std::sqrt((double)fp.spp);
+  while ((uint64_t)(d + 1) * (d + 1) <= fp.spp) ++d;
+  while ((uint64_t)d * d > fp.spp) --d;
+  fp.strat_d = d;
+  fp.strat_inv = 1.0f / (float)d;
+  fp.seed_lo = (uint32_t)seed;
+  fp.seed_hi = (uint32_t)(seed >> 32);
+  for (int i = 0; i < 3; ++i) {
+    fp.pos[i] = (float)h->vp.pos[i];
+    fp.pixel_center[i] = (float)h->vp.pixel_center[i];
+    fp.viewport_u[i] = (float)h->vp.viewport_u[i];
+    fp.viewport_v[i] = (float)h->vp.viewport_v[i];
+    fp.defocus_u[i] = (float)h->vp.defocus_u[i];
+    fp.defocus_v[i] = (float)h->vp.defocus_v[i];
+  }
+  fp.accum = h->d_accum;
+  fp.out = h->d_out;
+  fp.frame_mean = h->d_fmean;
+  fp.frame_var = h->d_fvar;
+  fp.counters = h->d_counters;
+  fp.err = h->d_err;
+}
+
+}  // namespace rg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+uint32_t rg_abi_version(void) { return RG_ABI_VERSION; }
+
+rg_status rg_create(const rg_device_opts* opts, rg_handle* out) {
+  if (!out) return fail(nullptr, RG_INVALID_ARG, "rg_create: out is NULL");
+  *out = nullptr;
+  rg_device_opts o{};
+  if (opts) o = *opts;
+  if (o.form > RG_FORM_WAVEFRONT) return fail(nullptr, RG_INVALID_ARG, "unknown form %u", o.form);
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail(nullptr, RG_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  if (o.device < 0 || o.device >= count) return fail(nullptr, RG_INVALID_ARG, "device %d of %d", o.device, count);
+  rg_renderer* h = new (std::nothrow) rg_renderer();
+  if (!h) return fail(nullptr, RG_OOM, "rg_create: out of host memory");
+  h->device = o.device;
+  h->form = o.form;
+  h->flags = o.flags;
+  if ((e = cudaSetDevice(o.device)) != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaSetDevice"); }
+  if (o.stream) {
+    h->stream = (cudaStream_t)o.stream;
+    h->own_stream = false;
+  } else {
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+      delete h;
+      return cuda_fail(nullptr, e, "cudaStreamCreate");
+    }
+    h->own_stream = true;
+  }
+  if ((e = cudaMalloc((void**)&h->d_counters, CNT_N * sizeof(unsigned long long))) != cudaSuccess ||
+      (e = cudaMalloc((void**)&h->d_err, sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaEventCreate(&h->ev0)) != cudaSuccess || (e = cudaEventCreate(&h->ev1)) != cudaSuccess) {
+    rg_destroy(h);
+    return cuda_fail(nullptr, e, "rg_create resources");
+  }
+  cudaMemsetAsync(h->d_err, 0, sizeof(uint32_t), h->stream);
+  // Defaults of Renderer::new_default: Camera::default, RenderOpts::default, empty scene.
+  h->cam = rg_camera{{0, 0, 0}, {0, 0, 1}, 45.0 * M_PI / 180.0, 1.0, 0.0};
+  h->cam_ok = compute_viewport(h->cam, h->vp);
+  h->opts = rg_render_opts{740, 480, 1, RG_MODE_PBR, 5, 1};
+  h->gs = GpuScene{};
+  h->gs.sky = RG_SKY_SIMPLE;
+  *out = h;
+  return RG_OK;
+}
+
+rg_status rg_destroy(rg_handle h) {
+  if (!h) return RG_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_scene(h->dev);
+  free_extra(h);
+  dfree(h->d_accum); dfree(h->d_out); dfree(h->d_fmean); dfree(h->d_fvar);
+  dfree(h->d_counters); dfree(h->d_err);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return RG_OK;
+}
+
+rg_status rg_last_error(rg_handle h, char* buf, size_t len) {
+  if (!buf || len == 0) return RG_INVALID_ARG;
+  const std::string& s = h ? h->err : g_last_error;
+  size_t n = std::min(len - 1, s.size());
+  std::memcpy(buf, s.data(), n);
+  buf[n] = '\0';
+  return RG_OK;
+}
+
+rg_status rg_clear_accumulation(rg_handle h) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  cudaSetDevice(h->device);
+  // AccumulationBuffer::clear (accum_buffer.rs:68-71)
+  if (h->d_accum)
+    RG_CUDA(h, cudaMemsetAsync(h->d_accum, 0, (size_t)h->acc_w * h->acc_h * 3 * sizeof(float), h->stream), "clear");
+  h->frame_count = 0;
+  h->pixel_accum = 0;
+  return RG_OK;
+}
+
+rg_status rg_inspect_scene(const rg_scene_desc* scene, rg_scene_info* out) {
+  if (!scene || !out) return fail(nullptr, RG_INVALID_ARG, "rg_inspect_scene: NULL argument");
+  HostScene hs;
+  rg_status st = build_scene_host(nullptr, *scene, hs);
+  std::memset(out, 0, sizeof(*out));
+  if (st != RG_OK) return st;
+  out->n_prims = (uint32_t)hs.prims.size();
+  out->n_unbounded = hs.nsdf;
+  out->n_nodes = (uint32_t)hs.nodes.size();
+  out->max_depth = (uint32_t)hs.max_depth;
+  double root_area = 0.0, cost = 0.0;
+  auto area = [](float lx, float hx, float ly, float hy, float lz, float hz) {
+    if (!(lx <= hx)) return 0.0;
+    double x = (double)hx - lx, y = (double)hy - ly, z = (double)hz - lz;
+    return 2.0 * (x * y + y * z + z * x);
+  };
+  for (size_t i = 0; i < hs.nodes.size(); ++i) {
+    const BvhNode2& n = hs.nodes[i];
+    double a0 = area(n.xs.x, n.xs.y, n.ys.x, n.ys.y, n.zs.x, n.zs.y);
+    double a1 = area(n.xs.z, n.xs.w, n.ys.z, n.ys.w, n.zs.z, n.zs.w);
+    if (i == 0) {
+      float lx = std::fmin(n.xs.x, n.xs.z), hx = std::fmax(n.xs.y, n.xs.w);
+      float ly = std::fmin(n.ys.x, n.ys.z), hy = std::fmax(n.ys.y, n.ys.w);
+      float lz = std::fmin(n.zs.x, n.zs.z), hz = std::fmax(n.zs.y, n.zs.w);
+      root_area = area(lx, hx, ly, hy, lz, hz);
+    }
+    cost += a0 * (n.meta.z > 0 ? n.meta.z : 1) + a1 * (n.meta.w > 0 ? n.meta.w : 1);
+    if (n.meta.z > 0) { out->n_leaves++; out->max_leaf_size = std::max<uint32_t>(out->max_leaf_size, n.meta.z); }
+    if (n.meta.w > 0) { out->n_leaves++; out->max_leaf_size = std::max<uint32_t>(out->max_leaf_size, n.meta.w); }
+  }
+  out->sah_cost = root_area > 0.0 ? cost / root_area : 0.0;
+  out->device_bytes = hs.nodes.size() * sizeof(BvhNode2) + hs.prims.size() * sizeof(GpuPrim) +
+                      hs.tri_normals.size() * sizeof(float) + hs.materials.size() * sizeof(rg_material) +
+                      hs.sdfs.size() * sizeof(GpuSdf);
+  return RG_OK;
+}
+
+rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene) {
+  if (!h || !scene) return fail(h, RG_INVALID_ARG, "rg_set_scene: NULL argument");
+  cudaSetDevice(h->device);
+  HostScene hs;
+  rg_status st = build_scene_host(h, *scene, hs);
+  if (st != RG_OK) return st;
+  RG_CUDA(h, cudaStreamSynchronize(h->stream), "rg_set_scene");
+  if ((st = upload_scene(h, hs)) != RG_OK) return st;
+  h->host = std::move(hs);
+  h->have_scene = true;
+  on_scene_changed(h);
+  return rg_clear_accumulation(h);
+}
+
+rg_status rg_set_camera(rg_handle h, const rg_camera* camera) {
+  if (!h || !camera) return fail(h, RG_INVALID_ARG, "rg_set_camera: NULL argument");
+  h->cam = *camera;
+  h->cam_ok = compute_viewport(h->cam, h->vp);
+  return rg_clear_accumulation(h);
+}
+
+rg_status rg_set_options(rg_handle h, const rg_render_opts* opts) {
+  if (!h || !opts) return fail(h, RG_INVALID_ARG, "rg_set_options: NULL argument");
+  if (opts->width == 0 || opts->height == 0 || opts->samples == 0 || opts->ray_branching == 0)
+    return fail(h, RG_INVALID_ARG, "width, height, samples and ray_branching must be non-zero");
+  if ((uint64_t)opts->width * opts->height > (1ull << 30)) return fail(h, RG_INVALID_ARG, "image too large");
+  if (opts->mode != RG_MODE_PBR) return fail(h, RG_UNSUPPORTED_VARIANT, "only RenderMode::PBR is supported (mode %u)", opts->mode);
+  if (opts->ray_branching != 1) return fail(h, RG_UNSUPPORTED_VARIANT, "only ray_branching = 1 is supported");
+  if (opts->ray_depth > 4096) return fail(h, RG_INVALID_ARG, "ray_depth too large");
+  h->opts = *opts;
+  return rg_clear_accumulation(h);
+}
+
+static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override, rg_render_stats* stats) {
+  rg_status st = ensure_frame_buffers(h);
+  if (st != RG_OK) return st;
+  h->frame_count += 1;
+  h->pixel_accum += 1;
+  FrameParams fp;
+  fill_frame_params(h, seed, fp);
+  fp.accum_count = h->pixel_accum;
+  if (d_out_override) fp.out = d_out_override;
+  RG_CUDA(h, cudaMemsetAsync(h->d_counters, 0, CNT_N * sizeof(unsigned long long), h->stream), "reset counters");
+  RG_CUDA(h, cudaEventRecord(h->ev0, h->stream), "event");
+  cudaError_t e;
+  if (h->form == RG_FORM_WAVEFRONT) e = launch_wavefront(h, fp);
+  else e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "render launch");
+  RG_CUDA(h, cudaEventRecord(h->ev1, h->stream), "event");
+  h->last_samples = (uint64_t)fp.width * fp.height * fp.spp;
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->samples = h->last_samples;
+    stats->accum_frames = h->frame_count;
+    stats->img_width = fp.width;
+    stats->img_height = fp.height;
+  }
+  return RG_OK;
+}
+
+rg_status rg_sync_stats(rg_handle h, rg_render_stats* stats) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  cudaSetDevice(h->device);
+  RG_CUDA(h, cudaStreamSynchronize(h->stream), "rg_sync_stats");
+  if (!stats) return RG_OK;
+  float ms = 0.0f;
+  if (cudaEventElapsedTime(&ms, h->ev0, h->ev1) != cudaSuccess) { cudaGetLastError(); ms = 0.0f; }
+  unsigned long long c[CNT_N];
+  uint32_t err = 0;
+  RG_CUDA(h, cudaMemcpy(c, h->d_counters, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
+  RG_CUDA(h, cudaMemcpy(&err, h->d_err, sizeof(err), cudaMemcpyDeviceToHost), "read error flags");
+  stats->kernel_ms = ms;
+  stats->samples = h->last_samples;
+  stats->rays = c[CNT_RAYS];
+  stats->node_visits = c[CNT_NODES];
+  stats->prim_tests = c[CNT_PRIMS];
+  stats->sdf_steps = c[CNT_SDF];
+  stats->accum_frames = h->frame_count;
+  stats->img_width = h->opts.width;
+  stats->img_height = h->opts.height;
+  stats->num_threads = 0;
+  stats->error_flags = err;
+  return RG_OK;
+}
+
+rg_status rg_render(rg_handle h, uint64_t seed, float* out_rgb, rg_render_stats* stats) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  auto t0 = std::chrono::steady_clock::now();
+  cudaSetDevice(h->device);
+  const uint32_t w = h->opts.width, hh = h->opts.height;
+  if (!h->cam_ok) {
+    // Renderer::render_failed (renderer.rs:269-292): an ilog2(w) x ilog2(h) checker.
+    uint32_t fw = ilog2(w), fh = ilog2(hh);
+    if (out_rgb)
+      for (uint32_t x = 0; x < fw; ++x)
+        for (uint32_t y = 0; y < fh; ++y) {
+          float* p = out_rgb + ((size_t)x * fh + y) * 3;
+          bool black = (x + y) % 2 == 0;
+          p[0] = black ? 0.0f : 1.0f; p[1] = 0.0f; p[2] = black ? 0.0f : 1.0f;
+        }
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      stats->img_width = fw;
+      stats->img_height = fh;
+      stats->accum_frames = h->frame_count;
+      stats->duration_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return fail(h, RG_INVALID_CAMERA, "camera viewport could not be calculated");
+  }
+  rg_status st = render_frame(h, seed, nullptr, stats);
+  if (st != RG_OK) return st;
+  if (out_rgb)
+    RG_CUDA(h, cudaMemcpyAsync(out_rgb, h->d_out, (size_t)w * hh * 3 * sizeof(float), cudaMemcpyDeviceToHost, h->stream),
+            "copy image");
+  rg_render_stats tmp;
+  st = rg_sync_stats(h, stats ? stats : &tmp);
+  if (st != RG_OK) return st;
+  if (stats) stats->duration_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return RG_OK;
+}
+
+rg_status rg_render_async(rg_handle h, uint64_t seed, float* d_out_rgb, rg_render_stats* stats) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  cudaSetDevice(h->device);
+  if (!h->cam_ok) return fail(h, RG_INVALID_CAMERA, "camera viewport could not be calculated");
+  return render_frame(h, seed, d_out_rgb, stats);
+}
+
+rg_status rg_get_accumulation(rg_handle h, float* sum, uint32_t* frames) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  cudaSetDevice(h->device);
+  if (frames) *frames = h->pixel_accum;
+  if (!sum) return RG_OK;
+  size_t n = (size_t)h->opts.width * h->opts.height * 3;
+  if (!h->d_accum || h->acc_w != h->opts.width || h->acc_h != h->opts.height) {
+    std::memset(sum, 0, n * sizeof(float));
+    return RG_OK;
+  }
+  RG_CUDA(h, cudaMemcpyAsync(sum, h->d_accum, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "get accumulation");
+  RG_CUDA(h, cudaStreamSynchronize(h->stream), "get accumulation");
+  return RG_OK;
+}
+
+rg_status rg_set_accumulation(rg_handle h, const float* sum, uint32_t frames) {
+  if (!h || !sum) return fail(h, RG_INVALID_ARG, "rg_set_accumulation: NULL argument");
+  cudaSetDevice(h->device);
+  rg_status st = ensure_frame_buffers(h);
+  if (st != RG_OK) return st;
+  size_t n = (size_t)h->opts.width * h->opts.height * 3;
+  RG_CUDA(h, cudaMemcpyAsync(h->d_accum, sum, n * sizeof(float), cudaMemcpyHostToDevice, h->stream), "set accumulation");
+  RG_CUDA(h, cudaStreamSynchronize(h->stream), "set accumulation");
+  h->pixel_accum = frames;
+  h->frame_count = frames;
+  return RG_OK;
+}
+
+rg_status rg_frame_moments(rg_handle h, float* mean, float* variance) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  cudaSetDevice(h->device);
+  if (!h->d_fmean || h->frame_count == 0) return fail(h, RG_NOT_READY, "no frame has been rendered");
+  size_t n = (size_t)h->opts.width * h->opts.height * 3;
+  if (mean) RG_CUDA(h, cudaMemcpyAsync(mean, h->d_fmean, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "moments");
+  if (variance) RG_CUDA(h, cudaMemcpyAsync(variance, h->d_fvar, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "moments");
+  RG_CUDA(h, cudaStreamSynchronize(h->stream), "moments");
+  return RG_OK;
+}
+
+rg_status rg_query_rays(rg_handle h, uint32_t n, const float* origins, const float* dirs, const float* tmin,
+                        const float* tmax, const float* volume_u, rg_hit* out) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  if (n == 0) return RG_OK;
+  if (!origins || !dirs || !tmin || !tmax || !out) return fail(h, RG_INVALID_ARG, "rg_query_rays: NULL argument");
+  cudaSetDevice(h->device);
+  const size_t nv = h->gs.n_volumes;
+  float *d_o = nullptr, *d_d = nullptr, *d_t0 = nullptr, *d_t1 = nullptr, *d_u = nullptr;
+  rg_hit* d_out = nullptr;
+  rg_status st = RG_OK;
+  cudaError_t e = cudaSuccess;
+  do {
+    if ((e = cudaMalloc((void**)&d_o, 3ull * n * sizeof(float))) != cudaSuccess) break;
+    if ((e = cudaMalloc((void**)&d_d, 3ull * n * sizeof(float))) != cudaSuccess) break;
+    if ((e = cudaMalloc((void**)&d_t0, n * sizeof(float))) != cudaSuccess) break;
+    if ((e = cudaMalloc((void**)&d_t1, n * sizeof(float))) != cudaSuccess) break;
+    if ((e = cudaMalloc((void**)&d_out, n * sizeof(rg_hit))) != cudaSuccess) break;
+    if (volume_u && nv > 0 && (e = cudaMalloc((void**)&d_u, n * nv * sizeof(float))) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(d_o, origins, 3ull * n * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(d_d, dirs, 3ull * n * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(d_t0, tmin, n * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(d_t1, tmax, n * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
+    if (d_u && (e = cudaMemcpyAsync(d_u, volume_u, n * nv * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
+    if ((e = launch_query(h->gs, n, d_o, d_d, d_t0, d_t1, d_u, d_out, h->d_err, h->stream)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(out, d_out, n * sizeof(rg_hit), cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess) break;
+    e = cudaStreamSynchronize(h->stream);
+  } while (0);
+  if (e != cudaSuccess) st = cuda_fail(h, e, "rg_query_rays");
+  dfree(d_o); dfree(d_d); dfree(d_t0); dfree(d_t1); dfree(d_u); dfree(d_out);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,97 @@
+// renderer_state.h — the state behind an rg_handle, shared by the
+// translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rayna_gpu.h"
+#include "gpu_scene.h"
+
+namespace rg {
+
+struct HostViewport {
+  double pos[3], pixel_center[3], viewport_u[3], viewport_v[3], defocus_u[3], defocus_v[3];
+};
+
+// Host copy of a flattened scene (kept for the adjoint and for rebuilding).
+struct HostScene {
+  uint32_t ns = 0, nt = 0, nb = 0, nv = 0, nsdf = 0;
+  uint32_t sky = RG_SKY_SIMPLE;
+  uint32_t vol_base = 0;
+  int max_depth = 0;
+  std::vector<BvhNode2> nodes;
+  std::vector<GpuPrim> prims;
+  std::vector<float> tri_normals;
+  std::vector<rg_material> materials;
+  std::vector<rg_volume> volumes;
+  std::vector<GpuSdf> sdfs;
+};
+
+struct DeviceScene {
+  BvhNode2* nodes = nullptr;
+  GpuPrim* prims = nullptr;
+  float* tri_normals = nullptr;
+  rg_material* materials = nullptr;
+  GpuSdf* sdfs = nullptr;
+};
+
+// Wavefront queues (allocated on first use, sized by the path budget).
+struct WavefrontState {
+  size_t capacity = 0;
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+};
+
+}  // namespace rg
+
+struct rg_renderer {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  uint32_t form = RG_FORM_MEGAKERNEL;
+  uint32_t flags = 0;
+  std::string err;
+
+  bool have_scene = false;
+  rg::HostScene host;
+  rg::DeviceScene dev;
+  rg::GpuScene gs{};
+
+  rg_camera cam{};
+  bool cam_ok = false;
+  rg::HostViewport vp{};
+  rg_render_opts opts{};
+
+  uint32_t acc_w = 0, acc_h = 0;
+  float* d_accum = nullptr;
+  float* d_out = nullptr;
+  float* d_fmean = nullptr;
+  float* d_fvar = nullptr;
+  uint32_t frame_count = 0;   // AccumulationBuffer::counter
+  uint32_t pixel_accum = 0;   // AccumulationValue::accum (per pixel; equal for all pixels)
+  uint64_t last_samples = 0;
+
+  unsigned long long* d_counters = nullptr;
+  uint32_t* d_err = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  rg::WavefrontState wf;
+};
+
+namespace rg {
+
+// Defined in renderer.cpp
+rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs);
+void fill_frame_params(rg_renderer* h, uint64_t seed, FrameParams& fp);
+rg_status ensure_frame_buffers(rg_renderer* h);
+rg_status set_error(rg_renderer* h, rg_status st, const char* msg);
+
+// Defined in wavefront.cu
+cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp);
+void free_extra(rg_renderer* h);
+void on_scene_changed(rg_renderer* h);
+
+}  // namespace rg

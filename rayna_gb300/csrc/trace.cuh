@@ -1,0 +1,623 @@
+// trace.cuh — per-ray device code shared by every kernel form: camera rays,
+// closest-hit traversal of the binary BVH, the primitive tests, media,
+// sphere-traced SDFs, materials and the sky.
+//
+// Arithmetic contract: the library is compiled with -fmad=false, so every
+// fused multiply-add below is written out (__fmaf_rn) and every other
+// operation is a separately rounded IEEE op. With the same contract on the
+// host (-ffp-contract=off + explicit fma) the CPU oracle reproduces the
+// closed-form intersections bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "gpu_scene.h"
+
+namespace rg {
+
+// ---------------------------------------------------------------------------
+// Vector arithmetic
+// ---------------------------------------------------------------------------
+struct V3 { float x, y, z; };
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ V3 xyz(float4 f) { return v3(f.x, f.y, f.z); }
+
+// dot = fma(x, x', fma(y, y', z*z'))
+__device__ __forceinline__ float dot3(V3 a, V3 b) { return __fmaf_rn(a.x, b.x, __fmaf_rn(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ V3 cross3(V3 a, V3 b) {
+  return v3(__fmaf_rn(a.y, b.z, -(a.z * b.y)), __fmaf_rn(a.z, b.x, -(a.x * b.z)), __fmaf_rn(a.x, b.y, -(a.y * b.x)));
+}
+// Ray::at: pos + dir * t
+__device__ __forceinline__ V3 at3(V3 o, V3 d, float t) { return v3(__fmaf_rn(d.x, t, o.x), __fmaf_rn(d.y, t, o.y), __fmaf_rn(d.z, t, o.z)); }
+__device__ __forceinline__ float length3(V3 v) { return __fsqrt_rn(dot3(v, v)); }
+// glam normalize / try_normalize: v * (1 / |v|)
+__device__ __forceinline__ V3 normalize3(V3 v) { return v * __frcp_rn(length3(v)); }
+__device__ __forceinline__ bool try_normalize3(V3 v, V3& out) {
+  float r = __frcp_rn(length3(v));
+  if (isfinite(r) && r > 0.0f) { out = v * r; return true; }
+  return false;
+}
+__device__ __forceinline__ float signumf(float x) { return isnan(x) ? x : copysignf(1.0f, x); }
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based random numbers (Salmon et al., SC'11).
+// Block (pixel, sample, depth, purpose) keyed by the frame seed.
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+__device__ __forceinline__ U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return U4{c0, c1, c2, c3};
+}
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+__device__ __forceinline__ float u01_open0(uint32_t x) { return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f); }
+
+enum : uint32_t { kPurposeCamera = 0, kPurposeScatter = 1, kPurposeVolume0 = 2 };
+constexpr uint32_t kCameraDepth = 0xFFFFFFFFu;
+
+struct RngCtx {
+  uint32_t k0, k1, pix, smp, depth;
+  const float* vol_u;  // injected free-flight uniforms (ray queries) or null
+  __device__ __forceinline__ U4 block(uint32_t purpose) const { return philox(pix, smp, depth, purpose, k0, k1); }
+};
+
+// normal_on_unit_sphere (rayna_engine/src/shared/rng.rs:75-87)
+__device__ __forceinline__ V3 unit_sphere_from(float r1, float r2) {
+  const float two_pi = (float)(2.0 * 3.14159265358979323846);
+  float s = 2.0f * __fsqrt_rn(r2 * (1.0f - r2));
+  return v3(cosf(two_pi * r1) * s, sinf(two_pi * r1) * s, 1.0f - 2.0f * r2);
+}
+
+// ---------------------------------------------------------------------------
+// Rays
+// ---------------------------------------------------------------------------
+struct Ray {
+  V3 o, d, inv, noi;  // noi = -(o * inv), for the fused slab test
+};
+// Ray::new (rayna_engine/src/shared/ray.rs:15-23)
+__device__ __forceinline__ Ray make_ray(V3 o, V3 dir) {
+  Ray r;
+  r.o = o;
+  r.d = normalize3(dir);
+  r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
+  r.noi = v3(-(o.x * r.inv.x), -(o.y * r.inv.y), -(o.z * r.inv.z));
+  return r;
+}
+
+// Aabb::hit (rayna_engine/src/shared/aabb.rs:117-153) against [start, end];
+// returns the entry distance in `tnear`.
+__device__ __forceinline__ bool slab(float lx, float hx, float ly, float hy, float lz, float hz, const Ray& r, float start,
+                                     float end, float& tnear) {
+  float t1x = __fmaf_rn(lx, r.inv.x, r.noi.x), t2x = __fmaf_rn(hx, r.inv.x, r.noi.x);
+  float t1y = __fmaf_rn(ly, r.inv.y, r.noi.y), t2y = __fmaf_rn(hy, r.inv.y, r.noi.y);
+  float t1z = __fmaf_rn(lz, r.inv.z, r.noi.z), t2z = __fmaf_rn(hz, r.inv.z, r.noi.z);
+  float tmin = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fminf(t1z, t2z));
+  float tmax = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fmaxf(t1z, t2z));
+  float low = fmaxf(tmin, start), high = fminf(tmax, end);
+  tnear = low;
+  return low <= high;
+}
+
+// ---------------------------------------------------------------------------
+// Primitive tests. Each returns the hit distance through `t` when it hits
+// inside [start, end]. Full hit records are built once, for the closest hit.
+// ---------------------------------------------------------------------------
+// SphereMesh::intersect (mesh/primitive/sphere.rs:44-99)
+__device__ __forceinline__ bool sphere_t(V3 c, float r2, const Ray& r, float start, float end, float& t) {
+  V3 oc = r.o - c;
+  float half_b = dot3(oc, r.d);
+  float cc = __fmaf_rn(oc.x, oc.x, __fmaf_rn(oc.y, oc.y, __fmaf_rn(oc.z, oc.z, -r2)));
+  float disc = __fmaf_rn(half_b, half_b, -cc);
+  if (disc < 0.0f) return false;
+  float sq = __fsqrt_rn(disc);
+  float root = -half_b - sq;
+  if (!(start <= root && root <= end)) {
+    root = -half_b + sq;
+    if (!(start <= root && root <= end)) return false;
+  }
+  t = root;
+  return true;
+}
+
+// Triangle::intersect (mesh/primitive/triangle.rs:53-109), Moller-Trumbore
+// with precomputed edges e1 = v1 - v0, e2 = v2 - v0. Outputs u, v, det.
+__device__ __forceinline__ bool triangle_t(V3 v0, V3 e1, V3 e2, const Ray& r, float start, float end, float& t, float& u,
+                                           float& v, float& det) {
+  V3 pvec = cross3(r.d, e2);
+  det = dot3(e1, pvec);
+  if (det == 0.0f) return false;
+  float inv_det = __frcp_rn(det);
+  V3 tvec = r.o - v0;
+  u = dot3(tvec, pvec) * inv_det;
+  if (u < 0.0f || u > 1.0f) return false;
+  V3 qvec = cross3(tvec, e1);
+  v = dot3(r.d, qvec) * inv_det;
+  if (v < 0.0f || u + v > 1.0f) return false;
+  t = dot3(e2, qvec) * inv_det;
+  return start <= t && t <= end;
+}
+
+// Triangle::interpolate_normals (triangle.rs:114-119): fold from zero.
+__device__ __forceinline__ bool tri_normal(const float* n9, float u, float v, V3& out) {
+  float b0 = (1.0f - u) - v;
+  V3 n0 = v3(__ldg(n9 + 0), __ldg(n9 + 1), __ldg(n9 + 2));
+  V3 n1 = v3(__ldg(n9 + 3), __ldg(n9 + 4), __ldg(n9 + 5));
+  V3 n2 = v3(__ldg(n9 + 6), __ldg(n9 + 7), __ldg(n9 + 8));
+  V3 n = v3(__fmaf_rn(n2.x, v, __fmaf_rn(n1.x, u, n0.x * b0)), __fmaf_rn(n2.y, v, __fmaf_rn(n1.y, u, n0.y * b0)),
+            __fmaf_rn(n2.z, v, __fmaf_rn(n1.z, u, n0.z * b0)));
+  return try_normalize3(n, out);
+}
+
+struct BoxHit { float t; int axis; float u0, u1; float winding; float sgn; };
+
+// AxisBoxMesh::intersect (mesh/primitive/axis_box.rs:64-145), Majercik et al. 2018.
+__device__ __forceinline__ bool box_t(V3 centre, V3 radius, V3 inv_radius, const Ray& r, float start, float end, BoxHit& bh) {
+  V3 ro = r.o - centre;
+  V3 rd = r.d;
+  float qx = fabsf(ro.x) * inv_radius.x, qy = fabsf(ro.y) * inv_radius.y, qz = fabsf(ro.z) * inv_radius.z;
+  float winding = signumf(fmaxf(qx, fmaxf(qy, qz)) - 1.0f);
+  V3 sgn = v3(-signumf(rd.x), -signumf(rd.y), -signumf(rd.z));
+  float pd[3] = {((radius.x * winding) * sgn.x - ro.x) * r.inv.x, ((radius.y * winding) * sgn.y - ro.y) * r.inv.y,
+                 ((radius.z * winding) * sgn.z - ro.z) * r.inv.z};
+  float rov[3] = {ro.x, ro.y, ro.z}, rdv[3] = {rd.x, rd.y, rd.z}, rad[3] = {radius.x, radius.y, radius.z};
+  float sg[3] = {sgn.x, sgn.y, sgn.z};
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    float dist = pd[ax];
+    if (!(start <= dist && dist <= end)) continue;
+    int a1 = ax == 0 ? 1 : (ax == 1 ? 2 : 0);
+    int a2 = ax == 0 ? 2 : (ax == 1 ? 0 : 1);
+    float u0 = __fmaf_rn(rdv[a1], dist, rov[a1]);
+    float u1 = __fmaf_rn(rdv[a2], dist, rov[a2]);
+    if (fabsf(u0) < rad[a1] && fabsf(u1) < rad[a2]) {
+      bh.t = dist; bh.axis = ax; bh.u0 = u0 / rad[a1]; bh.u1 = u1 / rad[a2]; bh.winding = winding; bh.sgn = sg[ax];
+      return true;
+    }
+  }
+  return false;
+}
+
+__device__ __forceinline__ uint32_t prim_kind(const GpuPrim& p) { return __float_as_uint(p.a.w) >> kKindShift; }
+__device__ __forceinline__ uint32_t prim_material(const GpuPrim& p) { return __float_as_uint(p.a.w) & kMaterialMask; }
+__device__ __forceinline__ uint32_t prim_id(const GpuPrim& p) { return __float_as_uint(p.b.w); }
+
+// Boundary intersection of a medium with an interval given by [start, end]
+// (+-infinity stand for absent bounds).
+__device__ __forceinline__ bool boundary_t(const GpuPrim& p, uint32_t kind, const Ray& r, float start, float end, float& t) {
+  if (kind == PK_VOL_SPHERE) return sphere_t(xyz(p.a), p.b.y, r, start, end, t);
+  BoxHit bh;
+  if (!box_t(xyz(p.a), xyz(p.b), xyz(p.c), r, start, end, bh)) return false;
+  t = bh.t;
+  return true;
+}
+
+// VolumetricObject::full_intersect (object/volumetric.rs:86-160).
+__device__ __forceinline__ bool volume_t(const GpuPrim& p, uint32_t kind, uint32_t vol_index, const Ray& r, float start,
+                                         float end, const RngCtx& ctx, float& t) {
+  float d_enter, d_exit;
+  if (!boundary_t(p, kind, r, -CUDART_INF_F, CUDART_INF_F, d_enter)) return false;
+  float enter = fmaxf(d_enter, start);
+  if (!boundary_t(p, kind, r, enter + 0.001f, CUDART_INF_F, d_exit)) return false;
+  float exitd = fminf(d_exit, end);
+  float inside = exitd - enter;
+  float u = ctx.vol_u ? ctx.vol_u[vol_index] : u01_open0(ctx.block(kPurposeVolume0 + vol_index).x);
+  float neg_inv_density = kind == PK_VOL_SPHERE ? p.b.z : p.c.w;
+  float hit_dist = neg_inv_density * logf(u);
+  if (hit_dist > inside) return false;
+  t = enter + hit_dist;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Signed distance functions (world space) and the sphere tracer.
+// ---------------------------------------------------------------------------
+constexpr float kBulbInner = 1.2f, kBulbOuter = 1.5f;
+
+__device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x) {
+  V3 q = x - v3(s.cx, s.cy, s.cz);
+  if (s.kind == RG_SDF_SPHERE) return length3(q) - s.p0;
+  if (s.kind == RG_SDF_TORUS) {
+    float a = __fsqrt_rn(q.x * q.x + q.z * q.z) - s.p0;
+    return __fsqrt_rn(a * a + q.y * q.y) - s.p1;
+  }
+  // Mandelbulb distance estimator: z -> z^power + c in spherical coordinates
+  // with the running derivative dr; outside kBulbOuter the distance to the
+  // enclosing sphere of radius kBulbInner is used (a lower bound).
+  float sc = s.p2;
+  V3 z0 = v3(q.x / sc, q.y / sc, q.z / sc);
+  float rq = length3(z0);
+  if (rq > kBulbOuter) return (rq - kBulbInner) * sc;
+  float power = s.p0;
+  int iters = (int)s.p1;
+  V3 z = z0;
+  float dr = 1.0f, rr = 0.0f;
+  for (int i = 0; i < iters; ++i) {
+    rr = length3(z);
+    if (rr > 2.0f) break;
+    float theta = acosf(z.z / rr);
+    float phi = atan2f(z.y, z.x);
+    dr = powf(rr, power - 1.0f) * power * dr + 1.0f;
+    float zr = powf(rr, power);
+    theta = theta * power;
+    phi = phi * power;
+    float st = sinf(theta);
+    z = v3(zr * (st * cosf(phi)), zr * (sinf(phi) * st), zr * cosf(theta)) + z0;
+  }
+  return (0.5f * logf(rr) * rr / dr) * sc;
+}
+
+struct SdfHit { float t; V3 n; bool front; uint32_t side; };
+
+// RaymarchedIsosurfaceMesh::intersect (mesh/isosurface/raymarched.rs:73-122)
+// with two exact early exits that cannot change the result:
+//  - total distance is non-decreasing, so once it passes the distance that
+//    must be beaten (`beat`, inclusive when nothing has been hit yet) no later
+//    step can produce the closest hit;
+//  - outside the function's bound radius and moving away, every later step
+//    evaluates to more than epsilon, so no later step can hit.
+template <bool COUNT>
+__device__ bool sdf_march(const GpuSdf& s, const Ray& r, float start, float end, float beat, bool beat_inclusive, SdfHit& h,
+                          unsigned long long& steps) {
+  float eps = s.eps;
+  float total = start;
+  V3 c = v3(s.cx, s.cy, s.cz);
+  V3 point = at3(r.o, r.d, total);
+  float br2 = s.bound_radius * s.bound_radius;
+  for (uint32_t i = 0;; ++i) {
+    float d = sdf_eval(s, point);
+    if (COUNT) ++steps;
+    total = total + fabsf(d);
+    point = at3(r.o, r.d, total);
+    if (fabsf(d) < eps && start <= total && total <= end) {
+      if (!(beat_inclusive ? total <= beat : total < beat)) return false;
+      V3 pp = point;
+      V3 g = v3(sdf_eval(s, v3(pp.x + eps, pp.y, pp.z)) - sdf_eval(s, v3(pp.x - eps, pp.y, pp.z)),
+                sdf_eval(s, v3(pp.x, pp.y + eps, pp.z)) - sdf_eval(s, v3(pp.x, pp.y - eps, pp.z)),
+                sdf_eval(s, v3(pp.x, pp.y, pp.z + eps)) - sdf_eval(s, v3(pp.x, pp.y, pp.z - eps)));
+      h.t = total;
+      h.n = normalize3(g);
+      h.front = !signbit(d);
+      h.side = i;
+      return true;
+    }
+    if (i > s.max_iter) return false;
+    if (!(beat_inclusive ? total <= beat : total < beat)) return false;
+    V3 q = point - c;
+    if (dot3(q, q) > br2 && dot3(q, r.d) > 0.0f) return false;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Closest hit over the BVH and the unbounded list.
+// ---------------------------------------------------------------------------
+struct HitRec {
+  float t;
+  int prim;      // index into the reordered prim array, or -1
+  int sdf;       // SDF index when an unbounded object won, else -1
+  SdfHit sh;
+};
+
+struct Counters {
+  unsigned long long nodes = 0, prims = 0, sdf_steps = 0;
+};
+
+// Test the primitives of one leaf, shrinking `end` to each accepted hit
+// (object/bvh.rs:82-96: a later hit at equal distance replaces the earlier).
+template <bool COUNT>
+__device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int count, const Ray& r, float start, float& end,
+                                          int& best, const RngCtx& ctx, Counters& cnt) {
+  for (int i = first; i < first + count; ++i) {
+    const GpuPrim* pp = sc.prims + i;
+    float4 a = __ldg(&pp->a);
+    uint32_t kind = __float_as_uint(a.w) >> kKindShift;
+    if (COUNT) ++cnt.prims;
+    float t;
+    if (kind == PK_TRIANGLE) {
+      float4 b = __ldg(&pp->b), c = __ldg(&pp->c);
+      float u, v, det;
+      if (!triangle_t(xyz(a), xyz(b), xyz(c), r, start, end, t, u, v, det)) continue;
+      if (__float_as_uint(c.w) & kTriCheckNormals) {
+        V3 n;
+        if (!tri_normal(sc.tri_normals + 9ull * (__float_as_uint(b.w) - sc.tri_base), u, v, n)) continue;
+      }
+    } else if (kind == PK_SPHERE) {
+      float4 b = __ldg(&pp->b);
+      if (!sphere_t(xyz(a), b.y, r, start, end, t)) continue;
+    } else if (kind == PK_BOX) {
+      float4 b = __ldg(&pp->b), c = __ldg(&pp->c);
+      BoxHit bh;
+      if (!box_t(xyz(a), xyz(b), xyz(c), r, start, end, bh)) continue;
+      t = bh.t;
+    } else {
+      GpuPrim p;
+      p.a = a; p.b = __ldg(&pp->b); p.c = __ldg(&pp->c);
+      if (!volume_t(p, kind, __float_as_uint(p.b.w) - sc.vol_base, r, start, end, ctx, t)) continue;
+    }
+    end = t;
+    best = i;
+  }
+}
+
+template <bool COUNT>
+__device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float end, const RngCtx& ctx, HitRec& h,
+                            Counters& cnt, uint32_t* err) {
+  int best = -1;
+  float tmax = end;
+  if (sc.n_nodes > 0) {
+    int stack[kStackSize];
+    int sp = 0;
+    int node = 0;
+    while (node >= 0) {
+      const BvhNode2* np = sc.nodes + node;
+      float4 xs = __ldg(&np->xs), ys = __ldg(&np->ys), zs = __ldg(&np->zs);
+      int4 m = __ldg(&np->meta);
+      if (COUNT) ++cnt.nodes;
+      float tn0, tn1;
+      bool h0 = slab(xs.x, xs.y, ys.x, ys.y, zs.x, zs.y, r, start, tmax, tn0);
+      bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, tmax, tn1);
+      if (h0 && m.z > 0) { test_leaf<COUNT>(sc, m.x, m.z, r, start, tmax, best, ctx, cnt); h0 = false; }
+      if (h1 && m.w > 0) { test_leaf<COUNT>(sc, m.y, m.w, r, start, tmax, best, ctx, cnt); h1 = false; }
+      if (h0 && h1) {
+        bool swap = tn1 < tn0;
+        int nearc = swap ? m.y : m.x, farc = swap ? m.x : m.y;
+        if (sp < kStackSize) stack[sp++] = farc;
+        else atomicOr(err, ERR_STACK_OVERFLOW);
+        node = nearc;
+      } else if (h0) {
+        node = m.x;
+      } else if (h1) {
+        node = m.y;
+      } else {
+        node = sp > 0 ? stack[--sp] : -1;
+      }
+    }
+  }
+  h.prim = best;
+  h.sdf = -1;
+  h.t = tmax;
+  bool any = best >= 0;
+  // ObjectList::full_intersect (object/list.rs:112-129): every unbounded object
+  // with the original interval; it replaces the result only if strictly closer.
+  for (uint32_t k = 0; k < sc.n_sdfs; ++k) {
+    SdfHit sh;
+    if (sdf_march<COUNT>(sc.sdfs[k], r, start, end, any ? h.t : end, !any, sh, cnt.sdf_steps)) {
+      h.t = sh.t;
+      h.sdf = (int)k;
+      h.sh = sh;
+      any = true;
+    }
+  }
+  return any;
+}
+
+// Full hit record of the closest hit.
+struct Surface {
+  V3 pos, normal, ray_normal;
+  bool front;
+  uint32_t material, prim_id, side;
+  float u, v;
+};
+
+__device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, const HitRec& h, const RngCtx& ctx, Surface& s) {
+  if (h.sdf >= 0) {
+    const GpuSdf& f = sc.sdfs[h.sdf];
+    s.pos = at3(r.o, r.d, h.t);
+    s.normal = h.sh.n;
+    s.ray_normal = h.sh.n;  // raymarched.rs:113-114: not flipped
+    s.front = h.sh.front;
+    s.material = f.material;
+    s.prim_id = f.prim_id;
+    s.side = h.sh.side;
+    s.u = s.v = 0.0f;
+    return;
+  }
+  const GpuPrim p = sc.prims[h.prim];
+  uint32_t kind = prim_kind(p);
+  s.material = prim_material(p);
+  s.prim_id = prim_id(p);
+  s.pos = at3(r.o, r.d, h.t);
+  s.side = 0;
+  if (kind == PK_SPHERE) {
+    V3 c = xyz(p.a);
+    float rad = p.b.x;
+    V3 local = v3((s.pos.x - c.x) / rad, (s.pos.y - c.y) / rad, (s.pos.z - c.z) / rad);
+    bool inside = dot3(r.d, local) > 0.0f;
+    s.normal = local;
+    s.ray_normal = inside ? -local : local;
+    s.front = !inside;
+    s.u = s.v = 0.0f;  // sphere_uv is only needed by textured / Uv modes
+  } else if (kind == PK_TRIANGLE) {
+    float t, u, v, det;
+    triangle_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, CUDART_INF_F, t, u, v, det);
+    V3 n;
+    tri_normal(sc.tri_normals + 9ull * (s.prim_id - sc.tri_base), u, v, n);
+    s.normal = n;
+    s.ray_normal = n * (-signumf(det));
+    s.front = signbit(det);
+    s.u = u; s.v = v;
+  } else if (kind == PK_BOX) {
+    BoxHit bh;
+    box_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, h.t, bh);
+    V3 rn = v3(bh.axis == 0 ? bh.sgn : 0.0f, bh.axis == 1 ? bh.sgn : 0.0f, bh.axis == 2 ? bh.sgn : 0.0f);
+    s.ray_normal = rn;
+    s.normal = rn * bh.winding;
+    s.front = !signbit(bh.winding);
+    s.side = (uint32_t)bh.axis * 2u + (bh.sgn > 0.0f ? 1u : 0u);
+    s.u = (bh.u0 + 1.0f) / 2.0f;
+    s.v = (bh.u1 + 1.0f) / 2.0f;
+  } else {
+    // Media: arbitrary normals drawn from the free-flight block (volumetric.rs:147-153)
+    uint32_t vi = s.prim_id - sc.vol_base;
+    U4 b = ctx.vol_u ? U4{0, 0, 0, 0} : ctx.block(kPurposeVolume0 + vi);
+    s.normal = unit_sphere_from(u01(b.y), u01(b.z));
+    s.ray_normal = s.normal;
+    s.front = true;
+    s.u = s.v = u01(b.w);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Materials, sky
+// ---------------------------------------------------------------------------
+struct C3f { float r, g, b; };
+
+// Skybox::sky_colour (skybox/simple.rs:12-30, skybox/none.rs:8-13)
+__device__ __forceinline__ C3f sky_colour(uint32_t sky, V3 dir) {
+  if (sky == RG_SKY_WHITE) return C3f{1.0f, 1.0f, 1.0f};
+  if (sky == RG_SKY_NONE) return C3f{0.0f, 0.0f, 0.0f};
+  float a = 0.5f * dir.y + 0.5f;
+  return C3f{1.0f + (0.5f - 1.0f) * a, 1.0f + (0.7f - 1.0f) * a, 1.0f + (1.0f - 1.0f) * a};
+}
+
+// Material::scatter (material/*.rs) with inverse-CDF samplers of the same
+// distributions as the reference's rejection samplers.
+__device__ __forceinline__ bool scatter(const rg_material& m, const Ray& ray, const Surface& s, const RngCtx& ctx, V3& out) {
+  U4 b = ctx.block(kPurposeScatter);
+  switch (m.kind) {
+    case RG_MAT_LAMBERTIAN: {
+      // uniform in the unit ball: uniform direction times cbrt(U) radius
+      const float two_pi = (float)(2.0 * 3.14159265358979323846);
+      float z = 1.0f - 2.0f * u01(b.x);
+      float phi = two_pi * u01(b.y);
+      float sn = __fsqrt_rn(fmaxf(0.0f, 1.0f - z * z));
+      float rad = cbrtf(u01(b.z));
+      V3 rnd = v3(sn * cosf(phi) * rad, sn * sinf(phi) * rad, z * rad);
+      V3 vec = s.ray_normal + rnd;
+      if (!try_normalize3(vec, out)) out = s.ray_normal;
+      return true;
+    }
+    case RG_MAT_METAL: {
+      V3 d = ray.d;
+      V3 refl = d - s.ray_normal * (2.0f * dot3(d, s.ray_normal));
+      V3 rnd = unit_sphere_from(u01(b.x), u01(b.y));
+      V3 vec = refl + rnd * m.fuzz;
+      if (!(dot3(vec, s.ray_normal) > 0.0f)) return false;
+      out = normalize3(vec);
+      return true;
+    }
+    case RG_MAT_DIELECTRIC: {
+      float ior = m.refractive_index;
+      float ratio = s.front ? __frcp_rn(ior) : ior;
+      V3 d = ray.d;
+      float cos_t = fminf(dot3(-d, s.ray_normal), 1.0f);
+      float sin_t = __fsqrt_rn(1.0f - cos_t * cos_t);
+      bool tir = ratio * sin_t > 1.0f;
+      float r0 = (1.0f - ratio) / (1.0f + ratio);
+      float r02 = r0 * r0;
+      float x = 1.0f - cos_t;
+      float x2 = x * x;
+      float x5 = (x2 * x2) * x;
+      float refl_p = r02 + (1.0f - r02) * x5;
+      bool schlick = refl_p > u01(b.x);
+      if (tir || schlick) {
+        out = d - s.ray_normal * (2.0f * dot3(d, s.ray_normal));
+      } else {  // math::refract (shared/math.rs:20-25)
+        float c2 = fminf(dot3(-d, s.ray_normal), 1.0f);
+        V3 perp = (d + s.ray_normal * c2) * ratio;
+        V3 par = s.ray_normal * (-__fsqrt_rn(fabsf(1.0f - dot3(perp, perp))));
+        out = perp + par;
+      }
+      return true;
+    }
+    case RG_MAT_ISOTROPIC:
+      out = unit_sphere_from(u01(b.x), u01(b.y));
+      return true;
+    default:
+      return false;
+  }
+}
+
+// Material::reflected_light as the factor multiplying future_col.
+__device__ __forceinline__ C3f attenuation(const rg_material& m, const Ray& ray, const Surface& s) {
+  C3f alb{m.albedo[0], m.albedo[1], m.albedo[2]};
+  if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) return alb;
+  if (m.kind == RG_MAT_DIELECTRIC && s.front) return C3f{1.0f, 1.0f, 1.0f};
+  float dist = length3(s.pos - ray.o);
+  float e = expf(-m.density * dist);
+  return C3f{alb.r * e, alb.g * e, alb.b * e};
+}
+
+// ---------------------------------------------------------------------------
+// Camera: render_px_msaa stratification (render/renderer.rs:350-389) and
+// Viewport::calc_ray (scene/camera.rs:191-213).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ Ray camera_ray(const FrameParams& fp, uint32_t x, uint32_t y, uint32_t s, const RngCtx& ctx) {
+  const float two_pi = (float)(2.0 * 3.14159265358979323846);
+  U4 b = philox(ctx.pix, ctx.smp, kCameraDepth, kPurposeCamera, ctx.k0, ctx.k1);
+  float jx = u01(b.x) - 0.5f, jy = u01(b.y) - 0.5f;
+  float lr = __fsqrt_rn(u01(b.z));
+  float ph = two_pi * u01(b.w);
+  float lx = lr * cosf(ph), ly = lr * sinf(ph);
+  float fx, fy;
+  uint32_t d = fp.strat_d;
+  if (s < d * d) {
+    float dinv = fp.strat_inv;
+    uint32_t i = s % d, j = s / d;
+    fx = ((float)x + jx * dinv) + (float)i * dinv;
+    fy = ((float)y + jy * dinv) + (float)j * dinv;
+  } else {
+    fx = (float)x + jx;
+    fy = (float)y + jy;
+  }
+  float w = (float)fp.width, h = (float)fp.height;
+  float u = (fx - (w / 2.0f)) / h;
+  float v = (fy - (h / 2.0f)) / h;
+  V3 pc = v3(fp.pixel_center[0], fp.pixel_center[1], fp.pixel_center[2]);
+  V3 vu = v3(fp.viewport_u[0], fp.viewport_u[1], fp.viewport_u[2]);
+  V3 vv = v3(fp.viewport_v[0], fp.viewport_v[1], fp.viewport_v[2]);
+  V3 pos = v3(fp.pos[0], fp.pos[1], fp.pos[2]);
+  V3 du = v3(fp.defocus_u[0], fp.defocus_u[1], fp.defocus_u[2]);
+  V3 dv = v3(fp.defocus_v[0], fp.defocus_v[1], fp.defocus_v[2]);
+  V3 ps = (pc + vu * u) + vv * v;
+  V3 rpos = (pos + du * lx) + dv * ly;
+  return make_ray(rpos, ps - rpos);
+}
+
+// One path sample: ray_colour_recursive (renderer.rs:508-572) evaluated front
+// to back: L = sum_k beta_k * emitted_k + beta_K * sky.
+template <bool COUNT>
+__device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x, uint32_t y, uint32_t s, Counters& cnt,
+                          uint32_t& segments) {
+  RngCtx ctx{fp.seed_lo, fp.seed_hi, y * fp.width + x, s, 0, nullptr};
+  Ray ray = camera_ray(fp, x, y, s, ctx);
+  C3f L{0.0f, 0.0f, 0.0f}, beta{1.0f, 1.0f, 1.0f};
+  for (uint32_t depth = 0; depth <= fp.ray_depth; ++depth) {
+    ctx.depth = depth;
+    HitRec h;
+    ++segments;
+    if (!closest_hit<COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
+      C3f sk = sky_colour(sc.sky, ray.d);
+      L = C3f{L.r + beta.r * sk.r, L.g + beta.g * sk.g, L.b + beta.b * sk.b};
+      break;
+    }
+    Surface surf;
+    finalize_hit(sc, ray, h, ctx, surf);
+    const rg_material m = sc.materials[surf.material];
+    if (m.kind == RG_MAT_LIGHT) {
+      L = C3f{L.r + beta.r * m.albedo[0], L.g + beta.g * m.albedo[1], L.b + beta.b * m.albedo[2]};
+      break;
+    }
+    V3 dir;
+    if (!scatter(m, ray, surf, ctx, dir)) break;
+    C3f a = attenuation(m, ray, surf);
+    beta = C3f{beta.r * a.r, beta.g * a.g, beta.b * a.b};
+    ray = make_ray(surf.pos, dir);
+  }
+  return L;
+}
+
+}  // namespace rg

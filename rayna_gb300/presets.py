@@ -1,0 +1,248 @@
+"""Seeded synthetic workloads of the path-tracing hot path.
+
+* ``random_spheres`` — "Ray Tracing in One Weekend" random spheres, the scene
+  the reference's RTIAW_DEMO preset renders (scene/preset.rs:157-254), with
+  the sizes and material draws of the random-spheres workload: ground sphere
+  r=1000, 22x22 grid of r=0.2 spheres, three r=1 spheres. 400x225, 32 spp,
+  depth 50.
+* ``cornell_mesh`` — a displaced icosphere (8 subdivisions: 1,310,720
+  triangles) inside a Cornell box of 12 triangles lit by a 0.25x0.25 quad of
+  radiance 15, after the reference's CORNELL preset (preset.rs:608-683).
+  1024x1024, 64 spp, depth 8.
+* ``sdf_volumes`` — power-8 Mandelbulb (metal, fuzz 0.1) and torus
+  (dielectric 1.5) sphere-traced SDFs, a sphere medium of density 0.2 and a
+  box medium of random density/albedo, 100 random Lambertian spheres.
+  1280x720, 128 spp, depth 16.
+
+All draws come from numpy's PCG64 seeded with `seed`.
+
+Triangle winding: the reference's Triangle::intersect reports the front face
+when det < 0 and orients ray_normal by -sign(det) (triangle.rs:95-105), so a
+face is seen from the front when e1 x e2 points away from the viewer. Meshes
+here are wound that way: e1 x e2 opposite to the vertex normals.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .scene import (
+    Angle, AxisBoxMesh, BvhMesh, Camera, DielectricMaterial, IsotropicMaterial, LambertianMaterial,
+    LightMaterial, MetalMaterial, NoSkybox, RaymarchedIsosurfaceMesh, RenderOpts, Scene, SdfMandelbulb,
+    SdfTorus, SimpleObject, SimpleSkybox, SphereMesh, Triangle, VolumetricObject,
+)
+
+
+def look_at_camera(pos, target, v_fov_deg, focus_dist=None, defocus_angle_rad=0.0) -> Camera:
+    pos = np.asarray(pos, float)
+    d = np.asarray(target, float) - pos
+    fwd = d / np.linalg.norm(d)
+    return Camera(pos=tuple(pos), v_fov=Angle.from_degrees(v_fov_deg), fwd=tuple(fwd),
+                  focus_dist=float(np.linalg.norm(d) if focus_dist is None else focus_dist),
+                  defocus_angle=Angle(defocus_angle_rad))
+
+
+# ---------------------------------------------------------------------------
+# Random spheres
+# ---------------------------------------------------------------------------
+def random_spheres(seed: int = 0, grid: int = 11, extra_spheres: int = 0):
+    """Returns (scene, camera, opts) of the random-spheres workload.
+
+    `extra_spheres` adds further r=0.2 Lambertian spheres on a wider grid.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    objs = [SimpleObject(SphereMesh((0.0, -1000.0, 0.0), 1000.0), LambertianMaterial((0.5, 0.5, 0.5)))]
+    for a in range(-grid, grid):
+        for b in range(-grid, grid):
+            centre = (a + 0.9 * rng.random(), 0.2, b + 0.9 * rng.random())
+            choose = rng.random()
+            if choose < 0.8:
+                alb = tuple(rng.random(3) * rng.random(3))
+                mat = LambertianMaterial(alb)
+            elif choose < 0.95:
+                mat = MetalMaterial(tuple(0.5 + 0.5 * rng.random(3)), 0.5 * rng.random())
+            else:
+                mat = DielectricMaterial((1.0, 1.0, 1.0), 1.5, 0.0)
+            objs.append(SimpleObject(SphereMesh(centre, 0.2), mat))
+    side = int(math.ceil(math.sqrt(max(extra_spheres, 0))))
+    for k in range(extra_spheres):
+        i, j = divmod(k, side)
+        centre = (-side / 2 + i + 0.9 * rng.random(), 0.2, -side / 2 - 12 + j + 0.9 * rng.random())
+        objs.append(SimpleObject(SphereMesh(centre, 0.2), LambertianMaterial(tuple(rng.random(3)))))
+    objs.append(SimpleObject(SphereMesh((0.0, 1.0, 0.0), 1.0), DielectricMaterial((1.0, 1.0, 1.0), 1.5, 0.0)))
+    objs.append(SimpleObject(SphereMesh((-4.0, 1.0, 0.0), 1.0), LambertianMaterial((0.4, 0.2, 0.1))))
+    objs.append(SimpleObject(SphereMesh((4.0, 1.0, 0.0), 1.0), MetalMaterial((0.7, 0.6, 0.5), 0.0)))
+    scene = Scene(objects=objs, skybox=SimpleSkybox())
+    # aperture 0.1 at focus distance 10: lens radius 0.05 = 10 * tan(angle / 2)
+    cam = look_at_camera((13.0, 2.0, 3.0), (0.0, 0.0, 0.0), 20.0, focus_dist=10.0,
+                         defocus_angle_rad=2.0 * math.atan(0.05 / 10.0))
+    opts = RenderOpts(width=400, height=225, samples=32, ray_depth=50)
+    return scene, cam, opts
+
+
+# ---------------------------------------------------------------------------
+# Displaced icosphere in a Cornell box
+# ---------------------------------------------------------------------------
+def icosphere(level: int):
+    """Unit icosphere: (vertices (V,3) float64, faces (F,3) int64), outward CCW faces."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], float)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+                  [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5],
+                  [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]], np.int64)
+    for _ in range(level):
+        a, b, c = f[:, 0], f[:, 1], f[:, 2]
+        edges = np.concatenate([np.stack([a, b], 1), np.stack([b, c], 1), np.stack([c, a], 1)])
+        key = np.sort(edges, axis=1)
+        uniq, inv = np.unique(key[:, 0] * (v.shape[0] + 1) + key[:, 1], return_inverse=True)
+        e0 = uniq // (v.shape[0] + 1)
+        e1 = uniq % (v.shape[0] + 1)
+        mid = v[e0] + v[e1]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        base = v.shape[0]
+        v = np.concatenate([v, mid])
+        nf = f.shape[0]
+        ab, bc, ca = inv[:nf] + base, inv[nf:2 * nf] + base, inv[2 * nf:] + base
+        f = np.concatenate([np.stack([a, ab, ca], 1), np.stack([b, bc, ab], 1), np.stack([c, ca, bc], 1),
+                            np.stack([ab, bc, ca], 1)])
+    return v, f
+
+
+def _hash3(ix, iy, iz, seed: int):
+    """Lattice hash to [0,1): a 32-bit integer mix (PCG output permutation)."""
+    h = (ix.astype(np.uint64) * np.uint64(73856093)) ^ (iy.astype(np.uint64) * np.uint64(19349663)) ^ \
+        (iz.astype(np.uint64) * np.uint64(83492791)) ^ np.uint64(seed * 2654435761 & 0xFFFFFFFF)
+    h = h & np.uint64(0xFFFFFFFF)
+    h = (h * np.uint64(747796405) + np.uint64(2891336453)) & np.uint64(0xFFFFFFFF)
+    w = (((h >> ((h >> np.uint64(28)) + np.uint64(4))) ^ h) * np.uint64(277803737)) & np.uint64(0xFFFFFFFF)
+    w = (w >> np.uint64(22)) ^ w
+    return (w & np.uint64(0xFFFFFF)).astype(np.float64) / float(1 << 24)
+
+
+def value_noise(p: np.ndarray, seed: int, octaves: int = 3, freq: float = 4.0) -> np.ndarray:
+    """Seeded fractal value noise in [-1, 1]: trilinear lattice noise with a
+    smoothstep fade, octaves at doubling frequency and halving amplitude."""
+    total = np.zeros(p.shape[0])
+    amp, norm = 1.0, 0.0
+    for o in range(octaves):
+        q = p * freq * (2.0 ** o)
+        i = np.floor(q)
+        fr = q - i
+        s = fr * fr * (3.0 - 2.0 * fr)
+        i = i.astype(np.int64)
+        acc = np.zeros(p.shape[0])
+        for dx in (0, 1):
+            for dy in (0, 1):
+                for dz in (0, 1):
+                    w = (s[:, 0] if dx else 1 - s[:, 0]) * (s[:, 1] if dy else 1 - s[:, 1]) * (s[:, 2] if dz else 1 - s[:, 2])
+                    acc += w * _hash3(i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz, seed + 7919 * o)
+        total += amp * (2.0 * acc - 1.0)
+        norm += amp
+        amp *= 0.5
+    return total / norm
+
+
+def displaced_icosphere(level: int, centre, radius: float, seed: int = 0, amplitude: float = 0.05):
+    """Triangles (F,3,3) and vertex normals (F,3,3) of a noise-displaced
+    icosphere, wound with e1 x e2 opposite to the (outward) vertex normals."""
+    v, f = icosphere(level)
+    disp = v * (1.0 + amplitude * value_noise(v, seed))[:, None]
+    pos = disp * radius + np.asarray(centre, float)
+    tri = pos[f]
+    fn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])  # outward, area-weighted
+    vn = np.zeros_like(pos)
+    for k in range(3):
+        np.add.at(vn, f[:, k], fn)
+    vn /= np.linalg.norm(vn, axis=1, keepdims=True)
+    fr = f[:, [0, 2, 1]]  # reversed winding
+    return pos[fr].astype(np.float32), vn[fr].astype(np.float32)
+
+
+def _quad(p, u, v, normal):
+    """Two triangles of the parallelogram p, p+u, p+v, p+u+v with flat normal
+    `normal`, wound so that (e1 x e2) . normal < 0."""
+    p, u, v, n = (np.asarray(x, float) for x in (p, u, v, normal))
+    a, b, c, d = p, p + u, p + u + v, p + v
+    tris = [np.array([a, b, c]), np.array([a, c, d])]
+    out = []
+    for t in tris:
+        if np.dot(np.cross(t[1] - t[0], t[2] - t[0]), n) > 0:
+            t = t[[0, 2, 1]]
+        out.append(Triangle(t, [n, n, n]))
+    return out
+
+
+def cornell_box_triangles():
+    red, green, white = (0.65, 0.05, 0.05), (0.12, 0.45, 0.15), (0.65, 0.65, 0.65)
+    walls = [
+        ((0, 0, 0), (0, 1, 0), (0, 0, 1), (1, 0, 0), red),      # left, x = 0
+        ((1, 0, 0), (0, 0, 1), (0, 1, 0), (-1, 0, 0), green),   # right, x = 1
+        ((0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), white),    # back, z = 0
+        ((0, 0, 0), (0, 0, 1), (1, 0, 0), (0, 1, 0), white),    # floor, y = 0
+        ((0, 1, 0), (1, 0, 0), (0, 0, 1), (0, -1, 0), white),   # ceiling, y = 1
+    ]
+    objs = []
+    for p, u, v, n, col in walls:
+        mat = LambertianMaterial(col)
+        for t in _quad(p, u, v, n):
+            objs.append(SimpleObject(t, mat))
+    light = LightMaterial((15.0, 15.0, 15.0))
+    for t in _quad((0.375, 0.9999, 0.375), (0.25, 0, 0), (0, 0, 0.25), (0, -1, 0)):
+        objs.append(SimpleObject(t, light))
+    return objs
+
+
+def cornell_mesh(level: int = 8, seed: int = 0, width: int = 1024, height: int = 1024, spp: int = 64,
+                 centre=(0.5, 0.3, 0.5), radius: float = 0.25):
+    """Returns (scene, camera, opts) of the triangle-mesh workload."""
+    verts, norms = displaced_icosphere(level, centre, radius, seed)
+    objs = cornell_box_triangles()
+    objs.append(SimpleObject(BvhMesh.from_arrays(verts, norms), LambertianMaterial((0.7, 0.7, 0.7))))
+    scene = Scene(objects=objs, skybox=NoSkybox())
+    cam = Camera(pos=(0.5, 0.5, 2.3), v_fov=Angle.from_degrees(40.0), fwd=(0.0, 0.0, -1.0), focus_dist=1.0,
+                 defocus_angle=Angle(0.0))
+    opts = RenderOpts(width=width, height=height, samples=spp, ray_depth=8)
+    return scene, cam, opts
+
+
+# ---------------------------------------------------------------------------
+# SDFs and media
+# ---------------------------------------------------------------------------
+def sdf_volumes(seed: int = 0, width: int = 1280, height: int = 720, spp: int = 128, n_spheres: int = 100):
+    """Returns (scene, camera, opts) of the SDF + media workload.
+
+    Placement (not fixed by the workload definition, fixed here): Mandelbulb
+    at (0, 1.2, 0), torus at (2.8, 0.3, 0.8), sphere medium at (-2.6, 1, 0.6)
+    radius 0.9, box medium [-1, 1.5] x [-0.5, 0.6] x [2, 3.2], Lambertian
+    spheres of radius U[0.15, 0.45] scattered over [-6, 6] x [-1.5, 0] x [-6, 6].
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    objs = []
+    for _ in range(n_spheres):
+        r = 0.15 + 0.3 * rng.random()
+        c = (-6 + 12 * rng.random(), -1.5 + 1.5 * rng.random(), -6 + 12 * rng.random())
+        objs.append(SimpleObject(SphereMesh(c, r), LambertianMaterial(tuple(rng.random(3)))))
+    box_density = 0.01 + 0.49 * rng.random()
+    box_albedo = tuple(0.3 + 0.6 * rng.random(3))
+    objs.append(VolumetricObject(SphereMesh((-2.6, 1.0, 0.6), 0.9), IsotropicMaterial((0.8, 0.8, 0.8), 0.0), 0.2))
+    objs.append(VolumetricObject(AxisBoxMesh((-1.0, -0.5, 2.0), (1.5, 0.6, 3.2)), IsotropicMaterial(box_albedo, 0.0),
+                                 box_density))
+    objs.append(SimpleObject(RaymarchedIsosurfaceMesh(SdfMandelbulb((0.0, 1.2, 0.0), 8.0, 8, 1.0), 256, 1e-4),
+                             MetalMaterial((0.8, 0.85, 0.88), 0.1)))
+    objs.append(SimpleObject(RaymarchedIsosurfaceMesh(SdfTorus((2.8, 0.3, 0.8), 1.0, 0.3), 256, 1e-4),
+                             DielectricMaterial((1.0, 1.0, 1.0), 1.5, 0.0)))
+    scene = Scene(objects=objs, skybox=SimpleSkybox())
+    cam = look_at_camera((0.0, 2.2, 8.5), (0.0, 0.9, 0.0), 35.0)
+    opts = RenderOpts(width=width, height=height, samples=spp, ray_depth=16)
+    return scene, cam, opts
+
+
+def single_sphere(albedo, skybox=None):
+    """The scene of rayna_engine/tests/simple_renders.rs:36-48: a Lambertian
+    unit sphere at the origin under WhiteSkybox."""
+    from .scene import WhiteSkybox
+    return Scene(objects=[SimpleObject(SphereMesh((0.0, 0.0, 0.0), 1.0), LambertianMaterial(tuple(albedo)))],
+                 skybox=skybox if skybox is not None else WhiteSkybox())

@@ -1,0 +1,220 @@
+"""Renderer — the GPU stand-in for rayna_engine's `Renderer<Obj, Sky, Rng>`.
+
+Mirrors render/renderer.rs: `new_from(scene, camera, options, num_threads)`,
+`new_default()`, `render() -> Render`, `set_scene/set_camera/set_options`
+(each clears the accumulation), `clear_accumulation()`, `set_thread_count()`
+and the `scene/camera/options` getters. Every call goes through the C ABI of
+include/rayna_gpu.h; there is no CPU path.
+
+Images are numpy arrays of shape (width, height, 3) — the reference's
+`Image` is an ndarray of shape (width, height) of RGB pixels
+(core/image.rs:24-25).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi as A
+from .scene import Camera, RenderOpts, Scene, flatten
+
+
+@dataclass
+class RenderStats:
+    """render/render.rs:4-15 plus device figures."""
+    duration: float = 0.0          # seconds, wall time of render()
+    num_threads: int = 0           # 0: the device renders
+    opts: RenderOpts = field(default_factory=RenderOpts)
+    accum_frames: int = 0
+    kernel_ms: float = 0.0
+    samples: int = 0
+    rays: int = 0
+    node_visits: int = 0
+    prim_tests: int = 0
+    sdf_steps: int = 0
+    error_flags: int = 0
+
+
+@dataclass
+class Render:
+    img: np.ndarray
+    stats: RenderStats
+
+
+def _mix_seed(base: int, frame: int) -> int:
+    """SplitMix64 of (base, frame): the per-frame key of the random streams."""
+    z = (base + 0x9E3779B97F4A7C15 * (frame + 1)) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return z ^ (z >> 31)
+
+
+class Renderer:
+    """GPU renderer with the reference Renderer's methods."""
+
+    def __init__(self, scene: Scene, camera: Camera, options: RenderOpts, *, device: int = 0,
+                 form: str = "megakernel", seed: int = 0, stream: int | None = None, counters: bool = False):
+        self._lib = A.load_library()
+        dopts = A.rg_device_opts()
+        dopts.device = device
+        dopts.stream = stream
+        dopts.form = {"megakernel": A.RG_FORM_MEGAKERNEL, "wavefront": A.RG_FORM_WAVEFRONT}[form]
+        dopts.flags = A.RG_FLAG_COUNTERS if counters else 0
+        h = C.c_void_p()
+        st = self._lib.rg_create(C.byref(dopts), C.byref(h))
+        A.check(self._lib, None, st)
+        self._h = h
+        self.form = form
+        self.seed = int(seed)
+        self._frame = 0
+        self._scene = self._camera = self._options = None
+        self._flat = None
+        self.set_scene(scene)
+        self.set_camera(camera)
+        self.set_options(options)
+
+    # -- construction --------------------------------------------------------
+    @classmethod
+    def new_from(cls, scene: Scene, camera: Camera, options: RenderOpts, num_threads: int = 0, **kw) -> "Renderer":
+        """Renderer::new_from (renderer.rs:86-107). `num_threads` is accepted
+        for signature parity; the device decides its own parallelism."""
+        return cls(scene, camera, options, **kw)
+
+    @classmethod
+    def new_default(cls, **kw) -> "Renderer":
+        return cls(Scene(), Camera(), RenderOpts(), **kw)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.rg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- properties ----------------------------------------------------------
+    @property
+    def scene(self) -> Scene:
+        return self._scene
+
+    @property
+    def camera(self) -> Camera:
+        return self._camera
+
+    @property
+    def options(self) -> RenderOpts:
+        return self._options
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st: int):
+        A.check(self._lib, self._h, st)
+
+    def clear_accumulation(self):
+        self._check(self._lib.rg_clear_accumulation(self._h))
+
+    def set_scene(self, scene: Scene):
+        flat = flatten(scene)
+        self._check(self._lib.rg_set_scene(self._h, C.byref(flat.desc)))
+        self._scene, self._flat = scene, flat
+
+    def set_camera(self, camera: Camera):
+        self._check(self._lib.rg_set_camera(self._h, C.byref(camera.to_c())))
+        self._camera = camera
+
+    def set_options(self, options: RenderOpts):
+        self._check(self._lib.rg_set_options(self._h, C.byref(options.to_c())))
+        self._options = options
+
+    def set_thread_count(self, num_threads: int):
+        """Accepted for API parity (renderer.rs:179-182); the device is not thread-pooled."""
+        return None
+
+    # -- rendering -----------------------------------------------------------
+    def next_seed(self) -> int:
+        s = _mix_seed(self.seed, self._frame)
+        self._frame += 1
+        return s
+
+    def render(self, seed: int | None = None) -> Render:
+        """Renderer::render (renderer.rs:224-264): one progressive frame."""
+        o = self._options
+        img = np.empty((o.width, o.height, 3), dtype=np.float32)
+        stats = A.rg_render_stats()
+        t0 = time.perf_counter()
+        s = self.next_seed() if seed is None else int(seed)
+        st = self._lib.rg_render(self._h, s, img.ctypes.data_as(C.POINTER(C.c_float)), C.byref(stats))
+        dt = time.perf_counter() - t0
+        if st == A.RG_INVALID_CAMERA:
+            # render_failed: the magenta checker of ilog2 dimensions
+            img = np.ascontiguousarray(img.reshape(-1)[: stats.img_width * stats.img_height * 3]
+                                       .reshape(stats.img_width, stats.img_height, 3))
+        else:
+            self._check(st)
+        rs = RenderStats(duration=dt, num_threads=0, opts=o, accum_frames=stats.accum_frames,
+                         kernel_ms=stats.kernel_ms, samples=stats.samples, rays=stats.rays,
+                         node_visits=stats.node_visits, prim_tests=stats.prim_tests,
+                         sdf_steps=stats.sdf_steps, error_flags=stats.error_flags)
+        return Render(img=img, stats=rs)
+
+    def frame_moments(self):
+        """Per-pixel mean and sample variance of the last frame's samples."""
+        o = self._options
+        m = np.empty((o.width, o.height, 3), np.float32)
+        v = np.empty_like(m)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self._check(self._lib.rg_frame_moments(self._h, fp(m), fp(v)))
+        return m, v
+
+    def get_accumulation(self):
+        o = self._options
+        s = np.empty((o.width, o.height, 3), np.float32)
+        n = C.c_uint32()
+        self._check(self._lib.rg_get_accumulation(self._h, s.ctypes.data_as(C.POINTER(C.c_float)), C.byref(n)))
+        return s, n.value
+
+    def set_accumulation(self, sums: np.ndarray, frames: int):
+        s = np.ascontiguousarray(sums, dtype=np.float32)
+        self._check(self._lib.rg_set_accumulation(self._h, s.ctypes.data_as(C.POINTER(C.c_float)), int(frames)))
+
+    def query_rays(self, origins, dirs, tmin=1e-3, tmax=3.4028235e38, volume_u=None) -> np.ndarray:
+        """Closest-hit queries against the current scene; returns a structured
+        array with the fields of rg_hit."""
+        o = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        n = o.shape[0]
+        t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(tmin, np.float32), (n,)))
+        t1 = np.ascontiguousarray(np.broadcast_to(np.asarray(tmax, np.float32), (n,)))
+        out = (A.rg_hit * max(1, n))()
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        vu = None
+        if volume_u is not None:
+            vu_arr = np.ascontiguousarray(volume_u, np.float32)
+            vu = fp(vu_arr)
+        self._check(self._lib.rg_query_rays(self._h, n, fp(o), fp(d), fp(t0), fp(t1), vu, out))
+        return hits_to_numpy(out, n)
+
+
+HIT_DTYPE = np.dtype([("hit", np.uint32), ("prim", np.uint32), ("t", np.float32), ("normal", np.float32, 3),
+                      ("ray_normal", np.float32, 3), ("front_face", np.uint32), ("material", np.uint32),
+                      ("side", np.uint32)])
+assert HIT_DTYPE.itemsize == 48
+
+
+def hits_to_numpy(buf, n: int) -> np.ndarray:
+    raw = np.frombuffer(buf, dtype=HIT_DTYPE, count=n)
+    return raw.copy()

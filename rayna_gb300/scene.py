@@ -1,0 +1,498 @@
+"""Scene, camera and render-option types mirroring rayna_engine's public API.
+
+Names, fields and defaults follow the reference so that code written against
+`rayna_engine` reads the same here:
+
+* meshes        — SphereMesh (mesh/primitive/sphere.rs), Triangle
+                  (mesh/primitive/triangle.rs), BvhMesh (mesh/advanced/bvh.rs),
+                  AxisBoxMesh (mesh/primitive/axis_box.rs),
+                  RaymarchedIsosurfaceMesh (mesh/isosurface/raymarched.rs)
+* objects       — SimpleObject (object/simple.rs), VolumetricObject
+                  (object/volumetric.rs), ObjectList (object/list.rs)
+* materials     — Lambertian/Metal/Dielectric/Isotropic/LightMaterial
+                  (material/*.rs) with SolidTexture albedos (texture/solid.rs)
+* sky           — SimpleSkybox, WhiteSkybox, NoSkybox (skybox/*.rs)
+* Camera, Angle (scene/camera.rs), RenderOpts, RenderMode
+  (render/render_opts.rs), Scene / StandardScene (scene/mod.rs)
+
+`flatten()` turns a scene into the flat arrays of ``rg_scene_desc``. The
+reference takes SDFs as closures; closures cannot cross a C ABI, so an SDF is
+given as one of the descriptor types below. Variants this library does not
+run (non-identity transforms, dynamic meshes) raise UnsupportedVariant.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import math
+from dataclasses import dataclass, field
+from typing import Any, Iterable, Sequence
+
+import numpy as np
+
+from . import _abi as A
+
+
+class UnsupportedVariant(ValueError):
+    """A reference scene variant the GPU path does not run (RG_UNSUPPORTED_VARIANT)."""
+
+
+def _vec3(v) -> tuple:
+    t = tuple(float(x) for x in v)
+    if len(t) != 3:
+        raise ValueError(f"expected 3 components, got {v!r}")
+    return t
+
+
+# ---------------------------------------------------------------------------
+# Camera and options
+# ---------------------------------------------------------------------------
+@dataclass(frozen=True)
+class Angle:
+    """glamour::Angle<f64>: an angle stored in radians."""
+    radians: float
+
+    @staticmethod
+    def from_degrees(deg: float) -> "Angle":
+        return Angle(math.radians(deg))
+
+    @staticmethod
+    def from_radians(rad: float) -> "Angle":
+        return Angle(float(rad))
+
+    @property
+    def degrees(self) -> float:
+        return math.degrees(self.radians)
+
+
+@dataclass
+class Camera:
+    """scene/camera.rs:10-25. Defaults follow Camera::default (:27-37)."""
+    pos: tuple = (0.0, 0.0, 0.0)
+    v_fov: Angle = Angle.from_degrees(45.0)
+    fwd: tuple = (0.0, 0.0, 1.0)
+    focus_dist: float = 1.0
+    defocus_angle: Angle = Angle(0.0)
+
+    def to_c(self) -> A.rg_camera:
+        c = A.rg_camera()
+        c.pos[:] = _vec3(self.pos)
+        c.fwd[:] = _vec3(self.fwd)
+        c.v_fov = self.v_fov.radians
+        c.focus_dist = float(self.focus_dist)
+        c.defocus_angle = self.defocus_angle.radians
+        return c
+
+
+class RenderMode(enum.IntEnum):
+    """render/render_opts.rs:34-52."""
+    PBR = 0
+    RayNormal = 1
+    OutwardNormal = 2
+    Scatter = 3
+    FrontFace = 4
+    Distance = 5
+    Uv = 6
+    Side = 7
+
+
+@dataclass
+class RenderOpts:
+    """render/render_opts.rs:8-29; defaults from :61-72."""
+    width: int = 740
+    height: int = 480
+    samples: int = 1
+    mode: RenderMode = RenderMode.PBR
+    ray_depth: int = 5
+    ray_branching: int = 1
+
+    def dims(self) -> tuple:
+        return (self.width, self.height)
+
+    def aspect_ratio(self) -> float:
+        return self.width / self.height
+
+    def to_c(self) -> A.rg_render_opts:
+        for name in ("width", "height", "samples", "ray_branching"):
+            if int(getattr(self, name)) <= 0:
+                raise ValueError(f"RenderOpts.{name} is a NonZeroUsize; got {getattr(self, name)}")
+        o = A.rg_render_opts()
+        o.width, o.height, o.samples = int(self.width), int(self.height), int(self.samples)
+        o.mode, o.ray_depth, o.ray_branching = int(self.mode), int(self.ray_depth), int(self.ray_branching)
+        return o
+
+
+# ---------------------------------------------------------------------------
+# Textures and materials
+# ---------------------------------------------------------------------------
+@dataclass
+class SolidTexture:
+    """texture/solid.rs: a constant colour."""
+    albedo: tuple = (0.0, 0.0, 0.0)
+
+
+def _colour(tex) -> tuple:
+    if isinstance(tex, SolidTexture):
+        return _vec3(tex.albedo)
+    if isinstance(tex, (tuple, list, np.ndarray)):
+        return _vec3(tex)
+    raise UnsupportedVariant(f"only SolidTexture albedos cross the C ABI, got {type(tex).__name__}")
+
+
+@dataclass(eq=False)
+class LambertianMaterial:
+    albedo: Any = (0.5, 0.5, 0.5)
+
+
+@dataclass(eq=False)
+class MetalMaterial:
+    albedo: Any
+    fuzz: float
+
+
+@dataclass(eq=False)
+class DielectricMaterial:
+    albedo: Any
+    refractive_index: float
+    density: float
+
+
+@dataclass(eq=False)
+class IsotropicMaterial:
+    albedo: Any = (0.5, 0.5, 0.5)
+    density: float = 1.0
+
+
+@dataclass(eq=False)
+class LightMaterial:
+    emissive: Any
+
+
+def material_record(m) -> A.rg_material:
+    r = A.rg_material()
+    if isinstance(m, LambertianMaterial):
+        r.kind = A.RG_MAT_LAMBERTIAN
+        r.albedo[:] = _colour(m.albedo)
+    elif isinstance(m, MetalMaterial):
+        r.kind = A.RG_MAT_METAL
+        r.albedo[:] = _colour(m.albedo)
+        r.fuzz = float(m.fuzz)
+    elif isinstance(m, DielectricMaterial):
+        r.kind = A.RG_MAT_DIELECTRIC
+        r.albedo[:] = _colour(m.albedo)
+        r.refractive_index = float(m.refractive_index)
+        r.density = float(m.density)
+    elif isinstance(m, IsotropicMaterial):
+        r.kind = A.RG_MAT_ISOTROPIC
+        r.albedo[:] = _colour(m.albedo)
+        r.density = float(m.density)
+    elif isinstance(m, LightMaterial):
+        r.kind = A.RG_MAT_LIGHT
+        r.albedo[:] = _colour(m.emissive)
+    else:
+        raise UnsupportedVariant(f"material {type(m).__name__} cannot cross the C ABI")
+    return r
+
+
+# ---------------------------------------------------------------------------
+# Skyboxes
+# ---------------------------------------------------------------------------
+class SimpleSkybox:
+    kind = A.RG_SKY_SIMPLE
+
+
+class WhiteSkybox:
+    kind = A.RG_SKY_WHITE
+
+
+class NoSkybox:
+    kind = A.RG_SKY_NONE
+
+
+# ---------------------------------------------------------------------------
+# Meshes
+# ---------------------------------------------------------------------------
+@dataclass
+class SphereMesh:
+    pos: tuple
+    radius: float
+
+
+@dataclass
+class Triangle:
+    """mesh/primitive/triangle.rs:22-36; the constructor's asserts are kept."""
+    vertices: Sequence
+    normals: Sequence
+
+    def __post_init__(self):
+        v = np.asarray(self.vertices, dtype=np.float64).reshape(3, 3)
+        n = np.asarray(self.normals, dtype=np.float64).reshape(3, 3)
+        if (v[0] == v[1]).all() or (v[1] == v[2]).all() or (v[2] == v[0]).all():
+            raise ValueError("triangles cannot have duplicate vertices")
+        if not np.all(np.abs(np.linalg.norm(n, axis=1) - 1.0) < 2e-4):
+            raise ValueError("normals must be normalised")
+        self.vertices, self.normals = v, n
+
+
+class BvhMesh:
+    """mesh/advanced/bvh.rs: a BVH over triangles sharing one material.
+
+    ``BvhMesh(list_of_triangles)`` mirrors the reference constructor;
+    ``BvhMesh.from_arrays(vertices, normals)`` takes (n, 3, 3) arrays.
+    """
+
+    def __init__(self, meshes: Iterable[Triangle] = ()):
+        tris = list(meshes)
+        for t in tris:
+            if not isinstance(t, Triangle):
+                raise UnsupportedVariant(f"BvhMesh over {type(t).__name__} cannot cross the C ABI")
+        if tris:
+            self.vertices = np.stack([t.vertices for t in tris]).astype(np.float32)
+            self.normals = np.stack([t.normals for t in tris]).astype(np.float32)
+        else:
+            self.vertices = np.zeros((0, 3, 3), np.float32)
+            self.normals = np.zeros((0, 3, 3), np.float32)
+
+    @staticmethod
+    def from_arrays(vertices, normals) -> "BvhMesh":
+        m = BvhMesh()
+        m.vertices = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3, 3)
+        m.normals = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3, 3)
+        if m.vertices.shape != m.normals.shape:
+            raise ValueError("vertices and normals must have the same shape")
+        return m
+
+    def __len__(self):
+        return self.vertices.shape[0]
+
+
+@dataclass
+class AxisBoxMesh:
+    a: tuple
+    b: tuple
+
+    @staticmethod
+    def new_centred(centre, size) -> "AxisBoxMesh":
+        c, s = np.asarray(centre, float), np.asarray(size, float)
+        return AxisBoxMesh(tuple(c + s / 2), tuple(c - s / 2))
+
+
+@dataclass
+class SdfSphere:
+    centre: tuple
+    radius: float
+
+
+@dataclass
+class SdfTorus:
+    """Torus around the +y axis: length((length(p.xz) - major, p.y)) - minor."""
+    centre: tuple
+    major: float
+    minor: float
+
+
+@dataclass
+class SdfMandelbulb:
+    """Power-n Mandelbulb distance estimator, scaled by `scale` world units."""
+    centre: tuple
+    power: float = 8.0
+    iterations: int = 8
+    scale: float = 1.0
+
+
+@dataclass
+class RaymarchedIsosurfaceMesh:
+    """mesh/isosurface/raymarched.rs; defaults from :36-37."""
+    sdf: Any
+    max_iterations: int = 150
+    epsilon: float = 1e-7
+
+    DEFAULT_EPSILON = 1e-7
+    DEFAULT_ITERATIONS = 150
+
+
+# ---------------------------------------------------------------------------
+# Objects and scene
+# ---------------------------------------------------------------------------
+@dataclass(eq=False)
+class SimpleObject:
+    mesh: Any
+    material: Any
+    transform: Any = None
+
+
+@dataclass(eq=False)
+class VolumetricObject:
+    mesh: Any
+    material: Any
+    density: float
+    transform: Any = None
+
+
+class ObjectList(list):
+    """object/list.rs: a list of objects (BVH over bounded ones + unbounded list)."""
+
+
+@dataclass
+class Scene:
+    """scene/mod.rs:11-24 (StandardScene)."""
+    objects: Any = field(default_factory=ObjectList)
+    skybox: Any = field(default_factory=SimpleSkybox)
+
+
+StandardScene = Scene
+
+
+# ---------------------------------------------------------------------------
+# Flattening
+# ---------------------------------------------------------------------------
+def _identity(t) -> bool:
+    if t is None:
+        return True
+    a = np.asarray(t, dtype=float)
+    return a.shape == (4, 4) and np.array_equal(a, np.eye(4))
+
+
+class FlatScene:
+    """Flat host arrays of one scene plus the rg_scene_desc pointing at them."""
+
+    def __init__(self):
+        self.materials: list = []
+        self._mat_index: dict = {}
+        self.spheres, self.sphere_mat = [], []
+        self.tri_v, self.tri_n, self.tri_mat, self.tri_mesh = [], [], [], []
+        self.boxes, self.box_mat = [], []
+        self.volumes: list = []
+        self.sdfs: list = []
+        self.skybox = A.RG_SKY_SIMPLE
+        self.n_meshes = 0
+
+    def material(self, m) -> int:
+        k = id(m)
+        if k not in self._mat_index:
+            self._mat_index[k] = (len(self.materials), m)
+            self.materials.append(material_record(m))
+        return self._mat_index[k][0]
+
+    def add(self, obj):
+        if isinstance(obj, (list, tuple, ObjectList)):
+            for o in obj:
+                self.add(o)
+            return
+        if isinstance(obj, SimpleObject):
+            if not _identity(obj.transform):
+                raise UnsupportedVariant("non-identity ObjectTransform is not supported by the GPU path")
+            mesh, mat = obj.mesh, self.material(obj.material)
+            if isinstance(mesh, SphereMesh):
+                self.spheres.append((*_vec3(mesh.pos), float(mesh.radius)))
+                self.sphere_mat.append(mat)
+            elif isinstance(mesh, Triangle):
+                self.tri_v.append(np.asarray(mesh.vertices, np.float32).reshape(1, 3, 3))
+                self.tri_n.append(np.asarray(mesh.normals, np.float32).reshape(1, 3, 3))
+                self.tri_mat.append(np.full(1, mat, np.uint32))
+                self.tri_mesh.append(np.full(1, -1, np.int32))
+            elif isinstance(mesh, BvhMesh):
+                n = len(mesh)
+                if n:
+                    self.tri_v.append(mesh.vertices)
+                    self.tri_n.append(mesh.normals)
+                    self.tri_mat.append(np.full(n, mat, np.uint32))
+                    self.tri_mesh.append(np.full(n, self.n_meshes, np.int32))
+                    self.n_meshes += 1
+            elif isinstance(mesh, AxisBoxMesh):
+                self.boxes.append((*_vec3(mesh.a), *_vec3(mesh.b)))
+                self.box_mat.append(mat)
+            elif isinstance(mesh, RaymarchedIsosurfaceMesh):
+                self.sdfs.append(self._sdf(mesh, mat))
+            else:
+                raise UnsupportedVariant(f"mesh {type(mesh).__name__} cannot cross the C ABI")
+        elif isinstance(obj, VolumetricObject):
+            if not _identity(obj.transform):
+                raise UnsupportedVariant("non-identity ObjectTransform is not supported by the GPU path")
+            v = A.rg_volume()
+            if isinstance(obj.mesh, SphereMesh):
+                v.boundary = A.RG_BOUNDARY_SPHERE
+                v.a[:] = _vec3(obj.mesh.pos)
+                v.b[:] = (float(obj.mesh.radius), 0.0, 0.0)
+            elif isinstance(obj.mesh, AxisBoxMesh):
+                v.boundary = A.RG_BOUNDARY_BOX
+                v.a[:] = _vec3(obj.mesh.a)
+                v.b[:] = _vec3(obj.mesh.b)
+            else:
+                raise UnsupportedVariant(f"volume boundary {type(obj.mesh).__name__} is not supported")
+            v.density = float(obj.density)
+            v.material = self.material(obj.material)
+            self.volumes.append(v)
+        else:
+            raise UnsupportedVariant(f"object {type(obj).__name__} cannot cross the C ABI")
+
+    @staticmethod
+    def _sdf(mesh: RaymarchedIsosurfaceMesh, mat: int) -> A.rg_sdf:
+        s = A.rg_sdf()
+        f = mesh.sdf
+        if isinstance(f, SdfSphere):
+            s.kind, s.centre[:], s.params[:] = A.RG_SDF_SPHERE, _vec3(f.centre), (float(f.radius), 0, 0, 0)
+        elif isinstance(f, SdfTorus):
+            s.kind, s.centre[:], s.params[:] = A.RG_SDF_TORUS, _vec3(f.centre), (float(f.major), float(f.minor), 0, 0)
+        elif isinstance(f, SdfMandelbulb):
+            s.kind, s.centre[:] = A.RG_SDF_MANDELBULB, _vec3(f.centre)
+            s.params[:] = (float(f.power), float(f.iterations), float(f.scale), 0.0)
+        else:
+            raise UnsupportedVariant("SDF closures cannot cross the C ABI; use SdfSphere/SdfTorus/SdfMandelbulb")
+        s.max_iterations = int(mesh.max_iterations)
+        s.epsilon = float(mesh.epsilon)
+        s.material = mat
+        return s
+
+    def finish(self) -> "FlatScene":
+        f32, u32 = np.float32, np.uint32
+        self.a_spheres = np.ascontiguousarray(np.asarray(self.spheres, f32).reshape(-1, 4))
+        self.a_sphere_mat = np.ascontiguousarray(np.asarray(self.sphere_mat, u32))
+        if self.tri_v:
+            self.a_tri_v = np.ascontiguousarray(np.concatenate(self.tri_v).astype(f32))
+            self.a_tri_n = np.ascontiguousarray(np.concatenate(self.tri_n).astype(f32))
+            self.a_tri_mat = np.ascontiguousarray(np.concatenate(self.tri_mat))
+            self.a_tri_mesh = np.ascontiguousarray(np.concatenate(self.tri_mesh))
+        else:
+            self.a_tri_v = np.zeros((0, 3, 3), f32)
+            self.a_tri_n = np.zeros((0, 3, 3), f32)
+            self.a_tri_mat = np.zeros(0, u32)
+            self.a_tri_mesh = np.zeros(0, np.int32)
+        self.a_boxes = np.ascontiguousarray(np.asarray(self.boxes, f32).reshape(-1, 6))
+        self.a_box_mat = np.ascontiguousarray(np.asarray(self.box_mat, u32))
+        self.c_volumes = (A.rg_volume * max(1, len(self.volumes)))(*self.volumes)
+        self.c_sdfs = (A.rg_sdf * max(1, len(self.sdfs)))(*self.sdfs)
+        self.c_materials = (A.rg_material * max(1, len(self.materials)))(*self.materials)
+        d = A.rg_scene_desc()
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        up = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint32))
+        d.n_spheres, d.spheres, d.sphere_material = len(self.a_spheres), fp(self.a_spheres), up(self.a_sphere_mat)
+        d.n_triangles = self.a_tri_v.shape[0]
+        d.tri_vertices, d.tri_normals = fp(self.a_tri_v), fp(self.a_tri_n)
+        d.tri_material = up(self.a_tri_mat)
+        d.tri_mesh = self.a_tri_mesh.ctypes.data_as(C.POINTER(C.c_int32))
+        d.n_boxes, d.boxes, d.box_material = len(self.a_boxes), fp(self.a_boxes), up(self.a_box_mat)
+        d.n_volumes, d.volumes = len(self.volumes), self.c_volumes
+        d.n_sdfs, d.sdfs = len(self.sdfs), self.c_sdfs
+        d.n_materials, d.materials = len(self.materials), self.c_materials
+        d.skybox = self.skybox
+        self.desc = d
+        return self
+
+    @property
+    def n_prims(self) -> int:
+        return self.desc.n_spheres + self.desc.n_triangles + self.desc.n_boxes + self.desc.n_volumes + self.desc.n_sdfs
+
+
+def flatten(scene: Scene) -> FlatScene:
+    """Flattens a Scene into rg_scene_desc arrays (object order: spheres,
+    standalone triangles, meshes, boxes, volumes, SDFs)."""
+    fs = FlatScene()
+    sky = scene.skybox
+    if sky is None:
+        sky = NoSkybox()  # `None.into()` is NoSkybox (skybox/mod.rs:39-43)
+    if not hasattr(sky, "kind"):
+        raise UnsupportedVariant(f"skybox {type(sky).__name__} cannot cross the C ABI")
+    fs.skybox = sky.kind
+    fs.add(scene.objects)
+    return fs.finish()

@@ -1,0 +1,75 @@
+"""Seeded ray-query suites and small scenes for the parity tests."""
+import numpy as np
+
+from rayna_gb300 import presets
+from rayna_gb300.scene import (
+    AxisBoxMesh, BvhMesh, DielectricMaterial, IsotropicMaterial, LambertianMaterial, MetalMaterial,
+    RaymarchedIsosurfaceMesh, Scene, SdfMandelbulb, SdfSphere, SdfTorus, SimpleObject, SimpleSkybox, SphereMesh,
+    VolumetricObject,
+)
+
+
+def rays_at(rng, n, lo, hi, targets=None, inside_frac=0.1, miss_frac=0.2):
+    """Origins on a shell around the box [lo, hi] (some inside it), directions
+    aimed at random targets (primitive points when given) or random."""
+    lo, hi = np.asarray(lo, float), np.asarray(hi, float)
+    c, ext = (lo + hi) / 2, np.linalg.norm(hi - lo) / 2 + 1e-3
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o = c + d * ext * (1.2 + 1.5 * rng.random((n, 1)))
+    k_in = int(n * inside_frac)
+    o[:k_in] = lo + (hi - lo) * rng.random((k_in, 3))
+    if targets is not None and len(targets):
+        tgt = targets[rng.integers(0, len(targets), n)]
+    else:
+        tgt = lo + (hi - lo) * rng.random((n, 3))
+    dirs = tgt - o
+    k_miss = int(n * miss_frac)
+    rnd = rng.normal(size=(k_miss, 3))
+    dirs[-k_miss:] = rnd
+    # a stratum of near-grazing directions: perturb aimed directions slightly
+    k_g = n // 10
+    dirs[k_in:k_in + k_g] += rng.normal(scale=0.02, size=(k_g, 3)) * np.linalg.norm(dirs[k_in:k_in + k_g], axis=1, keepdims=True)
+    return o.astype(np.float32), dirs.astype(np.float32)
+
+
+def sphere_scene(seed=0):
+    scene, _, _ = presets.random_spheres(seed=seed)
+    return scene
+
+
+def triangle_scene(level=4, seed=0):
+    verts, norms = presets.displaced_icosphere(level, (0.5, 0.3, 0.5), 0.25, seed)
+    objs = presets.cornell_box_triangles()
+    objs.append(SimpleObject(BvhMesh.from_arrays(verts, norms), LambertianMaterial((0.7, 0.7, 0.7))))
+    return Scene(objects=objs), verts
+
+
+def box_scene(seed=0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    objs = []
+    for _ in range(40):
+        c = rng.uniform(-3, 3, 3)
+        s = rng.uniform(0.1, 1.0, 3)
+        objs.append(SimpleObject(AxisBoxMesh(tuple(c - s / 2), tuple(c + s / 2)), LambertianMaterial(tuple(rng.random(3)))))
+    return Scene(objects=objs)
+
+
+def volume_scene():
+    objs = [
+        VolumetricObject(SphereMesh((0.0, 0.0, 0.0), 1.0), IsotropicMaterial((0.8, 0.8, 0.8), 0.0), 0.7),
+        VolumetricObject(AxisBoxMesh((1.5, -0.5, -0.5), (2.5, 0.5, 0.5)), IsotropicMaterial((0.5, 0.6, 0.7), 0.0), 1.5),
+        SimpleObject(SphereMesh((0.3, 0.0, 0.0), 0.3), LambertianMaterial((0.5, 0.5, 0.5))),
+        SimpleObject(SphereMesh((-3.0, 0.0, 0.0), 0.5), LambertianMaterial((0.5, 0.5, 0.5))),
+    ]
+    return Scene(objects=objs)
+
+
+def sdf_scene():
+    objs = [
+        SimpleObject(RaymarchedIsosurfaceMesh(SdfTorus((0.0, 0.0, 0.0), 1.0, 0.3), 256, 1e-4), DielectricMaterial((1, 1, 1), 1.5, 0)),
+        SimpleObject(RaymarchedIsosurfaceMesh(SdfSphere((2.5, 0.0, 0.0), 0.5), 256, 1e-4), LambertianMaterial((0.5, 0.5, 0.5))),
+        SimpleObject(RaymarchedIsosurfaceMesh(SdfMandelbulb((-2.5, 0.0, 0.0), 8.0, 8, 1.0), 256, 1e-4), MetalMaterial((0.8, 0.8, 0.8), 0.1)),
+        SimpleObject(SphereMesh((0.0, 1.5, 0.0), 0.4), LambertianMaterial((0.5, 0.5, 0.5))),
+    ]
+    return Scene(objects=objs, skybox=SimpleSkybox())

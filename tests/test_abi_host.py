@@ -1,0 +1,151 @@
+"""C-ABI and host-logic tests that need no GPU.
+
+The library must load, export every entry point include/rayna_gpu.h declares,
+report RG_NO_DEVICE cleanly when no GPU is visible, and validate/build scenes
+on the host (rg_inspect_scene) exactly as rg_set_scene would.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from rayna_gb300 import _abi as A
+from rayna_gb300 import presets
+from rayna_gb300.scene import (
+    AxisBoxMesh, BvhMesh, DielectricMaterial, LambertianMaterial, RaymarchedIsosurfaceMesh, Scene, SdfTorus,
+    SimpleObject, SphereMesh, Triangle, UnsupportedVariant, VolumetricObject, IsotropicMaterial, flatten,
+)
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "rayna_gpu.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rg_[a-z_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = A.load_library()
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) == set(A.SIGNATURES), "ctypes signatures must cover the header exactly"
+    assert lib.rg_abi_version() == 1
+
+
+def test_struct_sizes_match_header_layout():
+    assert C.sizeof(A.rg_material) == 32
+    assert C.sizeof(A.rg_hit) == 48
+    assert C.sizeof(A.rg_camera) == 9 * 8
+    assert C.sizeof(A.rg_render_opts) == 24
+
+
+def test_create_without_device_reports_no_device(gpu_available):
+    if gpu_available:
+        pytest.skip("a GPU is visible")
+    lib = A.load_library()
+    h = C.c_void_p()
+    st = lib.rg_create(None, C.byref(h))
+    assert st == A.RG_NO_DEVICE
+    assert "no CUDA device" in A.last_error(lib, None)
+
+
+def inspect(scene):
+    lib = A.load_library()
+    flat = flatten(scene)
+    info = A.rg_scene_info()
+    st = lib.rg_inspect_scene(C.byref(flat.desc), C.byref(info))
+    return st, info, A.last_error(lib, None)
+
+
+def test_inspect_random_spheres_bvh():
+    scene, _, _ = presets.random_spheres(seed=0)
+    st, info, _ = inspect(scene)
+    assert st == A.RG_OK
+    assert info.n_prims == 488
+    assert info.max_leaf_size <= 4
+    assert info.n_leaves >= 488 // 4
+    assert info.max_depth < 60
+    assert info.n_nodes == info.n_leaves - 1 or info.n_nodes >= info.n_leaves // 2
+
+
+def test_inspect_mesh_bvh_depth_and_size():
+    scene, _, _ = presets.cornell_mesh(level=5)
+    st, info, _ = inspect(scene)
+    assert st == A.RG_OK
+    assert info.n_prims == 20 * 4 ** 5 + 12
+    assert info.max_leaf_size <= 4
+    assert info.max_depth < 60
+    assert info.sah_cost > 0
+    assert info.device_bytes >= info.n_prims * 48 + info.n_nodes * 64
+
+
+@pytest.mark.parametrize("bad,status", [
+    (Scene(objects=[SimpleObject(SphereMesh((float("nan"), 0, 0), 1.0), LambertianMaterial())]), A.RG_INVALID_ARG),
+    (Scene(objects=[VolumetricObject(SphereMesh((0, 0, 0), 1.0), IsotropicMaterial(), -1.0)]), A.RG_INVALID_ARG),
+    (Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), DielectricMaterial((1, 1, 1), float("inf"), 0.0))]),
+     A.RG_INVALID_ARG),
+])
+def test_inspect_rejects_invalid_descriptors(bad, status):
+    st, _, msg = inspect(bad)
+    assert st == status
+    assert msg
+
+
+def test_inspect_rejects_bad_material_index_and_null_arrays():
+    lib = A.load_library()
+    flat = flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial())]))
+    flat.a_sphere_mat[0] = 7
+    info = A.rg_scene_info()
+    assert lib.rg_inspect_scene(C.byref(flat.desc), C.byref(info)) == A.RG_INVALID_ARG
+    d = A.rg_scene_desc()
+    d.n_spheres = 3
+    assert lib.rg_inspect_scene(C.byref(d), C.byref(info)) == A.RG_INVALID_ARG
+    assert "NULL" in A.last_error(lib, None)
+
+
+def test_triangle_constructor_asserts():
+    with pytest.raises(ValueError):
+        Triangle([[0, 0, 0], [0, 0, 0], [1, 0, 0]], [[0, 0, 1]] * 3)
+    with pytest.raises(ValueError):
+        Triangle([[0, 0, 0], [0, 1, 0], [1, 0, 0]], [[0, 0, 2]] * 3)
+
+
+def test_flatten_order_and_unsupported_variants():
+    objs = [
+        SimpleObject(RaymarchedIsosurfaceMesh(SdfTorus((0, 0, 0), 1.0, 0.3)), LambertianMaterial()),
+        SimpleObject(AxisBoxMesh((0, 0, 0), (1, 1, 1)), LambertianMaterial()),
+        SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial()),
+    ]
+    flat = flatten(Scene(objects=objs))
+    assert (flat.desc.n_spheres, flat.desc.n_boxes, flat.desc.n_sdfs) == (1, 1, 1)
+    assert flat.desc.n_materials == 3
+    with pytest.raises(UnsupportedVariant):
+        flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial(), transform=np.eye(4) * 2)]))
+    with pytest.raises(UnsupportedVariant):
+        flatten(Scene(objects=[SimpleObject(RaymarchedIsosurfaceMesh(lambda p: 0.0), LambertianMaterial())]))
+
+
+def test_presets_shapes_and_winding():
+    scene, cam, opts = presets.random_spheres(seed=0)
+    flat = flatten(scene)
+    assert flat.desc.n_spheres == 488
+    assert (opts.width, opts.height, opts.samples, opts.ray_depth) == (400, 225, 32, 50)
+    v, f = presets.icosphere(3)
+    assert f.shape[0] == 20 * 4 ** 3 and v.shape[0] == 10 * 4 ** 3 + 2
+    verts, norms = presets.displaced_icosphere(3, (0.5, 0.3, 0.5), 0.25, seed=0)
+    e1 = verts[:, 1] - verts[:, 0]
+    e2 = verts[:, 2] - verts[:, 0]
+    g = np.cross(e1, e2)
+    # reference convention: e1 x e2 points away from the side the normals face
+    assert np.all(np.einsum("ij,ij->i", g, norms.mean(axis=1)) < 0)
+    np.testing.assert_allclose(np.linalg.norm(norms, axis=2), 1.0, atol=1e-5)
+    v2, n2 = presets.displaced_icosphere(3, (0.5, 0.3, 0.5), 0.25, seed=0)
+    assert np.array_equal(verts, v2)
+    for t in presets.cornell_box_triangles():
+        tv = t.mesh.vertices
+        assert np.dot(np.cross(tv[1] - tv[0], tv[2] - tv[0]), t.mesh.normals[0]) < 0

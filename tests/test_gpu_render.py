@@ -1,0 +1,162 @@
+"""Image parity and Renderer semantics on the GPU, through the C ABI.
+
+* The reference's known answers (simple_renders.rs:22-142) on the device.
+* Path-by-path parity: with the same frame seed, the device and the f32
+  oracle that mirrors its samplers trace the same paths; per-pixel means agree
+  to float rounding except where a transcendental's last ulp flips a discrete
+  decision (counted).
+* Statistical parity with the faithful f64 oracle (the reference's rejection
+  samplers): per-pixel means within 3 standard errors, relRMSE reported.
+* Accumulation, checkpoint/resume, invalid camera, unsupported variants.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import binding as ob
+from rayna_gb300 import RaynaError, Renderer, presets
+from rayna_gb300.scene import Angle, Camera, RenderMode, RenderOpts, flatten
+
+from test_oracle_pins import SIMPLE_OPTS, check_known_answers, seeded_colours
+
+pytestmark = pytest.mark.gpu
+
+
+def test_simple_renders_known_answers_gpu():
+    for k, colour in enumerate(seeded_colours(4, seed=99)):
+        scene = presets.single_sphere(colour)
+        with Renderer.new_from(scene, Camera(), SIMPLE_OPTS, 4, seed=k) as r:
+            def render(cam):
+                r.set_camera(cam)
+                return r.render().img
+            check_known_answers(render, colour)
+
+
+def small(scene_fn, w, h, spp, depth, **kw):
+    scene, cam, opts = scene_fn(**kw)
+    return scene, cam, RenderOpts(width=w, height=h, samples=spp, ray_depth=depth)
+
+
+CASES = {
+    "random_spheres": lambda: small(presets.random_spheres, 80, 45, 32, 50),
+    "cornell_mesh": lambda: small(presets.cornell_mesh, 48, 48, 16, 8, level=4),
+    "sdf_volumes": lambda: small(presets.sdf_volumes, 64, 36, 16, 16, n_spheres=30),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_path_by_path_parity_with_f32_oracle(case):
+    scene, cam, opts = CASES[case]()
+    flat = flatten(scene)
+    seed = 0x1234567 + len(case)
+    with Renderer.new_from(scene, cam, opts, 0) as r:
+        r.render(seed=seed)
+        gm, gv = r.frame_moments()
+    st, om, ov, _ = ob.render(flat, cam, opts, seed=seed, frames=1, policy=ob.POLICY_GPU_F32)
+    assert st == 0
+    diff = np.abs(gm - om)
+    close = np.all(diff <= 1e-4 * (1 + np.abs(om)), axis=2)
+    frac = close.mean()
+    print(f"{case}: {frac:.4f} of pixels match the f32 oracle path for path")
+    assert frac >= {"random_spheres": 0.97, "cornell_mesh": 0.97, "sdf_volumes": 0.9}[case]
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_statistical_parity_with_f64_oracle(case):
+    scene, cam, opts = CASES[case]()
+    flat = flatten(scene)
+    frames = {"random_spheres": 24, "cornell_mesh": 48, "sdf_volumes": 32}[case]
+    with Renderer.new_from(scene, cam, opts, 0, seed=7) as r:
+        for _ in range(frames):
+            out = r.render()
+        img = out.img.astype(np.float64)
+        assert out.stats.accum_frames == frames
+        assert out.stats.error_flags == 0
+    st, om, ov, _ = ob.render(flat, cam, opts, seed=11, frames=frames, policy=ob.POLICY_REF_F64)
+    assert st == 0
+    n = frames * opts.samples
+    se = np.sqrt(2 * ov / n)           # both sides estimate the same per-sample variance
+    z = (img - om) / np.maximum(se, 1e-6)
+    beyond = np.mean(np.abs(z) > 3)
+    rel_rmse = np.sqrt(np.mean((img - om) ** 2)) / max(np.sqrt(np.mean(om ** 2)), 1e-12)
+    print(f"{case}: {beyond:.4f} of pixel channels beyond 3 SE, relRMSE {rel_rmse:.4f}, mean z {np.mean(z):+.4f}")
+    assert beyond <= 0.01
+    # the image means agree within 4 standard errors of the mean over pixels
+    gm_img, om_img = img.mean(), om.mean()
+    se_img = math.sqrt(np.mean(2 * ov / n) / img.size) * 3  # pixels are correlated: allow 3x
+    assert abs(gm_img - om_img) <= 4 * se_img + 1e-6, (gm_img, om_img, se_img)
+
+
+def test_accumulation_is_the_running_mean():
+    scene, cam, _ = presets.random_spheres(seed=0)
+    opts = RenderOpts(width=32, height=18, samples=4, ray_depth=8)
+    with Renderer.new_from(scene, cam, opts, 0, seed=3) as r:
+        means = []
+        for _ in range(5):
+            out = r.render()
+            m, _ = r.frame_moments()
+            means.append(m.astype(np.float64))
+        np.testing.assert_allclose(out.img, np.mean(means, axis=0), rtol=2e-6, atol=1e-7)
+        sums, frames = r.get_accumulation()
+        assert frames == 5
+        # checkpoint / resume
+        r.clear_accumulation()
+        r.set_accumulation(sums, frames)
+        out2 = r.render(seed=12345)
+        m6, _ = r.frame_moments()
+        np.testing.assert_allclose(out2.img, (np.sum(means, axis=0) + m6) / 6, rtol=2e-6, atol=1e-7)
+        # set_camera clears the accumulation (renderer.rs:158-161)
+        r.set_camera(cam)
+        out3 = r.render(seed=777)
+        m7, _ = r.frame_moments()
+        assert out3.stats.accum_frames == 1
+        np.testing.assert_array_equal(out3.img, m7)
+
+
+def test_same_seed_is_deterministic():
+    scene, cam, _ = presets.sdf_volumes(n_spheres=10)
+    opts = RenderOpts(width=32, height=18, samples=8, ray_depth=8)
+    with Renderer.new_from(scene, cam, opts, 0) as r:
+        a = r.render(seed=42).img
+        r.clear_accumulation()
+        b = r.render(seed=42).img
+    np.testing.assert_array_equal(a, b)
+
+
+def test_invalid_camera_returns_checker():
+    scene = presets.single_sphere((0.5, 0.5, 0.5))
+    opts = RenderOpts(width=64, height=32, samples=1)
+    with Renderer.new_from(scene, Camera(v_fov=Angle(0.0)), opts, 0) as r:
+        out = r.render()
+    assert out.img.shape == (6, 5, 3)   # ilog2(64) x ilog2(32)
+    for x in range(6):
+        for y in range(5):
+            exp = [0, 0, 0] if (x + y) % 2 == 0 else [1, 0, 1]
+            np.testing.assert_array_equal(out.img[x, y], exp)
+
+
+def test_unsupported_mode_and_zero_sizes_are_rejected():
+    scene = presets.single_sphere((0.5, 0.5, 0.5))
+    with Renderer.new_from(scene, Camera(), RenderOpts(width=8, height=8), 0) as r:
+        with pytest.raises(RaynaError) as e:
+            r.set_options(RenderOpts(width=8, height=8, mode=RenderMode.Uv))
+        assert e.value.status == 2
+        with pytest.raises(ValueError):
+            r.set_options(RenderOpts(width=0, height=8))
+
+
+def test_large_spp_path_and_counters():
+    """spp > 256 takes the per-thread sample loop; counters are filled."""
+    scene = presets.single_sphere((0.3, 0.6, 0.9))
+    cam = Camera(pos=(0, 0, -2.7), v_fov=Angle.from_degrees(45), fwd=(0, 0, 1), focus_dist=1.0)
+    opts = RenderOpts(width=8, height=8, samples=300, ray_depth=5)
+    flat = flatten(scene)
+    with Renderer.new_from(scene, cam, opts, 0, counters=True) as r:
+        out = r.render(seed=9)
+        gm, _ = r.frame_moments()
+        assert out.stats.samples == 8 * 8 * 300
+        assert out.stats.rays >= out.stats.samples
+        assert out.stats.node_visits > 0 and out.stats.prim_tests > 0
+    st, om, _, _ = ob.render(flat, cam, opts, seed=9, frames=1, policy=ob.POLICY_GPU_F32)
+    np.testing.assert_allclose(gm, om, rtol=1e-4, atol=1e-5)
