@@ -255,6 +255,17 @@ rg_status rg_inspect_scene(const rg_scene_desc* scene, rg_scene_info* out);
  * builds the BVH and clears the accumulation buffer. */
 rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene);
 
+/* Launch-shape knobs of the kernel forms (no reference counterpart: the
+ * reference has no device; these are what the autotuner sets). Zero fields
+ * select the library defaults. Changing them does not change the image. */
+typedef struct rg_tuning {
+    uint32_t wave_paths;    /* wavefront: path slots per wave (whole pixels per wave) */
+    uint32_t reserved[7];   /* must be 0 */
+} rg_tuning;
+
+rg_status rg_set_tuning(rg_handle h, const rg_tuning* t);
+rg_status rg_get_tuning(rg_handle h, rg_tuning* out);
+
 /* Renderer::set_camera (renderer.rs:158-161): also clears accumulation. An
  * invalid camera is accepted here, as in the reference; render reports it. */
 rg_status rg_set_camera(rg_handle h, const rg_camera* camera);

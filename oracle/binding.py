@@ -55,8 +55,16 @@ def viewport(camera):
     return st, np.array(out).reshape(6, 3)
 
 
+STRUCT_NO_PRETEST = 0
+STRUCT_REFERENCE = 1
+STRUCT_BRUTE_FORCE = 2
+
+
 def query(flat, origins, dirs, tmin=1e-3, tmax=3.4028235e38, volume_u=None, policy=POLICY_GPU_F32, pretest=True):
-    """Closest hits from the oracle. Returns (hits structured array, t64, n64)."""
+    """Closest hits from the oracle. Returns (hits structured array, t64, n64).
+
+    `pretest`: True = the reference's BVH with its per-object box test,
+    False = the same BVH without it, "brute" = no bounding volumes."""
     o = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
     d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
     n = o.shape[0]
@@ -70,7 +78,8 @@ def query(flat, origins, dirs, tmin=1e-3, tmax=3.4028235e38, volume_u=None, poli
     if volume_u is not None:
         vu_arr = np.ascontiguousarray(volume_u, np.float32)
         vu = fp(vu_arr)
-    st = lib().orc_query(C.byref(flat.desc), policy, 1 if pretest else 0, n, fp(o), fp(d), fp(t0), fp(t1), vu, out,
+    structure = STRUCT_BRUTE_FORCE if pretest == "brute" else (STRUCT_REFERENCE if pretest else STRUCT_NO_PRETEST)
+    st = lib().orc_query(C.byref(flat.desc), policy, structure, n, fp(o), fp(d), fp(t0), fp(t1), vu, out,
                          t64.ctypes.data_as(C.POINTER(C.c_double)), n64.ctypes.data_as(C.POINTER(C.c_double)))
     assert st == 0
     hits = np.frombuffer(out, dtype=HIT_DTYPE, count=n).copy()

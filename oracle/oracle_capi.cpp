@@ -31,7 +31,8 @@ int query_impl(const rg_scene_desc* d, int pretest, uint32_t n, const float* o, 
   using T = typename P::T;
   Scene<P> sc;
   Options opt;
-  opt.prim_pretest = pretest != 0;
+  opt.prim_pretest = pretest == 1;
+  opt.brute_force = pretest == 2;
   sc.load(*d, opt);
   for (uint32_t i = 0; i < n; ++i) {
     Ray<P> r = Ray<P>::make({(T)o[3 * i], (T)o[3 * i + 1], (T)o[3 * i + 2]}, {(T)dir[3 * i], (T)dir[3 * i + 1], (T)dir[3 * i + 2]});
@@ -113,8 +114,9 @@ int orc_viewport(const rg_camera* cam, double* out) {
   return RG_OK;
 }
 
-// Closest-hit queries. policy 0 = RefF64, 1 = GpuF32. `pretest` follows the
-// reference's per-object Aabb test before each leaf object.
+// Closest-hit queries. policy 0 = RefF64, 1 = GpuF32. `structure` 1 follows
+// the reference's BVH with its per-object Aabb test before each leaf object,
+// 0 the same BVH without that test, 2 no bounding volumes at all.
 int orc_query(const rg_scene_desc* d, int policy, int pretest, uint32_t n, const float* o, const float* dir,
               const float* tmin, const float* tmax, const float* vol_u, rg_hit* out, double* t64, double* n64) {
   if (policy == 0) return query_impl<RefF64>(d, pretest, n, o, dir, tmin, tmax, vol_u, out, t64, n64);

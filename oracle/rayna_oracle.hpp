@@ -205,21 +205,17 @@ template <class T> struct Aabb {
   }
 };
 
-// Aabb::hit (aabb.rs:117-153). The device computes each slab distance as
-// fma(bound, inv, -(pos*inv)); the reference as (bound - pos) * inv.
+// Aabb::hit (aabb.rs:117-153). The GpuF32 policy follows the device, which
+// widens the exit side by 2^-20 relative so that roundoff never rejects a box
+// the ray meets (Ize, "Robust BVH Ray Traversal", JCGT 2013); the RefF64
+// policy is the reference's exact test.
 template <class P> inline bool aabb_hit(const Aabb<typename P::T>& b, const Ray<P>& r, const Interval<typename P::T>& iv) {
   using T = typename P::T;
   T t1[3], t2[3];
   for (int a = 0; a < 3; ++a) {
     T lo = comp(b.mn, a), hi = comp(b.mx, a), o = comp(r.pos, a), inv = comp(r.inv, a);
-    if constexpr (P::gpu) {
-      T oi = o * inv;
-      t1[a] = std::fma(lo, inv, -oi);
-      t2[a] = std::fma(hi, inv, -oi);
-    } else {
-      t1[a] = (lo - o) * inv;
-      t2[a] = (hi - o) * inv;
-    }
+    t1[a] = (lo - o) * inv;
+    t2[a] = (hi - o) * inv;
   }
   T tmin = std::fmin(t1[0], t2[0]);
   T tmax = std::fmax(t1[0], t2[0]);
@@ -227,7 +223,13 @@ template <class P> inline bool aabb_hit(const Aabb<typename P::T>& b, const Ray<
   tmax = std::fmin(tmax, std::fmax(t1[1], t2[1]));
   tmin = std::fmax(tmin, std::fmin(t1[2], t2[2]));
   tmax = std::fmin(tmax, std::fmax(t1[2], t2[2]));
-  return iv.range_overlaps(tmin, tmax);
+  if constexpr (P::gpu) {
+    T low = tmin > iv.start ? tmin : iv.start;
+    T high = tmax < iv.end ? tmax : iv.end;
+    return low <= std::fma(std::fabs(high), T(9.5367431640625e-7), high);
+  } else {
+    return iv.range_overlaps(tmin, tmax);
+  }
 }
 
 // Intersection (shared/intersect.rs:8-43) plus the material and primitive.
@@ -664,6 +666,7 @@ template <class T> inline void build_bvh(const std::vector<Aabb<T>>& boxes, Bvh<
 
 struct Options {
   bool prim_pretest = true;    // test each leaf object's own Aabb first (object/bvh.rs:100-106)
+  bool brute_force = false;    // no bounding volumes: every primitive, in object order
   size_t exact_bvh_limit = 200000;
 };
 
@@ -884,9 +887,38 @@ template <class P> struct Scene {
 
   // ObjectList::full_intersect (object/list.rs:112-129): the BVH result, then
   // every unbounded object with the original interval; the first minimum wins.
+  // Closest hit of the primitive tests alone, in object order, with the same
+  // shrinking interval (a later hit at equal distance replaces the earlier).
+  bool brute_force(const Ray<P>& ray, const Interval<T>& iv, PathRng& rng, uint32_t depth, Hit<T>& h) const {
+    Interval<T> sh = iv;
+    bool any = false;
+    for (const Object& o : bounded) {
+      if (o.kind == OBJ_MESH) {
+        const Mesh& m = meshes[o.index];
+        for (uint32_t t : m.tris) {
+          Hit<T> hc;
+          if (!tris[t].intersect(ray, sh, hc)) continue;
+          hc.prim = prim_tri(t);
+          hc.material = m.material;
+          sh = sh.with_end(hc.dist);
+          h = hc;
+          any = true;
+        }
+        continue;
+      }
+      Hit<T> hc;
+      if (!object_intersect(o, ray, sh, rng, depth, hc)) continue;
+      sh = sh.with_end(hc.dist);
+      h = hc;
+      any = true;
+    }
+    return any;
+  }
+
   bool intersect(const Ray<P>& ray, const Interval<T>& iv, PathRng& rng, uint32_t depth, Hit<T>& h) const {
     bool any = false;
-    if (top.root >= 0) any = top_node(top.root, ray, iv, rng, depth, h);
+    if (opt.brute_force) any = brute_force(ray, iv, rng, depth, h);
+    else if (top.root >= 0) any = top_node(top.root, ray, iv, rng, depth, h);
     for (uint32_t si : unbounded) {
       Hit<T> hs;
       if (!sdfs[si].intersect(ray, iv, hs)) continue;

@@ -94,6 +94,10 @@ class rg_scene_info(C.Structure):
                 ("sah_cost", C.c_double), ("device_bytes", C.c_uint64)]
 
 
+class rg_tuning(C.Structure):
+    _fields_ = [("wave_paths", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+
+
 class rg_hit(C.Structure):
     _fields_ = [("hit", C.c_uint32), ("prim", C.c_uint32), ("t", C.c_float), ("normal", C.c_float * 3),
                 ("ray_normal", C.c_float * 3), ("front_face", C.c_uint32), ("material", C.c_uint32),
@@ -113,6 +117,8 @@ SIGNATURES = {
     "rg_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
     "rg_inspect_scene": (C.c_int, [C.POINTER(rg_scene_desc), C.POINTER(rg_scene_info)]),
     "rg_set_scene": (C.c_int, [_P, C.POINTER(rg_scene_desc)]),
+    "rg_set_tuning": (C.c_int, [_P, C.POINTER(rg_tuning)]),
+    "rg_get_tuning": (C.c_int, [_P, C.POINTER(rg_tuning)]),
     "rg_set_camera": (C.c_int, [_P, C.POINTER(rg_camera)]),
     "rg_set_options": (C.c_int, [_P, C.POINTER(rg_render_opts)]),
     "rg_clear_accumulation": (C.c_int, [_P]),

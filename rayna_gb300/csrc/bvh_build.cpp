@@ -91,9 +91,9 @@ class Builder {
 
   static void put_child(BvhNode2& nd, int slot, const ChildRef& c) {
     float lx = c.box.lo[0], hx = c.box.hi[0], ly = c.box.lo[1], hy = c.box.hi[1], lz = c.box.lo[2], hz = c.box.hi[2];
-    if (c.index < 0) {  // absent child: an inverted box that no slab test accepts
-      lx = ly = lz = INFINITY;
-      hx = hy = hz = -INFINITY;
+    if (c.index < 0) {  // absent child (only beside a root leaf): skipped by its index
+      lx = ly = lz = 0.0f;
+      hx = hy = hz = 0.0f;
     }
     if (slot == 0) {
       nd.xs.x = lx; nd.xs.y = hx; nd.ys.x = ly; nd.ys.y = hy; nd.zs.x = lz; nd.zs.y = hz;

@@ -50,8 +50,8 @@ struct alignas(16) GpuPrim {
 // Binary BVH node holding both children (Aila & Laine 2009 layout):
 //   xs = (c0.lo.x, c0.hi.x, c1.lo.x, c1.hi.x), ys, zs likewise,
 //   meta = (c0, c1, n0, n1): n == 0 means child c is the internal node
-//   nodes[c]; n > 0 means a leaf over prims [c, c + n). An absent child has
-//   c = -1, n = 0 and an inverted (empty) box.
+//   nodes[c]; n > 0 means a leaf over prims [c, c + n). An absent child
+//   (only next to a root that is a single leaf) has c = -1, n = 0.
 struct alignas(64) BvhNode2 {
   float4 xs, ys, zs;
   int4 meta;
@@ -95,6 +95,7 @@ struct GpuScene {
 enum : uint32_t {
   ERR_STACK_OVERFLOW = 1u,
   ERR_BAD_INDEX = 2u,
+  ERR_QUEUE_OVERFLOW = 4u,
 };
 
 // Counters (RG_FLAG_COUNTERS): indices into the u64 counter array.

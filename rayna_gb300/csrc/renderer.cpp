@@ -518,6 +518,22 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene) {
   return rg_clear_accumulation(h);
 }
 
+rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
+  if (!h || !t) return fail(h, RG_INVALID_ARG, "rg_set_tuning: NULL argument");
+  for (uint32_t r : t->reserved)
+    if (r != 0) return fail(h, RG_INVALID_ARG, "rg_tuning: reserved fields must be 0");
+  if (t->wave_paths != h->wf_paths && h->wf.arena) free_extra(h);
+  h->wf_paths = t->wave_paths;
+  return RG_OK;
+}
+
+rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
+  if (!h || !out) return fail(h, RG_INVALID_ARG, "rg_get_tuning: NULL argument");
+  std::memset(out, 0, sizeof(*out));
+  out->wave_paths = (uint32_t)h->wf_paths;
+  return RG_OK;
+}
+
 rg_status rg_set_camera(rg_handle h, const rg_camera* camera) {
   if (!h || !camera) return fail(h, RG_INVALID_ARG, "rg_set_camera: NULL argument");
   h->cam = *camera;

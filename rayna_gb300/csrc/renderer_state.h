@@ -79,6 +79,7 @@ struct rg_renderer {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
   rg::WavefrontState wf;
+  size_t wf_paths = 0;        // wavefront path slots per wave (0: library default)
 };
 
 namespace rg {

@@ -86,7 +86,7 @@ __device__ __forceinline__ V3 unit_sphere_from(float r1, float r2) {
 // Rays
 // ---------------------------------------------------------------------------
 struct Ray {
-  V3 o, d, inv, noi;  // noi = -(o * inv), for the fused slab test
+  V3 o, d, inv;
 };
 // Ray::new (rayna_engine/src/shared/ray.rs:15-23)
 __device__ __forceinline__ Ray make_ray(V3 o, V3 dir) {
@@ -94,22 +94,29 @@ __device__ __forceinline__ Ray make_ray(V3 o, V3 dir) {
   r.o = o;
   r.d = normalize3(dir);
   r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
-  r.noi = v3(-(o.x * r.inv.x), -(o.y * r.inv.y), -(o.z * r.inv.z));
   return r;
 }
+
+// Relative slack that makes the slab test conservative: the computed entry
+// and exit distances (b - o) * inv carry at most a few units of roundoff, so
+// widening the exit side by 2^-20 relative never rejects a box the ray
+// meets inside [start, end] (Ize, "Robust BVH Ray Traversal", JCGT 2013).
+// Bounding boxes therefore never change which primitive is closest: the
+// result equals the closest hit of the primitive tests alone.
+constexpr float kSlabSlack = 9.5367431640625e-7f;  // 2^-20
 
 // Aabb::hit (rayna_engine/src/shared/aabb.rs:117-153) against [start, end];
 // returns the entry distance in `tnear`.
 __device__ __forceinline__ bool slab(float lx, float hx, float ly, float hy, float lz, float hz, const Ray& r, float start,
                                      float end, float& tnear) {
-  float t1x = __fmaf_rn(lx, r.inv.x, r.noi.x), t2x = __fmaf_rn(hx, r.inv.x, r.noi.x);
-  float t1y = __fmaf_rn(ly, r.inv.y, r.noi.y), t2y = __fmaf_rn(hy, r.inv.y, r.noi.y);
-  float t1z = __fmaf_rn(lz, r.inv.z, r.noi.z), t2z = __fmaf_rn(hz, r.inv.z, r.noi.z);
+  float t1x = (lx - r.o.x) * r.inv.x, t2x = (hx - r.o.x) * r.inv.x;
+  float t1y = (ly - r.o.y) * r.inv.y, t2y = (hy - r.o.y) * r.inv.y;
+  float t1z = (lz - r.o.z) * r.inv.z, t2z = (hz - r.o.z) * r.inv.z;
   float tmin = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fminf(t1z, t2z));
   float tmax = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fmaxf(t1z, t2z));
   float low = fmaxf(tmin, start), high = fminf(tmax, end);
   tnear = low;
-  return low <= high;
+  return low <= __fmaf_rn(fabsf(high), kSlabSlack, high);
 }
 
 // ---------------------------------------------------------------------------
@@ -368,7 +375,7 @@ __device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float
       if (COUNT) ++cnt.nodes;
       float tn0, tn1;
       bool h0 = slab(xs.x, xs.y, ys.x, ys.y, zs.x, zs.y, r, start, tmax, tn0);
-      bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, tmax, tn1);
+      bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, tmax, tn1) && m.y >= 0;
       if (h0 && m.z > 0) { test_leaf<COUNT>(sc, m.x, m.z, r, start, tmax, best, ctx, cnt); h0 = false; }
       if (h1 && m.w > 0) { test_leaf<COUNT>(sc, m.y, m.w, r, start, tmax, best, ctx, cnt); h1 = false; }
       if (h0 && h1) {

@@ -140,6 +140,12 @@ class Renderer:
         self._check(self._lib.rg_set_options(self._h, C.byref(options.to_c())))
         self._options = options
 
+    def set_wave_paths(self, n: int):
+        """Wavefront path slots per wave (0: library default)."""
+        t = A.rg_tuning()
+        t.wave_paths = int(n)
+        self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
+
     def set_thread_count(self, num_threads: int):
         """Accepted for API parity (renderer.rs:179-182); the device is not thread-pooled."""
         return None

@@ -67,16 +67,21 @@ def test_statistical_parity_with_f64_oracle(case):
     scene, cam, opts = CASES[case]()
     flat = flatten(scene)
     frames = {"random_spheres": 24, "cornell_mesh": 48, "sdf_volumes": 32}[case]
+    spp = opts.samples
+    sq = 0.0
     with Renderer.new_from(scene, cam, opts, 0, seed=7) as r:
         for _ in range(frames):
             out = r.render()
+            fm, fv = r.frame_moments()
+            sq = sq + (spp - 1) * fv.astype(np.float64) + spp * fm.astype(np.float64) ** 2
         img = out.img.astype(np.float64)
         assert out.stats.accum_frames == frames
         assert out.stats.error_flags == 0
     st, om, ov, _ = ob.render(flat, cam, opts, seed=11, frames=frames, policy=ob.POLICY_REF_F64)
     assert st == 0
-    n = frames * opts.samples
-    se = np.sqrt(2 * ov / n)           # both sides estimate the same per-sample variance
+    n = frames * spp
+    gv = np.maximum(sq / n - img ** 2, 0.0) * n / (n - 1)   # device per-sample variance
+    se = np.sqrt((gv + ov) / n)
     z = (img - om) / np.maximum(se, 1e-6)
     beyond = np.mean(np.abs(z) > 3)
     rel_rmse = np.sqrt(np.mean((img - om) ** 2)) / max(np.sqrt(np.mean(om ** 2)), 1e-12)
@@ -84,7 +89,7 @@ def test_statistical_parity_with_f64_oracle(case):
     assert beyond <= 0.01
     # the image means agree within 4 standard errors of the mean over pixels
     gm_img, om_img = img.mean(), om.mean()
-    se_img = math.sqrt(np.mean(2 * ov / n) / img.size) * 3  # pixels are correlated: allow 3x
+    se_img = math.sqrt(np.mean((gv + ov) / n) / img.size) * 3  # pixels are correlated: allow 3x
     assert abs(gm_img - om_img) <= 4 * se_img + 1e-6, (gm_img, om_img, se_img)
 
 
@@ -160,3 +165,39 @@ def test_large_spp_path_and_counters():
         assert out.stats.node_visits > 0 and out.stats.prim_tests > 0
     st, om, _, _ = ob.render(flat, cam, opts, seed=9, frames=1, policy=ob.POLICY_GPU_F32)
     np.testing.assert_allclose(gm, om, rtol=1e-4, atol=1e-5)
+
+
+@pytest.mark.parametrize("case", list(CASES) + ["large_spp"])
+def test_wavefront_equals_megakernel(case):
+    """Both kernel forms run the same per-path code with the same random
+    streams and sum samples in the same order: identical images."""
+    if case == "large_spp":
+        scene = presets.single_sphere((0.3, 0.6, 0.9))
+        cam = Camera(pos=(0, 0, -2.7), v_fov=Angle.from_degrees(45), fwd=(0, 0, 1), focus_dist=1.0)
+        opts = RenderOpts(width=8, height=8, samples=300, ray_depth=5)
+    else:
+        scene, cam, opts = CASES[case]()
+    imgs = {}
+    for form in ("megakernel", "wavefront"):
+        with Renderer.new_from(scene, cam, opts, 0, form=form, counters=True) as r:
+            for k in range(2):
+                out = r.render(seed=500 + k)
+            imgs[form] = (out.img.copy(), r.frame_moments(), out.stats)
+    a, b = imgs["megakernel"], imgs["wavefront"]
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1][0], b[1][0])
+    np.testing.assert_array_equal(a[1][1], b[1][1])
+    assert a[2].rays == b[2].rays
+    assert a[2].node_visits == b[2].node_visits and a[2].prim_tests == b[2].prim_tests
+
+
+def test_wavefront_small_waves():
+    """A path budget smaller than the frame splits it into many waves."""
+    import ctypes as C
+    scene, cam, opts = CASES["random_spheres"]()
+    with Renderer.new_from(scene, cam, opts, 0, form="megakernel") as r:
+        ref = r.render(seed=77).img
+    with Renderer.new_from(scene, cam, opts, 0, form="wavefront") as r:
+        r.set_wave_paths(1000)
+        img = r.render(seed=77).img
+    np.testing.assert_array_equal(ref, img)
