@@ -313,6 +313,36 @@ rg_status rg_frame_moments(rg_handle h, float* mean, float* variance);
 rg_status rg_query_rays(rg_handle h, uint32_t n, const float* origins, const float* dirs,
                         const float* tmin, const float* tmax, const float* volume_u, rg_hit* out);
 
+/* Path slots of the fixed device array used by rg_render_static_scratch
+ * (31 x 4 bytes each: about 8 MB, held by every device that loads the library). */
+#define RG_STATIC_WAVE_PATHS 65536u
+
+/* No counterpart in the reference: the reference renders on the CPU and never
+ * allocates device memory.
+ *
+ * Renders one frame of the handle's current scene, camera and options with the
+ * wavefront kernels, without allocating anything. It is for callers that cannot
+ * call cudaMalloc: a host that hands out all device memory from its own pool or
+ * arena, or a render loop in which allocation is not allowed. The path queues of
+ * the frame live in one fixed, library-owned device array of RG_STATIC_WAVE_PATHS
+ * path slots instead of cudaMalloc'ed scratch; the frame runs in waves of whole
+ * pixels that fit in it.
+ *
+ * The caller passes the outputs: `d_accum` is a device buffer of width*height*3
+ * floats ([x][y][rgb]) holding the running sum, updated in place, and
+ * `accum_count` the number of frames in it after this one (>= 1); `d_out`, if not
+ * NULL, is a device buffer of the same size that receives the running mean. The
+ * scene must already be on the device (rg_set_scene). The image is the same as
+ * rg_render's for the same seed.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. Every
+ * call shares the one array and finds it as the last call left it: calls whose
+ * kernels overlap on the GPU (other streams, other handles) race. Samples per
+ * pixel above RG_STATIC_WAVE_PATHS are rejected with RG_INVALID_ARG. Returns
+ * once the kernels are queued on the handle's stream. */
+rg_status rg_render_static_scratch(rg_handle h, uint64_t seed, float* d_accum, uint32_t accum_count, float* d_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -129,6 +129,7 @@ SIGNATURES = {
     "rg_set_accumulation": (C.c_int, [_P, _F, C.c_uint32]),
     "rg_frame_moments": (C.c_int, [_P, _F, _F]),
     "rg_query_rays": (C.c_int, [_P, C.c_uint32, _F, _F, _F, _F, _F, C.POINTER(rg_hit)]),
+    "rg_render_static_scratch": (C.c_int, [_P, C.c_uint64, _P, C.c_uint32, _P]),
 }
 
 _lib = None

@@ -92,6 +92,7 @@ rg_status set_error(rg_renderer* h, rg_status st, const char* msg);
 
 // Defined in wavefront.cu
 cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp);
+cudaError_t launch_wavefront_static(rg_renderer* h, const FrameParams& fp);
 void free_extra(rg_renderer* h);
 void on_scene_changed(rg_renderer* h);
 

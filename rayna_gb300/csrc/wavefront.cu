@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "kernels.h"
 #include "renderer_state.h"
@@ -350,6 +351,106 @@ cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp) {
   }
   return cudaSuccess;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant: the path state of one wave lives in a fixed
+// file-scope device array instead of a cudaMalloc'ed arena.
+// ---------------------------------------------------------------------------
+constexpr size_t kStaticArenaBytes = 31ull * 4ull * RG_STATIC_WAVE_PATHS + 256ull;
+static __device__ __align__(256) unsigned char g_wave_scratch[kStaticArenaBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of g_wave_scratch on `device` (which must be current),
+// looked up once per device. In host code the array's name is only a
+// host-side stand-in, so kernels get this address instead.
+static cudaError_t static_scratch(int device, void** out) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_wave_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[device] = p;
+  }
+  *out = g_scratch_ptr[device];
+  return cudaSuccess;
+}
+
+cudaError_t launch_wavefront_static(rg_renderer* h, const FrameParams& fp) {
+  const size_t spp = fp.spp;
+  const size_t n_pix = (size_t)fp.width * fp.height;
+  const size_t cap = RG_STATIC_WAVE_PATHS;
+  if (arena_bytes(cap) > kStaticArenaBytes || spp > cap) return cudaErrorInvalidValue;
+  void* arena = nullptr;
+  cudaError_t e = static_scratch(h->device, &arena);
+  if (e != cudaSuccess) return e;
+  PathSoA s;
+  carve((char*)arena, cap, s);
+  const size_t pix_per_wave = std::min(cap / spp, n_pix);
+  const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
+  const int grid = sm_count(h->device) * 8;
+  cudaStream_t st = h->stream;
+  for (size_t first = 0; first < n_pix; first += pix_per_wave) {
+    WaveParams wp;
+    wp.first_pixel = (uint32_t)first;
+    wp.n_pixels = (uint32_t)std::min(pix_per_wave, n_pix - first);
+    wp.n_paths = (uint32_t)(wp.n_pixels * spp);
+    wp.capacity = (uint32_t)cap;
+    uint32_t gen_blocks = (uint32_t)std::min<size_t>((wp.n_paths + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
+    k_generate<<<gen_blocks, kWfBlock, 0, st>>>(fp, s, wp);
+    int cur = 0;
+    for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
+      if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+      if (counters) k_extend<true><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      else k_extend<false><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      k_shade<<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      cur ^= 1;
+    }
+    uint32_t acc_blocks = (uint32_t)std::min<size_t>((wp.n_pixels * 3 + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
+    k_accumulate<<<acc_blocks, kWfBlock, 0, st>>>(fp, s, wp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace rg
+
+// The allocation-free entry point (see rayna_gpu.h).
+extern "C" rg_status rg_render_static_scratch(rg_handle h, uint64_t seed, float* d_accum, uint32_t accum_count,
+                                              float* d_out) {
+  using namespace rg;
+  if (!h) return RG_INVALID_ARG;
+  if (!d_accum || accum_count == 0)
+    return set_error(h, RG_INVALID_ARG, "rg_render_static_scratch: d_accum must be a device buffer and accum_count >= 1");
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return set_error(h, RG_CUDA_ERROR, cudaGetErrorString(e));
+  if (!h->cam_ok) return set_error(h, RG_INVALID_CAMERA, "camera viewport could not be calculated");
+  if (h->opts.samples > RG_STATIC_WAVE_PATHS)
+    return set_error(h, RG_INVALID_ARG,
+                     "rg_render_static_scratch: samples per pixel exceed the 65536 path slots of the static scratch");
+  FrameParams fp;
+  fill_frame_params(h, seed, fp);
+  fp.accum = d_accum;
+  fp.out = d_out;
+  fp.frame_mean = nullptr;
+  fp.frame_var = nullptr;
+  fp.accum_count = accum_count;
+  if ((e = cudaMemsetAsync(h->d_counters, 0, CNT_N * sizeof(unsigned long long), h->stream)) != cudaSuccess)
+    return set_error(h, RG_CUDA_ERROR, cudaGetErrorString(e));
+  if ((e = launch_wavefront_static(h, fp)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(h, RG_CUDA_ERROR, cudaGetErrorString(e));
+  }
+  return RG_OK;
+}
+
+namespace rg {
 
 void free_extra(rg_renderer* h) {
   if (h->wf.arena) cudaFree(h->wf.arena);
