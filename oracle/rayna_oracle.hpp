@@ -420,6 +420,33 @@ template <class P> struct Sdf {
     int iters = (int)p[1];
     V3<T> z = z0;
     T dr = T(1), r = T(0);
+    if (power == T(8)) {
+      // z^8 without transcendentals: with cos t = z/r, sin t = rho/r and
+      // cos p + i sin p = (x + i y)/rho, three complex squarings give 8t, 8p.
+      for (int i = 0; i < iters; ++i) {
+        T rho2 = z.x * z.x + z.y * z.y;
+        T r2 = rho2 + z.z * z.z;
+        r = std::sqrt(r2);
+        if (r > T(2)) break;
+        T rho = std::sqrt(rho2);
+        T ct = T(1), st = T(0), cp = T(1), sp = T(0);
+        if (r > T(0)) { ct = z.z / r; st = rho / r; }
+        if (rho > T(0)) { cp = z.x / rho; sp = z.y / rho; }
+        for (int k = 0; k < 3; ++k) {
+          T c2 = ct * ct - st * st;
+          st = T(2) * ct * st;
+          ct = c2;
+          T d2 = cp * cp - sp * sp;
+          sp = T(2) * cp * sp;
+          cp = d2;
+        }
+        T r4 = r2 * r2;
+        T zr = r4 * r4;
+        dr = (r4 * r2 * r) * T(8) * dr + T(1);
+        z = V3<T>{zr * (st * cp), zr * (sp * st), zr * ct} + z0;
+      }
+      return (T(0.5) * std::log(r) * r / dr) * s;
+    }
     for (int i = 0; i < iters; ++i) {
       r = Math<P>::length(z);
       if (r > T(2)) break;

@@ -89,6 +89,7 @@ struct GpuScene {
   uint32_t tri_base;   // global id of triangle 0
   uint32_t vol_base;   // global id of volume 0
   uint32_t n_tris;
+  uint32_t features;   // F_* bits of the kernel variant to launch (primitive kinds present)
 };
 
 // Device error bits (rg_render_stats::error_flags).

@@ -1,13 +1,17 @@
 // megakernel.cu — the plain kernel form: one thread per pixel-sample.
 //
-// A block of 256 threads takes 256/spp consecutive pixels (row-major) and all
-// of their samples, so the primary rays of a warp are coherent. Each thread
-// traces one full path (trace.cuh); the block then sums every pixel's samples
-// in sample order (the order of render_px_msaa's fold, renderer.rs:396-401),
-// divides by spp, and updates the accumulation buffer in place
-// (AccumulationValue::insert_sample, accum_buffer.rs:37-42). For spp > 256
-// each thread loops over samples s = tid, tid + 256, ... and the block sums
-// the per-thread partials in thread order.
+// Each warp owns whole pixels: 32/spp pixels when spp <= 32 (lane l traces
+// sample l % spp of pixel l / spp), or one pixel when spp > 32 (lane l traces
+// samples l, l+32, ... one after another). Each thread traces full paths
+// (trace.cuh); the warp then sums every pixel's samples with shuffles, divides
+// by spp, and updates the accumulation buffer in place
+// (AccumulationValue::insert_sample, accum_buffer.rs:37-42). There is no
+// block-wide barrier: a warp finishes as soon as its own paths do.
+//
+// Sample sums follow one canonical order, shared with the wavefront form:
+// for spp <= 32 samples 0..spp-1 in turn (the order of render_px_msaa's fold,
+// renderer.rs:396-401); for spp > 32 lane partials (samples l, l+32, ... in
+// turn) added for l = 0..31 in turn.
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -16,6 +20,7 @@
 namespace rg {
 
 constexpr int kMegaBlock = 256;
+constexpr int kWarpsPerBlock = kMegaBlock / 32;
 
 __device__ __forceinline__ void write_pixel(const FrameParams& fp, uint32_t pix, int c, float sum, double sumd, double sqd,
                                             uint32_t n) {
@@ -32,60 +37,70 @@ __device__ __forceinline__ void write_pixel(const FrameParams& fp, uint32_t pix,
   }
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(kMegaBlock) k_megakernel(GpuScene sc, FrameParams fp, uint32_t ppb, uint32_t n_pix) {
-  __shared__ float sh[kMegaBlock][3];
-  __shared__ unsigned long long sh_seg;
-  const uint32_t tid = threadIdx.x;
+template <uint32_t F, bool COUNT>
+__global__ void __launch_bounds__(kMegaBlock) k_megakernel(GpuScene sc, FrameParams fp, uint32_t n_pix) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   const uint32_t spp = fp.spp;
-  if (tid == 0) sh_seg = 0;
   Counters cnt;
   uint32_t segments = 0;
-  if (spp <= kMegaBlock) {
-    uint32_t lp = tid / spp, s = tid % spp;
-    uint32_t pix = blockIdx.x * ppb + lp;
+  if (spp <= 32) {
+    const uint32_t ppw = 32 / spp;
+    const uint32_t lp = lane / spp, s = lane % spp;
+    const uint32_t pix = warp * ppw + lp;
+    const bool active = lp < ppw && pix < n_pix;
     C3f col{0.0f, 0.0f, 0.0f};
-    if (lp < ppb && pix < n_pix) col = trace_path<COUNT>(sc, fp, pix % fp.width, pix / fp.width, s, cnt, segments);
-    sh[tid][0] = col.r; sh[tid][1] = col.g; sh[tid][2] = col.b;
-    __syncthreads();
-    if (tid < ppb * 3) {
-      uint32_t p = tid / 3, c = tid % 3;
-      uint32_t px = blockIdx.x * ppb + p;
-      if (px < n_pix) {
-        float sum = 0.0f;
-        double sumd = 0.0, sqd = 0.0;
-        for (uint32_t k = 0; k < spp; ++k) {
-          float v = sh[p * spp + k][c];
-          sum = sum + v;
-          sumd += v;
-          sqd += (double)v * v;
-        }
-        write_pixel(fp, px, (int)c, sum, sumd, sqd, spp);
+    if (active) col = trace_path<F, COUNT>(sc, fp, pix % fp.width, pix / fp.width, s, cnt, segments);
+    // Lane holding sample 0 of a pixel adds samples 1..spp-1 in order.
+    const uint32_t base = lp * spp;
+    float v[3] = {col.r, col.g, col.b};
+    float sum[3] = {v[0], v[1], v[2]};
+    double sumd[3] = {v[0], v[1], v[2]};
+    double sqd[3] = {(double)v[0] * v[0], (double)v[1] * v[1], (double)v[2] * v[2]};
+    for (uint32_t k = 1; k < spp; ++k) {
+      uint32_t src = (base + k) & 31;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float o = __shfl_sync(0xffffffffu, v[c], src);
+        sum[c] = sum[c] + o;
+        sumd[c] += o;
+        sqd[c] += (double)o * o;
       }
     }
+    if (active && s == 0)
+      for (int c = 0; c < 3; ++c) write_pixel(fp, pix, c, sum[c], sumd[c], sqd[c], spp);
   } else {
-    __shared__ double shd[kMegaBlock][3];
-    uint32_t pix = blockIdx.x;
-    float sum[3] = {0.0f, 0.0f, 0.0f};
-    double sq[3] = {0.0, 0.0, 0.0};
-    for (uint32_t s = tid; s < spp; s += kMegaBlock) {
-      C3f col = trace_path<COUNT>(sc, fp, pix % fp.width, pix / fp.width, s, cnt, segments);
-      sum[0] = sum[0] + col.r; sum[1] = sum[1] + col.g; sum[2] = sum[2] + col.b;
-      sq[0] += (double)col.r * col.r; sq[1] += (double)col.g * col.g; sq[2] += (double)col.b * col.b;
+    const uint32_t pix = warp;
+    const bool active = pix < n_pix;
+    float part[3] = {0.0f, 0.0f, 0.0f};
+    double psq[3] = {0.0, 0.0, 0.0};
+    if (active) {
+      for (uint32_t s = lane; s < spp; s += 32) {
+        C3f col = trace_path<F, COUNT>(sc, fp, pix % fp.width, pix / fp.width, s, cnt, segments);
+        part[0] = part[0] + col.r; part[1] = part[1] + col.g; part[2] = part[2] + col.b;
+        psq[0] += (double)col.r * col.r; psq[1] += (double)col.g * col.g; psq[2] += (double)col.b * col.b;
+      }
     }
-    for (int c = 0; c < 3; ++c) { sh[tid][c] = sum[c]; shd[tid][c] = sq[c]; }
-    __syncthreads();
-    if (tid < 3) {
-      float total = 0.0f;
-      double td = 0.0, tq = 0.0;
-      for (int k = 0; k < kMegaBlock; ++k) { total = total + sh[k][tid]; td += sh[k][tid]; tq += shd[k][tid]; }
-      write_pixel(fp, pix, (int)tid, total, td, tq, spp);
+    float sum[3] = {part[0], part[1], part[2]};
+    double sumd[3] = {part[0], part[1], part[2]};
+    double sqd[3] = {psq[0], psq[1], psq[2]};
+    for (uint32_t k = 1; k < 32; ++k) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float o = __shfl_sync(0xffffffffu, part[c], k);
+        double oq = __shfl_sync(0xffffffffu, psq[c], k);
+        sum[c] = sum[c] + o;
+        sumd[c] += o;
+        sqd[c] += oq;
+      }
     }
+    if (active && lane == 0)
+      for (int c = 0; c < 3; ++c) write_pixel(fp, pix, c, sum[c], sumd[c], sqd[c], spp);
   }
   // Work counters: one atomic per warp.
   unsigned long long seg = segments;
   for (int o = 16; o > 0; o >>= 1) seg += __shfl_down_sync(0xffffffffu, seg, o);
-  if ((tid & 31) == 0) atomicAdd(&sh_seg, seg);
+  if (lane == 0 && seg) atomicAdd(fp.counters + CNT_RAYS, seg);
   if (COUNT) {
     unsigned long long a = cnt.nodes, b = cnt.prims, c = cnt.sdf_steps;
     for (int o = 16; o > 0; o >>= 1) {
@@ -93,22 +108,29 @@ __global__ void __launch_bounds__(kMegaBlock) k_megakernel(GpuScene sc, FramePar
       b += __shfl_down_sync(0xffffffffu, b, o);
       c += __shfl_down_sync(0xffffffffu, c, o);
     }
-    if ((tid & 31) == 0) {
+    if (lane == 0) {
       atomicAdd(fp.counters + CNT_NODES, a);
       atomicAdd(fp.counters + CNT_PRIMS, b);
       atomicAdd(fp.counters + CNT_SDF, c);
     }
   }
-  __syncthreads();
-  if (tid == 0) atomicAdd(fp.counters + CNT_RAYS, sh_seg);
+}
+
+template <uint32_t F>
+static void launch_mega(const GpuScene& sc, const FrameParams& fp, bool counters, uint32_t blocks, uint32_t n_pix,
+                        cudaStream_t stream) {
+  if (counters) k_megakernel<F, true><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+  else k_megakernel<F, false><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
 }
 
 cudaError_t launch_megakernel(const GpuScene& sc, const FrameParams& fp, bool counters, cudaStream_t stream) {
   const uint32_t n_pix = fp.width * fp.height;
-  uint32_t ppb = fp.spp <= (uint32_t)kMegaBlock ? kMegaBlock / fp.spp : 1u;
-  uint32_t blocks = (n_pix + ppb - 1) / ppb;
-  if (counters) k_megakernel<true><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, ppb, n_pix);
-  else k_megakernel<false><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, ppb, n_pix);
+  const uint32_t ppw = fp.spp <= 32 ? 32 / fp.spp : 1u;
+  const uint32_t warps = (n_pix + ppw - 1) / ppw;
+  const uint32_t blocks = (warps + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (sc.features == F_TRI) launch_mega<F_TRI>(sc, fp, counters, blocks, n_pix, stream);
+  else if (sc.features == F_SPHERE) launch_mega<F_SPHERE>(sc, fp, counters, blocks, n_pix, stream);
+  else launch_mega<F_ALL>(sc, fp, counters, blocks, n_pix, stream);
   return cudaGetLastError();
 }
 
@@ -128,9 +150,9 @@ __global__ void k_query(GpuScene sc, uint32_t n, const float* o, const float* d,
   res.normal[0] = res.normal[1] = res.normal[2] = 0.0f;
   res.ray_normal[0] = res.ray_normal[1] = res.ray_normal[2] = 0.0f;
   res.front_face = 0; res.material = 0; res.side = 0;
-  if (closest_hit<false>(sc, r, tmin[i], tmax[i], ctx, h, cnt, err)) {
+  if (closest_hit<F_ALL, false>(sc, r, tmin[i], tmax[i], ctx, h, cnt, err)) {
     Surface s;
-    finalize_hit(sc, r, h, ctx, s);
+    finalize_hit<F_ALL>(sc, r, h, ctx, s);
     res.hit = 1;
     res.prim = s.prim_id;
     res.t = h.t;

@@ -114,7 +114,7 @@ rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
       !need(d.n_sdfs, d.sdfs, "sdfs") || !need(d.n_materials, d.materials, "materials"))
     return RG_INVALID_ARG;
   uint64_t total = (uint64_t)d.n_spheres + d.n_triangles + d.n_boxes + d.n_volumes + d.n_sdfs;
-  if (total >= (1ull << 31)) return fail(h, RG_INVALID_ARG, "too many primitives (%llu)", (unsigned long long)total);
+  if (total >= (1ull << 28)) return fail(h, RG_INVALID_ARG, "too many primitives (%llu; limit 2^28)", (unsigned long long)total);
   if (d.n_materials > kMaterialMask) return fail(h, RG_INVALID_ARG, "too many materials");
   if (d.skybox > RG_SKY_NONE) return fail(h, RG_UNSUPPORTED_VARIANT, "skybox kind %u", d.skybox);
   for (uint32_t i = 0; i < d.n_materials; ++i) {
@@ -323,6 +323,10 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.tri_base = hs.ns;
   g.vol_base = hs.vol_base;
   g.n_tris = hs.nt;
+  // Kernel variant: triangles only, spheres only, or every kind (F_* bits of trace.cuh).
+  const uint32_t kSphere = 1, kTri = 2, kAll = 31;
+  uint32_t have = (hs.ns ? kSphere : 0) | (hs.nt ? kTri : 0) | (hs.nb ? 4u : 0) | (hs.nv ? 8u : 0) | (hs.nsdf ? 16u : 0);
+  g.features = have == kTri ? kTri : (have == kSphere ? kSphere : kAll);
   return RG_OK;
 }
 
@@ -428,6 +432,7 @@ rg_status rg_create(const rg_device_opts* opts, rg_handle* out) {
   h->opts = rg_render_opts{740, 480, 1, RG_MODE_PBR, 5, 1};
   h->gs = GpuScene{};
   h->gs.sky = RG_SKY_SIMPLE;
+  h->gs.features = 31;
   *out = h;
   return RG_OK;
 }

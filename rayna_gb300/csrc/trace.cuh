@@ -252,17 +252,45 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x) {
   int iters = (int)s.p1;
   V3 z = z0;
   float dr = 1.0f, rr = 0.0f;
-  for (int i = 0; i < iters; ++i) {
-    rr = length3(z);
-    if (rr > 2.0f) break;
-    float theta = acosf(z.z / rr);
-    float phi = atan2f(z.y, z.x);
-    dr = powf(rr, power - 1.0f) * power * dr + 1.0f;
-    float zr = powf(rr, power);
-    theta = theta * power;
-    phi = phi * power;
-    float st = sinf(theta);
-    z = v3(zr * (st * cosf(phi)), zr * (sinf(phi) * st), zr * cosf(theta)) + z0;
+  if (power == 8.0f) {
+    // z^8 without transcendentals: with cos t = z/r, sin t = rho/r and
+    // cos p + i sin p = (x + i y)/rho, three complex squarings give 8t and 8p.
+    for (int i = 0; i < iters; ++i) {
+      float rho2 = z.x * z.x + z.y * z.y;
+      float r2 = rho2 + z.z * z.z;
+      rr = __fsqrt_rn(r2);
+      if (rr > 2.0f) break;
+      float rho = __fsqrt_rn(rho2);
+      float ct = 1.0f, st = 0.0f, cp = 1.0f, sp = 0.0f;
+      if (rr > 0.0f) { ct = z.z / rr; st = rho / rr; }
+      if (rho > 0.0f) { cp = z.x / rho; sp = z.y / rho; }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float c2 = ct * ct - st * st;
+        st = 2.0f * ct * st;
+        ct = c2;
+        float d2 = cp * cp - sp * sp;
+        sp = 2.0f * cp * sp;
+        cp = d2;
+      }
+      float r4 = r2 * r2;
+      float zr = r4 * r4;
+      dr = (r4 * r2 * rr) * 8.0f * dr + 1.0f;
+      z = v3(zr * (st * cp), zr * (sp * st), zr * ct) + z0;
+    }
+  } else {
+    for (int i = 0; i < iters; ++i) {
+      rr = length3(z);
+      if (rr > 2.0f) break;
+      float theta = acosf(z.z / rr);
+      float phi = atan2f(z.y, z.x);
+      dr = powf(rr, power - 1.0f) * power * dr + 1.0f;
+      float zr = powf(rr, power);
+      theta = theta * power;
+      phi = phi * power;
+      float st = sinf(theta);
+      z = v3(zr * (st * cosf(phi)), zr * (sinf(phi) * st), zr * cosf(theta)) + z0;
+    }
   }
   return (0.5f * logf(rr) * rr / dr) * sc;
 }
@@ -322,18 +350,21 @@ struct Counters {
   unsigned long long nodes = 0, prims = 0, sdf_steps = 0;
 };
 
+// Primitive kinds a kernel is specialised for (GpuScene::features).
+enum : uint32_t { F_SPHERE = 1u, F_TRI = 2u, F_BOX = 4u, F_VOL = 8u, F_SDF = 16u, F_ALL = 31u };
+
 // Test the primitives of one leaf, shrinking `end` to each accepted hit
 // (object/bvh.rs:82-96: a later hit at equal distance replaces the earlier).
-template <bool COUNT>
+template <uint32_t F, bool COUNT>
 __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int count, const Ray& r, float start, float& end,
                                           int& best, const RngCtx& ctx, Counters& cnt) {
   for (int i = first; i < first + count; ++i) {
     const GpuPrim* pp = sc.prims + i;
     float4 a = __ldg(&pp->a);
-    uint32_t kind = __float_as_uint(a.w) >> kKindShift;
+    uint32_t kind = F == F_TRI ? (uint32_t)PK_TRIANGLE : (F == F_SPHERE ? (uint32_t)PK_SPHERE : __float_as_uint(a.w) >> kKindShift);
     if (COUNT) ++cnt.prims;
     float t;
-    if (kind == PK_TRIANGLE) {
+    if ((F & F_TRI) && kind == PK_TRIANGLE) {
       float4 b = __ldg(&pp->b), c = __ldg(&pp->c);
       float u, v, det;
       if (!triangle_t(xyz(a), xyz(b), xyz(c), r, start, end, t, u, v, det)) continue;
@@ -341,56 +372,101 @@ __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int cou
         V3 n;
         if (!tri_normal(sc.tri_normals + 9ull * (__float_as_uint(b.w) - sc.tri_base), u, v, n)) continue;
       }
-    } else if (kind == PK_SPHERE) {
+    } else if ((F & F_SPHERE) && kind == PK_SPHERE) {
       float4 b = __ldg(&pp->b);
       if (!sphere_t(xyz(a), b.y, r, start, end, t)) continue;
-    } else if (kind == PK_BOX) {
+    } else if ((F & F_BOX) && kind == PK_BOX) {
       float4 b = __ldg(&pp->b), c = __ldg(&pp->c);
       BoxHit bh;
       if (!box_t(xyz(a), xyz(b), xyz(c), r, start, end, bh)) continue;
       t = bh.t;
-    } else {
+    } else if ((F & F_VOL) && (kind == PK_VOL_SPHERE || kind == PK_VOL_BOX)) {
       GpuPrim p;
       p.a = a; p.b = __ldg(&pp->b); p.c = __ldg(&pp->c);
       if (!volume_t(p, kind, __float_as_uint(p.b.w) - sc.vol_base, r, start, end, ctx, t)) continue;
+    } else {
+      continue;
     }
     end = t;
     best = i;
   }
 }
 
-template <bool COUNT>
+// Child reference: an internal node pair index (>= 0), or a leaf encoded as
+// ~(first << 3 | count) (< 0). kDone ends the traversal.
+constexpr int kDone = 0x7FFFFFFF;
+__device__ __forceinline__ int child_ref(int index, int count) { return count > 0 ? ~((index << 3) | count) : index; }
+
+// Closest hit over the BVH, then the unbounded list. Traversal follows Aila &
+// Laine ("Understanding the efficiency of ray traversal on GPUs", HPG 2009):
+// an inner-node loop that postpones the first leaf it meets and keeps going
+// until every lane of the warp holds a leaf, then a leaf loop, so that lanes
+// step through nodes together and through primitives together. Near children
+// go first; far children wait on a stack with their entry distance and are
+// dropped on pop once they lie beyond the closest hit (the same conservative
+// comparison as the slab test, so the result does not change).
+template <uint32_t F, bool COUNT>
 __device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float end, const RngCtx& ctx, HitRec& h,
                             Counters& cnt, uint32_t* err) {
   int best = -1;
   float tmax = end;
   if (sc.n_nodes > 0) {
     int stack[kStackSize];
+    float stack_t[kStackSize];
     int sp = 0;
-    int node = 0;
-    while (node >= 0) {
-      const BvhNode2* np = sc.nodes + node;
-      float4 xs = __ldg(&np->xs), ys = __ldg(&np->ys), zs = __ldg(&np->zs);
-      int4 m = __ldg(&np->meta);
-      if (COUNT) ++cnt.nodes;
-      float tn0, tn1;
-      bool h0 = slab(xs.x, xs.y, ys.x, ys.y, zs.x, zs.y, r, start, tmax, tn0);
-      bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, tmax, tn1) && m.y >= 0;
-      if (h0 && m.z > 0) { test_leaf<COUNT>(sc, m.x, m.z, r, start, tmax, best, ctx, cnt); h0 = false; }
-      if (h1 && m.w > 0) { test_leaf<COUNT>(sc, m.y, m.w, r, start, tmax, best, ctx, cnt); h1 = false; }
-      if (h0 && h1) {
-        bool swap = tn1 < tn0;
-        int nearc = swap ? m.y : m.x, farc = swap ? m.x : m.y;
-        if (sp < kStackSize) stack[sp++] = farc;
-        else atomicOr(err, ERR_STACK_OVERFLOW);
-        node = nearc;
-      } else if (h0) {
-        node = m.x;
-      } else if (h1) {
-        node = m.y;
-      } else {
-        node = sp > 0 ? stack[--sp] : -1;
+    int ref = 0;
+    int leaf = 0;
+    auto pop = [&]() -> int {
+      float lim = __fmaf_rn(fabsf(tmax), kSlabSlack, tmax);
+      while (sp > 0) {
+        --sp;
+        if (stack_t[sp] <= lim) return stack[sp];
       }
+      return kDone;
+    };
+    for (;;) {
+      while (ref >= 0 && ref != kDone) {
+        const BvhNode2* np = sc.nodes + ref;
+        float4 xs = __ldg(&np->xs), ys = __ldg(&np->ys), zs = __ldg(&np->zs);
+        int4 m = __ldg(&np->meta);
+        if (COUNT) ++cnt.nodes;
+        float tn0, tn1;
+        bool h0 = slab(xs.x, xs.y, ys.x, ys.y, zs.x, zs.y, r, start, tmax, tn0);
+        bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, tmax, tn1) && m.y >= 0;
+        int r0 = child_ref(m.x, m.z), r1 = child_ref(m.y, m.w);
+        if (h0 && h1) {
+          bool swap = tn1 < tn0;
+          ref = swap ? r1 : r0;
+          if (sp < kStackSize) {
+            stack[sp] = swap ? r0 : r1;
+            stack_t[sp] = swap ? tn0 : tn1;
+            ++sp;
+          } else {
+            atomicOr(err, ERR_STACK_OVERFLOW);
+          }
+        } else if (h0) {
+          ref = r0;
+        } else if (h1) {
+          ref = r1;
+        } else {
+          ref = pop();
+        }
+        if (ref < 0 && leaf == 0) {  // postpone the first leaf and keep traversing
+          leaf = ref;
+          ref = pop();
+        }
+        if (!__any_sync(__activemask(), leaf == 0)) break;
+      }
+      while (leaf < 0) {
+        int code = ~leaf;
+        test_leaf<F, COUNT>(sc, code >> 3, code & 7, r, start, tmax, best, ctx, cnt);
+        leaf = 0;
+        if (ref < 0) {
+          leaf = ref;
+          ref = pop();
+        }
+      }
+      if (ref == kDone) break;
     }
   }
   h.prim = best;
@@ -399,13 +475,15 @@ __device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float
   bool any = best >= 0;
   // ObjectList::full_intersect (object/list.rs:112-129): every unbounded object
   // with the original interval; it replaces the result only if strictly closer.
-  for (uint32_t k = 0; k < sc.n_sdfs; ++k) {
-    SdfHit sh;
-    if (sdf_march<COUNT>(sc.sdfs[k], r, start, end, any ? h.t : end, !any, sh, cnt.sdf_steps)) {
-      h.t = sh.t;
-      h.sdf = (int)k;
-      h.sh = sh;
-      any = true;
+  if (F & F_SDF) {
+    for (uint32_t k = 0; k < sc.n_sdfs; ++k) {
+      SdfHit sh;
+      if (sdf_march<COUNT>(sc.sdfs[k], r, start, end, any ? h.t : end, !any, sh, cnt.sdf_steps)) {
+        h.t = sh.t;
+        h.sdf = (int)k;
+        h.sh = sh;
+        any = true;
+      }
     }
   }
   return any;
@@ -419,8 +497,9 @@ struct Surface {
   float u, v;
 };
 
+template <uint32_t F>
 __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, const HitRec& h, const RngCtx& ctx, Surface& s) {
-  if (h.sdf >= 0) {
+  if ((F & F_SDF) && h.sdf >= 0) {
     const GpuSdf& f = sc.sdfs[h.sdf];
     s.pos = at3(r.o, r.d, h.t);
     s.normal = h.sh.n;
@@ -438,7 +517,9 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
   s.prim_id = prim_id(p);
   s.pos = at3(r.o, r.d, h.t);
   s.side = 0;
-  if (kind == PK_SPHERE) {
+  if (F == F_TRI) kind = PK_TRIANGLE;
+  if (F == F_SPHERE) kind = PK_SPHERE;
+  if ((F & F_SPHERE) && kind == PK_SPHERE) {
     V3 c = xyz(p.a);
     float rad = p.b.x;
     V3 local = v3((s.pos.x - c.x) / rad, (s.pos.y - c.y) / rad, (s.pos.z - c.z) / rad);
@@ -447,7 +528,7 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
     s.ray_normal = inside ? -local : local;
     s.front = !inside;
     s.u = s.v = 0.0f;  // sphere_uv is only needed by textured / Uv modes
-  } else if (kind == PK_TRIANGLE) {
+  } else if ((F & F_TRI) && kind == PK_TRIANGLE) {
     float t, u, v, det;
     triangle_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, CUDART_INF_F, t, u, v, det);
     V3 n;
@@ -456,7 +537,7 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
     s.ray_normal = n * (-signumf(det));
     s.front = signbit(det);
     s.u = u; s.v = v;
-  } else if (kind == PK_BOX) {
+  } else if ((F & F_BOX) && kind == PK_BOX) {
     BoxHit bh;
     box_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, h.t, bh);
     V3 rn = v3(bh.axis == 0 ? bh.sgn : 0.0f, bh.axis == 1 ? bh.sgn : 0.0f, bh.axis == 2 ? bh.sgn : 0.0f);
@@ -596,7 +677,7 @@ __device__ __forceinline__ Ray camera_ray(const FrameParams& fp, uint32_t x, uin
 
 // One path sample: ray_colour_recursive (renderer.rs:508-572) evaluated front
 // to back: L = sum_k beta_k * emitted_k + beta_K * sky.
-template <bool COUNT>
+template <uint32_t F, bool COUNT>
 __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x, uint32_t y, uint32_t s, Counters& cnt,
                           uint32_t& segments) {
   RngCtx ctx{fp.seed_lo, fp.seed_hi, y * fp.width + x, s, 0, nullptr};
@@ -606,13 +687,13 @@ __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x,
     ctx.depth = depth;
     HitRec h;
     ++segments;
-    if (!closest_hit<COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
+    if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
       C3f sk = sky_colour(sc.sky, ray.d);
       L = C3f{L.r + beta.r * sk.r, L.g + beta.g * sk.g, L.b + beta.b * sk.b};
       break;
     }
     Surface surf;
-    finalize_hit(sc, ray, h, ctx, surf);
+    finalize_hit<F>(sc, ray, h, ctx, surf);
     const rg_material m = sc.materials[surf.material];
     if (m.kind == RG_MAT_LIGHT) {
       L = C3f{L.r + beta.r * m.albedo[0], L.g + beta.g * m.albedo[1], L.b + beta.b * m.albedo[2]};

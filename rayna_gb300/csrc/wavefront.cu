@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kWfBlock) k_generate(FrameParams fp, PathSoA s
   }
 }
 
-template <bool COUNT>
+template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathSoA s, WaveParams wp, int cur) {
   uint32_t n = s.counts[cur];
   if (n > wp.n_paths) {  // never expected: record and clamp instead of reading past the queue
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
     RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, s.depth[p], nullptr};
     HitRec h;
     ++queries;
-    bool hit = closest_hit<COUNT>(sc, r, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
+    bool hit = closest_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
     uint32_t kind = KQ_MISS;
     if (hit) {
       uint32_t mat;
@@ -149,6 +149,7 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
   }
 }
 
+template <uint32_t F>
 __global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp, PathSoA s, WaveParams wp, int cur) {
   __shared__ uint32_t off[kKinds + 1];
   if (threadIdx.x == 0) {
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp,
         h.sh.t = h.t;
       }
       Surface surf;
-      finalize_hit(sc, r, h, ctx, surf);
+      finalize_hit<F>(sc, r, h, ctx, surf);
       const rg_material m = sc.materials[surf.material];
       if (m.kind == RG_MAT_LIGHT) {
         L = C3f{L.r + beta.r * m.albedo[0], L.g + beta.g * m.albedo[1], L.b + beta.b * m.albedo[2]};
@@ -223,8 +224,9 @@ __global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp,
   }
 }
 
-// Per-pixel sums in the megakernel's order: sequential over samples for
-// spp <= 256; for larger spp, 256 strided partial sums added in thread order.
+// Per-pixel sums in the megakernel's canonical order: samples 0..spp-1 in
+// turn for spp <= 32; for larger spp, lane partials (samples l, l+32, ...)
+// added for l = 0..31 in turn.
 __global__ void __launch_bounds__(kWfBlock) k_accumulate(FrameParams fp, PathSoA s, WaveParams wp) {
   const uint32_t spp = fp.spp;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < wp.n_pixels * 3; q += gridDim.x * blockDim.x) {
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(kWfBlock) k_accumulate(FrameParams fp, PathSoA
     const float* base = src + (size_t)lp * spp;
     float sum = 0.0f;
     double sumd = 0.0, sqd = 0.0;
-    if (spp <= 256) {
+    if (spp <= 32) {
       for (uint32_t k = 0; k < spp; ++k) {
         float v = base[k];
         sum = sum + v;
@@ -241,15 +243,17 @@ __global__ void __launch_bounds__(kWfBlock) k_accumulate(FrameParams fp, PathSoA
         sqd += (double)v * v;
       }
     } else {
-      for (uint32_t t = 0; t < 256; ++t) {
+      for (uint32_t l = 0; l < 32; ++l) {
         float part = 0.0f;
-        for (uint32_t k = t; k < spp; k += 256) {
+        double psq = 0.0;
+        for (uint32_t k = l; k < spp; k += 32) {
           float v = base[k];
           part = part + v;
-          sqd += (double)v * v;
+          psq += (double)v * v;
         }
         sum = sum + part;
         sumd += part;
+        sqd += psq;
       }
     }
     uint32_t pix = wp.first_pixel + lp;
@@ -301,6 +305,45 @@ int sm_count(int device) {
   return n > 0 ? n : 1;
 }
 
+// Runs every wave of one frame on the path arrays `s` (capacity `cap` slots).
+template <uint32_t F>
+cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathSoA& s, size_t cap, size_t pix_per_wave) {
+  const size_t spp = fp.spp;
+  const size_t n_pix = (size_t)fp.width * fp.height;
+  const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
+  const int grid = sm_count(h->device) * 8;
+  cudaStream_t st = h->stream;
+  cudaError_t e;
+  for (size_t first = 0; first < n_pix; first += pix_per_wave) {
+    WaveParams wp;
+    wp.first_pixel = (uint32_t)first;
+    wp.n_pixels = (uint32_t)std::min(pix_per_wave, n_pix - first);
+    wp.n_paths = (uint32_t)(wp.n_pixels * spp);
+    wp.capacity = (uint32_t)cap;
+    uint32_t gen_blocks = (uint32_t)std::min<size_t>((wp.n_paths + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
+    k_generate<<<gen_blocks, kWfBlock, 0, st>>>(fp, s, wp);
+    int cur = 0;
+    for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
+      if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+      if (counters) k_extend<F, true><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      else k_extend<F, false><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      cur ^= 1;
+    }
+    uint32_t acc_blocks = (uint32_t)std::min<size_t>((wp.n_pixels * 3 + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
+    k_accumulate<<<acc_blocks, kWfBlock, 0, st>>>(fp, s, wp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t run_frame(rg_renderer* h, const FrameParams& fp, const PathSoA& s, size_t cap, size_t pix_per_wave) {
+  if (h->gs.features == F_TRI) return run_waves<F_TRI>(h, fp, s, cap, pix_per_wave);
+  if (h->gs.features == F_SPHERE) return run_waves<F_SPHERE>(h, fp, s, cap, pix_per_wave);
+  return run_waves<F_ALL>(h, fp, s, cap, pix_per_wave);
+}
+
 }  // namespace
 
 // Default path budget per wave: 2^23 slots (about 700 MB of path state).
@@ -324,32 +367,7 @@ cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp) {
   }
   PathSoA s;
   carve((char*)h->wf.arena, h->wf.capacity, s);
-  const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
-  const int grid = sm_count(h->device) * 8;
-  cudaStream_t st = h->stream;
-  for (size_t first = 0; first < n_pix; first += pix_per_wave) {
-    WaveParams wp;
-    wp.first_pixel = (uint32_t)first;
-    wp.n_pixels = (uint32_t)std::min(pix_per_wave, n_pix - first);
-    wp.n_paths = (uint32_t)(wp.n_pixels * spp);
-    wp.capacity = (uint32_t)h->wf.capacity;
-    cudaError_t e;
-    uint32_t gen_blocks = (uint32_t)std::min<size_t>((wp.n_paths + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
-    k_generate<<<gen_blocks, kWfBlock, 0, st>>>(fp, s, wp);
-    int cur = 0;
-    for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
-      if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
-      if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-      if (counters) k_extend<true><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-      else k_extend<false><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-      k_shade<<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-      cur ^= 1;
-    }
-    uint32_t acc_blocks = (uint32_t)std::min<size_t>((wp.n_pixels * 3 + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
-    k_accumulate<<<acc_blocks, kWfBlock, 0, st>>>(fp, s, wp);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  return run_frame(h, fp, s, h->wf.capacity, pix_per_wave);
 }
 
 // ---------------------------------------------------------------------------
@@ -391,32 +409,7 @@ cudaError_t launch_wavefront_static(rg_renderer* h, const FrameParams& fp) {
   if (e != cudaSuccess) return e;
   PathSoA s;
   carve((char*)arena, cap, s);
-  const size_t pix_per_wave = std::min(cap / spp, n_pix);
-  const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
-  const int grid = sm_count(h->device) * 8;
-  cudaStream_t st = h->stream;
-  for (size_t first = 0; first < n_pix; first += pix_per_wave) {
-    WaveParams wp;
-    wp.first_pixel = (uint32_t)first;
-    wp.n_pixels = (uint32_t)std::min(pix_per_wave, n_pix - first);
-    wp.n_paths = (uint32_t)(wp.n_pixels * spp);
-    wp.capacity = (uint32_t)cap;
-    uint32_t gen_blocks = (uint32_t)std::min<size_t>((wp.n_paths + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
-    k_generate<<<gen_blocks, kWfBlock, 0, st>>>(fp, s, wp);
-    int cur = 0;
-    for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
-      if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
-      if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-      if (counters) k_extend<true><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-      else k_extend<false><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-      k_shade<<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-      cur ^= 1;
-    }
-    uint32_t acc_blocks = (uint32_t)std::min<size_t>((wp.n_pixels * 3 + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
-    k_accumulate<<<acc_blocks, kWfBlock, 0, st>>>(fp, s, wp);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  return run_frame(h, fp, s, cap, std::min(cap / spp, n_pix));
 }
 
 }  // namespace rg

@@ -188,7 +188,11 @@ def test_wavefront_equals_megakernel(case):
     np.testing.assert_array_equal(a[1][0], b[1][0])
     np.testing.assert_array_equal(a[1][1], b[1][1])
     assert a[2].rays == b[2].rays
-    assert a[2].node_visits == b[2].node_visits and a[2].prim_tests == b[2].prim_tests
+    # Node and primitive counts depend slightly on which rays share a warp (the
+    # traversal postpones leaves until every lane holds one, which changes when
+    # the closest distance shrinks and so how many far nodes are culled).
+    assert abs(a[2].node_visits - b[2].node_visits) <= 0.01 * a[2].node_visits
+    assert abs(a[2].prim_tests - b[2].prim_tests) <= 0.01 * a[2].prim_tests
 
 
 def test_wavefront_small_waves():
