@@ -313,6 +313,33 @@ rg_status rg_frame_moments(rg_handle h, float* mean, float* variance);
 rg_status rg_query_rays(rg_handle h, uint32_t n, const float* origins, const float* dirs,
                         const float* tmin, const float* tmax, const float* volume_u, rg_hit* out);
 
+/* ------------------------------------------------------------------------ */
+/* Differentiation (no reference counterpart: the adjoint of render())        */
+/* ------------------------------------------------------------------------ */
+
+/* Gradient outputs of rg_backward (host arrays; NULL entries are skipped). */
+typedef struct rg_gradients {
+    float* albedo;     /* n_materials x 3: d loss / d material albedo (isotropic media included) */
+    float* emission;   /* n_materials x 3: d loss / d emissive radiance of light materials */
+    float* density;    /* n_volumes: d loss / d VolumetricObject::density (score-function estimator) */
+    double loss;       /* with a target: sum over pixels and channels of (I - target)^2; else 0 */
+} rg_gradients;
+
+/* Replaces material albedos (emissive radiance for lights), n_materials x 3,
+ * and media densities, n_volumes, without rebuilding the BVH. NULL leaves a
+ * group unchanged. Clears the accumulation, as set_scene does. */
+rg_status rg_set_parameters(rg_handle h, const float* albedo, const float* density);
+
+/* Adjoint of one frame by path-replay backpropagation: the frame `seed`
+ * renders image I (mean of `samples` paths per pixel, [x][y][rgb]). With
+ * `target_rgb` (host, width*height*3) the loss is sum (I - target)^2, I is
+ * rendered on the device and the loss returned; otherwise `adjoint_rgb` (host)
+ * is dLoss/dI. Every path is re-traced from its random stream (memory stays
+ * O(pixels)); gradients are returned for albedos, emissions and media
+ * densities. Supports ray_depth <= 16 and at most 4 media. The accumulation
+ * buffer is not touched. */
+rg_status rg_backward(rg_handle h, uint64_t seed, const float* adjoint_rgb, const float* target_rgb, rg_gradients* out);
+
 /* Path slots of the fixed device array used by rg_render_static_scratch
  * (31 x 4 bytes each: about 8 MB, held by every device that loads the library). */
 #define RG_STATIC_WAVE_PATHS 65536u

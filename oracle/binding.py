@@ -100,3 +100,34 @@ def render(flat, camera, opts, seed=0, frames=1, policy=POLICY_REF_F64, gpu_samp
 
 def hardware_threads() -> int:
     return int(lib().orc_hardware_threads())
+
+
+def backward(flat, camera, opts, seed, target=None, adjoint=None, policy=POLICY_REF_F64, threads=0):
+    """Path-replay adjoint on the CPU. Returns dict(loss, albedo, emission, density)."""
+    L = lib()
+    if not hasattr(L, "_bw_bound"):
+        fp, dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
+        L.orc_backward.argtypes = [C.POINTER(A.rg_scene_desc), C.POINTER(A.rg_camera), C.POINTER(A.rg_render_opts),
+                                   C.c_uint64, C.c_int, C.c_int, fp, fp, dp, dp, dp, dp]
+        L.orc_backward.restype = C.c_int
+        L._bw_bound = True
+    nm, nv = flat.desc.n_materials, flat.desc.n_volumes
+    ga, ge, gd = np.zeros(nm * 3), np.zeros(nm * 3), np.zeros(max(nv, 1))
+    loss = C.c_double(0.0)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    t = np.ascontiguousarray(target, np.float32) if target is not None else None
+    a = np.ascontiguousarray(adjoint, np.float32) if adjoint is not None else None
+    st = L.orc_backward(C.byref(flat.desc), C.byref(camera.to_c()), C.byref(opts.to_c()), int(seed), int(policy),
+                        int(threads), fp(t), fp(a), dp(ga), dp(ge), dp(gd), C.byref(loss))
+    assert st == 0, st
+    return {"loss": loss.value, "albedo": ga.reshape(nm, 3), "emission": ge.reshape(nm, 3), "density": gd[:nv]}
+
+
+def set_albedo(flat, m, c, value):
+    """Sets one albedo channel of material m in a flattened scene (in place)."""
+    flat.c_materials[m].albedo[c] = value
+
+
+def set_density(flat, v, value):
+    flat.c_volumes[v].density = value

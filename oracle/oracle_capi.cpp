@@ -95,9 +95,76 @@ int render_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_op
   return RG_OK;
 }
 
+template <class P>
+int backward_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_opts* opts, uint64_t seed, int threads,
+                  const float* target, const float* adjoint, double* g_alb, double* g_em, double* g_den, double* loss) {
+  Viewport vp;
+  if (!calculate_viewport(*cam, vp)) return RG_INVALID_CAMERA;
+  const uint32_t W = opts->width, H = opts->height;
+  const size_t n3 = (size_t)W * H * 3;
+  std::vector<double> delta(n3, 0.0);
+  double l = 0.0;
+  if (target) {
+    std::vector<double> img(n3);
+    int st = render_impl<P>(d, cam, opts, seed, 1, 1, threads, img.data(), nullptr, nullptr);
+    if (st != RG_OK) return st;
+    for (size_t i = 0; i < n3; ++i) {
+      double e = img[i] - (double)target[i];
+      delta[i] = 2.0 * e;
+      l += e * e;
+    }
+  } else {
+    for (size_t i = 0; i < n3; ++i) delta[i] = adjoint[i];
+  }
+  Scene<P> sc;
+  sc.load(*d, Options{});
+  RenderParams rp{W, H, opts->samples, opts->ray_depth, seed};
+  Renderer<P> R(sc, vp, rp);
+  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  const size_t nm = sc.materials.size();
+  std::vector<typename Renderer<P>::Grad> grads(threads);
+  for (auto& g : grads) { g.alb.assign(nm * 3, 0.0); g.em.assign(nm * 3, 0.0); g.den.assign(sc.nv, 0.0); }
+  std::atomic<uint32_t> next_row{0};
+  auto work = [&](int t) {
+    for (;;) {
+      uint32_t y = next_row.fetch_add(1);
+      if (y >= H) break;
+      for (uint32_t x = 0; x < W; ++x) {
+        const double* dl = delta.data() + ((size_t)x * H + y) * 3;
+        for (uint32_t s = 0; s < opts->samples; ++s) R.adjoint_sample(x, y, s, dl, grads[t]);
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& t : pool) t.join();
+  for (size_t i = 0; i < nm * 3; ++i) {
+    g_alb[i] = 0.0;
+    g_em[i] = 0.0;
+    for (auto& g : grads) { g_alb[i] += g.alb[i]; g_em[i] += g.em[i]; }
+  }
+  for (uint32_t v = 0; v < sc.nv; ++v) {
+    g_den[v] = 0.0;
+    for (auto& g : grads) g_den[v] += g.den[v];
+  }
+  if (loss) *loss = l;
+  return RG_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Path-replay adjoint on the CPU (device sampler assignment). policy 0 = f64,
+// 1 = f32. With `target` the loss is sum (I - target)^2 for the frame `seed`;
+// otherwise `adjoint` is dLoss/dI. Gradients in double.
+int orc_backward(const rg_scene_desc* d, const rg_camera* cam, const rg_render_opts* opts, uint64_t seed, int policy,
+                 int threads, const float* target, const float* adjoint, double* g_alb, double* g_em, double* g_den,
+                 double* loss) {
+  if (policy == 0) return backward_impl<RefF64>(d, cam, opts, seed, threads, target, adjoint, g_alb, g_em, g_den, loss);
+  return backward_impl<GpuF32>(d, cam, opts, seed, threads, target, adjoint, g_alb, g_em, g_den, loss);
+}
 
 // Philox4x32-10 known-answer access.
 void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {

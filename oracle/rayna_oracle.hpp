@@ -1182,6 +1182,109 @@ template <class P> struct Renderer {
     return Ray<P>::make(rpos, ps - rpos);
   }
 
+  // Gradient accumulators of the adjoint (double).
+  struct Grad {
+    std::vector<double> alb, em, den;
+  };
+
+  // Free-flight scores of every medium on one segment ending at t_final.
+  void medium_scores(const Ray<P>& ray, T t_final, int winner, std::vector<double>& score) const {
+    score.assign(sc.nv, 0.0);
+    for (uint32_t v = 0; v < sc.nv; ++v) {
+      Hit<T> tmp;
+      if (!sc.boundary_hit(sc.volumes[v], ray, Interval<T>::full(), tmp)) continue;
+      T enter = std::fmax(tmp.dist, T(1e-3));
+      if (!sc.boundary_hit(sc.volumes[v], ray, Interval<T>::from(enter + T(0.001)), tmp)) continue;
+      if ((int)v == winner) {
+        score[v] = 1.0 / (double)sc.volumes[v].density - ((double)t_final - (double)enter);
+      } else {
+        double l = (double)std::fmin(tmp.dist, t_final) - (double)enter;
+        score[v] = l > 0.0 ? -l : 0.0;
+      }
+    }
+  }
+
+  // Path-replay adjoint of one sample (device sampler assignment): the same
+  // estimator as the device's replay kernel, accumulated in double.
+  void adjoint_sample(uint32_t x, uint32_t y, uint32_t s, const double* delta, Grad& g) const {
+    const double inv = 1.0 / (double)rp.spp;
+    const double d[3] = {delta[0] * inv, delta[1] * inv, delta[2] * inv};
+    uint32_t dd = (uint32_t)std::sqrt((double)rp.spp);
+    while ((dd + 1) * (dd + 1) <= rp.spp) ++dd;
+    while (dd * dd > rp.spp) --dd;
+    PathRng rng(true, rp.seed, y * rp.width + x, s);
+    U4 b = rng.block(0xFFFFFFFFu, kPurposeCamera);
+    T jx = (T)u01f(b.v[0]) - T(0.5), jy = (T)u01f(b.v[1]) - T(0.5);
+    T lr = std::sqrt((T)u01f(b.v[2])), ph = T(2 * M_PI) * (T)u01f(b.v[3]);
+    T fx, fy;
+    if (s < dd * dd) {
+      T dinv = T(1) / (T)dd;
+      fx = ((T)x + jx * dinv) + (T)(s % dd) * dinv;
+      fy = ((T)y + jy * dinv) + (T)(s / dd) * dinv;
+    } else {
+      fx = (T)x + jx;
+      fy = (T)y + jy;
+    }
+    Ray<P> ray = camera_ray(fx, fy, lr * std::cos(ph), lr * std::sin(ph));
+    struct Vtx { uint32_t mat; bool light, albdep; double g, beta[3]; std::vector<double> score; };
+    std::vector<Vtx> vs;
+    double bt[3] = {1, 1, 1};
+    bool escaped = false;
+    C3 sky{0, 0, 0};
+    std::vector<double> esc_score;
+    for (uint32_t depth = 0; depth <= rp.ray_depth; ++depth) {
+      Hit<T> h;
+      Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
+      bool hit = sc.intersect(ray, iv, rng, depth, h);
+      int winner = -1;
+      if (hit && h.prim >= sc.prim_vol(0) && h.prim < sc.prim_vol(sc.nv)) winner = (int)(h.prim - sc.prim_vol(0));
+      std::vector<double> score;
+      medium_scores(ray, hit ? h.dist : std::numeric_limits<T>::infinity(), winner, score);
+      if (!hit) {
+        escaped = true;
+        sky = sky_colour<P>(sc.skybox, ray);
+        esc_score = score;
+        break;
+      }
+      const rg_material& m = sc.materials[h.material];
+      Vtx vx{h.material, m.kind == RG_MAT_LIGHT, false, 1.0, {bt[0], bt[1], bt[2]}, score};
+      vs.push_back(vx);
+      if (m.kind == RG_MAT_LIGHT || depth == rp.ray_depth) break;
+      V dir;
+      if (!scatter<P>(m, ray, h, rng, depth, dir)) break;
+      C3 a = attenuation<P>(m, ray, h);
+      if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) {
+        vs.back().albdep = true;
+      } else if (!(m.kind == RG_MAT_DIELECTRIC && h.front_face)) {
+        vs.back().albdep = true;
+        vs.back().g = std::exp(-(double)m.density * (double)Math<P>::length(h.pos_w - ray.pos));
+      }
+      bt[0] *= a.r; bt[1] *= a.g; bt[2] *= a.b;
+      ray = Ray<P>::make(h.pos_w, dir);
+    }
+    double c[3] = {0, 0, 0};
+    if (escaped) {
+      c[0] = sky.r; c[1] = sky.g; c[2] = sky.b;
+      for (uint32_t v = 0; v < sc.nv; ++v)
+        g.den[v] += esc_score[v] * (d[0] * bt[0] * c[0] + d[1] * bt[1] * c[1] + d[2] * bt[2] * c[2]);
+    }
+    for (int j = (int)vs.size() - 1; j >= 0; --j) {
+      const Vtx& vx = vs[j];
+      const rg_material& m = sc.materials[vx.mat];
+      if (vx.light) {
+        for (int k = 0; k < 3; ++k) g.em[3 * vx.mat + k] += d[k] * vx.beta[k];
+        for (int k = 0; k < 3; ++k) c[k] = m.albedo[k];
+      } else if (vx.albdep) {
+        for (int k = 0; k < 3; ++k) {
+          g.alb[3 * vx.mat + k] += d[k] * vx.beta[k] * vx.g * c[k];
+          c[k] *= (double)m.albedo[k] * vx.g;
+        }
+      }
+      for (uint32_t v = 0; v < sc.nv; ++v)
+        g.den[v] += vx.score[v] * (d[0] * vx.beta[0] * c[0] + d[1] * vx.beta[1] * c[1] + d[2] * vx.beta[2] * c[2]);
+    }
+  }
+
   // One sample of pixel (x, y); sample index s of spp.
   C3 sample(uint32_t x, uint32_t y, uint32_t s, bool gpu_sampling, SeqRng* msaa) const {
     uint32_t d = (uint32_t)std::sqrt((double)rp.spp);

@@ -98,6 +98,11 @@ class rg_tuning(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("reserved", C.c_uint32 * 7)]
 
 
+class rg_gradients(C.Structure):
+    _fields_ = [("albedo", C.POINTER(C.c_float)), ("emission", C.POINTER(C.c_float)),
+                ("density", C.POINTER(C.c_float)), ("loss", C.c_double)]
+
+
 class rg_hit(C.Structure):
     _fields_ = [("hit", C.c_uint32), ("prim", C.c_uint32), ("t", C.c_float), ("normal", C.c_float * 3),
                 ("ray_normal", C.c_float * 3), ("front_face", C.c_uint32), ("material", C.c_uint32),
@@ -130,6 +135,8 @@ SIGNATURES = {
     "rg_frame_moments": (C.c_int, [_P, _F, _F]),
     "rg_query_rays": (C.c_int, [_P, C.c_uint32, _F, _F, _F, _F, _F, C.POINTER(rg_hit)]),
     "rg_render_static_scratch": (C.c_int, [_P, C.c_uint64, _P, C.c_uint32, _P]),
+    "rg_set_parameters": (C.c_int, [_P, _F, _F]),
+    "rg_backward": (C.c_int, [_P, C.c_uint64, _F, _F, C.POINTER(rg_gradients)]),
 }
 
 _lib = None

@@ -1,0 +1,297 @@
+// adjoint.cu — gradients of an image loss by path-replay backpropagation
+// (Vicini, Speierer, Jakob, "Path Replay Backpropagation", SIGGRAPH 2021).
+//
+// The frame's image I (mean of spp path samples per pixel) is a function of
+// the material albedos and emissions and of the media densities. Given the
+// adjoint image dLoss/dI, each path is traced again from its counter-based
+// random stream (nothing of the forward pass is stored: memory stays
+// O(pixels)); the replay records the path's vertices in thread-local memory
+// and a backward loop over them accumulates
+//   dL/d albedo_m   += delta * beta_j * g_j * c_{j+1}   (vertex j of material m)
+//   dL/d emission_m += delta * beta_j                    (light vertex j)
+//   dL/d density_v  += sum_c delta_c * s_{j,v} * beta_j,c * c_j,c
+// where beta_j is the throughput before vertex j, g_j the attenuation factor
+// other than the albedo (Beer term), c_j = e_j + a_j * c_{j+1} the radiance
+// leaving vertex j (sky or 0 at the end), and s_{j,v} the score of the
+// free-flight decision of medium v on segment j: 1/density - (t - enter) for
+// the medium that scattered, -(min(exit, t) - enter) for one passed through.
+// Scattered directions do not depend on albedos, so the albedo and emission
+// gradients of a sample are exact; density gradients are the score-function
+// estimator of the derivative of the expectation. Geometric edges are out of
+// scope. Gradients are summed with warp-aggregated atomics
+// (__match_any_sync on the material or medium index).
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "kernels.h"
+#include "renderer_state.h"
+#include "trace.cuh"
+
+namespace rg {
+
+namespace {
+
+constexpr int kAdjBlock = 256;
+constexpr int kAdjMaxVertices = 17;  // ray_depth + 1
+constexpr int kAdjMaxVolumes = 4;
+
+struct AdjParams {
+  const float* adjoint;  // [x][y][rgb] dLoss/dI
+  float* g_albedo;       // n_mat x 3
+  float* g_emission;     // n_mat x 3
+  float* g_density;      // n_vol
+  uint32_t n_vol;
+};
+
+// Adds (v0, v1, v2) to base[3*key .. 3*key+2], one atomic per distinct key in the warp.
+__device__ __forceinline__ void warp_add3(float* base, int key, float v0, float v1, float v2) {
+  unsigned act = __activemask();
+  unsigned peers = __match_any_sync(act, key);
+  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+  for (unsigned m = peers; m; m &= m - 1) {
+    int src = __ffs(m) - 1;
+    s0 += __shfl_sync(peers, v0, src);
+    s1 += __shfl_sync(peers, v1, src);
+    s2 += __shfl_sync(peers, v2, src);
+  }
+  if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+    atomicAdd(base + 3 * key, s0);
+    atomicAdd(base + 3 * key + 1, s1);
+    atomicAdd(base + 3 * key + 2, s2);
+  }
+}
+
+__device__ __forceinline__ void warp_add1(float* base, int key, float v) {
+  unsigned act = __activemask();
+  unsigned peers = __match_any_sync(act, key);
+  float s = 0.0f;
+  for (unsigned m = peers; m; m &= m - 1) s += __shfl_sync(peers, v, __ffs(m) - 1);
+  if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(base + key, s);
+}
+
+// Free-flight scores of every medium for one ray segment that ended at
+// `t_final` (+inf when it escaped); `winner` is the medium that scattered, or -1.
+__device__ __forceinline__ void medium_scores(const GpuScene& sc, const Ray& r, float start, float t_final, int winner,
+                                              uint32_t n_vol, float* score) {
+  for (uint32_t v = 0; v < n_vol; ++v) {
+    score[v] = 0.0f;
+    const GpuPrim p = sc.prims[sc.vol_prim[v]];
+    uint32_t kind = prim_kind(p);
+    float d_enter, d_exit;
+    if (!boundary_t(p, kind, r, -CUDART_INF_F, CUDART_INF_F, d_enter)) continue;
+    float enter = fmaxf(d_enter, start);
+    if (!boundary_t(p, kind, r, enter + 0.001f, CUDART_INF_F, d_exit)) continue;
+    if ((int)v == winner) {
+      score[v] = __frcp_rn(sc.vol_density[v]) - (t_final - enter);
+    } else {
+      float l = fminf(d_exit, t_final) - enter;
+      score[v] = l > 0.0f ? -l : 0.0f;
+    }
+  }
+}
+
+template <uint32_t F>
+__device__ void replay_sample(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, uint32_t x, uint32_t y, uint32_t s,
+                              float d0, float d1, float d2) {
+  RngCtx ctx{fp.seed_lo, fp.seed_hi, y * fp.width + x, s, 0, nullptr};
+  Ray ray = camera_ray(fp, x, y, s, ctx);
+  int mat[kAdjMaxVertices];
+  bool light[kAdjMaxVertices], albdep[kAdjMaxVertices];
+  float g[kAdjMaxVertices][3], beta[kAdjMaxVertices + 1][3], score[kAdjMaxVertices + 1][kAdjMaxVolumes];
+  float b0 = 1.0f, b1 = 1.0f, b2 = 1.0f;
+  int K = 0;
+  bool escaped = false;
+  C3f sky{0.0f, 0.0f, 0.0f};
+  Counters cnt;
+  const uint32_t n_vol = ap.n_vol;
+  for (uint32_t depth = 0; depth <= fp.ray_depth; ++depth) {
+    ctx.depth = depth;
+    HitRec h;
+    bool hit = closest_hit<F, false>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
+    int winner = -1;
+    if (hit && h.sdf < 0 && (F & F_VOL)) {
+      uint32_t kind = prim_kind(sc.prims[h.prim]);
+      if (kind == PK_VOL_SPHERE || kind == PK_VOL_BOX) winner = (int)(prim_id(sc.prims[h.prim]) - sc.vol_base);
+    }
+    beta[K][0] = b0; beta[K][1] = b1; beta[K][2] = b2;
+    if (F & F_VOL) medium_scores(sc, ray, 1e-3f, hit ? h.t : CUDART_INF_F, winner, n_vol, score[K]);
+    if (!hit) {
+      escaped = true;
+      sky = sky_colour(sc.sky, ray.d);
+      break;
+    }
+    Surface surf;
+    finalize_hit<F>(sc, ray, h, ctx, surf);
+    const rg_material m = sc.materials[surf.material];
+    mat[K] = (int)surf.material;
+    light[K] = m.kind == RG_MAT_LIGHT;
+    albdep[K] = false;
+    g[K][0] = g[K][1] = g[K][2] = 1.0f;
+    ++K;
+    if (m.kind == RG_MAT_LIGHT || depth == fp.ray_depth) break;
+    V3 dir;
+    if (!scatter(m, ray, surf, ctx, dir)) break;
+    C3f a = attenuation(m, ray, surf);
+    if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) {
+      albdep[K - 1] = true;
+    } else if (!(m.kind == RG_MAT_DIELECTRIC && surf.front)) {
+      float e = expf(-m.density * length3(surf.pos - ray.o));
+      albdep[K - 1] = true;
+      g[K - 1][0] = g[K - 1][1] = g[K - 1][2] = e;
+    }
+    b0 = b0 * a.r; b1 = b1 * a.g; b2 = b2 * a.b;
+    ray = make_ray(surf.pos, dir);
+  }
+  // Backward over the vertices.
+  float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+  if (escaped) {
+    c0 = sky.r; c1 = sky.g; c2 = sky.b;
+    if (F & F_VOL)
+      for (uint32_t v = 0; v < n_vol; ++v) {
+        float sv = score[K][v];
+        float gv = sv * (d0 * beta[K][0] * c0 + d1 * beta[K][1] * c1 + d2 * beta[K][2] * c2);
+        if (gv != 0.0f) warp_add1(ap.g_density, (int)v, gv);
+      }
+  }
+  for (int j = K - 1; j >= 0; --j) {
+    const int m = mat[j];
+    const rg_material mm = sc.materials[m];
+    if (light[j]) {
+      warp_add3(ap.g_emission, m, d0 * beta[j][0], d1 * beta[j][1], d2 * beta[j][2]);
+      c0 = mm.albedo[0]; c1 = mm.albedo[1]; c2 = mm.albedo[2];
+    } else {
+      if (albdep[j]) {
+        warp_add3(ap.g_albedo, m, d0 * beta[j][0] * g[j][0] * c0, d1 * beta[j][1] * g[j][1] * c1,
+                  d2 * beta[j][2] * g[j][2] * c2);
+        c0 = c0 * (mm.albedo[0] * g[j][0]);
+        c1 = c1 * (mm.albedo[1] * g[j][1]);
+        c2 = c2 * (mm.albedo[2] * g[j][2]);
+      }
+      // a vertex that does not depend on the albedo (dielectric entry) passes c on unchanged
+    }
+    if (F & F_VOL)
+      for (uint32_t v = 0; v < n_vol; ++v) {
+        float sv = score[j][v];
+        float gv = sv * (d0 * beta[j][0] * c0 + d1 * beta[j][1] * c1 + d2 * beta[j][2] * c2);
+        if (gv != 0.0f) warp_add1(ap.g_density, (int)v, gv);
+      }
+  }
+}
+
+template <uint32_t F>
+__global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_pix) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = blockIdx.x * (kAdjBlock / 32) + (threadIdx.x >> 5);
+  const uint32_t spp = fp.spp;
+  const float inv = 1.0f / (float)spp;
+  if (spp <= 32) {
+    const uint32_t ppw = 32 / spp;
+    const uint32_t lp = lane / spp, s = lane % spp;
+    const uint32_t pix = warp * ppw + lp;
+    if (lp < ppw && pix < n_pix) {
+      uint32_t x = pix % fp.width, y = pix / fp.width;
+      size_t idx = ((size_t)x * fp.height + y) * 3;
+      replay_sample<F>(sc, fp, ap, x, y, s, ap.adjoint[idx] * inv, ap.adjoint[idx + 1] * inv, ap.adjoint[idx + 2] * inv);
+    }
+  } else {
+    const uint32_t pix = warp;
+    if (pix < n_pix) {
+      uint32_t x = pix % fp.width, y = pix / fp.width;
+      size_t idx = ((size_t)x * fp.height + y) * 3;
+      float d0 = ap.adjoint[idx] * inv, d1 = ap.adjoint[idx + 1] * inv, d2 = ap.adjoint[idx + 2] * inv;
+      for (uint32_t s = lane; s < spp; s += 32) replay_sample<F>(sc, fp, ap, x, y, s, d0, d1, d2);
+    }
+  }
+}
+
+// L2 loss against a target: adjoint = 2 (I - T), loss = sum (I - T)^2.
+__global__ void k_l2_adjoint(const float* image, const float* target, float* adjoint, size_t n, double* loss) {
+  double acc = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float d = image[i] - target[i];
+    adjoint[i] = 2.0f * d;
+    acc += (double)d * d;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc);
+}
+
+template <uint32_t F>
+void launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, cudaStream_t st) {
+  const uint32_t n_pix = fp.width * fp.height;
+  const uint32_t ppw = fp.spp <= 32 ? 32 / fp.spp : 1u;
+  const uint32_t warps = (n_pix + ppw - 1) / ppw;
+  const uint32_t blocks = (warps + kAdjBlock / 32 - 1) / (kAdjBlock / 32);
+  k_replay<F><<<blocks, kAdjBlock, 0, st>>>(sc, fp, ap, n_pix);
+}
+
+}  // namespace
+
+rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, const float* target, rg_gradients* out) {
+  const uint32_t w = h->opts.width, hh = h->opts.height;
+  const size_t npx3 = (size_t)w * hh * 3;
+  const uint32_t n_mat = (uint32_t)h->host.materials.size(), n_vol = h->host.nv;
+  if (h->opts.ray_depth + 1 > (uint32_t)kAdjMaxVertices)
+    return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward supports ray_depth <= 16");
+  if (n_vol > (uint32_t)kAdjMaxVolumes) return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward supports at most 4 media");
+  cudaStream_t st = h->stream;
+  // Device scratch of the adjoint: image, target/adjoint image, gradients, loss.
+  size_t need = (2 * npx3 + 2 * (size_t)n_mat * 3 + n_vol + 4) * sizeof(float) + sizeof(double) + 512;
+  if (h->adj_bytes < need) {
+    if (h->d_adj) cudaFree(h->d_adj);
+    h->d_adj = nullptr;
+    h->adj_bytes = 0;
+    cudaError_t e = cudaMalloc(&h->d_adj, need);
+    if (e != cudaSuccess) { cudaGetLastError(); return set_error(h, RG_OOM, "rg_backward: device scratch"); }
+    h->adj_bytes = need;
+  }
+  char* p = (char*)h->d_adj;
+  double* d_loss = (double*)p; p += 256;
+  float* d_image = (float*)p; p += npx3 * sizeof(float);
+  float* d_adjoint = (float*)p; p += npx3 * sizeof(float);
+  float* d_galb = (float*)p; p += (size_t)n_mat * 3 * sizeof(float);
+  float* d_gem = (float*)p; p += (size_t)n_mat * 3 * sizeof(float);
+  float* d_gden = (float*)p;
+  cudaError_t e;
+  auto cuda_err = [&](cudaError_t err) { cudaGetLastError(); return set_error(h, RG_CUDA_ERROR, cudaGetErrorString(err)); };
+  if ((e = cudaMemsetAsync(h->d_adj, 0, need, st)) != cudaSuccess) return cuda_err(e);
+  FrameParams fp;
+  fill_frame_params(h, seed, fp);
+  if (target) {
+    // Forward frame into a scratch image (the accumulation buffer is untouched).
+    FrameParams ff = fp;
+    ff.accum = d_adjoint;  // used as a zeroed running-sum scratch, overwritten below
+    ff.out = nullptr;
+    ff.frame_mean = d_image;
+    ff.frame_var = nullptr;
+    ff.accum_count = 1;
+    if ((e = launch_megakernel(h->gs, ff, false, st)) != cudaSuccess) return cuda_err(e);
+    if ((e = cudaMemcpyAsync(d_adjoint, target, npx3 * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      return cuda_err(e);
+    k_l2_adjoint<<<1024, 256, 0, st>>>(d_image, d_adjoint, d_adjoint, npx3, d_loss);
+  } else {
+    if ((e = cudaMemcpyAsync(d_adjoint, adjoint, npx3 * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      return cuda_err(e);
+  }
+  AdjParams ap{d_adjoint, d_galb, d_gem, d_gden, n_vol};
+  if (h->gs.features == F_SPHERE) launch_replay<F_SPHERE>(h->gs, fp, ap, st);
+  else if (h->gs.features == F_TRI) launch_replay<F_TRI>(h->gs, fp, ap, st);
+  else launch_replay<F_ALL>(h->gs, fp, ap, st);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e);
+  double loss = 0.0;
+  if (out->albedo && (e = cudaMemcpyAsync(out->albedo, d_galb, (size_t)n_mat * 3 * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return cuda_err(e);
+  if (out->emission && (e = cudaMemcpyAsync(out->emission, d_gem, (size_t)n_mat * 3 * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return cuda_err(e);
+  if (out->density && n_vol && (e = cudaMemcpyAsync(out->density, d_gden, n_vol * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return cuda_err(e);
+  if ((e = cudaMemcpyAsync(&loss, d_loss, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return cuda_err(e);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e);
+  out->loss = loss;
+  return RG_OK;
+}
+
+}  // namespace rg

@@ -90,6 +90,8 @@ struct GpuScene {
   uint32_t vol_base;   // global id of volume 0
   uint32_t n_tris;
   uint32_t features;   // F_* bits of the kernel variant to launch (primitive kinds present)
+  const float* vol_density;   // per medium: VolumetricObject::density
+  const uint32_t* vol_prim;   // per medium: its position in `prims`
 };
 
 // Device error bits (rg_render_stats::error_flags).

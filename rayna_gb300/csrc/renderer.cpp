@@ -295,6 +295,11 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
   hs.max_depth = bvh.max_depth;
   hs.prims.resize(nbounded);
   for (uint32_t i = 0; i < nbounded; ++i) hs.prims[i] = prims[bvh.order[i]];
+  hs.vol_prim.assign(hs.nv, 0);
+  for (uint32_t i = 0; i < nbounded; ++i)
+    if (bvh.order[i] >= hs.vol_base && bvh.order[i] < hs.vol_base + hs.nv) hs.vol_prim[bvh.order[i] - hs.vol_base] = i;
+  hs.vol_density.resize(hs.nv);
+  for (uint32_t i = 0; i < hs.nv; ++i) hs.vol_density[i] = d.volumes[i].density;
   if (hs.max_depth >= kMaxBuildDepth)
     return fail(h, RG_INVALID_ARG, "BVH depth %d exceeds the traversal stack", hs.max_depth);
   return RG_OK;
@@ -308,6 +313,8 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   if ((st = upload(h, ds.tri_normals, hs.tri_normals.data(), hs.tri_normals.size(), "upload normals")) != RG_OK) return st;
   if ((st = upload(h, ds.materials, hs.materials.data(), hs.materials.size(), "upload materials")) != RG_OK) return st;
   if ((st = upload(h, ds.sdfs, hs.sdfs.data(), hs.sdfs.size(), "upload sdfs")) != RG_OK) return st;
+  if ((st = upload(h, ds.vol_density, hs.vol_density.data(), hs.vol_density.size(), "upload media")) != RG_OK) return st;
+  if ((st = upload(h, ds.vol_prim, hs.vol_prim.data(), hs.vol_prim.size(), "upload media")) != RG_OK) return st;
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "upload scene");
   GpuScene& g = h->gs;
   g.nodes = ds.nodes;
@@ -315,6 +322,8 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.tri_normals = ds.tri_normals;
   g.materials = ds.materials;
   g.sdfs = ds.sdfs;
+  g.vol_density = ds.vol_density;
+  g.vol_prim = ds.vol_prim;
   g.n_nodes = (uint32_t)hs.nodes.size();
   g.n_prims = (uint32_t)hs.prims.size();
   g.n_sdfs = hs.nsdf;
@@ -332,6 +341,7 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
 
 void free_scene(DeviceScene& ds) {
   dfree(ds.nodes); dfree(ds.prims); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
+  dfree(ds.vol_density); dfree(ds.vol_prim);
 }
 
 rg_status set_error(rg_renderer* h, rg_status st, const char* msg) { return fail(h, st, "%s", msg); }
@@ -443,6 +453,7 @@ rg_status rg_destroy(rg_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_scene(h->dev);
   free_extra(h);
+  if (h->d_adj) cudaFree(h->d_adj);
   dfree(h->d_accum); dfree(h->d_out); dfree(h->d_fmean); dfree(h->d_fvar);
   dfree(h->d_counters); dfree(h->d_err);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -521,6 +532,48 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene) {
   h->have_scene = true;
   on_scene_changed(h);
   return rg_clear_accumulation(h);
+}
+
+rg_status rg_set_parameters(rg_handle h, const float* albedo, const float* density) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  cudaSetDevice(h->device);
+  HostScene& hs = h->host;
+  if (albedo) {
+    for (size_t i = 0; i < hs.materials.size() * 3; ++i)
+      if (!std::isfinite(albedo[i])) return fail(h, RG_INVALID_ARG, "albedo %zu is not finite", i / 3);
+    for (size_t i = 0; i < hs.materials.size(); ++i)
+      for (int c = 0; c < 3; ++c) hs.materials[i].albedo[c] = albedo[3 * i + c];
+    RG_CUDA(h, cudaMemcpyAsync(h->dev.materials, hs.materials.data(), hs.materials.size() * sizeof(rg_material),
+                               cudaMemcpyHostToDevice, h->stream), "rg_set_parameters");
+  }
+  if (density) {
+    for (uint32_t v = 0; v < hs.nv; ++v)
+      if (!std::isfinite(density[v]) || density[v] < 0.0f) return fail(h, RG_INVALID_ARG, "density %u is invalid", v);
+    for (uint32_t v = 0; v < hs.nv; ++v) {
+      hs.vol_density[v] = density[v];
+      hs.volumes[v].density = density[v];
+      GpuPrim& p = hs.prims[hs.vol_prim[v]];
+      float nid = -1.0f / density[v];
+      uint32_t kind = float_bits(p.a.w) >> kKindShift;
+      if (kind == PK_VOL_SPHERE) p.b.z = nid;
+      else p.c.w = nid;
+      RG_CUDA(h, cudaMemcpyAsync(h->dev.prims + hs.vol_prim[v], &p, sizeof(GpuPrim), cudaMemcpyHostToDevice, h->stream),
+              "rg_set_parameters");
+    }
+    if (hs.nv)
+      RG_CUDA(h, cudaMemcpyAsync(h->dev.vol_density, hs.vol_density.data(), hs.nv * sizeof(float), cudaMemcpyHostToDevice,
+                                 h->stream), "rg_set_parameters");
+  }
+  RG_CUDA(h, cudaStreamSynchronize(h->stream), "rg_set_parameters");
+  return rg_clear_accumulation(h);
+}
+
+rg_status rg_backward(rg_handle h, uint64_t seed, const float* adjoint_rgb, const float* target_rgb, rg_gradients* out) {
+  if (!h || !out) return fail(h, RG_INVALID_ARG, "rg_backward: NULL argument");
+  if (!adjoint_rgb && !target_rgb) return fail(h, RG_INVALID_ARG, "rg_backward: give an adjoint image or a target");
+  cudaSetDevice(h->device);
+  if (!h->cam_ok) return fail(h, RG_INVALID_CAMERA, "camera viewport could not be calculated");
+  return backward_device(h, seed, adjoint_rgb, target_rgb, out);
 }
 
 rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {

@@ -28,6 +28,8 @@ struct HostScene {
   std::vector<rg_material> materials;
   std::vector<rg_volume> volumes;
   std::vector<GpuSdf> sdfs;
+  std::vector<float> vol_density;      // per medium
+  std::vector<uint32_t> vol_prim;      // per medium: position in `prims`
 };
 
 struct DeviceScene {
@@ -36,6 +38,8 @@ struct DeviceScene {
   float* tri_normals = nullptr;
   rg_material* materials = nullptr;
   GpuSdf* sdfs = nullptr;
+  float* vol_density = nullptr;
+  uint32_t* vol_prim = nullptr;
 };
 
 // Wavefront queues (allocated on first use, sized by the path budget).
@@ -80,6 +84,9 @@ struct rg_renderer {
 
   rg::WavefrontState wf;
   size_t wf_paths = 0;        // wavefront path slots per wave (0: library default)
+
+  void* d_adj = nullptr;      // adjoint scratch (image, adjoint image, gradients)
+  size_t adj_bytes = 0;
 };
 
 namespace rg {
@@ -89,6 +96,9 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
 void fill_frame_params(rg_renderer* h, uint64_t seed, FrameParams& fp);
 rg_status ensure_frame_buffers(rg_renderer* h);
 rg_status set_error(rg_renderer* h, rg_status st, const char* msg);
+
+// Defined in adjoint.cu
+rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, const float* target, rg_gradients* out);
 
 // Defined in wavefront.cu
 cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp);

@@ -240,6 +240,45 @@ def sdf_volumes(seed: int = 0, width: int = 1280, height: int = 720, spp: int = 
     return scene, cam, opts
 
 
+def adjoint_scene(n_spheres: int = 1000, seed: int = 0, ground_truth: bool = True, width: int = 512,
+                  height: int = 512, spp: int = 16, ray_depth: int = 8, medium_density: float | None = None):
+    """Returns (scene, camera, opts) of the differentiable-rendering workload.
+
+    The random-spheres layout with `n_spheres` Lambertian spheres, each with
+    its own material (one RGB albedo parameter per sphere: ground, three r=1
+    spheres, and r=0.2 spheres on a grid), plus one constant-density medium
+    (a sphere of radius 1 at (0, 1, 0) with an isotropic material). With
+    `ground_truth` the albedos are U[0.05, 0.95] and the medium has density
+    0.8 and albedo (0.8, 0.6, 0.4); otherwise the albedos start at U[0.2, 0.8]
+    and the medium at density 0.4, albedo 0.5. Parameters: 3 x n_spheres
+    albedos + 3 medium albedos + 1 medium density.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    init = np.random.Generator(np.random.PCG64(seed + 7))
+
+    def albedo():
+        gt = tuple(0.05 + 0.9 * rng.random(3))
+        return gt if ground_truth else tuple(0.2 + 0.6 * init.random(3))
+
+    objs = [SimpleObject(SphereMesh((0.0, -1000.0, 0.0), 1000.0), LambertianMaterial(albedo()))]
+    for c in [(-4.0, 1.0, 0.0), (4.0, 1.0, 0.0), (0.0, 1.0, -3.0)]:
+        objs.append(SimpleObject(SphereMesh(c, 1.0), LambertianMaterial(albedo())))
+    n_small = max(0, n_spheres - 4)
+    side = int(math.ceil(math.sqrt(max(n_small, 1))))
+    for k in range(n_small):
+        a, b = divmod(k, side)
+        centre = (a - side / 2 + 0.9 * rng.random(), 0.2, b - side / 2 + 0.9 * rng.random())
+        objs.append(SimpleObject(SphereMesh(centre, 0.2), LambertianMaterial(albedo())))
+    if medium_density is None:
+        medium_density = 0.8 if ground_truth else 0.4
+    mat = IsotropicMaterial((0.8, 0.6, 0.4) if ground_truth else (0.5, 0.5, 0.5), 0.0)
+    objs.append(VolumetricObject(SphereMesh((0.0, 1.0, 0.0), 1.0), mat, medium_density))
+    scene = Scene(objects=objs, skybox=SimpleSkybox())
+    cam = look_at_camera((13.0, 2.0, 3.0), (0.0, 0.0, 0.0), 20.0, focus_dist=10.0)
+    opts = RenderOpts(width=width, height=height, samples=spp, ray_depth=ray_depth)
+    return scene, cam, opts
+
+
 def single_sphere(albedo, skybox=None):
     """The scene of rayna_engine/tests/simple_renders.rs:36-48: a Lambertian
     unit sphere at the origin under WhiteSkybox."""

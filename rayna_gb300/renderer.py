@@ -140,6 +140,59 @@ class Renderer:
         self._check(self._lib.rg_set_options(self._h, C.byref(options.to_c())))
         self._options = options
 
+    @property
+    def n_materials(self) -> int:
+        return int(self._flat.desc.n_materials)
+
+    @property
+    def n_volumes(self) -> int:
+        return int(self._flat.desc.n_volumes)
+
+    def set_parameters(self, albedo=None, density=None):
+        """Replaces material albedos (emissive radiance for lights), shape
+        (n_materials, 3), and media densities, shape (n_volumes,), without
+        rebuilding the BVH. Clears the accumulation."""
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        a = d = None
+        if albedo is not None:
+            a = np.ascontiguousarray(albedo, np.float32).reshape(self.n_materials, 3)
+        if density is not None:
+            d = np.ascontiguousarray(density, np.float32).reshape(self.n_volumes)
+        self._check(self._lib.rg_set_parameters(self._h, fp(a) if a is not None else None,
+                                                fp(d) if d is not None else None))
+
+    def backward(self, seed: int, target=None, adjoint=None):
+        """Adjoint of frame `seed` (rg_backward). With `target` (w, h, 3) the
+        loss is sum (I - target)^2; otherwise `adjoint` is dLoss/dI. Returns a
+        dict with 'loss', 'albedo' (n_materials, 3), 'emission' (n_materials, 3)
+        and 'density' (n_volumes,)."""
+        o = self._options
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        t = adj = None
+        if target is not None:
+            t = np.ascontiguousarray(target, np.float32).reshape(o.width, o.height, 3)
+        elif adjoint is not None:
+            adj = np.ascontiguousarray(adjoint, np.float32).reshape(o.width, o.height, 3)
+        else:
+            raise ValueError("give a target or an adjoint image")
+        ga = np.zeros((self.n_materials, 3), np.float32)
+        ge = np.zeros((self.n_materials, 3), np.float32)
+        gd = np.zeros(max(self.n_volumes, 1), np.float32)
+        g = A.rg_gradients()
+        g.albedo, g.emission, g.density = fp(ga), fp(ge), fp(gd)
+        self._check(self._lib.rg_backward(self._h, int(seed), fp(adj) if adj is not None else None,
+                                          fp(t) if t is not None else None, C.byref(g)))
+        return {"loss": g.loss, "albedo": ga, "emission": ge, "density": gd[: self.n_volumes]}
+
+    def frame(self, seed: int) -> np.ndarray:
+        """The image of frame `seed` alone (mean of its samples), leaving the
+        running accumulation where it was."""
+        sums, frames = self.get_accumulation()
+        self.render(seed=seed)
+        m, _ = self.frame_moments()
+        self.set_accumulation(sums, frames)
+        return m
+
     def set_wave_paths(self, n: int):
         """Wavefront path slots per wave (0: library default)."""
         t = A.rg_tuning()
