@@ -141,6 +141,53 @@ def cpu_baseline(name: str, threads: int, target_s: float = 15.0):
                       f"({ns / 1e6:.2f} M samples, {secs:.1f} s), f64 oracle, {threads} threads"}, secs
 
 
+def run_adjoint(iters: int = 5, stream=None):
+    """Differentiable-rendering workload: 1000 Lambertian spheres (3000 albedo
+    parameters) + one medium (3 albedo + 1 density), 512x512, forward and
+    backward at 16 spp, depth 8, L2 loss against a 1024-spp target of the
+    ground-truth parameters; Adam steps on the host. Returns timings."""
+    import torch
+
+    from rayna_gb300 import Renderer, presets
+    scene, cam, opts = presets.adjoint_scene(n_spheres=1000, ground_truth=False)
+    gt, _, _ = presets.adjoint_scene(n_spheres=1000, ground_truth=True)
+    s = stream.cuda_stream if stream is not None else None
+    topts = type(opts)(width=opts.width, height=opts.height, samples=1024, ray_depth=opts.ray_depth)
+    with Renderer.new_from(gt, cam, topts, 0, stream=s) as r:
+        target = r.frame(seed=1)
+    r = Renderer.new_from(scene, cam, opts, 0, stream=s)
+    p = np.array([[m.albedo[c] for c in range(3)] for m in r._flat.materials], np.float64)
+    dens = np.array([v.density for v in r._flat.volumes], np.float64)
+    theta = np.concatenate([p.ravel(), dens])
+    m1, m2 = np.zeros_like(theta), np.zeros_like(theta)
+    lr, b1, b2 = 0.02, 0.9, 0.999
+    fwd_ms, it_ms, losses = [], [], []
+    for k in range(iters + 2):
+        t0 = time.perf_counter()
+        r.render(seed=10_000 + k)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        g = r.backward(seed=20_000 + k, target=target)
+        grad = np.concatenate([g["albedo"].astype(np.float64).ravel(), g["density"].astype(np.float64)])
+        m1 = b1 * m1 + (1 - b1) * grad
+        m2 = b2 * m2 + (1 - b2) * grad * grad
+        theta = theta - lr * (m1 / (1 - b1 ** (k + 1))) / (np.sqrt(m2 / (1 - b2 ** (k + 1))) + 1e-8)
+        theta = np.clip(theta, 1e-3, None)
+        r.set_parameters(albedo=theta[:p.size].reshape(p.shape).astype(np.float32),
+                         density=theta[p.size:].astype(np.float32))
+        t2 = time.perf_counter()
+        if k >= 2:
+            fwd_ms.append((t1 - t0) * 1e3)
+            it_ms.append((t2 - t1) * 1e3)
+        losses.append(g["loss"])
+    r.close()
+    f, i = statistics.median(fwd_ms), statistics.median(it_ms)
+    return {"workload": "1000 spheres (3000 albedos) + 1 medium (3 albedo + density), 512x512, 16 spp, depth 8, "
+                        "L2 vs 1024-spp target, Adam",
+            "ms_per_iter": i, "forward_ms": f, "iter_over_forward": i / f, "iters": iters,
+            "loss_first": losses[0], "loss_last": losses[-1], "n_params": int(theta.size)}
+
+
 def run_reference(args, rank, world):
     from oracle import binding as ob
     name = args.workload
@@ -282,6 +329,8 @@ def run_gpu(args, rank, world):
         "gpu_launches": args.steps,
         "clocks": b["clocks"],
     }
+    if world == 1 and not args.no_adjoint:
+        line["adjoint"] = run_adjoint(stream=stream)
     if world == 1 and not args.no_cpu_baseline:
         from oracle import binding as ob
         cb, _ = cpu_baseline(args.workload, ob.hardware_threads(), target_s=args.ref_seconds)
@@ -305,6 +354,7 @@ def main():
     ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
