@@ -314,6 +314,45 @@ rg_status rg_query_rays(rg_handle h, uint32_t n, const float* origins, const flo
                         const float* tmin, const float* tmax, const float* volume_u, rg_hit* out);
 
 /* ------------------------------------------------------------------------ */
+/* Batched rendering (no reference counterpart: many Renderers at once)       */
+/* ------------------------------------------------------------------------ */
+
+typedef struct rg_batch* rg_batch_handle;
+
+/* Launch shape of the persistent batch kernel (what the autotuner sets). */
+typedef struct rg_batch_tuning {
+    uint32_t block;            /* threads per block, multiple of 32 in [64, 512]; 0 = 256 */
+    uint32_t blocks_per_sm;    /* blocks launched per SM; 0 = as many as fit */
+    uint32_t rounds_per_item;  /* warp rounds of pixels per work item taken from the queue; 0 = 4 */
+    uint32_t reserved[5];      /* must be 0 */
+} rg_batch_tuning;
+
+/* Creates a batch of `n` independent renders (scene, camera, options each,
+ * as rg_set_scene/rg_set_camera/rg_set_options take them). */
+rg_status rg_batch_create(const rg_device_opts* opts, uint32_t n, const rg_scene_desc* const* scenes,
+                          const rg_camera* cameras, const rg_render_opts* options, rg_batch_handle* out);
+rg_status rg_batch_destroy(rg_batch_handle b);
+rg_status rg_batch_last_error(rg_batch_handle b, char* buf, size_t len);
+rg_status rg_batch_set_tuning(rg_batch_handle b, const rg_batch_tuning* t);
+
+/* Adds one frame to every render of the batch in a single persistent launch:
+ * warps take (scene, tile) work items from one global queue until it is empty
+ * (work stealing by atomic counter). The frame's launch sequence is captured
+ * once as a CUDA graph and replayed. Render i uses the frame key
+ * splitmix64(seed + i). Waits for the device; stats cover the whole batch. */
+rg_status rg_batch_render(rg_batch_handle b, uint64_t seed, rg_render_stats* stats);
+
+/* The same frame as one megakernel launch per render, in sequence (the
+ * comparison form). Produces the same images as rg_batch_render. */
+rg_status rg_batch_render_sequential(rg_batch_handle b, uint64_t seed, rg_render_stats* stats);
+
+/* Running mean of render `index`, [x][y][rgb], host memory. */
+rg_status rg_batch_image(rg_batch_handle b, uint32_t index, float* out_rgb);
+
+/* Frame key rg_batch_render gives render `index` for `seed`. */
+uint64_t rg_batch_item_seed(uint64_t seed, uint32_t index);
+
+/* ------------------------------------------------------------------------ */
 /* Differentiation (no reference counterpart: the adjoint of render())        */
 /* ------------------------------------------------------------------------ */
 

@@ -103,6 +103,11 @@ class rg_gradients(C.Structure):
                 ("density", C.POINTER(C.c_float)), ("loss", C.c_double)]
 
 
+class rg_batch_tuning(C.Structure):
+    _fields_ = [("block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("rounds_per_item", C.c_uint32),
+                ("reserved", C.c_uint32 * 5)]
+
+
 class rg_hit(C.Structure):
     _fields_ = [("hit", C.c_uint32), ("prim", C.c_uint32), ("t", C.c_float), ("normal", C.c_float * 3),
                 ("ray_normal", C.c_float * 3), ("front_face", C.c_uint32), ("material", C.c_uint32),
@@ -136,6 +141,15 @@ SIGNATURES = {
     "rg_query_rays": (C.c_int, [_P, C.c_uint32, _F, _F, _F, _F, _F, C.POINTER(rg_hit)]),
     "rg_render_static_scratch": (C.c_int, [_P, C.c_uint64, _P, C.c_uint32, _P]),
     "rg_set_parameters": (C.c_int, [_P, _F, _F]),
+    "rg_batch_create": (C.c_int, [C.POINTER(rg_device_opts), C.c_uint32, C.POINTER(C.POINTER(rg_scene_desc)),
+                                  C.POINTER(rg_camera), C.POINTER(rg_render_opts), C.POINTER(_P)]),
+    "rg_batch_destroy": (C.c_int, [_P]),
+    "rg_batch_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
+    "rg_batch_set_tuning": (C.c_int, [_P, C.c_void_p]),
+    "rg_batch_render": (C.c_int, [_P, C.c_uint64, C.POINTER(rg_render_stats)]),
+    "rg_batch_render_sequential": (C.c_int, [_P, C.c_uint64, C.POINTER(rg_render_stats)]),
+    "rg_batch_image": (C.c_int, [_P, C.c_uint32, _F]),
+    "rg_batch_item_seed": (C.c_uint64, [C.c_uint64, C.c_uint32]),
     "rg_backward": (C.c_int, [_P, C.c_uint64, _F, _F, C.POINTER(rg_gradients)]),
 }
 

@@ -20,7 +20,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(ROOT, "_build", "rayna_gpu")
 LIB = os.path.join(OUT_DIR, "librayna_gpu.so")
 
-SOURCES = ["renderer.cpp", "bvh_build.cpp", "megakernel.cu", "wavefront.cu", "adjoint.cu"]
+SOURCES = ["renderer.cpp", "bvh_build.cpp", "megakernel.cu", "wavefront.cu", "adjoint.cu", "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1,0 +1,366 @@
+// batch.cu — many renders in one persistent launch.
+//
+// Every render of a batch is an ordinary handle (its own scene buffers,
+// camera, options and accumulation). A frame of the whole batch is one
+// launch of k_batch: as many blocks as fit on the SMs, whose warps take work
+// items from one global queue (an atomic counter) until it is empty. A work
+// item is `rounds_per_item` consecutive warp rounds (mega.cuh) of one render;
+// items of all renders are numbered one after another, so a warp finds its
+// render by a binary search over the prefix sums of item counts. Renders of
+// uneven size therefore share the GPU without a tail of idle SMs per render.
+//
+// The frame's launch sequence (parameter table upload, counter reset, kernel)
+// is captured once as a CUDA graph and replayed; the host only rewrites the
+// pinned parameter table (frame keys, accumulation counts) before each replay.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "mega.cuh"
+#include "renderer_state.h"
+
+namespace rg {
+
+struct BatchItemDev {
+  GpuScene sc;
+  FrameParams fp;
+};
+
+namespace {
+
+template <uint32_t F>
+__global__ void k_batch(const BatchItemDev* __restrict__ items, const uint32_t* __restrict__ prefix, uint32_t n_items,
+                        uint32_t total, uint32_t rounds_per_item, uint32_t* counter, unsigned long long* counters) {
+  const uint32_t lane = threadIdx.x & 31;
+  Counters cnt;
+  uint32_t segments = 0;
+  for (;;) {
+    uint32_t w = 0;
+    if (lane == 0) w = atomicAdd(counter, 1u);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= total) break;
+    uint32_t lo = 0, hi = n_items;  // largest lo with prefix[lo] <= w
+    while (hi - lo > 1) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (prefix[mid] <= w) lo = mid;
+      else hi = mid;
+    }
+    const GpuScene sc = items[lo].sc;
+    const FrameParams fp = items[lo].fp;
+    const uint32_t n_pix = fp.width * fp.height;
+    const uint32_t ppr = pixels_per_round(fp.spp);
+    const uint32_t round0 = (w - prefix[lo]) * rounds_per_item;
+    for (uint32_t r = 0; r < rounds_per_item; ++r) {
+      uint32_t first = (round0 + r) * ppr;
+      if (first >= n_pix) break;
+      mega_round<F, false>(sc, fp, first, n_pix, cnt, segments);
+    }
+  }
+  FrameParams f0;
+  f0.counters = counters;
+  flush_counters<false>(f0, cnt, segments);
+}
+
+uint64_t splitmix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+}  // namespace rg
+
+using namespace rg;
+
+struct rg_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<rg_renderer*> items;
+  std::string err;
+  BatchItemDev* d_items = nullptr;
+  BatchItemDev* h_items = nullptr;  // pinned
+  uint32_t* d_prefix = nullptr;
+  uint32_t* d_counter = nullptr;
+  unsigned long long* d_counters = nullptr;
+  uint32_t total_work = 0;
+  uint32_t features = 0;
+  rg_batch_tuning tuning{};
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+rg_status bfail(rg_batch* b, rg_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  return st;
+}
+
+rg_status bcuda(rg_batch* b, cudaError_t e, const char* what) {
+  cudaGetLastError();
+  return bfail(b, e == cudaErrorMemoryAllocation ? RG_OOM : RG_CUDA_ERROR, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define BCUDA(b, call, what)                                  \
+  do {                                                        \
+    cudaError_t e__ = (call);                                 \
+    if (e__ != cudaSuccess) return bcuda(b, e__, what);       \
+  } while (0)
+
+void drop_graph(rg_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+}
+
+// Work-item prefix sums for the current tuning.
+rg_status layout(rg_batch* b) {
+  const uint32_t rpi = b->tuning.rounds_per_item ? b->tuning.rounds_per_item : 4u;
+  std::vector<uint32_t> prefix(b->items.size() + 1, 0);
+  uint64_t acc = 0;
+  for (size_t i = 0; i < b->items.size(); ++i) {
+    const rg_render_opts& o = b->items[i]->opts;
+    uint64_t npix = (uint64_t)o.width * o.height;
+    uint64_t ppr = pixels_per_round(o.samples);
+    uint64_t rounds = (npix + ppr - 1) / ppr;
+    prefix[i] = (uint32_t)acc;
+    acc += (rounds + rpi - 1) / rpi;
+  }
+  if (acc >= 0xFFFFFFFFull) return bfail(b, RG_INVALID_ARG, "batch too large");
+  prefix[b->items.size()] = (uint32_t)acc;
+  b->total_work = (uint32_t)acc;
+  BCUDA(b, cudaMemcpy(b->d_prefix, prefix.data(), prefix.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "batch layout");
+  return RG_OK;
+}
+
+template <uint32_t F>
+cudaError_t launch_batch_kernel(rg_batch* b) {
+  const int block = b->tuning.block ? (int)b->tuning.block : 256;
+  int sms = 1, fit = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batch<F>, block, 0);
+  int per_sm = b->tuning.blocks_per_sm ? std::min<int>((int)b->tuning.blocks_per_sm, std::max(fit, 1)) : std::max(fit, 1);
+  const uint32_t rpi = b->tuning.rounds_per_item ? b->tuning.rounds_per_item : 4u;
+  k_batch<F><<<sms * per_sm, block, 0, b->stream>>>(b->d_items, b->d_prefix, (uint32_t)b->items.size(), b->total_work, rpi,
+                                                    b->d_counter, b->d_counters);
+  return cudaGetLastError();
+}
+
+cudaError_t enqueue_frame(rg_batch* b) {
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(b->d_items, b->h_items, b->items.size() * sizeof(BatchItemDev), cudaMemcpyHostToDevice,
+                           b->stream)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), b->stream)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(b->d_counters, 0, CNT_N * sizeof(unsigned long long), b->stream)) != cudaSuccess) return e;
+  if (b->features == F_TRI) return launch_batch_kernel<F_TRI>(b);
+  if (b->features == F_SPHERE) return launch_batch_kernel<F_SPHERE>(b);
+  return launch_batch_kernel<F_ALL>(b);
+}
+
+// Fills the pinned parameter table for frame `seed` (one frame per render).
+rg_status prepare_frame(rg_batch* b, uint64_t seed) {
+  for (size_t i = 0; i < b->items.size(); ++i) {
+    rg_renderer* h = b->items[i];
+    rg_status st = ensure_frame_buffers(h);
+    if (st != RG_OK) return bfail(b, st, "render %zu: %s", i, h->err.c_str());
+    h->frame_count += 1;
+    h->pixel_accum += 1;
+    FrameParams fp;
+    fill_frame_params(h, rg_batch_item_seed(seed, (uint32_t)i), fp);
+    fp.accum_count = h->pixel_accum;
+    fp.counters = b->d_counters;
+    b->h_items[i].sc = h->gs;
+    b->h_items[i].fp = fp;
+  }
+  return RG_OK;
+}
+
+rg_status finish_stats(rg_batch* b, rg_render_stats* stats, std::chrono::steady_clock::time_point t0) {
+  BCUDA(b, cudaStreamSynchronize(b->stream), "batch frame");
+  if (!stats) return RG_OK;
+  std::memset(stats, 0, sizeof(*stats));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+  unsigned long long c[CNT_N];
+  BCUDA(b, cudaMemcpy(c, b->d_counters, sizeof(c), cudaMemcpyDeviceToHost), "batch counters");
+  uint32_t err = 0;
+  for (rg_renderer* h : b->items) {
+    stats->samples += (uint64_t)h->opts.width * h->opts.height * h->opts.samples;
+    uint32_t e1 = 0;
+    cudaMemcpy(&e1, h->d_err, sizeof(e1), cudaMemcpyDeviceToHost);
+    err |= e1;
+  }
+  stats->kernel_ms = ms;
+  stats->rays = c[CNT_RAYS];
+  stats->accum_frames = b->items.empty() ? 0 : b->items[0]->frame_count;
+  stats->error_flags = err;
+  stats->duration_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return RG_OK;
+}
+
+}  // namespace
+
+uint64_t rg_batch_item_seed(uint64_t seed, uint32_t index) { return splitmix64(seed + index); }
+
+rg_status rg_batch_create(const rg_device_opts* opts, uint32_t n, const rg_scene_desc* const* scenes, const rg_camera* cameras,
+                          const rg_render_opts* options, rg_batch_handle* out) {
+  if (!out || (n && (!scenes || !cameras || !options))) return RG_INVALID_ARG;
+  *out = nullptr;
+  rg_batch* b = new (std::nothrow) rg_batch();
+  if (!b) return RG_OOM;
+  rg_device_opts o{};
+  if (opts) o = *opts;
+  b->device = o.device;
+  cudaError_t e = cudaSetDevice(o.device);
+  if (e != cudaSuccess) { delete b; cudaGetLastError(); return RG_NO_DEVICE; }
+  if (o.stream) {
+    b->stream = (cudaStream_t)o.stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) { delete b; return RG_CUDA_ERROR; }
+    b->own_stream = true;
+  }
+  rg_status st = RG_OK;
+  rg_device_opts io = o;
+  io.stream = b->stream;
+  io.form = RG_FORM_MEGAKERNEL;
+  for (uint32_t i = 0; i < n && st == RG_OK; ++i) {
+    rg_renderer* h = nullptr;
+    st = rg_create(&io, &h);
+    if (st != RG_OK) break;
+    b->items.push_back(h);
+    if ((st = rg_set_scene(h, scenes[i])) != RG_OK) { b->err = h->err; break; }
+    if ((st = rg_set_camera(h, &cameras[i])) != RG_OK) { b->err = h->err; break; }
+    if ((st = rg_set_options(h, &options[i])) != RG_OK) { b->err = h->err; break; }
+    if (!h->cam_ok) { st = bfail(b, RG_INVALID_CAMERA, "render %u: invalid camera", i); break; }
+    if ((st = ensure_frame_buffers(h)) != RG_OK) { b->err = h->err; break; }
+    b->features |= h->gs.features;
+  }
+  if (st == RG_OK) {
+    b->features = b->features == F_TRI ? F_TRI : (b->features == F_SPHERE ? F_SPHERE : F_ALL);
+    size_t nb = std::max<size_t>(1, n);
+    if ((e = cudaMalloc((void**)&b->d_items, nb * sizeof(BatchItemDev))) != cudaSuccess ||
+        (e = cudaMallocHost((void**)&b->h_items, nb * sizeof(BatchItemDev))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_prefix, (nb + 1) * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_counter, sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_counters, CNT_N * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess) {
+      st = bcuda(b, e, "rg_batch_create");
+    } else {
+      st = layout(b);
+    }
+  }
+  if (st != RG_OK) {
+    std::string msg = b->err;
+    rg_batch_destroy(b);
+    return st;
+  }
+  *out = b;
+  return RG_OK;
+}
+
+rg_status rg_batch_destroy(rg_batch_handle b) {
+  if (!b) return RG_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graph(b);
+  for (rg_renderer* h : b->items) rg_destroy(h);
+  if (b->d_items) cudaFree(b->d_items);
+  if (b->h_items) cudaFreeHost(b->h_items);
+  if (b->d_prefix) cudaFree(b->d_prefix);
+  if (b->d_counter) cudaFree(b->d_counter);
+  if (b->d_counters) cudaFree(b->d_counters);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return RG_OK;
+}
+
+rg_status rg_batch_last_error(rg_batch_handle b, char* buf, size_t len) {
+  if (!b || !buf || len == 0) return RG_INVALID_ARG;
+  size_t n = std::min(len - 1, b->err.size());
+  std::memcpy(buf, b->err.data(), n);
+  buf[n] = '\0';
+  return RG_OK;
+}
+
+rg_status rg_batch_set_tuning(rg_batch_handle b, const rg_batch_tuning* t) {
+  if (!b || !t) return RG_INVALID_ARG;
+  for (uint32_t r : t->reserved)
+    if (r) return bfail(b, RG_INVALID_ARG, "rg_batch_tuning: reserved fields must be 0");
+  if (t->block && (t->block % 32 || t->block < 64 || t->block > 512))
+    return bfail(b, RG_INVALID_ARG, "block must be a multiple of 32 in [64, 512]");
+  if (t->rounds_per_item > 4096) return bfail(b, RG_INVALID_ARG, "rounds_per_item too large");
+  cudaSetDevice(b->device);
+  b->tuning = *t;
+  drop_graph(b);
+  return layout(b);
+}
+
+rg_status rg_batch_render(rg_batch_handle b, uint64_t seed, rg_render_stats* stats) {
+  if (!b) return RG_INVALID_ARG;
+  auto t0 = std::chrono::steady_clock::now();
+  cudaSetDevice(b->device);
+  if (b->items.empty()) return RG_OK;
+  BCUDA(b, cudaStreamSynchronize(b->stream), "batch");  // the pinned table is rewritten below
+  rg_status st = prepare_frame(b, seed);
+  if (st != RG_OK) return st;
+  if (!b->graph) {
+    cudaGraph_t g = nullptr;
+    BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    cudaError_t e = enqueue_frame(b);
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return bcuda(b, e, "graph capture"); }
+    if (e2 != cudaSuccess) return bcuda(b, e2, "graph capture");
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { b->graph = nullptr; return bcuda(b, e, "graph instantiate"); }
+  }
+  BCUDA(b, cudaEventRecord(b->ev0, b->stream), "event");
+  BCUDA(b, cudaGraphLaunch(b->graph, b->stream), "graph launch");
+  BCUDA(b, cudaEventRecord(b->ev1, b->stream), "event");
+  return finish_stats(b, stats, t0);
+}
+
+rg_status rg_batch_render_sequential(rg_batch_handle b, uint64_t seed, rg_render_stats* stats) {
+  if (!b) return RG_INVALID_ARG;
+  auto t0 = std::chrono::steady_clock::now();
+  cudaSetDevice(b->device);
+  BCUDA(b, cudaStreamSynchronize(b->stream), "batch");
+  rg_status st = prepare_frame(b, seed);
+  if (st != RG_OK) return st;
+  BCUDA(b, cudaMemsetAsync(b->d_counters, 0, CNT_N * sizeof(unsigned long long), b->stream), "batch counters");
+  BCUDA(b, cudaEventRecord(b->ev0, b->stream), "event");
+  for (size_t i = 0; i < b->items.size(); ++i) {
+    cudaError_t e = launch_megakernel(b->h_items[i].sc, b->h_items[i].fp, false, b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "sequential launch");
+  }
+  BCUDA(b, cudaEventRecord(b->ev1, b->stream), "event");
+  return finish_stats(b, stats, t0);
+}
+
+rg_status rg_batch_image(rg_batch_handle b, uint32_t index, float* out_rgb) {
+  if (!b || !out_rgb || index >= b->items.size()) return RG_INVALID_ARG;
+  cudaSetDevice(b->device);
+  rg_renderer* h = b->items[index];
+  size_t n = (size_t)h->opts.width * h->opts.height * 3;
+  BCUDA(b, cudaMemcpyAsync(out_rgb, h->d_out, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream), "batch image");
+  BCUDA(b, cudaStreamSynchronize(b->stream), "batch image");
+  return RG_OK;
+}

@@ -279,6 +279,61 @@ def adjoint_scene(n_spheres: int = 1000, seed: int = 0, ground_truth: bool = Tru
     return scene, cam, opts
 
 
+def decimated_icosphere(n_tris: int, centre, radius: float, seed: int = 0):
+    """A displaced icosphere with about `n_tris` triangles: the nearest
+    subdivision level at or above the count, then a seeded random subset."""
+    level = 0
+    while 20 * 4 ** level < n_tris:
+        level += 1
+    verts, norms = displaced_icosphere(level, centre, radius, seed)
+    if verts.shape[0] > n_tris:
+        keep = np.sort(np.random.Generator(np.random.PCG64(seed + 3)).choice(verts.shape[0], n_tris, replace=False))
+        verts, norms = verts[keep], norms[keep]
+    return verts, norms
+
+
+RESOLUTIONS = [(256, 256), (640, 480), (1280, 720), (1920, 1080)]
+
+
+def batch_scenes(n: int = 64, seed: int = 0, scale: float = 1.0, max_tris: int = 500_000):
+    """The batched workload: `n` seeded scenes of uneven size. Sphere counts
+    log-uniform in [10, 5000]; with probability 1/2 a displaced mesh of
+    log-uniform [1k, max_tris] triangles; 0 to 2 media; resolution from
+    {256^2, 640x480, 1280x720, 1920x1080}; 16 to 64 spp; depth 8. `scale`
+    shrinks resolutions (for tests). Returns a list of (scene, camera, opts)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(n):
+        n_sph = int(round(math.exp(rng.uniform(math.log(10), math.log(5000)))))
+        extent = 2.0 + 0.08 * math.sqrt(n_sph)
+        objs = [SimpleObject(SphereMesh((0.0, -1000.0, 0.0), 1000.0), LambertianMaterial((0.5, 0.5, 0.5)))]
+        for _ in range(n_sph - 1):
+            r = 0.1 + 0.25 * rng.random()
+            c = (extent * (2 * rng.random() - 1), r, extent * (2 * rng.random() - 1))
+            u = rng.random()
+            if u < 0.75:
+                mat = LambertianMaterial(tuple(rng.random(3)))
+            elif u < 0.92:
+                mat = MetalMaterial(tuple(0.5 + 0.5 * rng.random(3)), 0.3 * rng.random())
+            else:
+                mat = DielectricMaterial((1.0, 1.0, 1.0), 1.5, 0.0)
+            objs.append(SimpleObject(SphereMesh(c, r), mat))
+        if rng.random() < 0.5:
+            n_tris = int(round(math.exp(rng.uniform(math.log(1000), math.log(max_tris)))))
+            v, nn = decimated_icosphere(n_tris, (0.0, 1.2, 0.0), 1.0, seed=seed * 1000 + k)
+            objs.append(SimpleObject(BvhMesh.from_arrays(v, nn), LambertianMaterial(tuple(0.3 + 0.6 * rng.random(3)))))
+        for _ in range(int(rng.integers(0, 3))):
+            c = (extent * (rng.random() - 0.5), 0.8, extent * (rng.random() - 0.5))
+            objs.append(VolumetricObject(SphereMesh(c, 0.8), IsotropicMaterial(tuple(0.3 + 0.6 * rng.random(3)), 0.0),
+                                         0.05 + 0.5 * rng.random()))
+        w, h = RESOLUTIONS[int(rng.integers(0, len(RESOLUTIONS)))]
+        w, h = max(8, int(w * scale)), max(8, int(h * scale))
+        spp = int(rng.integers(16, 65))
+        cam = look_at_camera((extent * 1.6, 2.0 + 0.3 * extent, extent * 1.2), (0.0, 0.6, 0.0), 40.0)
+        out.append((Scene(objects=objs, skybox=SimpleSkybox()), cam, RenderOpts(width=w, height=h, samples=spp, ray_depth=8)))
+    return out
+
+
 def single_sphere(albedo, skybox=None):
     """The scene of rayna_engine/tests/simple_renders.rs:36-48: a Lambertian
     unit sphere at the origin under WhiteSkybox."""
