@@ -308,6 +308,16 @@ rg_status rg_batch_set_tuning(rg_batch_handle b, const rg_batch_tuning* t) {
     return bfail(b, RG_INVALID_ARG, "block must be a multiple of 32 in [64, 512]");
   if (t->rounds_per_item > 4096) return bfail(b, RG_INVALID_ARG, "rounds_per_item too large");
   cudaSetDevice(b->device);
+  if (t->block) {
+    cudaFuncAttributes fa{};
+    cudaError_t e = b->features == F_TRI ? cudaFuncGetAttributes(&fa, k_batch<F_TRI>)
+                    : b->features == F_SPHERE ? cudaFuncGetAttributes(&fa, k_batch<F_SPHERE>)
+                                              : cudaFuncGetAttributes(&fa, k_batch<F_ALL>);
+    if (e != cudaSuccess) return bcuda(b, e, "rg_batch_set_tuning");
+    if ((int)t->block > fa.maxThreadsPerBlock)
+      return bfail(b, RG_INVALID_ARG, "block %u exceeds the kernel's %d threads per block (registers)", t->block,
+                   fa.maxThreadsPerBlock);
+  }
   b->tuning = *t;
   drop_graph(b);
   return layout(b);

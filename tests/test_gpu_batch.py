@@ -39,7 +39,7 @@ def test_batch_equals_sequential_and_standalone():
 def test_batch_tuning_does_not_change_images():
     items = small_batch()[:4]
     imgs = []
-    for tune in [dict(), dict(block=128, rounds_per_item=1), dict(block=512, blocks_per_sm=1, rounds_per_item=16)]:
+    for tune in [dict(), dict(block=128, rounds_per_item=1), dict(block=64, blocks_per_sm=1, rounds_per_item=16)]:
         with BatchRenderer(items) as b:
             b.set_tuning(**tune)
             b.render(seed=5)
@@ -48,3 +48,11 @@ def test_batch_tuning_does_not_change_images():
     for other in imgs[1:]:
         for a, c in zip(imgs[0], other):
             np.testing.assert_array_equal(a, c)
+
+
+def test_batch_rejects_a_block_the_kernel_cannot_launch():
+    from rayna_gb300._abi import RaynaError
+    with BatchRenderer(small_batch()[:2]) as b:
+        with pytest.raises(RaynaError) as e:
+            b.set_tuning(block=512)
+        assert e.value.status == 1 and "threads per block" in str(e.value)
