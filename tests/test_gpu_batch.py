@@ -50,9 +50,15 @@ def test_batch_tuning_does_not_change_images():
             np.testing.assert_array_equal(a, c)
 
 
-def test_batch_rejects_a_block_the_kernel_cannot_launch():
+def test_batch_rejects_launch_shapes_it_cannot_run():
     from rayna_gb300._abi import RaynaError
     with BatchRenderer(small_batch()[:2]) as b:
         with pytest.raises(RaynaError) as e:
+            b.set_tuning(block=1024)
+        assert e.value.status == 1
+        try:  # 512 threads fit only if the kernel uses <= 128 registers
             b.set_tuning(block=512)
-        assert e.value.status == 1 and "threads per block" in str(e.value)
+        except RaynaError as err:
+            assert err.status == 1 and "threads per block" in str(err)
+        else:
+            b.render(seed=1)
