@@ -188,6 +188,32 @@ def run_adjoint(iters: int = 5, stream=None):
             "loss_first": losses[0], "loss_last": losses[-1], "n_params": int(theta.size)}
 
 
+def run_batch(scale: float, steps: int, stream=None):
+    """Batched workload: 64 seeded scenes of uneven size (sphere counts
+    log-uniform in [10, 5000], half with a displaced mesh of log-uniform
+    [1k, 500k] triangles, 0-2 media, resolutions from {256^2, 640x480,
+    1280x720, 1920x1080} scaled by `scale`, 16-64 spp, depth 8). One
+    persistent work-stealing launch (CUDA graph) per frame, shape from the
+    autotuner, against 64 sequential megakernel launches of the same frame."""
+    from rayna_gb300 import presets
+    from rayna_gb300.autotune import Tuner
+    from rayna_gb300.batch import BatchRenderer
+    items = presets.batch_scenes(64, seed=0, scale=scale)
+    s = stream.cuda_stream if stream is not None else None
+    with BatchRenderer(items, stream=s) as b:
+        cfg = Tuner().tune_batch(b)
+        res = {}
+        for name, fn in (("persistent_graph", b.render), ("sequential_megakernel", b.render_sequential)):
+            fn(seed=7)
+            ms = [fn(seed=100 + k).kernel_ms for k in range(steps)]
+            res[name] = statistics.median(ms)
+        ns = b.n_samples
+    return {"workload": f"64 scenes, resolutions x{scale}, {ns / 1e9:.3f} G samples per frame", "tuning": cfg,
+            "persistent_msamples_s": ns / res["persistent_graph"] / 1e3,
+            "sequential_msamples_s": ns / res["sequential_megakernel"] / 1e3,
+            "speedup": res["sequential_megakernel"] / res["persistent_graph"]}
+
+
 def run_reference(args, rank, world):
     from oracle import binding as ob
     name = args.workload
@@ -331,6 +357,8 @@ def run_gpu(args, rank, world):
     }
     if world == 1 and not args.no_adjoint:
         line["adjoint"] = run_adjoint(stream=stream)
+    if world == 1 and args.batch_scale > 0:
+        line["batch"] = run_batch(args.batch_scale, max(2, args.steps), stream=stream)
     if world == 1 and not args.no_cpu_baseline:
         from oracle import binding as ob
         cb, _ = cpu_baseline(args.workload, ob.hardware_threads(), target_s=args.ref_seconds)
@@ -355,6 +383,7 @@ def main():
     ap.add_argument("--spp", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--batch-scale", type=float, default=0.25, help="resolution scale of the batched workload (0: skip)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))

@@ -1,0 +1,126 @@
+"""Autotuner of the launch shapes, keyed on primitive count and resolution.
+
+The image never depends on these knobs (every form and shape renders the same
+bits); only the time does. A key is
+
+    kind : log2 bucket of primitives : log2 bucket of pixels : log2 bucket of spp
+
+and its entry records the best configuration found and the timings of every
+candidate. Single renders choose between the megakernel and the wavefront
+form and, for the wavefront, the path budget per wave (queue capacity); batches
+choose the persistent kernel's block size, blocks per SM and the work-item
+granularity of the global queue. Entries live in a JSON file
+(RAYNA_GB300_TUNE_CACHE, default rayna_gb300/tuning_cache.json) and are
+measured with CUDA events on the device the first time a key is seen.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import time
+
+from . import _abi as A
+
+DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_cache.json")
+
+WAVE_PATHS = [1 << 20, 1 << 22, 1 << 23, 1 << 24]
+BATCH_SHAPES = [dict(block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)]
+
+
+def _bucket(n: int) -> int:
+    return int(math.floor(math.log2(max(int(n), 1))))
+
+
+def render_key(n_prims: int, width: int, height: int, spp: int) -> str:
+    return f"render:p{_bucket(n_prims)}:r{_bucket(width * height)}:s{_bucket(spp)}"
+
+
+def batch_key(n_items: int, n_prims: int, n_pixels: int, n_samples: int) -> str:
+    return f"batch:n{_bucket(n_items)}:p{_bucket(n_prims)}:r{_bucket(n_pixels)}:s{_bucket(n_samples)}"
+
+
+class Tuner:
+    def __init__(self, path: str | None = None):
+        self.path = path or os.environ.get("RAYNA_GB300_TUNE_CACHE", DEFAULT_CACHE)
+        self.table = {}
+        if os.path.exists(self.path):
+            try:
+                with open(self.path) as f:
+                    self.table = json.load(f)
+            except (OSError, ValueError):
+                self.table = {}
+
+    def lookup(self, key: str):
+        e = self.table.get(key)
+        return e["best"] if e else None
+
+    def store(self, key: str, best: dict, timings: list):
+        self.table[key] = {"best": best, "timings": timings, "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
+        tmp = self.path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(self.table, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.path)
+
+    # -- single renders ------------------------------------------------------
+    @staticmethod
+    def _frame_ms(r, frames: int, seed0: int) -> float:
+        import ctypes as C
+        ms = []
+        st = A.rg_render_stats()
+        for k in range(frames + 1):
+            A.check(r._lib, r.handle, r._lib.rg_render_async(r.handle, seed0 + k, None, C.byref(st)))
+            A.check(r._lib, r.handle, r._lib.rg_sync_stats(r.handle, C.byref(st)))
+            if k:
+                ms.append(st.kernel_ms)
+        return sorted(ms)[len(ms) // 2]
+
+    def tune_render(self, scene, camera, opts, frames: int = 2, force: bool = False, **renderer_kw) -> dict:
+        """Best {form, wave_paths} for this scene size; measured once per key."""
+        from .renderer import Renderer
+        from .scene import flatten
+        flat = flatten(scene)
+        key = render_key(flat.n_prims, opts.width, opts.height, opts.samples)
+        if not force and self.lookup(key):
+            return self.lookup(key)
+        timings = []
+        with Renderer.new_from(scene, camera, opts, 0, form="megakernel", **renderer_kw) as r:
+            timings.append({"form": "megakernel", "wave_paths": 0, "ms": self._frame_ms(r, frames, 1000)})
+        with Renderer.new_from(scene, camera, opts, 0, form="wavefront", **renderer_kw) as r:
+            for wp in WAVE_PATHS:
+                if wp < opts.samples:
+                    continue
+                r.set_wave_paths(wp)
+                timings.append({"form": "wavefront", "wave_paths": wp, "ms": self._frame_ms(r, frames, 2000)})
+        best = min(timings, key=lambda t: t["ms"])
+        cfg = {"form": best["form"], "wave_paths": best["wave_paths"]}
+        self.store(key, cfg, timings)
+        return cfg
+
+    # -- batches -------------------------------------------------------------
+    def tune_batch(self, batch, frames: int = 1, force: bool = False) -> dict:
+        """Best persistent-kernel shape for this batch size; measured once per key."""
+        from .scene import flatten
+        n_prims = sum(flatten(s).n_prims for s, _, _ in batch.items)
+        n_pix = sum(o.width * o.height for _, _, o in batch.items)
+        key = batch_key(len(batch.items), n_prims, n_pix, batch.n_samples)
+        if not force and self.lookup(key):
+            cfg = self.lookup(key)
+            batch.set_tuning(**cfg)
+            return cfg
+        timings = []
+        for shape in BATCH_SHAPES:
+            try:
+                batch.set_tuning(**shape)
+            except A.RaynaError:
+                continue
+            batch.render(seed=1)
+            ms = []
+            for k in range(frames):
+                ms.append(batch.render(seed=2 + k).kernel_ms)
+            timings.append(dict(shape, ms=sorted(ms)[len(ms) // 2]))
+        best = min(timings, key=lambda t: t["ms"])
+        cfg = {k: best[k] for k in ("block", "blocks_per_sm", "rounds_per_item")}
+        batch.set_tuning(**cfg)
+        self.store(key, cfg, timings)
+        return cfg

@@ -84,6 +84,17 @@ class Renderer:
         return cls(scene, camera, options, **kw)
 
     @classmethod
+    def tuned(cls, scene: Scene, camera: Camera, options: RenderOpts, tuner=None, **kw) -> "Renderer":
+        """A renderer with the kernel form and wave size the autotuner picked
+        for this scene size (measured on first sight of the size, then cached)."""
+        from .autotune import Tuner
+        cfg = (tuner or Tuner()).tune_render(scene, camera, options, **kw)
+        r = cls(scene, camera, options, form=cfg["form"], **kw)
+        if cfg["form"] == "wavefront":
+            r.set_wave_paths(cfg["wave_paths"])
+        return r
+
+    @classmethod
     def new_default(cls, **kw) -> "Renderer":
         return cls(Scene(), Camera(), RenderOpts(), **kw)
 
