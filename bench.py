@@ -263,18 +263,22 @@ def run_gpu(args, rank, world):
     # a dedicated stream: the library launches on it, so events on it time its kernels
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    forms = ["megakernel", "wavefront"] if args.form == "best" else [args.form]
+    forms = ["megakernel", "wavefront", "wavefront_sorted"] if args.form == "best" else [args.form]
     results = {}
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     t_setup = time.perf_counter()
     for form in forms:
+        kind = "wavefront" if form.startswith("wavefront") else form
+        sort = form == "wavefront_sorted"
         try:
-            r = Renderer.new_from(scene, cam, opts, 0, form=form, stream=stream.cuda_stream, seed=1000 + rank)
+            r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank)
+            if kind == "wavefront":
+                r.set_wave_paths(0, sort_materials=sort)
         except A.RaynaError as e:
             results[form] = {"error": str(e)}
             continue
         # counting frame: algorithmic work per frame (node visits, primitive tests)
-        rc = Renderer.new_from(scene, cam, opts, 0, form=form, stream=stream.cuda_stream, seed=99, counters=True)
+        rc = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=99, counters=True)
         cst = rc.render().stats
         rc.close()
         lib, h = r._lib, r.handle
@@ -375,7 +379,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="mesh")
-    ap.add_argument("--form", choices=["best", "megakernel", "wavefront"], default="best")
+    ap.add_argument("--form", choices=["best", "megakernel", "wavefront", "wavefront_sorted"], default="best")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=0, help="override the workload resolution (profiling)")

@@ -259,8 +259,9 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene);
  * reference has no device; these are what the autotuner sets). Zero fields
  * select the library defaults. Changing them does not change the image. */
 typedef struct rg_tuning {
-    uint32_t wave_paths;    /* wavefront: path slots per wave (whole pixels per wave) */
-    uint32_t reserved[7];   /* must be 0 */
+    uint32_t wave_paths;      /* wavefront: path slots per wave (whole pixels per wave) */
+    uint32_t sort_materials;  /* wavefront: 1 = separate extend and shade stages, shading in material-kind order */
+    uint32_t reserved[6];     /* must be 0 */
 } rg_tuning;
 
 rg_status rg_set_tuning(rg_handle h, const rg_tuning* t);

@@ -95,7 +95,7 @@ class rg_scene_info(C.Structure):
 
 
 class rg_tuning(C.Structure):
-    _fields_ = [("wave_paths", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+    _fields_ = [("wave_paths", C.c_uint32), ("sort_materials", C.c_uint32), ("reserved", C.c_uint32 * 6)]
 
 
 class rg_gradients(C.Structure):

@@ -87,13 +87,15 @@ class Tuner:
         with Renderer.new_from(scene, camera, opts, 0, form="megakernel", **renderer_kw) as r:
             timings.append({"form": "megakernel", "wave_paths": 0, "ms": self._frame_ms(r, frames, 1000)})
         with Renderer.new_from(scene, camera, opts, 0, form="wavefront", **renderer_kw) as r:
-            for wp in WAVE_PATHS:
-                if wp < opts.samples:
-                    continue
-                r.set_wave_paths(wp)
-                timings.append({"form": "wavefront", "wave_paths": wp, "ms": self._frame_ms(r, frames, 2000)})
+            for sort in (False, True):
+                for wp in WAVE_PATHS:
+                    if wp < opts.samples:
+                        continue
+                    r.set_wave_paths(wp, sort_materials=sort)
+                    timings.append({"form": "wavefront", "wave_paths": wp, "sort_materials": sort,
+                                    "ms": self._frame_ms(r, frames, 2000)})
         best = min(timings, key=lambda t: t["ms"])
-        cfg = {"form": best["form"], "wave_paths": best["wave_paths"]}
+        cfg = {"form": best["form"], "wave_paths": best["wave_paths"], "sort_materials": best.get("sort_materials", False)}
         self.store(key, cfg, timings)
         return cfg
 

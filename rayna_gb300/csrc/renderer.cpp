@@ -580,8 +580,10 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   if (!h || !t) return fail(h, RG_INVALID_ARG, "rg_set_tuning: NULL argument");
   for (uint32_t r : t->reserved)
     if (r != 0) return fail(h, RG_INVALID_ARG, "rg_tuning: reserved fields must be 0");
+  if (t->sort_materials > 1) return fail(h, RG_INVALID_ARG, "rg_tuning: sort_materials must be 0 or 1");
   if (t->wave_paths != h->wf_paths && h->wf.arena) free_extra(h);
   h->wf_paths = t->wave_paths;
+  h->wf_sort = t->sort_materials;
   return RG_OK;
 }
 
@@ -589,6 +591,7 @@ rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
   if (!h || !out) return fail(h, RG_INVALID_ARG, "rg_get_tuning: NULL argument");
   std::memset(out, 0, sizeof(*out));
   out->wave_paths = (uint32_t)h->wf_paths;
+  out->sort_materials = h->wf_sort;
   return RG_OK;
 }
 

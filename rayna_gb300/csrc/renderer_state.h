@@ -84,6 +84,7 @@ struct rg_renderer {
 
   rg::WavefrontState wf;
   size_t wf_paths = 0;        // wavefront path slots per wave (0: library default)
+  uint32_t wf_sort = 0;       // wavefront: shade in material-kind order (separate extend/shade stages)
 
   void* d_adj = nullptr;      // adjoint scratch (image, adjoint image, gradients)
   size_t adj_bytes = 0;

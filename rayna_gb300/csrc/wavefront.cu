@@ -3,20 +3,26 @@
 // A frame is split into waves of whole pixels (all samples of a pixel are in
 // one wave). For every wave:
 //   generate    one camera ray per path slot (slot p = pixel-in-wave * spp + sample)
-//   extend      closest hit of every active path (BVH + unbounded list); each
-//               path is appended to the queue of its hit's material kind
-//               (warp-ballot compaction: one atomic per warp and kind), which
-//               sorts the shade work by material key
-//   shade       over the kind queues laid end to end: emission, sky, scatter,
-//               attenuation; survivors are compacted into the next active queue
-//   accumulate  per-pixel sums in sample order, then the accumulation buffer
+//   bounce      (default) one kernel per bounce over the compacted queue of
+//               live paths: closest hit, emission/sky, scatter, attenuation;
+//               survivors are compacted into the next queue with warp ballots
+//               (one atomic per warp)
+//   extend +    (material-sorted variant) the closest hit of every live path,
+//   shade       each path appended to the queue of its hit's material kind,
+//               then shading over the kind queues laid end to end, so warps
+//               shade one material kind at a time
+//   accumulate  per-pixel sums in the megakernel's order, then the
+//               accumulation buffer
 // Paths run the same per-path functions as the megakernel (trace.cuh) with the
-// same counter-based random streams, and the per-pixel sums are taken in the
-// same order, so both forms produce the same image bit for bit.
+// same counter-based random streams, and per-pixel sums are taken in the same
+// order, so every form produces the same image bit for bit.
 //
-// Path state is structure-of-arrays in one device arena (80 bytes per slot);
-// counts live in device memory, so a wave is a fixed launch sequence with no
-// host round trip.
+// Path state is one 48-byte record per slot (origin + depth, direction + hit
+// distance, throughput + hit primitive), read and written as three float4. A
+// path's radiance is zero until it ends (emission is only met at a light,
+// which ends the path, or at the sky), so it is written once, at the end, to
+// the per-slot sample buffer. Counts live in device memory, so a wave is a
+// fixed launch sequence with no host round trip.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,20 +39,15 @@ namespace {
 constexpr int kWfBlock = 256;
 constexpr int kKinds = 6;  // miss, lambertian, metal, dielectric, isotropic, light
 enum : uint32_t { KQ_MISS = 0 };
+constexpr int kPrimMiss = -1;  // rec[2].w: >= 0 BVH primitive, -1 miss, -2 - k SDF k
 
-struct PathSoA {
-  float *ox, *oy, *oz, *dx, *dy, *dz;
-  float *br, *bg, *bb, *lr, *lg, *lb;
-  float* t;
-  int* prim;
-  int* sdf;
-  float *snx, *sny, *snz;
-  uint32_t* sflags;  // front bit 31 | side
-  uint32_t* depth;
+struct PathState {
+  float4* rec;          // 3 x float4 per slot: (origin, depth) (direction, t) (throughput, prim)
+  float4* aux;          // per slot: SDF hit normal + (front bit 31 | side)
+  float *sr, *sg, *sb;  // per-slot sample radiance
   uint32_t* active[2];
-  uint32_t* kindq;     // kKinds x capacity
-  uint32_t* counts;    // [0], [1]: active counts; [2 .. 2+kKinds): kind counts
-  float *sr, *sg, *sb; // per-slot sample radiance
+  uint32_t* kindq;      // kKinds x capacity
+  uint32_t* counts;     // [0], [1]: active counts; [2 .. 2+kKinds): kind counts
 };
 
 struct WaveParams {
@@ -64,7 +65,17 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
   return base + __popc(ballot & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(kWfBlock) k_generate(FrameParams fp, PathSoA s, WaveParams wp) {
+__device__ __forceinline__ void store_path(const PathState& s, uint32_t p, V3 o, uint32_t depth, V3 d, C3f beta) {
+  s.rec[3 * (size_t)p] = make_float4(o.x, o.y, o.z, __uint_as_float(depth));
+  s.rec[3 * (size_t)p + 1] = make_float4(d.x, d.y, d.z, 0.0f);
+  s.rec[3 * (size_t)p + 2] = make_float4(beta.r, beta.g, beta.b, __int_as_float(kPrimMiss));
+}
+
+__device__ __forceinline__ void finish_path(const PathState& s, uint32_t p, C3f L) {
+  s.sr[p] = L.r; s.sg[p] = L.g; s.sb[p] = L.b;
+}
+
+__global__ void __launch_bounds__(kWfBlock) k_generate(FrameParams fp, PathState s, WaveParams wp) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     s.counts[0] = wp.n_paths;
     s.counts[1] = 0;
@@ -74,63 +85,55 @@ __global__ void __launch_bounds__(kWfBlock) k_generate(FrameParams fp, PathSoA s
     uint32_t x = pix % fp.width, y = pix / fp.width;
     RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, 0, nullptr};
     Ray r = camera_ray(fp, x, y, smp, ctx);
-    s.ox[p] = r.o.x; s.oy[p] = r.o.y; s.oz[p] = r.o.z;
-    s.dx[p] = r.d.x; s.dy[p] = r.d.y; s.dz[p] = r.d.z;
-    s.br[p] = 1.0f; s.bg[p] = 1.0f; s.bb[p] = 1.0f;
-    s.lr[p] = 0.0f; s.lg[p] = 0.0f; s.lb[p] = 0.0f;
-    s.depth[p] = 0;
+    store_path(s, p, r.o, 0, r.d, C3f{1.0f, 1.0f, 1.0f});
     s.active[0][p] = p;
   }
 }
 
-template <uint32_t F, bool COUNT>
-__global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathSoA s, WaveParams wp, int cur) {
-  uint32_t n = s.counts[cur];
+__device__ __forceinline__ uint32_t clamp_count(uint32_t n, const WaveParams& wp, uint32_t* err) {
   if (n > wp.n_paths) {  // never expected: record and clamp instead of reading past the queue
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
-    n = wp.n_paths;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_QUEUE_OVERFLOW);
+    return wp.n_paths;
   }
-  Counters cnt;
-  uint32_t queries = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t p = s.active[cur][i];
-    uint32_t pix = wp.first_pixel + p / fp.spp, smp = p % fp.spp;
-    Ray r;
-    r.o = v3(s.ox[p], s.oy[p], s.oz[p]);
-    r.d = v3(s.dx[p], s.dy[p], s.dz[p]);
-    r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
-    RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, s.depth[p], nullptr};
-    HitRec h;
-    ++queries;
-    bool hit = closest_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
-    uint32_t kind = KQ_MISS;
-    if (hit) {
-      uint32_t mat;
-      if (h.sdf >= 0) {
-        mat = sc.sdfs[h.sdf].material;
-        s.snx[p] = h.sh.n.x; s.sny[p] = h.sh.n.y; s.snz[p] = h.sh.n.z;
-        s.sflags[p] = (h.sh.front ? 0x80000000u : 0u) | (h.sh.side & 0x7FFFFFFFu);
-      } else {
-        mat = prim_material(sc.prims[h.prim]);
-      }
-      kind = 1u + sc.materials[mat].kind;
-      s.t[p] = h.t;
-      s.prim[p] = h.prim;
-      s.sdf[p] = h.sdf;
-    }
-    // Append to the queue of this kind: one atomic per warp and kind present.
-#pragma unroll
-    for (uint32_t k = 0; k < kKinds; ++k) {
-      bool mine = kind == k;
-      if (__any_sync(__activemask(), mine)) {
-        uint32_t slot = warp_append(s.counts + 2 + k, mine);
-        if (mine) {
-          if (slot < wp.capacity) s.kindq[(size_t)k * wp.capacity + slot] = p;
-          else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
-        }
-      }
+  return n;
+}
+
+// Shading of one path at its closest hit (or miss). Returns true when the path
+// continues; then its record holds the scattered ray. Ended paths write their
+// radiance.
+template <uint32_t F>
+__device__ __forceinline__ bool shade_path(const GpuScene& sc, const FrameParams& fp, const PathState& s, uint32_t p,
+                                           uint32_t pix, uint32_t smp, uint32_t depth, const Ray& r, C3f beta,
+                                           bool hit, const HitRec& h) {
+  if (!hit) {
+    C3f sk = sky_colour(sc.sky, r.d);
+    finish_path(s, p, C3f{0.0f + beta.r * sk.r, 0.0f + beta.g * sk.g, 0.0f + beta.b * sk.b});
+    return false;
+  }
+  RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
+  Surface surf;
+  finalize_hit<F>(sc, r, h, ctx, surf);
+  const rg_material m = sc.materials[surf.material];
+  if (m.kind == RG_MAT_LIGHT) {
+    finish_path(s, p, C3f{0.0f + beta.r * m.albedo[0], 0.0f + beta.g * m.albedo[1], 0.0f + beta.b * m.albedo[2]});
+    return false;
+  }
+  if (depth < fp.ray_depth) {
+    V3 dir;
+    if (scatter(m, r, surf, ctx, dir)) {
+      C3f a = attenuation(m, r, surf);
+      beta = C3f{beta.r * a.r, beta.g * a.g, beta.b * a.b};
+      Ray nr = make_ray(surf.pos, dir);
+      store_path(s, p, nr.o, depth + 1, nr.d, beta);
+      return true;
     }
   }
+  finish_path(s, p, C3f{0.0f, 0.0f, 0.0f});
+  return false;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void flush_wave_counters(const FrameParams& fp, const Counters& cnt, uint32_t queries) {
   unsigned long long q = queries;
   for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(0xffffffffu, q, o);
   if ((threadIdx.x & 31) == 0 && q) atomicAdd(fp.counters + CNT_RAYS, q);
@@ -149,8 +152,89 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
   }
 }
 
+// One bounce of every live path: closest hit and shading in one kernel.
+template <uint32_t F, bool COUNT>
+__global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur) {
+  const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
+  const int nxt = cur ^ 1;
+  Counters cnt;
+  uint32_t queries = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t p = s.active[cur][i];
+    const uint32_t pix = wp.first_pixel + p / fp.spp, smp = p % fp.spp;
+    const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1], r2 = s.rec[3 * (size_t)p + 2];
+    const uint32_t depth = __float_as_uint(r0.w);
+    Ray r;
+    r.o = v3(r0.x, r0.y, r0.z);
+    r.d = v3(r1.x, r1.y, r1.z);
+    r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
+    RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
+    HitRec h;
+    ++queries;
+    const bool hit = closest_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
+    const bool alive = shade_path<F>(sc, fp, s, p, pix, smp, depth, r, C3f{r2.x, r2.y, r2.z}, hit, h);
+    if (alive) {
+      uint32_t slot = warp_append(s.counts + nxt, true);
+      if (slot < wp.n_paths) s.active[nxt][slot] = p;
+      else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+    }
+  }
+  flush_wave_counters<COUNT>(fp, cnt, queries);
+}
+
+// Material-sorted variant, stage 1: closest hit; each path goes to the queue
+// of its hit's material kind.
+template <uint32_t F, bool COUNT>
+__global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur) {
+  const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
+  Counters cnt;
+  uint32_t queries = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t p = s.active[cur][i];
+    const uint32_t pix = wp.first_pixel + p / fp.spp, smp = p % fp.spp;
+    const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1];
+    Ray r;
+    r.o = v3(r0.x, r0.y, r0.z);
+    r.d = v3(r1.x, r1.y, r1.z);
+    r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
+    RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, __float_as_uint(r0.w), nullptr};
+    HitRec h;
+    ++queries;
+    const bool hit = closest_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
+    uint32_t kind = KQ_MISS;
+    if (hit) {
+      uint32_t mat;
+      int code = h.prim;
+      if (h.sdf >= 0) {
+        mat = sc.sdfs[h.sdf].material;
+        code = -2 - h.sdf;
+        s.aux[p] = make_float4(h.sh.n.x, h.sh.n.y, h.sh.n.z,
+                               __uint_as_float((h.sh.front ? 0x80000000u : 0u) | (h.sh.side & 0x7FFFFFFFu)));
+      } else {
+        mat = prim_material(sc.prims[h.prim]);
+      }
+      kind = 1u + sc.materials[mat].kind;
+      s.rec[3 * (size_t)p + 1].w = h.t;
+      s.rec[3 * (size_t)p + 2].w = __int_as_float(code);
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kKinds; ++k) {
+      bool mine = kind == k;
+      if (__any_sync(__activemask(), mine)) {
+        uint32_t slot = warp_append(s.counts + 2 + k, mine);
+        if (mine) {
+          if (slot < wp.capacity) s.kindq[(size_t)k * wp.capacity + slot] = p;
+          else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+        }
+      }
+    }
+  }
+  flush_wave_counters<COUNT>(fp, cnt, queries);
+}
+
+// Material-sorted variant, stage 2: shading over the kind queues end to end.
 template <uint32_t F>
-__global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp, PathSoA s, WaveParams wp, int cur) {
+__global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur) {
   __shared__ uint32_t off[kKinds + 1];
   if (threadIdx.x == 0) {
     uint32_t acc = 0;
@@ -169,57 +253,32 @@ __global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp,
     uint32_t k = 0;
 #pragma unroll
     for (int j = 1; j < kKinds; ++j) k += i >= off[j] ? 1u : 0u;
-    uint32_t p = s.kindq[(size_t)k * wp.capacity + (i - off[k])];
-    uint32_t pix = wp.first_pixel + p / fp.spp, smp = p % fp.spp;
-    uint32_t depth = s.depth[p];
+    const uint32_t p = s.kindq[(size_t)k * wp.capacity + (i - off[k])];
+    const uint32_t pix = wp.first_pixel + p / fp.spp, smp = p % fp.spp;
+    const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1], r2 = s.rec[3 * (size_t)p + 2];
     Ray r;
-    r.o = v3(s.ox[p], s.oy[p], s.oz[p]);
-    r.d = v3(s.dx[p], s.dy[p], s.dz[p]);
+    r.o = v3(r0.x, r0.y, r0.z);
+    r.d = v3(r1.x, r1.y, r1.z);
     r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
-    C3f L{s.lr[p], s.lg[p], s.lb[p]};
-    C3f beta{s.br[p], s.bg[p], s.bb[p]};
-    bool alive = false;
-    if (k == KQ_MISS) {
-      C3f sk = sky_colour(sc.sky, r.d);
-      L = C3f{L.r + beta.r * sk.r, L.g + beta.g * sk.g, L.b + beta.b * sk.b};
-    } else {
-      RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
-      HitRec h;
-      h.t = s.t[p];
-      h.prim = s.prim[p];
-      h.sdf = s.sdf[p];
-      if (h.sdf >= 0) {
-        h.sh.n = v3(s.snx[p], s.sny[p], s.snz[p]);
-        uint32_t f = s.sflags[p];
-        h.sh.front = (f >> 31) != 0;
-        h.sh.side = f & 0x7FFFFFFFu;
-        h.sh.t = h.t;
-      }
-      Surface surf;
-      finalize_hit<F>(sc, r, h, ctx, surf);
-      const rg_material m = sc.materials[surf.material];
-      if (m.kind == RG_MAT_LIGHT) {
-        L = C3f{L.r + beta.r * m.albedo[0], L.g + beta.g * m.albedo[1], L.b + beta.b * m.albedo[2]};
-      } else if (depth < fp.ray_depth) {
-        V3 dir;
-        if (scatter(m, r, surf, ctx, dir)) {
-          C3f a = attenuation(m, r, surf);
-          beta = C3f{beta.r * a.r, beta.g * a.g, beta.b * a.b};
-          Ray nr = make_ray(surf.pos, dir);
-          s.ox[p] = nr.o.x; s.oy[p] = nr.o.y; s.oz[p] = nr.o.z;
-          s.dx[p] = nr.d.x; s.dy[p] = nr.d.y; s.dz[p] = nr.d.z;
-          s.br[p] = beta.r; s.bg[p] = beta.g; s.bb[p] = beta.b;
-          s.depth[p] = depth + 1;
-          alive = true;
-        }
-      }
+    HitRec h;
+    h.t = r1.w;
+    const int code = __float_as_int(r2.w);
+    h.prim = code >= 0 ? code : -1;
+    h.sdf = code <= -2 ? -2 - code : -1;
+    if (h.sdf >= 0) {
+      float4 a = s.aux[p];
+      uint32_t f = __float_as_uint(a.w);
+      h.sh.n = v3(a.x, a.y, a.z);
+      h.sh.front = (f >> 31) != 0;
+      h.sh.side = f & 0x7FFFFFFFu;
+      h.sh.t = h.t;
     }
+    const bool alive = shade_path<F>(sc, fp, s, p, pix, smp, __float_as_uint(r0.w), r, C3f{r2.x, r2.y, r2.z},
+                                     k != KQ_MISS, h);
     if (alive) {
       uint32_t slot = warp_append(s.counts + nxt, true);
       if (slot < wp.n_paths) s.active[nxt][slot] = p;
       else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
-    } else {
-      s.sr[p] = L.r; s.sg[p] = L.g; s.sb[p] = L.b;
     }
   }
 }
@@ -227,7 +286,7 @@ __global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp,
 // Per-pixel sums in the megakernel's canonical order: samples 0..spp-1 in
 // turn for spp <= 32; for larger spp, lane partials (samples l, l+32, ...)
 // added for l = 0..31 in turn.
-__global__ void __launch_bounds__(kWfBlock) k_accumulate(FrameParams fp, PathSoA s, WaveParams wp) {
+__global__ void __launch_bounds__(kWfBlock) k_accumulate(FrameParams fp, PathState s, WaveParams wp) {
   const uint32_t spp = fp.spp;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < wp.n_pixels * 3; q += gridDim.x * blockDim.x) {
     uint32_t lp = q / 3, c = q % 3;
@@ -272,21 +331,20 @@ __global__ void __launch_bounds__(kWfBlock) k_accumulate(FrameParams fp, PathSoA
 }
 
 // Lays the path arrays out from `arena` (256-byte aligned each) and returns
-// the number of bytes used; with a null arena it only measures.
-size_t carve(char* arena, size_t cap, PathSoA& s) {
+// the number of bytes used (124 per slot plus the counts); with a null arena
+// it only measures.
+size_t carve(char* arena, size_t cap, PathState& s) {
   size_t used = 0;
   auto take = [&](size_t bytes) {
     char* r = arena ? arena + used : nullptr;
     used += (bytes + 255) & ~size_t(255);
     return r;
   };
-  float** fl[] = {&s.ox, &s.oy, &s.oz, &s.dx, &s.dy, &s.dz, &s.br, &s.bg, &s.bb, &s.lr, &s.lg, &s.lb, &s.t,
-                  &s.snx, &s.sny, &s.snz, &s.sr, &s.sg, &s.sb};
-  for (float** f : fl) *f = (float*)take(cap * 4);
-  s.prim = (int*)take(cap * 4);
-  s.sdf = (int*)take(cap * 4);
-  s.sflags = (uint32_t*)take(cap * 4);
-  s.depth = (uint32_t*)take(cap * 4);
+  s.rec = (float4*)take(cap * 48);
+  s.aux = (float4*)take(cap * 16);
+  s.sr = (float*)take(cap * 4);
+  s.sg = (float*)take(cap * 4);
+  s.sb = (float*)take(cap * 4);
   s.active[0] = (uint32_t*)take(cap * 4);
   s.active[1] = (uint32_t*)take(cap * 4);
   s.kindq = (uint32_t*)take(cap * 4 * kKinds);
@@ -295,7 +353,7 @@ size_t carve(char* arena, size_t cap, PathSoA& s) {
 }
 
 size_t arena_bytes(size_t cap) {
-  PathSoA s;
+  PathState s;
   return carve(nullptr, cap, s);
 }
 
@@ -307,10 +365,11 @@ int sm_count(int device) {
 
 // Runs every wave of one frame on the path arrays `s` (capacity `cap` slots).
 template <uint32_t F>
-cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathSoA& s, size_t cap, size_t pix_per_wave) {
+cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s, size_t cap, size_t pix_per_wave) {
   const size_t spp = fp.spp;
   const size_t n_pix = (size_t)fp.width * fp.height;
   const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
+  const bool sorted = h->wf_sort != 0;
   const int grid = sm_count(h->device) * 8;
   cudaStream_t st = h->stream;
   cudaError_t e;
@@ -324,11 +383,16 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathSoA& s, s
     k_generate<<<gen_blocks, kWfBlock, 0, st>>>(fp, s, wp);
     int cur = 0;
     for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
-      if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
       if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-      if (counters) k_extend<F, true><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-      else k_extend<F, false><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-      k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      if (sorted) {
+        if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
+        if (counters) k_extend<F, true><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+        else k_extend<F, false><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+        k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      } else {
+        if (counters) k_bounce<F, true><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+        else k_bounce<F, false><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+      }
       cur ^= 1;
     }
     uint32_t acc_blocks = (uint32_t)std::min<size_t>((wp.n_pixels * 3 + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
@@ -338,7 +402,7 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathSoA& s, s
   return cudaSuccess;
 }
 
-cudaError_t run_frame(rg_renderer* h, const FrameParams& fp, const PathSoA& s, size_t cap, size_t pix_per_wave) {
+cudaError_t run_frame(rg_renderer* h, const FrameParams& fp, const PathState& s, size_t cap, size_t pix_per_wave) {
   if (h->gs.features == F_TRI) return run_waves<F_TRI>(h, fp, s, cap, pix_per_wave);
   if (h->gs.features == F_SPHERE) return run_waves<F_SPHERE>(h, fp, s, cap, pix_per_wave);
   return run_waves<F_ALL>(h, fp, s, cap, pix_per_wave);
@@ -365,7 +429,7 @@ cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp) {
     h->wf.capacity = cap;
     h->wf.arena_bytes = arena_bytes(cap);
   }
-  PathSoA s;
+  PathState s;
   carve((char*)h->wf.arena, h->wf.capacity, s);
   return run_frame(h, fp, s, h->wf.capacity, pix_per_wave);
 }
@@ -407,7 +471,7 @@ cudaError_t launch_wavefront_static(rg_renderer* h, const FrameParams& fp) {
   void* arena = nullptr;
   cudaError_t e = static_scratch(h->device, &arena);
   if (e != cudaSuccess) return e;
-  PathSoA s;
+  PathState s;
   carve((char*)arena, cap, s);
   return run_frame(h, fp, s, cap, std::min(cap / spp, n_pix));
 }

@@ -91,7 +91,7 @@ class Renderer:
         cfg = (tuner or Tuner()).tune_render(scene, camera, options, **kw)
         r = cls(scene, camera, options, form=cfg["form"], **kw)
         if cfg["form"] == "wavefront":
-            r.set_wave_paths(cfg["wave_paths"])
+            r.set_wave_paths(cfg["wave_paths"], sort_materials=cfg.get("sort_materials", False))
         return r
 
     @classmethod
@@ -204,10 +204,14 @@ class Renderer:
         self.set_accumulation(sums, frames)
         return m
 
-    def set_wave_paths(self, n: int):
-        """Wavefront path slots per wave (0: library default)."""
+    def set_wave_paths(self, n: int, sort_materials: bool | None = None):
+        """Wavefront path slots per wave (0: library default) and, optionally,
+        whether shading runs in material-kind order (separate stages)."""
         t = A.rg_tuning()
+        self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
         t.wave_paths = int(n)
+        if sort_materials is not None:
+            t.sort_materials = 1 if sort_materials else 0
         self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
 
     def set_thread_count(self, num_threads: int):
