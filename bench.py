@@ -239,6 +239,19 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# Kernel configurations timed per workload: (form, material-sorted shading,
+# BVH width). "megakernel" is the plain form: one thread per pixel-sample over
+# binary node pairs.
+FORMS = {
+    "megakernel": ("megakernel", False, 2),
+    "megakernel_wide": ("megakernel", False, 8),
+    "wavefront": ("wavefront", False, 2),
+    "wavefront_sorted": ("wavefront", True, 2),
+    "wavefront_wide": ("wavefront", False, 8),
+    "wavefront_sorted_wide": ("wavefront", True, 8),
+}
+
+
 def run_gpu(args, rank, world):
     import ctypes as C
 
@@ -263,22 +276,21 @@ def run_gpu(args, rank, world):
     # a dedicated stream: the library launches on it, so events on it time its kernels
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    forms = ["megakernel", "wavefront", "wavefront_sorted"] if args.form == "best" else [args.form]
+    forms = list(FORMS) if args.form == "best" else [args.form]
     results = {}
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     t_setup = time.perf_counter()
     for form in forms:
-        kind = "wavefront" if form.startswith("wavefront") else form
-        sort = form == "wavefront_sorted"
+        kind, sort, width = FORMS[form]
         try:
             r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank)
-            if kind == "wavefront":
-                r.set_wave_paths(0, sort_materials=sort)
+            r.set_tuning(sort_materials=sort, bvh_width=width)
         except A.RaynaError as e:
             results[form] = {"error": str(e)}
             continue
         # counting frame: algorithmic work per frame (node visits, primitive tests)
         rc = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=99, counters=True)
+        rc.set_tuning(sort_materials=sort, bvh_width=width)
         cst = rc.render().stats
         rc.close()
         lib, h = r._lib, r.handle
@@ -330,6 +342,7 @@ def run_gpu(args, rank, world):
             "mrays_s": cst.rays * args.steps * world / dev_s / 1e6,
             "rays_per_frame": cst.rays, "node_visits": cst.node_visits, "prim_tests": cst.prim_tests,
             "sdf_steps": cst.sdf_steps, "wall_s": wall, "clocks": clk.summary(), "device_ms": ms,
+            "launches_per_frame": st.kernel_launches, "bvh_width": width,
         }
         r.close()
     if rank != 0:
@@ -339,7 +352,8 @@ def run_gpu(args, rank, world):
     b = ok[best]
     hbm, peak_kind = measured_peaks()
     npx = opts.width * opts.height
-    alg_bytes = 64 * b["node_visits"] + 48 * b["prim_tests"] + 32 * b["rays_per_frame"] + 12 * npx
+    node_bytes = 80 if b["bvh_width"] == 8 else 64
+    alg_bytes = node_bytes * b["node_visits"] + 48 * b["prim_tests"] + 32 * b["rays_per_frame"] + 12 * npx
     achieved = alg_bytes / (b["ms_per_step"] / 1e3) / 1e9
     line = {
         "metric": "Msamples/s", "value": b["msamples_s"], "unit": "Msamples/s", "n_gpus": world,
@@ -351,12 +365,13 @@ def run_gpu(args, rank, world):
                 "d2h_bytes_per_step": npx * 12},
         "mrays_s": b["mrays_s"],
         "forms": {f: {k: v[k] for k in ("msamples_s", "mrays_s", "e2e_msamples_s", "ms_per_step", "rays_per_frame",
-                                         "node_visits", "prim_tests", "sdf_steps", "wall_s")} if "error" not in v
+                                         "node_visits", "prim_tests", "sdf_steps", "wall_s", "launches_per_frame",
+                                         "bvh_width")} if "error" not in v
                   else v for f, v in results.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_frame": alg_bytes},
-        "gpu_launches": args.steps,
+        "gpu_launches": b["launches_per_frame"] * args.steps,
         "clocks": b["clocks"],
     }
     if world == 1 and not args.no_adjoint:
@@ -379,7 +394,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="mesh")
-    ap.add_argument("--form", choices=["best", "megakernel", "wavefront", "wavefront_sorted"], default="best")
+    ap.add_argument("--form", choices=["best"] + list(FORMS), default="best")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=0, help="override the workload resolution (profiling)")

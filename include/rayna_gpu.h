@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 1u
+#define RG_ABI_VERSION 2u
 
 /* Status codes. 0 is success. */
 typedef enum rg_status {
@@ -201,7 +201,7 @@ typedef struct rg_render_stats {
     uint32_t img_height;
     uint32_t num_threads;     /* 0: the device renders */
     uint32_t error_flags;     /* device-side error bits seen this frame (0 = none) */
-    uint32_t reserved;
+    uint32_t kernel_launches; /* kernels the library launched for this frame */
 } rg_render_stats;
 
 /* Hit record of rg_query_rays. */
@@ -225,7 +225,9 @@ typedef struct rg_scene_info {
     uint32_t n_leaves;
     uint32_t max_leaf_size;
     double sah_cost;         /* sum over node pairs of child area x prims / root area */
-    uint64_t device_bytes;   /* bytes the scene occupies in device memory */
+    uint64_t device_bytes;   /* bytes the scene occupies in device memory (both trees) */
+    uint32_t n_wide_nodes;   /* 80-byte nodes of the 8-wide tree (0: the scene traverses the binary tree only) */
+    uint32_t wide_depth;     /* deepest 8-wide node */
 } rg_scene_info;
 
 /* ------------------------------------------------------------------------ */
@@ -261,7 +263,10 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene);
 typedef struct rg_tuning {
     uint32_t wave_paths;      /* wavefront: path slots per wave (whole pixels per wave) */
     uint32_t sort_materials;  /* wavefront: 1 = separate extend and shade stages, shading in material-kind order */
-    uint32_t reserved[6];     /* must be 0 */
+    uint32_t bvh_width;       /* 2 = binary node pairs, 8 = compressed 8-wide nodes; 0 = library default
+                                 (8 for RG_FORM_WAVEFRONT, 2 for RG_FORM_MEGAKERNEL). rg_get_tuning reports
+                                 the width in effect. Either tree gives the same closest hits. */
+    uint32_t reserved[5];     /* must be 0 */
 } rg_tuning;
 
 rg_status rg_set_tuning(rg_handle h, const rg_tuning* t);
@@ -325,7 +330,8 @@ typedef struct rg_batch_tuning {
     uint32_t block;            /* threads per block, multiple of 32 in [64, 512]; 0 = 256 */
     uint32_t blocks_per_sm;    /* blocks launched per SM; 0 = as many as fit */
     uint32_t rounds_per_item;  /* warp rounds of pixels per work item taken from the queue; 0 = 4 */
-    uint32_t reserved[5];      /* must be 0 */
+    uint32_t bvh_width;        /* 2 or 8 as in rg_tuning; 0 = library default (2) */
+    uint32_t reserved[4];      /* must be 0 */
 } rg_batch_tuning;
 
 /* Creates a batch of `n` independent renders (scene, camera, options each,

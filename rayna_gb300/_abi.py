@@ -85,17 +85,19 @@ class rg_render_stats(C.Structure):
                 ("rays", C.c_uint64), ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64),
                 ("sdf_steps", C.c_uint64), ("accum_frames", C.c_uint32), ("img_width", C.c_uint32),
                 ("img_height", C.c_uint32), ("num_threads", C.c_uint32), ("error_flags", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("kernel_launches", C.c_uint32)]
 
 
 class rg_scene_info(C.Structure):
     _fields_ = [("n_prims", C.c_uint32), ("n_unbounded", C.c_uint32), ("n_nodes", C.c_uint32),
                 ("max_depth", C.c_uint32), ("n_leaves", C.c_uint32), ("max_leaf_size", C.c_uint32),
-                ("sah_cost", C.c_double), ("device_bytes", C.c_uint64)]
+                ("sah_cost", C.c_double), ("device_bytes", C.c_uint64), ("n_wide_nodes", C.c_uint32),
+                ("wide_depth", C.c_uint32)]
 
 
 class rg_tuning(C.Structure):
-    _fields_ = [("wave_paths", C.c_uint32), ("sort_materials", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+    _fields_ = [("wave_paths", C.c_uint32), ("sort_materials", C.c_uint32), ("bvh_width", C.c_uint32),
+                ("reserved", C.c_uint32 * 5)]
 
 
 class rg_gradients(C.Structure):
@@ -105,7 +107,7 @@ class rg_gradients(C.Structure):
 
 class rg_batch_tuning(C.Structure):
     _fields_ = [("block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("rounds_per_item", C.c_uint32),
-                ("reserved", C.c_uint32 * 5)]
+                ("bvh_width", C.c_uint32), ("reserved", C.c_uint32 * 4)]
 
 
 class rg_hit(C.Structure):

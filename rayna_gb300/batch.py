@@ -62,9 +62,10 @@ class BatchRenderer:
     def n_samples(self) -> int:
         return sum(o.width * o.height * o.samples for _, _, o in self.items)
 
-    def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, rounds_per_item: int = 0):
+    def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, rounds_per_item: int = 0, bvh_width: int = 0):
         t = A.rg_batch_tuning()
         t.block, t.blocks_per_sm, t.rounds_per_item = int(block), int(blocks_per_sm), int(rounds_per_item)
+        t.bvh_width = int(bvh_width)
         self._check(self._lib.rg_batch_set_tuning(self._h, C.byref(t)))
 
     def next_seed(self) -> int:

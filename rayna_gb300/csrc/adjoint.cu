@@ -277,9 +277,10 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
       return cuda_err(e);
   }
   AdjParams ap{d_adjoint, d_galb, d_gem, d_gden, n_vol};
-  if (h->gs.features == F_SPHERE) launch_replay<F_SPHERE>(h->gs, fp, ap, st);
-  else if (h->gs.features == F_TRI) launch_replay<F_TRI>(h->gs, fp, ap, st);
-  else launch_replay<F_ALL>(h->gs, fp, ap, st);
+  dispatch_features(h->gs.features, [&](auto f) {
+    launch_replay<decltype(f)::value>(h->gs, fp, ap, st);
+    return 0;
+  });
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e);
   double loss = 0.0;
   if (out->albedo && (e = cudaMemcpyAsync(out->albedo, d_galb, (size_t)n_mat * 3 * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess)

@@ -161,6 +161,16 @@ cudaError_t launch_batch_kernel(rg_batch* b) {
   return cudaGetLastError();
 }
 
+// Kernel variant of the batch: the union of the renders' primitive kinds,
+// traversing the 8-wide trees when the tuning asks for them and every render
+// has one.
+uint32_t batch_features(const rg_batch* b) {
+  bool wide = !b->items.empty();
+  for (const rg_renderer* h : b->items)
+    wide = wide && effective_bvh_width(b->tuning.bvh_width, h->gs, RG_FORM_MEGAKERNEL) == 8;
+  return b->features | (wide ? F_WIDE : 0u);
+}
+
 cudaError_t enqueue_frame(rg_batch* b) {
   cudaError_t e;
   if ((e = cudaMemcpyAsync(b->d_items, b->h_items, b->items.size() * sizeof(BatchItemDev), cudaMemcpyHostToDevice,
@@ -168,9 +178,7 @@ cudaError_t enqueue_frame(rg_batch* b) {
     return e;
   if ((e = cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), b->stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(b->d_counters, 0, CNT_N * sizeof(unsigned long long), b->stream)) != cudaSuccess) return e;
-  if (b->features == F_TRI) return launch_batch_kernel<F_TRI>(b);
-  if (b->features == F_SPHERE) return launch_batch_kernel<F_SPHERE>(b);
-  return launch_batch_kernel<F_ALL>(b);
+  return dispatch_features(batch_features(b), [&](auto f) { return launch_batch_kernel<decltype(f)::value>(b); });
 }
 
 // Fills the pinned parameter table for frame `seed` (one frame per render).
@@ -249,7 +257,7 @@ rg_status rg_batch_create(const rg_device_opts* opts, uint32_t n, const rg_scene
     if ((st = rg_set_options(h, &options[i])) != RG_OK) { b->err = h->err; break; }
     if (!h->cam_ok) { st = bfail(b, RG_INVALID_CAMERA, "render %u: invalid camera", i); break; }
     if ((st = ensure_frame_buffers(h)) != RG_OK) { b->err = h->err; break; }
-    b->features |= h->gs.features;
+    b->features |= kinds_of(h->gs.features);
   }
   if (st == RG_OK) {
     b->features = b->features == F_TRI ? F_TRI : (b->features == F_SPHERE ? F_SPHERE : F_ALL);
@@ -307,12 +315,16 @@ rg_status rg_batch_set_tuning(rg_batch_handle b, const rg_batch_tuning* t) {
   if (t->block && (t->block % 32 || t->block < 64 || t->block > 512))
     return bfail(b, RG_INVALID_ARG, "block must be a multiple of 32 in [64, 512]");
   if (t->rounds_per_item > 4096) return bfail(b, RG_INVALID_ARG, "rounds_per_item too large");
+  if (t->bvh_width != 0 && t->bvh_width != 2 && t->bvh_width != 8)
+    return bfail(b, RG_INVALID_ARG, "rg_batch_tuning: bvh_width must be 0, 2 or 8");
   cudaSetDevice(b->device);
   if (t->block) {
     cudaFuncAttributes fa{};
-    cudaError_t e = b->features == F_TRI ? cudaFuncGetAttributes(&fa, k_batch<F_TRI>)
-                    : b->features == F_SPHERE ? cudaFuncGetAttributes(&fa, k_batch<F_SPHERE>)
-                                              : cudaFuncGetAttributes(&fa, k_batch<F_ALL>);
+    rg_batch_tuning prev = b->tuning;
+    b->tuning.bvh_width = t->bvh_width;
+    const uint32_t feats = batch_features(b);
+    b->tuning = prev;
+    cudaError_t e = dispatch_features(feats, [&](auto f) { return cudaFuncGetAttributes(&fa, k_batch<decltype(f)::value>); });
     if (e != cudaSuccess) return bcuda(b, e, "rg_batch_set_tuning");
     if ((int)t->block > fa.maxThreadsPerBlock)
       return bfail(b, RG_INVALID_ARG, "block %u exceeds the kernel's %d threads per block (registers)", t->block,

@@ -4,6 +4,8 @@
 // HBM layout (structure of arrays, every array 256-byte aligned by cudaMalloc):
 //   nodes       BvhNode2[n_nodes]      64 B each: the two child boxes of one
 //                                      binary node plus their child words
+//   wnodes      WideNode[n_wnodes]     80 B each: the same tree collapsed to
+//                                      eight children per node
 //   prims       float4[3 * n_prims]    48 B each, reordered so that every
 //                                      leaf is a contiguous range
 //   tri_normals float[9 * n_tris]      vertex normals, by triangle id,
@@ -13,6 +15,8 @@
 #pragma once
 
 #include <stdint.h>
+
+#include <type_traits>
 
 #include "../../include/rayna_gpu.h"
 
@@ -59,6 +63,38 @@ struct alignas(64) BvhNode2 {
 static_assert(sizeof(BvhNode2) == 64, "node pair must be 64 bytes");
 static_assert(sizeof(GpuPrim) == 48, "primitive must be 48 bytes");
 
+// Compressed 8-wide node, 80 bytes (five float4), after Ylitie, Karras and
+// Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
+// BVHs" (HPG 2017). Up to eight children; each child box is quantised to 8
+// bits per plane on a per-node grid:
+//   plane = p[a] + q * 2^(e[a] - 127),  q in 0..255,
+// rounded outward, so the real (unrounded) grid box contains the child's box.
+//   w0 = (p.x, p.y, p.z, bits e.x | e.y << 8 | e.z << 16 | imask << 24)
+//   w1 = (child_base, prim_base, meta[0..3], meta[4..7])   (u32 bits)
+//   w2 = (qlo.x[0..3], qlo.x[4..7], qhi.x[0..3], qhi.x[4..7]), w3 / w4 for y / z
+// Child slot s is internal when imask bit s is set; internal children are
+// stored contiguously from child_base in slot order, so slot s is node
+// child_base + popc(imask & ((1 << s) - 1)). meta[s] is
+//   0                                   empty slot
+//   0x20 | (24 + s)                     internal child
+//   ((1 << count) - 1) << 5 | offset    leaf over prims [prim_base + offset,
+//                                       + count), count <= 3, offset <= 21
+// so a hit child contributes the bits (meta >> 5) << (meta & 31) to one
+// 32-bit hit mask: bits 24..31 internal children, bits 0..23 primitives.
+// Slots are assigned per node so that visiting the internal hits in the
+// order of slot ^ (ray octant) is roughly front to back.
+struct alignas(16) WideNode {
+  float4 w0;
+  uint4 w1;
+  uint4 qx, qy, qz;
+};
+static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
+constexpr int kWideMaxLeaf = 3;
+// The wide traversal's stack holds at most two entries per tree level (one
+// node group, one postponed primitive group), so trees deeper than this
+// traverse the binary layout instead.
+constexpr int kWideMaxDepth = 31;
+
 // Traversal stack depth; the builder keeps the tree shallower than this.
 constexpr int kStackSize = 64;
 constexpr int kMaxBuildDepth = 60;
@@ -75,6 +111,28 @@ struct GpuSdf {
   float pad[3];
 };
 
+// Kernel variant bits (GpuScene::features): the primitive kinds a kernel is
+// specialised for, and F_WIDE when it traverses the 8-wide tree.
+enum : uint32_t { F_SPHERE = 1u, F_TRI = 2u, F_BOX = 4u, F_VOL = 8u, F_SDF = 16u, F_ALL = 31u, F_WIDE = 32u };
+constexpr uint32_t kinds_of(uint32_t f) { return f & F_ALL; }
+
+// Host-side dispatch: calls fn(std::integral_constant<uint32_t, F>{}) with
+// the compiled kernel variant F for `features` (triangles only, spheres only
+// or every kind; binary or 8-wide traversal).
+template <class Fn>
+auto dispatch_features(uint32_t features, Fn&& fn) {
+  const bool wide = (features & F_WIDE) != 0;
+  switch (kinds_of(features)) {
+    case F_TRI:
+      return wide ? fn(std::integral_constant<uint32_t, F_TRI | F_WIDE>{}) : fn(std::integral_constant<uint32_t, F_TRI>{});
+    case F_SPHERE:
+      return wide ? fn(std::integral_constant<uint32_t, F_SPHERE | F_WIDE>{})
+                  : fn(std::integral_constant<uint32_t, F_SPHERE>{});
+    default:
+      return wide ? fn(std::integral_constant<uint32_t, F_ALL | F_WIDE>{}) : fn(std::integral_constant<uint32_t, F_ALL>{});
+  }
+}
+
 struct GpuScene {
   const BvhNode2* nodes;
   const GpuPrim* prims;
@@ -89,9 +147,11 @@ struct GpuScene {
   uint32_t tri_base;   // global id of triangle 0
   uint32_t vol_base;   // global id of volume 0
   uint32_t n_tris;
-  uint32_t features;   // F_* bits of the kernel variant to launch (primitive kinds present)
+  uint32_t features;   // F_* bits of the kernel variant to launch (primitive kinds present, F_WIDE)
   const float* vol_density;   // per medium: VolumetricObject::density
   const uint32_t* vol_prim;   // per medium: its position in `prims`
+  const WideNode* wnodes;     // the same primitives under the 8-wide tree (node 0 is the root)
+  uint32_t n_wnodes;
 };
 
 // Device error bits (rg_render_stats::error_flags).

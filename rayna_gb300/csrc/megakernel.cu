@@ -32,15 +32,17 @@ cudaError_t launch_megakernel(const GpuScene& sc, const FrameParams& fp, bool co
   const uint32_t ppw = pixels_per_round(fp.spp);
   const uint32_t warps = (n_pix + ppw - 1) / ppw;
   const uint32_t blocks = (warps + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  if (sc.features == F_TRI) launch_mega<F_TRI>(sc, fp, counters, blocks, n_pix, stream);
-  else if (sc.features == F_SPHERE) launch_mega<F_SPHERE>(sc, fp, counters, blocks, n_pix, stream);
-  else launch_mega<F_ALL>(sc, fp, counters, blocks, n_pix, stream);
+  dispatch_features(sc.features, [&](auto f) {
+    launch_mega<decltype(f)::value>(sc, fp, counters, blocks, n_pix, stream);
+    return 0;
+  });
   return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
 // Ray queries: one thread per ray, closest hit with the full hit record.
 // ---------------------------------------------------------------------------
+template <uint32_t F>
 __global__ void k_query(GpuScene sc, uint32_t n, const float* o, const float* d, const float* tmin, const float* tmax,
                         const float* vol_u, rg_hit* out, uint32_t* err) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -54,9 +56,9 @@ __global__ void k_query(GpuScene sc, uint32_t n, const float* o, const float* d,
   res.normal[0] = res.normal[1] = res.normal[2] = 0.0f;
   res.ray_normal[0] = res.ray_normal[1] = res.ray_normal[2] = 0.0f;
   res.front_face = 0; res.material = 0; res.side = 0;
-  if (closest_hit<F_ALL, false>(sc, r, tmin[i], tmax[i], ctx, h, cnt, err)) {
+  if (closest_hit<F, false>(sc, r, tmin[i], tmax[i], ctx, h, cnt, err)) {
     Surface s;
-    finalize_hit<F_ALL>(sc, r, h, ctx, s);
+    finalize_hit<F>(sc, r, h, ctx, s);
     res.hit = 1;
     res.prim = s.prim_id;
     res.t = h.t;
@@ -72,7 +74,9 @@ __global__ void k_query(GpuScene sc, uint32_t n, const float* o, const float* d,
 cudaError_t launch_query(const GpuScene& sc, uint32_t n, const float* o, const float* d, const float* tmin, const float* tmax,
                          const float* vol_u, rg_hit* out, uint32_t* err, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  k_query<<<(n + 127) / 128, 128, 0, stream>>>(sc, n, o, d, tmin, tmax, vol_u, out, err);
+  // The query traverses the tree the handle renders with, over every primitive kind.
+  if (sc.features & F_WIDE) k_query<F_ALL | F_WIDE><<<(n + 127) / 128, 128, 0, stream>>>(sc, n, o, d, tmin, tmax, vol_u, out, err);
+  else k_query<F_ALL><<<(n + 127) / 128, 128, 0, stream>>>(sc, n, o, d, tmin, tmax, vol_u, out, err);
   return cudaGetLastError();
 }
 

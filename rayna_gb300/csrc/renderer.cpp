@@ -290,14 +290,31 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
     g.bound_radius = (float)((r0 + margin) * (1.0 + 1e-4));
     hs.sdfs.push_back(g);
   }
-  BvhBuildResult bvh = build_bvh(lo.data(), hi.data(), nbounded, 4, 16, 40);
+  // Binary tree (leaves of at most kWideMaxLeaf primitives), then its 8-wide
+  // collapse; both index one primitive order.
+  BvhBuildResult bvh = build_bvh(lo.data(), hi.data(), nbounded, kWideMaxLeaf, 16, 40);
+  WideBvhResult wide = build_wide_bvh(bvh.nodes, nbounded);
+  std::vector<uint32_t> order(nbounded);
+  for (uint32_t i = 0; i < nbounded; ++i) order[i] = wide.perm.empty() ? bvh.order[i] : bvh.order[wide.perm[i]];
   hs.nodes = std::move(bvh.nodes);
   hs.max_depth = bvh.max_depth;
+  hs.wide_depth = wide.max_depth;
+  if (!wide.nodes.empty() && wide.max_depth <= kWideMaxDepth) {
+    std::vector<float> olo(3ull * nbounded), ohi(3ull * nbounded);
+    for (uint32_t i = 0; i < nbounded; ++i)
+      for (int a = 0; a < 3; ++a) {
+        olo[3ull * i + a] = lo[3ull * order[i] + a];
+        ohi[3ull * i + a] = hi[3ull * order[i] + a];
+      }
+    std::string bad = check_wide_bvh(wide.nodes, olo.data(), ohi.data(), nbounded);
+    if (!bad.empty()) return fail(h, RG_INVALID_ARG, "internal error: 8-wide tree check failed: %s", bad.c_str());
+    hs.wnodes = std::move(wide.nodes);
+  }
   hs.prims.resize(nbounded);
-  for (uint32_t i = 0; i < nbounded; ++i) hs.prims[i] = prims[bvh.order[i]];
+  for (uint32_t i = 0; i < nbounded; ++i) hs.prims[i] = prims[order[i]];
   hs.vol_prim.assign(hs.nv, 0);
   for (uint32_t i = 0; i < nbounded; ++i)
-    if (bvh.order[i] >= hs.vol_base && bvh.order[i] < hs.vol_base + hs.nv) hs.vol_prim[bvh.order[i] - hs.vol_base] = i;
+    if (order[i] >= hs.vol_base && order[i] < hs.vol_base + hs.nv) hs.vol_prim[order[i] - hs.vol_base] = i;
   hs.vol_density.resize(hs.nv);
   for (uint32_t i = 0; i < hs.nv; ++i) hs.vol_density[i] = d.volumes[i].density;
   if (hs.max_depth >= kMaxBuildDepth)
@@ -309,6 +326,7 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   DeviceScene& ds = h->dev;
   rg_status st;
   if ((st = upload(h, ds.nodes, hs.nodes.data(), hs.nodes.size(), "upload nodes")) != RG_OK) return st;
+  if ((st = upload(h, ds.wnodes, hs.wnodes.data(), hs.wnodes.size(), "upload wide nodes")) != RG_OK) return st;
   if ((st = upload(h, ds.prims, hs.prims.data(), hs.prims.size(), "upload prims")) != RG_OK) return st;
   if ((st = upload(h, ds.tri_normals, hs.tri_normals.data(), hs.tri_normals.size(), "upload normals")) != RG_OK) return st;
   if ((st = upload(h, ds.materials, hs.materials.data(), hs.materials.size(), "upload materials")) != RG_OK) return st;
@@ -318,6 +336,8 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "upload scene");
   GpuScene& g = h->gs;
   g.nodes = ds.nodes;
+  g.wnodes = ds.wnodes;
+  g.n_wnodes = (uint32_t)hs.wnodes.size();
   g.prims = ds.prims;
   g.tri_normals = ds.tri_normals;
   g.materials = ds.materials;
@@ -332,15 +352,25 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.tri_base = hs.ns;
   g.vol_base = hs.vol_base;
   g.n_tris = hs.nt;
-  // Kernel variant: triangles only, spheres only, or every kind (F_* bits of trace.cuh).
-  const uint32_t kSphere = 1, kTri = 2, kAll = 31;
-  uint32_t have = (hs.ns ? kSphere : 0) | (hs.nt ? kTri : 0) | (hs.nb ? 4u : 0) | (hs.nv ? 8u : 0) | (hs.nsdf ? 16u : 0);
-  g.features = have == kTri ? kTri : (have == kSphere ? kSphere : kAll);
+  // Kernel variant: triangles only, spheres only, or every kind.
+  uint32_t have = (hs.ns ? F_SPHERE : 0) | (hs.nt ? F_TRI : 0) | (hs.nb ? F_BOX : 0) | (hs.nv ? F_VOL : 0) |
+                  (hs.nsdf ? F_SDF : 0);
+  h->kinds = have == F_TRI ? F_TRI : (have == F_SPHERE ? F_SPHERE : F_ALL);
+  apply_features(h);
   return RG_OK;
 }
 
+uint32_t effective_bvh_width(uint32_t requested, const GpuScene& g, uint32_t form) {
+  uint32_t w = requested ? requested : (form == RG_FORM_WAVEFRONT ? kDefaultBvhWidthWavefront : kDefaultBvhWidthMegakernel);
+  return (w == 8 && g.n_wnodes > 0) ? 8u : 2u;
+}
+
+void apply_features(rg_renderer* h) {
+  h->gs.features = h->kinds | (effective_bvh_width(h->bvh_width, h->gs, h->form) == 8 ? F_WIDE : 0u);
+}
+
 void free_scene(DeviceScene& ds) {
-  dfree(ds.nodes); dfree(ds.prims); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
+  dfree(ds.nodes); dfree(ds.wnodes); dfree(ds.prims); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
   dfree(ds.vol_density); dfree(ds.vol_prim);
 }
 
@@ -442,7 +472,8 @@ rg_status rg_create(const rg_device_opts* opts, rg_handle* out) {
   h->opts = rg_render_opts{740, 480, 1, RG_MODE_PBR, 5, 1};
   h->gs = GpuScene{};
   h->gs.sky = RG_SKY_SIMPLE;
-  h->gs.features = 31;
+  h->kinds = F_ALL;
+  apply_features(h);
   *out = h;
   return RG_OK;
 }
@@ -514,9 +545,11 @@ rg_status rg_inspect_scene(const rg_scene_desc* scene, rg_scene_info* out) {
     if (n.meta.w > 0) { out->n_leaves++; out->max_leaf_size = std::max<uint32_t>(out->max_leaf_size, n.meta.w); }
   }
   out->sah_cost = root_area > 0.0 ? cost / root_area : 0.0;
-  out->device_bytes = hs.nodes.size() * sizeof(BvhNode2) + hs.prims.size() * sizeof(GpuPrim) +
-                      hs.tri_normals.size() * sizeof(float) + hs.materials.size() * sizeof(rg_material) +
-                      hs.sdfs.size() * sizeof(GpuSdf);
+  out->device_bytes = hs.nodes.size() * sizeof(BvhNode2) + hs.wnodes.size() * sizeof(WideNode) +
+                      hs.prims.size() * sizeof(GpuPrim) + hs.tri_normals.size() * sizeof(float) +
+                      hs.materials.size() * sizeof(rg_material) + hs.sdfs.size() * sizeof(GpuSdf);
+  out->n_wide_nodes = (uint32_t)hs.wnodes.size();
+  out->wide_depth = hs.wide_depth > 0 ? (uint32_t)hs.wide_depth : 0u;
   return RG_OK;
 }
 
@@ -581,9 +614,13 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   for (uint32_t r : t->reserved)
     if (r != 0) return fail(h, RG_INVALID_ARG, "rg_tuning: reserved fields must be 0");
   if (t->sort_materials > 1) return fail(h, RG_INVALID_ARG, "rg_tuning: sort_materials must be 0 or 1");
+  if (t->bvh_width != 0 && t->bvh_width != 2 && t->bvh_width != 8)
+    return fail(h, RG_INVALID_ARG, "rg_tuning: bvh_width must be 0, 2 or 8");
   if (t->wave_paths != h->wf_paths && h->wf.arena) free_extra(h);
   h->wf_paths = t->wave_paths;
   h->wf_sort = t->sort_materials;
+  h->bvh_width = t->bvh_width;
+  apply_features(h);
   return RG_OK;
 }
 
@@ -592,6 +629,7 @@ rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
   std::memset(out, 0, sizeof(*out));
   out->wave_paths = (uint32_t)h->wf_paths;
   out->sort_materials = h->wf_sort;
+  out->bvh_width = effective_bvh_width(h->bvh_width, h->gs, h->form);
   return RG_OK;
 }
 
@@ -626,6 +664,7 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
   RG_CUDA(h, cudaMemsetAsync(h->d_counters, 0, CNT_N * sizeof(unsigned long long), h->stream), "reset counters");
   RG_CUDA(h, cudaEventRecord(h->ev0, h->stream), "event");
   cudaError_t e;
+  h->last_launches = 1;
   if (h->form == RG_FORM_WAVEFRONT) e = launch_wavefront(h, fp);
   else e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream);
   if (e != cudaSuccess) return cuda_fail(h, e, "render launch");
@@ -637,6 +676,7 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
     stats->accum_frames = h->frame_count;
     stats->img_width = fp.width;
     stats->img_height = fp.height;
+    stats->kernel_launches = h->last_launches;
   }
   return RG_OK;
 }
@@ -663,6 +703,7 @@ rg_status rg_sync_stats(rg_handle h, rg_render_stats* stats) {
   stats->img_height = h->opts.height;
   stats->num_threads = 0;
   stats->error_flags = err;
+  stats->kernel_launches = h->last_launches;
   return RG_OK;
 }
 

@@ -23,6 +23,8 @@ struct HostScene {
   uint32_t vol_base = 0;
   int max_depth = 0;
   std::vector<BvhNode2> nodes;
+  std::vector<WideNode> wnodes;        // empty when the 8-wide tree is not usable
+  int wide_depth = 0;
   std::vector<GpuPrim> prims;
   std::vector<float> tri_normals;
   std::vector<rg_material> materials;
@@ -34,6 +36,7 @@ struct HostScene {
 
 struct DeviceScene {
   BvhNode2* nodes = nullptr;
+  WideNode* wnodes = nullptr;
   GpuPrim* prims = nullptr;
   float* tri_normals = nullptr;
   rg_material* materials = nullptr;
@@ -77,6 +80,7 @@ struct rg_renderer {
   uint32_t frame_count = 0;   // AccumulationBuffer::counter
   uint32_t pixel_accum = 0;   // AccumulationValue::accum (per pixel; equal for all pixels)
   uint64_t last_samples = 0;
+  uint32_t last_launches = 0; // kernels launched by the last frame
 
   unsigned long long* d_counters = nullptr;
   uint32_t* d_err = nullptr;
@@ -85,6 +89,8 @@ struct rg_renderer {
   rg::WavefrontState wf;
   size_t wf_paths = 0;        // wavefront path slots per wave (0: library default)
   uint32_t wf_sort = 0;       // wavefront: shade in material-kind order (separate extend/shade stages)
+  uint32_t bvh_width = 0;     // requested traversal: 2, 8, or 0 for the library default
+  uint32_t kinds = 0;         // F_* primitive-kind bits of the scene's kernel variant
 
   void* d_adj = nullptr;      // adjoint scratch (image, adjoint image, gradients)
   size_t adj_bytes = 0;
@@ -92,7 +98,18 @@ struct rg_renderer {
 
 namespace rg {
 
+// Traversal width used when the tuning leaves it at 0: the wavefront's
+// traversal kernels are lean enough in registers for the 8-wide test, the
+// megakernel runs faster on the binary tree.
+constexpr uint32_t kDefaultBvhWidthWavefront = 8;
+constexpr uint32_t kDefaultBvhWidthMegakernel = 2;
+
 // Defined in renderer.cpp
+// Traversal width in effect for a request (0 = default) on a scene.
+uint32_t effective_bvh_width(uint32_t requested, const GpuScene& g, uint32_t form);
+// Kernel variant bits: the scene's primitive kinds, plus F_WIDE when the
+// handle traverses the 8-wide tree.
+void apply_features(rg_renderer* h);
 rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs);
 void fill_frame_params(rg_renderer* h, uint64_t seed, FrameParams& fp);
 rg_status ensure_frame_buffers(rg_renderer* h);

@@ -350,8 +350,6 @@ struct Counters {
   unsigned long long nodes = 0, prims = 0, sdf_steps = 0;
 };
 
-// Primitive kinds a kernel is specialised for (GpuScene::features).
-enum : uint32_t { F_SPHERE = 1u, F_TRI = 2u, F_BOX = 4u, F_VOL = 8u, F_SDF = 16u, F_ALL = 31u };
 
 // Test the primitives of one leaf, shrinking `end` to each accepted hit
 // (object/bvh.rs:82-96: a later hit at equal distance replaces the earlier).
@@ -361,7 +359,8 @@ __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int cou
   for (int i = first; i < first + count; ++i) {
     const GpuPrim* pp = sc.prims + i;
     float4 a = __ldg(&pp->a);
-    uint32_t kind = F == F_TRI ? (uint32_t)PK_TRIANGLE : (F == F_SPHERE ? (uint32_t)PK_SPHERE : __float_as_uint(a.w) >> kKindShift);
+    uint32_t kind = kinds_of(F) == F_TRI ? (uint32_t)PK_TRIANGLE
+                  : (kinds_of(F) == F_SPHERE ? (uint32_t)PK_SPHERE : __float_as_uint(a.w) >> kKindShift);
     if (COUNT) ++cnt.prims;
     float t;
     if ((F & F_TRI) && kind == PK_TRIANGLE) {
@@ -397,77 +396,227 @@ __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int cou
 constexpr int kDone = 0x7FFFFFFF;
 __device__ __forceinline__ int child_ref(int index, int count) { return count > 0 ? ~((index << 3) | count) : index; }
 
-// Closest hit over the BVH, then the unbounded list. Traversal follows Aila &
-// Laine ("Understanding the efficiency of ray traversal on GPUs", HPG 2009):
-// an inner-node loop that postpones the first leaf it meets and keeps going
-// until every lane of the warp holds a leaf, then a leaf loop, so that lanes
-// step through nodes together and through primitives together. Near children
-// go first; far children wait on a stack with their entry distance and are
-// dropped on pop once they lie beyond the closest hit (the same conservative
-// comparison as the slab test, so the result does not change).
+// Binary traversal, after Aila & Laine ("Understanding the efficiency of ray
+// traversal on GPUs", HPG 2009): an inner-node loop that postpones the first
+// leaf it meets and keeps going until every lane of the warp holds a leaf,
+// then a leaf loop, so that lanes step through nodes together and through
+// primitives together. Near children go first; far children wait on a stack
+// with their entry distance and are dropped on pop once they lie beyond the
+// closest hit (the same conservative comparison as the slab test, so the
+// result does not change).
+template <uint32_t F, bool COUNT>
+__device__ __forceinline__ void traverse_binary(const GpuScene& sc, const Ray& r, float start, float& tmax, int& best,
+                                                const RngCtx& ctx, Counters& cnt, uint32_t* err) {
+  int stack[kStackSize];
+  float stack_t[kStackSize];
+  int sp = 0;
+  int ref = 0;
+  int leaf = 0;
+  auto pop = [&]() -> int {
+    float lim = __fmaf_rn(fabsf(tmax), kSlabSlack, tmax);
+    while (sp > 0) {
+      --sp;
+      if (stack_t[sp] <= lim) return stack[sp];
+    }
+    return kDone;
+  };
+  for (;;) {
+    while (ref >= 0 && ref != kDone) {
+      const BvhNode2* np = sc.nodes + ref;
+      float4 xs = __ldg(&np->xs), ys = __ldg(&np->ys), zs = __ldg(&np->zs);
+      int4 m = __ldg(&np->meta);
+      if (COUNT) ++cnt.nodes;
+      float tn0, tn1;
+      bool h0 = slab(xs.x, xs.y, ys.x, ys.y, zs.x, zs.y, r, start, tmax, tn0);
+      bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, tmax, tn1) && m.y >= 0;
+      int r0 = child_ref(m.x, m.z), r1 = child_ref(m.y, m.w);
+      if (h0 && h1) {
+        bool swap = tn1 < tn0;
+        ref = swap ? r1 : r0;
+        if (sp < kStackSize) {
+          stack[sp] = swap ? r0 : r1;
+          stack_t[sp] = swap ? tn0 : tn1;
+          ++sp;
+        } else {
+          atomicOr(err, ERR_STACK_OVERFLOW);
+        }
+      } else if (h0) {
+        ref = r0;
+      } else if (h1) {
+        ref = r1;
+      } else {
+        ref = pop();
+      }
+      if (ref < 0 && leaf == 0) {  // postpone the first leaf and keep traversing
+        leaf = ref;
+        ref = pop();
+      }
+      if (!__any_sync(__activemask(), leaf == 0)) break;
+    }
+    while (leaf < 0) {
+      int code = ~leaf;
+      test_leaf<F, COUNT>(sc, code >> 3, code & 7, r, start, tmax, best, ctx, cnt);
+      leaf = 0;
+      if (ref < 0) {
+        leaf = ref;
+        ref = pop();
+      }
+    }
+    if (ref == kDone) break;
+  }
+}
+
+// 2^23 + byte `sel` (0..3) of w, as a float (bit pattern 0x4B0000bb): one
+// byte permute instead of an integer-to-float conversion.
+__device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t sel) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | sel));
+}
+
+constexpr int kWideStack = 2 * kWideMaxDepth + 2;
+// Primitive tests are postponed while fewer lanes than this want them and
+// the lane still has nodes to visit (Ylitie et al. 2017, section 4).
+constexpr int kPostponeLanes = 6;
+
+// Traversal of the compressed 8-wide tree (layout in gpu_scene.h), after
+// Ylitie, Karras and Laine (HPG 2017). A group is (base, bits): a node group
+// holds the not yet visited hit internal children of one node in bits 24..31
+// (in visit order: bit 24 + (slot ^ octant)) and the node's imask in bits
+// 0..7; a primitive group holds hit primitives prim_base + b in bits 0..23.
+// The stack holds groups, at most two per tree level.
+//
+// Child boxes. A plane at grid step q is t* = (p + q s - o) / d. With
+//   A = s / d (exact: s is a power of two),  B = fl((p - o) / d),
+//   C = fl(B - 2^23 A),  e = 1.0005 |A| + 2^-19 |B|,
+// near planes are evaluated as fma(2^23 + q, A, fl(C - e)) and far planes as
+// fma(2^23 + q, A, fl(C + e)) (2^23 + q comes from one byte permute). The
+// roundings of 1/d, p - o, B, C, C -+ e and the fma move a plane by at most
+// |A| (1 + 512u) + 6u |B| + O(u^2) (u = 2^-24; the |A| from C, whose
+// magnitude is about 2^23 |A|), which e exceeds, so every near plane comes out
+// at or before its exact value and every far plane at or after it. A child is
+// entered when max(near planes, start) <= min(far planes, tmax): no box is
+// rejected that its exact grid box (which contains the child's box) would
+// accept, so the closest hit is the one the primitive tests alone give. The
+// widening is per axis and amounts to one grid step in that axis's own
+// coordinate, whatever the direction. Rays with a zero direction component
+// do not come here (closest_hit sends them to the binary tree); an axis whose
+// A or C still overflows (a huge node, a tiny component) yields NaN planes,
+// which fminf/fmaxf skip: that axis then does not cull.
+template <uint32_t F, bool COUNT>
+__device__ __forceinline__ void traverse_wide(const GpuScene& sc, const Ray& r, float start, float& tmax, int& best,
+                                              const RngCtx& ctx, Counters& cnt, uint32_t* err) {
+  const uint32_t oct = (__float_as_uint(r.inv.x) >> 31) | ((__float_as_uint(r.inv.y) >> 31) << 1) |
+                       ((__float_as_uint(r.inv.z) >> 31) << 2);
+  const float kNaN = __int_as_float(0x7fffffff), kInf = __int_as_float(0x7f800000);
+  uint2 stack[kWideStack];
+  int sp = 0;
+  auto push = [&](uint2 g) {
+    if (sp < kWideStack) stack[sp++] = g;
+    else atomicOr(err, ERR_STACK_OVERFLOW);
+  };
+  uint2 ng = make_uint2(0u, (1u << (24 + oct)) | 1u);  // the root, as slot 0 of a one-child group
+  uint32_t visits = 0;
+  for (;;) {
+    uint2 pg = make_uint2(0u, 0u);
+    if (ng.y > 0x00FFFFFFu) {
+      const uint32_t k = __ffs(ng.y >> 24) - 1;
+      ng.y &= ~(1u << (24 + k));
+      const uint32_t slot = k ^ oct;
+      const uint32_t idx = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+      // A tree visits each node at most once per ray; the host checks the
+      // tree's structure, and this guard keeps a damaged one bounded (the
+      // traversal ends through the loop's one exit, keeping the warp's
+      // reconvergence point there).
+      if (ng.y > 0x00FFFFFFu) push(ng);
+      const bool bad = idx >= sc.n_wnodes || ++visits > sc.n_wnodes;
+      if (bad) {
+        atomicOr(err, ERR_BAD_INDEX);
+        sp = 0;
+      }
+      const WideNode* np = sc.wnodes + (bad ? 0u : idx);
+      const float4 w0 = __ldg(&np->w0);
+      const uint4 w1 = __ldg(&np->w1), qx = __ldg(&np->qx), qy = __ldg(&np->qy), qz = __ldg(&np->qz);
+      if (COUNT) ++cnt.nodes;
+      const uint32_t hdr = __float_as_uint(w0.w);
+      float ax = __uint_as_float((hdr & 0xFFu) << 23) * r.inv.x;
+      float ay = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * r.inv.y;
+      float az = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * r.inv.z;
+      const float bx = (w0.x - r.o.x) * r.inv.x, by = (w0.y - r.o.y) * r.inv.y, bz = (w0.z - r.o.z) * r.inv.z;
+      const float cx = __fmaf_rn(-8388608.0f, ax, bx), cy = __fmaf_rn(-8388608.0f, ay, by),
+                  cz = __fmaf_rn(-8388608.0f, az, bz);
+      const float ex = __fmaf_rn(fabsf(ax), 1.0005f, 1.9073486328125e-6f * fabsf(bx));
+      const float ey = __fmaf_rn(fabsf(ay), 1.0005f, 1.9073486328125e-6f * fabsf(by));
+      const float ez = __fmaf_rn(fabsf(az), 1.0005f, 1.9073486328125e-6f * fabsf(bz));
+      float cnx = cx - ex, cfx = cx + ex, cny = cy - ey, cfy = cy + ey, cnz = cz - ez, cfz = cz + ez;
+      if (!(fabsf(ax) < kInf && fabsf(cx) < kInf)) cnx = cfx = kNaN;
+      if (!(fabsf(ay) < kInf && fabsf(cy) < kInf)) cny = cfy = kNaN;
+      if (!(fabsf(az) < kInf && fabsf(cz) < kInf)) cnz = cfz = kNaN;
+      // near planes: lo for a positive direction component, hi for a negative one
+      const bool sx = oct & 1u, sy = oct & 2u, sz = oct & 4u;
+      const uint32_t nx0 = sx ? qx.z : qx.x, nx1 = sx ? qx.w : qx.y, fx0 = sx ? qx.x : qx.z, fx1 = sx ? qx.y : qx.w;
+      const uint32_t ny0 = sy ? qy.z : qy.x, ny1 = sy ? qy.w : qy.y, fy0 = sy ? qy.x : qy.z, fy1 = sy ? qy.y : qy.w;
+      const uint32_t nz0 = sz ? qz.z : qz.x, nz1 = sz ? qz.w : qz.y, fz0 = sz ? qz.x : qz.z, fz1 = sz ? qz.y : qz.w;
+      // internal children's meta bytes (0x38..0x3F) get the octant folded into their slot bits
+      uint32_t m0 = w1.z, m1 = w1.w;
+      m0 ^= ((m0 >> 3) & (m0 >> 4) & 0x01010101u) * oct;
+      m1 ^= ((m1 >> 3) & (m1 >> 4) & 0x01010101u) * oct;
+      uint32_t hits = 0;
+#pragma unroll
+      for (uint32_t c = 0; c < 8; ++c) {
+        const uint32_t b = c & 3u;
+        const float tnx = __fmaf_rn(byte_plus_2p23(c < 4 ? nx0 : nx1, b), ax, cnx);
+        const float tny = __fmaf_rn(byte_plus_2p23(c < 4 ? ny0 : ny1, b), ay, cny);
+        const float tnz = __fmaf_rn(byte_plus_2p23(c < 4 ? nz0 : nz1, b), az, cnz);
+        const float tfx = __fmaf_rn(byte_plus_2p23(c < 4 ? fx0 : fx1, b), ax, cfx);
+        const float tfy = __fmaf_rn(byte_plus_2p23(c < 4 ? fy0 : fy1, b), ay, cfy);
+        const float tfz = __fmaf_rn(byte_plus_2p23(c < 4 ? fz0 : fz1, b), az, cfz);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, start));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        const uint32_t meta = ((c < 4 ? m0 : m1) >> (8 * b)) & 0xFFu;
+        if (tn <= tf) hits |= (meta >> 5) << (meta & 31u);
+      }
+      if (bad) hits = 0;
+      ng = make_uint2(w1.x, (hits & 0xFF000000u) | (hdr >> 24));
+      pg = make_uint2(w1.y, hits & 0x00FFFFFFu);
+    } else {
+      pg = ng;  // a primitive group from the stack
+      ng = make_uint2(0u, 0u);
+    }
+    while (pg.y) {
+      if (ng.y > 0x00FFFFFFu && __popc(__activemask()) < kPostponeLanes) {
+        push(pg);
+        break;
+      }
+      const uint32_t pi = pg.x + (uint32_t)(__ffs(pg.y) - 1);
+      pg.y &= pg.y - 1u;
+      if (pi < sc.n_prims) test_leaf<F, COUNT>(sc, (int)pi, 1, r, start, tmax, best, ctx, cnt);
+      else atomicOr(err, ERR_BAD_INDEX);
+    }
+    if (ng.y <= 0x00FFFFFFu) {
+      if (sp == 0) break;
+      ng = stack[--sp];
+    }
+  }
+}
+
+// Closest hit over the BVH (binary or 8-wide, by F_WIDE), then the unbounded
+// list. A ray with a zero (or underflowing) direction component has an
+// infinite inverse on that axis; the 8-wide box test cannot cull on such an
+// axis, while the binary slab test handles the infinities exactly, so those
+// rays (which the samplers do produce, e.g. a ball sample of exactly (0, 0, r)
+// off an axis-aligned wall) take the binary tree. Both trees index the same
+// primitives, so the closest hit is the same.
 template <uint32_t F, bool COUNT>
 __device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float end, const RngCtx& ctx, HitRec& h,
                             Counters& cnt, uint32_t* err) {
   int best = -1;
   float tmax = end;
-  if (sc.n_nodes > 0) {
-    int stack[kStackSize];
-    float stack_t[kStackSize];
-    int sp = 0;
-    int ref = 0;
-    int leaf = 0;
-    auto pop = [&]() -> int {
-      float lim = __fmaf_rn(fabsf(tmax), kSlabSlack, tmax);
-      while (sp > 0) {
-        --sp;
-        if (stack_t[sp] <= lim) return stack[sp];
-      }
-      return kDone;
-    };
-    for (;;) {
-      while (ref >= 0 && ref != kDone) {
-        const BvhNode2* np = sc.nodes + ref;
-        float4 xs = __ldg(&np->xs), ys = __ldg(&np->ys), zs = __ldg(&np->zs);
-        int4 m = __ldg(&np->meta);
-        if (COUNT) ++cnt.nodes;
-        float tn0, tn1;
-        bool h0 = slab(xs.x, xs.y, ys.x, ys.y, zs.x, zs.y, r, start, tmax, tn0);
-        bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, tmax, tn1) && m.y >= 0;
-        int r0 = child_ref(m.x, m.z), r1 = child_ref(m.y, m.w);
-        if (h0 && h1) {
-          bool swap = tn1 < tn0;
-          ref = swap ? r1 : r0;
-          if (sp < kStackSize) {
-            stack[sp] = swap ? r0 : r1;
-            stack_t[sp] = swap ? tn0 : tn1;
-            ++sp;
-          } else {
-            atomicOr(err, ERR_STACK_OVERFLOW);
-          }
-        } else if (h0) {
-          ref = r0;
-        } else if (h1) {
-          ref = r1;
-        } else {
-          ref = pop();
-        }
-        if (ref < 0 && leaf == 0) {  // postpone the first leaf and keep traversing
-          leaf = ref;
-          ref = pop();
-        }
-        if (!__any_sync(__activemask(), leaf == 0)) break;
-      }
-      while (leaf < 0) {
-        int code = ~leaf;
-        test_leaf<F, COUNT>(sc, code >> 3, code & 7, r, start, tmax, best, ctx, cnt);
-        leaf = 0;
-        if (ref < 0) {
-          leaf = ref;
-          ref = pop();
-        }
-      }
-      if (ref == kDone) break;
-    }
+  if (F & F_WIDE) {
+    const float kInf = __int_as_float(0x7f800000);
+    const bool finite = fabsf(r.inv.x) < kInf && fabsf(r.inv.y) < kInf && fabsf(r.inv.z) < kInf;
+    if (sc.n_wnodes > 0 && finite) traverse_wide<F, COUNT>(sc, r, start, tmax, best, ctx, cnt, err);
+    else if (sc.n_nodes > 0) traverse_binary<F, COUNT>(sc, r, start, tmax, best, ctx, cnt, err);
+  } else {
+    if (sc.n_nodes > 0) traverse_binary<F, COUNT>(sc, r, start, tmax, best, ctx, cnt, err);
   }
   h.prim = best;
   h.sdf = -1;
@@ -517,8 +666,8 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
   s.prim_id = prim_id(p);
   s.pos = at3(r.o, r.d, h.t);
   s.side = 0;
-  if (F == F_TRI) kind = PK_TRIANGLE;
-  if (F == F_SPHERE) kind = PK_SPHERE;
+  if (kinds_of(F) == F_TRI) kind = PK_TRIANGLE;
+  if (kinds_of(F) == F_SPHERE) kind = PK_SPHERE;
   if ((F & F_SPHERE) && kind == PK_SPHERE) {
     V3 c = xyz(p.a);
     float rad = p.b.x;

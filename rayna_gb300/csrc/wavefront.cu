@@ -373,6 +373,7 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   const int grid = sm_count(h->device) * 8;
   cudaStream_t st = h->stream;
   cudaError_t e;
+  uint32_t launches = 0;
   for (size_t first = 0; first < n_pix; first += pix_per_wave) {
     WaveParams wp;
     wp.first_pixel = (uint32_t)first;
@@ -381,6 +382,7 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
     wp.capacity = (uint32_t)cap;
     uint32_t gen_blocks = (uint32_t)std::min<size_t>((wp.n_paths + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
     k_generate<<<gen_blocks, kWfBlock, 0, st>>>(fp, s, wp);
+    launches += 2 + fp.ray_depth + 1 + (sorted ? fp.ray_depth + 1 : 0);  // generate, accumulate, bounce stages
     int cur = 0;
     for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
       if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
@@ -399,13 +401,13 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
     k_accumulate<<<acc_blocks, kWfBlock, 0, st>>>(fp, s, wp);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
+  h->last_launches = launches;
   return cudaSuccess;
 }
 
 cudaError_t run_frame(rg_renderer* h, const FrameParams& fp, const PathState& s, size_t cap, size_t pix_per_wave) {
-  if (h->gs.features == F_TRI) return run_waves<F_TRI>(h, fp, s, cap, pix_per_wave);
-  if (h->gs.features == F_SPHERE) return run_waves<F_SPHERE>(h, fp, s, cap, pix_per_wave);
-  return run_waves<F_ALL>(h, fp, s, cap, pix_per_wave);
+  return dispatch_features(h->gs.features,
+                           [&](auto f) { return run_waves<decltype(f)::value>(h, fp, s, cap, pix_per_wave); });
 }
 
 }  // namespace

@@ -204,15 +204,32 @@ class Renderer:
         self.set_accumulation(sums, frames)
         return m
 
+    def set_tuning(self, wave_paths: int | None = None, sort_materials: bool | None = None,
+                   bvh_width: int | None = None):
+        """Launch knobs (rg_tuning); None leaves a knob as it is. wave_paths:
+        wavefront path slots per wave (0 = library default); sort_materials:
+        wavefront shading in material-kind order; bvh_width: 2 (binary node
+        pairs) or 8 (compressed 8-wide nodes), 0 = library default."""
+        t = A.rg_tuning()
+        self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
+        if wave_paths is not None:
+            t.wave_paths = int(wave_paths)
+        if sort_materials is not None:
+            t.sort_materials = 1 if sort_materials else 0
+        if bvh_width is not None:
+            t.bvh_width = int(bvh_width)
+        self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
+
+    def tuning(self) -> dict:
+        """The knobs in effect (bvh_width is the traversal actually used)."""
+        t = A.rg_tuning()
+        self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
+        return {"wave_paths": t.wave_paths, "sort_materials": bool(t.sort_materials), "bvh_width": t.bvh_width}
+
     def set_wave_paths(self, n: int, sort_materials: bool | None = None):
         """Wavefront path slots per wave (0: library default) and, optionally,
         whether shading runs in material-kind order (separate stages)."""
-        t = A.rg_tuning()
-        self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
-        t.wave_paths = int(n)
-        if sort_materials is not None:
-            t.sort_materials = 1 if sort_materials else 0
-        self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
+        self.set_tuning(wave_paths=n, sort_materials=sort_materials)
 
     def set_thread_count(self, num_threads: int):
         """Accepted for API parity (renderer.rs:179-182); the device is not thread-pooled."""
@@ -287,6 +304,21 @@ HIT_DTYPE = np.dtype([("hit", np.uint32), ("prim", np.uint32), ("t", np.float32)
                       ("ray_normal", np.float32, 3), ("front_face", np.uint32), ("material", np.uint32),
                       ("side", np.uint32)])
 assert HIT_DTYPE.itemsize == 48
+
+
+def inspect_scene(scene) -> dict:
+    """Builds a scene's trees on the host only (rg_inspect_scene) and returns
+    their statistics; raises RaynaError when the scene is rejected."""
+    from .scene import flatten
+    lib = A.load_library()
+    flat = flatten(scene)
+    info = A.rg_scene_info()
+    st = lib.rg_inspect_scene(C.byref(flat.desc), C.byref(info))
+    if st != A.RG_OK:
+        buf = C.create_string_buffer(1024)
+        lib.rg_last_error(None, buf, len(buf))
+        raise A.RaynaError(st, buf.value.decode(errors="replace"))
+    return {k: getattr(info, k) for k, _ in A.rg_scene_info._fields_}
 
 
 def hits_to_numpy(buf, n: int) -> np.ndarray:

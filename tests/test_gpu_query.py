@@ -25,8 +25,11 @@ pytestmark = pytest.mark.gpu
 EPS32 = np.finfo(np.float32).eps
 
 
-def renderer_for(scene):
-    return Renderer.new_from(scene, Camera(), RenderOpts(width=8, height=8))
+def renderer_for(scene, bvh_width=2):
+    r = Renderer.new_from(scene, Camera(), RenderOpts(width=8, height=8))
+    r.set_tuning(bvh_width=bvh_width)
+    assert r.tuning()["bvh_width"] == bvh_width
+    return r
 
 
 def bits(a):
@@ -86,15 +89,36 @@ def compare_f64(flat, o, d, g, label, min_agree=0.999):
     return float(agree), float(ill), float(np.median(rel)) if rel.size else 0.0
 
 
-@pytest.mark.parametrize("suite", ["spheres", "triangles", "boxes", "sdf_analytic"])
-def test_query_bit_exact_vs_f32_oracle(suite):
-    rng = np.random.Generator(np.random.PCG64({"spheres": 1, "triangles": 2, "boxes": 3, "sdf_analytic": 4}[suite]))
+def axis_aligned_rays(rng, n, lo, hi):
+    """Rays whose directions have exact zero components (along an axis or in
+    an axis plane): the traversal's zero-direction handling."""
+    lo, hi = np.asarray(lo, np.float32), np.asarray(hi, np.float32)
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    zero = rng.integers(0, 3, n)
+    d[np.arange(n), zero] = 0.0
+    both = rng.random(n) < 0.5
+    d[np.arange(n)[both], (zero[both] + 1) % 3] = 0.0
+    return o, d
+
+
+@pytest.mark.parametrize("bvh_width", [2, 8])
+@pytest.mark.parametrize("suite", ["spheres", "triangles", "mesh", "boxes", "sdf_analytic", "axis_aligned"])
+def test_query_bit_exact_vs_f32_oracle(suite, bvh_width):
+    seeds = {"spheres": 1, "triangles": 2, "mesh": 7, "boxes": 3, "sdf_analytic": 4, "axis_aligned": 8}
+    rng = np.random.Generator(np.random.PCG64(seeds[suite]))
     if suite == "spheres":
         scene = sphere_scene()
         o, d = rays_at(rng, 20000, (-12, -1, -12), (12, 2.5, 12))
     elif suite == "triangles":
         scene, verts = triangle_scene(level=4)
         o, d = rays_at(rng, 20000, (0, 0, 0), (1, 1, 1), targets=verts.reshape(-1, 3))
+    elif suite == "mesh":
+        scene = presets.cornell_mesh(level=5)[0]
+        o, d = rays_at(rng, 10000, (0.02, 0.02, 0.02), (0.98, 0.98, 0.98))
+    elif suite == "axis_aligned":
+        scene = presets.cornell_mesh(level=4)[0]
+        o, d = axis_aligned_rays(rng, 10000, (0.02, 0.02, 0.02), (0.98, 0.98, 0.98))
     elif suite == "boxes":
         scene = box_scene()
         o, d = rays_at(rng, 20000, (-3.5, -3.5, -3.5), (3.5, 3.5, 3.5))
@@ -104,24 +128,25 @@ def test_query_bit_exact_vs_f32_oracle(suite):
         scene = Scene(objects=[s.objects[0], s.objects[1], s.objects[3]])
         o, d = rays_at(rng, 4000, (-1.5, -1, -1.5), (3.2, 2, 1.5))
     flat = flatten(scene)
-    with renderer_for(scene) as r:
+    with renderer_for(scene, bvh_width) as r:
         g = r.query_rays(o, d)
     h, _, _ = ob.query(flat, o, d, policy=ob.POLICY_GPU_F32, pretest="brute")
     nhit, nties = compare_bit_exact(g, h, suite)
     assert nhit > 0.2 * len(o)
-    print(f"{suite}: {nhit} hits bit-exact, {nties} exact-distance ties")
+    print(f"{suite} (bvh width {bvh_width}): {nhit} hits bit-exact, {nties} exact-distance ties")
     if suite in ("spheres", "triangles"):
         agree, ill, med = compare_f64(flat, o, d, g, suite)
         print(f"{suite}: f64 agreement {agree:.5f}, ill-conditioned {ill:.4f}, median rel err {med:.2e}")
 
 
-def test_query_volumes_injected_uniforms():
+@pytest.mark.parametrize("bvh_width", [2, 8])
+def test_query_volumes_injected_uniforms(bvh_width):
     rng = np.random.Generator(np.random.PCG64(5))
     scene = volume_scene()
     flat = flatten(scene)
     o, d = rays_at(rng, 20000, (-1.2, -1.2, -1.2), (2.7, 1.2, 1.2), inside_frac=0.3)
     u = rng.uniform(1e-6, 1.0, (len(o), flat.desc.n_volumes)).astype(np.float32)
-    with renderer_for(scene) as r:
+    with renderer_for(scene, bvh_width) as r:
         g = r.query_rays(o, d, volume_u=u)
     h, _, _ = ob.query(flat, o, d, volume_u=u, policy=ob.POLICY_GPU_F32, pretest=False)
     agree = np.mean((g["hit"] == h["hit"]) & ((g["hit"] == 0) | (g["prim"] == h["prim"])))

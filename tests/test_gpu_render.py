@@ -178,26 +178,37 @@ def test_wavefront_equals_megakernel(case):
     else:
         scene, cam, opts = CASES[case]()
     imgs = {}
-    for form, sort in (("megakernel", None), ("wavefront", False), ("wavefront", True)):
-        with Renderer.new_from(scene, cam, opts, 0, form=form, counters=True) as r:
-            if sort is not None:
-                r.set_wave_paths(0, sort_materials=sort)
-            for k in range(2):
-                out = r.render(seed=500 + k)
-            imgs[(form, sort)] = (out.img.copy(), r.frame_moments(), out.stats)
-    a = imgs[("megakernel", None)]
-    for key in (("wavefront", False), ("wavefront", True)):
-        b = imgs[key]
-        np.testing.assert_array_equal(a[0], b[0])
-        np.testing.assert_array_equal(a[1][0], b[1][0])
-        np.testing.assert_array_equal(a[1][1], b[1][1])
-        assert a[2].rays == b[2].rays
-        # Node and primitive counts depend slightly on which rays share a warp
-        # (the traversal postpones leaves until every lane holds one, which
-        # changes when the closest distance shrinks and so how many far nodes
-        # are culled).
-        assert abs(a[2].node_visits - b[2].node_visits) <= 0.01 * a[2].node_visits
-        assert abs(a[2].prim_tests - b[2].prim_tests) <= 0.01 * a[2].prim_tests
+    for width in (2, 8):
+        for form, sort in (("megakernel", None), ("wavefront", False), ("wavefront", True)):
+            with Renderer.new_from(scene, cam, opts, 0, form=form, counters=True) as r:
+                r.set_tuning(bvh_width=width, sort_materials=sort)
+                assert r.tuning()["bvh_width"] == width
+                for k in range(2):
+                    out = r.render(seed=500 + k)
+                assert out.stats.error_flags == 0
+                imgs[(width, form, sort)] = (out.img.copy(), r.frame_moments(), out.stats)
+    for width in (2, 8):
+        a = imgs[(width, "megakernel", None)]
+        for key in ((width, "wavefront", False), (width, "wavefront", True)):
+            b = imgs[key]
+            np.testing.assert_array_equal(a[0], b[0])
+            np.testing.assert_array_equal(a[1][0], b[1][0])
+            np.testing.assert_array_equal(a[1][1], b[1][1])
+            assert a[2].rays == b[2].rays
+            # Node and primitive counts depend slightly on which rays share a
+            # warp (both traversals postpone work by warp occupancy, which
+            # changes when the closest distance shrinks and so how many far
+            # nodes are culled).
+            assert abs(a[2].node_visits - b[2].node_visits) <= 0.01 * a[2].node_visits
+            assert abs(a[2].prim_tests - b[2].prim_tests) <= 0.01 * a[2].prim_tests
+    # The two trees give the same closest hits except at exact-distance ties
+    # between primitives (a shared edge hit exactly), where the traversal
+    # order picks the primitive.
+    a, b = imgs[(2, "megakernel", None)], imgs[(8, "megakernel", None)]
+    same = np.all(a[1][0] == b[1][0], axis=2).mean()
+    print(f"{case}: binary and 8-wide trees agree on {same:.5f} of pixels")
+    assert same >= 0.999
+    assert a[2].rays == b[2].rays or same < 1.0
 
 
 def test_wavefront_small_waves():
