@@ -90,10 +90,9 @@ struct alignas(16) WideNode {
 };
 static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
 constexpr int kWideMaxLeaf = 3;
-// The wide traversal's stack holds at most two entries per tree level (one
-// node group, one postponed primitive group), so trees deeper than this
-// traverse the binary layout instead.
-constexpr int kWideMaxDepth = 31;
+// The wide traversal's stack holds at most one node group per tree level, so
+// trees deeper than this traverse the binary layout instead.
+constexpr int kWideMaxDepth = 60;
 
 // Traversal stack depth; the builder keeps the tree shallower than this.
 constexpr int kStackSize = 64;

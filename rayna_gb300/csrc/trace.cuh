@@ -396,93 +396,135 @@ __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int cou
 constexpr int kDone = 0x7FFFFFFF;
 __device__ __forceinline__ int child_ref(int index, int count) { return count > 0 ? ~((index << 3) | count) : index; }
 
-// Binary traversal, after Aila & Laine ("Understanding the efficiency of ray
-// traversal on GPUs", HPG 2009): an inner-node loop that postpones the first
-// leaf it meets and keeps going until every lane of the warp holds a leaf,
-// then a leaf loop, so that lanes step through nodes together and through
-// primitives together. Near children go first; far children wait on a stack
-// with their entry distance and are dropped on pop once they lie beyond the
-// closest hit (the same conservative comparison as the slab test, so the
-// result does not change).
-template <uint32_t F, bool COUNT>
-__device__ __forceinline__ void traverse_binary(const GpuScene& sc, const Ray& r, float start, float& tmax, int& best,
-                                                const RngCtx& ctx, Counters& cnt, uint32_t* err) {
-  int stack[kStackSize];
-  float stack_t[kStackSize];
-  int sp = 0;
-  int ref = 0;
-  int leaf = 0;
-  auto pop = [&]() -> int {
-    float lim = __fmaf_rn(fabsf(tmax), kSlabSlack, tmax);
-    while (sp > 0) {
-      --sp;
-      if (stack_t[sp] <= lim) return stack[sp];
-    }
-    return kDone;
-  };
-  for (;;) {
-    while (ref >= 0 && ref != kDone) {
-      const BvhNode2* np = sc.nodes + ref;
-      float4 xs = __ldg(&np->xs), ys = __ldg(&np->ys), zs = __ldg(&np->zs);
-      int4 m = __ldg(&np->meta);
-      if (COUNT) ++cnt.nodes;
-      float tn0, tn1;
-      bool h0 = slab(xs.x, xs.y, ys.x, ys.y, zs.x, zs.y, r, start, tmax, tn0);
-      bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, tmax, tn1) && m.y >= 0;
-      int r0 = child_ref(m.x, m.z), r1 = child_ref(m.y, m.w);
-      if (h0 && h1) {
-        bool swap = tn1 < tn0;
-        ref = swap ? r1 : r0;
-        if (sp < kStackSize) {
-          stack[sp] = swap ? r0 : r1;
-          stack_t[sp] = swap ? tn0 : tn1;
-          ++sp;
-        } else {
-          atomicOr(err, ERR_STACK_OVERFLOW);
-        }
-      } else if (h0) {
-        ref = r0;
-      } else if (h1) {
-        ref = r1;
-      } else {
-        ref = pop();
-      }
-      if (ref < 0 && leaf == 0) {  // postpone the first leaf and keep traversing
-        leaf = ref;
-        ref = pop();
-      }
-      if (!__any_sync(__activemask(), leaf == 0)) break;
-    }
-    while (leaf < 0) {
-      int code = ~leaf;
-      test_leaf<F, COUNT>(sc, code >> 3, code & 7, r, start, tmax, best, ctx, cnt);
-      leaf = 0;
-      if (ref < 0) {
-        leaf = ref;
-        ref = pop();
-      }
-    }
-    if (ref == kDone) break;
-  }
-}
-
 // 2^23 + byte `sel` (0..3) of w, as a float (bit pattern 0x4B0000bb): one
 // byte permute instead of an integer-to-float conversion.
 __device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t sel) {
   return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | sel));
 }
 
-constexpr int kWideStack = 2 * kWideMaxDepth + 2;
-// Primitive tests are postponed while fewer lanes than this want them and
-// the lane still has nodes to visit (Ylitie et al. 2017, section 4).
-constexpr int kPostponeLanes = 6;
+constexpr int kTravStack = 64;
+static_assert(kTravStack >= kStackSize && kTravStack >= kWideMaxDepth + 1, "traversal stack too small");
+
+// Resumable traversal of one ray over the binary or the 8-wide tree. A run
+// goes on to completion, or (BOUNDED) for at most `budget` node visits, and
+// returns true once the traversal is complete (the closest hit so far is in
+// best / tmax), so a persistent kernel can hand idle lanes new rays between
+// runs. The stack is a separate array (local memory) so that these scalars
+// stay in registers.
+struct Traversal {
+  int sp;
+  float tmax;
+  int best;
+  bool wide;
+  int ref, leaf;          // binary: next node (or leaf code, or kDone), postponed leaf
+  uint2 ng;               // wide: current node group
+  uint32_t visits, oct;   // wide: node visits so far, ray octant
+};
+
+template <uint32_t F>
+__device__ __forceinline__ void trav_init(Traversal& t, const GpuScene& sc, const Ray& r, float end) {
+  t.sp = 0;
+  t.tmax = end;
+  t.best = -1;
+  t.wide = false;
+  if (F & F_WIDE) {
+    // A zero (or underflowing) direction component makes that axis's inverse
+    // infinite: the 8-wide box test cannot cull on such an axis, while the
+    // binary slab test handles the infinities exactly, so those rays (which
+    // the samplers do produce, e.g. a ball sample of exactly (0, 0, r) off an
+    // axis-aligned wall) take the binary tree. Both trees index the same
+    // primitives, so the closest hit is the same.
+    const float kInf = __int_as_float(0x7f800000);
+    t.wide = sc.n_wnodes > 0 && fabsf(r.inv.x) < kInf && fabsf(r.inv.y) < kInf && fabsf(r.inv.z) < kInf;
+  }
+  if (t.wide) {
+    t.oct = (__float_as_uint(r.inv.x) >> 31) | ((__float_as_uint(r.inv.y) >> 31) << 1) |
+            ((__float_as_uint(r.inv.z) >> 31) << 2);
+    t.ng = make_uint2(0u, (1u << (24 + t.oct)) | 1u);  // the root, as slot 0 of a one-child group
+    t.visits = 0;
+  } else {
+    t.ref = sc.n_nodes > 0 ? 0 : kDone;
+    t.leaf = 0;
+  }
+}
+
+// Binary traversal, after Aila & Laine ("Understanding the efficiency of ray
+// traversal on GPUs", HPG 2009): an inner-node loop that postpones the first
+// leaf it meets and keeps going until every lane of the warp holds a leaf,
+// then a leaf loop, so that lanes step through nodes together and through
+// primitives together. Near children go first; far children wait on the
+// stack as (node, entry distance) and are dropped on pop once they lie beyond
+// the closest hit (the same conservative comparison as the slab test, so the
+// result does not change).
+template <uint32_t F, bool COUNT, bool BOUNDED>
+__device__ __forceinline__ bool run_binary(Traversal& t, uint2* stack, const GpuScene& sc, const Ray& r, float start,
+                                           const RngCtx& ctx, Counters& cnt, uint32_t* err, int budget) {
+  auto pop = [&]() -> int {
+    const float lim = __fmaf_rn(fabsf(t.tmax), kSlabSlack, t.tmax);
+    while (t.sp > 0) {
+      --t.sp;
+      if (__uint_as_float(stack[t.sp].y) <= lim) return (int)stack[t.sp].x;
+    }
+    return kDone;
+  };
+  int it = 0;
+  for (;;) {
+    while (t.ref >= 0 && t.ref != kDone) {
+      const BvhNode2* np = sc.nodes + t.ref;
+      float4 xs = __ldg(&np->xs), ys = __ldg(&np->ys), zs = __ldg(&np->zs);
+      int4 m = __ldg(&np->meta);
+      if (COUNT) ++cnt.nodes;
+      if (BOUNDED) ++it;
+      float tn0, tn1;
+      bool h0 = slab(xs.x, xs.y, ys.x, ys.y, zs.x, zs.y, r, start, t.tmax, tn0);
+      bool h1 = slab(xs.z, xs.w, ys.z, ys.w, zs.z, zs.w, r, start, t.tmax, tn1) && m.y >= 0;
+      int r0 = child_ref(m.x, m.z), r1 = child_ref(m.y, m.w);
+      if (h0 && h1) {
+        bool swap = tn1 < tn0;
+        t.ref = swap ? r1 : r0;
+        if (t.sp < kStackSize) {
+          stack[t.sp] = make_uint2((uint32_t)(swap ? r0 : r1), __float_as_uint(swap ? tn0 : tn1));
+          ++t.sp;
+        } else {
+          atomicOr(err, ERR_STACK_OVERFLOW);
+        }
+      } else if (h0) {
+        t.ref = r0;
+      } else if (h1) {
+        t.ref = r1;
+      } else {
+        t.ref = pop();
+      }
+      if (t.ref < 0 && t.leaf == 0) {  // postpone the first leaf and keep traversing
+        t.leaf = t.ref;
+        t.ref = pop();
+      }
+      if (!__any_sync(__activemask(), t.leaf == 0) || (BOUNDED && it >= budget)) break;
+    }
+    while (t.leaf < 0) {
+      int code = ~t.leaf;
+      test_leaf<F, COUNT>(sc, code >> 3, code & 7, r, start, t.tmax, t.best, ctx, cnt);
+      t.leaf = 0;
+      if (t.ref < 0) {
+        t.leaf = t.ref;
+        t.ref = pop();
+      }
+    }
+    if (t.ref == kDone) return true;
+    if (BOUNDED && it >= budget) return false;
+  }
+}
 
 // Traversal of the compressed 8-wide tree (layout in gpu_scene.h), after
 // Ylitie, Karras and Laine (HPG 2017). A group is (base, bits): a node group
 // holds the not yet visited hit internal children of one node in bits 24..31
 // (in visit order: bit 24 + (slot ^ octant)) and the node's imask in bits
 // 0..7; a primitive group holds hit primitives prim_base + b in bits 0..23.
-// The stack holds groups, at most two per tree level.
+// The stack holds node groups, at most one per tree level. Primitive tests
+// run as soon as their leaf is hit: postponing them while few lanes want
+// them (as Ylitie et al. do) keeps tmax at its initial value for longer, and
+// where lanes are not converged (the persistent extend kernel) it defers
+// every test and culls nothing.
 //
 // Child boxes. A plane at grid step q is t* = (p + q s - o) / d. With
 //   A = s / d (exact: s is a power of two),  B = fl((p - o) / d),
@@ -501,45 +543,40 @@ constexpr int kPostponeLanes = 6;
 // do not come here (closest_hit sends them to the binary tree); an axis whose
 // A or C still overflows (a huge node, a tiny component) yields NaN planes,
 // which fminf/fmaxf skip: that axis then does not cull.
-template <uint32_t F, bool COUNT>
-__device__ __forceinline__ void traverse_wide(const GpuScene& sc, const Ray& r, float start, float& tmax, int& best,
-                                              const RngCtx& ctx, Counters& cnt, uint32_t* err) {
-  const uint32_t oct = (__float_as_uint(r.inv.x) >> 31) | ((__float_as_uint(r.inv.y) >> 31) << 1) |
-                       ((__float_as_uint(r.inv.z) >> 31) << 2);
+template <uint32_t F, bool COUNT, bool BOUNDED>
+__device__ __forceinline__ bool run_wide(Traversal& t, uint2* stack, const GpuScene& sc, const Ray& r, float start,
+                                         const RngCtx& ctx, Counters& cnt, uint32_t* err, int budget) {
   const float kNaN = __int_as_float(0x7fffffff), kInf = __int_as_float(0x7f800000);
-  uint2 stack[kWideStack];
-  int sp = 0;
-  auto push = [&](uint2 g) {
-    if (sp < kWideStack) stack[sp++] = g;
-    else atomicOr(err, ERR_STACK_OVERFLOW);
-  };
-  uint2 ng = make_uint2(0u, (1u << (24 + oct)) | 1u);  // the root, as slot 0 of a one-child group
-  uint32_t visits = 0;
+  const uint32_t oct = t.oct;
+  int it = 0;
   for (;;) {
     uint2 pg = make_uint2(0u, 0u);
-    if (ng.y > 0x00FFFFFFu) {
-      const uint32_t k = __ffs(ng.y >> 24) - 1;
-      ng.y &= ~(1u << (24 + k));
+    if (t.ng.y > 0x00FFFFFFu) {
+      const uint32_t k = __ffs(t.ng.y >> 24) - 1;
+      t.ng.y &= ~(1u << (24 + k));
       const uint32_t slot = k ^ oct;
-      const uint32_t idx = ng.x + __popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+      const uint32_t idx = t.ng.x + __popc(t.ng.y & ((1u << slot) - 1u) & 0xFFu);
+      if (t.ng.y > 0x00FFFFFFu) {
+        if (t.sp < kTravStack) stack[t.sp++] = t.ng;
+        else atomicOr(err, ERR_STACK_OVERFLOW);
+      }
       // A tree visits each node at most once per ray; the host checks the
       // tree's structure, and this guard keeps a damaged one bounded (the
-      // traversal ends through the loop's one exit, keeping the warp's
-      // reconvergence point there).
-      if (ng.y > 0x00FFFFFFu) push(ng);
-      const bool bad = idx >= sc.n_wnodes || ++visits > sc.n_wnodes;
+      // traversal then ends through the loop's normal exit).
+      const bool bad = idx >= sc.n_wnodes || ++t.visits > sc.n_wnodes;
       if (bad) {
         atomicOr(err, ERR_BAD_INDEX);
-        sp = 0;
+        t.sp = 0;
       }
       const WideNode* np = sc.wnodes + (bad ? 0u : idx);
       const float4 w0 = __ldg(&np->w0);
       const uint4 w1 = __ldg(&np->w1), qx = __ldg(&np->qx), qy = __ldg(&np->qy), qz = __ldg(&np->qz);
       if (COUNT) ++cnt.nodes;
+      if (BOUNDED) ++it;
       const uint32_t hdr = __float_as_uint(w0.w);
-      float ax = __uint_as_float((hdr & 0xFFu) << 23) * r.inv.x;
-      float ay = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * r.inv.y;
-      float az = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * r.inv.z;
+      const float ax = __uint_as_float((hdr & 0xFFu) << 23) * r.inv.x;
+      const float ay = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * r.inv.y;
+      const float az = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * r.inv.z;
       const float bx = (w0.x - r.o.x) * r.inv.x, by = (w0.y - r.o.y) * r.inv.y, bz = (w0.z - r.o.z) * r.inv.z;
       const float cx = __fmaf_rn(-8388608.0f, ax, bx), cy = __fmaf_rn(-8388608.0f, ay, by),
                   cz = __fmaf_rn(-8388608.0f, az, bz);
@@ -570,60 +607,47 @@ __device__ __forceinline__ void traverse_wide(const GpuScene& sc, const Ray& r, 
         const float tfy = __fmaf_rn(byte_plus_2p23(c < 4 ? fy0 : fy1, b), ay, cfy);
         const float tfz = __fmaf_rn(byte_plus_2p23(c < 4 ? fz0 : fz1, b), az, cfz);
         const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, start));
-        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, t.tmax));
         const uint32_t meta = ((c < 4 ? m0 : m1) >> (8 * b)) & 0xFFu;
         if (tn <= tf) hits |= (meta >> 5) << (meta & 31u);
       }
       if (bad) hits = 0;
-      ng = make_uint2(w1.x, (hits & 0xFF000000u) | (hdr >> 24));
+      t.ng = make_uint2(w1.x, (hits & 0xFF000000u) | (hdr >> 24));
       pg = make_uint2(w1.y, hits & 0x00FFFFFFu);
-    } else {
-      pg = ng;  // a primitive group from the stack
-      ng = make_uint2(0u, 0u);
     }
     while (pg.y) {
-      if (ng.y > 0x00FFFFFFu && __popc(__activemask()) < kPostponeLanes) {
-        push(pg);
-        break;
-      }
       const uint32_t pi = pg.x + (uint32_t)(__ffs(pg.y) - 1);
       pg.y &= pg.y - 1u;
-      if (pi < sc.n_prims) test_leaf<F, COUNT>(sc, (int)pi, 1, r, start, tmax, best, ctx, cnt);
+      if (pi < sc.n_prims) test_leaf<F, COUNT>(sc, (int)pi, 1, r, start, t.tmax, t.best, ctx, cnt);
       else atomicOr(err, ERR_BAD_INDEX);
     }
-    if (ng.y <= 0x00FFFFFFu) {
-      if (sp == 0) break;
-      ng = stack[--sp];
+    if (t.ng.y <= 0x00FFFFFFu) {
+      if (t.sp == 0) return true;
+      t.ng = stack[--t.sp];
     }
+    if (BOUNDED && it >= budget) return false;
   }
 }
 
-// Closest hit over the BVH (binary or 8-wide, by F_WIDE), then the unbounded
-// list. A ray with a zero (or underflowing) direction component has an
-// infinite inverse on that axis; the 8-wide box test cannot cull on such an
-// axis, while the binary slab test handles the infinities exactly, so those
-// rays (which the samplers do produce, e.g. a ball sample of exactly (0, 0, r)
-// off an axis-aligned wall) take the binary tree. Both trees index the same
-// primitives, so the closest hit is the same.
+// Runs a traversal to completion (BOUNDED false) or for at most `budget`
+// node visits (BOUNDED true); returns true once it is complete.
+template <uint32_t F, bool COUNT, bool BOUNDED>
+__device__ __forceinline__ bool trav_run(Traversal& t, uint2* stack, const GpuScene& sc, const Ray& r, float start,
+                                         const RngCtx& ctx, Counters& cnt, uint32_t* err, int budget) {
+  if ((F & F_WIDE) && t.wide) return run_wide<F, COUNT, BOUNDED>(t, stack, sc, r, start, ctx, cnt, err, budget);
+  return run_binary<F, COUNT, BOUNDED>(t, stack, sc, r, start, ctx, cnt, err, budget);
+}
+
+// ObjectList::full_intersect (object/list.rs:112-129) after the tree: every
+// unbounded object with the original interval [start, end]; it replaces the
+// result only if strictly closer.
 template <uint32_t F, bool COUNT>
-__device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float end, const RngCtx& ctx, HitRec& h,
-                            Counters& cnt, uint32_t* err) {
-  int best = -1;
-  float tmax = end;
-  if (F & F_WIDE) {
-    const float kInf = __int_as_float(0x7f800000);
-    const bool finite = fabsf(r.inv.x) < kInf && fabsf(r.inv.y) < kInf && fabsf(r.inv.z) < kInf;
-    if (sc.n_wnodes > 0 && finite) traverse_wide<F, COUNT>(sc, r, start, tmax, best, ctx, cnt, err);
-    else if (sc.n_nodes > 0) traverse_binary<F, COUNT>(sc, r, start, tmax, best, ctx, cnt, err);
-  } else {
-    if (sc.n_nodes > 0) traverse_binary<F, COUNT>(sc, r, start, tmax, best, ctx, cnt, err);
-  }
-  h.prim = best;
+__device__ __forceinline__ bool finish_hit(const GpuScene& sc, const Ray& r, float start, float end, const Traversal& t,
+                                           HitRec& h, Counters& cnt) {
+  h.prim = t.best;
   h.sdf = -1;
-  h.t = tmax;
-  bool any = best >= 0;
-  // ObjectList::full_intersect (object/list.rs:112-129): every unbounded object
-  // with the original interval; it replaces the result only if strictly closer.
+  h.t = t.tmax;
+  bool any = t.best >= 0;
   if (F & F_SDF) {
     for (uint32_t k = 0; k < sc.n_sdfs; ++k) {
       SdfHit sh;
@@ -636,6 +660,17 @@ __device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float
     }
   }
   return any;
+}
+
+// Closest hit over the BVH (binary or 8-wide, by F_WIDE), then the unbounded list.
+template <uint32_t F, bool COUNT>
+__device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float end, const RngCtx& ctx, HitRec& h,
+                            Counters& cnt, uint32_t* err) {
+  Traversal t;
+  uint2 stack[kTravStack];
+  trav_init<F>(t, sc, r, end);
+  trav_run<F, COUNT, false>(t, stack, sc, r, start, ctx, cnt, err, 0);
+  return finish_hit<F, COUNT>(sc, r, start, end, t, h, cnt);
 }
 
 // Full hit record of the closest hit.

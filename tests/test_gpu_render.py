@@ -196,11 +196,12 @@ def test_wavefront_equals_megakernel(case):
             np.testing.assert_array_equal(a[1][1], b[1][1])
             assert a[2].rays == b[2].rays
             # Node and primitive counts depend slightly on which rays share a
-            # warp (both traversals postpone work by warp occupancy, which
-            # changes when the closest distance shrinks and so how many far
-            # nodes are culled).
-            assert abs(a[2].node_visits - b[2].node_visits) <= 0.01 * a[2].node_visits
-            assert abs(a[2].prim_tests - b[2].prim_tests) <= 0.01 * a[2].prim_tests
+            # warp (the binary traversal postpones leaves by warp occupancy,
+            # which changes when the closest distance shrinks and so how many
+            # far nodes are culled; the persistent extend kernel regroups rays
+            # as lanes refill). They are work counters, not results.
+            assert abs(a[2].node_visits - b[2].node_visits) <= 0.03 * a[2].node_visits
+            assert abs(a[2].prim_tests - b[2].prim_tests) <= 0.03 * a[2].prim_tests
     # The two trees give the same closest hits except at exact-distance ties
     # between primitives (a shared edge hit exactly), where the traversal
     # order picks the primitive.

@@ -18,7 +18,7 @@ from rayna_gb300.scene import (
     SdfTorus, SimpleObject, SphereMesh, Triangle, VolumetricObject,
 )
 
-MAX_WIDE_DEPTH = 31
+MAX_WIDE_DEPTH = 60
 
 
 def check(scene, n_prims):
