@@ -47,7 +47,7 @@ struct PathState {
   float *sr, *sg, *sb;  // per-slot sample radiance
   uint32_t* active[2];
   uint32_t* kindq;      // kKinds x capacity
-  uint32_t* counts;     // [0], [1]: active counts; [2 .. 2+kKinds): kind counts; [kFetchCounter]: extend's fetch counter
+  uint32_t* counts;     // [0], [1]: active counts; [2 .. 2+kKinds): kind counts; [kFetchCounter]: the traversal kernels' fetch counter
 };
 constexpr int kFetchCounter = 2 + kKinds;
 
@@ -153,31 +153,67 @@ __device__ __forceinline__ void flush_wave_counters(const FrameParams& fp, const
   }
 }
 
-// One bounce of every live path: closest hit and shading in one kernel.
+// Node visits a persistent traversal kernel runs between refills.
+constexpr int kFetchBudget = 16;
+
+// One bounce of every live path: closest hit and shading in one kernel,
+// persistent with dynamic ray fetch (Aila & Laine 2009, "replacing terminated
+// rays"): a warp keeps 32 paths in flight, traverses for a bounded number of
+// node visits, and a lane whose traversal has finished shades its path and
+// then takes the next one from the queue (one atomic per warp and refill), so
+// lanes do not idle while the warp's longest ray finishes.
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   const int nxt = cur ^ 1;
+  uint32_t* next = s.counts + kFetchCounter;
+  const uint32_t lane = threadIdx.x & 31u;
   Counters cnt;
   uint32_t queries = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint32_t p = s.active[cur][i];
-    const uint32_t pix = wp.first_pixel + p / fp.spp, smp = p % fp.spp;
-    const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1], r2 = s.rec[3 * (size_t)p + 2];
-    const uint32_t depth = __float_as_uint(r0.w);
-    Ray r;
-    r.o = v3(r0.x, r0.y, r0.z);
-    r.d = v3(r1.x, r1.y, r1.z);
-    r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
-    RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
-    HitRec h;
-    ++queries;
-    const bool hit = closest_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
-    const bool alive = shade_path<F>(sc, fp, s, p, pix, smp, depth, r, C3f{r2.x, r2.y, r2.z}, hit, h);
-    if (alive) {
-      uint32_t slot = warp_append(s.counts + nxt, true);
-      if (slot < wp.n_paths) s.active[nxt][slot] = p;
-      else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+  bool has = false, drained = false;
+  uint32_t p = 0, pix = 0, smp = 0, depth = 0;
+  Ray r;
+  C3f beta;
+  Traversal t;
+  uint2 stack[kTravStack];
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !has);
+    if (idle && !drained) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(next, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= n) drained = true;
+      if (!has) {
+        const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (i < n) {
+          p = s.active[cur][i];
+          pix = wp.first_pixel + p / fp.spp;
+          smp = p % fp.spp;
+          const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1], r2 = s.rec[3 * (size_t)p + 2];
+          depth = __float_as_uint(r0.w);
+          r.o = v3(r0.x, r0.y, r0.z);
+          r.d = v3(r1.x, r1.y, r1.z);
+          r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
+          beta = C3f{r2.x, r2.y, r2.z};
+          trav_init<F>(t, sc, r, 3.402823466e38f);
+          has = true;
+          ++queries;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, has)) break;
+    if (has) {
+      const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
+      if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, kFetchBudget)) {
+        HitRec h;
+        const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
+        if (shade_path<F>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
+          uint32_t slot = warp_append(s.counts + nxt, true);
+          if (slot < wp.n_paths) s.active[nxt][slot] = p;
+          else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+        }
+        has = false;
+      }
     }
   }
   flush_wave_counters<COUNT>(fp, cnt, queries);
@@ -189,7 +225,6 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
 // flight, traverses for a bounded number of node visits, and lanes whose ray
 // has finished take the next rays from the queue (one atomic per warp), so
 // lanes do not idle while the warp's longest ray finishes.
-constexpr int kFetchBudget = 16;  // node visits between refills
 
 template <uint32_t F, bool COUNT>
 __device__ __forceinline__ void record_hit(const GpuScene& sc, const FrameParams& fp, const PathState& s,
@@ -412,11 +447,15 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
   const bool sorted = h->wf_sort != 0;
   const int grid = sm_count(h->device) * 8;
-  // The persistent extend kernel runs as many blocks as are resident at once.
+  // The persistent traversal kernels run as many blocks as are resident at once.
   int ext_per_sm = 0;
   if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_extend<F, true>, kWfBlock, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_extend<F, false>, kWfBlock, 0);
   const int ext_grid = sm_count(h->device) * std::max(ext_per_sm, 1);
+  int bounce_per_sm = 0;
+  if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bounce_per_sm, k_bounce<F, true>, kWfBlock, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bounce_per_sm, k_bounce<F, false>, kWfBlock, 0);
+  const int bounce_grid = sm_count(h->device) * std::max(bounce_per_sm, 1);
   cudaStream_t st = h->stream;
   cudaError_t e;
   uint32_t launches = 0;
@@ -432,14 +471,15 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
     int cur = 0;
     for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
       if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
       if (sorted) {
-        if ((e = cudaMemsetAsync(s.counts + 2, 0, (kKinds + 1) * sizeof(uint32_t), st)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
         if (counters) k_extend<F, true><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
         else k_extend<F, false><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
         k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
       } else {
-        if (counters) k_bounce<F, true><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-        else k_bounce<F, false><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+        else k_bounce<F, false><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
       }
       cur ^= 1;
     }
