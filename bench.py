@@ -284,13 +284,13 @@ def run_gpu(args, rank, world):
         kind, sort, width = FORMS[form]
         try:
             r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank)
-            r.set_tuning(sort_materials=sort, bvh_width=width)
+            r.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
         except A.RaynaError as e:
             results[form] = {"error": str(e)}
             continue
         # counting frame: algorithmic work per frame (node visits, primitive tests)
         rc = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=99, counters=True)
-        rc.set_tuning(sort_materials=sort, bvh_width=width)
+        rc.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
         cst = rc.render().stats
         rc.close()
         lib, h = r._lib, r.handle
@@ -395,6 +395,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="mesh")
     ap.add_argument("--form", choices=["best"] + list(FORMS), default="best")
+    ap.add_argument("--fetch-budget", type=int, default=0,
+                    help="node visits between refills in the persistent wavefront kernels (0: library default)")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=0, help="override the workload resolution (profiling)")

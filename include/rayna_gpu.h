@@ -261,15 +261,18 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene);
  * reference has no device; these are what the autotuner sets). Zero fields
  * select the library defaults. Changing them does not change the image. */
 typedef struct rg_tuning {
-    uint32_t wave_paths;      /* wavefront: path slots per wave (whole pixels per wave) */
-    uint32_t sort_materials;  /* wavefront: 1 = separate extend and shade stages, shading in material-kind order */
-    uint32_t bvh_width;       /* 2 = binary node pairs, 8 = compressed 8-wide nodes; 0 = library default
-                                 (8 for RG_FORM_WAVEFRONT, 2 for RG_FORM_MEGAKERNEL). rg_get_tuning reports
-                                 the width in effect. Either tree gives the same closest hits. */
-    uint32_t reserved[5];     /* must be 0 */
+    uint32_t wave_paths;      /* wavefront: path slots per wave (whole pixels per wave); 0 = 2^23 */
+    uint32_t sort_materials;  /* wavefront: 1 = separate extend and shade stages, shading in material-kind order;
+                                 2 = one fused bounce kernel; 0 = library default (fused for scenes of spheres
+                                 only, sorted otherwise) */
+    uint32_t bvh_width;       /* 2 = binary node pairs, 8 = compressed 8-wide nodes; 0 = library default (2).
+                                 Either tree gives the same closest hits. */
+    uint32_t fetch_budget;    /* wavefront: node visits a lane traverses between refills of idle lanes; 0 = 8 */
+    uint32_t reserved[4];     /* must be 0 */
 } rg_tuning;
 
 rg_status rg_set_tuning(rg_handle h, const rg_tuning* t);
+/* The knobs in effect: library defaults appear resolved (never 0). */
 rg_status rg_get_tuning(rg_handle h, rg_tuning* out);
 
 /* Renderer::set_camera (renderer.rs:158-161): also clears accumulation. An

@@ -97,7 +97,7 @@ class rg_scene_info(C.Structure):
 
 class rg_tuning(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("sort_materials", C.c_uint32), ("bvh_width", C.c_uint32),
-                ("reserved", C.c_uint32 * 5)]
+                ("fetch_budget", C.c_uint32), ("reserved", C.c_uint32 * 4)]
 
 
 class rg_gradients(C.Structure):

@@ -7,7 +7,9 @@ bits); only the time does. A key is
 
 and its entry records the best configuration found and the timings of every
 candidate. Single renders choose between the megakernel and the wavefront
-form and, for the wavefront, the path budget per wave (queue capacity); batches
+form, the tree (binary or 8-wide) and, for the wavefront, the path budget
+per wave (queue capacity), fused or material-sorted shading and the node
+visits between refills of the persistent traversal kernels; batches
 choose the persistent kernel's block size, blocks per SM and the work-item
 granularity of the global queue. Entries live in a JSON file
 (RAYNA_GB300_TUNE_CACHE, default rayna_gb300/tuning_cache.json) and are
@@ -24,7 +26,9 @@ from . import _abi as A
 
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_cache.json")
 
-WAVE_PATHS = [1 << 20, 1 << 22, 1 << 23, 1 << 24]
+WAVE_PATHS = [1 << 22, 1 << 23]
+FETCH_BUDGETS = [4, 8, 16]
+BVH_WIDTHS = [2, 8]
 BATCH_SHAPES = [dict(block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)]
 
 
@@ -76,7 +80,7 @@ class Tuner:
         return sorted(ms)[len(ms) // 2]
 
     def tune_render(self, scene, camera, opts, frames: int = 2, force: bool = False, **renderer_kw) -> dict:
-        """Best {form, wave_paths} for this scene size; measured once per key."""
+        """Best launch configuration for this scene size; measured once per key."""
         from .renderer import Renderer
         from .scene import flatten
         flat = flatten(scene)
@@ -85,17 +89,22 @@ class Tuner:
             return self.lookup(key)
         timings = []
         with Renderer.new_from(scene, camera, opts, 0, form="megakernel", **renderer_kw) as r:
-            timings.append({"form": "megakernel", "wave_paths": 0, "ms": self._frame_ms(r, frames, 1000)})
+            for width in BVH_WIDTHS:
+                r.set_tuning(bvh_width=width)
+                timings.append({"form": "megakernel", "bvh_width": width, "ms": self._frame_ms(r, frames, 1000)})
         with Renderer.new_from(scene, camera, opts, 0, form="wavefront", **renderer_kw) as r:
             for sort in (False, True):
-                for wp in WAVE_PATHS:
-                    if wp < opts.samples:
-                        continue
-                    r.set_wave_paths(wp, sort_materials=sort)
-                    timings.append({"form": "wavefront", "wave_paths": wp, "sort_materials": sort,
-                                    "ms": self._frame_ms(r, frames, 2000)})
+                for width in BVH_WIDTHS:
+                    for budget in FETCH_BUDGETS:
+                        for wp in WAVE_PATHS:
+                            if wp < opts.samples:
+                                continue
+                            r.set_tuning(wave_paths=wp, sort_materials=sort, bvh_width=width, fetch_budget=budget)
+                            timings.append({"form": "wavefront", "wave_paths": wp, "sort_materials": sort,
+                                            "bvh_width": width, "fetch_budget": budget,
+                                            "ms": self._frame_ms(r, frames, 2000)})
         best = min(timings, key=lambda t: t["ms"])
-        cfg = {"form": best["form"], "wave_paths": best["wave_paths"], "sort_materials": best.get("sort_materials", False)}
+        cfg = {k: v for k, v in best.items() if k != "ms"}
         self.store(key, cfg, timings)
         return cfg
 

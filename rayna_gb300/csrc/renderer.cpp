@@ -365,6 +365,11 @@ uint32_t effective_bvh_width(uint32_t requested, const GpuScene& g, uint32_t for
   return (w == 8 && g.n_wnodes > 0) ? 8u : 2u;
 }
 
+bool effective_sort(const rg_renderer* h) {
+  if (h->wf_sort) return h->wf_sort == 1;
+  return h->kinds != F_SPHERE;
+}
+
 void apply_features(rg_renderer* h) {
   h->gs.features = h->kinds | (effective_bvh_width(h->bvh_width, h->gs, h->form) == 8 ? F_WIDE : 0u);
 }
@@ -613,12 +618,14 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   if (!h || !t) return fail(h, RG_INVALID_ARG, "rg_set_tuning: NULL argument");
   for (uint32_t r : t->reserved)
     if (r != 0) return fail(h, RG_INVALID_ARG, "rg_tuning: reserved fields must be 0");
-  if (t->sort_materials > 1) return fail(h, RG_INVALID_ARG, "rg_tuning: sort_materials must be 0 or 1");
+  if (t->sort_materials > 2) return fail(h, RG_INVALID_ARG, "rg_tuning: sort_materials must be 0, 1 or 2");
+  if (t->fetch_budget > 4096) return fail(h, RG_INVALID_ARG, "rg_tuning: fetch_budget must be at most 4096");
   if (t->bvh_width != 0 && t->bvh_width != 2 && t->bvh_width != 8)
     return fail(h, RG_INVALID_ARG, "rg_tuning: bvh_width must be 0, 2 or 8");
   if (t->wave_paths != h->wf_paths && h->wf.arena) free_extra(h);
   h->wf_paths = t->wave_paths;
   h->wf_sort = t->sort_materials;
+  h->wf_budget = t->fetch_budget;
   h->bvh_width = t->bvh_width;
   apply_features(h);
   return RG_OK;
@@ -627,8 +634,9 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
 rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
   if (!h || !out) return fail(h, RG_INVALID_ARG, "rg_get_tuning: NULL argument");
   std::memset(out, 0, sizeof(*out));
-  out->wave_paths = (uint32_t)h->wf_paths;
-  out->sort_materials = h->wf_sort;
+  out->wave_paths = (uint32_t)(h->wf_paths ? h->wf_paths : kDefaultWavePaths);
+  out->sort_materials = effective_sort(h) ? 1u : 2u;
+  out->fetch_budget = h->wf_budget ? h->wf_budget : kDefaultFetchBudget;
   out->bvh_width = effective_bvh_width(h->bvh_width, h->gs, h->form);
   return RG_OK;
 }

@@ -88,7 +88,8 @@ struct rg_renderer {
 
   rg::WavefrontState wf;
   size_t wf_paths = 0;        // wavefront path slots per wave (0: library default)
-  uint32_t wf_sort = 0;       // wavefront: shade in material-kind order (separate extend/shade stages)
+  uint32_t wf_sort = 0;       // wavefront: 1 sorted extend/shade stages, 2 fused bounce kernel, 0 by scene
+  uint32_t wf_budget = 0;     // wavefront: node visits between refills (0: library default)
   uint32_t bvh_width = 0;     // requested traversal: 2, 8, or 0 for the library default
   uint32_t kinds = 0;         // F_* primitive-kind bits of the scene's kernel variant
 
@@ -98,15 +99,22 @@ struct rg_renderer {
 
 namespace rg {
 
-// Traversal width used when the tuning leaves it at 0: the wavefront's
-// traversal kernels are lean enough in registers for the 8-wide test, the
-// megakernel runs faster on the binary tree.
-constexpr uint32_t kDefaultBvhWidthWavefront = 8;
+// Traversal width used when the tuning leaves it at 0. The 8-wide tree
+// visits about a third of the nodes, but each visit tests eight boxes, and
+// every form measured faster on the binary tree.
+constexpr uint32_t kDefaultBvhWidthWavefront = 2;
 constexpr uint32_t kDefaultBvhWidthMegakernel = 2;
+constexpr uint32_t kDefaultFetchBudget = 8;
+// Default path slots per wave (about 0.9 GB of path state).
+constexpr size_t kDefaultWavePaths = size_t(1) << 23;
 
 // Defined in renderer.cpp
 // Traversal width in effect for a request (0 = default) on a scene.
 uint32_t effective_bvh_width(uint32_t requested, const GpuScene& g, uint32_t form);
+// Whether the wavefront shades in material-kind order: as requested, else
+// fused for scenes of spheres only (short traversals, where the extra pass
+// costs more than it saves) and sorted otherwise.
+bool effective_sort(const rg_renderer* h);
 // Kernel variant bits: the scene's primitive kinds, plus F_WIDE when the
 // handle traverses the 8-wide tree.
 void apply_features(rg_renderer* h);

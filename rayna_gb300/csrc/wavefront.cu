@@ -153,17 +153,15 @@ __device__ __forceinline__ void flush_wave_counters(const FrameParams& fp, const
   }
 }
 
-// Node visits a persistent traversal kernel runs between refills.
-constexpr int kFetchBudget = 16;
-
 // One bounce of every live path: closest hit and shading in one kernel,
 // persistent with dynamic ray fetch (Aila & Laine 2009, "replacing terminated
-// rays"): a warp keeps 32 paths in flight, traverses for a bounded number of
-// node visits, and a lane whose traversal has finished shades its path and
+// rays"): a warp keeps 32 paths in flight, traverses for `budget` node visits
+// at a time, and a lane whose traversal has finished shades its path and
 // then takes the next one from the queue (one atomic per warp and refill), so
 // lanes do not idle while the warp's longest ray finishes.
 template <uint32_t F, bool COUNT>
-__global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur) {
+__global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
+                                                     int budget) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   const int nxt = cur ^ 1;
   uint32_t* next = s.counts + kFetchCounter;
@@ -204,7 +202,7 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
     if (!__any_sync(0xffffffffu, has)) break;
     if (has) {
       const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
-      if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, kFetchBudget)) {
+      if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget)) {
         HitRec h;
         const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
         if (shade_path<F>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
@@ -222,7 +220,7 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
 // Material-sorted variant, stage 1: closest hit; each path goes to the queue
 // of its hit's material kind. The kernel is persistent with dynamic ray fetch
 // (Aila & Laine 2009, "replacing terminated rays"): a warp keeps 32 rays in
-// flight, traverses for a bounded number of node visits, and lanes whose ray
+// flight, traverses for `budget` node visits at a time, and lanes whose ray
 // has finished take the next rays from the queue (one atomic per warp), so
 // lanes do not idle while the warp's longest ray finishes.
 
@@ -259,7 +257,8 @@ __device__ __forceinline__ void record_hit(const GpuScene& sc, const FrameParams
 }
 
 template <uint32_t F, bool COUNT>
-__global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur) {
+__global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
+                                                     int budget) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
@@ -297,7 +296,7 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
     if (!__any_sync(0xffffffffu, has)) break;
     if (has) {
       const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
-      if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, kFetchBudget)) {
+      if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget)) {
         HitRec h;
         const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
         record_hit<F, COUNT>(sc, fp, s, wp, p, hit, h);
@@ -445,7 +444,8 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   const size_t spp = fp.spp;
   const size_t n_pix = (size_t)fp.width * fp.height;
   const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
-  const bool sorted = h->wf_sort != 0;
+  const bool sorted = effective_sort(h);
+  const int budget = (int)(h->wf_budget ? h->wf_budget : kDefaultFetchBudget);
   const int grid = sm_count(h->device) * 8;
   // The persistent traversal kernels run as many blocks as are resident at once.
   int ext_per_sm = 0;
@@ -474,12 +474,12 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
       if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
       if (sorted) {
         if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
-        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-        else k_extend<F, false><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
+        else k_extend<F, false><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
         k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
       } else {
-        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
-        else k_bounce<F, false><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
+        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
+        else k_bounce<F, false><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
       }
       cur ^= 1;
     }
@@ -498,8 +498,6 @@ cudaError_t run_frame(rg_renderer* h, const FrameParams& fp, const PathState& s,
 
 }  // namespace
 
-// Default path budget per wave: 2^23 slots (about 700 MB of path state).
-constexpr size_t kDefaultWavePaths = size_t(1) << 23;
 
 cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp) {
   const size_t spp = fp.spp;

@@ -85,13 +85,16 @@ class Renderer:
 
     @classmethod
     def tuned(cls, scene: Scene, camera: Camera, options: RenderOpts, tuner=None, **kw) -> "Renderer":
-        """A renderer with the kernel form and wave size the autotuner picked
-        for this scene size (measured on first sight of the size, then cached)."""
+        """A renderer with the kernel form and launch knobs the autotuner
+        picked for this scene size (measured on first sight of the size, then
+        cached)."""
         from .autotune import Tuner
         cfg = (tuner or Tuner()).tune_render(scene, camera, options, **kw)
         r = cls(scene, camera, options, form=cfg["form"], **kw)
+        r.set_tuning(bvh_width=cfg.get("bvh_width", 0))
         if cfg["form"] == "wavefront":
-            r.set_wave_paths(cfg["wave_paths"], sort_materials=cfg.get("sort_materials", False))
+            r.set_tuning(wave_paths=cfg["wave_paths"], sort_materials=cfg.get("sort_materials", False),
+                         fetch_budget=cfg.get("fetch_budget", 0))
         return r
 
     @classmethod
@@ -205,26 +208,31 @@ class Renderer:
         return m
 
     def set_tuning(self, wave_paths: int | None = None, sort_materials: bool | None = None,
-                   bvh_width: int | None = None):
+                   bvh_width: int | None = None, fetch_budget: int | None = None):
         """Launch knobs (rg_tuning); None leaves a knob as it is. wave_paths:
         wavefront path slots per wave (0 = library default); sort_materials:
-        wavefront shading in material-kind order; bvh_width: 2 (binary node
-        pairs) or 8 (compressed 8-wide nodes), 0 = library default."""
+        wavefront shading in material-kind order (True) or one fused bounce
+        kernel (False); bvh_width: 2 (binary node pairs) or 8 (compressed
+        8-wide nodes), 0 = library default; fetch_budget: node visits a
+        wavefront lane traverses between refills (0 = library default)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
         if wave_paths is not None:
             t.wave_paths = int(wave_paths)
         if sort_materials is not None:
-            t.sort_materials = 1 if sort_materials else 0
+            t.sort_materials = 1 if sort_materials else 2
         if bvh_width is not None:
             t.bvh_width = int(bvh_width)
+        if fetch_budget is not None:
+            t.fetch_budget = int(fetch_budget)
         self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
 
     def tuning(self) -> dict:
-        """The knobs in effect (bvh_width is the traversal actually used)."""
+        """The knobs in effect (library defaults resolved)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
-        return {"wave_paths": t.wave_paths, "sort_materials": bool(t.sort_materials), "bvh_width": t.bvh_width}
+        return {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials == 1, "bvh_width": t.bvh_width,
+                "fetch_budget": t.fetch_budget}
 
     def set_wave_paths(self, n: int, sort_materials: bool | None = None):
         """Wavefront path slots per wave (0: library default) and, optionally,
