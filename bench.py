@@ -239,6 +239,14 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes (read + write) per ray segment of the traversal kernels, from an
+# ncu capture of every traversal launch of one frame (profiles/), by
+# (workload, form, BVH width); scaled to a frame by its ray segments.
+DRAM_BYTES_PER_SEGMENT = {
+    # 18 k_extend launches of one 512x512x64 frame: 20.76 GB over 86.67 M segments
+    ("mesh", "wavefront", 2): 239.5,
+}
+
 # Kernel configurations timed per workload: (form, material-sorted shading,
 # BVH width). "megakernel" is the plain form: one thread per pixel-sample over
 # binary node pairs.
@@ -283,7 +291,8 @@ def run_gpu(args, rank, world):
     for form in forms:
         kind, sort, width = FORMS[form]
         try:
-            r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank)
+            r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank,
+                                  stage_times=True)
             r.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
         except A.RaynaError as e:
             results[form] = {"error": str(e)}
@@ -304,6 +313,7 @@ def run_gpu(args, rank, world):
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
         rays = 0
         torch.cuda.synchronize()
+        traverse_ms = 0.0
         with ClockSampler(dev) as clk:
             w0 = time.perf_counter()
             for k in range(args.steps):
@@ -311,9 +321,11 @@ def run_gpu(args, rank, world):
                 starts[k].record(stream)
                 A.check(lib, h, lib.rg_render_async(h, r.next_seed(), None, C.byref(st)))
                 ends[k].record(stream)
+                # the traversal kernels' own event pairs, read back after each frame
+                A.check(lib, h, lib.rg_sync_stats(h, C.byref(st)))
+                traverse_ms += st.traverse_ms
             torch.cuda.synchronize()
             wall = time.perf_counter() - w0
-        A.check(lib, h, lib.rg_sync_stats(h, C.byref(st)))
         if dist:
             dist.barrier()
         ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
@@ -343,6 +355,7 @@ def run_gpu(args, rank, world):
             "rays_per_frame": cst.rays, "node_visits": cst.node_visits, "prim_tests": cst.prim_tests,
             "sdf_steps": cst.sdf_steps, "wall_s": wall, "clocks": clk.summary(), "device_ms": ms,
             "launches_per_frame": st.kernel_launches, "bvh_width": width,
+            "traverse_ms_per_step": traverse_ms / args.steps,
         }
         r.close()
     if rank != 0:
@@ -352,9 +365,16 @@ def run_gpu(args, rank, world):
     b = ok[best]
     hbm, peak_kind = measured_peaks()
     npx = opts.width * opts.height
+    # Roofline of the dominant kernels, the traversal launches of a frame (the
+    # megakernel, or the wavefront's extend / bounce kernels), timed live with
+    # their own CUDA events: algorithmic bytes = one node fetch per node visit
+    # (64 B pair, 80 B wide node) + 48 B per primitive test + the 48-byte path
+    # record per ray segment.
     node_bytes = 80 if b["bvh_width"] == 8 else 64
-    alg_bytes = node_bytes * b["node_visits"] + 48 * b["prim_tests"] + 32 * b["rays_per_frame"] + 12 * npx
-    achieved = alg_bytes / (b["ms_per_step"] / 1e3) / 1e9
+    alg_bytes = node_bytes * b["node_visits"] + 48 * b["prim_tests"] + 48 * b["rays_per_frame"]
+    achieved = alg_bytes / (b["traverse_ms_per_step"] / 1e3) / 1e9
+    dram_per_segment = DRAM_BYTES_PER_SEGMENT.get((args.workload, FORMS[best][0], FORMS[best][2]))
+    traffic = dram_per_segment * b["rays_per_frame"] if dram_per_segment else None
     line = {
         "metric": "Msamples/s", "value": b["msamples_s"], "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
@@ -369,8 +389,9 @@ def run_gpu(args, rank, world):
                                          "bvh_width")} if "error" not in v
                   else v for f, v in results.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_kind": peak_kind, "traffic": None,
-                     "algorithmic_bytes_per_frame": alg_bytes},
+                     "peak_kind": peak_kind, "traffic": traffic, "per": "frame (all traversal launches of one frame)",
+                     "algorithmic_bytes": alg_bytes, "kernel_ms": b["traverse_ms_per_step"],
+                     "kernel_share": b["traverse_ms_per_step"] / b["ms_per_step"]},
         "gpu_launches": b["launches_per_frame"] * args.steps,
         "clocks": b["clocks"],
     }

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 2u
+#define RG_ABI_VERSION 3u
 
 /* Status codes. 0 is success. */
 typedef enum rg_status {
@@ -185,7 +185,10 @@ typedef struct rg_device_opts {
     uint32_t flags;        /* RG_FLAG_* */
 } rg_device_opts;
 
-enum { RG_FLAG_COUNTERS = 1u };  /* maintain device work counters (node visits, tests) for the roofline */
+enum {
+    RG_FLAG_COUNTERS = 1u,     /* maintain device work counters (node visits, tests) for the roofline */
+    RG_FLAG_STAGE_TIMES = 2u   /* time the traversal kernels of each frame with CUDA events (traverse_ms) */
+};
 
 /* RenderStats (render/render.rs:4-15) plus device figures. */
 typedef struct rg_render_stats {
@@ -202,6 +205,8 @@ typedef struct rg_render_stats {
     uint32_t num_threads;     /* 0: the device renders */
     uint32_t error_flags;     /* device-side error bits seen this frame (0 = none) */
     uint32_t kernel_launches; /* kernels the library launched for this frame */
+    double traverse_ms;       /* device time of the frame's traversal kernels (RG_FLAG_STAGE_TIMES only, else 0):
+                                 the megakernel, or the wavefront's extend / bounce launches */
 } rg_render_stats;
 
 /* Hit record of rg_query_rays. */

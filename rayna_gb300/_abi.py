@@ -36,6 +36,7 @@ RG_BOUNDARY_SPHERE, RG_BOUNDARY_BOX = range(2)
 RG_SDF_SPHERE, RG_SDF_TORUS, RG_SDF_MANDELBULB = range(3)
 RG_FORM_MEGAKERNEL, RG_FORM_WAVEFRONT = range(2)
 RG_FLAG_COUNTERS = 1
+RG_FLAG_STAGE_TIMES = 2
 
 
 class rg_material(C.Structure):
@@ -85,7 +86,7 @@ class rg_render_stats(C.Structure):
                 ("rays", C.c_uint64), ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64),
                 ("sdf_steps", C.c_uint64), ("accum_frames", C.c_uint32), ("img_width", C.c_uint32),
                 ("img_height", C.c_uint32), ("num_threads", C.c_uint32), ("error_flags", C.c_uint32),
-                ("kernel_launches", C.c_uint32)]
+                ("kernel_launches", C.c_uint32), ("traverse_ms", C.c_double)]
 
 
 class rg_scene_info(C.Structure):

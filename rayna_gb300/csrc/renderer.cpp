@@ -365,6 +365,16 @@ uint32_t effective_bvh_width(uint32_t requested, const GpuScene& g, uint32_t for
   return (w == 8 && g.n_wnodes > 0) ? 8u : 2u;
 }
 
+cudaError_t stage_mark(rg_renderer* h) {
+  if (h->stage_used == h->stage_ev.size()) {
+    cudaEvent_t ev;
+    cudaError_t e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) return e;
+    h->stage_ev.push_back(ev);
+  }
+  return cudaEventRecord(h->stage_ev[h->stage_used++], h->stream);
+}
+
 bool effective_sort(const rg_renderer* h) {
   if (h->wf_sort) return h->wf_sort == 1;
   return h->kinds != F_SPHERE;
@@ -494,6 +504,7 @@ rg_status rg_destroy(rg_handle h) {
   dfree(h->d_counters); dfree(h->d_err);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  for (cudaEvent_t ev : h->stage_ev) cudaEventDestroy(ev);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return RG_OK;
@@ -673,8 +684,14 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
   RG_CUDA(h, cudaEventRecord(h->ev0, h->stream), "event");
   cudaError_t e;
   h->last_launches = 1;
-  if (h->form == RG_FORM_WAVEFRONT) e = launch_wavefront(h, fp);
-  else e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream);
+  h->stage_used = 0;
+  if (h->form == RG_FORM_WAVEFRONT) {
+    e = launch_wavefront(h, fp);
+  } else {
+    if ((h->flags & RG_FLAG_STAGE_TIMES) && (e = stage_mark(h)) != cudaSuccess) return cuda_fail(h, e, "stage event");
+    e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream);
+    if (e == cudaSuccess && (h->flags & RG_FLAG_STAGE_TIMES)) e = stage_mark(h);
+  }
   if (e != cudaSuccess) return cuda_fail(h, e, "render launch");
   RG_CUDA(h, cudaEventRecord(h->ev1, h->stream), "event");
   h->last_samples = (uint64_t)fp.width * fp.height * fp.spp;
@@ -712,8 +729,15 @@ rg_status rg_sync_stats(rg_handle h, rg_render_stats* stats) {
   stats->num_threads = 0;
   stats->error_flags = err;
   stats->kernel_launches = h->last_launches;
+  stats->traverse_ms = 0.0;
+  for (uint32_t i = 0; i + 1 < h->stage_used; i += 2) {
+    float t = 0.0f;
+    if (cudaEventElapsedTime(&t, h->stage_ev[i], h->stage_ev[i + 1]) != cudaSuccess) { cudaGetLastError(); t = 0.0f; }
+    stats->traverse_ms += t;
+  }
   return RG_OK;
 }
+
 
 rg_status rg_render(rg_handle h, uint64_t seed, float* out_rgb, rg_render_stats* stats) {
   if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");

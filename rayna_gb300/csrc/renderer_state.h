@@ -81,6 +81,8 @@ struct rg_renderer {
   uint32_t pixel_accum = 0;   // AccumulationValue::accum (per pixel; equal for all pixels)
   uint64_t last_samples = 0;
   uint32_t last_launches = 0; // kernels launched by the last frame
+  std::vector<cudaEvent_t> stage_ev;  // RG_FLAG_STAGE_TIMES: (start, end) pairs of traversal launches
+  uint32_t stage_used = 0;            // events of stage_ev recorded by the last frame
 
   unsigned long long* d_counters = nullptr;
   uint32_t* d_err = nullptr;
@@ -109,6 +111,9 @@ constexpr uint32_t kDefaultFetchBudget = 8;
 constexpr size_t kDefaultWavePaths = size_t(1) << 23;
 
 // Defined in renderer.cpp
+// RG_FLAG_STAGE_TIMES: records the next event of the frame's traversal timing
+// (start before a traversal launch, end after it) on the handle's stream.
+cudaError_t stage_mark(rg_renderer* h);
 // Traversal width in effect for a request (0 = default) on a scene.
 uint32_t effective_bvh_width(uint32_t requested, const GpuScene& g, uint32_t form);
 // Whether the wavefront shades in material-kind order: as requested, else

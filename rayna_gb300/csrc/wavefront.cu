@@ -445,6 +445,7 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   const size_t n_pix = (size_t)fp.width * fp.height;
   const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
   const bool sorted = effective_sort(h);
+  const bool timed = (h->flags & RG_FLAG_STAGE_TIMES) != 0;
   const int budget = (int)(h->wf_budget ? h->wf_budget : kDefaultFetchBudget);
   const int grid = sm_count(h->device) * 8;
   // The persistent traversal kernels run as many blocks as are resident at once.
@@ -474,12 +475,16 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
       if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
       if (sorted) {
         if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
+        if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
         if (counters) k_extend<F, true><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
         else k_extend<F, false><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
+        if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
         k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
       } else {
+        if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
         if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
         else k_bounce<F, false><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
+        if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
       }
       cur ^= 1;
     }

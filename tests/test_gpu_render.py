@@ -222,3 +222,16 @@ def test_wavefront_small_waves():
         r.set_wave_paths(1000)
         img = r.render(seed=77).img
     np.testing.assert_array_equal(ref, img)
+
+
+@pytest.mark.parametrize("form", ["megakernel", "wavefront"])
+def test_stage_times_bracket_the_traversal(form):
+    """RG_FLAG_STAGE_TIMES: the traversal kernels' time is positive and part
+    of the frame's kernel time; the image is unchanged by the timing."""
+    scene, cam, opts = CASES["cornell_mesh"]()
+    with Renderer.new_from(scene, cam, opts, 0, form=form) as r:
+        ref = r.render(seed=31).img
+    with Renderer.new_from(scene, cam, opts, 0, form=form, stage_times=True) as r:
+        out = r.render(seed=31)
+    np.testing.assert_array_equal(ref, out.img)
+    assert 0.0 < out.stats.traverse_ms <= out.stats.kernel_ms * 1.001 + 1e-3
