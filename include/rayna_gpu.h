@@ -334,12 +334,21 @@ rg_status rg_query_rays(rg_handle h, uint32_t n, const float* origins, const flo
 typedef struct rg_batch* rg_batch_handle;
 
 /* Launch shape of the persistent batch kernel (what the autotuner sets). */
+/* Batched forms (rg_batch_tuning.form). */
+enum {
+    RG_BATCH_WAVEFRONT = 0,  /* default: the paths of every render in shared waves of path slots; one persistent
+                                dynamic-fetch bounce launch per bounce serves all renders */
+    RG_BATCH_TILES = 1       /* one persistent launch whose warps take (render, tile) items, megakernel style */
+};
+
 typedef struct rg_batch_tuning {
-    uint32_t block;            /* threads per block, multiple of 32 in [64, 512]; 0 = 256 */
-    uint32_t blocks_per_sm;    /* blocks launched per SM; 0 = as many as fit */
-    uint32_t rounds_per_item;  /* warp rounds of pixels per work item taken from the queue; 0 = 4 */
+    uint32_t block;            /* RG_BATCH_TILES: threads per block, multiple of 32 in [64, 512]; 0 = 256 */
+    uint32_t blocks_per_sm;    /* RG_BATCH_TILES: blocks launched per SM; 0 = as many as fit */
+    uint32_t rounds_per_item;  /* RG_BATCH_TILES: warp rounds of pixels per work item; 0 = 4 */
     uint32_t bvh_width;        /* 2 or 8 as in rg_tuning; 0 = library default (2) */
-    uint32_t reserved[4];      /* must be 0 */
+    uint32_t form;             /* RG_BATCH_WAVEFRONT or RG_BATCH_TILES */
+    uint32_t wave_paths;       /* RG_BATCH_WAVEFRONT: path slots per wave; 0 = min(2^23, all paths of a frame) */
+    uint32_t reserved[2];      /* must be 0 */
 } rg_batch_tuning;
 
 /* Creates a batch of `n` independent renders (scene, camera, options each,
@@ -350,11 +359,14 @@ rg_status rg_batch_destroy(rg_batch_handle b);
 rg_status rg_batch_last_error(rg_batch_handle b, char* buf, size_t len);
 rg_status rg_batch_set_tuning(rg_batch_handle b, const rg_batch_tuning* t);
 
-/* Adds one frame to every render of the batch in a single persistent launch:
- * warps take (scene, tile) work items from one global queue until it is empty
- * (work stealing by atomic counter). The frame's launch sequence is captured
- * once as a CUDA graph and replayed. Render i uses the frame key
- * splitmix64(seed + i). Waits for the device; stats cover the whole batch. */
+/* Adds one frame to every render of the batch. RG_BATCH_WAVEFRONT (default):
+ * the paths of all renders fill shared waves of path slots and each bounce is
+ * one persistent launch over every render's live paths, warps refilling idle
+ * lanes from one queue (work stealing by atomic counter). RG_BATCH_TILES: one
+ * persistent launch whose warps take (scene, tile) work items from one global
+ * queue. Either way the frame's launch sequence is captured once as a CUDA
+ * graph and replayed. Render i uses the frame key splitmix64(seed + i). Waits
+ * for the device; stats cover the whole batch. */
 rg_status rg_batch_render(rg_batch_handle b, uint64_t seed, rg_render_stats* stats);
 
 /* The same frame as one megakernel launch per render, in sequence (the

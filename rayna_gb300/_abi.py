@@ -37,6 +37,8 @@ RG_SDF_SPHERE, RG_SDF_TORUS, RG_SDF_MANDELBULB = range(3)
 RG_FORM_MEGAKERNEL, RG_FORM_WAVEFRONT = range(2)
 RG_FLAG_COUNTERS = 1
 RG_FLAG_STAGE_TIMES = 2
+RG_BATCH_WAVEFRONT = 0
+RG_BATCH_TILES = 1
 
 
 class rg_material(C.Structure):
@@ -108,7 +110,8 @@ class rg_gradients(C.Structure):
 
 class rg_batch_tuning(C.Structure):
     _fields_ = [("block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("rounds_per_item", C.c_uint32),
-                ("bvh_width", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+                ("bvh_width", C.c_uint32), ("form", C.c_uint32), ("wave_paths", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 class rg_hit(C.Structure):

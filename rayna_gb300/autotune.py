@@ -10,8 +10,9 @@ candidate. Single renders choose between the megakernel and the wavefront
 form, the tree (binary or 8-wide) and, for the wavefront, the path budget
 per wave (queue capacity), fused or material-sorted shading and the node
 visits between refills of the persistent traversal kernels; batches
-choose the persistent kernel's block size, blocks per SM and the work-item
-granularity of the global queue. Entries live in a JSON file
+choose the batched form (wavefront with its path slots per wave, or tiles with
+the persistent kernel's block size, blocks per SM and the work-item
+granularity of the global queue). Entries live in a JSON file
 (RAYNA_GB300_TUNE_CACHE, default rayna_gb300/tuning_cache.json) and are
 measured with CUDA events on the device the first time a key is seen.
 """
@@ -29,7 +30,8 @@ DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning
 WAVE_PATHS = [1 << 22, 1 << 23]
 FETCH_BUDGETS = [4, 8, 16]
 BVH_WIDTHS = [2, 8]
-BATCH_SHAPES = [dict(block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)]
+BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 22, 1 << 23)] +
+                [dict(form="tiles", block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)])
 
 
 def _bucket(n: int) -> int:
@@ -131,7 +133,7 @@ class Tuner:
                 ms.append(batch.render(seed=2 + k).kernel_ms)
             timings.append(dict(shape, ms=sorted(ms)[len(ms) // 2]))
         best = min(timings, key=lambda t: t["ms"])
-        cfg = {k: best[k] for k in ("block", "blocks_per_sm", "rounds_per_item")}
+        cfg = {k: v for k, v in best.items() if k != "ms"}
         batch.set_tuning(**cfg)
         self.store(key, cfg, timings)
         return cfg

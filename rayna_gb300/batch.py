@@ -1,9 +1,11 @@
 """BatchRenderer — many independent renders in one persistent launch.
 
 Wraps rg_batch_* of include/rayna_gpu.h. `render()` adds one frame to every
-render with one work-stealing launch over a global (scene, tile) queue,
-replayed as a CUDA graph; `render_sequential()` produces the same frame with
-one megakernel launch per render (the comparison form).
+render: by default as a batched wavefront (the paths of all renders in shared
+waves, one persistent work-stealing launch per bounce), or as one persistent
+launch over a global (scene, tile) queue; the frame is replayed as a CUDA
+graph. `render_sequential()` produces the same frame with one megakernel
+launch per render (the comparison form).
 """
 from __future__ import annotations
 
@@ -62,10 +64,17 @@ class BatchRenderer:
     def n_samples(self) -> int:
         return sum(o.width * o.height * o.samples for _, _, o in self.items)
 
-    def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, rounds_per_item: int = 0, bvh_width: int = 0):
+    def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, rounds_per_item: int = 0, bvh_width: int = 0,
+                   form="wavefront", wave_paths: int = 0):
+        """rg_batch_tuning. form: "wavefront" (shared waves of path slots, the
+        default) or "tiles" (a persistent megakernel over (render, tile) work
+        items); block / blocks_per_sm / rounds_per_item shape the tile form,
+        wave_paths the wavefront's path slots per wave (0 = library default)."""
         t = A.rg_batch_tuning()
         t.block, t.blocks_per_sm, t.rounds_per_item = int(block), int(blocks_per_sm), int(rounds_per_item)
         t.bvh_width = int(bvh_width)
+        t.form = {"wavefront": A.RG_BATCH_WAVEFRONT, "tiles": A.RG_BATCH_TILES}.get(form, form)
+        t.wave_paths = int(wave_paths)
         self._check(self._lib.rg_batch_set_tuning(self._h, C.byref(t)))
 
     def next_seed(self) -> int:

@@ -1,17 +1,29 @@
-// batch.cu — many renders in one persistent launch.
+// batch.cu — many renders in one graph-replayed frame.
 //
 // Every render of a batch is an ordinary handle (its own scene buffers,
-// camera, options and accumulation). A frame of the whole batch is one
-// launch of k_batch: as many blocks as fit on the SMs, whose warps take work
-// items from one global queue (an atomic counter) until it is empty. A work
-// item is `rounds_per_item` consecutive warp rounds (mega.cuh) of one render;
-// items of all renders are numbered one after another, so a warp finds its
-// render by a binary search over the prefix sums of item counts. Renders of
-// uneven size therefore share the GPU without a tail of idle SMs per render.
+// camera, options and accumulation). Two batched forms:
 //
-// The frame's launch sequence (parameter table upload, counter reset, kernel)
-// is captured once as a CUDA graph and replayed; the host only rewrites the
-// pinned parameter table (frame keys, accumulation counts) before each replay.
+// RG_BATCH_WAVEFRONT (default). The paths of all renders fill shared waves of
+// path slots: a wave is a list of chunks (render, run of whole pixels), laid
+// out one after another, and each slot remembers its chunk. Per wave:
+// k_bgenerate (camera rays of every chunk), one persistent dynamic-fetch
+// k_bbounce per bounce over the live paths of all renders (each lane reads
+// its render's scene and frame parameters through its chunk), and
+// k_baccumulate (per-pixel sums in the canonical order into each render's
+// accumulation buffer). Renders of uneven size share every launch, so no
+// render's tail leaves SMs idle and small renders cost no launch of their own.
+//
+// RG_BATCH_TILES. One launch of k_batch: as many blocks as fit on the SMs,
+// whose warps take work items from one global queue (an atomic counter) until
+// it is empty. A work item is `rounds_per_item` consecutive warp rounds
+// (mega.cuh) of one render; items of all renders are numbered one after
+// another, so a warp finds its render by a binary search over the prefix sums
+// of item counts.
+//
+// The frame's launch sequence (parameter table upload, counter resets,
+// kernels) is captured once as a CUDA graph and replayed; the host only
+// rewrites the pinned parameter table (frame keys, accumulation counts)
+// before each replay.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,12 +38,24 @@
 #include "kernels.h"
 #include "mega.cuh"
 #include "renderer_state.h"
+#include "wavefront.cuh"
 
 namespace rg {
 
 struct BatchItemDev {
   GpuScene sc;
   FrameParams fp;
+};
+
+// A run of whole pixels of one render inside a wave.
+struct BatchChunk {
+  uint32_t item;         // render index
+  uint32_t first_pixel;  // first pixel (row-major index) of the run in its render
+  uint32_t n_pixels;
+  uint32_t spp;
+  uint32_t slot0;        // first path slot of the run in the wave
+  uint32_t pix0;         // position of the run's first pixel among the wave's pixels
+  uint32_t pad[2];
 };
 
 namespace {
@@ -69,6 +93,127 @@ __global__ void k_batch(const BatchItemDev* __restrict__ items, const uint32_t* 
   flush_counters<false>(f0, cnt, segments);
 }
 
+// ---------------------------------------------------------------------------
+// Batched wavefront
+// ---------------------------------------------------------------------------
+// Largest c in [first, first + n) with key(c) <= v (chunks are in ascending key order).
+template <class Key>
+__device__ __forceinline__ uint32_t find_chunk(uint32_t first, uint32_t n, uint32_t v, Key key) {
+  uint32_t lo = first, hi = first + n;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (key(mid) <= v) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kWfBlock) k_bgenerate(const BatchItemDev* __restrict__ items,
+                                                        const BatchChunk* __restrict__ chunks, uint32_t first_chunk,
+                                                        uint32_t n_chunks, uint32_t n_paths, PathState s,
+                                                        uint32_t* __restrict__ chunk_of) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    s.counts[0] = n_paths;
+    s.counts[1] = 0;
+  }
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_paths; p += gridDim.x * blockDim.x) {
+    const uint32_t c = find_chunk(first_chunk, n_chunks, p, [&](uint32_t i) { return chunks[i].slot0; });
+    const BatchChunk ch = chunks[c];
+    const FrameParams& fp = items[ch.item].fp;
+    const uint32_t rel = p - ch.slot0;
+    const uint32_t pix = ch.first_pixel + rel / ch.spp, smp = rel % ch.spp;
+    const uint32_t x = pix % fp.width, y = pix / fp.width;
+    RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, 0, nullptr};
+    Ray r = camera_ray(fp, x, y, smp, ctx);
+    store_path(s, p, r.o, 0, r.d, C3f{1.0f, 1.0f, 1.0f});
+    s.active[0][p] = p;
+    chunk_of[p] = c;
+  }
+}
+
+// One bounce of the live paths of every render of the wave: closest hit and
+// shading, persistent with dynamic ray fetch as in the single-render form; a
+// lane reads its render's scene and frame parameters through its chunk.
+template <uint32_t F>
+__global__ void __launch_bounds__(kWfBlock) k_bbounce(const BatchItemDev* __restrict__ items,
+                                                      const BatchChunk* __restrict__ chunks, WaveParams wp, PathState s,
+                                                      const uint32_t* __restrict__ chunk_of, int cur, int budget,
+                                                      uint32_t* err, unsigned long long* counters) {
+  const uint32_t n = clamp_count(s.counts[cur], wp, err);
+  const int nxt = cur ^ 1;
+  uint32_t* next = s.counts + kFetchCounter;
+  const uint32_t lane = threadIdx.x & 31u;
+  Counters cnt;
+  uint32_t queries = 0;
+  bool has = false, drained = false;
+  uint32_t p = 0, pix = 0, smp = 0, depth = 0, item = 0;
+  Ray r;
+  C3f beta;
+  Traversal t;
+  uint2 stack[kTravStack];
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !has);
+    if (idle && !drained) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(next, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= n) drained = true;
+      if (!has) {
+        const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (i < n) {
+          p = s.active[cur][i];
+          const BatchChunk ch = chunks[chunk_of[p]];
+          item = ch.item;
+          const uint32_t rel = p - ch.slot0;
+          pix = ch.first_pixel + rel / ch.spp;
+          smp = rel % ch.spp;
+          const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1], r2 = s.rec[3 * (size_t)p + 2];
+          depth = __float_as_uint(r0.w);
+          r.o = v3(r0.x, r0.y, r0.z);
+          r.d = v3(r1.x, r1.y, r1.z);
+          r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
+          beta = C3f{r2.x, r2.y, r2.z};
+          trav_init<F>(t, items[item].sc, r, 3.402823466e38f);
+          has = true;
+          ++queries;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, has)) break;
+    if (has) {
+      const GpuScene& sc = items[item].sc;
+      const FrameParams& fp = items[item].fp;
+      const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
+      if (trav_run<F, false, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget)) {
+        HitRec h;
+        const bool hit = finish_hit<F, false>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
+        if (shade_path<F>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
+          uint32_t slot = warp_append(s.counts + nxt, true);
+          if (slot < wp.n_paths) s.active[nxt][slot] = p;
+          else atomicOr(err, ERR_QUEUE_OVERFLOW);
+        }
+        has = false;
+      }
+    }
+  }
+  FrameParams f0;
+  f0.counters = counters;
+  flush_wave_counters<false>(f0, cnt, queries);
+}
+
+// Per-pixel sums of every render of the wave, in the canonical order.
+__global__ void __launch_bounds__(kWfBlock) k_baccumulate(const BatchItemDev* __restrict__ items,
+                                                          const BatchChunk* __restrict__ chunks, uint32_t first_chunk,
+                                                          uint32_t n_chunks, uint32_t n_pixels, PathState s) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n_pixels * 3; q += gridDim.x * blockDim.x) {
+    const uint32_t lp = q / 3, c = q % 3;
+    const uint32_t k = find_chunk(first_chunk, n_chunks, lp, [&](uint32_t i) { return chunks[i].pix0; });
+    const BatchChunk ch = chunks[k];
+    const uint32_t rel = lp - ch.pix0;
+    accumulate_pixel(items[ch.item].fp, s, (size_t)ch.slot0 + (size_t)rel * ch.spp, ch.first_pixel + rel, c);
+  }
+}
+
 uint64_t splitmix64(uint64_t z) {
   z += 0x9E3779B97F4A7C15ull;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -98,6 +243,16 @@ struct rg_batch {
   rg_batch_tuning tuning{};
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint32_t launches = 0;            // kernels of one frame
+  // RG_BATCH_WAVEFRONT
+  struct Wave {
+    uint32_t first_chunk, n_chunks, n_paths, n_pixels, max_depth;
+  };
+  std::vector<Wave> waves;
+  BatchChunk* d_chunks = nullptr;
+  void* wf_arena = nullptr;         // path state of one wave + per-slot chunk index
+  size_t wf_cap = 0;
+  uint32_t* d_err = nullptr;        // queue overflows of the batched kernels
 };
 
 namespace {
@@ -128,6 +283,99 @@ void drop_graph(rg_batch* b) {
   b->graph = nullptr;
 }
 
+// Waves of the batched wavefront: renders in order, each cut into runs of
+// whole pixels that fill waves of `cap` path slots.
+rg_status plan_waves(rg_batch* b) {
+  uint64_t total = 0;
+  for (rg_renderer* h : b->items) total += (uint64_t)h->opts.width * h->opts.height * h->opts.samples;
+  uint64_t cap = b->tuning.wave_paths ? b->tuning.wave_paths : std::min<uint64_t>(kDefaultWavePaths, total);
+  for (rg_renderer* h : b->items) cap = std::max<uint64_t>(cap, h->opts.samples);  // a wave holds whole pixels
+  if (cap > 0x7FFFFFFFull) return bfail(b, RG_INVALID_ARG, "wave_paths too large");
+  std::vector<BatchChunk> chunks;
+  b->waves.clear();
+  rg_batch::Wave cur{0, 0, 0, 0, 0};
+  auto close = [&]() {
+    if (cur.n_chunks) b->waves.push_back(cur);
+    cur = rg_batch::Wave{(uint32_t)chunks.size(), 0, 0, 0, 0};
+  };
+  for (size_t i = 0; i < b->items.size(); ++i) {
+    const rg_render_opts& o = b->items[i]->opts;
+    const uint64_t npix = (uint64_t)o.width * o.height;
+    uint64_t done = 0;
+    while (done < npix) {
+      uint64_t fit = (cap - cur.n_paths) / o.samples;
+      if (fit == 0) { close(); continue; }
+      const uint64_t take = std::min(fit, npix - done);
+      BatchChunk c{};
+      c.item = (uint32_t)i;
+      c.first_pixel = (uint32_t)done;
+      c.n_pixels = (uint32_t)take;
+      c.spp = o.samples;
+      c.slot0 = cur.n_paths;
+      c.pix0 = cur.n_pixels;
+      chunks.push_back(c);
+      cur.n_chunks += 1;
+      cur.n_paths += (uint32_t)(take * o.samples);
+      cur.n_pixels += (uint32_t)take;
+      cur.max_depth = std::max(cur.max_depth, o.ray_depth);
+      done += take;
+    }
+  }
+  close();
+  if (b->d_chunks) cudaFree(b->d_chunks);
+  b->d_chunks = nullptr;
+  BCUDA(b, cudaMalloc((void**)&b->d_chunks, std::max<size_t>(1, chunks.size()) * sizeof(BatchChunk)), "batch waves");
+  if (!chunks.empty())
+    BCUDA(b, cudaMemcpy(b->d_chunks, chunks.data(), chunks.size() * sizeof(BatchChunk), cudaMemcpyHostToDevice), "batch waves");
+  if (b->wf_cap != cap) {
+    if (b->wf_arena) cudaFree(b->wf_arena);
+    b->wf_arena = nullptr;
+    b->wf_cap = 0;
+    BCUDA(b, cudaMalloc(&b->wf_arena, arena_bytes(cap) + cap * sizeof(uint32_t)), "batch path state");
+    b->wf_cap = cap;
+  }
+  return RG_OK;
+}
+
+template <uint32_t F>
+cudaError_t launch_batch_wavefront(rg_batch* b) {
+  PathState s;
+  const size_t used = carve((char*)b->wf_arena, b->wf_cap, s);
+  uint32_t* chunk_of = (uint32_t*)((char*)b->wf_arena + used);
+  const int sms = sm_count(b->device);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bbounce<F>, kWfBlock, 0);
+  const int bounce_grid = sms * std::max(per_sm, 1);
+  const int grid = sms * 8;
+  const int budget = (int)kDefaultFetchBudget;
+  cudaStream_t st = b->stream;
+  cudaError_t e;
+  b->launches = 0;
+  for (const rg_batch::Wave& w : b->waves) {
+    WaveParams wp;
+    wp.first_pixel = 0;
+    wp.n_pixels = w.n_pixels;
+    wp.n_paths = w.n_paths;
+    wp.capacity = (uint32_t)b->wf_cap;
+    const uint32_t gen_blocks = (uint32_t)std::min<size_t>((w.n_paths + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
+    k_bgenerate<<<gen_blocks, kWfBlock, 0, st>>>(b->d_items, b->d_chunks, w.first_chunk, w.n_chunks, w.n_paths, s,
+                                                 chunk_of);
+    int cur = 0;
+    for (uint32_t d = 0; d <= w.max_depth; ++d) {
+      if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+      k_bbounce<F><<<bounce_grid, kWfBlock, 0, st>>>(b->d_items, b->d_chunks, wp, s, chunk_of, cur, budget, b->d_err,
+                                                     b->d_counters);
+      cur ^= 1;
+    }
+    const uint32_t acc_blocks = (uint32_t)std::min<size_t>((w.n_pixels * 3 + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
+    k_baccumulate<<<acc_blocks, kWfBlock, 0, st>>>(b->d_items, b->d_chunks, w.first_chunk, w.n_chunks, w.n_pixels, s);
+    b->launches += w.max_depth + 3;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // Work-item prefix sums for the current tuning.
 rg_status layout(rg_batch* b) {
   const uint32_t rpi = b->tuning.rounds_per_item ? b->tuning.rounds_per_item : 4u;
@@ -145,6 +393,7 @@ rg_status layout(rg_batch* b) {
   prefix[b->items.size()] = (uint32_t)acc;
   b->total_work = (uint32_t)acc;
   BCUDA(b, cudaMemcpy(b->d_prefix, prefix.data(), prefix.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "batch layout");
+  if (b->tuning.form == RG_BATCH_WAVEFRONT) return plan_waves(b);
   return RG_OK;
 }
 
@@ -178,6 +427,9 @@ cudaError_t enqueue_frame(rg_batch* b) {
     return e;
   if ((e = cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), b->stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(b->d_counters, 0, CNT_N * sizeof(unsigned long long), b->stream)) != cudaSuccess) return e;
+  if (b->tuning.form == RG_BATCH_WAVEFRONT)
+    return dispatch_features(batch_features(b), [&](auto f) { return launch_batch_wavefront<decltype(f)::value>(b); });
+  b->launches = 1;
   return dispatch_features(batch_features(b), [&](auto f) { return launch_batch_kernel<decltype(f)::value>(b); });
 }
 
@@ -208,6 +460,7 @@ rg_status finish_stats(rg_batch* b, rg_render_stats* stats, std::chrono::steady_
   unsigned long long c[CNT_N];
   BCUDA(b, cudaMemcpy(c, b->d_counters, sizeof(c), cudaMemcpyDeviceToHost), "batch counters");
   uint32_t err = 0;
+  BCUDA(b, cudaMemcpy(&err, b->d_err, sizeof(err), cudaMemcpyDeviceToHost), "batch error flags");
   for (rg_renderer* h : b->items) {
     stats->samples += (uint64_t)h->opts.width * h->opts.height * h->opts.samples;
     uint32_t e1 = 0;
@@ -218,6 +471,7 @@ rg_status finish_stats(rg_batch* b, rg_render_stats* stats, std::chrono::steady_
   stats->rays = c[CNT_RAYS];
   stats->accum_frames = b->items.empty() ? 0 : b->items[0]->frame_count;
   stats->error_flags = err;
+  stats->kernel_launches = b->launches;
   stats->duration_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return RG_OK;
 }
@@ -267,6 +521,8 @@ rg_status rg_batch_create(const rg_device_opts* opts, uint32_t n, const rg_scene
         (e = cudaMalloc((void**)&b->d_prefix, (nb + 1) * sizeof(uint32_t))) != cudaSuccess ||
         (e = cudaMalloc((void**)&b->d_counter, sizeof(uint32_t))) != cudaSuccess ||
         (e = cudaMalloc((void**)&b->d_counters, CNT_N * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_err, sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMemset(b->d_err, 0, sizeof(uint32_t))) != cudaSuccess ||
         (e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess) {
       st = bcuda(b, e, "rg_batch_create");
     } else {
@@ -293,6 +549,9 @@ rg_status rg_batch_destroy(rg_batch_handle b) {
   if (b->d_prefix) cudaFree(b->d_prefix);
   if (b->d_counter) cudaFree(b->d_counter);
   if (b->d_counters) cudaFree(b->d_counters);
+  if (b->d_err) cudaFree(b->d_err);
+  if (b->d_chunks) cudaFree(b->d_chunks);
+  if (b->wf_arena) cudaFree(b->wf_arena);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -317,6 +576,8 @@ rg_status rg_batch_set_tuning(rg_batch_handle b, const rg_batch_tuning* t) {
   if (t->rounds_per_item > 4096) return bfail(b, RG_INVALID_ARG, "rounds_per_item too large");
   if (t->bvh_width != 0 && t->bvh_width != 2 && t->bvh_width != 8)
     return bfail(b, RG_INVALID_ARG, "rg_batch_tuning: bvh_width must be 0, 2 or 8");
+  if (t->form > RG_BATCH_TILES) return bfail(b, RG_INVALID_ARG, "rg_batch_tuning: unknown form %u", t->form);
+  if (t->wave_paths > 0x7FFFFFFFu) return bfail(b, RG_INVALID_ARG, "rg_batch_tuning: wave_paths too large");
   cudaSetDevice(b->device);
   if (t->block) {
     cudaFuncAttributes fa{};

@@ -1,0 +1,197 @@
+// wavefront.cuh — path state and per-path device functions shared by the
+// wavefront form (wavefront.cu) and the batched wavefront (batch.cu).
+//
+// Path state is one 48-byte record per slot (origin + depth, direction + hit
+// distance, throughput + hit primitive), read and written as three float4. A
+// path's radiance is zero until it ends (emission is only met at a light,
+// which ends the path, or at the sky), so it is written once, at the end, to
+// the per-slot sample buffer.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "renderer_state.h"
+#include "trace.cuh"
+
+namespace rg {
+
+constexpr int kWfBlock = 256;
+constexpr int kKinds = 6;  // miss, lambertian, metal, dielectric, isotropic, light
+enum : uint32_t { KQ_MISS = 0 };
+constexpr int kPrimMiss = -1;  // rec[2].w: >= 0 BVH primitive, -1 miss, -2 - k SDF k
+
+struct PathState {
+  float4* rec;          // 3 x float4 per slot: (origin, depth) (direction, t) (throughput, prim)
+  float4* aux;          // per slot: SDF hit normal + (front bit 31 | side)
+  float *sr, *sg, *sb;  // per-slot sample radiance
+  uint32_t* active[2];
+  uint32_t* kindq;      // kKinds x capacity
+  uint32_t* counts;     // [0], [1]: active counts; [2 .. 2+kKinds): kind counts; [kFetchCounter]: the traversal kernels' fetch counter
+};
+constexpr int kFetchCounter = 2 + kKinds;
+
+struct WaveParams {
+  uint32_t first_pixel, n_pixels, n_paths, capacity;
+};
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+  unsigned mask = __activemask();
+  unsigned ballot = __ballot_sync(mask, pred);
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader && ballot) base = atomicAdd(counter, (uint32_t)__popc(ballot));
+  base = __shfl_sync(mask, base, leader);
+  return base + __popc(ballot & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void store_path(const PathState& s, uint32_t p, V3 o, uint32_t depth, V3 d, C3f beta) {
+  s.rec[3 * (size_t)p] = make_float4(o.x, o.y, o.z, __uint_as_float(depth));
+  s.rec[3 * (size_t)p + 1] = make_float4(d.x, d.y, d.z, 0.0f);
+  s.rec[3 * (size_t)p + 2] = make_float4(beta.r, beta.g, beta.b, __int_as_float(kPrimMiss));
+}
+
+__device__ __forceinline__ void finish_path(const PathState& s, uint32_t p, C3f L) {
+  s.sr[p] = L.r; s.sg[p] = L.g; s.sb[p] = L.b;
+}
+
+__device__ __forceinline__ uint32_t clamp_count(uint32_t n, const WaveParams& wp, uint32_t* err) {
+  if (n > wp.n_paths) {  // never expected: record and clamp instead of reading past the queue
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_QUEUE_OVERFLOW);
+    return wp.n_paths;
+  }
+  return n;
+}
+
+// Shading of one path at its closest hit (or miss). Returns true when the path
+// continues; then its record holds the scattered ray. Ended paths write their
+// radiance.
+template <uint32_t F>
+__device__ __forceinline__ bool shade_path(const GpuScene& sc, const FrameParams& fp, const PathState& s, uint32_t p,
+                                           uint32_t pix, uint32_t smp, uint32_t depth, const Ray& r, C3f beta,
+                                           bool hit, const HitRec& h) {
+  if (!hit) {
+    C3f sk = sky_colour(sc.sky, r.d);
+    finish_path(s, p, C3f{0.0f + beta.r * sk.r, 0.0f + beta.g * sk.g, 0.0f + beta.b * sk.b});
+    return false;
+  }
+  RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
+  Surface surf;
+  finalize_hit<F>(sc, r, h, ctx, surf);
+  const rg_material m = sc.materials[surf.material];
+  if (m.kind == RG_MAT_LIGHT) {
+    finish_path(s, p, C3f{0.0f + beta.r * m.albedo[0], 0.0f + beta.g * m.albedo[1], 0.0f + beta.b * m.albedo[2]});
+    return false;
+  }
+  if (depth < fp.ray_depth) {
+    V3 dir;
+    if (scatter(m, r, surf, ctx, dir)) {
+      C3f a = attenuation(m, r, surf);
+      beta = C3f{beta.r * a.r, beta.g * a.g, beta.b * a.b};
+      Ray nr = make_ray(surf.pos, dir);
+      store_path(s, p, nr.o, depth + 1, nr.d, beta);
+      return true;
+    }
+  }
+  finish_path(s, p, C3f{0.0f, 0.0f, 0.0f});
+  return false;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void flush_wave_counters(const FrameParams& fp, const Counters& cnt, uint32_t queries) {
+  unsigned long long q = queries;
+  for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(0xffffffffu, q, o);
+  if ((threadIdx.x & 31) == 0 && q) atomicAdd(fp.counters + CNT_RAYS, q);
+  if (COUNT) {
+    unsigned long long a = cnt.nodes, b = cnt.prims, c = cnt.sdf_steps;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(fp.counters + CNT_NODES, a);
+      atomicAdd(fp.counters + CNT_PRIMS, b);
+      atomicAdd(fp.counters + CNT_SDF, c);
+    }
+  }
+}
+
+// Per-pixel sums in the megakernel's canonical order: samples 0..spp-1 in
+// turn for spp <= 32; for larger spp, lane partials (samples l, l+32, ...)
+// added for l = 0..31 in turn. `base` is the pixel's first slot; `pix` its
+// index in the frame (x-major output order [x][y][rgb]).
+__device__ __forceinline__ void accumulate_pixel(const FrameParams& fp, const PathState& s, size_t base, uint32_t pix,
+                                                 uint32_t c) {
+  const uint32_t spp = fp.spp;
+  const float* src = (c == 0 ? s.sr : (c == 1 ? s.sg : s.sb)) + base;
+  float sum = 0.0f;
+  double sumd = 0.0, sqd = 0.0;
+  if (spp <= 32) {
+    for (uint32_t k = 0; k < spp; ++k) {
+      float v = src[k];
+      sum = sum + v;
+      sumd += v;
+      sqd += (double)v * v;
+    }
+  } else {
+    for (uint32_t l = 0; l < 32; ++l) {
+      float part = 0.0f;
+      double psq = 0.0;
+      for (uint32_t k = l; k < spp; k += 32) {
+        float v = src[k];
+        part = part + v;
+        psq += (double)v * v;
+      }
+      sum = sum + part;
+      sumd += part;
+      sqd += psq;
+    }
+  }
+  uint32_t x = pix % fp.width, y = pix / fp.width;
+  size_t idx = ((size_t)x * fp.height + y) * 3 + c;
+  float mean = sum / (float)spp;
+  float acc = fp.accum[idx] + mean;
+  fp.accum[idx] = acc;
+  if (fp.out) fp.out[idx] = (float)((double)acc / (double)fp.accum_count);
+  if (fp.frame_mean) fp.frame_mean[idx] = mean;
+  if (fp.frame_var) {
+    double m = sumd / spp;
+    fp.frame_var[idx] = spp > 1 ? (float)fmax(0.0, (sqd - spp * m * m) / (spp - 1)) : 0.0f;
+  }
+}
+
+// Lays the path arrays out from `arena` (256-byte aligned each) and returns
+// the number of bytes used (108 per slot plus the counts); with a null arena
+// it only measures.
+inline size_t carve(char* arena, size_t cap, PathState& s) {
+  size_t used = 0;
+  auto take = [&](size_t bytes) {
+    char* r = arena ? arena + used : nullptr;
+    used += (bytes + 255) & ~size_t(255);
+    return r;
+  };
+  s.rec = (float4*)take(cap * 48);
+  s.aux = (float4*)take(cap * 16);
+  s.sr = (float*)take(cap * 4);
+  s.sg = (float*)take(cap * 4);
+  s.sb = (float*)take(cap * 4);
+  s.active[0] = (uint32_t*)take(cap * 4);
+  s.active[1] = (uint32_t*)take(cap * 4);
+  s.kindq = (uint32_t*)take(cap * 4 * kKinds);
+  s.counts = (uint32_t*)take(64 * 4);
+  return used;
+}
+
+inline size_t arena_bytes(size_t cap) {
+  PathState s;
+  return carve(nullptr, cap, s);
+}
+
+inline int sm_count(int device) {
+  int n = 0;
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
+  return n > 0 ? n : 1;
+}
+
+}  // namespace rg

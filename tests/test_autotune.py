@@ -39,5 +39,5 @@ def test_tuning_pass_picks_a_measured_candidate(tmp_path):
         r.render()
     with BatchRenderer(presets.batch_scenes(n=4, seed=2, scale=0.05, max_tris=5000)) as b:
         bcfg = t.tune_batch(b)
-        assert bcfg["block"] in (64, 128, 256)
+        assert bcfg["form"] in ("wavefront", "tiles")
         b.render(seed=3)

@@ -1,6 +1,7 @@
-"""The batched form through the C ABI: one persistent work-stealing launch
-(replayed as a CUDA graph) renders the same images as one megakernel launch
-per scene, and as standalone renderers given the same frame keys."""
+"""The batched forms through the C ABI: the batched wavefront and the
+persistent tile launch (each replayed as a CUDA graph) render the same images
+as one megakernel launch per scene, and as standalone renderers given the
+same frame keys."""
 import numpy as np
 import pytest
 
@@ -39,7 +40,11 @@ def test_batch_equals_sequential_and_standalone():
 def test_batch_tuning_does_not_change_images():
     items = small_batch()[:4]
     imgs = []
-    for tune in [dict(), dict(block=128, rounds_per_item=1), dict(block=64, blocks_per_sm=1, rounds_per_item=16)]:
+    # tiles in three shapes; the wavefront with waves small enough that renders
+    # are cut into runs spanning several waves, on either tree
+    for tune in [dict(), dict(form="tiles"), dict(form="tiles", block=128, rounds_per_item=1),
+                 dict(form="tiles", block=64, blocks_per_sm=1, rounds_per_item=16),
+                 dict(wave_paths=50_000), dict(wave_paths=50_000, bvh_width=8)]:
         with BatchRenderer(items) as b:
             b.set_tuning(**tune)
             b.render(seed=5)
