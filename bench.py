@@ -435,7 +435,8 @@ def main():
     ap.add_argument("--spp", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--batch-scale", type=float, default=0.25, help="resolution scale of the batched workload (0: skip)")
+    ap.add_argument("--batch-scale", type=float, default=1.0,
+                    help="resolution scale of the batched workload (1: the configured resolutions; 0: skip)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
