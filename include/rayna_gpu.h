@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 3u
+#define RG_ABI_VERSION 4u
 
 /* Status codes. 0 is success. */
 typedef enum rg_status {
@@ -112,9 +112,11 @@ typedef struct rg_sdf {
 
 /* A flattened scene. Object order (which decides exact-distance ties and the
  * order of unbounded objects) is: spheres, standalone triangles, triangle
- * meshes (by mesh id), boxes, volumes, SDFs. Global primitive ids, as
- * reported by rg_query_rays, number the same arrays in the same order:
- * spheres [0, ns), triangles [ns, ns+nt), boxes, volumes, SDFs. */
+ * meshes (by mesh id), boxes, volumes, parallelograms, cylinders; then the
+ * unbounded objects: SDFs, infinite planes. Global primitive ids, as reported
+ * by rg_query_rays, number the arrays in this order: spheres [0, ns),
+ * triangles [ns, ns+nt), boxes, volumes, SDFs, parallelograms, cylinders,
+ * infinite planes. */
 typedef struct rg_scene_desc {
     uint32_t n_spheres;
     const float* spheres;            /* n x 4: centre xyz, radius */
@@ -140,6 +142,18 @@ typedef struct rg_scene_desc {
     const rg_material* materials;
 
     uint32_t skybox;                 /* RG_SKY_* */
+
+    uint32_t n_quads;                /* ParallelogramMesh (mesh/planar/parallelogram.rs) */
+    const float* quads;              /* n x 9: Planar p, u, v (corner and two sides; uv in [0,1]^2 is inside) */
+    const uint32_t* quad_material;   /* n */
+
+    uint32_t n_cylinders;            /* CylinderMesh (mesh/primitive/cylinder.rs) */
+    const float* cylinders;          /* n x 7: p1 xyz, p2 xyz, radius (> 0, p1 != p2) */
+    const uint32_t* cylinder_material;
+
+    uint32_t n_planes;               /* InfinitePlaneMesh (mesh/planar/infinite_plane.rs): unbounded */
+    const float* planes;             /* n x 9: Planar p, u, v */
+    const uint32_t* plane_material;
 } rg_scene_desc;
 
 /* Camera (rayna_engine/src/scene/camera.rs:10-25), angles in radians. */
@@ -224,7 +238,7 @@ typedef struct rg_hit {
 /* Host-side summary of a scene as the library would build it. */
 typedef struct rg_scene_info {
     uint32_t n_prims;        /* bounded primitives in the BVH */
-    uint32_t n_unbounded;    /* SDFs */
+    uint32_t n_unbounded;    /* SDFs and infinite planes */
     uint32_t n_nodes;        /* 64-byte node pairs */
     uint32_t max_depth;      /* deepest node pair (traversal stack bound) */
     uint32_t n_leaves;

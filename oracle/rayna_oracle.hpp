@@ -392,6 +392,163 @@ template <class P> struct AxisBox {
   }
 };
 
+// Planar (mesh/planar/mod.rs:33-194). n, d and w are derived in f64 exactly
+// as Planar::new does; the f32 policy takes them rounded to f32, as the device
+// does.
+template <class P> struct Planar {
+  using T = typename P::T;
+  V3<T> p, u, v, n, w;
+  T d;
+  static bool make(const float* q, Planar& out) {
+    double pp[3], uu[3], vv[3];
+    for (int k = 0; k < 3; ++k) { pp[k] = q[k]; uu[k] = q[3 + k]; vv[k] = q[6 + k]; }
+    const double nr[3] = {uu[1] * vv[2] - vv[1] * uu[2], uu[2] * vv[0] - vv[2] * uu[0], uu[0] * vv[1] - vv[0] * uu[1]};
+    const double l2 = nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2];
+    const double rl = 1.0 / std::sqrt(l2);
+    if (!std::isfinite(rl) || !(rl > 0.0)) return false;
+    const double nn[3] = {nr[0] * rl, nr[1] * rl, nr[2] * rl};
+    out.p = {(T)pp[0], (T)pp[1], (T)pp[2]};
+    out.u = {(T)uu[0], (T)uu[1], (T)uu[2]};
+    out.v = {(T)vv[0], (T)vv[1], (T)vv[2]};
+    out.n = {(T)nn[0], (T)nn[1], (T)nn[2]};
+    out.d = (T)(-(nn[0] * pp[0] + nn[1] * pp[1] + nn[2] * pp[2]));
+    out.w = {(T)(nr[0] / l2), (T)(nr[1] / l2), (T)(nr[2] / l2)};
+    return true;
+  }
+  // Planar::intersect_bounded (mod.rs:161-194)
+  bool intersect(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
+    using M = Math<P>;
+    T denom = M::dot(n, ray.dir);
+    if (denom == T(0)) return false;
+    T t = -(M::dot(n, ray.pos) + d) / denom;
+    if (!iv.contains(t)) return false;
+    h.dist = t;
+    h.pos_w = M::at(ray.pos, ray.dir, t);
+    V3<T> pl = h.pos_w - p;
+    h.u = M::dot(w, M::cross(pl, v));
+    h.v = M::dot(w, M::cross(u, pl));
+    h.normal = n;
+    h.front_face = std::signbit(denom);
+    h.ray_normal = (-n) * M::signum(denom);
+    h.side = 0;
+    return true;
+  }
+};
+
+// ParallelogramMesh (mesh/planar/parallelogram.rs): the plane hit with uv in [0, 1]^2.
+template <class P> struct Parallelogram {
+  using T = typename P::T;
+  Planar<P> pl;
+  Aabb<T> aabb() const {  // encompass the corners, min_padded(AABB_PADDING = 1e-6) (parallelogram.rs:24-34)
+    V3<T> c[4] = {pl.p, pl.p + pl.u, pl.p + pl.v, pl.p + pl.u + pl.v};
+    V3<T> mn = c[0], mx = c[0];
+    for (int k = 1; k < 4; ++k) {
+      mn = {std::fmin(mn.x, c[k].x), std::fmin(mn.y, c[k].y), std::fmin(mn.z, c[k].z)};
+      mx = {std::fmax(mx.x, c[k].x), std::fmax(mx.y, c[k].y), std::fmax(mx.z, c[k].z)};
+    }
+    V3<T> size = mx - mn, centre = mn + size / T(2);
+    size = {std::fmax(size.x, T(1e-6)), std::fmax(size.y, T(1e-6)), std::fmax(size.z, T(1e-6))};
+    return Aabb<T>::make(centre - size / T(2), centre + size / T(2));
+  }
+  bool intersect(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
+    if (!pl.intersect(ray, iv, h)) return false;
+    return h.u >= T(0) && h.u <= T(1) && h.v >= T(0) && h.v <= T(1);
+  }
+};
+
+// CylinderMesh (mesh/primitive/cylinder.rs:24-183). The f32 policy follows the
+// device's operation order (explicit fused multiply-adds) and, like the
+// device, evaluates the test against [start, inf) before clipping to the
+// interval's end: the reference's test is not monotone in the end (a cap
+// nearer than the body roots is dropped when both roots lie beyond it), so
+// only the open-ended evaluation is independent of the traversal order. The
+// f64 policy keeps the reference's exact semantics. uv is left at 0.
+template <class P> struct Cylinder {
+  using T = typename P::T;
+  V3<T> origin, along;
+  T lsq, length, radius;
+  static Cylinder make(const float* c) {
+    const double al[3] = {(double)c[3] - c[0], (double)c[4] - c[1], (double)c[5] - c[2]};
+    const double l2 = al[0] * al[0] + al[1] * al[1] + al[2] * al[2];
+    Cylinder y;
+    y.origin = {(T)c[0], (T)c[1], (T)c[2]};
+    y.along = {(T)al[0], (T)al[1], (T)al[2]};
+    y.lsq = (T)l2;
+    y.length = (T)std::sqrt(l2);
+    y.radius = (T)c[6];
+    return y;
+  }
+  Aabb<T> aabb() const {
+    V3<T> p2 = origin + along, r{radius, radius, radius};
+    V3<T> mn{std::fmin(origin.x, p2.x), std::fmin(origin.y, p2.y), std::fmin(origin.z, p2.z)};
+    V3<T> mx{std::fmax(origin.x, p2.x), std::fmax(origin.y, p2.y), std::fmax(origin.z, p2.z)};
+    return Aabb<T>::make(mn - r, mx + r);
+  }
+  bool intersect(const Ray<P>& ray, const Interval<T>& iv_in, Hit<T>& h) const {
+    if constexpr (P::gpu) {
+      Interval<T> open = iv_in;
+      open.has_end = false;
+      return test(ray, open, h) && iv_in.contains(h.dist);
+    } else {
+      return test(ray, iv_in, h);
+    }
+  }
+  bool test(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
+    using M = Math<P>;
+    V3<T> rd = ray.dir, oc = ray.pos - origin;
+    T bard = M::dot(along, rd), baoc = M::dot(along, oc);
+    T a, b, c, disc;
+    if constexpr (P::gpu) {
+      a = std::fma(-bard, bard, lsq);
+      b = std::fma(lsq, M::dot(oc, rd), -(baoc * bard));
+      c = std::fma(lsq, M::dot(oc, oc), -(baoc * baoc)) - (radius * radius) * lsq;
+      disc = std::fma(b, b, -(c * a));
+    } else {
+      a = lsq - bard * bard;
+      b = lsq * M::dot(oc, rd) - baoc * bard;
+      c = lsq * M::dot(oc, oc) - baoc * baoc - radius * radius * lsq;
+      disc = b * b - c * a;
+    }
+    if (disc < T(0)) return false;
+    T sq = std::sqrt(disc);
+    T dist = (-b - sq) / a;
+    if (!iv.contains(dist)) dist = (-b + sq) / a;
+    if (!iv.contains(dist)) return false;
+    T dan;
+    if constexpr (P::gpu) dan = std::fma(dist, bard, baoc) / lsq;
+    else dan = (baoc + dist * bard) / lsq;
+    V3<T> normal;
+    uint32_t face;
+    if (dan > T(0) && dan < T(1)) {
+      V3<T> rel = M::at(oc, rd, dist);
+      V3<T> out = rel - along * dan;
+      normal = out / radius;
+      face = 0;
+    } else {
+      T dn, df;
+      if (std::signbit(baoc) == std::signbit(bard)) { dn = (T(0) - baoc) / bard; df = (lsq - baoc) / bard; }
+      else { dn = (lsq - baoc) / bard; df = (T(0) - baoc) / bard; }
+      dn = std::fmin(dn, df);
+      df = std::fmax(dn, df);  // as the reference: max of the new near and the far
+      auto radial = [&](T x) { if constexpr (P::gpu) return std::fabs(std::fma(a, x, b)); else return std::fabs(b + a * x); };
+      if (iv.contains(dn) && radial(dn) < sq) dist = dn;
+      else if (iv.contains(df) && radial(df) < sq) dist = df;
+      else return false;
+      normal = (along / length) * M::signum(dan);
+      face = std::signbit(dan) ? 1u : 2u;
+    }
+    T inside = -M::signum(M::dot(rd, normal));
+    h.dist = dist;
+    h.pos_w = M::at(ray.pos, ray.dir, dist);
+    h.normal = normal;
+    h.ray_normal = normal * inside;
+    h.front_face = std::signbit(inside);
+    h.u = h.v = T(0);
+    h.side = face;
+    return true;
+  }
+};
+
 // Signed distance functions evaluated in world space.
 template <class P> struct Sdf {
   using T = typename P::T;
@@ -519,7 +676,7 @@ template <class T> inline V3<T> unit_sphere_from(T r1, T r2) {
 // ---------------------------------------------------------------------------
 // Scene
 // ---------------------------------------------------------------------------
-enum ObjKind : uint32_t { OBJ_SPHERE, OBJ_TRIANGLE, OBJ_MESH, OBJ_BOX, OBJ_VOLUME, OBJ_SDF };
+enum ObjKind : uint32_t { OBJ_SPHERE, OBJ_TRIANGLE, OBJ_MESH, OBJ_BOX, OBJ_VOLUME, OBJ_SDF, OBJ_QUAD, OBJ_CYLINDER };
 
 template <class P> struct Scene;
 
@@ -705,16 +862,20 @@ template <class P> struct Scene {
   struct Volume { uint32_t boundary; Sphere<P> s; AxisBox<P> b; T density, neg_inv_density; uint32_t material; };
   std::vector<Volume> volumes;
   std::vector<Sdf<P>> sdfs;
-  std::vector<uint32_t> sphere_mat, tri_mat, box_mat;
+  std::vector<Parallelogram<P>> quads;
+  std::vector<Cylinder<P>> cylinders;
+  std::vector<Planar<P>> planes;
+  std::vector<uint32_t> sphere_mat, tri_mat, box_mat, quad_mat, cyl_mat, plane_mat;
   std::vector<rg_material> materials;
   uint32_t skybox = RG_SKY_SIMPLE;
-  uint32_t ns = 0, nt = 0, nb = 0, nv = 0, nsdf = 0;
+  uint32_t ns = 0, nt = 0, nb = 0, nv = 0, nsdf = 0, nq = 0, nc = 0, npl = 0;
 
   struct Mesh { std::vector<uint32_t> tris; Bvh<T> bvh; uint32_t material; Aabb<T> box; };
   std::vector<Mesh> meshes;
   struct Object { uint32_t kind, index; Aabb<T> box; };
   std::vector<Object> bounded;    // ObjectList::bvh items, in list order
-  std::vector<uint32_t> unbounded; // SDF indices, in list order
+  struct Unbounded { bool plane; uint32_t index; };
+  std::vector<Unbounded> unbounded; // SDFs, then infinite planes, in list order
   Bvh<T> top;
   Options opt;
 
@@ -723,11 +884,31 @@ template <class P> struct Scene {
   uint32_t prim_box(uint32_t i) const { return ns + nt + i; }
   uint32_t prim_vol(uint32_t i) const { return ns + nt + nb + i; }
   uint32_t prim_sdf(uint32_t i) const { return ns + nt + nb + nv + i; }
+  uint32_t prim_quad(uint32_t i) const { return ns + nt + nb + nv + nsdf + i; }
+  uint32_t prim_cyl(uint32_t i) const { return ns + nt + nb + nv + nsdf + nq + i; }
+  uint32_t prim_plane(uint32_t i) const { return ns + nt + nb + nv + nsdf + nq + nc + i; }
 
   void load(const rg_scene_desc& d, const Options& o) {
     opt = o;
     ns = d.n_spheres; nt = d.n_triangles; nb = d.n_boxes; nv = d.n_volumes; nsdf = d.n_sdfs;
+    nq = d.n_quads; nc = d.n_cylinders; npl = d.n_planes;
     skybox = d.skybox;
+    for (uint32_t i = 0; i < nq; ++i) {
+      Parallelogram<P> q;
+      Planar<P>::make(d.quads + 9 * i, q.pl);
+      quads.push_back(q);
+      quad_mat.push_back(d.quad_material[i]);
+    }
+    for (uint32_t i = 0; i < nc; ++i) {
+      cylinders.push_back(Cylinder<P>::make(d.cylinders + 7 * i));
+      cyl_mat.push_back(d.cylinder_material[i]);
+    }
+    for (uint32_t i = 0; i < npl; ++i) {
+      Planar<P> q;
+      Planar<P>::make(d.planes + 9 * i, q);
+      planes.push_back(q);
+      plane_mat.push_back(d.plane_material[i]);
+    }
     materials.assign(d.materials, d.materials + d.n_materials);
     for (uint32_t i = 0; i < ns; ++i) {
       Sphere<P> s;
@@ -774,7 +955,8 @@ template <class P> struct Scene {
       f.max_iter = s.max_iterations; f.eps = (T)s.epsilon;
       sdfs.push_back(f);
     }
-    // Objects in list order: spheres, standalone triangles, meshes, boxes, volumes; SDFs unbounded.
+    // Objects in list order: spheres, standalone triangles, meshes, boxes, volumes, parallelograms,
+    // cylinders; SDFs and infinite planes unbounded.
     for (uint32_t i = 0; i < ns; ++i) bounded.push_back({OBJ_SPHERE, i, spheres[i].aabb()});
     std::vector<int32_t> mesh_ids;
     for (uint32_t i = 0; i < nt; ++i) {
@@ -798,7 +980,10 @@ template <class P> struct Scene {
     for (uint32_t i = 0; i < nb; ++i) bounded.push_back({OBJ_BOX, i, boxes[i].aabb()});
     for (uint32_t i = 0; i < nv; ++i)
       bounded.push_back({OBJ_VOLUME, i, volumes[i].boundary == RG_BOUNDARY_SPHERE ? volumes[i].s.aabb() : volumes[i].b.aabb()});
-    for (uint32_t i = 0; i < nsdf; ++i) unbounded.push_back(i);
+    for (uint32_t i = 0; i < nq; ++i) bounded.push_back({OBJ_QUAD, i, quads[i].aabb()});
+    for (uint32_t i = 0; i < nc; ++i) bounded.push_back({OBJ_CYLINDER, i, cylinders[i].aabb()});
+    for (uint32_t i = 0; i < nsdf; ++i) unbounded.push_back({false, i});
+    for (uint32_t i = 0; i < npl; ++i) unbounded.push_back({true, i});
     std::vector<Aabb<T>> bx;
     for (auto& o : bounded) bx.push_back(o.box);
     build_bvh(bx, top, opt.exact_bvh_limit);
@@ -865,6 +1050,12 @@ template <class P> struct Scene {
         h.material = box_mat[o.index]; h.prim = prim_box(o.index); return true;
       case OBJ_VOLUME:
         return volume_intersect(o.index, ray, iv, rng, depth, h);
+      case OBJ_QUAD:
+        if (!quads[o.index].intersect(ray, iv, h)) return false;
+        h.material = quad_mat[o.index]; h.prim = prim_quad(o.index); return true;
+      case OBJ_CYLINDER:
+        if (!cylinders[o.index].intersect(ray, iv, h)) return false;
+        h.material = cyl_mat[o.index]; h.prim = prim_cyl(o.index); return true;
     }
     return false;
   }
@@ -946,13 +1137,17 @@ template <class P> struct Scene {
     bool any = false;
     if (opt.brute_force) any = brute_force(ray, iv, rng, depth, h);
     else if (top.root >= 0) any = top_node(top.root, ray, iv, rng, depth, h);
-    for (uint32_t si : unbounded) {
+    for (const Unbounded& u : unbounded) {
       Hit<T> hs;
-      if (!sdfs[si].intersect(ray, iv, hs)) continue;
+      if (u.plane) {
+        if (!planes[u.index].intersect(ray, iv, hs)) continue;  // InfinitePlaneMesh::intersect (infinite_plane.rs:87-92)
+      } else if (!sdfs[u.index].intersect(ray, iv, hs)) {
+        continue;
+      }
       if (!any || hs.dist < h.dist) {
         h = hs;
-        h.prim = prim_sdf(si);
-        h.material = sdf_material[si];
+        h.prim = u.plane ? prim_plane(u.index) : prim_sdf(u.index);
+        h.material = u.plane ? plane_mat[u.index] : sdf_material[u.index];
         any = true;
       }
     }

@@ -7,7 +7,8 @@ include/rayna_gpu.h. This package is the host-side mirror of the reference's
 scene, camera, options and Renderer types over that ABI.
 """
 from .scene import (  # noqa: F401
-    Angle, AxisBoxMesh, BvhMesh, Camera, DielectricMaterial, IsotropicMaterial, LambertianMaterial,
+    Angle, AxisBoxMesh, BvhMesh, Camera, CylinderMesh, DielectricMaterial, InfinitePlaneMesh, IsotropicMaterial,
+    LambertianMaterial, ParallelogramMesh, Planar,
     LightMaterial, MetalMaterial, NoSkybox, ObjectList, RaymarchedIsosurfaceMesh, RenderMode, RenderOpts,
     Scene, SdfMandelbulb, SdfSphere, SdfTorus, SimpleObject, SimpleSkybox, SolidTexture, SphereMesh,
     StandardScene, Triangle, UnsupportedVariant, VolumetricObject, WhiteSkybox, flatten,

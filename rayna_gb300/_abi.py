@@ -66,6 +66,10 @@ class rg_scene_desc(C.Structure):
         ("n_sdfs", C.c_uint32), ("sdfs", C.POINTER(rg_sdf)),
         ("n_materials", C.c_uint32), ("materials", C.POINTER(rg_material)),
         ("skybox", C.c_uint32),
+        ("n_quads", C.c_uint32), ("quads", C.POINTER(C.c_float)), ("quad_material", C.POINTER(C.c_uint32)),
+        ("n_cylinders", C.c_uint32), ("cylinders", C.POINTER(C.c_float)),
+        ("cylinder_material", C.POINTER(C.c_uint32)),
+        ("n_planes", C.c_uint32), ("planes", C.POINTER(C.c_float)), ("plane_material", C.POINTER(C.c_uint32)),
     ]
 
 

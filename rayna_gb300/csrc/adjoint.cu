@@ -124,7 +124,7 @@ __device__ void replay_sample(const GpuScene& sc, const FrameParams& fp, const A
       break;
     }
     Surface surf;
-    finalize_hit<F>(sc, ray, h, ctx, surf);
+    finalize_hit<F>(sc, ray, h, ctx, surf, 1e-3f);
     const rg_material m = sc.materials[surf.material];
     mat[K] = (int)surf.material;
     light[K] = m.kind == RG_MAT_LIGHT;

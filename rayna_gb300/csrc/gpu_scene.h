@@ -31,6 +31,8 @@ enum : uint32_t {
   PK_BOX = 2,
   PK_VOL_SPHERE = 3,
   PK_VOL_BOX = 4,
+  PK_QUAD = 5,
+  PK_CYLINDER = 6,
 };
 constexpr uint32_t kKindShift = 29;
 constexpr uint32_t kMaterialMask = (1u << kKindShift) - 1u;
@@ -46,6 +48,9 @@ constexpr uint32_t kTriCheckNormals = 1u;
 //   box         a = (centre, bits)           b = (radius, id)             c = (1/radius, 0)
 //   vol sphere  a = (centre, bits)           b = (r, r*r, -1/density, id) c = unused
 //   vol box     a = (centre, bits)           b = (radius, id)             c = (1/radius, -1/density)
+//   quad        a = (n, bits)                b = (d, 0, 0, id)            c = (p, quad index)
+//               (plane n.x + d = 0; u, v, w of the Planar in quad_ext, read after a plane hit)
+//   cylinder    a = (p1, bits)               b = (p2 - p1, id)            c = (|p2-p1|^2, radius, |p2-p1|, 0)
 // `id` is the global primitive id (see rg_scene_desc).
 struct alignas(16) GpuPrim {
   float4 a, b, c;
@@ -98,6 +103,10 @@ constexpr int kWideMaxDepth = 60;
 constexpr int kStackSize = 64;
 constexpr int kMaxBuildDepth = 60;
 
+// Unbounded objects, tested after the tree in list order: the SDF kinds of
+// rg_sdf, and infinite planes (kind kUnboundedPlane: normal in (cx, cy, cz),
+// plane offset d in p0).
+constexpr uint32_t kUnboundedPlane = 16;
 struct GpuSdf {
   uint32_t kind;
   float cx, cy, cz;
@@ -112,7 +121,18 @@ struct GpuSdf {
 
 // Kernel variant bits (GpuScene::features): the primitive kinds a kernel is
 // specialised for, and F_WIDE when it traverses the 8-wide tree.
-enum : uint32_t { F_SPHERE = 1u, F_TRI = 2u, F_BOX = 4u, F_VOL = 8u, F_SDF = 16u, F_ALL = 31u, F_WIDE = 32u };
+enum : uint32_t {
+  F_SPHERE = 1u,
+  F_TRI = 2u,
+  F_BOX = 4u,
+  F_VOL = 8u,
+  F_SDF = 16u,
+  F_QUAD = 32u,
+  F_CYLINDER = 64u,
+  F_PLANE = 128u,  // unbounded infinite planes
+  F_ALL = 255u,
+  F_WIDE = 256u,
+};
 constexpr uint32_t kinds_of(uint32_t f) { return f & F_ALL; }
 
 // Host-side dispatch: calls fn(std::integral_constant<uint32_t, F>{}) with
@@ -151,6 +171,7 @@ struct GpuScene {
   const uint32_t* vol_prim;   // per medium: its position in `prims`
   const WideNode* wnodes;     // the same primitives under the 8-wide tree (node 0 is the root)
   uint32_t n_wnodes;
+  const float* quad_ext;      // per parallelogram: Planar u, v, w (9 floats)
 };
 
 // Device error bits (rg_render_stats::error_flags).

@@ -58,7 +58,7 @@ __global__ void k_query(GpuScene sc, uint32_t n, const float* o, const float* d,
   res.front_face = 0; res.material = 0; res.side = 0;
   if (closest_hit<F, false>(sc, r, tmin[i], tmax[i], ctx, h, cnt, err)) {
     Surface s;
-    finalize_hit<F>(sc, r, h, ctx, s);
+    finalize_hit<F>(sc, r, h, ctx, s, tmin[i]);
     res.hit = 1;
     res.prim = s.prim_id;
     res.t = h.t;

@@ -102,6 +102,24 @@ float bits_float(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 
 uint32_t ilog2(uint32_t v) { uint32_t r = 0; while (v >>= 1) ++r; return r; }
 
+// Planar::new (mesh/planar/mod.rs:69-80) in f64: n = try_normalize(cross(u, v)),
+// d = -dot(n, p), w = cross(u, v) / |cross(u, v)|^2. The device and the f32
+// oracle take these rounded to f32.
+struct PlanarF64 {
+  double p[3], u[3], v[3], n[3], d, w[3];
+};
+bool planar_f64(const float* q, PlanarF64& o) {
+  for (int k = 0; k < 3; ++k) { o.p[k] = q[k]; o.u[k] = q[3 + k]; o.v[k] = q[6 + k]; }
+  const double nr[3] = {o.u[1] * o.v[2] - o.v[1] * o.u[2], o.u[2] * o.v[0] - o.v[2] * o.u[0],
+                        o.u[0] * o.v[1] - o.v[0] * o.u[1]};
+  const double l2 = nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2];
+  const double rl = 1.0 / std::sqrt(l2);
+  if (!std::isfinite(rl) || !(rl > 0.0)) return false;
+  for (int k = 0; k < 3; ++k) { o.n[k] = nr[k] * rl; o.w[k] = nr[k] / l2; }
+  o.d = -(o.n[0] * o.p[0] + o.n[1] * o.p[1] + o.n[2] * o.p[2]);
+  return true;
+}
+
 rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
   auto need = [&](uint32_t n, const void* p, const char* what) -> bool {
     if (n > 0 && p == nullptr) { fail(h, RG_INVALID_ARG, "%s is NULL but its count is %u", what, n); return false; }
@@ -111,9 +129,13 @@ rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
       !need(d.n_triangles, d.tri_vertices, "tri_vertices") || !need(d.n_triangles, d.tri_normals, "tri_normals") ||
       !need(d.n_triangles, d.tri_material, "tri_material") || !need(d.n_boxes, d.boxes, "boxes") ||
       !need(d.n_boxes, d.box_material, "box_material") || !need(d.n_volumes, d.volumes, "volumes") ||
-      !need(d.n_sdfs, d.sdfs, "sdfs") || !need(d.n_materials, d.materials, "materials"))
+      !need(d.n_sdfs, d.sdfs, "sdfs") || !need(d.n_materials, d.materials, "materials") ||
+      !need(d.n_quads, d.quads, "quads") || !need(d.n_quads, d.quad_material, "quad_material") ||
+      !need(d.n_cylinders, d.cylinders, "cylinders") || !need(d.n_cylinders, d.cylinder_material, "cylinder_material") ||
+      !need(d.n_planes, d.planes, "planes") || !need(d.n_planes, d.plane_material, "plane_material"))
     return RG_INVALID_ARG;
-  uint64_t total = (uint64_t)d.n_spheres + d.n_triangles + d.n_boxes + d.n_volumes + d.n_sdfs;
+  uint64_t total = (uint64_t)d.n_spheres + d.n_triangles + d.n_boxes + d.n_volumes + d.n_sdfs + d.n_quads +
+                   d.n_cylinders + d.n_planes;
   if (total >= (1ull << 28)) return fail(h, RG_INVALID_ARG, "too many primitives (%llu; limit 2^28)", (unsigned long long)total);
   if (d.n_materials > kMaterialMask) return fail(h, RG_INVALID_ARG, "too many materials");
   if (d.skybox > RG_SKY_NONE) return fail(h, RG_UNSUPPORTED_VARIANT, "skybox kind %u", d.skybox);
@@ -167,6 +189,25 @@ rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
     if (s.max_iterations > (1u << 20)) return fail(h, RG_INVALID_ARG, "sdf %u: max_iterations too large", i);
     if (!mat_ok(s.material, "sdf", i)) return RG_INVALID_ARG;
   }
+  // Planar::new (mesh/planar/mod.rs:69-80) panics when cross(u, v) cannot be normalised.
+  auto planar_ok = [&](const float* q, const char* what, uint32_t i) -> bool {
+    if (!finite3(q) || !finite3(q + 3) || !finite3(q + 6)) { fail(h, RG_INVALID_ARG, "%s %u is not finite", what, i); return false; }
+    PlanarF64 pl;
+    if (!planar_f64(q, pl)) { fail(h, RG_INVALID_ARG, "%s %u: cross(u, v) cannot be normalised", what, i); return false; }
+    return true;
+  };
+  for (uint32_t i = 0; i < d.n_quads; ++i)
+    if (!planar_ok(d.quads + 9ull * i, "parallelogram", i) || !mat_ok(d.quad_material[i], "parallelogram", i))
+      return RG_INVALID_ARG;
+  for (uint32_t i = 0; i < d.n_planes; ++i)
+    if (!planar_ok(d.planes + 9ull * i, "plane", i) || !mat_ok(d.plane_material[i], "plane", i)) return RG_INVALID_ARG;
+  for (uint32_t i = 0; i < d.n_cylinders; ++i) {
+    const float* c = d.cylinders + 7ull * i;
+    if (!finite3(c) || !finite3(c + 3) || !std::isfinite(c[6])) return fail(h, RG_INVALID_ARG, "cylinder %u is not finite", i);
+    if (!(c[6] > 0.0f)) return fail(h, RG_INVALID_ARG, "cylinder %u: radius must be positive", i);
+    if (c[0] == c[3] && c[1] == c[4] && c[2] == c[5]) return fail(h, RG_INVALID_ARG, "cylinder %u: p1 == p2", i);
+    if (!mat_ok(d.cylinder_material[i], "cylinder", i)) return RG_INVALID_ARG;
+  }
   return RG_OK;
 }
 
@@ -191,10 +232,11 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
   if (st != RG_OK) return st;
   hs = HostScene{};
   hs.ns = d.n_spheres; hs.nt = d.n_triangles; hs.nb = d.n_boxes; hs.nv = d.n_volumes; hs.nsdf = d.n_sdfs;
+  hs.nq = d.n_quads; hs.nc = d.n_cylinders; hs.npl = d.n_planes;
   hs.sky = d.skybox;
   hs.materials.assign(d.materials, d.materials + d.n_materials);
   hs.volumes.assign(d.volumes, d.volumes + d.n_volumes);
-  const uint32_t nbounded = hs.ns + hs.nt + hs.nb + hs.nv;
+  const uint32_t nbounded = hs.ns + hs.nt + hs.nb + hs.nv + hs.nq + hs.nc;
   std::vector<GpuPrim> prims(nbounded);
   std::vector<float> lo(3ull * nbounded), hi(3ull * nbounded);
   auto bits = [](uint32_t kind, uint32_t mat) { return bits_float((kind << kKindShift) | mat); };
@@ -290,6 +332,66 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
     g.bound_radius = (float)((r0 + margin) * (1.0 + 1e-4));
     hs.sdfs.push_back(g);
   }
+  // Parallelograms and cylinders: bounded, stored after the volumes in the
+  // primitive array; their global ids follow the SDFs.
+  uint32_t pi = hs.ns + hs.nt + hs.nb + hs.nv;
+  // Bounds rounded outward with a margin that covers the f32 tests' rounding
+  // (the traversal's box tests are conservative on top of this).
+  auto setbox_pad = [&](uint32_t k, const double* mn, const double* mx) {
+    double ext = 0.0;
+    for (int a = 0; a < 3; ++a) ext = std::max(ext, mx[a] - mn[a]);
+    for (int a = 0; a < 3; ++a) {
+      const double pad = 1e-6 + 1e-5 * ext + 1e-6 * std::max(std::fabs(mn[a]), std::fabs(mx[a]));
+      lo[3ull * k + a] = std::nextafter((float)(mn[a] - pad), -INFINITY);
+      hi[3ull * k + a] = std::nextafter((float)(mx[a] + pad), INFINITY);
+    }
+  };
+  hs.quad_ext.resize(9ull * hs.nq);
+  for (uint32_t i = 0; i < hs.nq; ++i, ++id, ++pi) {
+    PlanarF64 q;
+    planar_f64(d.quads + 9ull * i, q);
+    GpuPrim& p = prims[pi];
+    p.a = {(float)q.n[0], (float)q.n[1], (float)q.n[2], bits(PK_QUAD, d.quad_material[i])};
+    p.b = {(float)q.d, 0.0f, 0.0f, bits_float(id)};
+    p.c = {(float)q.p[0], (float)q.p[1], (float)q.p[2], bits_float(i)};
+    float* e = hs.quad_ext.data() + 9ull * i;
+    for (int k = 0; k < 3; ++k) { e[k] = (float)q.u[k]; e[3 + k] = (float)q.v[k]; e[6 + k] = (float)q.w[k]; }
+    double mn[3], mx[3];
+    for (int k = 0; k < 3; ++k) {
+      const double c0 = q.p[k], c1 = q.p[k] + q.u[k], c2 = q.p[k] + q.v[k], c3 = q.p[k] + q.u[k] + q.v[k];
+      mn[k] = std::min(std::min(c0, c1), std::min(c2, c3));
+      mx[k] = std::max(std::max(c0, c1), std::max(c2, c3));
+    }
+    setbox_pad(pi, mn, mx);
+  }
+  for (uint32_t i = 0; i < hs.nc; ++i, ++id, ++pi) {
+    const float* c = d.cylinders + 7ull * i;
+    // CylinderMesh::new (cylinder.rs:24-48)
+    const double along[3] = {(double)c[3] - c[0], (double)c[4] - c[1], (double)c[5] - c[2]};
+    const double lsq = along[0] * along[0] + along[1] * along[1] + along[2] * along[2];
+    GpuPrim& p = prims[pi];
+    p.a = {c[0], c[1], c[2], bits(PK_CYLINDER, d.cylinder_material[i])};
+    p.b = {(float)along[0], (float)along[1], (float)along[2], bits_float(id)};
+    p.c = {(float)lsq, c[6], (float)std::sqrt(lsq), 0.0f};
+    double mn[3], mx[3];
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = std::min((double)c[k], (double)c[3 + k]) - c[6];
+      mx[k] = std::max((double)c[k], (double)c[3 + k]) + c[6];
+    }
+    setbox_pad(pi, mn, mx);
+  }
+  // Infinite planes: unbounded, after the SDFs.
+  for (uint32_t i = 0; i < hs.npl; ++i, ++id) {
+    PlanarF64 q;
+    planar_f64(d.planes + 9ull * i, q);
+    GpuSdf g{};
+    g.kind = kUnboundedPlane;
+    g.cx = (float)q.n[0]; g.cy = (float)q.n[1]; g.cz = (float)q.n[2];
+    g.p0 = (float)q.d;
+    g.material = d.plane_material[i];
+    g.prim_id = id;
+    hs.sdfs.push_back(g);
+  }
   // Binary tree (leaves of at most kWideMaxLeaf primitives), then its 8-wide
   // collapse; both index one primitive order.
   BvhBuildResult bvh = build_bvh(lo.data(), hi.data(), nbounded, kWideMaxLeaf, 16, 40);
@@ -331,6 +433,7 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   if ((st = upload(h, ds.tri_normals, hs.tri_normals.data(), hs.tri_normals.size(), "upload normals")) != RG_OK) return st;
   if ((st = upload(h, ds.materials, hs.materials.data(), hs.materials.size(), "upload materials")) != RG_OK) return st;
   if ((st = upload(h, ds.sdfs, hs.sdfs.data(), hs.sdfs.size(), "upload sdfs")) != RG_OK) return st;
+  if ((st = upload(h, ds.quad_ext, hs.quad_ext.data(), hs.quad_ext.size(), "upload parallelograms")) != RG_OK) return st;
   if ((st = upload(h, ds.vol_density, hs.vol_density.data(), hs.vol_density.size(), "upload media")) != RG_OK) return st;
   if ((st = upload(h, ds.vol_prim, hs.vol_prim.data(), hs.vol_prim.size(), "upload media")) != RG_OK) return st;
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "upload scene");
@@ -342,11 +445,12 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.tri_normals = ds.tri_normals;
   g.materials = ds.materials;
   g.sdfs = ds.sdfs;
+  g.quad_ext = ds.quad_ext;
   g.vol_density = ds.vol_density;
   g.vol_prim = ds.vol_prim;
   g.n_nodes = (uint32_t)hs.nodes.size();
   g.n_prims = (uint32_t)hs.prims.size();
-  g.n_sdfs = hs.nsdf;
+  g.n_sdfs = (uint32_t)hs.sdfs.size();
   g.n_volumes = hs.nv;
   g.sky = hs.sky;
   g.tri_base = hs.ns;
@@ -354,7 +458,7 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.n_tris = hs.nt;
   // Kernel variant: triangles only, spheres only, or every kind.
   uint32_t have = (hs.ns ? F_SPHERE : 0) | (hs.nt ? F_TRI : 0) | (hs.nb ? F_BOX : 0) | (hs.nv ? F_VOL : 0) |
-                  (hs.nsdf ? F_SDF : 0);
+                  (hs.nsdf ? F_SDF : 0) | (hs.nq ? F_QUAD : 0) | (hs.nc ? F_CYLINDER : 0) | (hs.npl ? F_PLANE : 0);
   h->kinds = have == F_TRI ? F_TRI : (have == F_SPHERE ? F_SPHERE : F_ALL);
   apply_features(h);
   return RG_OK;
@@ -385,7 +489,7 @@ void apply_features(rg_renderer* h) {
 }
 
 void free_scene(DeviceScene& ds) {
-  dfree(ds.nodes); dfree(ds.wnodes); dfree(ds.prims); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
+  dfree(ds.nodes); dfree(ds.wnodes); dfree(ds.prims); dfree(ds.quad_ext); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
   dfree(ds.vol_density); dfree(ds.vol_prim);
 }
 
@@ -537,7 +641,7 @@ rg_status rg_inspect_scene(const rg_scene_desc* scene, rg_scene_info* out) {
   std::memset(out, 0, sizeof(*out));
   if (st != RG_OK) return st;
   out->n_prims = (uint32_t)hs.prims.size();
-  out->n_unbounded = hs.nsdf;
+  out->n_unbounded = (uint32_t)hs.sdfs.size();
   out->n_nodes = (uint32_t)hs.nodes.size();
   out->max_depth = (uint32_t)hs.max_depth;
   double root_area = 0.0, cost = 0.0;
@@ -563,7 +667,8 @@ rg_status rg_inspect_scene(const rg_scene_desc* scene, rg_scene_info* out) {
   out->sah_cost = root_area > 0.0 ? cost / root_area : 0.0;
   out->device_bytes = hs.nodes.size() * sizeof(BvhNode2) + hs.wnodes.size() * sizeof(WideNode) +
                       hs.prims.size() * sizeof(GpuPrim) + hs.tri_normals.size() * sizeof(float) +
-                      hs.materials.size() * sizeof(rg_material) + hs.sdfs.size() * sizeof(GpuSdf);
+                      hs.materials.size() * sizeof(rg_material) + hs.sdfs.size() * sizeof(GpuSdf) +
+                      hs.quad_ext.size() * sizeof(float);
   out->n_wide_nodes = (uint32_t)hs.wnodes.size();
   out->wide_depth = hs.wide_depth > 0 ? (uint32_t)hs.wide_depth : 0u;
   return RG_OK;

@@ -18,7 +18,7 @@ struct HostViewport {
 
 // Host copy of a flattened scene (kept for the adjoint and for rebuilding).
 struct HostScene {
-  uint32_t ns = 0, nt = 0, nb = 0, nv = 0, nsdf = 0;
+  uint32_t ns = 0, nt = 0, nb = 0, nv = 0, nsdf = 0, nq = 0, nc = 0, npl = 0;
   uint32_t sky = RG_SKY_SIMPLE;
   uint32_t vol_base = 0;
   int max_depth = 0;
@@ -29,7 +29,8 @@ struct HostScene {
   std::vector<float> tri_normals;
   std::vector<rg_material> materials;
   std::vector<rg_volume> volumes;
-  std::vector<GpuSdf> sdfs;
+  std::vector<GpuSdf> sdfs;            // unbounded list: SDFs, then infinite planes
+  std::vector<float> quad_ext;         // per parallelogram: u, v, w
   std::vector<float> vol_density;      // per medium
   std::vector<uint32_t> vol_prim;      // per medium: position in `prims`
 };
@@ -41,6 +42,7 @@ struct DeviceScene {
   float* tri_normals = nullptr;
   rg_material* materials = nullptr;
   GpuSdf* sdfs = nullptr;
+  float* quad_ext = nullptr;
   float* vol_density = nullptr;
   uint32_t* vol_prim = nullptr;
 };

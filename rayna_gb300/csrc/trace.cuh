@@ -295,7 +295,89 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x) {
   return (0.5f * logf(rr) * rr / dr) * sc;
 }
 
-struct SdfHit { float t; V3 n; bool front; uint32_t side; };
+// Planar::intersect_bounded (mesh/planar/mod.rs:161-194): the distance to
+// the plane n.x + d = 0 if it lies in [start, end]; `denom` = dot(n, dir).
+__device__ __forceinline__ bool plane_t(V3 n, float dc, const Ray& r, float start, float end, float& t, float& denom) {
+  denom = dot3(n, r.d);
+  if (denom == 0.0f) return false;
+  t = __fdiv_rn(-(dot3(n, r.o) + dc), denom);
+  return start <= t && t <= end;
+}
+
+// The hit's planar coordinates (mesh/planar/mod.rs:181-185): alpha along u,
+// beta along v, from w = cross(u, v) / |cross(u, v)|^2. `ext` = u, v, w.
+__device__ __forceinline__ void planar_uv(const float* ext, V3 p, V3 pos, float& alpha, float& beta) {
+  const V3 u = v3(__ldg(ext), __ldg(ext + 1), __ldg(ext + 2));
+  const V3 v = v3(__ldg(ext + 3), __ldg(ext + 4), __ldg(ext + 5));
+  const V3 w = v3(__ldg(ext + 6), __ldg(ext + 7), __ldg(ext + 8));
+  const V3 pl = v3(pos.x - p.x, pos.y - p.y, pos.z - p.z);
+  alpha = dot3(w, cross3(pl, v));
+  beta = dot3(w, cross3(u, pl));
+}
+
+// ParallelogramMesh::intersect (mesh/planar/parallelogram.rs:49-57): the
+// plane hit with both planar coordinates in [0, 1].
+__device__ __forceinline__ bool quad_t(const GpuPrim& p, const float* quad_ext, const Ray& r, float start, float end,
+                                       float& t) {
+  float denom;
+  if (!plane_t(xyz(p.a), p.b.x, r, start, end, t, denom)) return false;
+  float al, be;
+  planar_uv(quad_ext + 9ull * __float_as_uint(p.c.w), xyz(p.c), at3(r.o, r.d, t), al, be);
+  return al >= 0.0f && al <= 1.0f && be >= 0.0f && be <= 1.0f;
+}
+
+// CylinderMesh::intersect (mesh/primitive/cylinder.rs:64-183): distance and
+// face (0 body, 1 the p1 cap, 2 the p2 cap), including the reference's cap
+// choice (its far-cap distance is max(min(near, far), far)) and its miss of
+// rays parallel to the axis (a = 0). The reference's test is not monotone in
+// the interval's end (a cap nearer than the body roots is dropped when both
+// body roots lie beyond the end), so its closest hit can depend on the order
+// objects are tested in; callers evaluate it against [start, inf) and clip
+// the result to their end, which is order-independent and equals the
+// reference's answer for the first object tested.
+struct CylHit { float t, dan; uint32_t face; };
+__device__ __forceinline__ bool cylinder_t(const GpuPrim& p, const Ray& r, float start, float end, CylHit& ch) {
+  const V3 o1 = xyz(p.a), along = xyz(p.b);
+  const float lsq = p.c.x, rad = p.c.y;
+  const V3 oc = v3(r.o.x - o1.x, r.o.y - o1.y, r.o.z - o1.z);
+  const float bard = dot3(along, r.d), baoc = dot3(along, oc);
+  const float a = __fmaf_rn(-bard, bard, lsq);
+  const float b = __fmaf_rn(lsq, dot3(oc, r.d), -(baoc * bard));
+  const float c = __fmaf_rn(lsq, dot3(oc, oc), -(baoc * baoc)) - (rad * rad) * lsq;
+  const float disc = __fmaf_rn(b, b, -(c * a));
+  if (disc < 0.0f) return false;
+  const float sq = __fsqrt_rn(disc);
+  float dist = __fdiv_rn(-b - sq, a);
+  if (!(start <= dist && dist <= end)) dist = __fdiv_rn(-b + sq, a);
+  if (!(start <= dist && dist <= end)) return false;
+  const float dan = __fdiv_rn(__fmaf_rn(dist, bard, baoc), lsq);
+  ch.dan = dan;
+  if (dan > 0.0f && dan < 1.0f) {
+    ch.t = dist;
+    ch.face = 0;
+    return true;
+  }
+  float dn, df;
+  if (signbit(baoc) == signbit(bard)) {
+    dn = __fdiv_rn(0.0f - baoc, bard);
+    df = __fdiv_rn(lsq - baoc, bard);
+  } else {
+    dn = __fdiv_rn(lsq - baoc, bard);
+    df = __fdiv_rn(0.0f - baoc, bard);
+  }
+  dn = fminf(dn, df);
+  df = fmaxf(dn, df);
+  if (start <= dn && dn <= end && fabsf(__fmaf_rn(a, dn, b)) < sq) dist = dn;
+  else if (start <= df && df <= end && fabsf(__fmaf_rn(a, df, b)) < sq) dist = df;
+  else return false;
+  ch.t = dist;
+  ch.face = signbit(dan) ? 1u : 2u;
+  return true;
+}
+
+// Hit on an unbounded object. `flip`: the ray normal is -n (infinite planes
+// face the ray; raymarched surfaces keep their normal).
+struct SdfHit { float t; V3 n; bool front; uint32_t side; bool flip; };
 
 // RaymarchedIsosurfaceMesh::intersect (mesh/isosurface/raymarched.rs:73-122)
 // with two exact early exits that cannot change the result:
@@ -327,6 +409,7 @@ __device__ bool sdf_march(const GpuSdf& s, const Ray& r, float start, float end,
       h.n = normalize3(g);
       h.front = !signbit(d);
       h.side = i;
+      h.flip = false;
       return true;
     }
     if (i > s.max_iter) return false;
@@ -379,6 +462,16 @@ __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int cou
       BoxHit bh;
       if (!box_t(xyz(a), xyz(b), xyz(c), r, start, end, bh)) continue;
       t = bh.t;
+    } else if ((F & F_QUAD) && kind == PK_QUAD) {
+      GpuPrim p;
+      p.a = a; p.b = __ldg(&pp->b); p.c = __ldg(&pp->c);
+      if (!quad_t(p, sc.quad_ext, r, start, end, t)) continue;
+    } else if ((F & F_CYLINDER) && kind == PK_CYLINDER) {
+      GpuPrim p;
+      p.a = a; p.b = __ldg(&pp->b); p.c = __ldg(&pp->c);
+      CylHit ch;
+      if (!cylinder_t(p, r, start, CUDART_INF_F, ch) || !(ch.t <= end)) continue;
+      t = ch.t;
     } else if ((F & F_VOL) && (kind == PK_VOL_SPHERE || kind == PK_VOL_BOX)) {
       GpuPrim p;
       p.a = a; p.b = __ldg(&pp->b); p.c = __ldg(&pp->c);
@@ -648,15 +741,24 @@ __device__ __forceinline__ bool finish_hit(const GpuScene& sc, const Ray& r, flo
   h.sdf = -1;
   h.t = t.tmax;
   bool any = t.best >= 0;
-  if (F & F_SDF) {
+  if (F & (F_SDF | F_PLANE)) {
     for (uint32_t k = 0; k < sc.n_sdfs; ++k) {
+      const GpuSdf& f = sc.sdfs[k];
       SdfHit sh;
-      if (sdf_march<COUNT>(sc.sdfs[k], r, start, end, any ? h.t : end, !any, sh, cnt.sdf_steps)) {
-        h.t = sh.t;
-        h.sdf = (int)k;
-        h.sh = sh;
-        any = true;
+      if ((F & F_PLANE) && f.kind == kUnboundedPlane) {
+        // InfinitePlaneMesh::intersect (mesh/planar/infinite_plane.rs:87-92)
+        float pt, denom;
+        if (!plane_t(v3(f.cx, f.cy, f.cz), f.p0, r, start, end, pt, denom) || (any && !(pt < h.t))) continue;
+        sh = SdfHit{pt, v3(f.cx, f.cy, f.cz), (bool)signbit(denom), 0u, !signbit(denom)};
+      } else if (F & F_SDF) {
+        if (!sdf_march<COUNT>(f, r, start, end, any ? h.t : end, !any, sh, cnt.sdf_steps)) continue;
+      } else {
+        continue;
       }
+      h.t = sh.t;
+      h.sdf = (int)k;
+      h.sh = sh;
+      any = true;
     }
   }
   return any;
@@ -682,12 +784,14 @@ struct Surface {
 };
 
 template <uint32_t F>
-__device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, const HitRec& h, const RngCtx& ctx, Surface& s) {
-  if ((F & F_SDF) && h.sdf >= 0) {
+__device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, const HitRec& h, const RngCtx& ctx, Surface& s,
+                                             float start) {
+  if ((F & (F_SDF | F_PLANE)) && h.sdf >= 0) {
     const GpuSdf& f = sc.sdfs[h.sdf];
     s.pos = at3(r.o, r.d, h.t);
     s.normal = h.sh.n;
-    s.ray_normal = h.sh.n;  // raymarched.rs:113-114: not flipped
+    // raymarched.rs:113-114: not flipped; planar/mod.rs:190: -n * signum(denom)
+    s.ray_normal = h.sh.flip ? -h.sh.n : h.sh.n;
     s.front = h.sh.front;
     s.material = f.material;
     s.prim_id = f.prim_id;
@@ -731,6 +835,34 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
     s.side = (uint32_t)bh.axis * 2u + (bh.sgn > 0.0f ? 1u : 0u);
     s.u = (bh.u0 + 1.0f) / 2.0f;
     s.v = (bh.u1 + 1.0f) / 2.0f;
+  } else if ((F & F_QUAD) && kind == PK_QUAD) {
+    const V3 n = xyz(p.a);
+    const float denom = dot3(n, r.d);
+    s.normal = n;
+    s.ray_normal = (-n) * signumf(denom);
+    s.front = signbit(denom);
+    planar_uv(sc.quad_ext + 9ull * __float_as_uint(p.c.w), xyz(p.c), s.pos, s.u, s.v);
+  } else if ((F & F_CYLINDER) && kind == PK_CYLINDER) {
+    // cylinder.rs:118-172: the same root, then its normal
+    CylHit ch;
+    cylinder_t(p, r, start, CUDART_INF_F, ch);
+    const V3 o1 = xyz(p.a), along = xyz(p.b);
+    const float rad = p.c.y, len = p.c.z;
+    V3 n;
+    if (ch.face == 0) {
+      const V3 oc = v3(r.o.x - o1.x, r.o.y - o1.y, r.o.z - o1.z);
+      const V3 rel = at3(oc, r.d, ch.t);
+      const V3 out = v3(rel.x - along.x * ch.dan, rel.y - along.y * ch.dan, rel.z - along.z * ch.dan);
+      n = v3(__fdiv_rn(out.x, rad), __fdiv_rn(out.y, rad), __fdiv_rn(out.z, rad));
+    } else {
+      n = v3(__fdiv_rn(along.x, len), __fdiv_rn(along.y, len), __fdiv_rn(along.z, len)) * signumf(ch.dan);
+    }
+    const float inside = -signumf(dot3(r.d, n));
+    s.normal = n;
+    s.ray_normal = n * inside;
+    s.front = signbit(inside);
+    s.side = ch.face;
+    s.u = s.v = 0.0f;  // cylinder uv is only needed by textured / Uv modes
   } else {
     // Media: arbitrary normals drawn from the free-flight block (volumetric.rs:147-153)
     uint32_t vi = s.prim_id - sc.vol_base;
@@ -877,7 +1009,7 @@ __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x,
       break;
     }
     Surface surf;
-    finalize_hit<F>(sc, ray, h, ctx, surf);
+    finalize_hit<F>(sc, ray, h, ctx, surf, 1e-3f);
     const rg_material m = sc.materials[surf.material];
     if (m.kind == RG_MAT_LIGHT) {
       L = C3f{L.r + beta.r * m.albedo[0], L.g + beta.g * m.albedo[1], L.b + beta.b * m.albedo[2]};

@@ -125,11 +125,12 @@ __device__ __forceinline__ void record_hit(const GpuScene& sc, const FrameParams
   if (hit) {
     uint32_t mat;
     int code = h.prim;
-    if ((F & F_SDF) && h.sdf >= 0) {
+    if ((F & (F_SDF | F_PLANE)) && h.sdf >= 0) {
       mat = sc.sdfs[h.sdf].material;
       code = -2 - h.sdf;
       s.aux[p] = make_float4(h.sh.n.x, h.sh.n.y, h.sh.n.z,
-                             __uint_as_float((h.sh.front ? 0x80000000u : 0u) | (h.sh.side & 0x7FFFFFFFu)));
+                             __uint_as_float((h.sh.front ? 0x80000000u : 0u) | (h.sh.flip ? 0x40000000u : 0u) |
+                                             (h.sh.side & 0x3FFFFFFFu)));
     } else {
       mat = prim_material(sc.prims[h.prim]);
     }
@@ -239,7 +240,8 @@ __global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp,
       uint32_t f = __float_as_uint(a.w);
       h.sh.n = v3(a.x, a.y, a.z);
       h.sh.front = (f >> 31) != 0;
-      h.sh.side = f & 0x7FFFFFFFu;
+      h.sh.flip = ((f >> 30) & 1u) != 0;
+      h.sh.side = f & 0x3FFFFFFFu;
       h.sh.t = h.t;
     }
     const bool alive = shade_path<F>(sc, fp, s, p, pix, smp, __float_as_uint(r0.w), r, C3f{r2.x, r2.y, r2.z},

@@ -77,7 +77,7 @@ __device__ __forceinline__ bool shade_path(const GpuScene& sc, const FrameParams
   }
   RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
   Surface surf;
-  finalize_hit<F>(sc, r, h, ctx, surf);
+  finalize_hit<F>(sc, r, h, ctx, surf, 1e-3f);
   const rg_material m = sc.materials[surf.material];
   if (m.kind == RG_MAT_LIGHT) {
     finish_path(s, p, C3f{0.0f + beta.r * m.albedo[0], 0.0f + beta.g * m.albedo[1], 0.0f + beta.b * m.albedo[2]});

@@ -5,7 +5,9 @@ Names, fields and defaults follow the reference so that code written against
 
 * meshes        — SphereMesh (mesh/primitive/sphere.rs), Triangle
                   (mesh/primitive/triangle.rs), BvhMesh (mesh/advanced/bvh.rs),
-                  AxisBoxMesh (mesh/primitive/axis_box.rs),
+                  AxisBoxMesh (mesh/primitive/axis_box.rs), CylinderMesh
+                  (mesh/primitive/cylinder.rs), ParallelogramMesh and
+                  InfinitePlaneMesh over a Planar (mesh/planar/*.rs),
                   RaymarchedIsosurfaceMesh (mesh/isosurface/raymarched.rs)
 * objects       — SimpleObject (object/simple.rs), VolumetricObject
                   (object/volumetric.rs), ObjectList (object/list.rs)
@@ -278,6 +280,69 @@ class AxisBoxMesh:
 
 
 @dataclass
+class Planar:
+    """mesh/planar/mod.rs:33-121: a corner `p` and two sides `u`, `v`."""
+    p: tuple
+    u: tuple
+    v: tuple
+
+    @staticmethod
+    def new(p, u, v) -> "Planar":
+        return Planar(_vec3(p), _vec3(u), _vec3(v))
+
+    @staticmethod
+    def new_centred(centre, u, v) -> "Planar":
+        """Planar::new_centred (mod.rs:82-86): sides 2u and 2v around `centre`."""
+        c, u, v = np.asarray(_vec3(centre)), np.asarray(_vec3(u)), np.asarray(_vec3(v))
+        return Planar.new(c - u - v, u * 2.0, v * 2.0)
+
+    @staticmethod
+    def new_points(a, b, c) -> "Planar":
+        """Planar::new_points (mod.rs:116-119): corner b, sides a - b and c - b."""
+        a, b, c = np.asarray(_vec3(a)), np.asarray(_vec3(b)), np.asarray(_vec3(c))
+        return Planar.new(b, a - b, c - b)
+
+    def flat(self) -> tuple:
+        return (*self.p, *self.u, *self.v)
+
+
+def _planar(x) -> Planar:
+    if isinstance(x, Planar):
+        return x
+    if isinstance(x, (tuple, list)) and len(x) == 3:  # From<[P; 3]>: three points (mod.rs:124-131)
+        return Planar.new_points(*x)
+    raise TypeError(f"cannot make a Planar from {type(x).__name__}")
+
+
+@dataclass
+class ParallelogramMesh:
+    """mesh/planar/parallelogram.rs: the points p + a u + b v with a, b in [0, 1]."""
+    plane: Any
+
+    def __post_init__(self):
+        self.plane = _planar(self.plane)
+
+
+@dataclass
+class InfinitePlaneMesh:
+    """mesh/planar/infinite_plane.rs: the whole plane (unbounded). uv_wrap only
+    affects texture coordinates, which solid textures do not read."""
+    plane: Any
+    uv_wrap: str = "wrap"
+
+    def __post_init__(self):
+        self.plane = _planar(self.plane)
+
+
+@dataclass
+class CylinderMesh:
+    """mesh/primitive/cylinder.rs: capped cylinder from p1 to p2."""
+    p1: tuple
+    p2: tuple
+    radius: float
+
+
+@dataclass
 class SdfSphere:
     centre: tuple
     radius: float
@@ -364,6 +429,9 @@ class FlatScene:
         self.boxes, self.box_mat = [], []
         self.volumes: list = []
         self.sdfs: list = []
+        self.quads, self.quad_mat = [], []
+        self.cylinders, self.cyl_mat = [], []
+        self.planes, self.plane_mat = [], []
         self.skybox = A.RG_SKY_SIMPLE
         self.n_meshes = 0
 
@@ -404,6 +472,15 @@ class FlatScene:
                 self.box_mat.append(mat)
             elif isinstance(mesh, RaymarchedIsosurfaceMesh):
                 self.sdfs.append(self._sdf(mesh, mat))
+            elif isinstance(mesh, ParallelogramMesh):
+                self.quads.append(mesh.plane.flat())
+                self.quad_mat.append(mat)
+            elif isinstance(mesh, CylinderMesh):
+                self.cylinders.append((*_vec3(mesh.p1), *_vec3(mesh.p2), float(mesh.radius)))
+                self.cyl_mat.append(mat)
+            elif isinstance(mesh, InfinitePlaneMesh):
+                self.planes.append(mesh.plane.flat())
+                self.plane_mat.append(mat)
             else:
                 raise UnsupportedVariant(f"mesh {type(mesh).__name__} cannot cross the C ABI")
         elif isinstance(obj, VolumetricObject):
@@ -460,6 +537,12 @@ class FlatScene:
             self.a_tri_mesh = np.zeros(0, np.int32)
         self.a_boxes = np.ascontiguousarray(np.asarray(self.boxes, f32).reshape(-1, 6))
         self.a_box_mat = np.ascontiguousarray(np.asarray(self.box_mat, u32))
+        self.a_quads = np.ascontiguousarray(np.asarray(self.quads, f32).reshape(-1, 9))
+        self.a_quad_mat = np.ascontiguousarray(np.asarray(self.quad_mat, u32))
+        self.a_cyls = np.ascontiguousarray(np.asarray(self.cylinders, f32).reshape(-1, 7))
+        self.a_cyl_mat = np.ascontiguousarray(np.asarray(self.cyl_mat, u32))
+        self.a_planes = np.ascontiguousarray(np.asarray(self.planes, f32).reshape(-1, 9))
+        self.a_plane_mat = np.ascontiguousarray(np.asarray(self.plane_mat, u32))
         self.c_volumes = (A.rg_volume * max(1, len(self.volumes)))(*self.volumes)
         self.c_sdfs = (A.rg_sdf * max(1, len(self.sdfs)))(*self.sdfs)
         self.c_materials = (A.rg_material * max(1, len(self.materials)))(*self.materials)
@@ -476,17 +559,23 @@ class FlatScene:
         d.n_sdfs, d.sdfs = len(self.sdfs), self.c_sdfs
         d.n_materials, d.materials = len(self.materials), self.c_materials
         d.skybox = self.skybox
+        d.n_quads, d.quads, d.quad_material = len(self.a_quads), fp(self.a_quads), up(self.a_quad_mat)
+        d.n_cylinders, d.cylinders, d.cylinder_material = len(self.a_cyls), fp(self.a_cyls), up(self.a_cyl_mat)
+        d.n_planes, d.planes, d.plane_material = len(self.a_planes), fp(self.a_planes), up(self.a_plane_mat)
         self.desc = d
         return self
 
     @property
     def n_prims(self) -> int:
-        return self.desc.n_spheres + self.desc.n_triangles + self.desc.n_boxes + self.desc.n_volumes + self.desc.n_sdfs
+        d = self.desc
+        return (d.n_spheres + d.n_triangles + d.n_boxes + d.n_volumes + d.n_sdfs + d.n_quads + d.n_cylinders +
+                d.n_planes)
 
 
 def flatten(scene: Scene) -> FlatScene:
     """Flattens a Scene into rg_scene_desc arrays (object order: spheres,
-    standalone triangles, meshes, boxes, volumes, SDFs)."""
+    standalone triangles, meshes, boxes, volumes, parallelograms, cylinders;
+    unbounded: SDFs, infinite planes)."""
     fs = FlatScene()
     sky = scene.skybox
     if sky is None:

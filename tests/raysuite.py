@@ -73,3 +73,27 @@ def sdf_scene():
         SimpleObject(SphereMesh((0.0, 1.5, 0.0), 0.4), LambertianMaterial((0.5, 0.5, 0.5))),
     ]
     return Scene(objects=objs, skybox=SimpleSkybox())
+
+
+def planar_scene(seed=0):
+    """Parallelograms of random orientation and shape (some thin, some large),
+    cylinders of random axis, two infinite planes, and a few spheres."""
+    from rayna_gb300.scene import CylinderMesh, InfinitePlaneMesh, ParallelogramMesh, Planar
+    rng = np.random.Generator(np.random.PCG64(seed))
+    objs = []
+    for _ in range(150):
+        p = rng.uniform(-3, 3, 3)
+        u = rng.normal(size=3) * rng.uniform(0.05, 1.5)
+        v = rng.normal(size=3) * rng.uniform(0.05, 1.5)
+        objs.append(SimpleObject(ParallelogramMesh(Planar.new(p, u, v)), LambertianMaterial(tuple(rng.random(3)))))
+    for _ in range(60):
+        p1 = rng.uniform(-3, 3, 3)
+        p2 = p1 + rng.normal(size=3) * rng.uniform(0.1, 1.5)
+        objs.append(SimpleObject(CylinderMesh(tuple(p1), tuple(p2), float(rng.uniform(0.05, 0.5))),
+                                 MetalMaterial(tuple(rng.uniform(0.5, 1, 3)), 0.1)))
+    objs.append(SimpleObject(InfinitePlaneMesh(Planar.new((0, -3.5, 0), (1, 0, 0), (0, 0, 1))), LambertianMaterial((0.5, 0.5, 0.5))))
+    objs.append(SimpleObject(InfinitePlaneMesh(Planar.new((0, 0, -4), (0.3, 1, 0), (1, 0, 0.2))), LambertianMaterial((0.3, 0.6, 0.3))))
+    for _ in range(10):
+        objs.append(SimpleObject(SphereMesh(tuple(rng.uniform(-3, 3, 3)), float(rng.uniform(0.1, 0.6))),
+                                 LambertianMaterial((0.5, 0.5, 0.5))))
+    return Scene(objects=objs)
