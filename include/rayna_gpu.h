@@ -39,7 +39,7 @@ extern "C" {
 typedef enum rg_status {
     RG_OK = 0,
     RG_INVALID_ARG = 1,          /* malformed descriptor, NaN/Inf parameter, bad size */
-    RG_UNSUPPORTED_VARIANT = 2,  /* a reference variant this library does not run (e.g. RenderMode other than PBR) */
+    RG_UNSUPPORTED_VARIANT = 2,  /* a reference variant this library does not run (e.g. a non-identity transform) */
     RG_INVALID_CAMERA = 3,       /* Camera::calculate_viewport returned Err (scene/camera.rs:114-167) */
     RG_OOM = 4,                  /* device or host allocation failed */
     RG_CUDA_ERROR = 5,           /* a CUDA runtime call failed; see rg_last_error */
@@ -154,7 +154,11 @@ typedef struct rg_scene_desc {
     uint32_t n_planes;               /* InfinitePlaneMesh (mesh/planar/infinite_plane.rs): unbounded */
     const float* planes;             /* n x 9: Planar p, u, v */
     const uint32_t* plane_material;
+    const uint32_t* plane_uv_wrap;   /* n: RG_UV_WRAP_* (UvWrappingMode, infinite_plane.rs:18-45); NULL = all WRAP */
 } rg_scene_desc;
+
+/* UvWrappingMode of an infinite plane's texture coordinates. */
+enum { RG_UV_WRAP = 0, RG_UV_MIRROR = 1, RG_UV_CLAMP_ZERO = 2 };
 
 /* Camera (rayna_engine/src/scene/camera.rs:10-25), angles in radians. */
 typedef struct rg_camera {
@@ -177,7 +181,9 @@ enum {
     RG_MODE_SIDE = 7
 };
 
-/* RenderOpts (render_opts.rs:8-29). width/height/samples/ray_branching are
+/* RenderOpts (render_opts.rs:8-29). Every RenderMode renders (the debug modes
+ * and ray_branching > 1 by the megakernel, whatever the handle's form);
+ * ray_branching^(ray_depth + 1) must stay below 2^32. width/height/samples/ray_branching are
  * NonZeroUsize in the reference: 0 is rejected with RG_INVALID_ARG. */
 typedef struct rg_render_opts {
     uint32_t width;

@@ -51,8 +51,8 @@ int render_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_op
                 int gpu_sampling, int threads, double* out_mean, double* out_var, double* out_seconds) {
   Viewport vp;
   if (!calculate_viewport(*cam, vp)) return RG_INVALID_CAMERA;
-  if (opts->width == 0 || opts->height == 0 || opts->samples == 0 || opts->ray_branching != 1) return RG_INVALID_ARG;
-  if (opts->mode != RG_MODE_PBR) return RG_UNSUPPORTED_VARIANT;
+  if (opts->width == 0 || opts->height == 0 || opts->samples == 0 || opts->ray_branching == 0) return RG_INVALID_ARG;
+  if (opts->mode > RG_MODE_SIDE) return RG_UNSUPPORTED_VARIANT;
   Scene<P> sc;
   sc.load(*d, Options{});
   const uint32_t W = opts->width, H = opts->height;
@@ -62,6 +62,8 @@ int render_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_op
   for (uint32_t f = 0; f < frames; ++f) {
     uint64_t fseed = seed + (uint64_t)f * 0x9E3779B97F4A7C15ull;
     RenderParams rp{W, H, opts->samples, opts->ray_depth, fseed};
+    rp.mode = opts->mode;
+    rp.branching = opts->ray_branching;
     Renderer<P> R(sc, vp, rp);
     std::atomic<uint32_t> next_row{0};
     auto work = [&]() {

@@ -543,11 +543,44 @@ template <class P> struct Cylinder {
     h.normal = normal;
     h.ray_normal = normal * inside;
     h.front_face = std::signbit(inside);
-    h.u = h.v = T(0);
     h.side = face;
+    // uv (cylinder.rs:130-172) in the frame of Vector3::any_orthonormal_pair of the axis
+    V3<T> o0, o1;
+    orthonormal_pair(along / length, o0, o1);
+    if (face == 0) {
+      T theta = std::acos(M::dot(normal, o1)) * M::signum(M::dot(normal, o0));
+      h.u = theta / T(M_PI) / T(2) + T(0.5);
+      h.v = dan;
+    } else {
+      V3<T> q = M::at(oc, rd, dist) / radius;
+      h.u = M::dot(q, o0) / T(2) + T(0.5);
+      h.v = M::dot(q, o1) / T(2) + T(0.5);
+    }
     return true;
   }
+  // Duff et al., "Building an Orthonormal Basis, Revisited" (JCGT 2017), the
+  // method of glam's any_orthonormal_pair.
+  static void orthonormal_pair(V3<T> n, V3<T>& b1, V3<T>& b2) {
+    T sign = std::copysign(T(1), n.z);
+    T a = T(-1) / (sign + n.z);
+    T b = n.x * n.y * a;
+    b1 = {T(1) + sign * n.x * n.x * a, sign * b, -sign * n.x};
+    b2 = {b, sign + n.y * n.y * a, -n.y};
+  }
 };
+
+// UvWrappingMode::apply (mesh/planar/infinite_plane.rs:26-41)
+template <class T> inline void wrap_uv(uint32_t mode, T& u, T& v) {
+  if (mode == RG_UV_WRAP) {
+    u = std::fmod(u, T(1)); if (u < T(0)) u = u + T(1);
+    v = std::fmod(v, T(1)); if (v < T(0)) v = v + T(1);
+  } else if (mode == RG_UV_MIRROR) {
+    u = std::fabs(std::fmod(u, T(2)) - T(1));
+    v = std::fabs(std::fmod(v, T(2)) - T(1));
+  } else if (!(T(0) <= u && u <= T(1) && T(0) <= v && v <= T(1))) {
+    u = v = T(0);
+  }
+}
 
 // Signed distance functions evaluated in world space.
 template <class P> struct Sdf {
@@ -865,7 +898,7 @@ template <class P> struct Scene {
   std::vector<Parallelogram<P>> quads;
   std::vector<Cylinder<P>> cylinders;
   std::vector<Planar<P>> planes;
-  std::vector<uint32_t> sphere_mat, tri_mat, box_mat, quad_mat, cyl_mat, plane_mat;
+  std::vector<uint32_t> sphere_mat, tri_mat, box_mat, quad_mat, cyl_mat, plane_mat, plane_wrap;
   std::vector<rg_material> materials;
   uint32_t skybox = RG_SKY_SIMPLE;
   uint32_t ns = 0, nt = 0, nb = 0, nv = 0, nsdf = 0, nq = 0, nc = 0, npl = 0;
@@ -908,6 +941,7 @@ template <class P> struct Scene {
       Planar<P>::make(d.planes + 9 * i, q);
       planes.push_back(q);
       plane_mat.push_back(d.plane_material[i]);
+      plane_wrap.push_back(d.plane_uv_wrap ? d.plane_uv_wrap[i] : (uint32_t)RG_UV_WRAP);
     }
     materials.assign(d.materials, d.materials + d.n_materials);
     for (uint32_t i = 0; i < ns; ++i) {
@@ -1141,6 +1175,7 @@ template <class P> struct Scene {
       Hit<T> hs;
       if (u.plane) {
         if (!planes[u.index].intersect(ray, iv, hs)) continue;  // InfinitePlaneMesh::intersect (infinite_plane.rs:87-92)
+        wrap_uv(plane_wrap[u.index], hs.u, hs.v);
       } else if (!sdfs[u.index].intersect(ray, iv, hs)) {
         continue;
       }
@@ -1311,6 +1346,8 @@ template <class P> inline C3 attenuation(const rg_material& m, const Ray<P>& ray
 struct RenderParams {
   uint32_t width, height, spp, ray_depth;
   uint64_t seed;
+  uint32_t mode = RG_MODE_PBR;  // RenderOpts::mode
+  uint32_t branching = 1;       // RenderOpts::ray_branching
 };
 
 template <class P> struct Renderer {
@@ -1321,7 +1358,9 @@ template <class P> struct Renderer {
   RenderParams rp;
   Renderer(const Scene<P>& s, const Viewport& v, const RenderParams& r) : sc(s), vp(v), rp(r) {}
 
-  // ray_colour_recursive (renderer.rs:508-572), branching 1.
+  // ray_colour_recursive (renderer.rs:508-572): `branching` scattered rays per
+  // bounce, a failed scatter counting as a black sample, their mean added to
+  // the emission.
   C3 colour_recursive(const Ray<P>& ray, uint32_t depth, PathRng& rng) const {
     if (depth > rp.ray_depth) return {0, 0, 0};
     Hit<T> h;
@@ -1329,12 +1368,88 @@ template <class P> struct Renderer {
     if (!sc.intersect(ray, iv, rng, depth, h)) return sky_colour<P>(sc.skybox, ray);
     const rg_material& m = sc.materials[h.material];
     C3 emitted = m.kind == RG_MAT_LIGHT ? C3{m.albedo[0], m.albedo[1], m.albedo[2]} : C3{0, 0, 0};
-    V dir;
-    if (!scatter<P>(m, ray, h, rng, depth, dir)) return emitted + C3{0, 0, 0} * (1.0f / 1.0f);
-    Ray<P> next = Ray<P>::make(h.pos_w, dir);
-    C3 fut = colour_recursive(next, depth + 1, rng);
-    C3 scattered = m.kind == RG_MAT_LIGHT ? C3{0, 0, 0} : fut * attenuation<P>(m, ray, h);
-    return emitted + scattered;
+    C3 sum{0, 0, 0};
+    for (uint32_t i = 0; i < rp.branching; ++i) {
+      V dir;
+      if (!scatter<P>(m, ray, h, rng, depth, dir)) continue;  // Colour::BLACK
+      Ray<P> next = Ray<P>::make(h.pos_w, dir);
+      C3 fut = colour_recursive(next, depth + 1, rng);
+      C3 scattered = m.kind == RG_MAT_LIGHT ? C3{0, 0, 0} : fut * attenuation<P>(m, ray, h);
+      sum = sum + scattered;
+    }
+    return emitted + sum * (1.0f / (float)rp.branching);
+  }
+
+  // The device's walk of the branching tree (trace.cuh, branch_sample): node
+  // weights pushed down, streams keyed by node (children n b + 1 + i, scatter
+  // of branch i keyed n b + i).
+  C3 colour_branch_gpu(Ray<P> ray, PathRng& rng) const {
+    struct Level { Hit<T> h; Ray<P> in; C3 w; uint32_t node, next; };
+    std::vector<Level> st;
+    const uint32_t b = rp.branching;
+    const float inv_b = 1.0f / (float)b;
+    C3 L{0, 0, 0}, w{1, 1, 1};
+    uint32_t node = 0, depth = 0;
+    for (;;) {
+      Hit<T> h;
+      Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
+      if (!sc.intersect(ray, iv, rng, node, h)) {
+        L = L + w * sky_colour<P>(sc.skybox, ray);
+      } else {
+        const rg_material& m = sc.materials[h.material];
+        if (m.kind == RG_MAT_LIGHT) L = L + w * C3{m.albedo[0], m.albedo[1], m.albedo[2]};
+        else if (depth < rp.ray_depth && st.size() < 32) st.push_back(Level{h, ray, w, node, 0});
+      }
+      bool found = false;
+      while (!st.empty()) {
+        Level& lv = st.back();
+        if (lv.next >= b) { st.pop_back(); continue; }
+        uint32_t i = lv.next++;
+        const rg_material& m = sc.materials[lv.h.material];
+        V dir;
+        if (!scatter<P>(m, lv.in, lv.h, rng, lv.node * b + i, dir)) continue;
+        C3 a = attenuation<P>(m, lv.in, lv.h);
+        w = lv.w * a * inv_b;
+        ray = Ray<P>::make(lv.h.pos_w, dir);
+        node = lv.node * b + 1 + i;
+        depth = (uint32_t)st.size();
+        found = true;
+        break;
+      }
+      if (!found) break;
+    }
+    return L;
+  }
+
+  // Render::render_px_once for the debug modes (renderer.rs:427-490).
+  C3 mode_colour(const Ray<P>& ray, PathRng& rng) const {
+    Hit<T> h;
+    Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
+    if (!sc.intersect(ray, iv, rng, 0, h)) return sky_colour<P>(sc.skybox, ray);
+    static const float kCol[13][3] = {{1, 1, 1}, {1, 0, 0}, {1, 0.5f, 0}, {1, 1, 0}, {0.5f, 1, 0}, {0, 1, 0}, {0, 1, 0.5f},
+                                      {0, 1, 1}, {0, 0.5f, 1}, {0, 0, 1}, {0.5f, 0, 1}, {1, 0, 1}, {0, 0, 0}};
+    auto half = [](V v) { return C3{(float)(v.x / T(2)) + 0.5f, (float)(v.y / T(2)) + 0.5f, (float)(v.z / T(2)) + 0.5f}; };
+    auto col = [&](int k) { return C3{kCol[k][0], kCol[k][1], kCol[k][2]}; };
+    switch (rp.mode) {
+      case RG_MODE_OUTWARD_NORMAL: return half(h.normal);
+      case RG_MODE_RAY_NORMAL: return half(h.ray_normal);
+      case RG_MODE_SCATTER: {
+        V dir{0, 0, 0};
+        if (!scatter<P>(sc.materials[h.material], ray, h, rng, 0, dir)) dir = V{0, 0, 0};
+        return half(dir);
+      }
+      case RG_MODE_UV:
+        return C3{std::fmin(std::fmax((float)h.u, 0.0f), 1.0f), std::fmin(std::fmax((float)h.v, 0.0f), 1.0f), 0.0f};
+      case RG_MODE_FRONT_FACE: return col(h.front_face ? 1 : 0);
+      case RG_MODE_SIDE: return col((int)(h.side % 12u + 1u));
+      default: {  // distance
+        T val = T(2) * std::cbrt(h.dist);
+        T fl = std::fmin(std::fmax(std::floor(val), T(0)), T(12)), ce = std::fmin(std::fmax(std::ceil(val), T(0)), T(12));
+        float frac = (float)(val - fl);
+        C3 a = col((int)fl), bcol = col((int)ce);
+        return C3{a.r + (bcol.r - a.r) * frac, a.g + (bcol.g - a.g) * frac, a.b + (bcol.b - a.b) * frac};
+      }
+    }
   }
 
   // The device integrator: the same recursion evaluated front to back.
@@ -1516,6 +1631,8 @@ template <class P> struct Renderer {
       fy = (T)y + jy;
     }
     Ray<P> ray = camera_ray(fx, fy, lx, ly);
+    if (rp.mode != RG_MODE_PBR) return mode_colour(ray, rng);
+    if (rp.branching > 1) return gpu_sampling ? colour_branch_gpu(ray, rng) : colour_recursive(ray, 0, rng);
     return gpu_sampling ? colour_iterative(ray, rng) : colour_recursive(ray, 0, rng);
   }
 };

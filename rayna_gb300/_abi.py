@@ -38,6 +38,7 @@ RG_FORM_MEGAKERNEL, RG_FORM_WAVEFRONT = range(2)
 RG_FLAG_COUNTERS = 1
 RG_FLAG_STAGE_TIMES = 2
 RG_BATCH_WAVEFRONT = 0
+RG_UV_WRAP, RG_UV_MIRROR, RG_UV_CLAMP_ZERO = 0, 1, 2
 RG_BATCH_TILES = 1
 
 
@@ -70,6 +71,7 @@ class rg_scene_desc(C.Structure):
         ("n_cylinders", C.c_uint32), ("cylinders", C.POINTER(C.c_float)),
         ("cylinder_material", C.POINTER(C.c_uint32)),
         ("n_planes", C.c_uint32), ("planes", C.POINTER(C.c_float)), ("plane_material", C.POINTER(C.c_uint32)),
+        ("plane_uv_wrap", C.POINTER(C.c_uint32)),
     ]
 
 

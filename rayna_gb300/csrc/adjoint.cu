@@ -234,6 +234,8 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
   const uint32_t w = h->opts.width, hh = h->opts.height;
   const size_t npx3 = (size_t)w * hh * 3;
   const uint32_t n_mat = (uint32_t)h->host.materials.size(), n_vol = h->host.nv;
+  if (h->opts.mode != RG_MODE_PBR || h->opts.ray_branching != 1)
+    return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward differentiates RenderMode::PBR with ray_branching 1");
   if (h->opts.ray_depth + 1 > (uint32_t)kAdjMaxVertices)
     return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward supports ray_depth <= 16");
   if (n_vol > (uint32_t)kAdjMaxVolumes) return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward supports at most 4 media");

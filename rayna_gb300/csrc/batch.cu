@@ -510,6 +510,10 @@ rg_status rg_batch_create(const rg_device_opts* opts, uint32_t n, const rg_scene
     if ((st = rg_set_camera(h, &cameras[i])) != RG_OK) { b->err = h->err; break; }
     if ((st = rg_set_options(h, &options[i])) != RG_OK) { b->err = h->err; break; }
     if (!h->cam_ok) { st = bfail(b, RG_INVALID_CAMERA, "render %u: invalid camera", i); break; }
+    if (h->opts.mode != RG_MODE_PBR || h->opts.ray_branching != 1) {
+      st = bfail(b, RG_UNSUPPORTED_VARIANT, "render %u: batches render RenderMode::PBR with ray_branching 1", i);
+      break;
+    }
     if ((st = ensure_frame_buffers(h)) != RG_OK) { b->err = h->err; break; }
     b->features |= kinds_of(h->gs.features);
   }

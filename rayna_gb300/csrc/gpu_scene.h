@@ -95,6 +95,10 @@ struct alignas(16) WideNode {
 };
 static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
 constexpr int kWideMaxLeaf = 3;
+// ray_branching > 1: largest branching factor, and depth of the per-sample
+// tree walk's stack (b^(ray_depth + 1) < 2^32 keeps ray_depth + 1 <= 32).
+constexpr uint32_t kMaxBranching = 64;
+constexpr int kBranchStack = 32;
 // The wide traversal's stack holds at most one node group per tree level, so
 // trees deeper than this traverse the binary layout instead.
 constexpr int kWideMaxDepth = 60;
@@ -105,7 +109,8 @@ constexpr int kMaxBuildDepth = 60;
 
 // Unbounded objects, tested after the tree in list order: the SDF kinds of
 // rg_sdf, and infinite planes (kind kUnboundedPlane: normal in (cx, cy, cz),
-// plane offset d in p0).
+// plane offset d in p0, corner p in (p1, p2, p3), its u, v, w at quad_ext
+// entry max_iter, uv wrap mode in the bits of pad[0]).
 constexpr uint32_t kUnboundedPlane = 16;
 struct GpuSdf {
   uint32_t kind;
@@ -187,6 +192,8 @@ enum : uint32_t { CNT_RAYS = 0, CNT_NODES = 1, CNT_PRIMS = 2, CNT_SDF = 3, CNT_S
 // Per-frame launch parameters (all f32 values rounded from the f64 host viewport).
 struct FrameParams {
   uint32_t width, height, spp, ray_depth;
+  uint32_t mode;          // RG_MODE_*: PBR, or a single-intersection visualisation
+  uint32_t branching;     // RenderOpts::ray_branching: scattered rays per bounce
   uint32_t strat_d;
   float strat_inv;
   uint32_t seed_lo, seed_hi;

@@ -11,12 +11,12 @@ namespace rg {
 constexpr int kMegaBlock = 256;
 constexpr int kWarpsPerBlock = kMegaBlock / 32;
 
-template <uint32_t F, bool COUNT>
+template <uint32_t F, bool COUNT, uint32_t KIND = kSamplePbr>
 __global__ void __launch_bounds__(kMegaBlock) k_megakernel(GpuScene sc, FrameParams fp, uint32_t n_pix) {
   const uint32_t warp = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   Counters cnt;
   uint32_t segments = 0;
-  mega_round<F, COUNT>(sc, fp, warp * pixels_per_round(fp.spp), n_pix, cnt, segments);
+  mega_round<F, COUNT, KIND>(sc, fp, warp * pixels_per_round(fp.spp), n_pix, cnt, segments);
   flush_counters<COUNT>(fp, cnt, segments);
 }
 
@@ -32,6 +32,20 @@ cudaError_t launch_megakernel(const GpuScene& sc, const FrameParams& fp, bool co
   const uint32_t ppw = pixels_per_round(fp.spp);
   const uint32_t warps = (n_pix + ppw - 1) / ppw;
   const uint32_t blocks = (warps + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (fp.mode != RG_MODE_PBR || fp.branching > 1) {
+    // Debug render modes and ray_branching > 1: one variant over every
+    // primitive kind (these are not throughput paths); work counters off.
+    const uint32_t kind = fp.mode != RG_MODE_PBR ? kSampleMode : kSampleBranch;
+    const bool wide = (sc.features & F_WIDE) != 0;
+    if (kind == kSampleMode) {
+      if (wide) k_megakernel<F_ALL | F_WIDE, false, kSampleMode><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+      else k_megakernel<F_ALL, false, kSampleMode><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+    } else {
+      if (wide) k_megakernel<F_ALL | F_WIDE, false, kSampleBranch><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+      else k_megakernel<F_ALL, false, kSampleBranch><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+    }
+    return cudaGetLastError();
+  }
   dispatch_features(sc.features, [&](auto f) {
     launch_mega<decltype(f)::value>(sc, fp, counters, blocks, n_pix, stream);
     return 0;

@@ -199,8 +199,11 @@ rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
   for (uint32_t i = 0; i < d.n_quads; ++i)
     if (!planar_ok(d.quads + 9ull * i, "parallelogram", i) || !mat_ok(d.quad_material[i], "parallelogram", i))
       return RG_INVALID_ARG;
-  for (uint32_t i = 0; i < d.n_planes; ++i)
+  for (uint32_t i = 0; i < d.n_planes; ++i) {
     if (!planar_ok(d.planes + 9ull * i, "plane", i) || !mat_ok(d.plane_material[i], "plane", i)) return RG_INVALID_ARG;
+    if (d.plane_uv_wrap && d.plane_uv_wrap[i] > RG_UV_CLAMP_ZERO)
+      return fail(h, RG_INVALID_ARG, "plane %u: uv wrap mode %u", i, d.plane_uv_wrap[i]);
+  }
   for (uint32_t i = 0; i < d.n_cylinders; ++i) {
     const float* c = d.cylinders + 7ull * i;
     if (!finite3(c) || !finite3(c + 3) || !std::isfinite(c[6])) return fail(h, RG_INVALID_ARG, "cylinder %u is not finite", i);
@@ -346,7 +349,7 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
       hi[3ull * k + a] = std::nextafter((float)(mx[a] + pad), INFINITY);
     }
   };
-  hs.quad_ext.resize(9ull * hs.nq);
+  hs.quad_ext.resize(9ull * (hs.nq + hs.npl));  // parallelograms, then infinite planes
   for (uint32_t i = 0; i < hs.nq; ++i, ++id, ++pi) {
     PlanarF64 q;
     planar_f64(d.quads + 9ull * i, q);
@@ -388,6 +391,11 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
     g.kind = kUnboundedPlane;
     g.cx = (float)q.n[0]; g.cy = (float)q.n[1]; g.cz = (float)q.n[2];
     g.p0 = (float)q.d;
+    g.p1 = (float)q.p[0]; g.p2 = (float)q.p[1]; g.p3 = (float)q.p[2];
+    g.max_iter = hs.nq + i;  // its u, v, w in quad_ext
+    g.pad[0] = bits_float(d.plane_uv_wrap ? d.plane_uv_wrap[i] : (uint32_t)RG_UV_WRAP);
+    float* e = hs.quad_ext.data() + 9ull * (hs.nq + i);
+    for (int k = 0; k < 3; ++k) { e[k] = (float)q.u[k]; e[3 + k] = (float)q.v[k]; e[6 + k] = (float)q.w[k]; }
     g.material = d.plane_material[i];
     g.prim_id = id;
     hs.sdfs.push_back(g);
@@ -517,6 +525,8 @@ void fill_frame_params(rg_renderer* h, uint64_t seed, FrameParams& fp) {
   fp.height = h->opts.height;
   fp.spp = h->opts.samples;
   fp.ray_depth = h->opts.ray_depth;
+  fp.mode = h->opts.mode;
+  fp.branching = h->opts.ray_branching;
   uint32_t d = (uint32_t)std::sqrt((double)fp.spp);
   while ((uint64_t)(d + 1) * (d + 1) <= fp.spp) ++d;
   while ((uint64_t)d * d > fp.spp) --d;
@@ -769,8 +779,17 @@ rg_status rg_set_options(rg_handle h, const rg_render_opts* opts) {
   if (opts->width == 0 || opts->height == 0 || opts->samples == 0 || opts->ray_branching == 0)
     return fail(h, RG_INVALID_ARG, "width, height, samples and ray_branching must be non-zero");
   if ((uint64_t)opts->width * opts->height > (1ull << 30)) return fail(h, RG_INVALID_ARG, "image too large");
-  if (opts->mode != RG_MODE_PBR) return fail(h, RG_UNSUPPORTED_VARIANT, "only RenderMode::PBR is supported (mode %u)", opts->mode);
-  if (opts->ray_branching != 1) return fail(h, RG_UNSUPPORTED_VARIANT, "only ray_branching = 1 is supported");
+  if (opts->mode > RG_MODE_SIDE) return fail(h, RG_UNSUPPORTED_VARIANT, "unknown RenderMode %u", opts->mode);
+  // With b > 1 a sample traces up to (b^(depth+1) - 1) / (b - 1) rays; the
+  // random streams key each tree node by a 32-bit id, so the tree must fit.
+  if (opts->ray_branching > 1) {
+    if (opts->ray_branching > kMaxBranching)
+      return fail(h, RG_INVALID_ARG, "ray_branching %u exceeds %u", opts->ray_branching, kMaxBranching);
+    double nodes = std::pow((double)opts->ray_branching, (double)opts->ray_depth + 1.0);
+    if (nodes > 4294967295.0 || opts->ray_depth + 1 > (uint32_t)kBranchStack)
+      return fail(h, RG_INVALID_ARG, "ray_branching^(ray_depth + 1) must stay below 2^32 (got %u^%u)", opts->ray_branching,
+                  opts->ray_depth + 1);
+  }
   if (opts->ray_depth > 4096) return fail(h, RG_INVALID_ARG, "ray_depth too large");
   h->opts = *opts;
   return rg_clear_accumulation(h);
@@ -790,7 +809,9 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
   cudaError_t e;
   h->last_launches = 1;
   h->stage_used = 0;
-  if (h->form == RG_FORM_WAVEFRONT) {
+  // The wavefront kernels run the PBR path with one scattered ray per
+  // bounce; debug render modes and ray_branching > 1 take the megakernel.
+  if (h->form == RG_FORM_WAVEFRONT && fp.mode == RG_MODE_PBR && fp.branching == 1) {
     e = launch_wavefront(h, fp);
   } else {
     if ((h->flags & RG_FLAG_STAGE_TIMES) && (e = stage_mark(h)) != cudaSuccess) return cuda_fail(h, e, "stage event");

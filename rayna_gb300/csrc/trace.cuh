@@ -783,7 +783,42 @@ struct Surface {
   float u, v;
 };
 
-template <uint32_t F>
+// sphere_uv (mesh/primitive/sphere.rs:114-121)
+__device__ __forceinline__ void sphere_uv(V3 local, float& u, float& v) {
+  const float kPi = 3.14159265358979323846f;
+  const float theta = acosf(-local.y);
+  const float phi = atan2f(-local.z, local.x) + kPi;
+  u = phi / (2.0f * kPi);
+  v = theta / kPi;
+}
+
+// Vector3::any_orthonormal_pair of a unit vector (cylinder.rs:41): Duff et
+// al., "Building an Orthonormal Basis, Revisited" (JCGT 2017).
+__device__ __forceinline__ void orthonormal_pair(V3 n, V3& b1, V3& b2) {
+  const float sign = copysignf(1.0f, n.z);
+  const float a = __fdiv_rn(-1.0f, sign + n.z);
+  const float b = n.x * n.y * a;
+  b1 = v3(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+  b2 = v3(b, sign + n.y * n.y * a, -n.y);
+}
+
+// UvWrappingMode::apply (mesh/planar/infinite_plane.rs:26-41)
+__device__ __forceinline__ void wrap_uv(uint32_t mode, float& u, float& v) {
+  if (mode == RG_UV_WRAP) {
+    u = fmodf(u, 1.0f); if (u < 0.0f) u = u + 1.0f;  // rem_euclid(1.0)
+    v = fmodf(v, 1.0f); if (v < 0.0f) v = v + 1.0f;
+  } else if (mode == RG_UV_MIRROR) {
+    u = fabsf(fmodf(u, 2.0f) - 1.0f);
+    v = fabsf(fmodf(v, 2.0f) - 1.0f);
+  } else if (!(0.0f <= u && u <= 1.0f && 0.0f <= v && v <= 1.0f)) {
+    u = v = 0.0f;
+  }
+}
+
+// Full hit record of the closest hit. UV: also the texture coordinates that
+// only the Uv render mode reads (sphere, cylinder and infinite-plane uv cost
+// transcendentals or extra fetches; the other kinds compute them anyway).
+template <uint32_t F, bool UV = false>
 __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, const HitRec& h, const RngCtx& ctx, Surface& s,
                                              float start) {
   if ((F & (F_SDF | F_PLANE)) && h.sdf >= 0) {
@@ -792,6 +827,17 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
     s.normal = h.sh.n;
     // raymarched.rs:113-114: not flipped; planar/mod.rs:190: -n * signum(denom)
     s.ray_normal = h.sh.flip ? -h.sh.n : h.sh.n;
+    if (UV && (F & F_PLANE) && f.kind == kUnboundedPlane) {
+      float u, v;
+      planar_uv(sc.quad_ext + 9ull * f.max_iter, v3(f.p1, f.p2, f.p3), s.pos, u, v);
+      wrap_uv(__float_as_uint(f.pad[0]), u, v);
+      s.front = h.sh.front;
+      s.material = f.material;
+      s.prim_id = f.prim_id;
+      s.side = 0;
+      s.u = u; s.v = v;
+      return;
+    }
     s.front = h.sh.front;
     s.material = f.material;
     s.prim_id = f.prim_id;
@@ -815,7 +861,8 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
     s.normal = local;
     s.ray_normal = inside ? -local : local;
     s.front = !inside;
-    s.u = s.v = 0.0f;  // sphere_uv is only needed by textured / Uv modes
+    s.u = s.v = 0.0f;
+    if (UV) sphere_uv(local, s.u, s.v);
   } else if ((F & F_TRI) && kind == PK_TRIANGLE) {
     float t, u, v, det;
     triangle_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, CUDART_INF_F, t, u, v, det);
@@ -862,7 +909,24 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
     s.ray_normal = n * inside;
     s.front = signbit(inside);
     s.side = ch.face;
-    s.u = s.v = 0.0f;  // cylinder uv is only needed by textured / Uv modes
+    s.u = s.v = 0.0f;
+    if (UV) {  // cylinder.rs:130-172
+      const V3 ax = v3(__fdiv_rn(along.x, len), __fdiv_rn(along.y, len), __fdiv_rn(along.z, len));
+      V3 o0, o1v;
+      orthonormal_pair(ax, o0, o1v);
+      const V3 oc = v3(r.o.x - o1.x, r.o.y - o1.y, r.o.z - o1.z);
+      if (ch.face == 0) {
+        const float kPi = 3.14159265358979323846f;
+        const float theta = acosf(dot3(n, o1v)) * signumf(dot3(n, o0));
+        s.u = theta / kPi / 2.0f + 0.5f;
+        s.v = ch.dan;
+      } else {
+        const V3 rel = at3(oc, r.d, ch.t);
+        const V3 q = v3(__fdiv_rn(rel.x, rad), __fdiv_rn(rel.y, rad), __fdiv_rn(rel.z, rad));
+        s.u = dot3(q, o0) / 2.0f + 0.5f;
+        s.v = dot3(q, o1v) / 2.0f + 0.5f;
+      }
+    }
   } else {
     // Media: arbitrary normals drawn from the free-flight block (volumetric.rs:147-153)
     uint32_t vi = s.prim_id - sc.vol_base;
@@ -991,13 +1055,131 @@ __device__ __forceinline__ Ray camera_ray(const FrameParams& fp, uint32_t x, uin
   return make_ray(rpos, ps - rpos);
 }
 
-// One path sample: ray_colour_recursive (renderer.rs:508-572) evaluated front
-// to back: L = sum_k beta_k * emitted_k + beta_K * sky.
+// What a megakernel sample computes (k_megakernel's KIND): the PBR path with
+// one scattered ray per bounce, a debug render mode, or ray_branching > 1.
+enum : uint32_t { kSamplePbr = 0, kSampleMode = 1, kSampleBranch = 2 };
+
+// Render::render_px_once for the debug modes (renderer.rs:427-490): one
+// intersection of the camera ray, coloured by mode; the sky on a miss.
 template <uint32_t F, bool COUNT>
+__device__ C3f mode_sample(const GpuScene& sc, const FrameParams& fp, const Ray& ray, RngCtx& ctx, Counters& cnt,
+                           uint32_t& segments) {
+  ctx.depth = 0;
+  HitRec h;
+  ++segments;
+  if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) return sky_colour(sc.sky, ray.d);
+  Surface s;
+  finalize_hit<F, true>(sc, ray, h, ctx, s, 1e-3f);
+  // The reference's visualisation colours (renderer.rs:439-453)
+  const float kCol[13][3] = {{1, 1, 1}, {1, 0, 0},     {1, 0.5f, 0}, {1, 1, 0}, {0.5f, 1, 0},  {0, 1, 0}, {0, 1, 0.5f},
+                             {0, 1, 1}, {0, 0.5f, 1}, {0, 0, 1},    {0.5f, 0, 1}, {1, 0, 1}, {0, 0, 0}};
+  auto half = [](V3 v) { return C3f{v.x / 2.0f + 0.5f, v.y / 2.0f + 0.5f, v.z / 2.0f + 0.5f}; };
+  switch (fp.mode) {
+    case RG_MODE_OUTWARD_NORMAL:
+      return half(s.normal);
+    case RG_MODE_RAY_NORMAL:
+      return half(s.ray_normal);
+    case RG_MODE_SCATTER: {
+      V3 dir = v3(0.0f, 0.0f, 0.0f);  // unwrap_or_default
+      if (!scatter(sc.materials[s.material], ray, s, ctx, dir)) dir = v3(0.0f, 0.0f, 0.0f);
+      return half(dir);
+    }
+    case RG_MODE_UV:
+      return C3f{fminf(fmaxf(s.u, 0.0f), 1.0f), fminf(fmaxf(s.v, 0.0f), 1.0f), 0.0f};
+    case RG_MODE_FRONT_FACE: {
+      const float* c = kCol[s.front ? 1 : 0];
+      return C3f{c[0], c[1], c[2]};
+    }
+    case RG_MODE_SIDE: {
+      const float* c = kCol[s.side % 12u + 1u];
+      return C3f{c[0], c[1], c[2]};
+    }
+    default: {  // RG_MODE_DISTANCE
+      const float val = 2.0f * cbrtf(h.t);
+      const float fl = fminf(fmaxf(floorf(val), 0.0f), 12.0f), ce = fminf(fmaxf(ceilf(val), 0.0f), 12.0f);
+      const float frac = val - fl;
+      const float* a = kCol[(int)fl];
+      const float* b = kCol[(int)ce];
+      return C3f{a[0] + (b[0] - a[0]) * frac, a[1] + (b[1] - a[1]) * frac, a[2] + (b[2] - a[2]) * frac};
+    }
+  }
+}
+
+// ray_colour_recursive with ray_branching b > 1 (renderer.rs:508-572): every
+// surface hit below ray_depth spawns b scattered rays and averages their
+// colours. Walked depth-first with an explicit stack; each tree node keeps its
+// weight (the product of attenuation / b down to it), so a node adds weight x
+// (emission or sky). Random streams are keyed by node: node n's children are
+// n b + 1 + i, its free-flight draws use key n and the scatter of branch i key
+// n b + i (for b = 1 these reduce to the depth keys of the PBR path).
+template <uint32_t F, bool COUNT>
+__device__ C3f branch_sample(const GpuScene& sc, const FrameParams& fp, Ray ray, RngCtx& ctx, Counters& cnt,
+                             uint32_t& segments) {
+  struct Level {
+    Surface surf;
+    Ray in;
+    C3f w;
+    uint32_t node, next;
+  };
+  Level st[kBranchStack];
+  int top = -1;
+  const uint32_t b = fp.branching;
+  const float inv_b = 1.0f / (float)b;
+  C3f L{0.0f, 0.0f, 0.0f}, w{1.0f, 1.0f, 1.0f};
+  uint32_t node = 0, depth = 0;
+  for (;;) {
+    ctx.depth = node;
+    HitRec h;
+    ++segments;
+    if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
+      const C3f sk = sky_colour(sc.sky, ray.d);
+      L = C3f{L.r + w.r * sk.r, L.g + w.g * sk.g, L.b + w.b * sk.b};
+    } else {
+      Surface surf;
+      finalize_hit<F>(sc, ray, h, ctx, surf, 1e-3f);
+      const rg_material m = sc.materials[surf.material];
+      if (m.kind == RG_MAT_LIGHT) {
+        L = C3f{L.r + w.r * m.albedo[0], L.g + w.g * m.albedo[1], L.b + w.b * m.albedo[2]};
+      } else if (depth < fp.ray_depth && top + 1 < kBranchStack) {
+        ++top;
+        st[top] = Level{surf, ray, w, node, 0u};
+      }
+    }
+    // next child: the deepest level with branches left
+    bool found = false;
+    while (top >= 0) {
+      Level& lv = st[top];
+      if (lv.next >= b) {
+        --top;
+        continue;
+      }
+      const uint32_t i = lv.next++;
+      const rg_material m = sc.materials[lv.surf.material];
+      ctx.depth = lv.node * b + i;
+      V3 dir;
+      if (!scatter(m, lv.in, lv.surf, ctx, dir)) continue;  // a black branch
+      const C3f a = attenuation(m, lv.in, lv.surf);
+      w = C3f{lv.w.r * a.r * inv_b, lv.w.g * a.g * inv_b, lv.w.b * a.b * inv_b};
+      ray = make_ray(lv.surf.pos, dir);
+      node = lv.node * b + 1u + i;
+      depth = (uint32_t)top + 1u;
+      found = true;
+      break;
+    }
+    if (!found) break;
+  }
+  return L;
+}
+
+// One sample of pixel (x, y). PBR: ray_colour_recursive (renderer.rs:508-572)
+// evaluated front to back, L = sum_k beta_k * emitted_k + beta_K * sky.
+template <uint32_t F, bool COUNT, uint32_t KIND = kSamplePbr>
 __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x, uint32_t y, uint32_t s, Counters& cnt,
                           uint32_t& segments) {
   RngCtx ctx{fp.seed_lo, fp.seed_hi, y * fp.width + x, s, 0, nullptr};
   Ray ray = camera_ray(fp, x, y, s, ctx);
+  if (KIND == kSampleMode) return mode_sample<F, COUNT>(sc, fp, ray, ctx, cnt, segments);
+  if (KIND == kSampleBranch) return branch_sample<F, COUNT>(sc, fp, ray, ctx, cnt, segments);
   C3f L{0.0f, 0.0f, 0.0f}, beta{1.0f, 1.0f, 1.0f};
   for (uint32_t depth = 0; depth <= fp.ray_depth; ++depth) {
     ctx.depth = depth;

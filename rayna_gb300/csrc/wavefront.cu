@@ -402,6 +402,9 @@ extern "C" rg_status rg_render_static_scratch(rg_handle h, uint64_t seed, float*
   cudaError_t e = cudaSetDevice(h->device);
   if (e != cudaSuccess) return set_error(h, RG_CUDA_ERROR, cudaGetErrorString(e));
   if (!h->cam_ok) return set_error(h, RG_INVALID_CAMERA, "camera viewport could not be calculated");
+  if (h->opts.mode != RG_MODE_PBR || h->opts.ray_branching != 1)
+    return set_error(h, RG_UNSUPPORTED_VARIANT,
+                     "rg_render_static_scratch renders RenderMode::PBR with ray_branching 1 only");
   if (h->opts.samples > RG_STATIC_WAVE_PATHS)
     return set_error(h, RG_INVALID_ARG,
                      "rg_render_static_scratch: samples per pixel exceed the 65536 path slots of the static scratch");

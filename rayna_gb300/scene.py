@@ -325,8 +325,9 @@ class ParallelogramMesh:
 
 @dataclass
 class InfinitePlaneMesh:
-    """mesh/planar/infinite_plane.rs: the whole plane (unbounded). uv_wrap only
-    affects texture coordinates, which solid textures do not read."""
+    """mesh/planar/infinite_plane.rs: the whole plane (unbounded). uv_wrap
+    ("wrap", "mirror" or "clamp_zero", UvWrappingMode) maps its texture
+    coordinates; solid textures do not read them, the Uv render mode does."""
     plane: Any
     uv_wrap: str = "wrap"
 
@@ -431,7 +432,7 @@ class FlatScene:
         self.sdfs: list = []
         self.quads, self.quad_mat = [], []
         self.cylinders, self.cyl_mat = [], []
-        self.planes, self.plane_mat = [], []
+        self.planes, self.plane_mat, self.plane_wrap = [], [], []
         self.skybox = A.RG_SKY_SIMPLE
         self.n_meshes = 0
 
@@ -481,6 +482,8 @@ class FlatScene:
             elif isinstance(mesh, InfinitePlaneMesh):
                 self.planes.append(mesh.plane.flat())
                 self.plane_mat.append(mat)
+                self.plane_wrap.append({"wrap": A.RG_UV_WRAP, "mirror": A.RG_UV_MIRROR,
+                                        "clamp_zero": A.RG_UV_CLAMP_ZERO}[mesh.uv_wrap])
             else:
                 raise UnsupportedVariant(f"mesh {type(mesh).__name__} cannot cross the C ABI")
         elif isinstance(obj, VolumetricObject):
@@ -543,6 +546,7 @@ class FlatScene:
         self.a_cyl_mat = np.ascontiguousarray(np.asarray(self.cyl_mat, u32))
         self.a_planes = np.ascontiguousarray(np.asarray(self.planes, f32).reshape(-1, 9))
         self.a_plane_mat = np.ascontiguousarray(np.asarray(self.plane_mat, u32))
+        self.a_plane_wrap = np.ascontiguousarray(np.asarray(self.plane_wrap, u32))
         self.c_volumes = (A.rg_volume * max(1, len(self.volumes)))(*self.volumes)
         self.c_sdfs = (A.rg_sdf * max(1, len(self.sdfs)))(*self.sdfs)
         self.c_materials = (A.rg_material * max(1, len(self.materials)))(*self.materials)
@@ -562,6 +566,7 @@ class FlatScene:
         d.n_quads, d.quads, d.quad_material = len(self.a_quads), fp(self.a_quads), up(self.a_quad_mat)
         d.n_cylinders, d.cylinders, d.cylinder_material = len(self.a_cyls), fp(self.a_cyls), up(self.a_cyl_mat)
         d.n_planes, d.planes, d.plane_material = len(self.a_planes), fp(self.a_planes), up(self.a_plane_mat)
+        d.plane_uv_wrap = up(self.a_plane_wrap)
         self.desc = d
         return self
 

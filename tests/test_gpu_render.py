@@ -142,14 +142,71 @@ def test_invalid_camera_returns_checker():
             np.testing.assert_array_equal(out.img[x, y], exp)
 
 
-def test_unsupported_mode_and_zero_sizes_are_rejected():
+def test_oversized_branching_and_zero_sizes_are_rejected():
     scene = presets.single_sphere((0.5, 0.5, 0.5))
     with Renderer.new_from(scene, Camera(), RenderOpts(width=8, height=8), 0) as r:
-        with pytest.raises(RaynaError) as e:
-            r.set_options(RenderOpts(width=8, height=8, mode=RenderMode.Uv))
-        assert e.value.status == 2
+        with pytest.raises(RaynaError) as e:  # 2^41 tree nodes per sample
+            r.set_options(RenderOpts(width=8, height=8, ray_depth=40, ray_branching=2))
+        assert e.value.status == 1
         with pytest.raises(ValueError):
             r.set_options(RenderOpts(width=0, height=8))
+
+
+MODE_CASES = {
+    "planar": lambda: small(presets.cornell_quads, 40, 40, 4, 8),
+    "spheres": lambda: small(presets.random_spheres, 48, 27, 4, 8),
+    "sdf_volumes": lambda: small(presets.sdf_volumes, 48, 27, 4, 8, n_spheres=20),
+}
+
+
+@pytest.mark.parametrize("mode", [m for m in RenderMode if m != RenderMode.PBR])
+@pytest.mark.parametrize("case", list(MODE_CASES))
+def test_debug_modes_path_by_path(case, mode):
+    """render_px_once's visualisations (renderer.rs:427-490) against the f32
+    oracle with the same streams. Exact except where a transcendental's last
+    ulp differs (sphere and cylinder uv, the Mandelbulb, cbrt of the distance)."""
+    scene, cam, opts = MODE_CASES[case]()
+    opts.mode = mode
+    flat = flatten(scene)
+    with Renderer.new_from(scene, cam, opts, 0, form="wavefront") as r:  # routes to the megakernel
+        r.render(seed=41)
+        gm, _ = r.frame_moments()
+    st, om, _, _ = ob.render(flat, cam, opts, seed=41, frames=1, policy=ob.POLICY_GPU_F32)
+    assert st == 0
+    close = np.all(np.abs(gm - om) <= 1e-5 * (1 + np.abs(om)), axis=2).mean()
+    print(f"{case} {mode.name}: {close:.4f} of pixels match")
+    assert close >= (0.95 if case == "sdf_volumes" else 0.99)
+
+
+def test_branching_path_by_path_and_statistics():
+    """ray_branching = 2 (renderer.rs:536-568): the device's tree walk equals the
+    f32 oracle's walk path for path, and its mean agrees with the faithful f64
+    recursion within 3 standard errors; branching 1 renders the usual image."""
+    scene, cam, opts = small(presets.cornell_quads, 24, 24, 4, 4)
+    flat = flatten(scene)
+    opts.ray_branching = 2
+    with Renderer.new_from(scene, cam, opts, 0) as r:
+        r.render(seed=5)
+        gm, _ = r.frame_moments()
+    st, om, _, _ = ob.render(flat, cam, opts, seed=5, frames=1, policy=ob.POLICY_GPU_F32)
+    close = np.all(np.abs(gm - om) <= 1e-4 * (1 + np.abs(om)), axis=2).mean()
+    print(f"branching 2: {close:.4f} of pixels match the f32 oracle")
+    assert close >= 0.97
+    frames, spp = 24, opts.samples
+    sq = 0.0
+    with Renderer.new_from(scene, cam, opts, 0, seed=3) as r:
+        for _ in range(frames):
+            out = r.render()
+            fm, fv = r.frame_moments()
+            sq = sq + (spp - 1) * fv.astype(np.float64) + spp * fm.astype(np.float64) ** 2
+        img = out.img.astype(np.float64)
+    st, om, ov, _ = ob.render(flat, cam, opts, seed=9, frames=frames, policy=ob.POLICY_REF_F64)
+    n = frames * spp
+    gv = np.maximum(sq / n - img ** 2, 0.0) * n / (n - 1)
+    z = (img - om) / np.maximum(np.sqrt((gv + ov) / n), 1e-6)
+    beyond = np.mean(np.abs(z) > 3)
+    print(f"branching 2: {beyond:.4f} of pixel channels beyond 3 SE")
+    assert beyond <= 0.01
 
 
 def test_large_spp_path_and_counters():
