@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 4u
+#define RG_ABI_VERSION 5u
 
 /* Status codes. 0 is success. */
 typedef enum rg_status {
@@ -155,7 +155,22 @@ typedef struct rg_scene_desc {
     const float* planes;             /* n x 9: Planar p, u, v */
     const uint32_t* plane_material;
     const uint32_t* plane_uv_wrap;   /* n: RG_UV_WRAP_* (UvWrappingMode, infinite_plane.rs:18-45); NULL = all WRAP */
+
+    /* ObjectTransform of SimpleObjects (object/transform.rs): a ray is mapped
+     * into mesh space by the inverse, tested against the mesh with the caller's
+     * interval, and the hit mapped back (point and normals by the transform,
+     * distance recomputed in world space). */
+    uint32_t n_transforms;
+    const double* transforms;            /* n x 12: 3 x 4 affine matrix, mesh space to world space, row-major, with
+                                            SimpleObject::new's correction about the mesh centre already applied */
+    const uint32_t* sphere_transform;    /* n_spheres: index into transforms or RG_NO_TRANSFORM; NULL = none */
+    const uint32_t* tri_transform;       /* n_triangles */
+    const uint32_t* box_transform;       /* n_boxes */
+    const uint32_t* quad_transform;      /* n_quads */
+    const uint32_t* cylinder_transform;  /* n_cylinders */
 } rg_scene_desc;
+
+#define RG_NO_TRANSFORM 0xFFFFFFFFu
 
 /* UvWrappingMode of an infinite plane's texture coordinates. */
 enum { RG_UV_WRAP = 0, RG_UV_MIRROR = 1, RG_UV_CLAMP_ZERO = 2 };

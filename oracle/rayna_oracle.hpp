@@ -711,6 +711,86 @@ template <class T> inline V3<T> unit_sphere_from(T r1, T r2) {
 // ---------------------------------------------------------------------------
 enum ObjKind : uint32_t { OBJ_SPHERE, OBJ_TRIANGLE, OBJ_MESH, OBJ_BOX, OBJ_VOLUME, OBJ_SDF, OBJ_QUAD, OBJ_CYLINDER };
 
+// ---------------------------------------------------------------------------
+// ObjectTransform (object/transform.rs): 3 x 4 affine matrices, row-major.
+// ---------------------------------------------------------------------------
+// [A | t]^-1 = [A^-1 | -A^-1 t] in double, A^-1 from cofactors; false if A is
+// singular. The device's host build computes the same, then rounds to f32.
+inline bool affine_inverse(const double* m, double* inv) {
+  const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], hh = m[9], i = m[10];
+  const double c00 = e * i - f * hh, c01 = f * g - d * i, c02 = d * hh - e * g;
+  const double det = a * c00 + b * c01 + c * c02;
+  if (!std::isfinite(det) || det == 0.0) return false;
+  const double r = 1.0 / det;
+  const double A[9] = {c00 * r, (c * hh - b * i) * r, (b * f - c * e) * r,
+                       c01 * r, (a * i - c * g) * r, (c * d - a * f) * r,
+                       c02 * r, (b * g - a * hh) * r, (a * e - b * d) * r};
+  for (int row = 0; row < 3; ++row) {
+    for (int k = 0; k < 3; ++k) inv[4 * row + k] = A[3 * row + k];
+    inv[4 * row + 3] = -(A[3 * row] * m[3] + A[3 * row + 1] * m[7] + A[3 * row + 2] * m[11]);
+  }
+  for (int k = 0; k < 12; ++k)
+    if (!std::isfinite(inv[k])) return false;
+  return true;
+}
+
+// Transform3::map_point / map_vector. RefF64: glam's column order
+// ((c0 x + c1 y) + c2 z) + t; GpuF32: the device's fma chain.
+template <class P> inline V3<typename P::T> xf_point(const typename P::T* m, V3<typename P::T> p) {
+  if constexpr (P::gpu)
+    return {std::fma(m[0], p.x, std::fma(m[1], p.y, std::fma(m[2], p.z, m[3]))),
+            std::fma(m[4], p.x, std::fma(m[5], p.y, std::fma(m[6], p.z, m[7]))),
+            std::fma(m[8], p.x, std::fma(m[9], p.y, std::fma(m[10], p.z, m[11])))};
+  else
+    return {((m[0] * p.x + m[1] * p.y) + m[2] * p.z) + m[3], ((m[4] * p.x + m[5] * p.y) + m[6] * p.z) + m[7],
+            ((m[8] * p.x + m[9] * p.y) + m[10] * p.z) + m[11]};
+}
+template <class P> inline V3<typename P::T> xf_vector(const typename P::T* m, V3<typename P::T> v) {
+  if constexpr (P::gpu)
+    return {std::fma(m[0], v.x, std::fma(m[1], v.y, m[2] * v.z)), std::fma(m[4], v.x, std::fma(m[5], v.y, m[6] * v.z)),
+            std::fma(m[8], v.x, std::fma(m[9], v.y, m[10] * v.z))};
+  else
+    return {(m[0] * v.x + m[1] * v.y) + m[2] * v.z, (m[4] * v.x + m[5] * v.y) + m[6] * v.z,
+            (m[8] * v.x + m[9] * v.y) + m[10] * v.z};
+}
+
+template <class P> struct Xform {
+  using T = typename P::T;
+  T inv[12], fwd[12];
+  double fwd64[12];
+  // ObjectTransform::incoming_ray (transform.rs:90-97)
+  Ray<P> incoming(const Ray<P>& r) const { return Ray<P>::make(xf_point<P>(inv, r.pos), xf_vector<P>(inv, r.dir)); }
+  // ObjectTransform::outgoing_intersection (transform.rs:101-130): the point
+  // at the mesh-space distance mapped out, both normals by the transform's
+  // linear part and normalised, the distance recomputed in world space.
+  void outgoing(const Ray<P>& world, const Ray<P>& local, Hit<T>& h) const {
+    h.pos_w = xf_point<P>(fwd, Math<P>::at(local.pos, local.dir, h.dist));
+    h.normal = Math<P>::normalize(xf_vector<P>(fwd, h.normal));
+    h.ray_normal = Math<P>::normalize(xf_vector<P>(fwd, h.ray_normal));
+    h.dist = Math<P>::length(h.pos_w - world.pos);
+  }
+  // ObjectTransform::calculate_aabb (transform.rs:133-144): the mapped
+  // corners, encompassed. In f64, rounded outward for the f32 policy.
+  Aabb<T> map_box(const Aabb<T>& b) const {
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 8; ++c) {
+      const double q[3] = {(double)((c & 1) ? b.mx.x : b.mn.x), (double)((c & 2) ? b.mx.y : b.mn.y),
+                           (double)((c & 4) ? b.mx.z : b.mn.z)};
+      for (int a = 0; a < 3; ++a) {
+        const double v = ((fwd64[4 * a] * q[0] + fwd64[4 * a + 1] * q[1]) + fwd64[4 * a + 2] * q[2]) + fwd64[4 * a + 3];
+        mn[a] = std::min(mn[a], v);
+        mx[a] = std::max(mx[a], v);
+      }
+    }
+    Aabb<T> r;
+    auto dn = [](double v) { return P::gpu ? (T)std::nextafter((float)v, -INFINITY) : (T)v; };
+    auto up = [](double v) { return P::gpu ? (T)std::nextafter((float)v, INFINITY) : (T)v; };
+    r.mn = {dn(mn[0]), dn(mn[1]), dn(mn[2])};
+    r.mx = {up(mx[0]), up(mx[1]), up(mx[2])};
+    return r;
+  }
+};
+
 template <class P> struct Scene;
 
 // GenericBvh node (shared/generic_bvh.rs:30-36): Nested(aabb) with children,
@@ -903,9 +983,11 @@ template <class P> struct Scene {
   uint32_t skybox = RG_SKY_SIMPLE;
   uint32_t ns = 0, nt = 0, nb = 0, nv = 0, nsdf = 0, nq = 0, nc = 0, npl = 0;
 
-  struct Mesh { std::vector<uint32_t> tris; Bvh<T> bvh; uint32_t material; Aabb<T> box; };
+  struct Mesh { std::vector<uint32_t> tris; Bvh<T> bvh; uint32_t material; Aabb<T> box; int32_t xf = -1; };
   std::vector<Mesh> meshes;
-  struct Object { uint32_t kind, index; Aabb<T> box; };
+  std::vector<Xform<P>> xforms;
+  std::vector<int32_t> sphere_xf, tri_xf, box_xf, quad_xf, cyl_xf;  // transform index, or -1
+  struct Object { uint32_t kind, index; Aabb<T> box; int32_t xf = -1; };
   std::vector<Object> bounded;    // ObjectList::bvh items, in list order
   struct Unbounded { bool plane; uint32_t index; };
   std::vector<Unbounded> unbounded; // SDFs, then infinite planes, in list order
@@ -944,6 +1026,27 @@ template <class P> struct Scene {
       plane_wrap.push_back(d.plane_uv_wrap ? d.plane_uv_wrap[i] : (uint32_t)RG_UV_WRAP);
     }
     materials.assign(d.materials, d.materials + d.n_materials);
+    for (uint32_t k = 0; k < d.n_transforms; ++k) {
+      Xform<P> x;
+      double inv[12];
+      affine_inverse(d.transforms + 12 * k, inv);
+      for (int j = 0; j < 12; ++j) {
+        x.fwd64[j] = d.transforms[12 * k + j];
+        x.inv[j] = P::gpu ? (T)(float)inv[j] : (T)inv[j];
+        x.fwd[j] = P::gpu ? (T)(float)d.transforms[12 * k + j] : (T)d.transforms[12 * k + j];
+      }
+      xforms.push_back(x);
+    }
+    auto xf_list = [](const uint32_t* idx, uint32_t n, std::vector<int32_t>& out) {
+      out.assign(n, -1);
+      if (idx)
+        for (uint32_t i = 0; i < n; ++i) out[i] = idx[i] == RG_NO_TRANSFORM ? -1 : (int32_t)idx[i];
+    };
+    xf_list(d.sphere_transform, ns, sphere_xf);
+    xf_list(d.tri_transform, nt, tri_xf);
+    xf_list(d.box_transform, nb, box_xf);
+    xf_list(d.quad_transform, nq, quad_xf);
+    xf_list(d.cylinder_transform, nc, cyl_xf);
     for (uint32_t i = 0; i < ns; ++i) {
       Sphere<P> s;
       s.c = {(T)d.spheres[4 * i], (T)d.spheres[4 * i + 1], (T)d.spheres[4 * i + 2]};
@@ -991,13 +1094,23 @@ template <class P> struct Scene {
     }
     // Objects in list order: spheres, standalone triangles, meshes, boxes, volumes, parallelograms,
     // cylinders; SDFs and infinite planes unbounded.
-    for (uint32_t i = 0; i < ns; ++i) bounded.push_back({OBJ_SPHERE, i, spheres[i].aabb()});
+    // SimpleObject::new (object/simple.rs:67-91): a transformed object's box
+    // is its mesh's box mapped by the transform.
+    auto obj = [&](uint32_t kind, uint32_t i, const Aabb<T>& box, int32_t xf) {
+      bounded.push_back({kind, i, xf >= 0 ? xforms[xf].map_box(box) : box, xf});
+    };
+    for (uint32_t i = 0; i < ns; ++i) obj(OBJ_SPHERE, i, spheres[i].aabb(), sphere_xf[i]);
     std::vector<int32_t> mesh_ids;
     for (uint32_t i = 0; i < nt; ++i) {
       int32_t g = d.tri_mesh ? d.tri_mesh[i] : -1;
-      if (g < 0) { bounded.push_back({OBJ_TRIANGLE, i, tris[i].aabb()}); continue; }
+      if (g < 0) { obj(OBJ_TRIANGLE, i, tris[i].aabb(), tri_xf[i]); continue; }
       size_t k = std::find(mesh_ids.begin(), mesh_ids.end(), g) - mesh_ids.begin();
-      if (k == mesh_ids.size()) { mesh_ids.push_back(g); meshes.push_back(Mesh{}); meshes.back().material = tri_mat[i]; }
+      if (k == mesh_ids.size()) {
+        mesh_ids.push_back(g);
+        meshes.push_back(Mesh{});
+        meshes.back().material = tri_mat[i];
+        meshes.back().xf = tri_xf[i];
+      }
       meshes[k].tris.push_back(i);
     }
     std::vector<size_t> order(meshes.size());
@@ -1009,13 +1122,13 @@ template <class P> struct Scene {
       for (uint32_t t : m.tris) bx.push_back(tris[t].aabb());
       build_bvh(bx, m.bvh, opt.exact_bvh_limit);
       m.box = m.bvh.nodes[m.bvh.root].box;  // BvhMesh::aabb: the root's box (mesh/advanced/bvh.rs:117-131)
-      bounded.push_back({OBJ_MESH, (uint32_t)k, m.box});
+      obj(OBJ_MESH, (uint32_t)k, m.box, m.xf);
     }
-    for (uint32_t i = 0; i < nb; ++i) bounded.push_back({OBJ_BOX, i, boxes[i].aabb()});
+    for (uint32_t i = 0; i < nb; ++i) obj(OBJ_BOX, i, boxes[i].aabb(), box_xf[i]);
     for (uint32_t i = 0; i < nv; ++i)
-      bounded.push_back({OBJ_VOLUME, i, volumes[i].boundary == RG_BOUNDARY_SPHERE ? volumes[i].s.aabb() : volumes[i].b.aabb()});
-    for (uint32_t i = 0; i < nq; ++i) bounded.push_back({OBJ_QUAD, i, quads[i].aabb()});
-    for (uint32_t i = 0; i < nc; ++i) bounded.push_back({OBJ_CYLINDER, i, cylinders[i].aabb()});
+      obj(OBJ_VOLUME, i, volumes[i].boundary == RG_BOUNDARY_SPHERE ? volumes[i].s.aabb() : volumes[i].b.aabb(), -1);
+    for (uint32_t i = 0; i < nq; ++i) obj(OBJ_QUAD, i, quads[i].aabb(), quad_xf[i]);
+    for (uint32_t i = 0; i < nc; ++i) obj(OBJ_CYLINDER, i, cylinders[i].aabb(), cyl_xf[i]);
     for (uint32_t i = 0; i < nsdf; ++i) unbounded.push_back({false, i});
     for (uint32_t i = 0; i < npl; ++i) unbounded.push_back({true, i});
     std::vector<Aabb<T>> bx;
@@ -1066,7 +1179,30 @@ template <class P> struct Scene {
     return true;
   }
 
+  // SimpleObject::full_intersect (object/simple.rs:107-116): a transformed
+  // object tests its mesh against the mapped ray with the caller's interval
+  // (RefF64). The device (GpuF32) tests from the same start without an end
+  // and bounds the world-space distance instead; both agree for rigid
+  // transforms, and under scaling the reference's result depends on the
+  // order in which objects are tested.
   bool object_intersect(const Object& o, const Ray<P>& ray, const Interval<T>& iv, PathRng& rng, uint32_t depth, Hit<T>& h) const {
+    if (o.xf < 0) return mesh_intersect(o, ray, iv, rng, depth, h);
+    const Xform<P>& x = xforms[o.xf];
+    const Ray<P> local = x.incoming(ray);
+    if constexpr (P::gpu) {
+      Interval<T> open = iv;
+      open.has_end = false;
+      if (!mesh_intersect(o, local, open, rng, depth, h)) return false;
+      x.outgoing(ray, local, h);
+      return !iv.has_end || h.dist <= iv.end;
+    } else {
+      if (!mesh_intersect(o, local, iv, rng, depth, h)) return false;
+      x.outgoing(ray, local, h);
+      return true;
+    }
+  }
+
+  bool mesh_intersect(const Object& o, const Ray<P>& ray, const Interval<T>& iv, PathRng& rng, uint32_t depth, Hit<T>& h) const {
     switch (o.kind) {
       case OBJ_SPHERE:
         if (!spheres[o.index].intersect(ray, iv, h)) return false;
@@ -1147,9 +1283,18 @@ template <class P> struct Scene {
     for (const Object& o : bounded) {
       if (o.kind == OBJ_MESH) {
         const Mesh& m = meshes[o.index];
+        const Ray<P> local = m.xf >= 0 ? xforms[m.xf].incoming(ray) : ray;
         for (uint32_t t : m.tris) {
           Hit<T> hc;
-          if (!tris[t].intersect(ray, sh, hc)) continue;
+          if (m.xf >= 0) {  // as object_intersect, one triangle at a time
+            Interval<T> ti = sh;
+            if (P::gpu) ti.has_end = false;
+            if (!tris[t].intersect(local, ti, hc)) continue;
+            xforms[m.xf].outgoing(ray, local, hc);
+            if (P::gpu && sh.has_end && !(hc.dist <= sh.end)) continue;
+          } else if (!tris[t].intersect(local, sh, hc)) {
+            continue;
+          }
           hc.prim = prim_tri(t);
           hc.material = m.material;
           sh = sh.with_end(hc.dist);

@@ -8,10 +8,10 @@ scene, camera, options and Renderer types over that ABI.
 """
 from .scene import (  # noqa: F401
     Angle, AxisBoxMesh, BvhMesh, Camera, CylinderMesh, DielectricMaterial, InfinitePlaneMesh, IsotropicMaterial,
-    LambertianMaterial, ParallelogramMesh, Planar,
+    LambertianMaterial, ObjectTransform, ParallelogramMesh, Planar,
     LightMaterial, MetalMaterial, NoSkybox, ObjectList, RaymarchedIsosurfaceMesh, RenderMode, RenderOpts,
     Scene, SdfMandelbulb, SdfSphere, SdfTorus, SimpleObject, SimpleSkybox, SolidTexture, SphereMesh,
-    StandardScene, Triangle, UnsupportedVariant, VolumetricObject, WhiteSkybox, flatten,
+    StandardScene, Transform3, Triangle, UnsupportedVariant, VolumetricObject, WhiteSkybox, flatten,
 )
 from .renderer import Render, Renderer, RenderStats  # noqa: F401
 from ._abi import RaynaError, load_library  # noqa: F401

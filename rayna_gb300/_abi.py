@@ -39,6 +39,7 @@ RG_FLAG_COUNTERS = 1
 RG_FLAG_STAGE_TIMES = 2
 RG_BATCH_WAVEFRONT = 0
 RG_UV_WRAP, RG_UV_MIRROR, RG_UV_CLAMP_ZERO = 0, 1, 2
+RG_NO_TRANSFORM = 0xFFFFFFFF
 RG_BATCH_TILES = 1
 
 
@@ -72,6 +73,10 @@ class rg_scene_desc(C.Structure):
         ("cylinder_material", C.POINTER(C.c_uint32)),
         ("n_planes", C.c_uint32), ("planes", C.POINTER(C.c_float)), ("plane_material", C.POINTER(C.c_uint32)),
         ("plane_uv_wrap", C.POINTER(C.c_uint32)),
+        ("n_transforms", C.c_uint32), ("transforms", C.POINTER(C.c_double)),
+        ("sphere_transform", C.POINTER(C.c_uint32)), ("tri_transform", C.POINTER(C.c_uint32)),
+        ("box_transform", C.POINTER(C.c_uint32)), ("quad_transform", C.POINTER(C.c_uint32)),
+        ("cylinder_transform", C.POINTER(C.c_uint32)),
     ]
 
 

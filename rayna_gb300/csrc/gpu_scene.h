@@ -35,7 +35,10 @@ enum : uint32_t {
   PK_CYLINDER = 6,
 };
 constexpr uint32_t kKindShift = 29;
-constexpr uint32_t kMaterialMask = (1u << kKindShift) - 1u;
+// Bit 28 of prim.a.w: the primitive belongs to a transformed object; its
+// transform index is prim_xform[position in prims].
+constexpr uint32_t kXformBit = 1u << 28;
+constexpr uint32_t kMaterialMask = kXformBit - 1u;
 
 // Triangle flag (prim.c.w bits): the three vertex normals can sum to zero
 // inside the triangle, so the interpolated normal must be checked while
@@ -135,14 +138,17 @@ enum : uint32_t {
   F_QUAD = 32u,
   F_CYLINDER = 64u,
   F_PLANE = 128u,  // unbounded infinite planes
-  F_ALL = 255u,
-  F_WIDE = 256u,
+  F_ALL = 255u,    // every primitive kind
+  F_XFORM = 256u,  // transformed objects (a separate variant, so that scenes without them keep their registers)
+  F_ANY = F_ALL | F_XFORM,
+  F_WIDE = 512u,
 };
-constexpr uint32_t kinds_of(uint32_t f) { return f & F_ALL; }
+constexpr uint32_t kinds_of(uint32_t f) { return f & F_ANY; }
 
 // Host-side dispatch: calls fn(std::integral_constant<uint32_t, F>{}) with
-// the compiled kernel variant F for `features` (triangles only, spheres only
-// or every kind; binary or 8-wide traversal).
+// the compiled kernel variant F for `features` (triangles only, spheres only,
+// every kind, or every kind with transformed objects; binary or 8-wide
+// traversal).
 template <class Fn>
 auto dispatch_features(uint32_t features, Fn&& fn) {
   const bool wide = (features & F_WIDE) != 0;
@@ -152,8 +158,10 @@ auto dispatch_features(uint32_t features, Fn&& fn) {
     case F_SPHERE:
       return wide ? fn(std::integral_constant<uint32_t, F_SPHERE | F_WIDE>{})
                   : fn(std::integral_constant<uint32_t, F_SPHERE>{});
-    default:
+    case F_ALL:
       return wide ? fn(std::integral_constant<uint32_t, F_ALL | F_WIDE>{}) : fn(std::integral_constant<uint32_t, F_ALL>{});
+    default:
+      return wide ? fn(std::integral_constant<uint32_t, F_ANY | F_WIDE>{}) : fn(std::integral_constant<uint32_t, F_ANY>{});
   }
 }
 
@@ -177,6 +185,8 @@ struct GpuScene {
   const WideNode* wnodes;     // the same primitives under the 8-wide tree (node 0 is the root)
   uint32_t n_wnodes;
   const float* quad_ext;      // per parallelogram: Planar u, v, w (9 floats)
+  const float* xforms;        // per transform: inverse then forward 3 x 4 matrix, row-major (24 floats)
+  const uint32_t* prim_xform; // per primitive position: its transform index (read only for flagged primitives)
 };
 
 // Device error bits (rg_render_stats::error_flags).

@@ -38,11 +38,11 @@ cudaError_t launch_megakernel(const GpuScene& sc, const FrameParams& fp, bool co
     const uint32_t kind = fp.mode != RG_MODE_PBR ? kSampleMode : kSampleBranch;
     const bool wide = (sc.features & F_WIDE) != 0;
     if (kind == kSampleMode) {
-      if (wide) k_megakernel<F_ALL | F_WIDE, false, kSampleMode><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
-      else k_megakernel<F_ALL, false, kSampleMode><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+      if (wide) k_megakernel<F_ANY | F_WIDE, false, kSampleMode><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+      else k_megakernel<F_ANY, false, kSampleMode><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
     } else {
-      if (wide) k_megakernel<F_ALL | F_WIDE, false, kSampleBranch><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
-      else k_megakernel<F_ALL, false, kSampleBranch><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+      if (wide) k_megakernel<F_ANY | F_WIDE, false, kSampleBranch><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+      else k_megakernel<F_ANY, false, kSampleBranch><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
     }
     return cudaGetLastError();
   }
@@ -89,8 +89,8 @@ cudaError_t launch_query(const GpuScene& sc, uint32_t n, const float* o, const f
                          const float* vol_u, rg_hit* out, uint32_t* err, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   // The query traverses the tree the handle renders with, over every primitive kind.
-  if (sc.features & F_WIDE) k_query<F_ALL | F_WIDE><<<(n + 127) / 128, 128, 0, stream>>>(sc, n, o, d, tmin, tmax, vol_u, out, err);
-  else k_query<F_ALL><<<(n + 127) / 128, 128, 0, stream>>>(sc, n, o, d, tmin, tmax, vol_u, out, err);
+  if (sc.features & F_WIDE) k_query<F_ANY | F_WIDE><<<(n + 127) / 128, 128, 0, stream>>>(sc, n, o, d, tmin, tmax, vol_u, out, err);
+  else k_query<F_ANY><<<(n + 127) / 128, 128, 0, stream>>>(sc, n, o, d, tmin, tmax, vol_u, out, err);
   return cudaGetLastError();
 }
 

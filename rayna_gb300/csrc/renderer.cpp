@@ -120,6 +120,26 @@ bool planar_f64(const float* q, PlanarF64& o) {
   return true;
 }
 
+// Inverse of a 3 x 4 affine matrix [A | t] (row-major) in double:
+// [A^-1 | -A^-1 t], A^-1 from cofactors. False if A is singular.
+bool affine_inverse(const double* m, double* inv) {
+  const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], hh = m[9], i = m[10];
+  const double c00 = e * i - f * hh, c01 = f * g - d * i, c02 = d * hh - e * g;
+  const double det = a * c00 + b * c01 + c * c02;
+  if (!std::isfinite(det) || det == 0.0) return false;
+  const double r = 1.0 / det;
+  const double A[9] = {c00 * r, (c * hh - b * i) * r, (b * f - c * e) * r,
+                       c01 * r, (a * i - c * g) * r, (c * d - a * f) * r,
+                       c02 * r, (b * g - a * hh) * r, (a * e - b * d) * r};
+  for (int row = 0; row < 3; ++row) {
+    for (int k = 0; k < 3; ++k) inv[4 * row + k] = A[3 * row + k];
+    inv[4 * row + 3] = -(A[3 * row] * m[3] + A[3 * row + 1] * m[7] + A[3 * row + 2] * m[11]);
+  }
+  for (int k = 0; k < 12; ++k)
+    if (!std::isfinite(inv[k])) return false;
+  return true;
+}
+
 rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
   auto need = [&](uint32_t n, const void* p, const char* what) -> bool {
     if (n > 0 && p == nullptr) { fail(h, RG_INVALID_ARG, "%s is NULL but its count is %u", what, n); return false; }
@@ -204,6 +224,26 @@ rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
     if (d.plane_uv_wrap && d.plane_uv_wrap[i] > RG_UV_CLAMP_ZERO)
       return fail(h, RG_INVALID_ARG, "plane %u: uv wrap mode %u", i, d.plane_uv_wrap[i]);
   }
+  if (d.n_transforms && !d.transforms) return fail(h, RG_INVALID_ARG, "transforms is NULL but its count is %u", d.n_transforms);
+  for (uint32_t i = 0; i < d.n_transforms; ++i) {
+    double inv[12];
+    for (int k = 0; k < 12; ++k)
+      if (!std::isfinite(d.transforms[12ull * i + k])) return fail(h, RG_INVALID_ARG, "transform %u is not finite", i);
+    if (!affine_inverse(d.transforms + 12ull * i, inv)) return fail(h, RG_INVALID_ARG, "transform %u is not invertible", i);
+  }
+  auto xf_ok = [&](const uint32_t* idx, uint32_t n, const char* what) -> bool {
+    if (!idx) return true;
+    for (uint32_t i = 0; i < n; ++i)
+      if (idx[i] != RG_NO_TRANSFORM && idx[i] >= d.n_transforms) {
+        fail(h, RG_INVALID_ARG, "%s %u uses transform %u of %u", what, i, idx[i], d.n_transforms);
+        return false;
+      }
+    return true;
+  };
+  if (!xf_ok(d.sphere_transform, d.n_spheres, "sphere") || !xf_ok(d.tri_transform, d.n_triangles, "triangle") ||
+      !xf_ok(d.box_transform, d.n_boxes, "box") || !xf_ok(d.quad_transform, d.n_quads, "parallelogram") ||
+      !xf_ok(d.cylinder_transform, d.n_cylinders, "cylinder"))
+    return RG_INVALID_ARG;
   for (uint32_t i = 0; i < d.n_cylinders; ++i) {
     const float* c = d.cylinders + 7ull * i;
     if (!finite3(c) || !finite3(c + 3) || !std::isfinite(c[6])) return fail(h, RG_INVALID_ARG, "cylinder %u is not finite", i);
@@ -242,6 +282,11 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
   const uint32_t nbounded = hs.ns + hs.nt + hs.nb + hs.nv + hs.nq + hs.nc;
   std::vector<GpuPrim> prims(nbounded);
   std::vector<float> lo(3ull * nbounded), hi(3ull * nbounded);
+  // Transform of each bounded primitive, in creation order (RG_NO_TRANSFORM: none).
+  std::vector<uint32_t> xf_of(nbounded, RG_NO_TRANSFORM);
+  auto take_xf = [&](const uint32_t* idx, uint32_t i, uint32_t prim) {
+    if (idx && idx[i] != RG_NO_TRANSFORM) xf_of[prim] = idx[i];
+  };
   auto bits = [](uint32_t kind, uint32_t mat) { return bits_float((kind << kKindShift) | mat); };
   auto setbox = [&](uint32_t i, float lx, float ly, float lz, float hx, float hy, float hz) {
     lo[3ull * i] = std::fmin(lx, hx); lo[3ull * i + 1] = std::fmin(ly, hy); lo[3ull * i + 2] = std::fmin(lz, hz);
@@ -251,6 +296,7 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
   for (uint32_t i = 0; i < hs.ns; ++i, ++id) {
     const float* s = d.spheres + 4ull * i;
     float r = s[3];
+    take_xf(d.sphere_transform, i, id);
     GpuPrim& p = prims[id];
     p.a = {s[0], s[1], s[2], bits(PK_SPHERE, d.sphere_material[i])};
     p.b = {r, r * r, 0.0f, bits_float(id)};
@@ -269,6 +315,7 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
       for (int b = a + 1; b < 3; ++b)
         if ((double)n[3 * a] * n[3 * b] + (double)n[3 * a + 1] * n[3 * b + 1] + (double)n[3 * a + 2] * n[3 * b + 2] <= 0.0)
           flags |= kTriCheckNormals;
+    take_xf(d.tri_transform, i, id);
     GpuPrim& p = prims[id];
     p.a = {v[0], v[1], v[2], bits(PK_TRIANGLE, d.tri_material[i])};
     p.b = {v[3] - v[0], v[4] - v[1], v[5] - v[2], bits_float(id)};
@@ -290,6 +337,7 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
   for (uint32_t i = 0; i < hs.nb; ++i, ++id) {
     float c[3], r[3], iv[3], mn[3], mx[3];
     axis_box(d.boxes + 6ull * i, d.boxes + 6ull * i + 3, c, r, iv, mn, mx);
+    take_xf(d.box_transform, i, id);
     GpuPrim& p = prims[id];
     p.a = {c[0], c[1], c[2], bits(PK_BOX, d.box_material[i])};
     p.b = {r[0], r[1], r[2], bits_float(id)};
@@ -353,6 +401,7 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
   for (uint32_t i = 0; i < hs.nq; ++i, ++id, ++pi) {
     PlanarF64 q;
     planar_f64(d.quads + 9ull * i, q);
+    take_xf(d.quad_transform, i, pi);
     GpuPrim& p = prims[pi];
     p.a = {(float)q.n[0], (float)q.n[1], (float)q.n[2], bits(PK_QUAD, d.quad_material[i])};
     p.b = {(float)q.d, 0.0f, 0.0f, bits_float(id)};
@@ -372,6 +421,7 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
     // CylinderMesh::new (cylinder.rs:24-48)
     const double along[3] = {(double)c[3] - c[0], (double)c[4] - c[1], (double)c[5] - c[2]};
     const double lsq = along[0] * along[0] + along[1] * along[1] + along[2] * along[2];
+    take_xf(d.cylinder_transform, i, pi);
     GpuPrim& p = prims[pi];
     p.a = {c[0], c[1], c[2], bits(PK_CYLINDER, d.cylinder_material[i])};
     p.b = {(float)along[0], (float)along[1], (float)along[2], bits_float(id)};
@@ -400,6 +450,34 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
     g.prim_id = id;
     hs.sdfs.push_back(g);
   }
+  // Transformed objects: the flag bit, and world bounds from the mapped
+  // corners of the mesh-space bounds (ObjectTransform::calculate_aabb,
+  // object/transform.rs:133-144), rounded outward.
+  hs.xforms.clear();
+  for (uint32_t k = 0; k < d.n_transforms; ++k) {
+    const double* m = d.transforms + 12ull * k;
+    double inv[12];
+    affine_inverse(m, inv);
+    for (int j = 0; j < 12; ++j) hs.xforms.push_back((float)inv[j]);
+    for (int j = 0; j < 12; ++j) hs.xforms.push_back((float)m[j]);
+  }
+  for (uint32_t k = 0; k < nbounded; ++k) {
+    if (xf_of[k] == RG_NO_TRANSFORM) continue;
+    uint32_t w = float_bits(prims[k].a.w) | kXformBit;
+    prims[k].a.w = bits_float(w);
+    const double* m = d.transforms + 12ull * xf_of[k];
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 8; ++c) {
+      const double q[3] = {(c & 1) ? hi[3ull * k] : lo[3ull * k], (c & 2) ? hi[3ull * k + 1] : lo[3ull * k + 1],
+                           (c & 4) ? hi[3ull * k + 2] : lo[3ull * k + 2]};
+      for (int a = 0; a < 3; ++a) {
+        const double v = m[4 * a] * q[0] + m[4 * a + 1] * q[1] + m[4 * a + 2] * q[2] + m[4 * a + 3];
+        mn[a] = std::min(mn[a], v);
+        mx[a] = std::max(mx[a], v);
+      }
+    }
+    setbox_pad(k, mn, mx);
+  }
   // Binary tree (leaves of at most kWideMaxLeaf primitives), then its 8-wide
   // collapse; both index one primitive order.
   BvhBuildResult bvh = build_bvh(lo.data(), hi.data(), nbounded, kWideMaxLeaf, 16, 40);
@@ -425,6 +503,11 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
   hs.vol_prim.assign(hs.nv, 0);
   for (uint32_t i = 0; i < nbounded; ++i)
     if (order[i] >= hs.vol_base && order[i] < hs.vol_base + hs.nv) hs.vol_prim[order[i] - hs.vol_base] = i;
+  hs.prim_xform.clear();
+  if (d.n_transforms) {
+    hs.prim_xform.resize(nbounded);
+    for (uint32_t i = 0; i < nbounded; ++i) hs.prim_xform[i] = xf_of[order[i]];
+  }
   hs.vol_density.resize(hs.nv);
   for (uint32_t i = 0; i < hs.nv; ++i) hs.vol_density[i] = d.volumes[i].density;
   if (hs.max_depth >= kMaxBuildDepth)
@@ -442,6 +525,8 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   if ((st = upload(h, ds.materials, hs.materials.data(), hs.materials.size(), "upload materials")) != RG_OK) return st;
   if ((st = upload(h, ds.sdfs, hs.sdfs.data(), hs.sdfs.size(), "upload sdfs")) != RG_OK) return st;
   if ((st = upload(h, ds.quad_ext, hs.quad_ext.data(), hs.quad_ext.size(), "upload parallelograms")) != RG_OK) return st;
+  if ((st = upload(h, ds.xforms, hs.xforms.data(), hs.xforms.size(), "upload transforms")) != RG_OK) return st;
+  if ((st = upload(h, ds.prim_xform, hs.prim_xform.data(), hs.prim_xform.size(), "upload transforms")) != RG_OK) return st;
   if ((st = upload(h, ds.vol_density, hs.vol_density.data(), hs.vol_density.size(), "upload media")) != RG_OK) return st;
   if ((st = upload(h, ds.vol_prim, hs.vol_prim.data(), hs.vol_prim.size(), "upload media")) != RG_OK) return st;
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "upload scene");
@@ -454,6 +539,8 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.materials = ds.materials;
   g.sdfs = ds.sdfs;
   g.quad_ext = ds.quad_ext;
+  g.xforms = ds.xforms;
+  g.prim_xform = ds.prim_xform;
   g.vol_density = ds.vol_density;
   g.vol_prim = ds.vol_prim;
   g.n_nodes = (uint32_t)hs.nodes.size();
@@ -464,10 +551,12 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.tri_base = hs.ns;
   g.vol_base = hs.vol_base;
   g.n_tris = hs.nt;
-  // Kernel variant: triangles only, spheres only, or every kind.
+  // Kernel variant: triangles only, spheres only, every kind, or every kind
+  // with transformed objects.
   uint32_t have = (hs.ns ? F_SPHERE : 0) | (hs.nt ? F_TRI : 0) | (hs.nb ? F_BOX : 0) | (hs.nv ? F_VOL : 0) |
-                  (hs.nsdf ? F_SDF : 0) | (hs.nq ? F_QUAD : 0) | (hs.nc ? F_CYLINDER : 0) | (hs.npl ? F_PLANE : 0);
-  h->kinds = have == F_TRI ? F_TRI : (have == F_SPHERE ? F_SPHERE : F_ALL);
+                  (hs.nsdf ? F_SDF : 0) | (hs.nq ? F_QUAD : 0) | (hs.nc ? F_CYLINDER : 0) | (hs.npl ? F_PLANE : 0) |
+                  (hs.prim_xform.empty() ? 0 : F_XFORM);
+  h->kinds = have == F_TRI ? F_TRI : (have == F_SPHERE ? F_SPHERE : ((have & F_XFORM) ? F_ANY : F_ALL));
   apply_features(h);
   return RG_OK;
 }
@@ -497,7 +586,7 @@ void apply_features(rg_renderer* h) {
 }
 
 void free_scene(DeviceScene& ds) {
-  dfree(ds.nodes); dfree(ds.wnodes); dfree(ds.prims); dfree(ds.quad_ext); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
+  dfree(ds.nodes); dfree(ds.wnodes); dfree(ds.prims); dfree(ds.quad_ext); dfree(ds.xforms); dfree(ds.prim_xform); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
   dfree(ds.vol_density); dfree(ds.vol_prim);
 }
 

@@ -31,6 +31,8 @@ struct HostScene {
   std::vector<rg_volume> volumes;
   std::vector<GpuSdf> sdfs;            // unbounded list: SDFs, then infinite planes
   std::vector<float> quad_ext;         // per parallelogram: u, v, w
+  std::vector<float> xforms;           // per transform: inverse, forward (3 x 4 each)
+  std::vector<uint32_t> prim_xform;    // per primitive position: transform index (empty: no transforms)
   std::vector<float> vol_density;      // per medium
   std::vector<uint32_t> vol_prim;      // per medium: position in `prims`
 };
@@ -43,6 +45,8 @@ struct DeviceScene {
   rg_material* materials = nullptr;
   GpuSdf* sdfs = nullptr;
   float* quad_ext = nullptr;
+  float* xforms = nullptr;
+  uint32_t* prim_xform = nullptr;
   float* vol_density = nullptr;
   uint32_t* vol_prim = nullptr;
 };

@@ -424,6 +424,7 @@ __device__ bool sdf_march(const GpuSdf& s, const Ray& r, float start, float end,
 // ---------------------------------------------------------------------------
 struct HitRec {
   float t;
+  float tl;      // transformed primitive: the distance along the mesh-space ray
   int prim;      // index into the reordered prim array, or -1
   int sdf;       // SDF index when an unbounded object won, else -1
   SdfHit sh;
@@ -434,43 +435,79 @@ struct Counters {
 };
 
 
+// A transformed object's matrices: inverse (world to mesh space) at m,
+// forward (mesh to world space) at m + 12, both 3 x 4 row-major.
+__device__ __forceinline__ const float* prim_xform_of(const GpuScene& sc, int i) {
+  return sc.xforms + 24ull * __ldg(sc.prim_xform + i);
+}
+__device__ __forceinline__ V3 xf_point(const float* m, V3 p) {
+  return v3(__fmaf_rn(__ldg(m + 0), p.x, __fmaf_rn(__ldg(m + 1), p.y, __fmaf_rn(__ldg(m + 2), p.z, __ldg(m + 3)))),
+            __fmaf_rn(__ldg(m + 4), p.x, __fmaf_rn(__ldg(m + 5), p.y, __fmaf_rn(__ldg(m + 6), p.z, __ldg(m + 7)))),
+            __fmaf_rn(__ldg(m + 8), p.x, __fmaf_rn(__ldg(m + 9), p.y, __fmaf_rn(__ldg(m + 10), p.z, __ldg(m + 11)))));
+}
+__device__ __forceinline__ V3 xf_vector(const float* m, V3 v) {
+  return v3(__fmaf_rn(__ldg(m + 0), v.x, __fmaf_rn(__ldg(m + 1), v.y, __ldg(m + 2) * v.z)),
+            __fmaf_rn(__ldg(m + 4), v.x, __fmaf_rn(__ldg(m + 5), v.y, __ldg(m + 6) * v.z)),
+            __fmaf_rn(__ldg(m + 8), v.x, __fmaf_rn(__ldg(m + 9), v.y, __ldg(m + 10) * v.z)));
+}
+// ObjectTransform::incoming_ray (object/transform.rs:90-97): origin and
+// direction mapped by the inverse, the direction normalised again (Ray::new).
+__device__ __forceinline__ Ray xf_incoming(const float* m, const Ray& r) { return make_ray(xf_point(m, r.o), xf_vector(m, r.d)); }
+
 // Test the primitives of one leaf, shrinking `end` to each accepted hit
 // (object/bvh.rs:82-96: a later hit at equal distance replaces the earlier).
+// A primitive of a transformed object (SimpleObject::full_intersect,
+// object/simple.rs:107-116) is tested against the mesh-space ray from the
+// same start; its distance is the world-space length from the ray's origin
+// to the mapped hit point (transform.rs:101-130), and that distance must lie
+// within `end`. (The reference bounds the mesh-space distance by the world
+// bound instead; the two agree for rigid transforms, and under scaling the
+// reference's result depends on its traversal order, while this one is the
+// closest world-space hit.) `best_tl` keeps the mesh-space distance of the
+// closest hit.
 template <uint32_t F, bool COUNT>
-__device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int count, const Ray& r, float start, float& end,
-                                          int& best, const RngCtx& ctx, Counters& cnt) {
+__device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int count, const Ray& rw, float start, float& end,
+                                          int& best, float& best_tl, const RngCtx& ctx, Counters& cnt) {
   for (int i = first; i < first + count; ++i) {
     const GpuPrim* pp = sc.prims + i;
     float4 a = __ldg(&pp->a);
     uint32_t kind = kinds_of(F) == F_TRI ? (uint32_t)PK_TRIANGLE
-                  : (kinds_of(F) == F_SPHERE ? (uint32_t)PK_SPHERE : __float_as_uint(a.w) >> kKindShift);
+                  : (kinds_of(F) == F_SPHERE ? (uint32_t)PK_SPHERE : (__float_as_uint(a.w) >> kKindShift));
     if (COUNT) ++cnt.prims;
+    const float* xf = nullptr;
+    Ray r = rw;
+    float tend = end;  // a transformed primitive is tested on [start, inf), then bounded in world space
+    if ((F & F_XFORM) && (__float_as_uint(a.w) & kXformBit)) {
+      xf = prim_xform_of(sc, i);
+      r = xf_incoming(xf, rw);
+      tend = CUDART_INF_F;
+    }
     float t;
     if ((F & F_TRI) && kind == PK_TRIANGLE) {
       float4 b = __ldg(&pp->b), c = __ldg(&pp->c);
       float u, v, det;
-      if (!triangle_t(xyz(a), xyz(b), xyz(c), r, start, end, t, u, v, det)) continue;
+      if (!triangle_t(xyz(a), xyz(b), xyz(c), r, start, tend, t, u, v, det)) continue;
       if (__float_as_uint(c.w) & kTriCheckNormals) {
         V3 n;
         if (!tri_normal(sc.tri_normals + 9ull * (__float_as_uint(b.w) - sc.tri_base), u, v, n)) continue;
       }
     } else if ((F & F_SPHERE) && kind == PK_SPHERE) {
       float4 b = __ldg(&pp->b);
-      if (!sphere_t(xyz(a), b.y, r, start, end, t)) continue;
+      if (!sphere_t(xyz(a), b.y, r, start, tend, t)) continue;
     } else if ((F & F_BOX) && kind == PK_BOX) {
       float4 b = __ldg(&pp->b), c = __ldg(&pp->c);
       BoxHit bh;
-      if (!box_t(xyz(a), xyz(b), xyz(c), r, start, end, bh)) continue;
+      if (!box_t(xyz(a), xyz(b), xyz(c), r, start, tend, bh)) continue;
       t = bh.t;
     } else if ((F & F_QUAD) && kind == PK_QUAD) {
       GpuPrim p;
       p.a = a; p.b = __ldg(&pp->b); p.c = __ldg(&pp->c);
-      if (!quad_t(p, sc.quad_ext, r, start, end, t)) continue;
+      if (!quad_t(p, sc.quad_ext, r, start, tend, t)) continue;
     } else if ((F & F_CYLINDER) && kind == PK_CYLINDER) {
       GpuPrim p;
       p.a = a; p.b = __ldg(&pp->b); p.c = __ldg(&pp->c);
       CylHit ch;
-      if (!cylinder_t(p, r, start, CUDART_INF_F, ch) || !(ch.t <= end)) continue;
+      if (!cylinder_t(p, r, start, CUDART_INF_F, ch) || !(ch.t <= tend)) continue;
       t = ch.t;
     } else if ((F & F_VOL) && (kind == PK_VOL_SPHERE || kind == PK_VOL_BOX)) {
       GpuPrim p;
@@ -478,6 +515,12 @@ __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int cou
       if (!volume_t(p, kind, __float_as_uint(p.b.w) - sc.vol_base, r, start, end, ctx, t)) continue;
     } else {
       continue;
+    }
+    if ((F & F_XFORM) && xf) {
+      const float tl = t;
+      t = length3(xf_point(xf + 12, at3(r.o, r.d, tl)) - rw.o);
+      if (!(t <= end)) continue;
+      best_tl = tl;
     }
     end = t;
     best = i;
@@ -508,6 +551,7 @@ struct Traversal {
   int sp;
   float tmax;
   int best;
+  float best_tl;          // transformed primitive: mesh-space distance of the closest hit
   bool wide;
   int ref, leaf;          // binary: next node (or leaf code, or kDone), postponed leaf
   uint2 ng;               // wide: current node group
@@ -519,6 +563,7 @@ __device__ __forceinline__ void trav_init(Traversal& t, const GpuScene& sc, cons
   t.sp = 0;
   t.tmax = end;
   t.best = -1;
+  t.best_tl = 0.0f;
   t.wide = false;
   if (F & F_WIDE) {
     // A zero (or underflowing) direction component makes that axis's inverse
@@ -596,7 +641,7 @@ __device__ __forceinline__ bool run_binary(Traversal& t, uint2* stack, const Gpu
     }
     while (t.leaf < 0) {
       int code = ~t.leaf;
-      test_leaf<F, COUNT>(sc, code >> 3, code & 7, r, start, t.tmax, t.best, ctx, cnt);
+      test_leaf<F, COUNT>(sc, code >> 3, code & 7, r, start, t.tmax, t.best, t.best_tl, ctx, cnt);
       t.leaf = 0;
       if (t.ref < 0) {
         t.leaf = t.ref;
@@ -711,7 +756,7 @@ __device__ __forceinline__ bool run_wide(Traversal& t, uint2* stack, const GpuSc
     while (pg.y) {
       const uint32_t pi = pg.x + (uint32_t)(__ffs(pg.y) - 1);
       pg.y &= pg.y - 1u;
-      if (pi < sc.n_prims) test_leaf<F, COUNT>(sc, (int)pi, 1, r, start, t.tmax, t.best, ctx, cnt);
+      if (pi < sc.n_prims) test_leaf<F, COUNT>(sc, (int)pi, 1, r, start, t.tmax, t.best, t.best_tl, ctx, cnt);
       else atomicOr(err, ERR_BAD_INDEX);
     }
     if (t.ng.y <= 0x00FFFFFFu) {
@@ -740,6 +785,7 @@ __device__ __forceinline__ bool finish_hit(const GpuScene& sc, const Ray& r, flo
   h.prim = t.best;
   h.sdf = -1;
   h.t = t.tmax;
+  h.tl = t.best_tl;
   bool any = t.best >= 0;
   if (F & (F_SDF | F_PLANE)) {
     for (uint32_t k = 0; k < sc.n_sdfs; ++k) {
@@ -815,41 +861,12 @@ __device__ __forceinline__ void wrap_uv(uint32_t mode, float& u, float& v) {
   }
 }
 
-// Full hit record of the closest hit. UV: also the texture coordinates that
-// only the Uv render mode reads (sphere, cylinder and infinite-plane uv cost
-// transcendentals or extra fetches; the other kinds compute them anyway).
-template <uint32_t F, bool UV = false>
-__device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, const HitRec& h, const RngCtx& ctx, Surface& s,
-                                             float start) {
-  if ((F & (F_SDF | F_PLANE)) && h.sdf >= 0) {
-    const GpuSdf& f = sc.sdfs[h.sdf];
-    s.pos = at3(r.o, r.d, h.t);
-    s.normal = h.sh.n;
-    // raymarched.rs:113-114: not flipped; planar/mod.rs:190: -n * signum(denom)
-    s.ray_normal = h.sh.flip ? -h.sh.n : h.sh.n;
-    if (UV && (F & F_PLANE) && f.kind == kUnboundedPlane) {
-      float u, v;
-      planar_uv(sc.quad_ext + 9ull * f.max_iter, v3(f.p1, f.p2, f.p3), s.pos, u, v);
-      wrap_uv(__float_as_uint(f.pad[0]), u, v);
-      s.front = h.sh.front;
-      s.material = f.material;
-      s.prim_id = f.prim_id;
-      s.side = 0;
-      s.u = u; s.v = v;
-      return;
-    }
-    s.front = h.sh.front;
-    s.material = f.material;
-    s.prim_id = f.prim_id;
-    s.side = h.sh.side;
-    s.u = s.v = 0.0f;
-    return;
-  }
-  const GpuPrim p = sc.prims[h.prim];
-  uint32_t kind = prim_kind(p);
-  s.material = prim_material(p);
-  s.prim_id = prim_id(p);
-  s.pos = at3(r.o, r.d, h.t);
+// The bounded primitive part of finalize_hit: the hit of `p` at distance `ht`
+// along `r` (world space, or mesh space for a transformed object).
+template <uint32_t F, bool UV>
+__device__ __forceinline__ void finalize_prim(const GpuScene& sc, const GpuPrim& p, uint32_t kind, const Ray& r, float ht,
+                                              const RngCtx& ctx, Surface& s, float start) {
+  s.pos = at3(r.o, r.d, ht);
   s.side = 0;
   if (kinds_of(F) == F_TRI) kind = PK_TRIANGLE;
   if (kinds_of(F) == F_SPHERE) kind = PK_SPHERE;
@@ -874,7 +891,7 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
     s.u = u; s.v = v;
   } else if ((F & F_BOX) && kind == PK_BOX) {
     BoxHit bh;
-    box_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, h.t, bh);
+    box_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, ht, bh);
     V3 rn = v3(bh.axis == 0 ? bh.sgn : 0.0f, bh.axis == 1 ? bh.sgn : 0.0f, bh.axis == 2 ? bh.sgn : 0.0f);
     s.ray_normal = rn;
     s.normal = rn * bh.winding;
@@ -936,6 +953,60 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& r, c
     s.front = true;
     s.u = s.v = u01(b.w);
   }
+}
+
+// A transformed object's hit, rebuilt in mesh space (the same ray and
+// distance as its test) and mapped out (ObjectTransform::
+// outgoing_intersection, transform.rs:101-130): the point by the transform,
+// both normals by its linear part and normalised (the reference maps normals
+// with the transform itself, not its inverse transpose). Not inlined: the
+// untransformed path keeps its registers.
+template <uint32_t F, bool UV>
+__device__ __forceinline__ void finalize_xformed(const GpuScene& sc, const GpuPrim& p, uint32_t kind, const Ray& rw,
+                                              const HitRec& h, const RngCtx& ctx, Surface& s, float start) {
+  const float* xf = prim_xform_of(sc, h.prim);
+  finalize_prim<F, UV>(sc, p, kind, xf_incoming(xf, rw), h.tl, ctx, s, start);
+  s.pos = xf_point(xf + 12, s.pos);
+  s.normal = normalize3(xf_vector(xf + 12, s.normal));
+  s.ray_normal = normalize3(xf_vector(xf + 12, s.ray_normal));
+}
+
+// Full hit record of the closest hit. UV: also the texture coordinates that
+// only the Uv render mode reads (sphere, cylinder and infinite-plane uv cost
+// transcendentals or extra fetches; the other kinds compute them anyway).
+template <uint32_t F, bool UV = false>
+__device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& rw, const HitRec& h, const RngCtx& ctx, Surface& s,
+                                             float start) {
+  if ((F & (F_SDF | F_PLANE)) && h.sdf >= 0) {
+    const GpuSdf& f = sc.sdfs[h.sdf];
+    s.pos = at3(rw.o, rw.d, h.t);
+    s.normal = h.sh.n;
+    // raymarched.rs:113-114: not flipped; planar/mod.rs:190: -n * signum(denom)
+    s.ray_normal = h.sh.flip ? -h.sh.n : h.sh.n;
+    if (UV && (F & F_PLANE) && f.kind == kUnboundedPlane) {
+      float u, v;
+      planar_uv(sc.quad_ext + 9ull * f.max_iter, v3(f.p1, f.p2, f.p3), s.pos, u, v);
+      wrap_uv(__float_as_uint(f.pad[0]), u, v);
+      s.front = h.sh.front;
+      s.material = f.material;
+      s.prim_id = f.prim_id;
+      s.side = 0;
+      s.u = u; s.v = v;
+      return;
+    }
+    s.front = h.sh.front;
+    s.material = f.material;
+    s.prim_id = f.prim_id;
+    s.side = h.sh.side;
+    s.u = s.v = 0.0f;
+    return;
+  }
+  const GpuPrim p = sc.prims[h.prim];
+  const uint32_t kind = prim_kind(p);
+  s.material = prim_material(p);
+  s.prim_id = prim_id(p);
+  if ((F & F_XFORM) && (__float_as_uint(p.a.w) & kXformBit)) finalize_xformed<F, UV>(sc, p, kind, rw, h, ctx, s, start);
+  else finalize_prim<F, UV>(sc, p, kind, rw, h.t, ctx, s, start);
 }
 
 // ---------------------------------------------------------------------------

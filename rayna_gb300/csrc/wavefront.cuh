@@ -22,7 +22,7 @@ constexpr int kPrimMiss = -1;  // rec[2].w: >= 0 BVH primitive, -1 miss, -2 - k 
 
 struct PathState {
   float4* rec;          // 3 x float4 per slot: (origin, depth) (direction, t) (throughput, prim)
-  float4* aux;          // per slot: SDF hit normal + (front bit 31 | side)
+  float4* aux;          // per slot: SDF hit normal + (front bit 31 | side); transformed hit: mesh-space distance in x
   float *sr, *sg, *sb;  // per-slot sample radiance
   uint32_t* active[2];
   uint32_t* kindq;      // kKinds x capacity

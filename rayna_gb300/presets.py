@@ -195,11 +195,36 @@ def cornell_box_triangles():
     return objs
 
 
+def cornell(width: int = 512, height: int = 512, spp: int = 64, ray_depth: int = 8):
+    """The reference's CORNELL preset (scene/preset.rs:608-687): five
+    ParallelogramMesh walls, a parallelogram light, and two boxes rotated
+    about Y by 15 and -18 degrees about their centres. Returns (scene,
+    camera, opts)."""
+    from .scene import AxisBoxMesh, ParallelogramMesh, Planar, Transform3
+    red, green, warm_grey = (0.65, 0.05, 0.05), (0.12, 0.45, 0.15), (0.85, 0.74, 0.55)
+    X, Y, Z = (1, 0, 0), (0, 1, 0), (0, 0, 1)
+
+    def quad(p, u, v, col):
+        return SimpleObject(ParallelogramMesh(Planar.new(p, u, v)), LambertianMaterial(col))
+
+    objs = [quad((0, 0, 0), Y, Z, red), quad((0, 0, 0), X, Y, warm_grey), quad((0, 0, 0), Z, X, warm_grey),
+            quad((1, 0, 0), Z, Y, green), quad((0, 1, 0), X, Z, warm_grey),
+            SimpleObject(ParallelogramMesh(Planar.new((0.4, 0.9999, 0.4), (0.2, 0, 0), (0, 0, 0.2))),
+                         LightMaterial((15.0, 15.0, 15.0))),
+            SimpleObject(AxisBoxMesh((0.231, 0.0, 0.117), (0.531, 0.595, 0.414)), LambertianMaterial(warm_grey),
+                         Transform3.from_axis_angle(Y, Angle.from_degrees(15.0))),
+            SimpleObject(AxisBoxMesh((0.477, 0.0, 0.531), (0.774, 0.297, 0.829)), LambertianMaterial(warm_grey),
+                         Transform3.from_axis_angle(Y, Angle.from_degrees(-18.0)))]
+    scene = Scene(objects=objs, skybox=NoSkybox())
+    cam = Camera(pos=(0.5, 0.5, 2.3), v_fov=Angle.from_degrees(40.0), fwd=(0.0, 0.0, -1.0), focus_dist=1.0,
+                 defocus_angle=Angle(0.0))
+    return scene, cam, RenderOpts(width=width, height=height, samples=spp, ray_depth=ray_depth)
+
+
 def cornell_quads(width: int = 512, height: int = 512, spp: int = 64, ray_depth: int = 8):
-    """The reference's CORNELL preset (scene/preset.rs:608-687) built from
-    ParallelogramMesh walls and light, as it is, except that its two boxes
-    stay axis-aligned (the preset rotates them about Y by 15 and -18 degrees;
-    object transforms do not cross the C ABI), with a capped cylinder added."""
+    """The reference's CORNELL preset (scene/preset.rs:608-687) with its two
+    boxes left axis-aligned (`cornell` rotates them as the preset does) and a
+    capped cylinder added."""
     from .scene import AxisBoxMesh, CylinderMesh, ParallelogramMesh, Planar
     red, green, warm_grey = (0.65, 0.05, 0.05), (0.12, 0.45, 0.15), (0.85, 0.74, 0.55)
     X, Y, Z = (1, 0, 0), (0, 1, 0), (0, 0, 1)

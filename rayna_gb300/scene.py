@@ -16,11 +16,15 @@ Names, fields and defaults follow the reference so that code written against
 * sky           — SimpleSkybox, WhiteSkybox, NoSkybox (skybox/*.rs)
 * Camera, Angle (scene/camera.rs), RenderOpts, RenderMode
   (render/render_opts.rs), Scene / StandardScene (scene/mod.rs)
+* transforms    — Transform3 (glamour 0.11 `Transform3<f64, f64>`, the
+                  core/types.rs alias) and ObjectTransform
+                  (object/transform.rs)
 
 `flatten()` turns a scene into the flat arrays of ``rg_scene_desc``. The
 reference takes SDFs as closures; closures cannot cross a C ABI, so an SDF is
 given as one of the descriptor types below. Variants this library does not
-run (non-identity transforms, dynamic meshes) raise UnsupportedVariant.
+run (transformed volumes, SDFs and infinite planes, dynamic meshes) raise
+UnsupportedVariant.
 """
 from __future__ import annotations
 
@@ -44,6 +48,132 @@ def _vec3(v) -> tuple:
     if len(t) != 3:
         raise ValueError(f"expected 3 components, got {v!r}")
     return t
+
+
+# ---------------------------------------------------------------------------
+# Transforms
+# ---------------------------------------------------------------------------
+class Transform3:
+    """An affine map from mesh space to world space, held as a 4 x 4 f64
+    matrix acting on column vectors (glamour's Transform3 over glam's DMat4).
+
+    ``a.then(b)`` applies ``a`` first, then ``b`` (matrix ``b @ a``).
+    """
+
+    __slots__ = ("matrix",)
+
+    def __init__(self, matrix=None):
+        m = np.eye(4) if matrix is None else np.array(matrix, dtype=np.float64)
+        if m.shape == (3, 4):
+            m = np.vstack([m, [0.0, 0.0, 0.0, 1.0]])
+        if m.shape != (4, 4):
+            raise ValueError(f"expected a 4 x 4 or 3 x 4 matrix, got shape {m.shape}")
+        if not np.array_equal(m[3], [0.0, 0.0, 0.0, 1.0]):
+            raise ValueError("a Transform3 is affine: its bottom row must be (0, 0, 0, 1)")
+        self.matrix = m
+
+    @staticmethod
+    def from_translation(v) -> "Transform3":
+        m = np.eye(4)
+        m[:3, 3] = _vec3(v)
+        return Transform3(m)
+
+    @staticmethod
+    def from_scale(v) -> "Transform3":
+        return Transform3(np.diag([*_vec3(v), 1.0]))
+
+    @staticmethod
+    def from_axis_angle(axis, angle: "Angle") -> "Transform3":
+        """Rotation by `angle` (right-handed) about the unit vector `axis`
+        (Rodrigues' rotation formula)."""
+        x, y, z = _vec3(axis)
+        a = angle.radians if isinstance(angle, Angle) else float(angle)
+        c, s_ = math.cos(a), math.sin(a)
+        k = 1.0 - c
+        m = np.eye(4)
+        m[:3, :3] = [[x * x * k + c, x * y * k - z * s_, x * z * k + y * s_],
+                     [x * y * k + z * s_, y * y * k + c, y * z * k - x * s_],
+                     [x * z * k - y * s_, y * z * k + x * s_, z * z * k + c]]
+        return Transform3(m)
+
+    @staticmethod
+    def from_scale_rotation_translation(scale, axis, angle: "Angle", translation) -> "Transform3":
+        """Scale, then rotate about `axis` by `angle`, then translate."""
+        return Transform3.from_scale(scale).then(Transform3.from_axis_angle(axis, angle)).then_translate(translation)
+
+    def then(self, other: "Transform3") -> "Transform3":
+        return Transform3(other.matrix @ self.matrix)
+
+    def then_translate(self, v) -> "Transform3":
+        return self.then(Transform3.from_translation(v))
+
+    def inverse(self) -> "Transform3":
+        return Transform3(np.linalg.inv(self.matrix))
+
+    def map_point(self, p) -> np.ndarray:
+        return self.matrix[:3, :3] @ np.asarray(_vec3(p)) + self.matrix[:3, 3]
+
+    def map_vector(self, v) -> np.ndarray:
+        return self.matrix[:3, :3] @ np.asarray(_vec3(v))
+
+    def is_identity(self) -> bool:
+        return bool(np.array_equal(self.matrix, np.eye(4)))
+
+    def __eq__(self, other):
+        return isinstance(other, Transform3) and np.array_equal(self.matrix, other.matrix)
+
+    def __repr__(self):
+        return f"Transform3({self.matrix[:3].tolist()})"
+
+
+Transform3.IDENTITY = Transform3()
+
+
+class ObjectTransform:
+    """object/transform.rs: a mesh-to-world Transform3 and its inverse.
+
+    ``ObjectTransform.new(t)`` is uncorrected; ``new_corrected(t, centre)``
+    rotates and scales about `centre` instead of the origin:
+    translate(-centre), then `t`, then translate(centre)."""
+
+    __slots__ = ("transform",)
+
+    def __init__(self, transform: Transform3 = None):
+        self.transform = Transform3.IDENTITY if transform is None else _transform3(transform)
+
+    @staticmethod
+    def new(transform) -> "ObjectTransform":
+        return ObjectTransform(_transform3(transform))
+
+    @staticmethod
+    def new_corrected(transform, obj_centre) -> "ObjectTransform":
+        c = np.asarray(_vec3(obj_centre))
+        t = Transform3.from_translation(-c).then(_transform3(transform)).then_translate(c)
+        return ObjectTransform(t)
+
+    def with_correction(self, obj_centre) -> "ObjectTransform":
+        return ObjectTransform.new_corrected(self.transform, obj_centre)
+
+    @property
+    def inv_transform(self) -> Transform3:
+        return self.transform.inverse()
+
+    @property
+    def is_identity(self) -> bool:
+        return self.transform.is_identity()
+
+
+ObjectTransform.IDENTITY = ObjectTransform()
+
+
+def _transform3(t) -> Transform3:
+    if t is None:
+        return Transform3.IDENTITY
+    if isinstance(t, ObjectTransform):
+        return t.transform
+    if isinstance(t, Transform3):
+        return t
+    return Transform3(t)
 
 
 # ---------------------------------------------------------------------------
@@ -219,6 +349,9 @@ class SphereMesh:
     pos: tuple
     radius: float
 
+    def centre(self) -> np.ndarray:  # sphere.rs:106
+        return np.asarray(_vec3(self.pos))
+
 
 @dataclass
 class Triangle:
@@ -235,25 +368,37 @@ class Triangle:
             raise ValueError("normals must be normalised")
         self.vertices, self.normals = v, n
 
+    def centre(self) -> np.ndarray:  # triangle.rs:42-45
+        return (self.vertices[0] + self.vertices[1] + self.vertices[2]) / 3.0
+
 
 class BvhMesh:
-    """mesh/advanced/bvh.rs: a BVH over triangles sharing one material.
+    """mesh/advanced/bvh.rs: a BVH over triangles and spheres sharing one
+    material (and one transform).
 
-    ``BvhMesh(list_of_triangles)`` mirrors the reference constructor;
+    ``BvhMesh(list_of_meshes)`` mirrors the reference constructor;
     ``BvhMesh.from_arrays(vertices, normals)`` takes (n, 3, 3) arrays.
     """
 
-    def __init__(self, meshes: Iterable[Triangle] = ()):
-        tris = list(meshes)
-        for t in tris:
-            if not isinstance(t, Triangle):
+    def __init__(self, meshes: Iterable = ()):
+        items = list(meshes)
+        for t in items:
+            if not isinstance(t, (Triangle, SphereMesh)):
                 raise UnsupportedVariant(f"BvhMesh over {type(t).__name__} cannot cross the C ABI")
+        tris = [t for t in items if isinstance(t, Triangle)]
+        self.spheres = np.asarray([(*_vec3(b.pos), float(b.radius)) for b in items if isinstance(b, SphereMesh)],
+                                  np.float32).reshape(-1, 4)
         if tris:
             self.vertices = np.stack([t.vertices for t in tris]).astype(np.float32)
             self.normals = np.stack([t.normals for t in tris]).astype(np.float32)
         else:
             self.vertices = np.zeros((0, 3, 3), np.float32)
             self.normals = np.zeros((0, 3, 3), np.float32)
+        # bvh.rs:36-44: the mean of the sub-meshes' centres, in f64
+        acc = np.zeros(3)
+        for m in items:
+            acc = acc + m.centre()
+        self._centre = acc / len(items) if items else np.full(3, np.nan)
 
     @staticmethod
     def from_arrays(vertices, normals) -> "BvhMesh":
@@ -262,10 +407,15 @@ class BvhMesh:
         m.normals = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3, 3)
         if m.vertices.shape != m.normals.shape:
             raise ValueError("vertices and normals must have the same shape")
+        if len(m.vertices):
+            m._centre = m.vertices.astype(np.float64).sum(axis=1).mean(axis=0) / 3.0
         return m
 
+    def centre(self) -> np.ndarray:
+        return self._centre
+
     def __len__(self):
-        return self.vertices.shape[0]
+        return self.vertices.shape[0] + self.spheres.shape[0]
 
 
 @dataclass
@@ -277,6 +427,10 @@ class AxisBoxMesh:
     def new_centred(centre, size) -> "AxisBoxMesh":
         c, s = np.asarray(centre, float), np.asarray(size, float)
         return AxisBoxMesh(tuple(c + s / 2), tuple(c - s / 2))
+
+    def centre(self) -> np.ndarray:  # axis_box.rs:26-33: (min + max) / 2
+        a, b = np.asarray(_vec3(self.a)), np.asarray(_vec3(self.b))
+        return (np.minimum(a, b) + np.maximum(a, b)) / 2.0
 
 
 @dataclass
@@ -322,6 +476,9 @@ class ParallelogramMesh:
     def __post_init__(self):
         self.plane = _planar(self.plane)
 
+    def centre(self) -> np.ndarray:  # parallelogram.rs:64: the corner p
+        return np.asarray(self.plane.p, np.float64)
+
 
 @dataclass
 class InfinitePlaneMesh:
@@ -341,6 +498,9 @@ class CylinderMesh:
     p1: tuple
     p2: tuple
     radius: float
+
+    def centre(self) -> np.ndarray:  # cylinder.rs:40
+        return (np.asarray(_vec3(self.p1)) + np.asarray(_vec3(self.p2))) / 2.0
 
 
 @dataclass
@@ -382,9 +542,29 @@ class RaymarchedIsosurfaceMesh:
 # ---------------------------------------------------------------------------
 @dataclass(eq=False)
 class SimpleObject:
+    """object/simple.rs. `transform` (None, a Transform3, an ObjectTransform
+    or a 4 x 4 / 3 x 4 matrix) maps mesh space to world space; like
+    SimpleObject::new it is corrected to act about the mesh's centre, unless
+    the object was made by `new_uncorrected`."""
     mesh: Any
     material: Any
     transform: Any = None
+    corrected: bool = True
+
+    @staticmethod
+    def new(mesh, material, transform=None) -> "SimpleObject":
+        return SimpleObject(mesh, material, transform)
+
+    @staticmethod
+    def new_uncorrected(mesh, material, transform=None) -> "SimpleObject":
+        return SimpleObject(mesh, material, transform, corrected=False)
+
+    def object_transform(self) -> ObjectTransform:
+        t = ObjectTransform(_transform3(self.transform))
+        if self.corrected and not t.is_identity:
+            centre = self.mesh.centre() if hasattr(self.mesh, "centre") else np.zeros(3)
+            t = t.with_correction(centre)
+        return t
 
 
 @dataclass(eq=False)
@@ -413,10 +593,7 @@ StandardScene = Scene
 # Flattening
 # ---------------------------------------------------------------------------
 def _identity(t) -> bool:
-    if t is None:
-        return True
-    a = np.asarray(t, dtype=float)
-    return a.shape == (4, 4) and np.array_equal(a, np.eye(4))
+    return _transform3(t).is_identity()
 
 
 class FlatScene:
@@ -433,6 +610,9 @@ class FlatScene:
         self.quads, self.quad_mat = [], []
         self.cylinders, self.cyl_mat = [], []
         self.planes, self.plane_mat, self.plane_wrap = [], [], []
+        # per transformed object: its corrected 3 x 4 matrix; per primitive: its index
+        self.transforms: list = []
+        self.sphere_xf, self.tri_xf, self.box_xf, self.quad_xf, self.cyl_xf = [], [], [], [], []
         self.skybox = A.RG_SKY_SIMPLE
         self.n_meshes = 0
 
@@ -449,36 +629,53 @@ class FlatScene:
                 self.add(o)
             return
         if isinstance(obj, SimpleObject):
-            if not _identity(obj.transform):
-                raise UnsupportedVariant("non-identity ObjectTransform is not supported by the GPU path")
             mesh, mat = obj.mesh, self.material(obj.material)
+            ot = obj.object_transform()
+            xf = A.RG_NO_TRANSFORM
+            if not ot.is_identity:
+                if isinstance(mesh, (RaymarchedIsosurfaceMesh, InfinitePlaneMesh)):
+                    raise UnsupportedVariant(f"a transformed {type(mesh).__name__} is not supported by the GPU path")
+                if not np.all(np.isfinite(ot.transform.matrix)) or abs(np.linalg.det(ot.transform.matrix[:3, :3])) == 0:
+                    raise ValueError("an object transform must be finite and invertible")
+                xf = len(self.transforms)
+                self.transforms.append(ot.transform.matrix[:3].copy())
             if isinstance(mesh, SphereMesh):
                 self.spheres.append((*_vec3(mesh.pos), float(mesh.radius)))
                 self.sphere_mat.append(mat)
+                self.sphere_xf.append(xf)
             elif isinstance(mesh, Triangle):
                 self.tri_v.append(np.asarray(mesh.vertices, np.float32).reshape(1, 3, 3))
                 self.tri_n.append(np.asarray(mesh.normals, np.float32).reshape(1, 3, 3))
                 self.tri_mat.append(np.full(1, mat, np.uint32))
                 self.tri_mesh.append(np.full(1, -1, np.int32))
+                self.tri_xf.append(np.full(1, xf, np.uint32))
             elif isinstance(mesh, BvhMesh):
-                n = len(mesh)
+                n = mesh.vertices.shape[0]
                 if n:
                     self.tri_v.append(mesh.vertices)
                     self.tri_n.append(mesh.normals)
                     self.tri_mat.append(np.full(n, mat, np.uint32))
                     self.tri_mesh.append(np.full(n, self.n_meshes, np.int32))
+                    self.tri_xf.append(np.full(n, xf, np.uint32))
                     self.n_meshes += 1
+                for b in mesh.spheres:  # spheres of the mesh: one object each, same material and transform
+                    self.spheres.append(tuple(float(x) for x in b))
+                    self.sphere_mat.append(mat)
+                    self.sphere_xf.append(xf)
             elif isinstance(mesh, AxisBoxMesh):
                 self.boxes.append((*_vec3(mesh.a), *_vec3(mesh.b)))
                 self.box_mat.append(mat)
+                self.box_xf.append(xf)
             elif isinstance(mesh, RaymarchedIsosurfaceMesh):
                 self.sdfs.append(self._sdf(mesh, mat))
             elif isinstance(mesh, ParallelogramMesh):
                 self.quads.append(mesh.plane.flat())
                 self.quad_mat.append(mat)
+                self.quad_xf.append(xf)
             elif isinstance(mesh, CylinderMesh):
                 self.cylinders.append((*_vec3(mesh.p1), *_vec3(mesh.p2), float(mesh.radius)))
                 self.cyl_mat.append(mat)
+                self.cyl_xf.append(xf)
             elif isinstance(mesh, InfinitePlaneMesh):
                 self.planes.append(mesh.plane.flat())
                 self.plane_mat.append(mat)
@@ -488,7 +685,7 @@ class FlatScene:
                 raise UnsupportedVariant(f"mesh {type(mesh).__name__} cannot cross the C ABI")
         elif isinstance(obj, VolumetricObject):
             if not _identity(obj.transform):
-                raise UnsupportedVariant("non-identity ObjectTransform is not supported by the GPU path")
+                raise UnsupportedVariant("a transformed VolumetricObject is not supported by the GPU path")
             v = A.rg_volume()
             if isinstance(obj.mesh, SphereMesh):
                 v.boundary = A.RG_BOUNDARY_SPHERE
@@ -533,11 +730,13 @@ class FlatScene:
             self.a_tri_n = np.ascontiguousarray(np.concatenate(self.tri_n).astype(f32))
             self.a_tri_mat = np.ascontiguousarray(np.concatenate(self.tri_mat))
             self.a_tri_mesh = np.ascontiguousarray(np.concatenate(self.tri_mesh))
+            self.a_tri_xf = np.ascontiguousarray(np.concatenate(self.tri_xf).astype(u32))
         else:
             self.a_tri_v = np.zeros((0, 3, 3), f32)
             self.a_tri_n = np.zeros((0, 3, 3), f32)
             self.a_tri_mat = np.zeros(0, u32)
             self.a_tri_mesh = np.zeros(0, np.int32)
+            self.a_tri_xf = np.zeros(0, u32)
         self.a_boxes = np.ascontiguousarray(np.asarray(self.boxes, f32).reshape(-1, 6))
         self.a_box_mat = np.ascontiguousarray(np.asarray(self.box_mat, u32))
         self.a_quads = np.ascontiguousarray(np.asarray(self.quads, f32).reshape(-1, 9))
@@ -547,6 +746,11 @@ class FlatScene:
         self.a_planes = np.ascontiguousarray(np.asarray(self.planes, f32).reshape(-1, 9))
         self.a_plane_mat = np.ascontiguousarray(np.asarray(self.plane_mat, u32))
         self.a_plane_wrap = np.ascontiguousarray(np.asarray(self.plane_wrap, u32))
+        self.a_transforms = np.ascontiguousarray(np.asarray(self.transforms, np.float64).reshape(-1, 12))
+        self.a_sphere_xf = np.ascontiguousarray(np.asarray(self.sphere_xf, u32))
+        self.a_box_xf = np.ascontiguousarray(np.asarray(self.box_xf, u32))
+        self.a_quad_xf = np.ascontiguousarray(np.asarray(self.quad_xf, u32))
+        self.a_cyl_xf = np.ascontiguousarray(np.asarray(self.cyl_xf, u32))
         self.c_volumes = (A.rg_volume * max(1, len(self.volumes)))(*self.volumes)
         self.c_sdfs = (A.rg_sdf * max(1, len(self.sdfs)))(*self.sdfs)
         self.c_materials = (A.rg_material * max(1, len(self.materials)))(*self.materials)
@@ -567,6 +771,12 @@ class FlatScene:
         d.n_cylinders, d.cylinders, d.cylinder_material = len(self.a_cyls), fp(self.a_cyls), up(self.a_cyl_mat)
         d.n_planes, d.planes, d.plane_material = len(self.a_planes), fp(self.a_planes), up(self.a_plane_mat)
         d.plane_uv_wrap = up(self.a_plane_wrap)
+        if len(self.a_transforms):
+            d.n_transforms = len(self.a_transforms)
+            d.transforms = self.a_transforms.ctypes.data_as(C.POINTER(C.c_double))
+            d.sphere_transform, d.tri_transform = up(self.a_sphere_xf), up(self.a_tri_xf)
+            d.box_transform, d.quad_transform = up(self.a_box_xf), up(self.a_quad_xf)
+            d.cylinder_transform = up(self.a_cyl_xf)
         self.desc = d
         return self
 

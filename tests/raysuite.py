@@ -97,3 +97,47 @@ def planar_scene(seed=0):
         objs.append(SimpleObject(SphereMesh(tuple(rng.uniform(-3, 3, 3)), float(rng.uniform(0.1, 0.6))),
                                  LambertianMaterial((0.5, 0.5, 0.5))))
     return Scene(objects=objs)
+
+
+def transform_scene(seed=0, rigid=True):
+    """Transformed boxes, spheres, parallelograms, cylinders and one triangle
+    mesh (rotations about random axes and translations; with rigid=False also
+    per-axis scales and shears), among a few untransformed primitives."""
+    from rayna_gb300.scene import CylinderMesh, ParallelogramMesh, Planar, Transform3
+    rng = np.random.Generator(np.random.PCG64(seed))
+
+    def xf():
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        t = Transform3.from_axis_angle(ax, float(rng.uniform(-np.pi, np.pi)))
+        if not rigid:
+            m = np.eye(4)
+            m[:3, :3] = np.diag(rng.uniform(0.4, 2.5, 3))
+            m[0, 1] = rng.uniform(-0.5, 0.5)
+            t = Transform3(m).then(t)
+        return t.then_translate(rng.uniform(-0.5, 0.5, 3))
+
+    objs = []
+    for _ in range(30):
+        c = rng.uniform(-3, 3, 3)
+        s = rng.uniform(0.1, 1.0, 3)
+        objs.append(SimpleObject(AxisBoxMesh(tuple(c - s / 2), tuple(c + s / 2)), LambertianMaterial(tuple(rng.random(3))), xf()))
+    for _ in range(20):
+        objs.append(SimpleObject(SphereMesh(tuple(rng.uniform(-3, 3, 3)), float(rng.uniform(0.1, 0.6))),
+                                 MetalMaterial((0.8, 0.8, 0.8), 0.1), xf()))
+    for _ in range(30):
+        p = rng.uniform(-3, 3, 3)
+        objs.append(SimpleObject(ParallelogramMesh(Planar.new(p, rng.normal(size=3) * 0.7, rng.normal(size=3) * 0.7)),
+                                 LambertianMaterial(tuple(rng.random(3))), xf()))
+    for _ in range(20):
+        p1 = rng.uniform(-3, 3, 3)
+        p2 = p1 + rng.normal(size=3) * rng.uniform(0.1, 1.5)
+        objs.append(SimpleObject(CylinderMesh(tuple(p1), tuple(p2), float(rng.uniform(0.05, 0.5))),
+                                 LambertianMaterial((0.5, 0.5, 0.5)), xf()))
+    verts, norms = presets.displaced_icosphere(3, (1.0, 0.5, -1.0), 0.8, seed)
+    objs.append(SimpleObject(BvhMesh.from_arrays(verts, norms), LambertianMaterial((0.7, 0.7, 0.7)), xf()))
+    for _ in range(10):
+        c = rng.uniform(-3, 3, 3)
+        objs.append(SimpleObject(AxisBoxMesh(tuple(c - 0.3), tuple(c + 0.3)), LambertianMaterial((0.5, 0.5, 0.5))))
+        objs.append(SimpleObject(SphereMesh(tuple(rng.uniform(-3, 3, 3)), 0.3), LambertianMaterial((0.5, 0.5, 0.5))))
+    return Scene(objects=objs)

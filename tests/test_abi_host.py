@@ -15,7 +15,7 @@ from rayna_gb300 import _abi as A
 from rayna_gb300 import presets
 from rayna_gb300.scene import (
     AxisBoxMesh, BvhMesh, DielectricMaterial, LambertianMaterial, RaymarchedIsosurfaceMesh, Scene, SdfTorus,
-    SimpleObject, SphereMesh, Triangle, UnsupportedVariant, VolumetricObject, IsotropicMaterial, flatten,
+    SimpleObject, SphereMesh, Transform3, Triangle, UnsupportedVariant, VolumetricObject, IsotropicMaterial, flatten,
 )
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "rayna_gpu.h")
@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
     for s in syms:
         assert hasattr(lib, s), s
     assert set(syms) == set(A.SIGNATURES), "ctypes signatures must cover the header exactly"
-    assert lib.rg_abi_version() == 4
+    assert lib.rg_abi_version() == 5
 
 
 def test_struct_sizes_match_header_layout():
@@ -124,8 +124,20 @@ def test_flatten_order_and_unsupported_variants():
     flat = flatten(Scene(objects=objs))
     assert (flat.desc.n_spheres, flat.desc.n_boxes, flat.desc.n_sdfs) == (1, 1, 1)
     assert flat.desc.n_materials == 3
-    with pytest.raises(UnsupportedVariant):
+    with pytest.raises(ValueError):  # not affine: the bottom row is not (0, 0, 0, 1)
         flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial(), transform=np.eye(4) * 2)]))
+    scaled = Transform3.from_scale((2, 2, 2))
+    flat = flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial(), transform=scaled)]))
+    assert flat.desc.n_transforms == 1 and flat.desc.sphere_transform[0] == 0
+    with pytest.raises(UnsupportedVariant):
+        flatten(Scene(objects=[SimpleObject(RaymarchedIsosurfaceMesh(SdfTorus((0, 0, 0), 1.0, 0.3)),
+                                            LambertianMaterial(), transform=scaled)]))
+    with pytest.raises(UnsupportedVariant):
+        flatten(Scene(objects=[VolumetricObject(SphereMesh((0, 0, 0), 1.0), IsotropicMaterial((1, 1, 1)), 0.5,
+                                                transform=scaled)]))
+    with pytest.raises(ValueError):
+        flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial(),
+                                            transform=Transform3.from_scale((1, 0, 1)))]))
     with pytest.raises(UnsupportedVariant):
         flatten(Scene(objects=[SimpleObject(RaymarchedIsosurfaceMesh(lambda p: 0.0), LambertianMaterial())]))
 

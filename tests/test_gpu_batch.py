@@ -67,3 +67,21 @@ def test_batch_rejects_launch_shapes_it_cannot_run():
             assert err.status == 1 and "threads per block" in str(err)
         else:
             b.render(seed=1)
+
+
+def test_batch_with_transformed_objects():
+    """The reference's Cornell preset (rotated boxes) in both batched forms
+    renders what a standalone renderer renders with the same frame keys."""
+    from rayna_gb300.scene import RenderOpts
+    scene, cam, _ = presets.cornell()
+    items = [(scene, cam, RenderOpts(width=40, height=32, samples=8, ray_depth=6))] + small_batch()[:2]
+    for form in ("wavefront", "tiles"):
+        with BatchRenderer(items) as b:
+            b.set_tuning(form=form)
+            st = b.render(seed=21)
+            assert st.error_flags == 0
+            img = b.image(0)
+            key = b.item_seed(21, 0)
+        with Renderer.new_from(scene, cam, items[0][2], 0) as r:
+            ref = r.render(seed=key).img
+        np.testing.assert_array_equal(img, ref)

@@ -19,7 +19,9 @@ from oracle import binding as ob
 from rayna_gb300 import Renderer, presets
 from rayna_gb300.scene import Camera, RenderOpts, flatten
 
-from raysuite import box_scene, planar_scene, rays_at, sdf_scene, sphere_scene, triangle_scene, volume_scene
+from raysuite import (
+    box_scene, planar_scene, rays_at, sdf_scene, sphere_scene, transform_scene, triangle_scene, volume_scene,
+)
 
 pytestmark = pytest.mark.gpu
 EPS32 = np.finfo(np.float32).eps
@@ -143,9 +145,11 @@ def axis_aligned_rays(rng, n, lo, hi):
 
 
 @pytest.mark.parametrize("bvh_width", [2, 8])
-@pytest.mark.parametrize("suite", ["spheres", "triangles", "mesh", "boxes", "sdf_analytic", "axis_aligned", "planar"])
+@pytest.mark.parametrize("suite", ["spheres", "triangles", "mesh", "boxes", "sdf_analytic", "axis_aligned", "planar",
+                                   "transformed", "transformed_scaled", "cornell"])
 def test_query_bit_exact_vs_f32_oracle(suite, bvh_width):
-    seeds = {"spheres": 1, "triangles": 2, "mesh": 7, "boxes": 3, "sdf_analytic": 4, "axis_aligned": 8, "planar": 9}
+    seeds = {"spheres": 1, "triangles": 2, "mesh": 7, "boxes": 3, "sdf_analytic": 4, "axis_aligned": 8, "planar": 9,
+             "transformed": 10, "transformed_scaled": 11, "cornell": 12}
     rng = np.random.Generator(np.random.PCG64(seeds[suite]))
     if suite == "spheres":
         scene = sphere_scene()
@@ -159,6 +163,12 @@ def test_query_bit_exact_vs_f32_oracle(suite, bvh_width):
     elif suite == "planar":
         scene = planar_scene()
         o, d = rays_at(rng, 20000, (-3, -3, -3), (3, 3, 3))
+    elif suite in ("transformed", "transformed_scaled"):
+        scene = transform_scene(seed=5, rigid=suite == "transformed")
+        o, d = rays_at(rng, 20000, (-3.5, -3.5, -3.5), (3.5, 3.5, 3.5))
+    elif suite == "cornell":
+        scene = presets.cornell()[0]
+        o, d = rays_at(rng, 10000, (0.02, 0.02, 0.02), (0.98, 0.98, 0.98))
     elif suite == "axis_aligned":
         scene = presets.cornell_mesh(level=4)[0]
         o, d = axis_aligned_rays(rng, 10000, (0.02, 0.02, 0.02), (0.98, 0.98, 0.98))

@@ -1,0 +1,172 @@
+"""Oracle pins for ObjectTransform (object/transform.rs) and the Transform3
+algebra of the scene API (CPU).
+
+Known answers worked out by hand from the reference's rules: the ray is
+mapped into mesh space by the inverse transform (origin and direction, the
+direction normalised again), the mesh is tested there, and the hit point is
+mapped back; both normals are mapped by the transform's linear part (not its
+inverse transpose) and normalised; the distance is the world-space length
+from the ray's origin to the mapped point. SimpleObject::new corrects the
+transform to act about the mesh's centre (object/simple.rs:67-71).
+Then the f32 oracle (the device's operation order) against the faithful f64
+oracle on seeded ray suites.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import binding as ob
+from rayna_gb300 import presets
+from rayna_gb300.scene import (
+    Angle, AxisBoxMesh, BvhMesh, LambertianMaterial, ObjectTransform, Scene, SimpleObject, SphereMesh, Transform3,
+    flatten,
+)
+
+from raysuite import rays_at, transform_scene
+
+POLICIES = [ob.POLICY_REF_F64, ob.POLICY_GPU_F32]
+Y = (0.0, 1.0, 0.0)
+
+
+def q(flat, o, d, policy, pretest=True):
+    h, t64, n64 = ob.query(flat, np.array([o], np.float32), np.array([d], np.float32), policy=policy, pretest=pretest)
+    return h[0], t64[0], n64[0]
+
+
+def test_transform3_algebra():
+    r = Transform3.from_axis_angle(Y, Angle.from_degrees(90.0))
+    np.testing.assert_allclose(r.map_vector((1, 0, 0)), (0, 0, -1), atol=1e-15)  # right-handed about +Y
+    np.testing.assert_allclose(r.map_vector((0, 0, 1)), (1, 0, 0), atol=1e-15)
+    t = Transform3.from_translation((1, 2, 3))
+    # `a.then(b)`: a first, then b
+    np.testing.assert_allclose(r.then(t).map_point((1, 0, 0)), (1, 2, 2), atol=1e-15)
+    np.testing.assert_allclose(t.then(r).map_point((1, 0, 0)), (3, 2, -2), atol=1e-15)
+    np.testing.assert_allclose(t.then_translate((1, 1, 1)).map_point((0, 0, 0)), (2, 3, 4))
+    m = Transform3.from_scale_rotation_translation((2, 1, 1), Y, Angle.from_degrees(90.0), (0, 0, 5))
+    np.testing.assert_allclose(m.map_point((1, 0, 0)), (0, 0, 3), atol=1e-15)
+    np.testing.assert_allclose(m.inverse().map_point((0, 0, 3)), (1, 0, 0), atol=1e-15)
+    # new_corrected: rotation and scale act about the centre, which stays put
+    c = (0.381, 0.2975, 0.2655)
+    ot = ObjectTransform.new_corrected(Transform3.from_axis_angle(Y, Angle.from_degrees(15.0)), c)
+    np.testing.assert_allclose(ot.transform.map_point(c), c, atol=1e-15)
+    assert ObjectTransform.new(None).is_identity and not ot.is_identity
+    with pytest.raises(ValueError):
+        Transform3(np.eye(4) * 2)
+
+
+def test_mesh_centres_for_the_correction():
+    assert np.allclose(AxisBoxMesh((1, 0, 0), (0, 2, 4)).centre(), (0.5, 1, 2))
+    m = BvhMesh([SphereMesh((0, 0, 0), 1.0), SphereMesh((2, 0, 0), 1.0)])
+    assert np.allclose(m.centre(), (1, 0, 0))  # bvh.rs:36-44: mean of the sub-meshes' centres
+    obj = SimpleObject(AxisBoxMesh((0, 0, 0), (2, 2, 2)), LambertianMaterial(), Transform3.from_scale((2, 2, 2)))
+    np.testing.assert_allclose(obj.object_transform().transform.map_point((1, 1, 1)), (1, 1, 1))
+    raw = SimpleObject.new_uncorrected(AxisBoxMesh((0, 0, 0), (2, 2, 2)), LambertianMaterial(),
+                                       Transform3.from_scale((2, 2, 2)))
+    np.testing.assert_allclose(raw.object_transform().transform.map_point((1, 1, 1)), (2, 2, 2))
+
+
+def one(mesh, transform, uncorrected=False):
+    make = SimpleObject.new_uncorrected if uncorrected else SimpleObject
+    return flatten(Scene(objects=[make(mesh, LambertianMaterial((0.5, 0.5, 0.5)), transform)]))
+
+
+@pytest.mark.parametrize("policy", POLICIES)
+def test_rotated_box_known_answers(policy):
+    # a 2 x 1 x 0.5 box about the origin, turned 90 degrees about +Y: x spans
+    # [-0.25, 0.25] and z spans [-1, 1] in world space
+    flat = one(AxisBoxMesh((-1, -0.5, -0.25), (1, 0.5, 0.25)), Transform3.from_axis_angle(Y, Angle.from_degrees(90)))
+    h, t, _ = q(flat, (0.1, 0.2, 5.0), (0, 0, -1), policy)
+    assert h["hit"] == 1 and abs(t - 4.0) < 1e-5
+    np.testing.assert_allclose(h["normal"], (0, 0, 1), atol=1e-6)
+    np.testing.assert_allclose(h["ray_normal"], (0, 0, 1), atol=1e-6)
+    h, t, _ = q(flat, (5.0, 0.2, 0.5), (-1, 0, 0), policy)
+    assert h["hit"] == 1 and abs(t - 4.75) < 1e-5
+    np.testing.assert_allclose(h["normal"], (1, 0, 0), atol=1e-6)
+    assert q(flat, (5.0, 0.2, 1.5), (-1, 0, 0), policy)[0]["hit"] == 0  # beyond the turned box's z extent
+    # the same ray would hit the unturned box
+    plain = one(AxisBoxMesh((-1, -0.5, -0.25), (1, 0.5, 0.25)), None)
+    assert q(plain, (5.0, 0.2, 0.1), (-1, 0, 0), policy)[0]["hit"] == 1
+
+
+@pytest.mark.parametrize("policy", POLICIES)
+def test_scaled_sphere_distance_and_normal(policy):
+    # unit sphere at the origin scaled by (2, 1, 1): an ellipsoid
+    flat = one(SphereMesh((0, 0, 0), 1.0), Transform3.from_scale((2, 1, 1)))
+    h, t, _ = q(flat, (5.0, 0.0, 0.0), (-1, 0, 0), policy)
+    assert h["hit"] == 1 and abs(t - 3.0) < 1e-5  # world distance, not the mesh-space 4
+    np.testing.assert_allclose(h["normal"], (1, 0, 0), atol=1e-6)
+    # a hit where the mesh-space normal is (1, 1, 0)/sqrt(2): the reference maps
+    # it by the transform itself, giving normalize(2, 1, 0) (the true surface
+    # normal of the ellipsoid would be normalize(0.5, 1, 0))
+    s = 1.0 / math.sqrt(2.0)
+    p = np.array([2 * s, s, 0.0])
+    o = p + np.array([0.0, 3.0, 0.0])
+    h, t, _ = q(flat, o, (0, -1, 0), policy)
+    assert h["hit"] == 1 and abs(t - 3.0) < 1e-5
+    np.testing.assert_allclose(h["normal"], np.array([2, 1, 0]) / math.sqrt(5), atol=1e-5)
+
+
+@pytest.mark.parametrize("policy", POLICIES)
+def test_uncorrected_transform_moves_the_mesh(policy):
+    box = AxisBoxMesh((1, -0.5, -0.5), (2, 0.5, 0.5))
+    turn = Transform3.from_axis_angle(Y, Angle.from_degrees(180))
+    # corrected: the box turns in place; uncorrected: about the origin, to x in [-2, -1]
+    assert q(one(box, turn), (1.5, 0, 5), (0, 0, -1), policy)[0]["hit"] == 1
+    assert q(one(box, turn, uncorrected=True), (1.5, 0, 5), (0, 0, -1), policy)[0]["hit"] == 0
+    h, t, _ = q(one(box, turn, uncorrected=True), (-1.5, 0, 5), (0, 0, -1), policy)
+    assert h["hit"] == 1 and abs(t - 4.5) < 1e-5
+
+
+@pytest.mark.parametrize("rigid", [True, False])
+def test_f32_oracle_agrees_with_f64_on_transform_suite(rigid):
+    rng = np.random.Generator(np.random.PCG64(31))
+    flat = flatten(transform_scene(seed=3, rigid=rigid))
+    o, d = rays_at(rng, 4000, (-3.5, -3.5, -3.5), (3.5, 3.5, 3.5))
+    h32, _, _ = ob.query(flat, o, d, policy=ob.POLICY_GPU_F32, pretest="brute")
+    h64, t64, _ = ob.query(flat, o, d, policy=ob.POLICY_REF_F64, pretest=True)
+    agree = np.mean(h32["hit"] == h64["hit"])
+    m = (h32["hit"] == 1) & (h64["hit"] == 1) & (h32["prim"] == h64["prim"])
+    same_prim = m.sum() / max(1, (h64["hit"] == 1).sum())
+    rel = np.abs(h32["t"][m] - t64[m]) / np.maximum(np.abs(t64[m]), 1e-30)
+    print(f"transform suite rigid={rigid}: hit agreement {agree:.5f}, same primitive {same_prim:.5f}, "
+          f"median rel err {np.median(rel):.2e}")
+    assert agree >= 0.998
+    assert np.median(rel) < 1e-6
+    if rigid:
+        assert same_prim >= 0.995
+    else:
+        # Under scaling the reference bounds mesh-space distances by the
+        # world-space bound, so it can keep a hit farther than the closest (on
+        # this suite it does for about a sixth of the rays); the device's rule
+        # keeps the closest, so its distance is never the larger one.
+        both = (h32["hit"] == 1) & (h64["hit"] == 1)
+        closer = h32["t"][both] <= t64[both] * (1 + 1e-4) + 1e-6  # f32 through an ill-conditioned map: ~1e-5 relative
+        assert np.mean(closer) >= 0.999
+        assert same_prim < 0.99  # the quirk shows on this suite
+
+
+def test_structured_oracle_equals_brute_force_on_transform_suite():
+    rng = np.random.Generator(np.random.PCG64(32))
+    flat = flatten(transform_scene(seed=4))
+    o, d = rays_at(rng, 3000, (-3.5, -3.5, -3.5), (3.5, 3.5, 3.5))
+    a, _, _ = ob.query(flat, o, d, policy=ob.POLICY_GPU_F32, pretest=True)
+    b, _, _ = ob.query(flat, o, d, policy=ob.POLICY_GPU_F32, pretest="brute")
+    assert np.mean(a["hit"] == b["hit"]) >= 0.9995
+    m = (a["hit"] == 1) & (b["hit"] == 1)
+    assert np.mean(a["t"][m] == b["t"][m]) >= 0.999
+
+
+def test_cornell_preset_rotated_boxes():
+    scene, cam, opts = presets.cornell()
+    flat = flatten(scene)
+    assert flat.desc.n_quads == 6 and flat.desc.n_boxes == 2 and flat.desc.n_transforms == 2
+    # the big box's centre stays put under its corrected rotation
+    m = flat.a_transforms[0].reshape(3, 4)
+    c = np.array([0.381, 0.2975, 0.2655])
+    np.testing.assert_allclose(m[:, :3] @ c + m[:, 3], c, atol=1e-12)
+    # a ray straight down onto the big box's top, through its centre
+    for policy in POLICIES:
+        h, t, _ = q(flat, (0.381, 0.9, 0.2655), (0, -1, 0), policy)
+        assert h["hit"] == 1 and abs(t - (0.9 - 0.595)) < 1e-5
+        np.testing.assert_allclose(h["normal"], (0, 1, 0), atol=1e-6)
