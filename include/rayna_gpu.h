@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 5u
+#define RG_ABI_VERSION 6u
 
 /* Status codes. 0 is success. */
 typedef enum rg_status {
@@ -56,8 +56,9 @@ typedef struct rg_renderer* rg_handle;
 /* Scene description (flattened StandardScene)                               */
 /* ------------------------------------------------------------------------ */
 
-/* Material kinds: MaterialInstance variants with a SolidTexture
- * (rayna_engine/src/material/mod.rs:168-175, texture/solid.rs:28-30). */
+/* Material kinds: MaterialInstance variants (rayna_engine/src/material/mod.rs:168-175).
+ * Their colour is `albedo` (a SolidTexture, texture/solid.rs:28-30) unless
+ * `texture` names an entry of rg_scene_desc.textures. */
 enum {
     RG_MAT_LAMBERTIAN = 0,  /* LambertianMaterial { albedo }                      material/lambertian.rs */
     RG_MAT_METAL = 1,       /* MetalMaterial { albedo, fuzz }                      material/metal.rs */
@@ -73,14 +74,55 @@ typedef struct rg_material {
     float fuzz;               /* metal */
     float refractive_index;   /* dielectric */
     float density;            /* dielectric / isotropic Beer term (material density) */
-    uint32_t reserved;        /* must be 0 */
+    uint32_t texture;         /* 0: the solid `albedo`; k > 0: texture k - 1 of rg_scene_desc.textures */
 } rg_material;
+
+/* Texture kinds (texture/mod.rs:27-37). */
+enum {
+    RG_TEX_SOLID = 0,          /* SolidTexture: `colour` (texture/solid.rs:28-30) */
+    RG_TEX_WORLD_CHECKER = 1,  /* WorldCheckerTexture (texture/checker.rs:20-27): pos_w / scale[0] + offset */
+    RG_TEX_UV_CHECKER = 2,     /* UvCheckerTexture (checker.rs:37-44): uv / scale[0] + offset.xy */
+    RG_TEX_IMAGE = 3,          /* ImageTexture (texture/image.rs:29-39): bilinear in image `image` at
+                                  offset.xy + uv * scale.xy, v flipped */
+    RG_TEX_NOISE = 4           /* World/Local/UvNoiseTexture over a Perlin source (texture/noise.rs) */
+};
+
+/* Where a noise texture samples its Perlin source (texture/noise.rs). */
+enum {
+    RG_NOISE_WORLD = 0,        /* WorldNoiseTexture: at pos_w */
+    RG_NOISE_LOCAL = 1,        /* LocalNoiseTexture: at the mesh-local point pos_l */
+    RG_NOISE_UV = 2            /* UvNoiseTexture: at uv (2-D) */
+};
+
+/* 64 bytes. A checker's `odd` / `even` are indices into the same table; the
+ * table must be acyclic, at most RG_MAX_TEXTURE_DEPTH checkers deep. */
+typedef struct rg_texture {
+    uint32_t kind;             /* RG_TEX_* */
+    uint32_t odd, even;        /* checker: the textures of odd / even cells */
+    uint32_t image;            /* image: index into rg_scene_desc.images */
+    float scale[2];            /* checker: scale[0]; image: Size2 scale; noise: the ScalePoint factor in scale[0] */
+    float offset[3];           /* world checker: xyz; uv checker and image: xy */
+    float colour[3];           /* solid: the colour */
+    uint32_t noise_seed;       /* noise: Perlin::new(seed) */
+    uint32_t noise_place;      /* noise: RG_NOISE_* */
+    uint32_t noise_channels;   /* noise: 1 = ColourSource::Greyscale; 3 = Rgb of sources seeded seed, seed+1, seed+2 */
+    uint32_t reserved;         /* must be 0 */
+} rg_texture;
+
+#define RG_MAX_TEXTURE_DEPTH 16u
+
+/* An RGB f32 image, [x][y][rgb] (core/image.rs: ndarray of shape (width, height)). */
+typedef struct rg_image {
+    uint32_t width, height;    /* both > 0 */
+    const float* rgb;          /* width x height x 3 */
+} rg_image;
 
 /* Skybox variants (rayna_engine/src/skybox/mod.rs:28-43). */
 enum {
     RG_SKY_SIMPLE = 0,  /* SimpleSkybox: lerp(white, (0.5,0.7,1), 0.5*dir.y+0.5) */
     RG_SKY_WHITE = 1,   /* WhiteSkybox */
-    RG_SKY_NONE = 2     /* NoSkybox (black) */
+    RG_SKY_NONE = 2,    /* NoSkybox (black) */
+    RG_SKY_IMAGE = 3    /* HdrImageSkybox (skybox/hdri.rs:17-26): bilinear in image `sky_image` at sphere_uv(dir) */
 };
 
 /* Constant-density medium: VolumetricObject (rayna_engine/src/object/volumetric.rs). */
@@ -157,9 +199,9 @@ typedef struct rg_scene_desc {
     const uint32_t* plane_uv_wrap;   /* n: RG_UV_WRAP_* (UvWrappingMode, infinite_plane.rs:18-45); NULL = all WRAP */
 
     /* ObjectTransform of SimpleObjects (object/transform.rs): a ray is mapped
-     * into mesh space by the inverse, tested against the mesh with the caller's
-     * interval, and the hit mapped back (point and normals by the transform,
-     * distance recomputed in world space). */
+     * into mesh space by the inverse, tested against the mesh from the caller's
+     * start, and the hit mapped back (point and normals by the transform,
+     * distance recomputed in world space and bounded by the caller's end). */
     uint32_t n_transforms;
     const double* transforms;            /* n x 12: 3 x 4 affine matrix, mesh space to world space, row-major, with
                                             SimpleObject::new's correction about the mesh centre already applied */
@@ -168,6 +210,13 @@ typedef struct rg_scene_desc {
     const uint32_t* box_transform;       /* n_boxes */
     const uint32_t* quad_transform;      /* n_quads */
     const uint32_t* cylinder_transform;  /* n_cylinders */
+
+    /* Non-solid textures (rg_material.texture) and images (ImageTexture, HdrImageSkybox). */
+    uint32_t n_textures;
+    const rg_texture* textures;
+    uint32_t n_images;
+    const rg_image* images;
+    uint32_t sky_image;              /* RG_SKY_IMAGE: index into images */
 } rg_scene_desc;
 
 #define RG_NO_TRANSFORM 0xFFFFFFFFu

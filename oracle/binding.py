@@ -37,6 +37,8 @@ def lib():
                                  C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_int, dp, dp, dp]
         L.orc_render.restype = C.c_int
         L.orc_hardware_threads.restype = C.c_int
+        L.orc_query_colour.argtypes = [C.POINTER(A.rg_scene_desc), C.c_int, C.c_uint32, fp, fp, fp]
+        L.orc_query_colour.restype = C.c_int
         _lib = L
     return _lib
 
@@ -84,6 +86,17 @@ def query(flat, origins, dirs, tmin=1e-3, tmax=3.4028235e38, volume_u=None, poli
     assert st == 0
     hits = np.frombuffer(out, dtype=HIT_DTYPE, count=n).copy()
     return hits, t64, n64
+
+
+def query_colour(flat, origins, dirs, policy=POLICY_REF_F64):
+    """The colour each ray sees at its closest hit (the material's texture
+    value or albedo, a light's emission) or the sky on a miss; (n, 3)."""
+    o = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    out = np.zeros((o.shape[0], 3), np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    assert lib().orc_query_colour(C.byref(flat.desc), policy, o.shape[0], fp(o), fp(d), fp(out)) == 0
+    return out
 
 
 def render(flat, camera, opts, seed=0, frames=1, policy=POLICY_REF_F64, gpu_sampling=False, threads=0):

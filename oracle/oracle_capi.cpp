@@ -156,6 +156,27 @@ int backward_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_
 
 }  // namespace
 
+// The colour each ray sees at its closest hit: the hit material's texture
+// value (or solid albedo; a light's emission), or the sky on a miss. For
+// known-answer tests of textures and skies.
+template <class P>
+int query_colour_impl(const rg_scene_desc* d, uint32_t n, const float* o, const float* dir, float* rgb) {
+  using T = typename P::T;
+  Scene<P> sc;
+  sc.load(*d, Options{});
+  for (uint32_t i = 0; i < n; ++i) {
+    Ray<P> r = Ray<P>::make({(T)o[3 * i], (T)o[3 * i + 1], (T)o[3 * i + 2]}, {(T)dir[3 * i], (T)dir[3 * i + 1], (T)dir[3 * i + 2]});
+    Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
+    PathRng rng(true, 0, i, 0);
+    Hit<T> h;
+    const C3 c = sc.intersect(r, iv, rng, 0, h) ? sc.colour(sc.materials[h.material], h) : sky_of<P>(sc, r);
+    rgb[3 * i] = c.r;
+    rgb[3 * i + 1] = c.g;
+    rgb[3 * i + 2] = c.b;
+  }
+  return 0;
+}
+
 extern "C" {
 
 // Path-replay adjoint on the CPU (device sampler assignment). policy 0 = f64,
@@ -200,6 +221,11 @@ int orc_render(const rg_scene_desc* d, const rg_camera* cam, const rg_render_opt
                int policy, int gpu_sampling, int threads, double* out_mean, double* out_var, double* out_seconds) {
   if (policy == 0) return render_impl<RefF64>(d, cam, opts, seed, frames, gpu_sampling, threads, out_mean, out_var, out_seconds);
   return render_impl<GpuF32>(d, cam, opts, seed, frames, 1, threads, out_mean, out_var, out_seconds);
+}
+
+int orc_query_colour(const rg_scene_desc* d, int policy, uint32_t n, const float* o, const float* dir, float* rgb) {
+  if (policy == 0) return query_colour_impl<RefF64>(d, n, o, dir, rgb);
+  return query_colour_impl<GpuF32>(d, n, o, dir, rgb);
 }
 
 int orc_hardware_threads(void) { return (int)std::thread::hardware_concurrency(); }

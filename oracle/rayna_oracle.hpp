@@ -236,6 +236,7 @@ template <class P> inline bool aabb_hit(const Aabb<typename P::T>& b, const Ray<
 template <class T> struct Hit {
   T dist = 0;
   V3<T> pos_w{0, 0, 0}, normal{0, 0, 0}, ray_normal{0, 0, 0};
+  V3<T> pos_l{0, 0, 0};  // the mesh-local point (noise textures)
   bool front_face = false;
   T u = 0, v = 0;
   uint32_t side = 0;
@@ -281,6 +282,7 @@ template <class P> struct Sphere {
     T theta = std::acos(-local.y);
     T phi = std::atan2(-local.z, local.x) + T(M_PI);
     h.u = phi / T(2 * M_PI);
+    h.pos_l = local;
     h.v = theta / T(M_PI);
     h.side = 0;
     return true;
@@ -328,6 +330,7 @@ template <class P> struct Triangle {
     h.front_face = std::signbit(det);
     h.u = u;
     h.v = v;
+    h.pos_l = {T(1) - u - v, u, v};  // barycentric (triangle.rs:92-101)
     h.side = 0;
     h.normal = nn;
     h.ray_normal = nn * (-M::signum(det));
@@ -383,6 +386,7 @@ template <class P> struct AxisBox {
         h.normal = rn * winding;
         h.front_face = !std::signbit(winding);
         h.u = (u0 / r1 + T(1)) / T(2);
+        h.pos_l = h.pos_w - centre;
         h.v = (u1 / r2 + T(1)) / T(2);
         h.side = (uint32_t)ax * 2u + (s > T(0) ? 1u : 0u);
         return true;
@@ -425,6 +429,7 @@ template <class P> struct Planar {
     h.dist = t;
     h.pos_w = M::at(ray.pos, ray.dir, t);
     V3<T> pl = h.pos_w - p;
+    h.pos_l = pl;
     h.u = M::dot(w, M::cross(pl, v));
     h.v = M::dot(w, M::cross(u, pl));
     h.normal = n;
@@ -544,6 +549,7 @@ template <class P> struct Cylinder {
     h.ray_normal = normal * inside;
     h.front_face = std::signbit(inside);
     h.side = face;
+    h.pos_l = h.pos_w - (origin + along / T(2));  // less the centre (cylinder.rs:171)
     // uv (cylinder.rs:130-172) in the frame of Vector3::any_orthonormal_pair of the axis
     V3<T> o0, o1;
     orthonormal_pair(along / length, o0, o1);
@@ -668,6 +674,7 @@ template <class P> struct Sdf {
         V3<T> n = Math<P>::normalize(g);
         h.dist = total;
         h.pos_w = pp;
+        h.pos_l = pp;
         h.normal = n;
         h.ray_normal = n;
         h.front_face = !std::signbit(d);
@@ -765,6 +772,7 @@ template <class P> struct Xform {
   // linear part and normalised, the distance recomputed in world space.
   void outgoing(const Ray<P>& world, const Ray<P>& local, Hit<T>& h) const {
     h.pos_w = xf_point<P>(fwd, Math<P>::at(local.pos, local.dir, h.dist));
+    h.pos_l = xf_point<P>(fwd, h.pos_l);
     h.normal = Math<P>::normalize(xf_vector<P>(fwd, h.normal));
     h.ray_normal = Math<P>::normalize(xf_vector<P>(fwd, h.ray_normal));
     h.dist = Math<P>::length(h.pos_w - world.pos);
@@ -967,6 +975,109 @@ struct Options {
   size_t exact_bvh_limit = 200000;
 };
 
+// ---------------------------------------------------------------------------
+// Colour arithmetic is f32 (Channel), as in the reference.
+// ---------------------------------------------------------------------------
+struct C3 { float r, g, b; };
+inline C3 operator+(C3 a, C3 b) { return {a.r + b.r, a.g + b.g, a.b + b.b}; }
+inline C3 operator*(C3 a, C3 b) { return {a.r * b.r, a.g * b.g, a.b * b.b}; }
+inline C3 operator*(C3 a, float s) { return {a.r * s, a.g * s, a.b * s}; }
+
+// ---------------------------------------------------------------------------
+// Textures (texture/*.rs), images (core/image.rs), the image sky (skybox/hdri.rs)
+// ---------------------------------------------------------------------------
+// A noise source's permutation: Fisher-Yates over 0..255 driven by SplitMix64
+// (Steele, Lea and Flood, OOPSLA 2014) seeded with `seed`, repeated to 512.
+inline void noise_permutation(uint32_t seed, uint8_t* out) {
+  uint64_t state = seed;
+  auto next = [&]() {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  uint8_t p[256];
+  for (int i = 0; i < 256; ++i) p[i] = (uint8_t)i;
+  for (int i = 255; i > 0; --i) std::swap(p[i], p[next() % (uint64_t)(i + 1)]);
+  for (int i = 0; i < 512; ++i) out[i] = p[i & 255];
+}
+
+// Perlin's improved noise (SIGGRAPH 2002) in T, the operation order of the
+// device's perlin3.
+template <class T> inline T perlin_fade(T t) { return t * t * t * (t * (t * T(6) - T(15)) + T(10)); }
+template <class T> inline T perlin_lerp(T t, T a, T b) { return a + t * (b - a); }
+template <class T> inline T perlin_grad(uint32_t h, T x, T y, T z) {
+  h &= 15u;
+  const T u = h < 8u ? x : y;
+  const T v = h < 4u ? y : (h == 12u || h == 14u ? x : z);
+  return ((h & 1u) ? -u : u) + ((h & 2u) ? -v : v);
+}
+// Saturating float-to-int conversion (NaN to 0), as the device's cvt.rzi.
+template <class T> inline uint32_t perlin_cell(T f) {
+  if (std::isnan(f)) return 0u;
+  if (f <= T(-2147483648.0)) return 0x80000000u & 255u;
+  if (f >= T(2147483647.0)) return 0x7FFFFFFFu & 255u;
+  return (uint32_t)(int64_t)f & 255u;
+}
+template <class T> inline T perlin3(const uint8_t* perm, T x, T y, T z) {
+  const T fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+  const uint32_t X = perlin_cell(fx), Y = perlin_cell(fy), Z = perlin_cell(fz);
+  x = x - fx;
+  y = y - fy;
+  z = z - fz;
+  const T u = perlin_fade(x), v = perlin_fade(y), w = perlin_fade(z);
+  auto Pm = [&](uint32_t i) { return (uint32_t)perm[i]; };
+  const uint32_t A = Pm(X) + Y, AA = Pm(A) + Z, AB = Pm(A + 1u) + Z;
+  const uint32_t B = Pm(X + 1u) + Y, BA = Pm(B) + Z, BB = Pm(B + 1u) + Z;
+  return perlin_lerp(w,
+                     perlin_lerp(v, perlin_lerp(u, perlin_grad(Pm(AA), x, y, z), perlin_grad(Pm(BA), x - T(1), y, z)),
+                                 perlin_lerp(u, perlin_grad(Pm(AB), x, y - T(1), z), perlin_grad(Pm(BB), x - T(1), y - T(1), z))),
+                     perlin_lerp(v,
+                                 perlin_lerp(u, perlin_grad(Pm(AA + 1u), x, y, z - T(1)),
+                                             perlin_grad(Pm(BA + 1u), x - T(1), y, z - T(1))),
+                                 perlin_lerp(u, perlin_grad(Pm(AB + 1u), x, y - T(1), z - T(1)),
+                                             perlin_grad(Pm(BB + 1u), x - T(1), y - T(1), z - T(1)))));
+}
+
+struct OImage { uint32_t w = 0, h = 0; std::vector<float> rgb; };  // [x][y][rgb]
+
+// Image::get_bilinear (core/image.rs:87-109). GpuF32: f32 as the device;
+// RefF64: coordinates and weights in f64, colours in f32.
+template <class P> inline C3 image_bilinear(const OImage& im, typename P::T px, typename P::T py) {
+  using T = typename P::T;
+  auto coords = [](T val, uint32_t max, uint32_t& lo, uint32_t& hi, T& frac) {
+    const T top = (T)(max - 1u);
+    T fl = std::floor(val), ce = std::ceil(val);
+    fl = std::isnan(fl) ? T(0) : std::fmin(std::fmax(fl, T(0)), top);
+    ce = std::isnan(ce) ? T(0) : std::fmin(std::fmax(ce, T(0)), top);
+    lo = (uint32_t)fl;
+    hi = (uint32_t)ce;
+    frac = val - fl;
+  };
+  uint32_t x1, x2, y1, y2;
+  T xl, yl;
+  coords(px, im.w, x1, x2, xl);
+  coords(py, im.h, y1, y2, yl);
+  auto at = [&](uint32_t x, uint32_t y) {
+    const float* c = im.rgb.data() + 3 * ((size_t)x * im.h + y);
+    return C3{c[0], c[1], c[2]};
+  };
+  auto lerp = [](C3 a, C3 b, T t) {
+    if constexpr (P::gpu) return C3{a.r + (b.r - a.r) * t, a.g + (b.g - a.g) * t, a.b + (b.b - a.b) * t};
+    else return C3{(float)(a.r + (double)(b.r - a.r) * t), (float)(a.g + (double)(b.g - a.g) * t),
+                   (float)(a.b + (double)(b.b - a.b) * t)};
+  };
+  return lerp(lerp(at(x1, y1), at(x2, y1), xl), lerp(at(x1, y2), at(x2, y2), xl), yl);
+}
+
+// rem_euclid(sum, 2) < 1: the even cells of do_checker (texture/checker.rs:46-63)
+template <class T> inline bool checker_even(T sum) {
+  T r = std::fmod(sum, T(2));
+  if (r < T(0)) r = r + T(2);
+  return r < T(1);
+}
+
 template <class P> struct Scene {
   using T = typename P::T;
   std::vector<Sphere<P>> spheres;
@@ -986,6 +1097,11 @@ template <class P> struct Scene {
   struct Mesh { std::vector<uint32_t> tris; Bvh<T> bvh; uint32_t material; Aabb<T> box; int32_t xf = -1; };
   std::vector<Mesh> meshes;
   std::vector<Xform<P>> xforms;
+  std::vector<rg_texture> textures;
+  std::vector<uint32_t> tex_perm;  // per texture: first permutation slot (noise)
+  std::vector<uint8_t> perm;       // 512 entries per slot
+  std::vector<OImage> images;
+  uint32_t sky_image = 0;
   std::vector<int32_t> sphere_xf, tri_xf, box_xf, quad_xf, cyl_xf;  // transform index, or -1
   struct Object { uint32_t kind, index; Aabb<T> box; int32_t xf = -1; };
   std::vector<Object> bounded;    // ObjectList::bvh items, in list order
@@ -1026,6 +1142,24 @@ template <class P> struct Scene {
       plane_wrap.push_back(d.plane_uv_wrap ? d.plane_uv_wrap[i] : (uint32_t)RG_UV_WRAP);
     }
     materials.assign(d.materials, d.materials + d.n_materials);
+    textures.assign(d.textures, d.textures + d.n_textures);
+    tex_perm.assign(d.n_textures, 0);
+    for (uint32_t i = 0; i < d.n_textures; ++i) {
+      if (textures[i].kind != RG_TEX_NOISE) continue;
+      tex_perm[i] = (uint32_t)(perm.size() / 512);
+      for (uint32_t c = 0; c < textures[i].noise_channels; ++c) {
+        perm.resize(perm.size() + 512);
+        noise_permutation(textures[i].noise_seed + c, perm.data() + perm.size() - 512);
+      }
+    }
+    for (uint32_t i = 0; i < d.n_images; ++i) {
+      OImage im;
+      im.w = d.images[i].width;
+      im.h = d.images[i].height;
+      im.rgb.assign(d.images[i].rgb, d.images[i].rgb + 3ull * im.w * im.h);
+      images.push_back(std::move(im));
+    }
+    sky_image = d.sky_image;
     for (uint32_t k = 0; k < d.n_transforms; ++k) {
       Xform<P> x;
       double inv[12];
@@ -1136,6 +1270,56 @@ template <class P> struct Scene {
     build_bvh(bx, top, opt.exact_bvh_limit);
   }
 
+  // Texture::value (texture/*.rs) of texture `t` at hit `h`.
+  C3 texture_value(uint32_t t, const Hit<T>& h) const {
+    for (uint32_t level = 0; level <= RG_MAX_TEXTURE_DEPTH; ++level) {
+      const rg_texture& tx = textures[t];
+      switch (tx.kind) {
+        case RG_TEX_WORLD_CHECKER: {  // WorldCheckerTexture (checker.rs:20-27)
+          const T k = (T)tx.scale[0];
+          const T sum = ((T(0) + std::floor(h.pos_w.x / k + (T)tx.offset[0])) + std::floor(h.pos_w.y / k + (T)tx.offset[1])) +
+                        std::floor(h.pos_w.z / k + (T)tx.offset[2]);
+          t = checker_even(sum) ? tx.even : tx.odd;
+          continue;
+        }
+        case RG_TEX_UV_CHECKER: {  // UvCheckerTexture (checker.rs:37-44)
+          const T k = (T)tx.scale[0];
+          const T sum = (T(0) + std::floor(h.u / k + (T)tx.offset[0])) + std::floor(h.v / k + (T)tx.offset[1]);
+          t = checker_even(sum) ? tx.even : tx.odd;
+          continue;
+        }
+        case RG_TEX_IMAGE: {  // ImageTexture::value (image.rs:29-39)
+          const T tu = (T)tx.offset[0] + h.u * (T)tx.scale[0];
+          const T tv = (T)tx.offset[1] + h.v * (T)tx.scale[1];
+          const OImage& im = images[tx.image];
+          return image_bilinear<P>(im, tu * (T)im.w, (T(1) - tv) * (T)im.h);
+        }
+        case RG_TEX_NOISE: {  // ColourSource::get (noise.rs): ScalePoint, then value / 2 + 0.5
+          V3<T> q = tx.noise_place == RG_NOISE_WORLD ? h.pos_w
+                  : (tx.noise_place == RG_NOISE_LOCAL ? h.pos_l : V3<T>{h.u, h.v, T(0)});
+          const T k = (T)tx.scale[0];
+          q = V3<T>{q.x * k, q.y * k, q.z * k};
+          const uint8_t* pm = perm.data() + 512ull * tex_perm[t];
+          const T g = perlin3<T>(pm, q.x, q.y, q.z);
+          if (tx.noise_channels == 1u) {
+            const float c = (float)(g / T(2) + T(0.5));
+            return C3{c, c, c};
+          }
+          const T gg = perlin3<T>(pm + 512, q.x, q.y, q.z), gb = perlin3<T>(pm + 1024, q.x, q.y, q.z);
+          return C3{(float)(g / T(2) + T(0.5)), (float)(gg / T(2) + T(0.5)), (float)(gb / T(2) + T(0.5))};
+        }
+        default:
+          return C3{tx.colour[0], tx.colour[1], tx.colour[2]};
+      }
+    }
+    return C3{0, 0, 0};
+  }
+  // The material's colour at a hit: its texture, or the solid albedo.
+  C3 colour(const rg_material& m, const Hit<T>& h) const {
+    if (m.texture != 0u) return texture_value(m.texture - 1u, h);
+    return C3{m.albedo[0], m.albedo[1], m.albedo[2]};
+  }
+
   bool boundary_hit(const Volume& v, const Ray<P>& r, const Interval<T>& iv, Hit<T>& h) const {
     return v.boundary == RG_BOUNDARY_SPHERE ? v.s.intersect(r, iv, h) : v.b.intersect(r, iv, h);
   }
@@ -1162,6 +1346,7 @@ template <class P> struct Scene {
     if (hit_dist > inside) return false;
     h.dist = dist;
     h.pos_w = Math<P>::at(ray.pos, ray.dir, dist);
+    h.pos_l = h.pos_w;
     if (rng.gpu || rng.injected_volume_u) {
       if (!rng.injected_volume_u) blk = rng.block(depth, kPurposeVolume0 + vi);
       h.normal = unit_sphere_from<T>((T)u01f(blk.v[1]), (T)u01f(blk.v[2]));
@@ -1371,14 +1556,6 @@ inline bool calculate_viewport(const rg_camera& c, Viewport& vp) {
   return true;
 }
 
-// ---------------------------------------------------------------------------
-// Colour arithmetic is f32 (Channel), as in the reference.
-// ---------------------------------------------------------------------------
-struct C3 { float r, g, b; };
-inline C3 operator+(C3 a, C3 b) { return {a.r + b.r, a.g + b.g, a.b + b.b}; }
-inline C3 operator*(C3 a, C3 b) { return {a.r * b.r, a.g * b.g, a.b * b.b}; }
-inline C3 operator*(C3 a, float s) { return {a.r * s, a.g * s, a.b * s}; }
-
 template <class P> inline C3 sky_colour(uint32_t sky, const Ray<P>& r) {
   if (sky == RG_SKY_WHITE) return {1, 1, 1};
   if (sky == RG_SKY_NONE) return {0, 0, 0};
@@ -1387,6 +1564,20 @@ template <class P> inline C3 sky_colour(uint32_t sky, const Ray<P>& r) {
   if constexpr (P::gpu) a = 0.5f * r.dir.y + 0.5f;
   else a = (float)((0.5 * r.dir.y) + 0.5);
   return {1.0f + (0.5f - 1.0f) * a, 1.0f + (0.7f - 1.0f) * a, 1.0f + (1.0f - 1.0f) * a};
+}
+
+// The sky of a missed ray; HdrImageSkybox (skybox/hdri.rs:17-26) samples its
+// image at sphere_uv(dir), v flipped.
+template <class P> inline C3 sky_of(const Scene<P>& sc, const Ray<P>& r) {
+  using T = typename P::T;
+  if (sc.skybox == RG_SKY_IMAGE) {
+    const T theta = std::acos(-r.dir.y);
+    const T phi = std::atan2(-r.dir.z, r.dir.x) + T(M_PI);
+    const T u = phi / T(2 * M_PI), v = theta / T(M_PI);
+    const OImage& im = sc.images[sc.sky_image];
+    return image_bilinear<P>(im, u * (T)im.w, (T(1) - v) * (T)im.h);
+  }
+  return sky_colour<P>(sc.skybox, r);
 }
 
 // Material::scatter for each variant. Returns false for None.
@@ -1464,25 +1655,17 @@ inline bool scatter(const rg_material& m, const Ray<P>& ray, const Hit<typename 
 }
 
 // Material::reflected_light factor: the colour multiplying future_col.
-template <class P> inline C3 attenuation(const rg_material& m, const Ray<P>& ray, const Hit<typename P::T>& h) {
-  C3 alb{m.albedo[0], m.albedo[1], m.albedo[2]};
-  switch (m.kind) {
-    case RG_MAT_LAMBERTIAN:
-    case RG_MAT_METAL:
-      return alb;
-    case RG_MAT_DIELECTRIC:
-      if (h.front_face) return {1, 1, 1};  // entering: future_col unchanged (dielectric.rs:63-65)
-      [[fallthrough]];
-    case RG_MAT_ISOTROPIC: {
-      double dist = (double)Math<P>::length(h.pos_w - ray.pos);
-      float tr = (float)(-(double)m.density * dist);
-      if constexpr (P::gpu) tr = -m.density * (float)dist;
-      float e = std::exp(tr);
-      return alb * e;
-    }
-    default:
-      return {0, 0, 0};
-  }
+template <class P>
+inline C3 attenuation(const Scene<P>& sc, const rg_material& m, const Ray<P>& ray, const Hit<typename P::T>& h) {
+  if (m.kind == RG_MAT_DIELECTRIC && h.front_face) return {1, 1, 1};  // entering: future_col unchanged (dielectric.rs:63-65)
+  if (m.kind > RG_MAT_ISOTROPIC) return {0, 0, 0};
+  const C3 alb = sc.colour(m, h);
+  if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) return alb;
+  double dist = (double)Math<P>::length(h.pos_w - ray.pos);
+  float tr = (float)(-(double)m.density * dist);
+  if constexpr (P::gpu) tr = -m.density * (float)dist;
+  float e = std::exp(tr);
+  return alb * e;
 }
 
 // ---------------------------------------------------------------------------
@@ -1510,16 +1693,16 @@ template <class P> struct Renderer {
     if (depth > rp.ray_depth) return {0, 0, 0};
     Hit<T> h;
     Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
-    if (!sc.intersect(ray, iv, rng, depth, h)) return sky_colour<P>(sc.skybox, ray);
+    if (!sc.intersect(ray, iv, rng, depth, h)) return sky_of<P>(sc, ray);
     const rg_material& m = sc.materials[h.material];
-    C3 emitted = m.kind == RG_MAT_LIGHT ? C3{m.albedo[0], m.albedo[1], m.albedo[2]} : C3{0, 0, 0};
+    C3 emitted = m.kind == RG_MAT_LIGHT ? sc.colour(m, h) : C3{0, 0, 0};
     C3 sum{0, 0, 0};
     for (uint32_t i = 0; i < rp.branching; ++i) {
       V dir;
       if (!scatter<P>(m, ray, h, rng, depth, dir)) continue;  // Colour::BLACK
       Ray<P> next = Ray<P>::make(h.pos_w, dir);
       C3 fut = colour_recursive(next, depth + 1, rng);
-      C3 scattered = m.kind == RG_MAT_LIGHT ? C3{0, 0, 0} : fut * attenuation<P>(m, ray, h);
+      C3 scattered = m.kind == RG_MAT_LIGHT ? C3{0, 0, 0} : fut * attenuation<P>(sc, m, ray, h);
       sum = sum + scattered;
     }
     return emitted + sum * (1.0f / (float)rp.branching);
@@ -1539,10 +1722,10 @@ template <class P> struct Renderer {
       Hit<T> h;
       Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
       if (!sc.intersect(ray, iv, rng, node, h)) {
-        L = L + w * sky_colour<P>(sc.skybox, ray);
+        L = L + w * sky_of<P>(sc, ray);
       } else {
         const rg_material& m = sc.materials[h.material];
-        if (m.kind == RG_MAT_LIGHT) L = L + w * C3{m.albedo[0], m.albedo[1], m.albedo[2]};
+        if (m.kind == RG_MAT_LIGHT) L = L + w * sc.colour(m, h);
         else if (depth < rp.ray_depth && st.size() < 32) st.push_back(Level{h, ray, w, node, 0});
       }
       bool found = false;
@@ -1553,7 +1736,7 @@ template <class P> struct Renderer {
         const rg_material& m = sc.materials[lv.h.material];
         V dir;
         if (!scatter<P>(m, lv.in, lv.h, rng, lv.node * b + i, dir)) continue;
-        C3 a = attenuation<P>(m, lv.in, lv.h);
+        C3 a = attenuation<P>(sc, m, lv.in, lv.h);
         w = lv.w * a * inv_b;
         ray = Ray<P>::make(lv.h.pos_w, dir);
         node = lv.node * b + 1 + i;
@@ -1570,7 +1753,7 @@ template <class P> struct Renderer {
   C3 mode_colour(const Ray<P>& ray, PathRng& rng) const {
     Hit<T> h;
     Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
-    if (!sc.intersect(ray, iv, rng, 0, h)) return sky_colour<P>(sc.skybox, ray);
+    if (!sc.intersect(ray, iv, rng, 0, h)) return sky_of<P>(sc, ray);
     static const float kCol[13][3] = {{1, 1, 1}, {1, 0, 0}, {1, 0.5f, 0}, {1, 1, 0}, {0.5f, 1, 0}, {0, 1, 0}, {0, 1, 0.5f},
                                       {0, 1, 1}, {0, 0.5f, 1}, {0, 0, 1}, {0.5f, 0, 1}, {1, 0, 1}, {0, 0, 0}};
     auto half = [](V v) { return C3{(float)(v.x / T(2)) + 0.5f, (float)(v.y / T(2)) + 0.5f, (float)(v.z / T(2)) + 0.5f}; };
@@ -1604,18 +1787,18 @@ template <class P> struct Renderer {
       Hit<T> h;
       Interval<T> iv = Interval<T>::range(T(1e-3), std::numeric_limits<T>::max());
       if (!sc.intersect(ray, iv, rng, depth, h)) {
-        C3 s = sky_colour<P>(sc.skybox, ray);
+        C3 s = sky_of<P>(sc, ray);
         L = L + beta * s;
         break;
       }
       const rg_material& m = sc.materials[h.material];
       if (m.kind == RG_MAT_LIGHT) {
-        L = L + beta * C3{m.albedo[0], m.albedo[1], m.albedo[2]};
+        L = L + beta * sc.colour(m, h);
         break;
       }
       V dir;
       if (!scatter<P>(m, ray, h, rng, depth, dir)) break;
-      beta = beta * attenuation<P>(m, ray, h);
+      beta = beta * attenuation<P>(sc, m, ray, h);
       ray = Ray<P>::make(h.pos_w, dir);
     }
     return L;
@@ -1697,7 +1880,7 @@ template <class P> struct Renderer {
       medium_scores(ray, hit ? h.dist : std::numeric_limits<T>::infinity(), winner, score);
       if (!hit) {
         escaped = true;
-        sky = sky_colour<P>(sc.skybox, ray);
+        sky = sky_of<P>(sc, ray);
         esc_score = score;
         break;
       }
@@ -1707,7 +1890,7 @@ template <class P> struct Renderer {
       if (m.kind == RG_MAT_LIGHT || depth == rp.ray_depth) break;
       V dir;
       if (!scatter<P>(m, ray, h, rng, depth, dir)) break;
-      C3 a = attenuation<P>(m, ray, h);
+      C3 a = attenuation<P>(sc, m, ray, h);
       if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) {
         vs.back().albdep = true;
       } else if (!(m.kind == RG_MAT_DIELECTRIC && h.front_face)) {

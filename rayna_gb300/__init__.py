@@ -12,6 +12,8 @@ from .scene import (  # noqa: F401
     LightMaterial, MetalMaterial, NoSkybox, ObjectList, RaymarchedIsosurfaceMesh, RenderMode, RenderOpts,
     Scene, SdfMandelbulb, SdfSphere, SdfTorus, SimpleObject, SimpleSkybox, SolidTexture, SphereMesh,
     StandardScene, Transform3, Triangle, UnsupportedVariant, VolumetricObject, WhiteSkybox, flatten,
+    ColourSource, DynamicTexture, HdrImageSkybox, Image, ImageTexture, LocalNoiseTexture, Perlin, ScalePoint,
+    UvCheckerTexture, UvNoiseTexture, WorldCheckerTexture, WorldNoiseTexture,
 )
 from .renderer import Render, Renderer, RenderStats  # noqa: F401
 from ._abi import RaynaError, load_library  # noqa: F401

@@ -31,7 +31,10 @@ STATUS_NAMES = {
 }
 
 RG_MAT_LAMBERTIAN, RG_MAT_METAL, RG_MAT_DIELECTRIC, RG_MAT_ISOTROPIC, RG_MAT_LIGHT = range(5)
-RG_SKY_SIMPLE, RG_SKY_WHITE, RG_SKY_NONE = range(3)
+RG_SKY_SIMPLE, RG_SKY_WHITE, RG_SKY_NONE, RG_SKY_IMAGE = range(4)
+RG_TEX_SOLID, RG_TEX_WORLD_CHECKER, RG_TEX_UV_CHECKER, RG_TEX_IMAGE, RG_TEX_NOISE = range(5)
+RG_NOISE_WORLD, RG_NOISE_LOCAL, RG_NOISE_UV = range(3)
+RG_MAX_TEXTURE_DEPTH = 16
 RG_BOUNDARY_SPHERE, RG_BOUNDARY_BOX = range(2)
 RG_SDF_SPHERE, RG_SDF_TORUS, RG_SDF_MANDELBULB = range(3)
 RG_FORM_MEGAKERNEL, RG_FORM_WAVEFRONT = range(2)
@@ -45,7 +48,18 @@ RG_BATCH_TILES = 1
 
 class rg_material(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("albedo", C.c_float * 3), ("fuzz", C.c_float),
-                ("refractive_index", C.c_float), ("density", C.c_float), ("reserved", C.c_uint32)]
+                ("refractive_index", C.c_float), ("density", C.c_float), ("texture", C.c_uint32)]
+
+
+class rg_texture(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("odd", C.c_uint32), ("even", C.c_uint32), ("image", C.c_uint32),
+                ("scale", C.c_float * 2), ("offset", C.c_float * 3), ("colour", C.c_float * 3),
+                ("noise_seed", C.c_uint32), ("noise_place", C.c_uint32), ("noise_channels", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class rg_image(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgb", C.POINTER(C.c_float))]
 
 
 class rg_volume(C.Structure):
@@ -77,6 +91,8 @@ class rg_scene_desc(C.Structure):
         ("sphere_transform", C.POINTER(C.c_uint32)), ("tri_transform", C.POINTER(C.c_uint32)),
         ("box_transform", C.POINTER(C.c_uint32)), ("quad_transform", C.POINTER(C.c_uint32)),
         ("cylinder_transform", C.POINTER(C.c_uint32)),
+        ("n_textures", C.c_uint32), ("textures", C.POINTER(rg_texture)),
+        ("n_images", C.c_uint32), ("images", C.POINTER(rg_image)), ("sky_image", C.c_uint32),
     ]
 
 

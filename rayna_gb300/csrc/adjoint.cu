@@ -134,7 +134,7 @@ __device__ void replay_sample(const GpuScene& sc, const FrameParams& fp, const A
     if (m.kind == RG_MAT_LIGHT || depth == fp.ray_depth) break;
     V3 dir;
     if (!scatter(m, ray, surf, ctx, dir)) break;
-    C3f a = attenuation(m, ray, surf);
+    C3f a = attenuation<F>(sc, m, ray, surf);
     if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) {
       albdep[K - 1] = true;
     } else if (!(m.kind == RG_MAT_DIELECTRIC && surf.front)) {
@@ -239,6 +239,8 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
   if (h->opts.ray_depth + 1 > (uint32_t)kAdjMaxVertices)
     return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward supports ray_depth <= 16");
   if (n_vol > (uint32_t)kAdjMaxVolumes) return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward supports at most 4 media");
+  if (h->host.textured)
+    return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward differentiates solid albedos: no textures or image sky");
   cudaStream_t st = h->stream;
   // Device scratch of the adjoint: image, target/adjoint image, gradients, loss.
   size_t need = (2 * npx3 + 2 * (size_t)n_mat * 3 + n_vol + 4) * sizeof(float) + sizeof(double) + 512;

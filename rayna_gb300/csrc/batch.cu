@@ -519,7 +519,7 @@ rg_status rg_batch_create(const rg_device_opts* opts, uint32_t n, const rg_scene
   }
   if (st == RG_OK) {
     b->features = b->features == F_TRI ? F_TRI
-                : (b->features == F_SPHERE ? F_SPHERE : ((b->features & F_XFORM) ? F_ANY : F_ALL));
+                : (b->features == F_SPHERE ? F_SPHERE : ((b->features & F_EXT) ? F_ANY : F_ALL));
     size_t nb = std::max<size_t>(1, n);
     if ((e = cudaMalloc((void**)&b->d_items, nb * sizeof(BatchItemDev))) != cudaSuccess ||
         (e = cudaMallocHost((void**)&b->h_items, nb * sizeof(BatchItemDev))) != cudaSuccess ||

@@ -139,8 +139,10 @@ enum : uint32_t {
   F_CYLINDER = 64u,
   F_PLANE = 128u,  // unbounded infinite planes
   F_ALL = 255u,    // every primitive kind
-  F_XFORM = 256u,  // transformed objects (a separate variant, so that scenes without them keep their registers)
-  F_ANY = F_ALL | F_XFORM,
+  // Transformed objects, non-solid textures or an image sky: a separate
+  // variant, so that scenes without them keep their registers.
+  F_EXT = 256u,
+  F_ANY = F_ALL | F_EXT,
   F_WIDE = 512u,
 };
 constexpr uint32_t kinds_of(uint32_t f) { return f & F_ANY; }
@@ -165,6 +167,11 @@ auto dispatch_features(uint32_t features, Fn&& fn) {
   }
 }
 
+// An image in HBM: `width` x `height` texels at texels[first + x * height + y].
+struct GpuImage {
+  uint32_t width, height, first, pad;
+};
+
 struct GpuScene {
   const BvhNode2* nodes;
   const GpuPrim* prims;
@@ -187,6 +194,11 @@ struct GpuScene {
   const float* quad_ext;      // per parallelogram: Planar u, v, w (9 floats)
   const float* xforms;        // per transform: inverse then forward 3 x 4 matrix, row-major (24 floats)
   const uint32_t* prim_xform; // per primitive position: its transform index (read only for flagged primitives)
+  const rg_texture* textures; // non-solid textures (rg_material::texture - 1)
+  const GpuImage* images;     // image headers; texels in `texels`
+  const float4* texels;       // every image's texels, RGB + pad, [x][y]
+  const uint8_t* perm;        // noise: per Perlin source, 512 permutation entries
+  uint32_t sky_image;         // RG_SKY_IMAGE: index into images
 };
 
 // Device error bits (rg_render_stats::error_flags).

@@ -140,6 +140,86 @@ bool affine_inverse(const double* m, double* inv) {
   return true;
 }
 
+// Textures, images and the image sky: kinds, indices, finite parameters, and
+// an acyclic checker graph at most RG_MAX_TEXTURE_DEPTH deep.
+rg_status validate_textures(rg_renderer* h, const rg_scene_desc& d) {
+  if (d.n_textures && !d.textures) return fail(h, RG_INVALID_ARG, "textures is NULL but its count is %u", d.n_textures);
+  if (d.n_images && !d.images) return fail(h, RG_INVALID_ARG, "images is NULL but its count is %u", d.n_images);
+  if (d.skybox == RG_SKY_IMAGE && d.sky_image >= d.n_images)
+    return fail(h, RG_INVALID_ARG, "sky image %u of %u", d.sky_image, d.n_images);
+  uint64_t texels = 0;
+  for (uint32_t i = 0; i < d.n_images; ++i) {
+    const rg_image& im = d.images[i];
+    if (im.width == 0 || im.height == 0 || !im.rgb) return fail(h, RG_INVALID_ARG, "image %u is empty", i);
+    const uint64_t n = (uint64_t)im.width * im.height;
+    texels += n;
+    if (texels >= (1ull << 31)) return fail(h, RG_INVALID_ARG, "images too large (limit 2^31 texels)");
+    for (uint64_t k = 0; k < 3 * n; ++k)
+      if (!std::isfinite(im.rgb[k])) return fail(h, RG_INVALID_ARG, "image %u has a non-finite texel", i);
+  }
+  for (uint32_t i = 0; i < d.n_textures; ++i) {
+    const rg_texture& t = d.textures[i];
+    if (t.kind > RG_TEX_NOISE) return fail(h, RG_UNSUPPORTED_VARIANT, "texture %u has kind %u", i, t.kind);
+    if (t.reserved != 0) return fail(h, RG_INVALID_ARG, "texture %u: reserved field must be 0", i);
+    if (!std::isfinite(t.scale[0]) || !std::isfinite(t.scale[1]) || !finite3(t.offset) || !finite3(t.colour))
+      return fail(h, RG_INVALID_ARG, "texture %u has a non-finite parameter", i);
+    if ((t.kind == RG_TEX_WORLD_CHECKER || t.kind == RG_TEX_UV_CHECKER) && (t.odd >= d.n_textures || t.even >= d.n_textures))
+      return fail(h, RG_INVALID_ARG, "checker texture %u uses textures %u, %u of %u", i, t.odd, t.even, d.n_textures);
+    if (t.kind == RG_TEX_IMAGE && t.image >= d.n_images)
+      return fail(h, RG_INVALID_ARG, "image texture %u uses image %u of %u", i, t.image, d.n_images);
+    if (t.kind == RG_TEX_NOISE && (t.noise_place > RG_NOISE_UV || (t.noise_channels != 1 && t.noise_channels != 3)))
+      return fail(h, RG_INVALID_ARG, "noise texture %u: placement %u, channels %u", i, t.noise_place, t.noise_channels);
+  }
+  // depth of each texture's checker chain; 0xFF marks one on the current path (a cycle)
+  std::vector<uint8_t> depth(d.n_textures, 0), state(d.n_textures, 0);
+  std::vector<std::pair<uint32_t, int>> stack;
+  for (uint32_t r = 0; r < d.n_textures; ++r) {
+    if (state[r] == 2) continue;
+    stack.push_back({r, 0});
+    state[r] = 1;
+    while (!stack.empty()) {
+      auto& [t, k] = stack.back();
+      const rg_texture& tx = d.textures[t];
+      const bool checker = tx.kind == RG_TEX_WORLD_CHECKER || tx.kind == RG_TEX_UV_CHECKER;
+      if (checker && k < 2) {
+        const uint32_t c = k == 0 ? tx.odd : tx.even;
+        ++k;
+        if (state[c] == 1) return fail(h, RG_INVALID_ARG, "texture %u is part of a cycle", c);
+        if (state[c] == 0) {
+          state[c] = 1;
+          stack.push_back({c, 0});
+        }
+        continue;
+      }
+      uint32_t dep = 0;
+      if (checker) dep = 1u + std::max<uint32_t>(depth[tx.odd], depth[tx.even]);
+      if (dep > RG_MAX_TEXTURE_DEPTH) return fail(h, RG_INVALID_ARG, "texture %u nests checkers deeper than %u", t, RG_MAX_TEXTURE_DEPTH);
+      depth[t] = (uint8_t)dep;
+      state[t] = 2;
+      stack.pop_back();
+    }
+  }
+  return RG_OK;
+}
+
+// A noise source's permutation of 0..255 (repeated to 512 entries): a
+// Fisher-Yates shuffle driven by SplitMix64 (Steele, Lea and Flood, OOPSLA
+// 2014) seeded with `seed`.
+void noise_permutation(uint32_t seed, uint8_t* out) {
+  uint64_t state = seed;
+  auto next = [&]() {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  uint8_t p[256];
+  for (int i = 0; i < 256; ++i) p[i] = (uint8_t)i;
+  for (int i = 255; i > 0; --i) std::swap(p[i], p[next() % (uint64_t)(i + 1)]);
+  for (int i = 0; i < 512; ++i) out[i] = p[i & 255];
+}
+
 rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
   auto need = [&](uint32_t n, const void* p, const char* what) -> bool {
     if (n > 0 && p == nullptr) { fail(h, RG_INVALID_ARG, "%s is NULL but its count is %u", what, n); return false; }
@@ -158,13 +238,18 @@ rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
                    d.n_cylinders + d.n_planes;
   if (total >= (1ull << 28)) return fail(h, RG_INVALID_ARG, "too many primitives (%llu; limit 2^28)", (unsigned long long)total);
   if (d.n_materials > kMaterialMask) return fail(h, RG_INVALID_ARG, "too many materials");
-  if (d.skybox > RG_SKY_NONE) return fail(h, RG_UNSUPPORTED_VARIANT, "skybox kind %u", d.skybox);
+  if (d.skybox > RG_SKY_IMAGE) return fail(h, RG_UNSUPPORTED_VARIANT, "skybox kind %u", d.skybox);
+  {
+    const rg_status st = validate_textures(h, d);
+    if (st != RG_OK) return st;
+  }
   for (uint32_t i = 0; i < d.n_materials; ++i) {
     const rg_material& m = d.materials[i];
     if (m.kind > RG_MAT_LIGHT) return fail(h, RG_UNSUPPORTED_VARIANT, "material %u has kind %u", i, m.kind);
     if (!finite3(m.albedo) || !std::isfinite(m.fuzz) || !std::isfinite(m.refractive_index) || !std::isfinite(m.density))
       return fail(h, RG_INVALID_ARG, "material %u has a non-finite parameter", i);
-    if (m.reserved != 0) return fail(h, RG_INVALID_ARG, "material %u: reserved field must be 0", i);
+    if (m.texture > d.n_textures)
+      return fail(h, RG_INVALID_ARG, "material %u uses texture %u of %u", i, m.texture, d.n_textures);
   }
   auto mat_ok = [&](uint32_t m, const char* what, uint32_t i) -> bool {
     if (m >= d.n_materials) { fail(h, RG_INVALID_ARG, "%s %u uses material %u of %u", what, i, m, d.n_materials); return false; }
@@ -278,6 +363,28 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
   hs.nq = d.n_quads; hs.nc = d.n_cylinders; hs.npl = d.n_planes;
   hs.sky = d.skybox;
   hs.materials.assign(d.materials, d.materials + d.n_materials);
+  // Textures and images. Each noise texture gets one permutation slot per
+  // channel (seeds seed, seed + 1, seed + 2); its `image` field holds the first.
+  hs.textures.assign(d.textures, d.textures + d.n_textures);
+  hs.perm.clear();
+  for (rg_texture& t : hs.textures) {
+    if (t.kind != RG_TEX_NOISE) continue;
+    const uint32_t slot = (uint32_t)(hs.perm.size() / 512);
+    hs.perm.resize(hs.perm.size() + 512ull * t.noise_channels);
+    for (uint32_t c = 0; c < t.noise_channels; ++c) noise_permutation(t.noise_seed + c, hs.perm.data() + 512ull * (slot + c));
+    t.image = slot;
+  }
+  hs.images.clear();
+  hs.texels.clear();
+  for (uint32_t i = 0; i < d.n_images; ++i) {
+    const rg_image& im = d.images[i];
+    hs.images.push_back(GpuImage{im.width, im.height, (uint32_t)hs.texels.size(), 0u});
+    const uint64_t n = (uint64_t)im.width * im.height;
+    for (uint64_t k = 0; k < n; ++k) hs.texels.push_back(float4{im.rgb[3 * k], im.rgb[3 * k + 1], im.rgb[3 * k + 2], 0.0f});
+  }
+  hs.sky_image = d.sky_image;
+  hs.textured = d.skybox == RG_SKY_IMAGE;
+  for (const rg_material& m : hs.materials) hs.textured = hs.textured || m.texture != 0;
   hs.volumes.assign(d.volumes, d.volumes + d.n_volumes);
   const uint32_t nbounded = hs.ns + hs.nt + hs.nb + hs.nv + hs.nq + hs.nc;
   std::vector<GpuPrim> prims(nbounded);
@@ -527,6 +634,10 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   if ((st = upload(h, ds.quad_ext, hs.quad_ext.data(), hs.quad_ext.size(), "upload parallelograms")) != RG_OK) return st;
   if ((st = upload(h, ds.xforms, hs.xforms.data(), hs.xforms.size(), "upload transforms")) != RG_OK) return st;
   if ((st = upload(h, ds.prim_xform, hs.prim_xform.data(), hs.prim_xform.size(), "upload transforms")) != RG_OK) return st;
+  if ((st = upload(h, ds.textures, hs.textures.data(), hs.textures.size(), "upload textures")) != RG_OK) return st;
+  if ((st = upload(h, ds.images, hs.images.data(), hs.images.size(), "upload images")) != RG_OK) return st;
+  if ((st = upload(h, ds.texels, hs.texels.data(), hs.texels.size(), "upload images")) != RG_OK) return st;
+  if ((st = upload(h, ds.perm, hs.perm.data(), hs.perm.size(), "upload noise")) != RG_OK) return st;
   if ((st = upload(h, ds.vol_density, hs.vol_density.data(), hs.vol_density.size(), "upload media")) != RG_OK) return st;
   if ((st = upload(h, ds.vol_prim, hs.vol_prim.data(), hs.vol_prim.size(), "upload media")) != RG_OK) return st;
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "upload scene");
@@ -541,6 +652,11 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.quad_ext = ds.quad_ext;
   g.xforms = ds.xforms;
   g.prim_xform = ds.prim_xform;
+  g.textures = ds.textures;
+  g.images = ds.images;
+  g.texels = ds.texels;
+  g.perm = ds.perm;
+  g.sky_image = hs.sky_image;
   g.vol_density = ds.vol_density;
   g.vol_prim = ds.vol_prim;
   g.n_nodes = (uint32_t)hs.nodes.size();
@@ -552,11 +668,11 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
   g.vol_base = hs.vol_base;
   g.n_tris = hs.nt;
   // Kernel variant: triangles only, spheres only, every kind, or every kind
-  // with transformed objects.
+  // with transformed objects, non-solid textures or an image sky.
   uint32_t have = (hs.ns ? F_SPHERE : 0) | (hs.nt ? F_TRI : 0) | (hs.nb ? F_BOX : 0) | (hs.nv ? F_VOL : 0) |
                   (hs.nsdf ? F_SDF : 0) | (hs.nq ? F_QUAD : 0) | (hs.nc ? F_CYLINDER : 0) | (hs.npl ? F_PLANE : 0) |
-                  (hs.prim_xform.empty() ? 0 : F_XFORM);
-  h->kinds = have == F_TRI ? F_TRI : (have == F_SPHERE ? F_SPHERE : ((have & F_XFORM) ? F_ANY : F_ALL));
+                  ((hs.textured || !hs.prim_xform.empty()) ? F_EXT : 0);
+  h->kinds = have == F_TRI ? F_TRI : (have == F_SPHERE ? F_SPHERE : ((have & F_EXT) ? F_ANY : F_ALL));
   apply_features(h);
   return RG_OK;
 }
@@ -586,7 +702,8 @@ void apply_features(rg_renderer* h) {
 }
 
 void free_scene(DeviceScene& ds) {
-  dfree(ds.nodes); dfree(ds.wnodes); dfree(ds.prims); dfree(ds.quad_ext); dfree(ds.xforms); dfree(ds.prim_xform); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
+  dfree(ds.nodes); dfree(ds.wnodes); dfree(ds.prims); dfree(ds.quad_ext); dfree(ds.xforms); dfree(ds.prim_xform);
+  dfree(ds.textures); dfree(ds.images); dfree(ds.texels); dfree(ds.perm); dfree(ds.tri_normals); dfree(ds.materials); dfree(ds.sdfs);
   dfree(ds.vol_density); dfree(ds.vol_prim);
 }
 

@@ -33,6 +33,12 @@ struct HostScene {
   std::vector<float> quad_ext;         // per parallelogram: u, v, w
   std::vector<float> xforms;           // per transform: inverse, forward (3 x 4 each)
   std::vector<uint32_t> prim_xform;    // per primitive position: transform index (empty: no transforms)
+  std::vector<rg_texture> textures;    // noise textures: `image` holds their first permutation slot
+  std::vector<GpuImage> images;
+  std::vector<float4> texels;
+  std::vector<uint8_t> perm;           // 512 entries per noise source
+  uint32_t sky_image = 0;
+  bool textured = false;               // non-solid textures or an image sky
   std::vector<float> vol_density;      // per medium
   std::vector<uint32_t> vol_prim;      // per medium: position in `prims`
 };
@@ -47,6 +53,10 @@ struct DeviceScene {
   float* quad_ext = nullptr;
   float* xforms = nullptr;
   uint32_t* prim_xform = nullptr;
+  rg_texture* textures = nullptr;
+  GpuImage* images = nullptr;
+  float4* texels = nullptr;
+  uint8_t* perm = nullptr;
   float* vol_density = nullptr;
   uint32_t* vol_prim = nullptr;
 };

@@ -477,7 +477,7 @@ __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int cou
     const float* xf = nullptr;
     Ray r = rw;
     float tend = end;  // a transformed primitive is tested on [start, inf), then bounded in world space
-    if ((F & F_XFORM) && (__float_as_uint(a.w) & kXformBit)) {
+    if ((F & F_EXT) && (__float_as_uint(a.w) & kXformBit)) {
       xf = prim_xform_of(sc, i);
       r = xf_incoming(xf, rw);
       tend = CUDART_INF_F;
@@ -516,7 +516,7 @@ __device__ __forceinline__ void test_leaf(const GpuScene& sc, int first, int cou
     } else {
       continue;
     }
-    if ((F & F_XFORM) && xf) {
+    if ((F & F_EXT) && xf) {
       const float tl = t;
       t = length3(xf_point(xf + 12, at3(r.o, r.d, tl)) - rw.o);
       if (!(t <= end)) continue;
@@ -824,6 +824,7 @@ __device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float
 // Full hit record of the closest hit.
 struct Surface {
   V3 pos, normal, ray_normal;
+  V3 pos_l;  // the mesh-local point (Intersection::pos_l), set by the extended variant only
   bool front;
   uint32_t material, prim_id, side;
   float u, v;
@@ -880,6 +881,7 @@ __device__ __forceinline__ void finalize_prim(const GpuScene& sc, const GpuPrim&
     s.front = !inside;
     s.u = s.v = 0.0f;
     if (UV) sphere_uv(local, s.u, s.v);
+    if (F & F_EXT) s.pos_l = local;  // sphere.rs:77-91
   } else if ((F & F_TRI) && kind == PK_TRIANGLE) {
     float t, u, v, det;
     triangle_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, CUDART_INF_F, t, u, v, det);
@@ -889,6 +891,7 @@ __device__ __forceinline__ void finalize_prim(const GpuScene& sc, const GpuPrim&
     s.ray_normal = n * (-signumf(det));
     s.front = signbit(det);
     s.u = u; s.v = v;
+    if (F & F_EXT) s.pos_l = v3(1.0f - u - v, u, v);  // barycentric (triangle.rs:92-101)
   } else if ((F & F_BOX) && kind == PK_BOX) {
     BoxHit bh;
     box_t(xyz(p.a), xyz(p.b), xyz(p.c), r, -CUDART_INF_F, ht, bh);
@@ -899,6 +902,7 @@ __device__ __forceinline__ void finalize_prim(const GpuScene& sc, const GpuPrim&
     s.side = (uint32_t)bh.axis * 2u + (bh.sgn > 0.0f ? 1u : 0u);
     s.u = (bh.u0 + 1.0f) / 2.0f;
     s.v = (bh.u1 + 1.0f) / 2.0f;
+    if (F & F_EXT) s.pos_l = s.pos - xyz(p.a);  // less the centre (axis_box.rs:122)
   } else if ((F & F_QUAD) && kind == PK_QUAD) {
     const V3 n = xyz(p.a);
     const float denom = dot3(n, r.d);
@@ -906,6 +910,7 @@ __device__ __forceinline__ void finalize_prim(const GpuScene& sc, const GpuPrim&
     s.ray_normal = (-n) * signumf(denom);
     s.front = signbit(denom);
     planar_uv(sc.quad_ext + 9ull * __float_as_uint(p.c.w), xyz(p.c), s.pos, s.u, s.v);
+    if (F & F_EXT) s.pos_l = s.pos - xyz(p.c);  // less the corner (planar/mod.rs:176)
   } else if ((F & F_CYLINDER) && kind == PK_CYLINDER) {
     // cylinder.rs:118-172: the same root, then its normal
     CylHit ch;
@@ -927,6 +932,10 @@ __device__ __forceinline__ void finalize_prim(const GpuScene& sc, const GpuPrim&
     s.front = signbit(inside);
     s.side = ch.face;
     s.u = s.v = 0.0f;
+    if (F & F_EXT) {  // less the centre (cylinder.rs:171)
+      const V3 c = v3(o1.x + along.x / 2.0f, o1.y + along.y / 2.0f, o1.z + along.z / 2.0f);
+      s.pos_l = s.pos - c;
+    }
     if (UV) {  // cylinder.rs:130-172
       const V3 ax = v3(__fdiv_rn(along.x, len), __fdiv_rn(along.y, len), __fdiv_rn(along.z, len));
       V3 o0, o1v;
@@ -952,6 +961,7 @@ __device__ __forceinline__ void finalize_prim(const GpuScene& sc, const GpuPrim&
     s.ray_normal = s.normal;
     s.front = true;
     s.u = s.v = u01(b.w);
+    if (F & F_EXT) s.pos_l = s.pos;  // volumetric.rs:143
   }
 }
 
@@ -967,6 +977,7 @@ __device__ __forceinline__ void finalize_xformed(const GpuScene& sc, const GpuPr
   const float* xf = prim_xform_of(sc, h.prim);
   finalize_prim<F, UV>(sc, p, kind, xf_incoming(xf, rw), h.tl, ctx, s, start);
   s.pos = xf_point(xf + 12, s.pos);
+  s.pos_l = xf_point(xf + 12, s.pos_l);  // the reference maps pos_l as a point too (transform.rs:123)
   s.normal = normalize3(xf_vector(xf + 12, s.normal));
   s.ray_normal = normalize3(xf_vector(xf + 12, s.ray_normal));
 }
@@ -974,12 +985,15 @@ __device__ __forceinline__ void finalize_xformed(const GpuScene& sc, const GpuPr
 // Full hit record of the closest hit. UV: also the texture coordinates that
 // only the Uv render mode reads (sphere, cylinder and infinite-plane uv cost
 // transcendentals or extra fetches; the other kinds compute them anyway).
-template <uint32_t F, bool UV = false>
+template <uint32_t F, bool UV = (F & F_EXT) != 0>
 __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& rw, const HitRec& h, const RngCtx& ctx, Surface& s,
                                              float start) {
   if ((F & (F_SDF | F_PLANE)) && h.sdf >= 0) {
     const GpuSdf& f = sc.sdfs[h.sdf];
     s.pos = at3(rw.o, rw.d, h.t);
+    // pos_l: the raymarched point itself (raymarched.rs:104-105), a plane's
+    // point less its corner (planar/mod.rs:176)
+    if (F & F_EXT) s.pos_l = ((F & F_PLANE) && f.kind == kUnboundedPlane) ? s.pos - v3(f.p1, f.p2, f.p3) : s.pos;
     s.normal = h.sh.n;
     // raymarched.rs:113-114: not flipped; planar/mod.rs:190: -n * signum(denom)
     s.ray_normal = h.sh.flip ? -h.sh.n : h.sh.n;
@@ -1005,7 +1019,7 @@ __device__ __forceinline__ void finalize_hit(const GpuScene& sc, const Ray& rw, 
   const uint32_t kind = prim_kind(p);
   s.material = prim_material(p);
   s.prim_id = prim_id(p);
-  if ((F & F_XFORM) && (__float_as_uint(p.a.w) & kXformBit)) finalize_xformed<F, UV>(sc, p, kind, rw, h, ctx, s, start);
+  if ((F & F_EXT) && (__float_as_uint(p.a.w) & kXformBit)) finalize_xformed<F, UV>(sc, p, kind, rw, h, ctx, s, start);
   else finalize_prim<F, UV>(sc, p, kind, rw, h.t, ctx, s, start);
 }
 
@@ -1020,6 +1034,23 @@ __device__ __forceinline__ C3f sky_colour(uint32_t sky, V3 dir) {
   if (sky == RG_SKY_NONE) return C3f{0.0f, 0.0f, 0.0f};
   float a = 0.5f * dir.y + 0.5f;
   return C3f{1.0f + (0.5f - 1.0f) * a, 1.0f + (0.7f - 1.0f) * a, 1.0f + (1.0f - 1.0f) * a};
+}
+
+}  // namespace rg
+#include "texture.cuh"
+namespace rg {
+
+// The sky of a missed ray: an HdrImageSkybox samples its image at
+// sphere_uv(dir), v flipped (skybox/hdri.rs:17-26).
+template <uint32_t F>
+__device__ __forceinline__ C3f sky_of(const GpuScene& sc, V3 dir) {
+  if ((F & F_EXT) && sc.sky == RG_SKY_IMAGE) {
+    float u, v;
+    sphere_uv(dir, u, v);
+    const GpuImage im = sc.images[sc.sky_image];
+    return image_bilinear(sc, sc.sky_image, u * (float)im.width, (1.0f - v) * (float)im.height);
+  }
+  return sky_colour(sc.sky, dir);
 }
 
 // Material::scatter (material/*.rs) with inverse-CDF samplers of the same
@@ -1081,10 +1112,11 @@ __device__ __forceinline__ bool scatter(const rg_material& m, const Ray& ray, co
 }
 
 // Material::reflected_light as the factor multiplying future_col.
-__device__ __forceinline__ C3f attenuation(const rg_material& m, const Ray& ray, const Surface& s) {
-  C3f alb{m.albedo[0], m.albedo[1], m.albedo[2]};
-  if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) return alb;
+template <uint32_t F>
+__device__ __forceinline__ C3f attenuation(const GpuScene& sc, const rg_material& m, const Ray& ray, const Surface& s) {
   if (m.kind == RG_MAT_DIELECTRIC && s.front) return C3f{1.0f, 1.0f, 1.0f};
+  const C3f alb = material_colour<F>(sc, m, s);
+  if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) return alb;
   float dist = length3(s.pos - ray.o);
   float e = expf(-m.density * dist);
   return C3f{alb.r * e, alb.g * e, alb.b * e};
@@ -1138,7 +1170,7 @@ __device__ C3f mode_sample(const GpuScene& sc, const FrameParams& fp, const Ray&
   ctx.depth = 0;
   HitRec h;
   ++segments;
-  if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) return sky_colour(sc.sky, ray.d);
+  if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) return sky_of<F>(sc, ray.d);
   Surface s;
   finalize_hit<F, true>(sc, ray, h, ctx, s, 1e-3f);
   // The reference's visualisation colours (renderer.rs:439-453)
@@ -1203,14 +1235,15 @@ __device__ C3f branch_sample(const GpuScene& sc, const FrameParams& fp, Ray ray,
     HitRec h;
     ++segments;
     if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
-      const C3f sk = sky_colour(sc.sky, ray.d);
+      const C3f sk = sky_of<F>(sc, ray.d);
       L = C3f{L.r + w.r * sk.r, L.g + w.g * sk.g, L.b + w.b * sk.b};
     } else {
       Surface surf;
       finalize_hit<F>(sc, ray, h, ctx, surf, 1e-3f);
       const rg_material m = sc.materials[surf.material];
       if (m.kind == RG_MAT_LIGHT) {
-        L = C3f{L.r + w.r * m.albedo[0], L.g + w.g * m.albedo[1], L.b + w.b * m.albedo[2]};
+        const C3f e = material_colour<F>(sc, m, surf);
+        L = C3f{L.r + w.r * e.r, L.g + w.g * e.g, L.b + w.b * e.b};
       } else if (depth < fp.ray_depth && top + 1 < kBranchStack) {
         ++top;
         st[top] = Level{surf, ray, w, node, 0u};
@@ -1229,7 +1262,7 @@ __device__ C3f branch_sample(const GpuScene& sc, const FrameParams& fp, Ray ray,
       ctx.depth = lv.node * b + i;
       V3 dir;
       if (!scatter(m, lv.in, lv.surf, ctx, dir)) continue;  // a black branch
-      const C3f a = attenuation(m, lv.in, lv.surf);
+      const C3f a = attenuation<F>(sc, m, lv.in, lv.surf);
       w = C3f{lv.w.r * a.r * inv_b, lv.w.g * a.g * inv_b, lv.w.b * a.b * inv_b};
       ray = make_ray(lv.surf.pos, dir);
       node = lv.node * b + 1u + i;
@@ -1257,7 +1290,7 @@ __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x,
     HitRec h;
     ++segments;
     if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
-      C3f sk = sky_colour(sc.sky, ray.d);
+      C3f sk = sky_of<F>(sc, ray.d);
       L = C3f{L.r + beta.r * sk.r, L.g + beta.g * sk.g, L.b + beta.b * sk.b};
       break;
     }
@@ -1265,12 +1298,13 @@ __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x,
     finalize_hit<F>(sc, ray, h, ctx, surf, 1e-3f);
     const rg_material m = sc.materials[surf.material];
     if (m.kind == RG_MAT_LIGHT) {
-      L = C3f{L.r + beta.r * m.albedo[0], L.g + beta.g * m.albedo[1], L.b + beta.b * m.albedo[2]};
+      const C3f e = material_colour<F>(sc, m, surf);
+      L = C3f{L.r + beta.r * e.r, L.g + beta.g * e.g, L.b + beta.b * e.b};
       break;
     }
     V3 dir;
     if (!scatter(m, ray, surf, ctx, dir)) break;
-    C3f a = attenuation(m, ray, surf);
+    C3f a = attenuation<F>(sc, m, ray, surf);
     beta = C3f{beta.r * a.r, beta.g * a.g, beta.b * a.b};
     ray = make_ray(surf.pos, dir);
   }

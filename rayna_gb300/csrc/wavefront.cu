@@ -133,7 +133,7 @@ __device__ __forceinline__ void record_hit(const GpuScene& sc, const FrameParams
                                              (h.sh.side & 0x3FFFFFFFu)));
     } else {
       mat = prim_material(sc.prims[h.prim]);
-      if ((F & F_XFORM) && sc.prim_xform) s.aux[p].x = h.tl;  // mesh-space distance of a transformed hit
+      if ((F & F_EXT) && sc.prim_xform) s.aux[p].x = h.tl;  // mesh-space distance of a transformed hit
     }
     kind = 1u + sc.materials[mat].kind;
     s.rec[3 * (size_t)p + 1].w = h.t;
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp,
       h.sh.flip = ((f >> 30) & 1u) != 0;
       h.sh.side = f & 0x3FFFFFFFu;
       h.sh.t = h.t;
-    } else if ((F & F_XFORM) && sc.prim_xform && h.prim >= 0) {
+    } else if ((F & F_EXT) && sc.prim_xform && h.prim >= 0) {
       h.tl = s.aux[p].x;
     }
     const bool alive = shade_path<F>(sc, fp, s, p, pix, smp, __float_as_uint(r0.w), r, C3f{r2.x, r2.y, r2.z},

@@ -71,7 +71,7 @@ __device__ __forceinline__ bool shade_path(const GpuScene& sc, const FrameParams
                                            uint32_t pix, uint32_t smp, uint32_t depth, const Ray& r, C3f beta,
                                            bool hit, const HitRec& h) {
   if (!hit) {
-    C3f sk = sky_colour(sc.sky, r.d);
+    C3f sk = sky_of<F>(sc, r.d);
     finish_path(s, p, C3f{0.0f + beta.r * sk.r, 0.0f + beta.g * sk.g, 0.0f + beta.b * sk.b});
     return false;
   }
@@ -80,13 +80,14 @@ __device__ __forceinline__ bool shade_path(const GpuScene& sc, const FrameParams
   finalize_hit<F>(sc, r, h, ctx, surf, 1e-3f);
   const rg_material m = sc.materials[surf.material];
   if (m.kind == RG_MAT_LIGHT) {
-    finish_path(s, p, C3f{0.0f + beta.r * m.albedo[0], 0.0f + beta.g * m.albedo[1], 0.0f + beta.b * m.albedo[2]});
+    const C3f e = material_colour<F>(sc, m, surf);
+    finish_path(s, p, C3f{0.0f + beta.r * e.r, 0.0f + beta.g * e.g, 0.0f + beta.b * e.b});
     return false;
   }
   if (depth < fp.ray_depth) {
     V3 dir;
     if (scatter(m, r, surf, ctx, dir)) {
-      C3f a = attenuation(m, r, surf);
+      C3f a = attenuation<F>(sc, m, r, surf);
       beta = C3f{beta.r * a.r, beta.g * a.g, beta.b * a.b};
       Ray nr = make_ray(surf.pos, dir);
       store_path(s, p, nr.o, depth + 1, nr.d, beta);

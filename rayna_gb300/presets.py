@@ -390,3 +390,68 @@ def single_sphere(albedo, skybox=None):
     from .scene import WhiteSkybox
     return Scene(objects=[SimpleObject(SphereMesh((0.0, 0.0, 0.0), 1.0), LambertianMaterial(tuple(albedo)))],
                  skybox=skybox if skybox is not None else WhiteSkybox())
+
+
+def synthetic_sky(width: int = 128, height: int = 64, seed: int = 0):
+    """An HDR environment image ([x][y][rgb]) standing in for an HDRI file: a
+    horizon gradient, a bright sun disc and seeded low-frequency clouds."""
+    from .scene import Image
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x = (np.arange(width) + 0.5) / width
+    y = (np.arange(height) + 0.5) / height
+    u, v = np.meshgrid(x, y, indexing="ij")        # v = 0 at the image top (the zenith, sphere_uv v = 1)
+    up = 1.0 - v
+    sky = np.stack([0.5 + 0.4 * up, 0.6 + 0.3 * up, 0.9 + 0.1 * up], axis=-1)
+    ground = np.stack([0.25 + 0 * up, 0.2 + 0 * up, 0.15 + 0 * up], axis=-1)
+    img = np.where((up > 0.5)[..., None], sky, ground)
+    cloud = np.zeros_like(u)
+    for k in range(1, 5):
+        ph = rng.uniform(0, 2 * math.pi, 2)
+        cloud += np.sin(2 * math.pi * k * u + ph[0]) * np.sin(math.pi * k * up + ph[1]) / k
+    img = img + 0.15 * np.clip(cloud, 0, None)[..., None] * (up > 0.5)[..., None]
+    su, sv = 0.3, 0.25                              # the sun
+    d2 = ((u - su) * 2) ** 2 + (v - sv) ** 2
+    img = img + (20.0 * np.exp(-d2 / 0.0008))[..., None]
+    return Image(img.astype(np.float32))
+
+
+def textures_demo(width: int = 320, height: int = 180, spp: int = 32, ray_depth: int = 16, seed: int = 0):
+    """Returns (scene, camera, opts) exercising every texture kind and the
+    image sky: a world-checker ground, an image-textured sphere, a world-noise
+    sphere (the reference's RTTNW noise sphere: Perlin(69) scaled by 4), a
+    rotated box with local RGB noise, a metal sphere with a uv checker, a
+    uv-noise parallelogram light, under an HdrImageSkybox."""
+    from .scene import (
+        ColourSource, HdrImageSkybox, Image, ImageTexture, LocalNoiseTexture, ParallelogramMesh, Perlin, Planar,
+        ScalePoint, Transform3, UvCheckerTexture, UvNoiseTexture, WorldCheckerTexture, WorldNoiseTexture,
+    )
+    rng = np.random.Generator(np.random.PCG64(seed))
+    # a 64 x 32 "planet" image: latitude bands and seeded blotches
+    u, v = np.meshgrid((np.arange(64) + 0.5) / 64, (np.arange(32) + 0.5) / 32, indexing="ij")
+    planet = np.stack([0.2 + 0.6 * v, 0.3 + 0.4 * np.abs(np.sin(6 * math.pi * v)), 0.8 - 0.5 * v], axis=-1)
+    for _ in range(12):
+        cu, cv, r = rng.uniform(0, 1), rng.uniform(0.1, 0.9), rng.uniform(0.03, 0.1)
+        planet[((u - cu) ** 2 + (v - cv) ** 2) < r * r] = rng.uniform(0.2, 0.9, 3)
+    planet_img = Image(planet.astype(np.float32))
+    Y = (0.0, 1.0, 0.0)
+    objs = [
+        SimpleObject(ParallelogramMesh(Planar.new((-50, 0, -50), (100, 0, 0), (0, 0, 100))),
+                     # offset half a cell in y: the ground plane then lies inside a cell, not on the cell
+                     # boundary y = 0, where the parity would follow the sign of the hit point's rounding
+                     LambertianMaterial(WorldCheckerTexture(even=(0.2, 0.3, 0.1), odd=(0.9, 0.9, 0.9), scale=1.0,
+                                                            offset=(0.0, 0.5, 0.0)))),
+        SimpleObject(SphereMesh((0.0, 1.0, 0.0), 1.0), LambertianMaterial(ImageTexture(planet_img))),
+        SimpleObject(SphereMesh((-2.4, 1.0, 0.6), 1.0),
+                     LambertianMaterial(WorldNoiseTexture(ColourSource.Greyscale(ScalePoint(Perlin(69)).set_scale(4.0))))),
+        SimpleObject(AxisBoxMesh((1.8, 0.0, -0.6), (3.0, 1.2, 0.6)),
+                     LambertianMaterial(LocalNoiseTexture(ColourSource.Rgb(
+                         [ScalePoint(Perlin(5 + i)).set_scale(3.0) for i in range(3)]))),
+                     Transform3.from_axis_angle(Y, Angle.from_degrees(30.0))),
+        SimpleObject(SphereMesh((1.2, 0.5, 2.0), 0.5),
+                     MetalMaterial(UvCheckerTexture(even=(0.9, 0.8, 0.3), odd=(0.5, 0.5, 0.6), scale=0.125), 0.05)),
+        SimpleObject(ParallelogramMesh(Planar.new((-1.0, 3.5, -1.0), (2.0, 0, 0), (0, 0, 2.0))),
+                     LightMaterial(UvNoiseTexture(ColourSource.Greyscale(ScalePoint(Perlin(11)).set_scale(6.0))))),
+    ]
+    scene = Scene(objects=objs, skybox=HdrImageSkybox(synthetic_sky(seed=seed)))
+    cam = look_at_camera((0.0, 2.2, 8.0), (0.0, 0.8, 0.0), 40.0)
+    return scene, cam, RenderOpts(width=width, height=height, samples=spp, ray_depth=ray_depth)

@@ -263,12 +263,166 @@ class SolidTexture:
     albedo: tuple = (0.0, 0.0, 0.0)
 
 
+class Image:
+    """core/image.rs: an RGB f32 image indexed [x][y] (an ndarray of shape
+    (width, height)); ``data`` has shape (width, height, 3)."""
+
+    def __init__(self, data):
+        a = np.ascontiguousarray(data, dtype=np.float32)
+        if a.ndim != 3 or a.shape[2] != 3 or a.shape[0] == 0 or a.shape[1] == 0:
+            raise ValueError(f"an Image is (width, height, 3), got shape {a.shape}")
+        self.data = a
+
+    @property
+    def width(self) -> int:
+        return self.data.shape[0]
+
+    @property
+    def height(self) -> int:
+        return self.data.shape[1]
+
+    @staticmethod
+    def new_filled(width: int, height: int, fill) -> "Image":
+        return Image(np.broadcast_to(np.asarray(_vec3(fill), np.float32), (width, height, 3)))
+
+    @staticmethod
+    def from_fn(width: int, height: int, func) -> "Image":
+        return Image(np.array([[_vec3(func(x, y)) for y in range(height)] for x in range(width)], np.float32))
+
+    def get_bilinear(self, px: float, py: float) -> np.ndarray:
+        """Image::get_bilinear (core/image.rs:87-109), in f64."""
+        def coords(val, n):
+            fl = min(max(math.floor(val), 0), n - 1) if not math.isnan(val) else 0
+            ce = min(max(math.ceil(val), 0), n - 1) if not math.isnan(val) else 0
+            return int(fl), int(ce), val - fl
+        x1, x2, xl = coords(px, self.width)
+        y1, y2, yl = coords(py, self.height)
+        d = self.data.astype(np.float64)
+        lerp = lambda a, b, t: a + (b - a) * t
+        return lerp(lerp(d[x1, y1], d[x2, y1], xl), lerp(d[x1, y2], d[x2, y2], xl), yl)
+
+
+@dataclass(eq=False)
+class WorldCheckerTexture:
+    """texture/checker.rs:20-27: cells of `scale` in world space, shifted by `offset`."""
+    even: Any
+    odd: Any
+    scale: float = 1.0
+    offset: tuple = (0.0, 0.0, 0.0)
+
+
+@dataclass(eq=False)
+class UvCheckerTexture:
+    """texture/checker.rs:37-44: cells of `scale` in uv, shifted by `offset`."""
+    even: Any
+    odd: Any
+    scale: float = 1.0
+    offset: tuple = (0.0, 0.0)
+
+
+@dataclass(eq=False)
+class ImageTexture:
+    """texture/image.rs:29-39: the image at offset + uv * scale, v flipped, bilinear."""
+    image: Image
+    scale: tuple = (1.0, 1.0)
+    offset: tuple = (0.0, 0.0)
+
+
+@dataclass(eq=False)
+class DynamicTexture:
+    """texture/dynamic.rs: a shared texture; flattened to its inner texture."""
+    inner: Any
+
+
+@dataclass(frozen=True)
+class Perlin:
+    """noise::Perlin::new(seed): gradient noise. The GPU path evaluates Perlin's
+    improved noise over its own seeded permutation, not the noise crate's."""
+    seed: int = 0
+
+
+class ScalePoint:
+    """noise::ScalePoint: the source evaluated at the point times `scale`."""
+
+    def __init__(self, source, scale=(1.0, 1.0, 1.0)):
+        self.source = source
+        self.scale = _vec3(scale)
+
+    def set_scale(self, s: float) -> "ScalePoint":
+        self.scale = (float(s),) * 3
+        return self
+
+
+class ColourSource:
+    """texture/noise.rs ColourSource: Greyscale(noise) or Rgb([r, g, b])."""
+
+    def __init__(self, kind: str, sources):
+        self.kind, self.sources = kind, list(sources)
+
+    @staticmethod
+    def Greyscale(noise) -> "ColourSource":  # noqa: N802 (the reference's variant name)
+        return ColourSource("greyscale", [noise])
+
+    @staticmethod
+    def Rgb(noises) -> "ColourSource":  # noqa: N802
+        return ColourSource("rgb", noises)
+
+    def to_dyn_box(self) -> "ColourSource":
+        return self
+
+
+@dataclass(eq=False)
+class WorldNoiseTexture:
+    source: ColourSource
+
+
+@dataclass(eq=False)
+class LocalNoiseTexture:
+    source: ColourSource
+
+
+@dataclass(eq=False)
+class UvNoiseTexture:
+    source: ColourSource
+
+
+def _noise_params(src: ColourSource) -> tuple:
+    """(seed, channels, scale) of a Perlin ColourSource: each source is
+    Perlin(seed) or ScalePoint(Perlin(seed)) with one scale on all axes; the
+    channels of an Rgb source must be seeded seed, seed + 1, seed + 2 and share
+    the scale."""
+    if not isinstance(src, ColourSource) or src.kind not in ("greyscale", "rgb"):
+        raise UnsupportedVariant("noise textures take ColourSource.Greyscale or ColourSource.Rgb")
+    parsed = []
+    for n in src.sources:
+        scale = 1.0
+        if isinstance(n, ScalePoint):
+            if len(set(n.scale)) != 1:
+                raise UnsupportedVariant("ScalePoint needs one scale on every axis")
+            scale, n = n.scale[0], n.source
+        if not isinstance(n, Perlin):
+            raise UnsupportedVariant(f"noise source {type(n).__name__} is not supported (Perlin only)")
+        parsed.append((int(n.seed), scale))
+    if src.kind == "rgb":
+        if len(parsed) != 3 or any(p[0] != parsed[0][0] + i or p[1] != parsed[0][1] for i, p in enumerate(parsed)):
+            raise UnsupportedVariant("Rgb noise must be three Perlin sources seeded s, s + 1, s + 2 with one scale")
+    return parsed[0][0], len(parsed), parsed[0][1]
+
+
+def _is_solid(tex) -> bool:
+    while isinstance(tex, DynamicTexture):
+        tex = tex.inner
+    return isinstance(tex, (SolidTexture, tuple, list, np.ndarray))
+
+
 def _colour(tex) -> tuple:
+    while isinstance(tex, DynamicTexture):
+        tex = tex.inner
     if isinstance(tex, SolidTexture):
         return _vec3(tex.albedo)
     if isinstance(tex, (tuple, list, np.ndarray)):
         return _vec3(tex)
-    raise UnsupportedVariant(f"only SolidTexture albedos cross the C ABI, got {type(tex).__name__}")
+    raise UnsupportedVariant(f"texture {type(tex).__name__} cannot cross the C ABI")
 
 
 @dataclass(eq=False)
@@ -300,27 +454,38 @@ class LightMaterial:
     emissive: Any
 
 
-def material_record(m) -> A.rg_material:
+def material_record(m, texture_index=None) -> A.rg_material:
+    """The rg_material of `m`. A non-solid texture is registered through
+    `texture_index(tex) -> int` (its position in the scene's texture table)."""
     r = A.rg_material()
+
+    def colour(tex):
+        if _is_solid(tex):
+            r.albedo[:] = _colour(tex)
+        elif texture_index is None:
+            raise UnsupportedVariant(f"texture {type(tex).__name__} needs a scene texture table")
+        else:
+            r.texture = texture_index(tex) + 1
+
     if isinstance(m, LambertianMaterial):
         r.kind = A.RG_MAT_LAMBERTIAN
-        r.albedo[:] = _colour(m.albedo)
+        colour(m.albedo)
     elif isinstance(m, MetalMaterial):
         r.kind = A.RG_MAT_METAL
-        r.albedo[:] = _colour(m.albedo)
+        colour(m.albedo)
         r.fuzz = float(m.fuzz)
     elif isinstance(m, DielectricMaterial):
         r.kind = A.RG_MAT_DIELECTRIC
-        r.albedo[:] = _colour(m.albedo)
+        colour(m.albedo)
         r.refractive_index = float(m.refractive_index)
         r.density = float(m.density)
     elif isinstance(m, IsotropicMaterial):
         r.kind = A.RG_MAT_ISOTROPIC
-        r.albedo[:] = _colour(m.albedo)
+        colour(m.albedo)
         r.density = float(m.density)
     elif isinstance(m, LightMaterial):
         r.kind = A.RG_MAT_LIGHT
-        r.albedo[:] = _colour(m.emissive)
+        colour(m.emissive)
     else:
         raise UnsupportedVariant(f"material {type(m).__name__} cannot cross the C ABI")
     return r
@@ -339,6 +504,14 @@ class WhiteSkybox:
 
 class NoSkybox:
     kind = A.RG_SKY_NONE
+
+
+class HdrImageSkybox:
+    """skybox/hdri.rs:17-26: the image sampled at sphere_uv(dir), v flipped."""
+    kind = A.RG_SKY_IMAGE
+
+    def __init__(self, image: Image):
+        self.image = image if isinstance(image, Image) else Image(image)
 
 
 # ---------------------------------------------------------------------------
@@ -602,6 +775,11 @@ class FlatScene:
     def __init__(self):
         self.materials: list = []
         self._mat_index: dict = {}
+        self.textures: list = []
+        self._tex_index: dict = {}
+        self.images: list = []
+        self._img_index: dict = {}
+        self.sky_image = 0
         self.spheres, self.sphere_mat = [], []
         self.tri_v, self.tri_n, self.tri_mat, self.tri_mesh = [], [], [], []
         self.boxes, self.box_mat = [], []
@@ -620,8 +798,58 @@ class FlatScene:
         k = id(m)
         if k not in self._mat_index:
             self._mat_index[k] = (len(self.materials), m)
-            self.materials.append(material_record(m))
+            self.materials.append(material_record(m, self.texture))
         return self._mat_index[k][0]
+
+    def image(self, img: Image) -> int:
+        k = id(img)
+        if k not in self._img_index:
+            self._img_index[k] = (len(self.images), img)
+            self.images.append(img)
+        return self._img_index[k][0]
+
+    def texture(self, tex) -> int:
+        """Index of `tex` in the texture table (registered on first use, its
+        checker cells first)."""
+        while isinstance(tex, DynamicTexture):
+            tex = tex.inner
+        k = id(tex)
+        if k in self._tex_index:
+            idx = self._tex_index[k][0]
+            if idx < 0:
+                raise ValueError("a checker texture contains itself")
+            return idx
+        self._tex_index[k] = (-1, tex)
+        t = A.rg_texture()
+        if _is_solid(tex):
+            t.kind = A.RG_TEX_SOLID
+            t.colour[:] = _colour(tex)
+        elif isinstance(tex, (WorldCheckerTexture, UvCheckerTexture)):
+            world = isinstance(tex, WorldCheckerTexture)
+            t.kind = A.RG_TEX_WORLD_CHECKER if world else A.RG_TEX_UV_CHECKER
+            t.odd, t.even = self.texture(tex.odd), self.texture(tex.even)
+            t.scale[0] = float(tex.scale)
+            off = _vec3(tex.offset) if world else tuple(float(x) for x in tex.offset) + (0.0,)
+            if len(off) != 3:
+                raise ValueError(f"a checker offset has {2 if not world else 3} components")
+            t.offset[:] = off
+        elif isinstance(tex, ImageTexture):
+            t.kind = A.RG_TEX_IMAGE
+            t.image = self.image(tex.image)
+            t.scale[:] = tuple(float(x) for x in tex.scale)
+            t.offset[:] = (float(tex.offset[0]), float(tex.offset[1]), 0.0)
+        elif isinstance(tex, (WorldNoiseTexture, LocalNoiseTexture, UvNoiseTexture)):
+            t.kind = A.RG_TEX_NOISE
+            t.noise_seed, t.noise_channels, scale = _noise_params(tex.source)
+            t.scale[0] = float(scale)
+            t.noise_place = {WorldNoiseTexture: A.RG_NOISE_WORLD, LocalNoiseTexture: A.RG_NOISE_LOCAL,
+                             UvNoiseTexture: A.RG_NOISE_UV}[type(tex)]
+        else:
+            raise UnsupportedVariant(f"texture {type(tex).__name__} cannot cross the C ABI")
+        idx = len(self.textures)
+        self.textures.append(t)
+        self._tex_index[k] = (idx, tex)
+        return idx
 
     def add(self, obj):
         if isinstance(obj, (list, tuple, ObjectList)):
@@ -754,6 +982,11 @@ class FlatScene:
         self.c_volumes = (A.rg_volume * max(1, len(self.volumes)))(*self.volumes)
         self.c_sdfs = (A.rg_sdf * max(1, len(self.sdfs)))(*self.sdfs)
         self.c_materials = (A.rg_material * max(1, len(self.materials)))(*self.materials)
+        self.c_textures = (A.rg_texture * max(1, len(self.textures)))(*self.textures)
+        self.c_images = (A.rg_image * max(1, len(self.images)))()
+        for i, img in enumerate(self.images):
+            self.c_images[i].width, self.c_images[i].height = img.width, img.height
+            self.c_images[i].rgb = img.data.ctypes.data_as(C.POINTER(C.c_float))
         d = A.rg_scene_desc()
         fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
         up = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint32))
@@ -771,6 +1004,9 @@ class FlatScene:
         d.n_cylinders, d.cylinders, d.cylinder_material = len(self.a_cyls), fp(self.a_cyls), up(self.a_cyl_mat)
         d.n_planes, d.planes, d.plane_material = len(self.a_planes), fp(self.a_planes), up(self.a_plane_mat)
         d.plane_uv_wrap = up(self.a_plane_wrap)
+        d.n_textures, d.textures = len(self.textures), self.c_textures
+        d.n_images, d.images = len(self.images), self.c_images
+        d.sky_image = self.sky_image
         if len(self.a_transforms):
             d.n_transforms = len(self.a_transforms)
             d.transforms = self.a_transforms.ctypes.data_as(C.POINTER(C.c_double))
@@ -798,5 +1034,7 @@ def flatten(scene: Scene) -> FlatScene:
     if not hasattr(sky, "kind"):
         raise UnsupportedVariant(f"skybox {type(sky).__name__} cannot cross the C ABI")
     fs.skybox = sky.kind
+    if isinstance(sky, HdrImageSkybox):
+        fs.sky_image = fs.image(sky.image)
     fs.add(scene.objects)
     return fs.finish()

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
     for s in syms:
         assert hasattr(lib, s), s
     assert set(syms) == set(A.SIGNATURES), "ctypes signatures must cover the header exactly"
-    assert lib.rg_abi_version() == 5
+    assert lib.rg_abi_version() == 6
 
 
 def test_struct_sizes_match_header_layout():

@@ -84,3 +84,15 @@ def test_backward_with_adjoint_image_and_parameter_updates():
         g2 = r.backward(5, adjoint=ones)
         assert g2["density"].shape == (dens,)
         assert np.isfinite(g2["density"]).all()
+
+
+def test_backward_rejects_textures():
+    """The adjoint differentiates solid albedos: a textured scene or an image
+    sky is refused with RG_UNSUPPORTED_VARIANT."""
+    from rayna_gb300._abi import RaynaError
+    scene, cam, _ = presets.textures_demo()
+    opts = RenderOpts(width=16, height=9, samples=2, ray_depth=4)
+    with Renderer.new_from(scene, cam, opts, 0) as r:
+        with pytest.raises(RaynaError) as e:
+            r.backward(seed=1, adjoint=np.ones((16, 9, 3), np.float32))
+        assert e.value.status == 2

@@ -85,3 +85,21 @@ def test_batch_with_transformed_objects():
         with Renderer.new_from(scene, cam, items[0][2], 0) as r:
             ref = r.render(seed=key).img
         np.testing.assert_array_equal(img, ref)
+
+
+def test_batch_with_textures_and_image_sky():
+    """A textured scene under an image sky in both batched forms renders what
+    a standalone renderer renders with the same frame keys."""
+    from rayna_gb300.scene import RenderOpts
+    scene, cam, _ = presets.textures_demo()
+    items = [(scene, cam, RenderOpts(width=48, height=27, samples=8, ray_depth=6))] + small_batch()[:2]
+    for form in ("wavefront", "tiles"):
+        with BatchRenderer(items) as b:
+            b.set_tuning(form=form)
+            st = b.render(seed=23)
+            assert st.error_flags == 0
+            img = b.image(0)
+            key = b.item_seed(23, 0)
+        with Renderer.new_from(scene, cam, items[0][2], 0) as r:
+            ref = r.render(seed=key).img
+        np.testing.assert_array_equal(img, ref)

@@ -44,6 +44,7 @@ CASES = {
     "sdf_volumes": lambda: small(presets.sdf_volumes, 64, 36, 16, 16, n_spheres=30),
     "cornell_quads": lambda: small(presets.cornell_quads, 48, 48, 16, 8),
     "cornell": lambda: small(presets.cornell, 48, 48, 16, 8),  # the preset's rotated boxes
+    "textures": lambda: small(presets.textures_demo, 64, 36, 16, 8),  # every texture kind, image sky
 }
 
 
@@ -62,14 +63,15 @@ def test_path_by_path_parity_with_f32_oracle(case):
     frac = close.mean()
     print(f"{case}: {frac:.4f} of pixels match the f32 oracle path for path")
     assert frac >= {"random_spheres": 0.97, "cornell_mesh": 0.97, "sdf_volumes": 0.9, "cornell_quads": 0.97,
-                    "cornell": 0.97}[case]
+                    "cornell": 0.97, "textures": 0.97}[case]
 
 
 @pytest.mark.parametrize("case", list(CASES))
 def test_statistical_parity_with_f64_oracle(case):
     scene, cam, opts = CASES[case]()
     flat = flatten(scene)
-    frames = {"random_spheres": 24, "cornell_mesh": 48, "sdf_volumes": 32, "cornell_quads": 48, "cornell": 48}[case]
+    frames = {"random_spheres": 24, "cornell_mesh": 48, "sdf_volumes": 32, "cornell_quads": 48, "cornell": 48,
+              "textures": 32}[case]
     spp = opts.samples
     sq = 0.0
     with Renderer.new_from(scene, cam, opts, 0, seed=7) as r:
@@ -157,6 +159,7 @@ def test_oversized_branching_and_zero_sizes_are_rejected():
 MODE_CASES = {
     "planar": lambda: small(presets.cornell_quads, 40, 40, 4, 8),
     "transformed": lambda: small(presets.cornell, 40, 40, 4, 8),
+    "textures": lambda: small(presets.textures_demo, 48, 27, 4, 8),
     "spheres": lambda: small(presets.random_spheres, 48, 27, 4, 8),
     "sdf_volumes": lambda: small(presets.sdf_volumes, 48, 27, 4, 8, n_spheres=20),
 }
