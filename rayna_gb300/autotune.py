@@ -27,10 +27,10 @@ from . import _abi as A
 
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_cache.json")
 
-WAVE_PATHS = [1 << 22, 1 << 23]
+WAVE_PATHS = [1 << 23, 1 << 24, 1 << 25]
 FETCH_BUDGETS = [4, 8, 16]
 BVH_WIDTHS = [2, 8]
-BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 22, 1 << 23)] +
+BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 23, 1 << 24, 1 << 25)] +
                 [dict(form="tiles", block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)])
 
 

@@ -694,7 +694,12 @@ cudaError_t stage_mark(rg_renderer* h) {
 
 bool effective_sort(const rg_renderer* h) {
   if (h->wf_sort) return h->wf_sort == 1;
-  return h->kinds != F_SPHERE;
+  return h->host.nsdf > 0 || h->host.nv > 0;
+}
+
+uint32_t effective_budget(const rg_renderer* h) {
+  if (h->wf_budget) return h->wf_budget;
+  return h->kinds == F_SPHERE ? kDefaultFetchBudgetSpheres : kDefaultFetchBudget;
 }
 
 void apply_features(rg_renderer* h) {
@@ -968,7 +973,7 @@ rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
   std::memset(out, 0, sizeof(*out));
   out->wave_paths = (uint32_t)(h->wf_paths ? h->wf_paths : kDefaultWavePaths);
   out->sort_materials = effective_sort(h) ? 1u : 2u;
-  out->fetch_budget = h->wf_budget ? h->wf_budget : kDefaultFetchBudget;
+  out->fetch_budget = effective_budget(h);
   out->bvh_width = effective_bvh_width(h->bvh_width, h->gs, h->form);
   return RG_OK;
 }

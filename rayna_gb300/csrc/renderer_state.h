@@ -122,9 +122,15 @@ namespace rg {
 // every form measured faster on the binary tree.
 constexpr uint32_t kDefaultBvhWidthWavefront = 2;
 constexpr uint32_t kDefaultBvhWidthMegakernel = 2;
+// Node visits between refills of the persistent traversal kernels: 8, or 6
+// for scenes of spheres only (measured best of 4-16 on the mesh, SDF and
+// sphere workloads).
 constexpr uint32_t kDefaultFetchBudget = 8;
-// Default path slots per wave (about 0.9 GB of path state).
-constexpr size_t kDefaultWavePaths = size_t(1) << 23;
+constexpr uint32_t kDefaultFetchBudgetSpheres = 6;
+// Default path slots per wave (about 3.6 GB of path state; clamped to the
+// frame). Larger waves keep more rays in flight at the tail of each bounce:
+// 2^25 measured 1.18x 2^23 on the SDF workload and 1.03x on the mesh.
+constexpr size_t kDefaultWavePaths = size_t(1) << 25;
 
 // Defined in renderer.cpp
 // RG_FLAG_STAGE_TIMES: records the next event of the frame's traversal timing
@@ -133,9 +139,14 @@ cudaError_t stage_mark(rg_renderer* h);
 // Traversal width in effect for a request (0 = default) on a scene.
 uint32_t effective_bvh_width(uint32_t requested, const GpuScene& g, uint32_t form);
 // Whether the wavefront shades in material-kind order: as requested, else
-// fused for scenes of spheres only (short traversals, where the extra pass
-// costs more than it saves) and sorted otherwise.
+// sorted for scenes with SDFs or media (whose marching and free-flight work
+// diverges inside one fused kernel) and fused otherwise (measured: SDF
+// workload 318 sorted vs 134 fused Msamples/s; mesh 543 vs 569; spheres 878
+// vs 1143).
 bool effective_sort(const rg_renderer* h);
+// Node visits between refills of the persistent kernels: as requested, else
+// the default for the scene's kinds.
+uint32_t effective_budget(const rg_renderer* h);
 // Kernel variant bits: the scene's primitive kinds, plus F_WIDE when the
 // handle traverses the 8-wide tree.
 void apply_features(rg_renderer* h);

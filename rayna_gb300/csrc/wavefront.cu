@@ -272,7 +272,7 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
   const bool sorted = effective_sort(h);
   const bool timed = (h->flags & RG_FLAG_STAGE_TIMES) != 0;
-  const int budget = (int)(h->wf_budget ? h->wf_budget : kDefaultFetchBudget);
+  const int budget = (int)effective_budget(h);
   const int grid = sm_count(h->device) * 8;
   // The persistent traversal kernels run as many blocks as are resident at once.
   int ext_per_sm = 0;
