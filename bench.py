@@ -251,10 +251,12 @@ def run_reference(args, rank, world):
 
 # DRAM bytes (read + write) per ray segment of the traversal kernels, from an
 # ncu capture of every traversal launch of one frame (profiles/), by
-# (workload, form, BVH width); scaled to a frame by its ray segments.
+# (workload, timed form); scaled to a frame by its ray segments.
 DRAM_BYTES_PER_SEGMENT = {
     # 18 k_extend launches of one 512x512x64 frame: 20.76 GB over 86.67 M segments
-    ("mesh", "wavefront", 2): 239.5,
+    ("mesh", "wavefront_sorted"): 239.5,
+    # 9 fused k_bounce launches of one 512x512x64 frame: 22.44 GB over 86.67 M segments
+    ("mesh", "wavefront"): 258.9,
 }
 
 # Kernel configurations timed per workload: (form, material-sorted shading,
@@ -383,7 +385,7 @@ def run_gpu(args, rank, world):
     node_bytes = 80 if b["bvh_width"] == 8 else 64
     alg_bytes = node_bytes * b["node_visits"] + 48 * b["prim_tests"] + 48 * b["rays_per_frame"]
     achieved = alg_bytes / (b["traverse_ms_per_step"] / 1e3) / 1e9
-    dram_per_segment = DRAM_BYTES_PER_SEGMENT.get((args.workload, FORMS[best][0], FORMS[best][2]))
+    dram_per_segment = DRAM_BYTES_PER_SEGMENT.get((args.workload, best))
     traffic = dram_per_segment * b["rays_per_frame"] if dram_per_segment else None
     line = {
         "metric": "Msamples/s", "value": b["msamples_s"], "unit": "Msamples/s", "n_gpus": world,
