@@ -271,7 +271,10 @@ typedef struct rg_device_opts {
 
 enum {
     RG_FLAG_COUNTERS = 1u,     /* maintain device work counters (node visits, tests) for the roofline */
-    RG_FLAG_STAGE_TIMES = 2u   /* time the traversal kernels of each frame with CUDA events (traverse_ms) */
+    RG_FLAG_STAGE_TIMES = 2u,  /* time the traversal kernels of each frame with CUDA events (traverse_ms) */
+    RG_FLAG_VALIDATE = 4u      /* check every closest hit and path colour against shared/validate.rs's invariants
+                                  (counted in invalid_hits / invalid_mask; implies RG_FLAG_COUNTERS; the wavefront
+                                  then shades fused) */
 };
 
 /* RenderStats (render/render.rs:4-15) plus device figures. */
@@ -291,7 +294,20 @@ typedef struct rg_render_stats {
     uint32_t kernel_launches; /* kernels the library launched for this frame */
     double traverse_ms;       /* device time of the frame's traversal kernels (RG_FLAG_STAGE_TIMES only, else 0):
                                  the megakernel, or the wavefront's extend / bounce launches */
+    uint64_t invalid_hits;    /* RG_FLAG_VALIDATE: hits or path colours that broke an invariant this frame */
+    uint32_t invalid_mask;    /* RG_FLAG_VALIDATE: RG_INVALID_* bits of the invariants broken */
+    uint32_t reserved0;
 } rg_render_stats;
+
+/* Invariants of RG_FLAG_VALIDATE (shared/validate.rs:21-197). */
+enum {
+    RG_INVALID_NONFINITE = 1u,       /* hit distance, point or a normal not finite */
+    RG_INVALID_NOT_NORMALISED = 2u,  /* |normal|^2 or |ray_normal|^2 off 1 by more than 2e-3 (length 1e-3 relative) */
+    RG_INVALID_INTERVAL = 4u,        /* hit distance outside the query interval */
+    RG_INVALID_POSITION = 8u,        /* the point is not at the distance along the ray (1e-6 abs or 1e-3 rel) */
+    RG_INVALID_UV = 16u,             /* uv outside [0, 1]^2 or NaN */
+    RG_INVALID_COLOUR = 32u          /* a path's colour channel negative or not finite */
+};
 
 /* Hit record of rg_query_rays. */
 typedef struct rg_hit {

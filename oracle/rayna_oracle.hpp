@@ -254,21 +254,33 @@ template <class P> struct Sphere {
   // SphereMesh::intersect (sphere.rs:44-99)
   bool intersect(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
     V3<T> oc = ray.pos - c;
-    T half_b, cc, disc;
+    T root, far_root;
     if constexpr (P::gpu) {
-      half_b = Math<P>::dot(oc, ray.dir);
-      cc = std::fma(oc.x, oc.x, std::fma(oc.y, oc.y, std::fma(oc.z, oc.z, -r2)));
-      disc = std::fma(half_b, half_b, -cc);
+      // the device's form: disc = r^2 - |oc - half_b d|^2, roots q and c / q
+      // (trace.cuh sphere_t; Ray Tracing Gems 2019, "Precision Improvements
+      // for Ray/Sphere Intersection")
+      const T half_b = Math<P>::dot(oc, ray.dir);
+      const V3<T> l{std::fma(-half_b, ray.dir.x, oc.x), std::fma(-half_b, ray.dir.y, oc.y),
+                    std::fma(-half_b, ray.dir.z, oc.z)};
+      const T disc = r2 - Math<P>::dot(l, l);
+      if (disc < T(0)) return false;
+      const T cc = std::fma(oc.x, oc.x, std::fma(oc.y, oc.y, std::fma(oc.z, oc.z, -r2)));
+      const T sq = std::sqrt(disc);
+      const T q = half_b > T(0) ? -half_b - sq : -half_b + sq;
+      const T other = q != T(0) ? cc / q : q;
+      root = std::fmin(q, other);
+      far_root = std::fmax(q, other);
     } else {
-      half_b = Math<P>::dot(oc, ray.dir);
-      cc = Math<P>::dot(oc, oc) - r2;
-      disc = (half_b * half_b) - cc;
+      const T half_b = Math<P>::dot(oc, ray.dir);
+      const T cc = Math<P>::dot(oc, oc) - r2;
+      const T disc = (half_b * half_b) - cc;
+      if (disc < T(0)) return false;
+      const T sq = std::sqrt(disc);
+      root = -half_b - sq;
+      far_root = -half_b + sq;
     }
-    if (disc < T(0)) return false;
-    T sq = std::sqrt(disc);
-    T root = -half_b - sq;
     if (!iv.contains(root)) {
-      root = -half_b + sq;
+      root = far_root;
       if (!iv.contains(root)) return false;
     }
     h.dist = root;

@@ -40,6 +40,9 @@ RG_SDF_SPHERE, RG_SDF_TORUS, RG_SDF_MANDELBULB = range(3)
 RG_FORM_MEGAKERNEL, RG_FORM_WAVEFRONT = range(2)
 RG_FLAG_COUNTERS = 1
 RG_FLAG_STAGE_TIMES = 2
+RG_FLAG_VALIDATE = 4
+(RG_INVALID_NONFINITE, RG_INVALID_NOT_NORMALISED, RG_INVALID_INTERVAL, RG_INVALID_POSITION, RG_INVALID_UV,
+ RG_INVALID_COLOUR) = (1, 2, 4, 8, 16, 32)
 RG_BATCH_WAVEFRONT = 0
 RG_UV_WRAP, RG_UV_MIRROR, RG_UV_CLAMP_ZERO = 0, 1, 2
 RG_NO_TRANSFORM = 0xFFFFFFFF
@@ -115,7 +118,8 @@ class rg_render_stats(C.Structure):
                 ("rays", C.c_uint64), ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64),
                 ("sdf_steps", C.c_uint64), ("accum_frames", C.c_uint32), ("img_width", C.c_uint32),
                 ("img_height", C.c_uint32), ("num_threads", C.c_uint32), ("error_flags", C.c_uint32),
-                ("kernel_launches", C.c_uint32), ("traverse_ms", C.c_double)]
+                ("kernel_launches", C.c_uint32), ("traverse_ms", C.c_double), ("invalid_hits", C.c_uint64),
+                ("invalid_mask", C.c_uint32), ("reserved0", C.c_uint32)]
 
 
 class rg_scene_info(C.Structure):

@@ -209,7 +209,11 @@ enum : uint32_t {
 };
 
 // Counters (RG_FLAG_COUNTERS): indices into the u64 counter array.
-enum : uint32_t { CNT_RAYS = 0, CNT_NODES = 1, CNT_PRIMS = 2, CNT_SDF = 3, CNT_SAMPLES = 4, CNT_N = 8 };
+enum : uint32_t {
+  CNT_RAYS = 0, CNT_NODES = 1, CNT_PRIMS = 2, CNT_SDF = 3, CNT_SAMPLES = 4,
+  CNT_INVALID = 5, CNT_INVALID_MASK = 6,  // RG_FLAG_VALIDATE: broken invariants, and which (RG_INVALID_*)
+  CNT_N = 8
+};
 
 // Per-frame launch parameters (all f32 values rounded from the f64 host viewport).
 struct FrameParams {
@@ -227,6 +231,7 @@ struct FrameParams {
   float* frame_var;       // [x][y][rgb] this frame's sample variance (may be null)
   unsigned long long* counters;
   uint32_t* err;
+  uint32_t validate;      // RG_FLAG_VALIDATE: the counting kernel variants check hits and colours
 };
 
 }  // namespace rg

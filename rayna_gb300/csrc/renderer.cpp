@@ -693,6 +693,7 @@ cudaError_t stage_mark(rg_renderer* h) {
 }
 
 bool effective_sort(const rg_renderer* h) {
+  if (h->flags & RG_FLAG_VALIDATE) return false;  // the fused bounce kernel carries the checks
   if (h->wf_sort) return h->wf_sort == 1;
   return h->host.nsdf > 0 || h->host.nv > 0;
 }
@@ -758,6 +759,7 @@ void fill_frame_params(rg_renderer* h, uint64_t seed, FrameParams& fp) {
   fp.frame_mean = h->d_fmean;
   fp.frame_var = h->d_fvar;
   fp.counters = h->d_counters;
+  fp.validate = (h->flags & RG_FLAG_VALIDATE) ? 1u : 0u;
   fp.err = h->d_err;
 }
 
@@ -788,6 +790,7 @@ rg_status rg_create(const rg_device_opts* opts, rg_handle* out) {
   h->device = o.device;
   h->form = o.form;
   h->flags = o.flags;
+  if (h->flags & RG_FLAG_VALIDATE) h->flags |= RG_FLAG_COUNTERS;  // the checks live in the counting variants
   if ((e = cudaSetDevice(o.device)) != cudaSuccess) { delete h; return cuda_fail(nullptr, e, "cudaSetDevice"); }
   if (o.stream) {
     h->stream = (cudaStream_t)o.stream;
@@ -1066,6 +1069,8 @@ rg_status rg_sync_stats(rg_handle h, rg_render_stats* stats) {
   stats->num_threads = 0;
   stats->error_flags = err;
   stats->kernel_launches = h->last_launches;
+  stats->invalid_hits = c[CNT_INVALID];
+  stats->invalid_mask = (uint32_t)c[CNT_INVALID_MASK];
   stats->traverse_ms = 0.0;
   for (uint32_t i = 0; i + 1 < h->stage_used; i += 2) {
     float t = 0.0f;

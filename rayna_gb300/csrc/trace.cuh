@@ -123,17 +123,28 @@ __device__ __forceinline__ bool slab(float lx, float hx, float ly, float hy, flo
 // Primitive tests. Each returns the hit distance through `t` when it hits
 // inside [start, end]. Full hit records are built once, for the closest hit.
 // ---------------------------------------------------------------------------
-// SphereMesh::intersect (mesh/primitive/sphere.rs:44-99)
+// SphereMesh::intersect (mesh/primitive/sphere.rs:44-99): the roots
+// -half_b -/+ sqrt(disc) of |oc + t d|^2 = r^2, the near one first, each
+// tested against [start, end]. In f32 the reference's disc = half_b^2 - c
+// cancels catastrophically for a small, distant sphere (both terms near
+// |oc|^2); for a unit d it equals r^2 - |l|^2 with l = oc - half_b d, the
+// centre-to-line vector, which does not. The roots are q = -(half_b +
+// sign(half_b) sqrt(disc)) and c / q (Vieta), so neither subtracts nearly
+// equal terms (Haines, Guenther, Akenine-Moller, "Precision Improvements for
+// Ray/Sphere Intersection", Ray Tracing Gems, 2019).
 __device__ __forceinline__ bool sphere_t(V3 c, float r2, const Ray& r, float start, float end, float& t) {
-  V3 oc = r.o - c;
-  float half_b = dot3(oc, r.d);
-  float cc = __fmaf_rn(oc.x, oc.x, __fmaf_rn(oc.y, oc.y, __fmaf_rn(oc.z, oc.z, -r2)));
-  float disc = __fmaf_rn(half_b, half_b, -cc);
+  const V3 oc = r.o - c;
+  const float half_b = dot3(oc, r.d);
+  const V3 l = v3(__fmaf_rn(-half_b, r.d.x, oc.x), __fmaf_rn(-half_b, r.d.y, oc.y), __fmaf_rn(-half_b, r.d.z, oc.z));
+  const float disc = r2 - dot3(l, l);
   if (disc < 0.0f) return false;
-  float sq = __fsqrt_rn(disc);
-  float root = -half_b - sq;
+  const float cc = __fmaf_rn(oc.x, oc.x, __fmaf_rn(oc.y, oc.y, __fmaf_rn(oc.z, oc.z, -r2)));
+  const float sq = __fsqrt_rn(disc);
+  const float q = half_b > 0.0f ? -half_b - sq : -half_b + sq;
+  const float other = q != 0.0f ? __fdiv_rn(cc, q) : q;
+  float root = fminf(q, other);
   if (!(start <= root && root <= end)) {
-    root = -half_b + sq;
+    root = fmaxf(q, other);
     if (!(start <= root && root <= end)) return false;
   }
   t = root;
@@ -1123,6 +1134,43 @@ __device__ __forceinline__ C3f attenuation(const GpuScene& sc, const rg_material
 }
 
 // ---------------------------------------------------------------------------
+// RG_FLAG_VALIDATE: the invariants of shared/validate.rs:21-197 (number,
+// normal3, uv, colour, intersection), counted instead of asserted.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool finite3(V3 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
+// approx::relative_eq with epsilon 1e-6 and max_relative 1e-3 (validate.rs:14-16)
+__device__ __forceinline__ bool rel_eq(float a, float b) {
+  const float d = fabsf(a - b);
+  return d <= 1e-6f || d <= 1e-3f * fmaxf(fabsf(a), fabsf(b));
+}
+static __device__ __noinline__ void validate_hit(const FrameParams& fp, const Ray& r, float t, const Surface& s, float start,
+                                          float end) {
+  uint32_t bad = 0;
+  if (!isfinite(t) || !finite3(s.pos) || !finite3(s.normal) || !finite3(s.ray_normal)) bad |= RG_INVALID_NONFINITE;
+  // unit length within the reference's relative tolerance 1e-3 (its f64
+  // normals pass glam's tighter is_normalized; an f32 sphere normal (p - c) / r
+  // carries the root's rounding divided by r, up to a few 1e-4 for small,
+  // distant spheres)
+  if (!(fabsf(dot3(s.normal, s.normal) - 1.0f) <= 2e-3f) || !(fabsf(dot3(s.ray_normal, s.ray_normal) - 1.0f) <= 2e-3f))
+    bad |= RG_INVALID_NOT_NORMALISED;
+  if (!(start <= t && t <= end)) bad |= RG_INVALID_INTERVAL;
+  const V3 at = at3(r.o, r.d, t);
+  if (!rel_eq(length3(s.pos - r.o), t) || !rel_eq(s.pos.x, at.x) || !rel_eq(s.pos.y, at.y) || !rel_eq(s.pos.z, at.z))
+    bad |= RG_INVALID_POSITION;
+  if (!(s.u >= 0.0f && s.u <= 1.0f && s.v >= 0.0f && s.v <= 1.0f)) bad |= RG_INVALID_UV;
+  if (bad) {
+    atomicAdd(fp.counters + CNT_INVALID, 1ull);
+    atomicOr(fp.counters + CNT_INVALID_MASK, (unsigned long long)bad);
+  }
+}
+__device__ __forceinline__ void validate_colour(const FrameParams& fp, C3f c) {
+  if (!(isfinite(c.r) && isfinite(c.g) && isfinite(c.b) && c.r >= 0.0f && c.g >= 0.0f && c.b >= 0.0f)) {
+    atomicAdd(fp.counters + CNT_INVALID, 1ull);
+    atomicOr(fp.counters + CNT_INVALID_MASK, (unsigned long long)RG_INVALID_COLOUR);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Camera: render_px_msaa stratification (render/renderer.rs:350-389) and
 // Viewport::calc_ray (scene/camera.rs:191-213).
 // ---------------------------------------------------------------------------
@@ -1296,6 +1344,7 @@ __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x,
     }
     Surface surf;
     finalize_hit<F>(sc, ray, h, ctx, surf, 1e-3f);
+    if (COUNT && fp.validate) validate_hit(fp, ray, h.t, surf, 1e-3f, 3.402823466e38f);
     const rg_material m = sc.materials[surf.material];
     if (m.kind == RG_MAT_LIGHT) {
       const C3f e = material_colour<F>(sc, m, surf);
@@ -1308,6 +1357,7 @@ __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x,
     beta = C3f{beta.r * a.r, beta.g * a.g, beta.b * a.b};
     ray = make_ray(surf.pos, dir);
   }
+  if (COUNT && fp.validate) validate_colour(fp, L);
   return L;
 }
 

@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
       if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget)) {
         HitRec h;
         const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
-        if (shade_path<F>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
+        if (shade_path<F, COUNT>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
           uint32_t slot = warp_append(s.counts + nxt, true);
           if (slot < wp.n_paths) s.active[nxt][slot] = p;
           else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);

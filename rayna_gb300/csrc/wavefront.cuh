@@ -66,22 +66,29 @@ __device__ __forceinline__ uint32_t clamp_count(uint32_t n, const WaveParams& wp
 // Shading of one path at its closest hit (or miss). Returns true when the path
 // continues; then its record holds the scattered ray. Ended paths write their
 // radiance.
-template <uint32_t F>
+// CHECK (the counting variants): RG_FLAG_VALIDATE's checks of the hit and of
+// the path's colour.
+template <uint32_t F, bool CHECK = false>
 __device__ __forceinline__ bool shade_path(const GpuScene& sc, const FrameParams& fp, const PathState& s, uint32_t p,
                                            uint32_t pix, uint32_t smp, uint32_t depth, const Ray& r, C3f beta,
                                            bool hit, const HitRec& h) {
   if (!hit) {
     C3f sk = sky_of<F>(sc, r.d);
-    finish_path(s, p, C3f{0.0f + beta.r * sk.r, 0.0f + beta.g * sk.g, 0.0f + beta.b * sk.b});
+    const C3f L{0.0f + beta.r * sk.r, 0.0f + beta.g * sk.g, 0.0f + beta.b * sk.b};
+    if (CHECK && fp.validate) validate_colour(fp, L);
+    finish_path(s, p, L);
     return false;
   }
   RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
   Surface surf;
   finalize_hit<F>(sc, r, h, ctx, surf, 1e-3f);
+  if (CHECK && fp.validate) validate_hit(fp, r, h.t, surf, 1e-3f, 3.402823466e38f);
   const rg_material m = sc.materials[surf.material];
   if (m.kind == RG_MAT_LIGHT) {
     const C3f e = material_colour<F>(sc, m, surf);
-    finish_path(s, p, C3f{0.0f + beta.r * e.r, 0.0f + beta.g * e.g, 0.0f + beta.b * e.b});
+    const C3f L{0.0f + beta.r * e.r, 0.0f + beta.g * e.g, 0.0f + beta.b * e.b};
+    if (CHECK && fp.validate) validate_colour(fp, L);
+    finish_path(s, p, L);
     return false;
   }
   if (depth < fp.ray_depth) {

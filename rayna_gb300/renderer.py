@@ -37,6 +37,8 @@ class RenderStats:
     sdf_steps: int = 0
     error_flags: int = 0
     traverse_ms: float = 0.0
+    invalid_hits: int = 0          # validate=True: hits / colours breaking shared/validate.rs's invariants
+    invalid_mask: int = 0          # which invariants (RG_INVALID_* bits)
 
 
 @dataclass
@@ -58,13 +60,14 @@ class Renderer:
 
     def __init__(self, scene: Scene, camera: Camera, options: RenderOpts, *, device: int = 0,
                  form: str = "megakernel", seed: int = 0, stream: int | None = None, counters: bool = False,
-                 stage_times: bool = False):
+                 stage_times: bool = False, validate: bool = False):
         self._lib = A.load_library()
         dopts = A.rg_device_opts()
         dopts.device = device
         dopts.stream = stream
         dopts.form = {"megakernel": A.RG_FORM_MEGAKERNEL, "wavefront": A.RG_FORM_WAVEFRONT}[form]
-        dopts.flags = (A.RG_FLAG_COUNTERS if counters else 0) | (A.RG_FLAG_STAGE_TIMES if stage_times else 0)
+        dopts.flags = ((A.RG_FLAG_COUNTERS if counters else 0) | (A.RG_FLAG_STAGE_TIMES if stage_times else 0) |
+                       (A.RG_FLAG_VALIDATE if validate else 0))
         h = C.c_void_p()
         st = self._lib.rg_create(C.byref(dopts), C.byref(h))
         A.check(self._lib, None, st)
@@ -269,7 +272,8 @@ class Renderer:
         rs = RenderStats(duration=dt, num_threads=0, opts=o, accum_frames=stats.accum_frames,
                          kernel_ms=stats.kernel_ms, samples=stats.samples, rays=stats.rays,
                          node_visits=stats.node_visits, prim_tests=stats.prim_tests,
-                         sdf_steps=stats.sdf_steps, error_flags=stats.error_flags, traverse_ms=stats.traverse_ms)
+                         sdf_steps=stats.sdf_steps, error_flags=stats.error_flags, traverse_ms=stats.traverse_ms,
+                         invalid_hits=stats.invalid_hits, invalid_mask=stats.invalid_mask)
         return Render(img=img, stats=rs)
 
     def frame_moments(self):

@@ -299,3 +299,22 @@ def test_stage_times_bracket_the_traversal(form):
         out = r.render(seed=31)
     np.testing.assert_array_equal(ref, out.img)
     assert 0.0 < out.stats.traverse_ms <= out.stats.kernel_ms * 1.001 + 1e-3
+
+
+@pytest.mark.parametrize("form", ["megakernel", "wavefront"])
+@pytest.mark.parametrize("case", list(CASES))
+def test_validate_mode_finds_no_broken_invariants(case, form):
+    """RG_FLAG_VALIDATE checks every closest hit and path colour against the
+    reference's debug invariants (shared/validate.rs: finite values, unit
+    normals, the distance inside the interval, the point at that distance
+    along the ray, uv in [0, 1]^2, colours finite and non-negative). The
+    checks only read: the image equals an unchecked render's."""
+    scene, cam, opts = CASES[case]()
+    with Renderer.new_from(scene, cam, opts, 0, form=form, validate=True) as r:
+        out = r.render(seed=3)
+        st = out.stats
+    assert st.rays > 0 and st.node_visits > 0  # validation runs the counting variants
+    assert st.invalid_hits == 0, (st.invalid_hits, st.invalid_mask)
+    with Renderer.new_from(scene, cam, opts, 0, form=form) as r:
+        img = r.render(seed=3).img
+    np.testing.assert_array_equal(out.img, img)
