@@ -455,3 +455,86 @@ def textures_demo(width: int = 320, height: int = 180, spp: int = 32, ray_depth:
     scene = Scene(objects=objs, skybox=HdrImageSkybox(synthetic_sky(seed=seed)))
     cam = look_at_camera((0.0, 2.2, 8.0), (0.0, 0.8, 0.0), 40.0)
     return scene, cam, RenderOpts(width=width, height=height, samples=spp, ray_depth=ray_depth)
+
+
+def rtiaw_demo(seed: int = 0, width: int = 400, height: int = 225, spp: int = 32, ray_depth: int = 50):
+    """The reference's RTIAW_DEMO preset (scene/preset.rs:157-254), its random
+    draws from PCG64(seed) instead of thread_rng: a 31 x 31 grid of r = 0.2
+    spheres (70 %) and boxes (30 %; AxisBoxMesh::new_centred with a size in
+    [0, 0.8]^3) with Lambertian (70 %), metal (20 %) or dielectric (ior in
+    [1, 10], density 69) materials, three r = 1 spheres, and the ground sphere
+    with LocalNoiseTexture(Perlin(69) scaled by 10000). Returns (scene,
+    camera, opts)."""
+    from .scene import ColourSource, LocalNoiseTexture, Perlin, ScalePoint
+    rng = np.random.Generator(np.random.PCG64(seed))
+    objs = []
+    big = np.array([4.0, 0.2, 0.0])
+    for a in range(-15, 16):
+        for b in range(-15, 16):
+            centre = np.array([a, 0.2, b], float) + np.array([rng.random(), 0.0, rng.random()]) * 0.9
+            if np.linalg.norm(centre - big) <= 0.9:
+                continue
+            choice = rng.random()
+            if choice < 0.7:
+                mat = LambertianMaterial(tuple(rng.random(3) * rng.random(3)))
+            elif choice <= 0.9:
+                mat = MetalMaterial(tuple(rng.uniform(0.5, 1.0, 3)), float(rng.uniform(0.0, 0.5)))
+            else:
+                mat = DielectricMaterial(tuple(rng.uniform(0.5, 1.0, 3)), float(rng.uniform(1.0, 10.0)), 69.0)
+            if rng.random() < 0.7:
+                mesh = SphereMesh(tuple(centre), 0.2)
+            else:
+                mesh = AxisBoxMesh.new_centred(centre, rng.random(3) * 0.8)
+            objs.append(SimpleObject(mesh, mat))
+    objs.append(SimpleObject(SphereMesh((0.0, 1.0, 0.0), 1.0), DielectricMaterial((1.0, 1.0, 1.0), 1.5, 69.0)))
+    objs.append(SimpleObject(SphereMesh((-4.0, 1.0, 0.0), 1.0), LambertianMaterial((0.4, 0.2, 0.1))))
+    objs.append(SimpleObject(SphereMesh((4.0, 1.0, 0.0), 1.0), MetalMaterial((0.7, 0.6, 0.5), 0.0)))
+    ground = LocalNoiseTexture(ColourSource.Greyscale(ScalePoint(Perlin(69)).set_scale(10000.0)))
+    objs.append(SimpleObject(SphereMesh((0.0, -1000.0, 0.0), 1000.0), LambertianMaterial(ground)))
+    fwd = np.array([-13.0, -2.0, -3.0])
+    cam = Camera(pos=(13.0, 2.0, 3.0), fwd=tuple(fwd / np.linalg.norm(fwd)), v_fov=Angle.from_degrees(20.0),
+                 focus_dist=10.0, defocus_angle=Angle.from_degrees(0.6))
+    return Scene(objects=objs, skybox=SimpleSkybox()), cam, RenderOpts(width=width, height=height, samples=spp,
+                                                                          ray_depth=ray_depth)
+
+
+def rttnw_demo(seed: int = 0, width: int = 400, height: int = 400, spp: int = 64, ray_depth: int = 16):
+    """The reference's RTTNW_DEMO preset (scene/preset.rs:394-604), its random
+    draws from PCG64(seed) instead of thread_rng: a BvhMesh floor of 20 x 20
+    boxes of random height, a parallelogram light, brown, glass, fuzzed-metal
+    spheres, a dielectric sphere holding a blue medium, the WorldNoiseTexture
+    sphere (Perlin(69) scaled by 4) and a BvhMesh "cube" of 1000 r = 0.1 balls
+    rotated 15 degrees about Y and translated. No sky. Returns (scene, camera,
+    opts)."""
+    from .scene import (
+        ColourSource, ParallelogramMesh, Perlin, Planar, ScalePoint, Transform3, WorldNoiseTexture,
+    )
+    rng = np.random.Generator(np.random.PCG64(seed))
+    floor = []
+    for i in range(20):
+        for j in range(20):
+            low = np.array([-10.0 + i, 0.0, -10.0 + j])
+            high = low + np.array([1.0, rng.uniform(0.0, 1.0), 1.0])
+            floor.append(AxisBoxMesh(tuple(low), tuple(high)))
+    objs = [
+        SimpleObject(BvhMesh(floor), LambertianMaterial((0.48, 0.83, 0.53))),
+        SimpleObject(ParallelogramMesh(Planar.new((1.23, 5.54, 1.47), (3.0, 0.0, 0.0), (0.0, 0.0, 2.65))),
+                     LightMaterial((7.0, 7.0, 7.0))),
+        SimpleObject(SphereMesh((4.0, 4.0, 2.0), 0.5), LambertianMaterial((0.7, 0.3, 0.1))),
+        SimpleObject(SphereMesh((2.6, 1.5, 0.45), 0.5), DielectricMaterial((1.0, 1.0, 1.0), 1.5, 1.0)),
+        SimpleObject(SphereMesh((0.0, 1.5, 1.45), 0.5), MetalMaterial((0.8, 0.8, 0.9), 1.0)),
+        SimpleObject(SphereMesh((3.6, 1.5, 1.45), 0.7), DielectricMaterial((1.0, 1.0, 1.0), 1.5, 0.0)),
+        VolumetricObject(SphereMesh((3.6, 1.5, 1.45), 0.6999), IsotropicMaterial((0.2, 0.4, 0.9), 0.3), 2.0),
+        SimpleObject(SphereMesh((2.2, 2.8, 3.0), 0.8),
+                     LambertianMaterial(WorldNoiseTexture(ColourSource.Greyscale(ScalePoint(Perlin(69)).set_scale(4.0))))),
+    ]
+    spread = 0.825
+    balls = [SphereMesh(tuple(rng.uniform(-1.0, 1.0, 3) * spread), 0.1) for _ in range(1000)]
+    turn = Transform3.from_scale_rotation_translation((1.0, 1.0, 1.0), (0.0, 1.0, 0.0), Angle.from_degrees(15.0),
+                                                      np.array([-1.0, 2.7, 3.95]) + spread)
+    objs.append(SimpleObject(BvhMesh(balls), LambertianMaterial((0.85, 0.85, 0.85)), turn))
+    fwd = np.array([-1.0, 0.0, 3.0])
+    cam = Camera(pos=(4.78, 2.78, -6.0), fwd=tuple(fwd / np.linalg.norm(fwd)), v_fov=Angle.from_degrees(40.0),
+                 focus_dist=1.0, defocus_angle=Angle(0.0))
+    return Scene(objects=objs, skybox=NoSkybox()), cam, RenderOpts(width=width, height=height, samples=spp,
+                                                                     ray_depth=ray_depth)

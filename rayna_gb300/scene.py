@@ -546,21 +546,22 @@ class Triangle:
 
 
 class BvhMesh:
-    """mesh/advanced/bvh.rs: a BVH over triangles and spheres sharing one
-    material (and one transform).
+    """mesh/advanced/bvh.rs: a BVH over bounded meshes (triangles, spheres,
+    boxes, parallelograms, cylinders, nested BvhMeshes) sharing one material
+    and one transform.
 
     ``BvhMesh(list_of_meshes)`` mirrors the reference constructor;
-    ``BvhMesh.from_arrays(vertices, normals)`` takes (n, 3, 3) arrays.
+    ``BvhMesh.from_arrays(vertices, normals)`` takes (n, 3, 3) triangle arrays.
     """
 
     def __init__(self, meshes: Iterable = ()):
         items = list(meshes)
         for t in items:
-            if not isinstance(t, (Triangle, SphereMesh)):
-                raise UnsupportedVariant(f"BvhMesh over {type(t).__name__} cannot cross the C ABI")
+            if not isinstance(t, (Triangle, SphereMesh, AxisBoxMesh, ParallelogramMesh, CylinderMesh, BvhMesh)):
+                raise UnsupportedVariant(f"BvhMesh over {type(t).__name__} cannot cross the C ABI "
+                                         "(a BvhMesh holds bounded meshes)")
         tris = [t for t in items if isinstance(t, Triangle)]
-        self.spheres = np.asarray([(*_vec3(b.pos), float(b.radius)) for b in items if isinstance(b, SphereMesh)],
-                                  np.float32).reshape(-1, 4)
+        self.items = [m for m in items if not isinstance(m, Triangle)]
         if tris:
             self.vertices = np.stack([t.vertices for t in tris]).astype(np.float32)
             self.normals = np.stack([t.normals for t in tris]).astype(np.float32)
@@ -576,6 +577,7 @@ class BvhMesh:
     @staticmethod
     def from_arrays(vertices, normals) -> "BvhMesh":
         m = BvhMesh()
+        m.items = []
         m.vertices = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3, 3)
         m.normals = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3, 3)
         if m.vertices.shape != m.normals.shape:
@@ -588,7 +590,7 @@ class BvhMesh:
         return self._centre
 
     def __len__(self):
-        return self.vertices.shape[0] + self.spheres.shape[0]
+        return self.vertices.shape[0] + len(self.items)
 
 
 @dataclass
@@ -867,50 +869,7 @@ class FlatScene:
                     raise ValueError("an object transform must be finite and invertible")
                 xf = len(self.transforms)
                 self.transforms.append(ot.transform.matrix[:3].copy())
-            if isinstance(mesh, SphereMesh):
-                self.spheres.append((*_vec3(mesh.pos), float(mesh.radius)))
-                self.sphere_mat.append(mat)
-                self.sphere_xf.append(xf)
-            elif isinstance(mesh, Triangle):
-                self.tri_v.append(np.asarray(mesh.vertices, np.float32).reshape(1, 3, 3))
-                self.tri_n.append(np.asarray(mesh.normals, np.float32).reshape(1, 3, 3))
-                self.tri_mat.append(np.full(1, mat, np.uint32))
-                self.tri_mesh.append(np.full(1, -1, np.int32))
-                self.tri_xf.append(np.full(1, xf, np.uint32))
-            elif isinstance(mesh, BvhMesh):
-                n = mesh.vertices.shape[0]
-                if n:
-                    self.tri_v.append(mesh.vertices)
-                    self.tri_n.append(mesh.normals)
-                    self.tri_mat.append(np.full(n, mat, np.uint32))
-                    self.tri_mesh.append(np.full(n, self.n_meshes, np.int32))
-                    self.tri_xf.append(np.full(n, xf, np.uint32))
-                    self.n_meshes += 1
-                for b in mesh.spheres:  # spheres of the mesh: one object each, same material and transform
-                    self.spheres.append(tuple(float(x) for x in b))
-                    self.sphere_mat.append(mat)
-                    self.sphere_xf.append(xf)
-            elif isinstance(mesh, AxisBoxMesh):
-                self.boxes.append((*_vec3(mesh.a), *_vec3(mesh.b)))
-                self.box_mat.append(mat)
-                self.box_xf.append(xf)
-            elif isinstance(mesh, RaymarchedIsosurfaceMesh):
-                self.sdfs.append(self._sdf(mesh, mat))
-            elif isinstance(mesh, ParallelogramMesh):
-                self.quads.append(mesh.plane.flat())
-                self.quad_mat.append(mat)
-                self.quad_xf.append(xf)
-            elif isinstance(mesh, CylinderMesh):
-                self.cylinders.append((*_vec3(mesh.p1), *_vec3(mesh.p2), float(mesh.radius)))
-                self.cyl_mat.append(mat)
-                self.cyl_xf.append(xf)
-            elif isinstance(mesh, InfinitePlaneMesh):
-                self.planes.append(mesh.plane.flat())
-                self.plane_mat.append(mat)
-                self.plane_wrap.append({"wrap": A.RG_UV_WRAP, "mirror": A.RG_UV_MIRROR,
-                                        "clamp_zero": A.RG_UV_CLAMP_ZERO}[mesh.uv_wrap])
-            else:
-                raise UnsupportedVariant(f"mesh {type(mesh).__name__} cannot cross the C ABI")
+            self._add_mesh(mesh, mat, xf)
         elif isinstance(obj, VolumetricObject):
             if not _identity(obj.transform):
                 raise UnsupportedVariant("a transformed VolumetricObject is not supported by the GPU path")
@@ -930,6 +889,52 @@ class FlatScene:
             self.volumes.append(v)
         else:
             raise UnsupportedVariant(f"object {type(obj).__name__} cannot cross the C ABI")
+
+    def _add_mesh(self, mesh, mat: int, xf: int):
+        """One mesh of a SimpleObject (or of a BvhMesh) with its material and
+        transform index."""
+        if isinstance(mesh, SphereMesh):
+            self.spheres.append((*_vec3(mesh.pos), float(mesh.radius)))
+            self.sphere_mat.append(mat)
+            self.sphere_xf.append(xf)
+        elif isinstance(mesh, Triangle):
+            self.tri_v.append(np.asarray(mesh.vertices, np.float32).reshape(1, 3, 3))
+            self.tri_n.append(np.asarray(mesh.normals, np.float32).reshape(1, 3, 3))
+            self.tri_mat.append(np.full(1, mat, np.uint32))
+            self.tri_mesh.append(np.full(1, -1, np.int32))
+            self.tri_xf.append(np.full(1, xf, np.uint32))
+        elif isinstance(mesh, BvhMesh):
+            n = mesh.vertices.shape[0]
+            if n:
+                self.tri_v.append(mesh.vertices)
+                self.tri_n.append(mesh.normals)
+                self.tri_mat.append(np.full(n, mat, np.uint32))
+                self.tri_mesh.append(np.full(n, self.n_meshes, np.int32))
+                self.tri_xf.append(np.full(n, xf, np.uint32))
+                self.n_meshes += 1
+            for m in mesh.items:  # its other meshes: one object each, with the mesh's material and transform
+                self._add_mesh(m, mat, xf)
+        elif isinstance(mesh, AxisBoxMesh):
+            self.boxes.append((*_vec3(mesh.a), *_vec3(mesh.b)))
+            self.box_mat.append(mat)
+            self.box_xf.append(xf)
+        elif isinstance(mesh, RaymarchedIsosurfaceMesh):
+            self.sdfs.append(self._sdf(mesh, mat))
+        elif isinstance(mesh, ParallelogramMesh):
+            self.quads.append(mesh.plane.flat())
+            self.quad_mat.append(mat)
+            self.quad_xf.append(xf)
+        elif isinstance(mesh, CylinderMesh):
+            self.cylinders.append((*_vec3(mesh.p1), *_vec3(mesh.p2), float(mesh.radius)))
+            self.cyl_mat.append(mat)
+            self.cyl_xf.append(xf)
+        elif isinstance(mesh, InfinitePlaneMesh):
+            self.planes.append(mesh.plane.flat())
+            self.plane_mat.append(mat)
+            self.plane_wrap.append({"wrap": A.RG_UV_WRAP, "mirror": A.RG_UV_MIRROR,
+                                    "clamp_zero": A.RG_UV_CLAMP_ZERO}[mesh.uv_wrap])
+        else:
+            raise UnsupportedVariant(f"mesh {type(mesh).__name__} cannot cross the C ABI")
 
     @staticmethod
     def _sdf(mesh: RaymarchedIsosurfaceMesh, mat: int) -> A.rg_sdf:

@@ -45,6 +45,8 @@ CASES = {
     "cornell_quads": lambda: small(presets.cornell_quads, 48, 48, 16, 8),
     "cornell": lambda: small(presets.cornell, 48, 48, 16, 8),  # the preset's rotated boxes
     "textures": lambda: small(presets.textures_demo, 64, 36, 16, 8),  # every texture kind, image sky
+    "rtiaw": lambda: small(presets.rtiaw_demo, 64, 36, 8, 12),  # the reference's RTIAW_DEMO preset
+    "rttnw": lambda: small(presets.rttnw_demo, 48, 48, 16, 8),  # the reference's RTTNW_DEMO preset
 }
 
 
@@ -63,7 +65,7 @@ def test_path_by_path_parity_with_f32_oracle(case):
     frac = close.mean()
     print(f"{case}: {frac:.4f} of pixels match the f32 oracle path for path")
     assert frac >= {"random_spheres": 0.97, "cornell_mesh": 0.97, "sdf_volumes": 0.9, "cornell_quads": 0.97,
-                    "cornell": 0.97, "textures": 0.97}[case]
+                    "cornell": 0.97, "textures": 0.97, "rtiaw": 0.97, "rttnw": 0.97}[case]
 
 
 @pytest.mark.parametrize("case", list(CASES))
@@ -71,7 +73,7 @@ def test_statistical_parity_with_f64_oracle(case):
     scene, cam, opts = CASES[case]()
     flat = flatten(scene)
     frames = {"random_spheres": 24, "cornell_mesh": 48, "sdf_volumes": 32, "cornell_quads": 48, "cornell": 48,
-              "textures": 32}[case]
+              "textures": 32, "rtiaw": 32, "rttnw": 32}[case]
     spp = opts.samples
     sq = 0.0
     with Renderer.new_from(scene, cam, opts, 0, seed=7) as r:
@@ -264,8 +266,8 @@ def test_wavefront_equals_megakernel(case):
             # which changes when the closest distance shrinks and so how many
             # far nodes are culled; the persistent extend kernel regroups rays
             # as lanes refill). They are work counters, not results.
-            assert abs(a[2].node_visits - b[2].node_visits) <= 0.03 * a[2].node_visits
-            assert abs(a[2].prim_tests - b[2].prim_tests) <= 0.03 * a[2].prim_tests
+            assert abs(a[2].node_visits - b[2].node_visits) <= 0.06 * a[2].node_visits
+            assert abs(a[2].prim_tests - b[2].prim_tests) <= 0.06 * a[2].prim_tests
     # The two trees give the same closest hits except at exact-distance ties
     # between primitives (a shared edge hit exactly), where the traversal
     # order picks the primitive.
