@@ -150,7 +150,9 @@ __global__ void __launch_bounds__(kWfBlock) k_bbounce(const BatchItemDev* __rest
   Ray r;
   C3f beta;
   Traversal t;
-  uint2 stack[kTravStack];
+  __shared__ uint2 stack_sh[kSharedStackOf<F> > 0 ? kSharedStackOf<F> * kWfBlock : 1];
+  uint2 stack_loc[kTravStack - kSharedStackOf<F>];
+  SplitStack<kSharedStackOf<F>, kWfBlock> stack{stack_sh + threadIdx.x, stack_loc};
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !has);
     if (idle && !drained) {

@@ -552,6 +552,33 @@ __device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t sel) {
 constexpr int kTravStack = 64;
 static_assert(kTravStack >= kStackSize && kTravStack >= kWideMaxDepth + 1, "traversal stack too small");
 
+// Traversal stacks. LocalStack: every entry in local memory. SplitStack: the
+// first SH entries of each thread in shared memory (entry i of thread x at
+// i * STRIDE + x, so a warp's 8-byte accesses are contiguous and no node data
+// evicts them from L1), the deeper ones in local memory.
+struct LocalStack {
+  uint2* s;
+  __device__ __forceinline__ uint2 get(int i) const { return s[i]; }
+  __device__ __forceinline__ void set(int i, uint2 v) { s[i] = v; }
+};
+template <int SH, int STRIDE>
+struct SplitStack {
+  uint2* sh;   // this thread's column of the block's shared array (unused when SH is 0)
+  uint2* loc;  // kTravStack - SH entries in local memory
+  __device__ __forceinline__ uint2 get(int i) const {
+    if constexpr (SH > 0) return i < SH ? sh[i * STRIDE] : loc[i - SH];
+    else return loc[i];
+  }
+  __device__ __forceinline__ void set(int i, uint2 v) {
+    if constexpr (SH > 0) {
+      if (i < SH) sh[i * STRIDE] = v;
+      else loc[i - SH] = v;
+    } else {
+      loc[i] = v;
+    }
+  }
+};
+
 // Resumable traversal of one ray over the binary or the 8-wide tree. A run
 // goes on to completion, or (BOUNDED) for at most `budget` node visits, and
 // returns true once the traversal is complete (the closest hit so far is in
@@ -605,14 +632,15 @@ __device__ __forceinline__ void trav_init(Traversal& t, const GpuScene& sc, cons
 // stack as (node, entry distance) and are dropped on pop once they lie beyond
 // the closest hit (the same conservative comparison as the slab test, so the
 // result does not change).
-template <uint32_t F, bool COUNT, bool BOUNDED>
-__device__ __forceinline__ bool run_binary(Traversal& t, uint2* stack, const GpuScene& sc, const Ray& r, float start,
+template <uint32_t F, bool COUNT, bool BOUNDED, class Stack>
+__device__ __forceinline__ bool run_binary(Traversal& t, Stack& stack, const GpuScene& sc, const Ray& r, float start,
                                            const RngCtx& ctx, Counters& cnt, uint32_t* err, int budget) {
   auto pop = [&]() -> int {
     const float lim = __fmaf_rn(fabsf(t.tmax), kSlabSlack, t.tmax);
     while (t.sp > 0) {
       --t.sp;
-      if (__uint_as_float(stack[t.sp].y) <= lim) return (int)stack[t.sp].x;
+      const uint2 e = stack.get(t.sp);
+      if (__uint_as_float(e.y) <= lim) return (int)e.x;
     }
     return kDone;
   };
@@ -632,7 +660,7 @@ __device__ __forceinline__ bool run_binary(Traversal& t, uint2* stack, const Gpu
         bool swap = tn1 < tn0;
         t.ref = swap ? r1 : r0;
         if (t.sp < kStackSize) {
-          stack[t.sp] = make_uint2((uint32_t)(swap ? r0 : r1), __float_as_uint(swap ? tn0 : tn1));
+          stack.set(t.sp, make_uint2((uint32_t)(swap ? r0 : r1), __float_as_uint(swap ? tn0 : tn1)));
           ++t.sp;
         } else {
           atomicOr(err, ERR_STACK_OVERFLOW);
@@ -692,8 +720,8 @@ __device__ __forceinline__ bool run_binary(Traversal& t, uint2* stack, const Gpu
 // do not come here (closest_hit sends them to the binary tree); an axis whose
 // A or C still overflows (a huge node, a tiny component) yields NaN planes,
 // which fminf/fmaxf skip: that axis then does not cull.
-template <uint32_t F, bool COUNT, bool BOUNDED>
-__device__ __forceinline__ bool run_wide(Traversal& t, uint2* stack, const GpuScene& sc, const Ray& r, float start,
+template <uint32_t F, bool COUNT, bool BOUNDED, class Stack>
+__device__ __forceinline__ bool run_wide(Traversal& t, Stack& stack, const GpuScene& sc, const Ray& r, float start,
                                          const RngCtx& ctx, Counters& cnt, uint32_t* err, int budget) {
   const float kNaN = __int_as_float(0x7fffffff), kInf = __int_as_float(0x7f800000);
   const uint32_t oct = t.oct;
@@ -706,8 +734,12 @@ __device__ __forceinline__ bool run_wide(Traversal& t, uint2* stack, const GpuSc
       const uint32_t slot = k ^ oct;
       const uint32_t idx = t.ng.x + __popc(t.ng.y & ((1u << slot) - 1u) & 0xFFu);
       if (t.ng.y > 0x00FFFFFFu) {
-        if (t.sp < kTravStack) stack[t.sp++] = t.ng;
-        else atomicOr(err, ERR_STACK_OVERFLOW);
+        if (t.sp < kTravStack) {
+          stack.set(t.sp, t.ng);
+          ++t.sp;
+        } else {
+          atomicOr(err, ERR_STACK_OVERFLOW);
+        }
       }
       // A tree visits each node at most once per ray; the host checks the
       // tree's structure, and this guard keeps a damaged one bounded (the
@@ -772,7 +804,8 @@ __device__ __forceinline__ bool run_wide(Traversal& t, uint2* stack, const GpuSc
     }
     if (t.ng.y <= 0x00FFFFFFu) {
       if (t.sp == 0) return true;
-      t.ng = stack[--t.sp];
+      --t.sp;
+      t.ng = stack.get(t.sp);
     }
     if (BOUNDED && it >= budget) return false;
   }
@@ -780,8 +813,8 @@ __device__ __forceinline__ bool run_wide(Traversal& t, uint2* stack, const GpuSc
 
 // Runs a traversal to completion (BOUNDED false) or for at most `budget`
 // node visits (BOUNDED true); returns true once it is complete.
-template <uint32_t F, bool COUNT, bool BOUNDED>
-__device__ __forceinline__ bool trav_run(Traversal& t, uint2* stack, const GpuScene& sc, const Ray& r, float start,
+template <uint32_t F, bool COUNT, bool BOUNDED, class Stack>
+__device__ __forceinline__ bool trav_run(Traversal& t, Stack& stack, const GpuScene& sc, const Ray& r, float start,
                                          const RngCtx& ctx, Counters& cnt, uint32_t* err, int budget) {
   if ((F & F_WIDE) && t.wide) return run_wide<F, COUNT, BOUNDED>(t, stack, sc, r, start, ctx, cnt, err, budget);
   return run_binary<F, COUNT, BOUNDED>(t, stack, sc, r, start, ctx, cnt, err, budget);
@@ -826,7 +859,8 @@ template <uint32_t F, bool COUNT>
 __device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float end, const RngCtx& ctx, HitRec& h,
                             Counters& cnt, uint32_t* err) {
   Traversal t;
-  uint2 stack[kTravStack];
+  uint2 entries[kTravStack];
+  LocalStack stack{entries};
   trav_init<F>(t, sc, r, end);
   trav_run<F, COUNT, false>(t, stack, sc, r, start, ctx, cnt, err, 0);
   return finish_hit<F, COUNT>(sc, r, start, end, t, h, cnt);

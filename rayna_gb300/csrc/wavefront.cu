@@ -67,7 +67,9 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
   Ray r;
   C3f beta;
   Traversal t;
-  uint2 stack[kTravStack];
+  __shared__ uint2 stack_sh[kSharedStackOf<F> > 0 ? kSharedStackOf<F> * kWfBlock : 1];
+  uint2 stack_loc[kTravStack - kSharedStackOf<F>];
+  SplitStack<kSharedStackOf<F>, kWfBlock> stack{stack_sh + threadIdx.x, stack_loc};
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !has);
     if (idle && !drained) {
@@ -164,7 +166,9 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
   uint32_t p = 0, pix = 0, smp = 0, depth = 0;
   Ray r;
   Traversal t;
-  uint2 stack[kTravStack];
+  __shared__ uint2 stack_sh[kSharedStackOf<F> > 0 ? kSharedStackOf<F> * kWfBlock : 1];
+  uint2 stack_loc[kTravStack - kSharedStackOf<F>];
+  SplitStack<kSharedStackOf<F>, kWfBlock> stack{stack_sh + threadIdx.x, stack_loc};
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !has);
     if (idle && !drained) {
