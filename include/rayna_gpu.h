@@ -259,7 +259,9 @@ typedef struct rg_render_opts {
 } rg_render_opts;
 
 /* Which kernel form renders a frame. Both forms run the same estimator and
- * produce the same image for the same seed. */
+ * produce the same image for the same seed. The wavefront is the fast form
+ * (the Python binding's default); the megakernel is the plain form that a
+ * zero-initialised rg_device_opts selects. */
 enum { RG_FORM_MEGAKERNEL = 0, RG_FORM_WAVEFRONT = 1 };
 
 typedef struct rg_device_opts {
