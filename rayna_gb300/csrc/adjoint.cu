@@ -93,9 +93,14 @@ __device__ __forceinline__ void medium_scores(const GpuScene& sc, const Ray& r, 
   }
 }
 
+// Traversal stack entries per thread in shared memory (the rest local), as
+// in the persistent wavefront kernels.
+constexpr int kAdjSharedStack = 8;
+using AdjStack = SplitStack<kAdjSharedStack, kAdjBlock>;
+
 template <uint32_t F>
-__device__ void replay_sample(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, uint32_t x, uint32_t y, uint32_t s,
-                              float d0, float d1, float d2) {
+__device__ void replay_sample(AdjStack& stack, const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, uint32_t x,
+                              uint32_t y, uint32_t s, float d0, float d1, float d2) {
   RngCtx ctx{fp.seed_lo, fp.seed_hi, y * fp.width + x, s, 0, nullptr};
   Ray ray = camera_ray(fp, x, y, s, ctx);
   int mat[kAdjMaxVertices];
@@ -110,7 +115,7 @@ __device__ void replay_sample(const GpuScene& sc, const FrameParams& fp, const A
   for (uint32_t depth = 0; depth <= fp.ray_depth; ++depth) {
     ctx.depth = depth;
     HitRec h;
-    bool hit = closest_hit<F, false>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
+    bool hit = closest_hit_with<F, false>(stack, sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
     int winner = -1;
     if (hit && h.sdf < 0 && (F & F_VOL)) {
       uint32_t kind = prim_kind(sc.prims[h.prim]);
@@ -183,6 +188,9 @@ __device__ void replay_sample(const GpuScene& sc, const FrameParams& fp, const A
 
 template <uint32_t F>
 __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_pix) {
+  __shared__ uint2 stack_sh[kAdjSharedStack * kAdjBlock];
+  uint2 stack_loc[kTravStack - kAdjSharedStack];
+  AdjStack stack{stack_sh + threadIdx.x, stack_loc};
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warp = blockIdx.x * (kAdjBlock / 32) + (threadIdx.x >> 5);
   const uint32_t spp = fp.spp;
@@ -194,7 +202,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams f
     if (lp < ppw && pix < n_pix) {
       uint32_t x = pix % fp.width, y = pix / fp.width;
       size_t idx = ((size_t)x * fp.height + y) * 3;
-      replay_sample<F>(sc, fp, ap, x, y, s, ap.adjoint[idx] * inv, ap.adjoint[idx + 1] * inv, ap.adjoint[idx + 2] * inv);
+      replay_sample<F>(stack, sc, fp, ap, x, y, s, ap.adjoint[idx] * inv, ap.adjoint[idx + 1] * inv, ap.adjoint[idx + 2] * inv);
     }
   } else {
     const uint32_t pix = warp;
@@ -202,7 +210,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams f
       uint32_t x = pix % fp.width, y = pix / fp.width;
       size_t idx = ((size_t)x * fp.height + y) * 3;
       float d0 = ap.adjoint[idx] * inv, d1 = ap.adjoint[idx + 1] * inv, d2 = ap.adjoint[idx + 2] * inv;
-      for (uint32_t s = lane; s < spp; s += 32) replay_sample<F>(sc, fp, ap, x, y, s, d0, d1, d2);
+      for (uint32_t s = lane; s < spp; s += 32) replay_sample<F>(stack, sc, fp, ap, x, y, s, d0, d1, d2);
     }
   }
 }
@@ -272,7 +280,9 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
     ff.frame_mean = d_image;
     ff.frame_var = nullptr;
     ff.accum_count = 1;
-    if ((e = launch_megakernel(h->gs, ff, false, st)) != cudaSuccess) return cuda_err(e);
+    // the handle's kernel form renders it (both forms give the same image)
+    e = h->form == RG_FORM_WAVEFRONT ? launch_wavefront(h, ff) : launch_megakernel(h->gs, ff, false, st);
+    if (e != cudaSuccess) return cuda_err(e);
     if ((e = cudaMemcpyAsync(d_adjoint, target, npx3 * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return cuda_err(e);
     k_l2_adjoint<<<1024, 256, 0, st>>>(d_image, d_adjoint, d_adjoint, npx3, d_loss);

@@ -854,16 +854,24 @@ __device__ __forceinline__ bool finish_hit(const GpuScene& sc, const Ray& r, flo
   return any;
 }
 
-// Closest hit over the BVH (binary or 8-wide, by F_WIDE), then the unbounded list.
-template <uint32_t F, bool COUNT>
-__device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float end, const RngCtx& ctx, HitRec& h,
-                            Counters& cnt, uint32_t* err) {
+// Closest hit over the BVH (binary or 8-wide, by F_WIDE), then the unbounded
+// list, with the caller's traversal stack.
+template <uint32_t F, bool COUNT, class Stack>
+__device__ bool closest_hit_with(Stack& stack, const GpuScene& sc, const Ray& r, float start, float end,
+                                 const RngCtx& ctx, HitRec& h, Counters& cnt, uint32_t* err) {
   Traversal t;
-  uint2 entries[kTravStack];
-  LocalStack stack{entries};
   trav_init<F>(t, sc, r, end);
   trav_run<F, COUNT, false>(t, stack, sc, r, start, ctx, cnt, err, 0);
   return finish_hit<F, COUNT>(sc, r, start, end, t, h, cnt);
+}
+
+// The same with the whole stack in local memory.
+template <uint32_t F, bool COUNT>
+__device__ bool closest_hit(const GpuScene& sc, const Ray& r, float start, float end, const RngCtx& ctx, HitRec& h,
+                            Counters& cnt, uint32_t* err) {
+  uint2 entries[kTravStack];
+  LocalStack stack{entries};
+  return closest_hit_with<F, COUNT>(stack, sc, r, start, end, ctx, h, cnt, err);
 }
 
 // Full hit record of the closest hit.
