@@ -145,7 +145,9 @@ def run_adjoint(iters: int = 5, stream=None):
     """Differentiable-rendering workload: 1000 Lambertian spheres (3000 albedo
     parameters) + one medium (3 albedo + 1 density), 512x512, forward and
     backward at 16 spp, depth 8, L2 loss against a 1024-spp target of the
-    ground-truth parameters; Adam steps on the host. Returns timings."""
+    ground-truth parameters; Adam steps on the host. Each iteration renders the
+    forward frame, then takes the adjoint of that frame (rg_backward_frame: its
+    image, the paths of an independent frame key replayed). Returns timings."""
     import torch
 
     from rayna_gb300 import Renderer, presets
@@ -167,7 +169,7 @@ def run_adjoint(iters: int = 5, stream=None):
         r.render(seed=10_000 + k)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        g = r.backward(seed=20_000 + k, target=target)
+        g = r.backward(seed=20_000 + k, target=target, last_frame=True)
         grad = np.concatenate([g["albedo"].astype(np.float64).ravel(), g["density"].astype(np.float64)])
         m1 = b1 * m1 + (1 - b1) * grad
         m2 = b2 * m2 + (1 - b2) * grad * grad

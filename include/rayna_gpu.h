@@ -509,6 +509,15 @@ rg_status rg_set_parameters(rg_handle h, const float* albedo, const float* densi
  * buffer is not touched. */
 rg_status rg_backward(rg_handle h, uint64_t seed, const float* adjoint_rgb, const float* target_rgb, rg_gradients* out);
 
+/* rg_backward with a target whose I is the handle's last rendered frame (its
+ * per-pixel mean), so the forward frame an optimisation loop renders anyway is
+ * not rendered again: the loss is sum (I - target)^2 and frame `seed`'s paths
+ * are replayed. With `seed` other than the rendered frame's, the image and
+ * the replayed paths are independent samples. RG_NOT_READY unless a PBR frame
+ * was rendered since the scene, camera, options, parameters or accumulation
+ * last changed. */
+rg_status rg_backward_frame(rg_handle h, uint64_t seed, const float* target_rgb, rg_gradients* out);
+
 /* Path slots of the fixed device array used by rg_render_static_scratch
  * (31 x 4 bytes each: about 8 MB, held by every device that loads the library). */
 #define RG_STATIC_WAVE_PATHS 65536u

@@ -188,6 +188,7 @@ SIGNATURES = {
     "rg_batch_image": (C.c_int, [_P, C.c_uint32, _F]),
     "rg_batch_item_seed": (C.c_uint64, [C.c_uint64, C.c_uint32]),
     "rg_backward": (C.c_int, [_P, C.c_uint64, _F, _F, C.POINTER(rg_gradients)]),
+    "rg_backward_frame": (C.c_int, [_P, C.c_uint64, _F, C.POINTER(rg_gradients)]),
 }
 
 _lib = None

@@ -238,7 +238,8 @@ void launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& a
 
 }  // namespace
 
-rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, const float* target, rg_gradients* out) {
+rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, const float* target, rg_gradients* out,
+                          bool last_frame) {
   const uint32_t w = h->opts.width, hh = h->opts.height;
   const size_t npx3 = (size_t)w * hh * 3;
   const uint32_t n_mat = (uint32_t)h->host.materials.size(), n_vol = h->host.nv;
@@ -272,7 +273,13 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
   if ((e = cudaMemsetAsync(h->d_adj, 0, need, st)) != cudaSuccess) return cuda_err(e);
   FrameParams fp;
   fill_frame_params(h, seed, fp);
-  if (target) {
+  if (target && last_frame) {
+    // I: the frame mean of the handle's last render (same scene and parameters)
+    d_image = h->d_fmean;
+    if ((e = cudaMemcpyAsync(d_adjoint, target, npx3 * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      return cuda_err(e);
+    k_l2_adjoint<<<1024, 256, 0, st>>>(d_image, d_adjoint, d_adjoint, npx3, d_loss);
+  } else if (target) {
     // Forward frame into a scratch image (the accumulation buffer is untouched).
     FrameParams ff = fp;
     ff.accum = d_adjoint;  // used as a zeroed running-sum scratch, overwritten below

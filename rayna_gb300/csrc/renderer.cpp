@@ -855,6 +855,7 @@ rg_status rg_clear_accumulation(rg_handle h) {
     RG_CUDA(h, cudaMemsetAsync(h->d_accum, 0, (size_t)h->acc_w * h->acc_h * 3 * sizeof(float), h->stream), "clear");
   h->frame_count = 0;
   h->pixel_accum = 0;
+  h->frame_current = false;
   return RG_OK;
 }
 
@@ -954,6 +955,16 @@ rg_status rg_backward(rg_handle h, uint64_t seed, const float* adjoint_rgb, cons
   return backward_device(h, seed, adjoint_rgb, target_rgb, out);
 }
 
+rg_status rg_backward_frame(rg_handle h, uint64_t seed, const float* target_rgb, rg_gradients* out) {
+  if (!h || !out || !target_rgb) return fail(h, RG_INVALID_ARG, "rg_backward_frame: NULL argument");
+  cudaSetDevice(h->device);
+  if (!h->cam_ok) return fail(h, RG_INVALID_CAMERA, "camera viewport could not be calculated");
+  if (!h->frame_current)
+    return fail(h, RG_NOT_READY, "rg_backward_frame: no PBR frame rendered since the scene, camera, options, "
+                                 "parameters or accumulation last changed");
+  return backward_device(h, seed, nullptr, target_rgb, out, true);
+}
+
 rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   if (!h || !t) return fail(h, RG_INVALID_ARG, "rg_set_tuning: NULL argument");
   for (uint32_t r : t->reserved)
@@ -1032,8 +1043,9 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
     e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream);
     if (e == cudaSuccess && (h->flags & RG_FLAG_STAGE_TIMES)) e = stage_mark(h);
   }
-  if (e != cudaSuccess) return cuda_fail(h, e, "render launch");
+  if (e != cudaSuccess) { h->frame_current = false; return cuda_fail(h, e, "render launch"); }
   RG_CUDA(h, cudaEventRecord(h->ev1, h->stream), "event");
+  h->frame_current = fp.mode == RG_MODE_PBR && fp.branching == 1 && fp.frame_mean != nullptr;
   h->last_samples = (uint64_t)fp.width * fp.height * fp.spp;
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));

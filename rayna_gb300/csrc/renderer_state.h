@@ -94,6 +94,7 @@ struct rg_renderer {
   float* d_fmean = nullptr;
   float* d_fvar = nullptr;
   uint32_t frame_count = 0;   // AccumulationBuffer::counter
+  bool frame_current = false; // d_fmean holds a PBR frame of the current scene, camera, options and parameters
   uint32_t pixel_accum = 0;   // AccumulationValue::accum (per pixel; equal for all pixels)
   uint64_t last_samples = 0;
   uint32_t last_launches = 0; // kernels launched by the last frame
@@ -156,7 +157,10 @@ rg_status ensure_frame_buffers(rg_renderer* h);
 rg_status set_error(rg_renderer* h, rg_status st, const char* msg);
 
 // Defined in adjoint.cu
-rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, const float* target, rg_gradients* out);
+// `last_frame`: with a target, I is the handle's last rendered frame (d_fmean)
+// instead of a frame rendered here.
+rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, const float* target, rg_gradients* out,
+                          bool last_frame = false);
 
 // Defined in wavefront.cu
 cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp);

@@ -404,6 +404,7 @@ extern "C" rg_status rg_render_static_scratch(rg_handle h, uint64_t seed, float*
                                               float* d_out) {
   using namespace rg;
   if (!h) return RG_INVALID_ARG;
+  h->frame_current = false;  // this entry does not write the handle's frame mean
   if (!d_accum || accum_count == 0)
     return set_error(h, RG_INVALID_ARG, "rg_render_static_scratch: d_accum must be a device buffer and accum_count >= 1");
   cudaError_t e = cudaSetDevice(h->device);

@@ -186,11 +186,13 @@ class Renderer:
         self._check(self._lib.rg_set_parameters(self._h, fp(a) if a is not None else None,
                                                 fp(d) if d is not None else None))
 
-    def backward(self, seed: int, target=None, adjoint=None):
+    def backward(self, seed: int, target=None, adjoint=None, last_frame: bool = False):
         """Adjoint of frame `seed` (rg_backward). With `target` (w, h, 3) the
-        loss is sum (I - target)^2; otherwise `adjoint` is dLoss/dI. Returns a
-        dict with 'loss', 'albedo' (n_materials, 3), 'emission' (n_materials, 3)
-        and 'density' (n_volumes,)."""
+        loss is sum (I - target)^2; otherwise `adjoint` is dLoss/dI. With
+        `last_frame` (and a target) I is the last render()'s frame instead of
+        frame `seed` rendered again (rg_backward_frame). Returns a dict with
+        'loss', 'albedo' (n_materials, 3), 'emission' (n_materials, 3) and
+        'density' (n_volumes,)."""
         o = self._options
         fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
         t = adj = None
@@ -205,8 +207,13 @@ class Renderer:
         gd = np.zeros(max(self.n_volumes, 1), np.float32)
         g = A.rg_gradients()
         g.albedo, g.emission, g.density = fp(ga), fp(ge), fp(gd)
-        self._check(self._lib.rg_backward(self._h, int(seed), fp(adj) if adj is not None else None,
-                                          fp(t) if t is not None else None, C.byref(g)))
+        if last_frame:
+            if t is None:
+                raise ValueError("last_frame needs a target")
+            self._check(self._lib.rg_backward_frame(self._h, int(seed), fp(t), C.byref(g)))
+        else:
+            self._check(self._lib.rg_backward(self._h, int(seed), fp(adj) if adj is not None else None,
+                                              fp(t) if t is not None else None, C.byref(g)))
         return {"loss": g.loss, "albedo": ga, "emission": ge, "density": gd[: self.n_volumes]}
 
     def frame(self, seed: int) -> np.ndarray:

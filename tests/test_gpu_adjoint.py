@@ -96,3 +96,26 @@ def test_backward_rejects_textures():
         with pytest.raises(RaynaError) as e:
             r.backward(seed=1, adjoint=np.ones((16, 9, 3), np.float32))
         assert e.value.status == 2
+
+
+def test_backward_frame_uses_the_last_render():
+    """rg_backward_frame takes I from the last render(): its gradients equal
+    rg_backward's with the adjoint image 2 (I - target) of that frame, and it
+    refuses once the parameters changed."""
+    from rayna_gb300._abi import RaynaError
+    scene, gt, cam, opts = small_case()
+    with Renderer.new_from(gt, cam, opts, 0) as r:
+        target = r.frame(seed=77)
+    with Renderer.new_from(scene, cam, opts, 0) as r:
+        r.render(seed=5)
+        image, _ = r.frame_moments()
+        g1 = r.backward(seed=9, target=target, last_frame=True)
+        g2 = r.backward(seed=9, adjoint=2.0 * (image.astype(np.float32) - target.astype(np.float32)))
+        np.testing.assert_allclose(g1["albedo"], g2["albedo"], rtol=1e-5, atol=1e-7)
+        np.testing.assert_allclose(g1["density"], g2["density"], rtol=1e-5, atol=1e-7)
+        want = float(np.sum((image.astype(np.float64) - target.astype(np.float64)) ** 2))
+        assert abs(g1["loss"] - want) <= 1e-4 * want
+        r.set_parameters(albedo=np.full((r.n_materials, 3), 0.5, np.float32))
+        with pytest.raises(RaynaError) as e:
+            r.backward(seed=9, target=target, last_frame=True)
+        assert e.value.status == 10  # RG_NOT_READY
