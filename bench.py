@@ -33,6 +33,24 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+def rank_max(value: float, dist=None, device=None) -> float:
+    """The largest `value` over all ranks (the slowest rank's time); `value`
+    itself on a single rank."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, seconds: float, world: int, dist=None, device=None) -> tuple:
+    """Whole-job throughput of `world` replicas: every rank's units over the
+    slowest rank's time. Returns (units per second, that time)."""
+    s = rank_max(seconds, dist, device)
+    return units_per_rank * world / s, s
+
+
 WORKLOADS = {
     "mesh": "triangle-mesh Cornell box: displaced icosphere 1,310,720 tris + 12 box tris, 1024x1024, 64 spp, depth 8",
     "spheres": "random spheres (488 spheres), 400x225, 32 spp, depth 50",
@@ -227,11 +245,11 @@ def run_batch(scale: float, steps: int, stream=None):
 
 
 def run_reference(args, rank, world):
+    if rank != 0:  # rank 0 alone times the CPU reference; the others exit without work
+        return
     from oracle import binding as ob
     name = args.workload
     threads = ob.hardware_threads()
-    if rank != 0:
-        return
     results = []
     for i in range(args.warmup + args.steps):
         res, secs = cpu_baseline(name, threads, target_s=args.ref_seconds)
@@ -343,11 +361,7 @@ def run_gpu(args, rank, world):
         if dist:
             dist.barrier()
         ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-        dev_s = sum(ms) / 1e3
-        if dist:
-            t = torch.tensor([dev_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dev_s = float(t.item())
+        dev_s = rank_max(sum(ms) / 1e3, dist, "cuda")
         samples = opts.width * opts.height * opts.samples
         assert st.error_flags == 0, st.error_flags
         # end-to-end: the public call with the image read back to host memory every frame
@@ -361,6 +375,7 @@ def run_gpu(args, rank, world):
                 out = r.render()
             e2e_s = time.perf_counter() - e0
             assert out.stats.error_flags == 0, out.stats.error_flags
+        e2e_s = rank_max(e2e_s, dist, "cuda")
         results[form] = {
             "msamples_s": samples * args.steps * world / dev_s / 1e6,
             "ms_per_step": dev_s * 1e3 / args.steps,
