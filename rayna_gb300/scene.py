@@ -666,6 +666,9 @@ class InfinitePlaneMesh:
     def __post_init__(self):
         self.plane = _planar(self.plane)
 
+    def centre(self) -> np.ndarray:  # infinite_plane.rs:100: the corner p
+        return np.asarray(self.plane.p, np.float64)
+
 
 @dataclass
 class CylinderMesh:
@@ -710,6 +713,9 @@ class RaymarchedIsosurfaceMesh:
 
     DEFAULT_EPSILON = 1e-7
     DEFAULT_ITERATIONS = 150
+
+    def centre(self) -> np.ndarray:  # raymarched.rs:69: the origin
+        return np.zeros(3)
 
 
 # ---------------------------------------------------------------------------
