@@ -18,11 +18,12 @@ namespace rg {
 constexpr int kWfBlock = 256;
 // Traversal stack entries per thread kept in shared memory by the persistent
 // kernels (16 KB per block of 256); deeper entries live in local memory. The
-// split measured 1.07x on the 1.3M-triangle mesh (8 and 16 entries alike);
-// for scenes of spheres only (shallow trees) it measured 0.98x, so those
-// kernels keep the whole stack in local memory.
+// split measured 1.07x on the 1.3M-triangle mesh (8 and 16 entries alike),
+// 0.98x on scenes of spheres only (shallow trees) and 1.00x on the SDF scene;
+// it is used where it was measured to pay, the triangle-only variants, and
+// every other variant keeps the whole stack in local memory.
 constexpr int kSharedStack = 8;
-template <uint32_t F> constexpr int kSharedStackOf = kinds_of(F) == F_SPHERE ? 0 : kSharedStack;
+template <uint32_t F> constexpr int kSharedStackOf = kinds_of(F) == F_TRI ? kSharedStack : 0;
 constexpr int kKinds = 6;  // miss, lambertian, metal, dielectric, isotropic, light
 enum : uint32_t { KQ_MISS = 0 };
 constexpr int kPrimMiss = -1;  // rec[2].w: >= 0 BVH primitive, -1 miss, -2 - k SDF k
