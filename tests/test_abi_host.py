@@ -161,3 +161,38 @@ def test_presets_shapes_and_winding():
     for t in presets.cornell_box_triangles():
         tv = t.mesh.vertices
         assert np.dot(np.cross(tv[1] - tv[0], tv[2] - tv[0]), t.mesh.normals[0]) < 0
+
+
+def test_flatten_textures_and_images():
+    """Non-solid textures go to the texture table once each (checker cells
+    first, DynamicTexture unwrapped); images once each; unsupported noise
+    sources and unbounded meshes in a BvhMesh are refused."""
+    from rayna_gb300.scene import (
+        ColourSource, DynamicTexture, HdrImageSkybox, Image, ImageTexture, InfinitePlaneMesh, LightMaterial, Perlin,
+        Planar, ScalePoint, UvCheckerTexture, WorldCheckerTexture, WorldNoiseTexture,
+    )
+    img = Image(np.zeros((4, 2, 3), np.float32))
+    inner = ImageTexture(img, scale=(2.0, 1.0))
+    chk = WorldCheckerTexture(even=(1, 1, 1), odd=DynamicTexture(inner), scale=0.5, offset=(0, 0.5, 0))
+    objs = [SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial(chk)),
+            SimpleObject(SphereMesh((3, 0, 0), 1.0), LambertianMaterial(DynamicTexture(chk))),
+            SimpleObject(SphereMesh((6, 0, 0), 1.0), LightMaterial(inner))]
+    flat = flatten(Scene(objects=objs, skybox=HdrImageSkybox(img)))
+    d = flat.desc
+    assert (d.n_textures, d.n_images, d.skybox, d.sky_image) == (3, 1, A.RG_SKY_IMAGE, 0)
+    kinds = [flat.c_textures[i].kind for i in range(3)]
+    assert kinds == [A.RG_TEX_IMAGE, A.RG_TEX_SOLID, A.RG_TEX_WORLD_CHECKER]
+    assert (flat.c_textures[2].odd, flat.c_textures[2].even) == (0, 1)
+    assert [m.texture for m in flat.materials] == [3, 3, 1]
+    assert flat.c_textures[0].scale[0] == 2.0 and flat.c_textures[2].offset[1] == 0.5
+    with pytest.raises(UnsupportedVariant):  # a non-uniform ScalePoint
+        flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial(
+            WorldNoiseTexture(ColourSource.Greyscale(ScalePoint(Perlin(1), scale=(1, 2, 1))))))]))
+    with pytest.raises(UnsupportedVariant):  # Rgb channels must be seeded s, s + 1, s + 2
+        flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial(
+            WorldNoiseTexture(ColourSource.Rgb([Perlin(1), Perlin(5), Perlin(3)]))))]))
+    with pytest.raises(UnsupportedVariant):  # a BvhMesh holds bounded meshes
+        BvhMesh([InfinitePlaneMesh(Planar.new((0, 0, 0), (1, 0, 0), (0, 0, 1)))])
+    flat = flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0),
+                                               LambertianMaterial(UvCheckerTexture(even=(1, 1, 1), odd=(0, 0, 0))))]))
+    assert flat.desc.n_textures == 3 and flat.materials[0].texture == 3
