@@ -206,3 +206,19 @@ def test_texture_table_validation():
     flat = floor_scene(WHITE)
     flat.c_materials[0].texture = 3
     assert lib.rg_inspect_scene(C.byref(flat.desc), C.byref(info)) == A.RG_INVALID_ARG
+
+
+@pytest.mark.parametrize("policy", POLICIES)
+def test_world_checker_on_a_transformed_object_reads_world_space(policy):
+    """WorldCheckerTexture reads pos_w, the mapped point (transform.rs:123): a
+    floor light moved 3 along x by its transform shows the cells of its world
+    position, not of its mesh-space one."""
+    q = ParallelogramMesh(Planar.new((-10, 0, -10), (20, 0, 0), (0, 0, 20)))
+    tex = WorldCheckerTexture(even=WHITE, odd=BLACK, scale=1.0, offset=(0.0, 0.5, 0.0))
+    flat = flatten(Scene(objects=[SimpleObject(q, LightMaterial(tex), Transform3.from_translation((3.0, 0.0, 0.0)))],
+                         skybox=NoSkybox()))
+    pts = [(0.5, 0.5), (1.5, 0.5), (-0.5, 0.5), (4.25, -2.5)]
+    c = ob.query_colour(flat, *down_at(pts), policy)
+    for (x, z), col in zip(pts, c):
+        want = WHITE if (math.floor(x) + math.floor(0.5) + math.floor(z)) % 2 < 1 else BLACK
+        np.testing.assert_array_equal(col, want, err_msg=f"{x}, {z}")
