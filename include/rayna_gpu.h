@@ -217,6 +217,8 @@ typedef struct rg_scene_desc {
     uint32_t n_images;
     const rg_image* images;
     uint32_t sky_image;              /* RG_SKY_IMAGE: index into images */
+    const uint32_t* volume_transform;/* n_volumes: ObjectTransform of VolumetricObjects (object/volumetric.rs:21-45),
+                                        index into transforms or RG_NO_TRANSFORM; NULL = none */
 } rg_scene_desc;
 
 #define RG_NO_TRANSFORM 0xFFFFFFFFu

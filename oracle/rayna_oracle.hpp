@@ -1114,7 +1114,7 @@ template <class P> struct Scene {
   std::vector<uint8_t> perm;       // 512 entries per slot
   std::vector<OImage> images;
   uint32_t sky_image = 0;
-  std::vector<int32_t> sphere_xf, tri_xf, box_xf, quad_xf, cyl_xf;  // transform index, or -1
+  std::vector<int32_t> sphere_xf, tri_xf, box_xf, quad_xf, cyl_xf, vol_xf;  // transform index, or -1
   struct Object { uint32_t kind, index; Aabb<T> box; int32_t xf = -1; };
   std::vector<Object> bounded;    // ObjectList::bvh items, in list order
   struct Unbounded { bool plane; uint32_t index; };
@@ -1193,6 +1193,7 @@ template <class P> struct Scene {
     xf_list(d.box_transform, nb, box_xf);
     xf_list(d.quad_transform, nq, quad_xf);
     xf_list(d.cylinder_transform, nc, cyl_xf);
+    xf_list(d.volume_transform, nv, vol_xf);
     for (uint32_t i = 0; i < ns; ++i) {
       Sphere<P> s;
       s.c = {(T)d.spheres[4 * i], (T)d.spheres[4 * i + 1], (T)d.spheres[4 * i + 2]};
@@ -1272,7 +1273,7 @@ template <class P> struct Scene {
     }
     for (uint32_t i = 0; i < nb; ++i) obj(OBJ_BOX, i, boxes[i].aabb(), box_xf[i]);
     for (uint32_t i = 0; i < nv; ++i)
-      obj(OBJ_VOLUME, i, volumes[i].boundary == RG_BOUNDARY_SPHERE ? volumes[i].s.aabb() : volumes[i].b.aabb(), -1);
+      obj(OBJ_VOLUME, i, volumes[i].boundary == RG_BOUNDARY_SPHERE ? volumes[i].s.aabb() : volumes[i].b.aabb(), vol_xf[i]);
     for (uint32_t i = 0; i < nq; ++i) obj(OBJ_QUAD, i, quads[i].aabb(), quad_xf[i]);
     for (uint32_t i = 0; i < nc; ++i) obj(OBJ_CYLINDER, i, cylinders[i].aabb(), cyl_xf[i]);
     for (uint32_t i = 0; i < nsdf; ++i) unbounded.push_back({false, i});

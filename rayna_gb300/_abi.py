@@ -96,6 +96,7 @@ class rg_scene_desc(C.Structure):
         ("cylinder_transform", C.POINTER(C.c_uint32)),
         ("n_textures", C.c_uint32), ("textures", C.POINTER(rg_texture)),
         ("n_images", C.c_uint32), ("images", C.POINTER(rg_image)), ("sky_image", C.c_uint32),
+        ("volume_transform", C.POINTER(C.c_uint32)),
     ]
 
 

@@ -250,6 +250,8 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
   if (n_vol > (uint32_t)kAdjMaxVolumes) return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward supports at most 4 media");
   if (h->host.textured)
     return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward differentiates solid albedos: no textures or image sky");
+  if (h->host.vol_transformed)
+    return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward's density scores need untransformed media");
   cudaStream_t st = h->stream;
   // Device scratch of the adjoint: image, target/adjoint image, gradients, loss.
   size_t need = (2 * npx3 + 2 * (size_t)n_mat * 3 + n_vol + 4) * sizeof(float) + sizeof(double) + 512;

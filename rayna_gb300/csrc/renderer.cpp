@@ -327,7 +327,7 @@ rg_status validate_scene(rg_renderer* h, const rg_scene_desc& d) {
   };
   if (!xf_ok(d.sphere_transform, d.n_spheres, "sphere") || !xf_ok(d.tri_transform, d.n_triangles, "triangle") ||
       !xf_ok(d.box_transform, d.n_boxes, "box") || !xf_ok(d.quad_transform, d.n_quads, "parallelogram") ||
-      !xf_ok(d.cylinder_transform, d.n_cylinders, "cylinder"))
+      !xf_ok(d.cylinder_transform, d.n_cylinders, "cylinder") || !xf_ok(d.volume_transform, d.n_volumes, "volume"))
     return RG_INVALID_ARG;
   for (uint32_t i = 0; i < d.n_cylinders; ++i) {
     const float* c = d.cylinders + 7ull * i;
@@ -452,8 +452,11 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
     setbox(id, mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]);
   }
   hs.vol_base = id;
+  hs.vol_transformed = false;
   for (uint32_t i = 0; i < hs.nv; ++i, ++id) {
     const rg_volume& v = d.volumes[i];
+    take_xf(d.volume_transform, i, id);
+    hs.vol_transformed = hs.vol_transformed || xf_of[id] != RG_NO_TRANSFORM;
     float nid = -1.0f / v.density;
     GpuPrim& p = prims[id];
     if (v.boundary == RG_BOUNDARY_SPHERE) {

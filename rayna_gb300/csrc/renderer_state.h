@@ -39,6 +39,7 @@ struct HostScene {
   std::vector<uint8_t> perm;           // 512 entries per noise source
   uint32_t sky_image = 0;
   bool textured = false;               // non-solid textures or an image sky
+  bool vol_transformed = false;        // a medium has an object transform
   std::vector<float> vol_density;      // per medium
   std::vector<uint32_t> vol_prim;      // per medium: position in `prims`
 };

@@ -750,10 +750,21 @@ class SimpleObject:
 
 @dataclass(eq=False)
 class VolumetricObject:
+    """object/volumetric.rs: a constant-density medium bounded by a sphere or
+    a box. `transform` is corrected about the mesh's centre, as
+    VolumetricObject::new does (volumetric.rs:21-30), unless `corrected` is
+    False (new_uncorrected)."""
     mesh: Any
     material: Any
     density: float
     transform: Any = None
+    corrected: bool = True
+
+    def object_transform(self) -> ObjectTransform:
+        t = ObjectTransform(_transform3(self.transform))
+        if self.corrected and not t.is_identity:
+            t = t.with_correction(self.mesh.centre())
+        return t
 
 
 class ObjectList(list):
@@ -799,6 +810,7 @@ class FlatScene:
         # per transformed object: its corrected 3 x 4 matrix; per primitive: its index
         self.transforms: list = []
         self.sphere_xf, self.tri_xf, self.box_xf, self.quad_xf, self.cyl_xf = [], [], [], [], []
+        self.vol_xf = []
         self.skybox = A.RG_SKY_SIMPLE
         self.n_meshes = 0
 
@@ -867,18 +879,11 @@ class FlatScene:
         if isinstance(obj, SimpleObject):
             mesh, mat = obj.mesh, self.material(obj.material)
             ot = obj.object_transform()
-            xf = A.RG_NO_TRANSFORM
-            if not ot.is_identity:
-                if isinstance(mesh, (RaymarchedIsosurfaceMesh, InfinitePlaneMesh)):
-                    raise UnsupportedVariant(f"a transformed {type(mesh).__name__} is not supported by the GPU path")
-                if not np.all(np.isfinite(ot.transform.matrix)) or abs(np.linalg.det(ot.transform.matrix[:3, :3])) == 0:
-                    raise ValueError("an object transform must be finite and invertible")
-                xf = len(self.transforms)
-                self.transforms.append(ot.transform.matrix[:3].copy())
-            self._add_mesh(mesh, mat, xf)
+            if not ot.is_identity and isinstance(mesh, (RaymarchedIsosurfaceMesh, InfinitePlaneMesh)):
+                raise UnsupportedVariant(f"a transformed {type(mesh).__name__} is not supported by the GPU path")
+            self._add_mesh(mesh, mat, self._transform_index(ot))
         elif isinstance(obj, VolumetricObject):
-            if not _identity(obj.transform):
-                raise UnsupportedVariant("a transformed VolumetricObject is not supported by the GPU path")
+            self.vol_xf.append(self._transform_index(obj.object_transform()))
             v = A.rg_volume()
             if isinstance(obj.mesh, SphereMesh):
                 v.boundary = A.RG_BOUNDARY_SPHERE
@@ -895,6 +900,17 @@ class FlatScene:
             self.volumes.append(v)
         else:
             raise UnsupportedVariant(f"object {type(obj).__name__} cannot cross the C ABI")
+
+    def _transform_index(self, ot: ObjectTransform) -> int:
+        """The index of an object's (corrected) transform in the transform
+        table, or RG_NO_TRANSFORM for the identity."""
+        if ot.is_identity:
+            return A.RG_NO_TRANSFORM
+        m = ot.transform.matrix
+        if not np.all(np.isfinite(m)) or abs(np.linalg.det(m[:3, :3])) == 0:
+            raise ValueError("an object transform must be finite and invertible")
+        self.transforms.append(m[:3].copy())
+        return len(self.transforms) - 1
 
     def _add_mesh(self, mesh, mat: int, xf: int):
         """One mesh of a SimpleObject (or of a BvhMesh) with its material and
@@ -990,6 +1006,7 @@ class FlatScene:
         self.a_box_xf = np.ascontiguousarray(np.asarray(self.box_xf, u32))
         self.a_quad_xf = np.ascontiguousarray(np.asarray(self.quad_xf, u32))
         self.a_cyl_xf = np.ascontiguousarray(np.asarray(self.cyl_xf, u32))
+        self.a_vol_xf = np.ascontiguousarray(np.asarray(self.vol_xf, u32))
         self.c_volumes = (A.rg_volume * max(1, len(self.volumes)))(*self.volumes)
         self.c_sdfs = (A.rg_sdf * max(1, len(self.sdfs)))(*self.sdfs)
         self.c_materials = (A.rg_material * max(1, len(self.materials)))(*self.materials)
@@ -1024,6 +1041,7 @@ class FlatScene:
             d.sphere_transform, d.tri_transform = up(self.a_sphere_xf), up(self.a_tri_xf)
             d.box_transform, d.quad_transform = up(self.a_box_xf), up(self.a_quad_xf)
             d.cylinder_transform = up(self.a_cyl_xf)
+            d.volume_transform = up(self.a_vol_xf)
         self.desc = d
         return self
 

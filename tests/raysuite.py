@@ -55,10 +55,18 @@ def box_scene(seed=0):
     return Scene(objects=objs)
 
 
-def volume_scene():
+def volume_scene(transformed=False):
+    """Two media (a sphere and a box) and two spheres; with `transformed` the
+    box medium is turned 30 degrees about a tilted axis and the sphere medium
+    moved, both as object transforms."""
+    from rayna_gb300.scene import Angle, Transform3
+    turn = Transform3.from_axis_angle(np.array([0.3, 1.0, 0.2]) / np.linalg.norm([0.3, 1.0, 0.2]),
+                                      Angle.from_degrees(30.0)) if transformed else None
+    move = Transform3.from_translation((0.1, 0.15, -0.1)) if transformed else None
     objs = [
-        VolumetricObject(SphereMesh((0.0, 0.0, 0.0), 1.0), IsotropicMaterial((0.8, 0.8, 0.8), 0.0), 0.7),
-        VolumetricObject(AxisBoxMesh((1.5, -0.5, -0.5), (2.5, 0.5, 0.5)), IsotropicMaterial((0.5, 0.6, 0.7), 0.0), 1.5),
+        VolumetricObject(SphereMesh((0.0, 0.0, 0.0), 1.0), IsotropicMaterial((0.8, 0.8, 0.8), 0.0), 0.7, move),
+        VolumetricObject(AxisBoxMesh((1.5, -0.5, -0.5), (2.5, 0.5, 0.5)), IsotropicMaterial((0.5, 0.6, 0.7), 0.0), 1.5,
+                         turn),
         SimpleObject(SphereMesh((0.3, 0.0, 0.0), 0.3), LambertianMaterial((0.5, 0.5, 0.5))),
         SimpleObject(SphereMesh((-3.0, 0.0, 0.0), 0.5), LambertianMaterial((0.5, 0.5, 0.5))),
     ]

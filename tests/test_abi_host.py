@@ -132,9 +132,9 @@ def test_flatten_order_and_unsupported_variants():
     with pytest.raises(UnsupportedVariant):
         flatten(Scene(objects=[SimpleObject(RaymarchedIsosurfaceMesh(SdfTorus((0, 0, 0), 1.0, 0.3)),
                                             LambertianMaterial(), transform=scaled)]))
-    with pytest.raises(UnsupportedVariant):
-        flatten(Scene(objects=[VolumetricObject(SphereMesh((0, 0, 0), 1.0), IsotropicMaterial((1, 1, 1)), 0.5,
-                                                transform=scaled)]))
+    flat = flatten(Scene(objects=[VolumetricObject(SphereMesh((0, 0, 0), 1.0), IsotropicMaterial((1, 1, 1)), 0.5,
+                                                   transform=scaled)]))
+    assert flat.desc.n_transforms == 1 and flat.desc.volume_transform[0] == 0
     with pytest.raises(ValueError):
         flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0), LambertianMaterial(),
                                             transform=Transform3.from_scale((1, 0, 1)))]))

@@ -193,9 +193,10 @@ def test_query_bit_exact_vs_f32_oracle(suite, bvh_width):
 
 
 @pytest.mark.parametrize("bvh_width", [2, 8])
-def test_query_volumes_injected_uniforms(bvh_width):
+@pytest.mark.parametrize("transformed", [False, True])
+def test_query_volumes_injected_uniforms(bvh_width, transformed):
     rng = np.random.Generator(np.random.PCG64(5))
-    scene = volume_scene()
+    scene = volume_scene(transformed)
     flat = flatten(scene)
     o, d = rays_at(rng, 20000, (-1.2, -1.2, -1.2), (2.7, 1.2, 1.2), inside_frac=0.3)
     u = rng.uniform(1e-6, 1.0, (len(o), flat.desc.n_volumes)).astype(np.float32)

@@ -170,3 +170,37 @@ def test_cornell_preset_rotated_boxes():
         h, t, _ = q(flat, (0.381, 0.9, 0.2655), (0, -1, 0), policy)
         assert h["hit"] == 1 and abs(t - (0.9 - 0.595)) < 1e-5
         np.testing.assert_allclose(h["normal"], (0, 1, 0), atol=1e-6)
+
+
+@pytest.mark.parametrize("policy", POLICIES)
+def test_transformed_medium_known_answers(policy):
+    """VolumetricObject's transform (object/volumetric.rs:21-45, 92): the
+    medium is entered and left in mesh space; the free-flight distance
+    -ln(u) / density is added to the entry. A unit sphere medium of density
+    0.5 moved to z = 5: a ray from the origin along +z enters at 4, so u =
+    exp(-0.5) puts the hit at 4 + 1."""
+    from rayna_gb300.scene import IsotropicMaterial, VolumetricObject
+    med = VolumetricObject(SphereMesh((0, 0, 0), 1.0), IsotropicMaterial((0.5, 0.5, 0.5), 0.0), 0.5,
+                           Transform3.from_translation((0, 0, 5)))
+    flat = flatten(Scene(objects=[med]))
+    u = np.array([[math.exp(-0.5)]], np.float32)
+    h, t, _ = ob.query(flat, np.zeros((1, 3), np.float32), np.array([[0, 0, 1]], np.float32), volume_u=u,
+                       policy=policy, pretest=True)
+    assert h[0]["hit"] == 1 and abs(t[0] - 5.0) < 1e-5
+    u = np.array([[math.exp(-0.5 * 2.5)]], np.float32)  # 2.5 > the 2 units inside: passes through
+    h, _, _ = ob.query(flat, np.zeros((1, 3), np.float32), np.array([[0, 0, 1]], np.float32), volume_u=u,
+                       policy=policy, pretest=True)
+    assert h[0]["hit"] == 0
+    # a box medium scatters nowhere, turned or not: VolumetricObject asks its
+    # mesh for the exit from the same origin with the interval moved past the
+    # entry, and AxisBoxMesh::intersect (axis_box.rs:64-145) only ever returns
+    # the faces it would cross first from that origin (the entry faces from
+    # outside, the exit face from inside)
+    for xf in (None, Transform3.from_axis_angle(Y, Angle.from_degrees(90))):
+        box = VolumetricObject(AxisBoxMesh((-1, -0.5, -0.25), (1, 0.5, 0.25)), IsotropicMaterial((0.5, 0.5, 0.5), 0.0),
+                               1.0, xf)
+        flat = flatten(Scene(objects=[box]))
+        for o in ((5.0, 0.1, 0.2), (0.1, 0.1, 0.1)):
+            h, _, _ = ob.query(flat, np.array([o], np.float32), np.array([[-1, 0, 0]], np.float32),
+                               volume_u=np.array([[0.999]], np.float32), policy=policy, pretest=True)
+            assert h[0]["hit"] == 0
