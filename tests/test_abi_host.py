@@ -196,3 +196,32 @@ def test_flatten_textures_and_images():
     flat = flatten(Scene(objects=[SimpleObject(SphereMesh((0, 0, 0), 1.0),
                                                LambertianMaterial(UvCheckerTexture(even=(1, 1, 1), odd=(0, 0, 0))))]))
     assert flat.desc.n_textures == 3 and flat.materials[0].texture == 3
+
+
+def test_ctypes_layout_equals_the_c_header(tmp_path):
+    """Every ctypes structure has the C header's size and, field by field,
+    its offsets (a small C program built with the host compiler prints them)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = [getattr(A, n) for n in dir(A) if n.startswith("rg_") and isinstance(getattr(A, n), type)
+               and issubclass(getattr(A, n), C.Structure)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rayna_gpu.h"', 'int main(void) {']
+    for s in structs:
+        lines.append(f'  printf("{s.__name__} size %zu\\n", sizeof({s.__name__}));')
+        for name, _ in s._fields_:
+            lines.append(f'  printf("{s.__name__} {name} %zu\\n", offsetof({s.__name__}, {name}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], check=True, stdout=subprocess.PIPE, text=True).stdout.split("\n")
+    want = []
+    for s in structs:
+        want.append(f"{s.__name__} size {C.sizeof(s)}")
+        for name, _ in s._fields_:
+            want.append(f"{s.__name__} {name} {getattr(s, name).offset}")
+    assert [g for g in got if g] == want
