@@ -225,3 +225,18 @@ def test_ctypes_layout_equals_the_c_header(tmp_path):
         for name, _ in s._fields_:
             want.append(f"{s.__name__} {name} {getattr(s, name).offset}")
     assert [g for g in got if g] == want
+
+
+@pytest.mark.parametrize("preset", ["cornell", "cornell_quads", "rtiaw_demo", "rttnw_demo", "textures_demo",
+                                    "sdf_volumes"])
+def test_inspect_every_preset(preset):
+    """The host side of rg_set_scene (validation, transforms, textures, both
+    trees) accepts every preset; the tree holds every bounded primitive (SDFs
+    and infinite planes stay in the unbounded list)."""
+    scene, _, _ = getattr(presets, preset)()
+    flat = flatten(scene)
+    st, info, _ = inspect(scene)
+    assert st == A.RG_OK, A.last_error(A.load_library(), None)
+    d = flat.desc
+    assert info.n_prims == d.n_spheres + d.n_triangles + d.n_boxes + d.n_volumes + d.n_quads + d.n_cylinders
+    assert info.max_depth < 60
