@@ -538,3 +538,67 @@ def rttnw_demo(seed: int = 0, width: int = 400, height: int = 400, spp: int = 64
                  focus_dist=1.0, defocus_angle=Angle(0.0))
     return Scene(objects=objs, skybox=NoSkybox()), cam, RenderOpts(width=width, height=height, samples=spp,
                                                                      ray_depth=ray_depth)
+
+
+def rtiaw_demo_dark(seed: int = 0, width: int = 400, height: int = 225, spp: int = 32, ray_depth: int = 50):
+    """The reference's RTIAW_DEMO_DARK preset (scene/preset.rs:257-392), its
+    random draws from PCG64(seed) instead of thread_rng: the RTIAW grid with
+    5 % emissive objects, a sparse second grid of bright lights at y = 3.2, the
+    three r = 1 spheres, and an infinite ground plane with
+    LocalNoiseTexture(Perlin(69) scaled by 10000), under no sky. Returns
+    (scene, camera, opts)."""
+    from .scene import ColourSource, InfinitePlaneMesh, LocalNoiseTexture, NoSkybox, Perlin, Planar, ScalePoint
+    rng = np.random.Generator(np.random.PCG64(seed))
+    objs = []
+    big = np.array([4.0, 0.2, 0.0])
+    for a in range(-15, 16):
+        for b in range(-15, 16):
+            centre = np.array([a, 0.2, b], float) + np.array([rng.random(), 0.0, rng.random()]) * 0.9
+            if np.linalg.norm(centre - big) <= 1.0:
+                continue
+            choice = rng.random()
+            if choice < 0.6:
+                mat = LambertianMaterial(tuple(rng.random(3) * rng.random(3)))
+            elif choice <= 0.8:
+                mat = MetalMaterial(tuple(rng.uniform(0.5, 1.0, 3)), float(rng.uniform(0.0, 0.5)))
+            elif choice <= 0.95:
+                mat = DielectricMaterial(tuple(rng.uniform(0.5, 1.0, 3)), float(rng.uniform(1.0, 10.0)), 69.0)
+            else:
+                mat = LightMaterial(tuple(rng.uniform(0.0, 0.8, 3)))
+            mesh = SphereMesh(tuple(centre), 0.2) if rng.random() < 0.7 else AxisBoxMesh.new_centred(
+                centre, rng.random(3) * 0.8)
+            objs.append(SimpleObject(mesh, mat))
+    for a in range(-15, 16):
+        for b in range(-15, 16):
+            centre = np.array([a, 3.2, b], float) + np.array([rng.random(), 0.0, rng.random()]) * 0.9
+            if np.linalg.norm(centre - big) <= 1.8:
+                continue
+            mat = LightMaterial(tuple(rng.uniform(10.0, 50.0, 3)))
+            choice = rng.random()
+            if choice <= 0.99:
+                continue
+            mesh = SphereMesh(tuple(centre), 0.2) if choice <= 0.995 else AxisBoxMesh.new_centred(
+                centre, rng.random(3) * 0.8)
+            objs.append(SimpleObject(mesh, mat))
+    objs.append(SimpleObject(SphereMesh((0.0, 1.0, 0.0), 1.0), DielectricMaterial((1.0, 1.0, 1.0), 1.5, 69.0)))
+    objs.append(SimpleObject(SphereMesh((-4.0, 1.0, 0.0), 1.0), LambertianMaterial((0.4, 0.2, 0.1))))
+    objs.append(SimpleObject(SphereMesh((4.0, 1.0, 0.0), 1.0), MetalMaterial((0.7, 0.6, 0.5), 0.0)))
+    ground = LocalNoiseTexture(ColourSource.Greyscale(ScalePoint(Perlin(69)).set_scale(10000.0)))
+    objs.append(SimpleObject(InfinitePlaneMesh(Planar.new((0, 0, 0), (1, 0, 0), (0, 0, 1)), uv_wrap="wrap"),
+                             LambertianMaterial(ground)))
+    fwd = np.array([-13.0, -2.0, -3.0])
+    cam = Camera(pos=(13.0, 2.0, 3.0), fwd=tuple(fwd / np.linalg.norm(fwd)), v_fov=Angle.from_degrees(20.0),
+                 focus_dist=10.0, defocus_angle=Angle.from_degrees(0.6))
+    return Scene(objects=objs, skybox=NoSkybox()), cam, RenderOpts(width=width, height=height, samples=spp,
+                                                                     ray_depth=ray_depth)
+
+
+def ALL(seed: int = 0) -> list:  # noqa: N802 (preset::ALL, scene/preset.rs:65)
+    """The reference's presets that run on this library, as (name, scene,
+    camera, opts): its RTIAW_DEMO, RTIAW_DEMO_DARK, RTTNW_DEMO and CORNELL
+    (TESTING needs a polygonised isosurface)."""
+    out = []
+    for name, fn in (("RTIAW Demo", rtiaw_demo), ("RTIAW Demo (Night)", rtiaw_demo_dark), ("RTTNW Demo", rttnw_demo)):
+        out.append((name, *fn(seed=seed)))
+    out.append(("Cornell Box", *cornell()))
+    return out

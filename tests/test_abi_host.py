@@ -227,8 +227,8 @@ def test_ctypes_layout_equals_the_c_header(tmp_path):
     assert [g for g in got if g] == want
 
 
-@pytest.mark.parametrize("preset", ["cornell", "cornell_quads", "rtiaw_demo", "rttnw_demo", "textures_demo",
-                                    "sdf_volumes"])
+@pytest.mark.parametrize("preset", ["cornell", "cornell_quads", "rtiaw_demo", "rtiaw_demo_dark", "rttnw_demo",
+                                    "textures_demo", "sdf_volumes"])
 def test_inspect_every_preset(preset):
     """The host side of rg_set_scene (validation, transforms, textures, both
     trees) accepts every preset; the tree holds every bounded primitive (SDFs
@@ -240,3 +240,18 @@ def test_inspect_every_preset(preset):
     d = flat.desc
     assert info.n_prims == d.n_spheres + d.n_triangles + d.n_boxes + d.n_volumes + d.n_quads + d.n_cylinders
     assert info.max_depth < 60
+
+
+def test_all_reference_presets_render_on_the_oracle():
+    """presets.ALL() (preset::ALL): each scene flattens, builds on the host,
+    and renders a few pixels on the f64 oracle with finite, non-negative
+    colours."""
+    from oracle import binding as ob
+    from rayna_gb300.scene import RenderOpts
+    names = []
+    for name, scene, cam, _ in presets.ALL():
+        names.append(name)
+        assert inspect(scene)[0] == A.RG_OK
+        st, mean, _, _ = ob.render(flatten(scene), cam, RenderOpts(width=8, height=6, samples=2, ray_depth=4), seed=3)
+        assert st == 0 and np.all(np.isfinite(mean)) and np.all(mean >= 0)
+    assert names == ["RTIAW Demo", "RTIAW Demo (Night)", "RTTNW Demo", "Cornell Box"]
