@@ -204,3 +204,25 @@ def test_transformed_medium_known_answers(policy):
             h, _, _ = ob.query(flat, np.array([o], np.float32), np.array([[-1, 0, 0]], np.float32),
                                volume_u=np.array([[0.999]], np.float32), policy=policy, pretest=True)
             assert h[0]["hit"] == 0
+
+
+def test_quarter_turn_equals_the_swapped_box():
+    """A box turned 90 degrees about Y about its centre (SimpleObject::new's
+    correction) is the axis-aligned box with its x and z extents swapped: the
+    f64 oracle renders the two scenes alike, path for path up to rounding."""
+    from rayna_gb300.scene import RenderOpts
+    scene, cam, _ = presets.cornell()
+    opts = RenderOpts(width=24, height=24, samples=4, ray_depth=4)
+    objs = list(scene.objects[:6])
+    c = np.array([0.381, 0.2975, 0.2655])
+    half = np.array([0.15, 0.2975, 0.1485])
+    turned = SimpleObject(AxisBoxMesh(tuple(c - half), tuple(c + half)), LambertianMaterial((0.85, 0.74, 0.55)),
+                          Transform3.from_axis_angle(Y, Angle.from_degrees(90)))
+    swapped = half[[2, 1, 0]]
+    plain = SimpleObject(AxisBoxMesh(tuple(c - swapped), tuple(c + swapped)), LambertianMaterial((0.85, 0.74, 0.55)))
+    a = ob.render(flatten(Scene(objects=objs + [turned], skybox=scene.skybox)), cam, opts, seed=5,
+                  policy=ob.POLICY_REF_F64, gpu_sampling=True)[1]
+    b = ob.render(flatten(Scene(objects=objs + [plain], skybox=scene.skybox)), cam, opts, seed=5,
+                  policy=ob.POLICY_REF_F64, gpu_sampling=True)[1]
+    close = np.all(np.abs(a - b) <= 1e-6 * (1 + np.abs(b)), axis=2)
+    assert close.mean() >= 0.98, close.mean()
