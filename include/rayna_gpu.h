@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 6u
+#define RG_ABI_VERSION 7u
 
 /* Status codes. 0 is success. */
 typedef enum rg_status {
@@ -294,7 +294,7 @@ typedef struct rg_render_stats {
     uint32_t img_width;       /* dimensions of the image written to out_rgb */
     uint32_t img_height;
     uint32_t num_threads;     /* 0: the device renders */
-    uint32_t error_flags;     /* device-side error bits seen this frame (0 = none) */
+    uint32_t error_flags;     /* device-side error bits seen this frame (0 = none): RG_DEVICE_* */
     uint32_t kernel_launches; /* kernels the library launched for this frame */
     double traverse_ms;       /* device time of the frame's traversal kernels (RG_FLAG_STAGE_TIMES only, else 0):
                                  the megakernel, or the wavefront's extend / bounce launches */
@@ -302,6 +302,18 @@ typedef struct rg_render_stats {
     uint32_t invalid_mask;    /* RG_FLAG_VALIDATE: RG_INVALID_* bits of the invariants broken */
     uint32_t reserved0;
 } rg_render_stats;
+
+/* Device error bits (rg_render_stats.error_flags). They are cleared at the start
+ * of every frame (and every query or backward call); a frame that sets any of
+ * them returns a status other than RG_OK from rg_render, rg_sync_stats,
+ * rg_batch_render and rg_query_rays, while the image is still written:
+ *   RG_DEVICE_STACK_OVERFLOW, RG_DEVICE_QUEUE_OVERFLOW -> RG_QUEUE_OVERFLOW
+ *   RG_DEVICE_BAD_INDEX (a damaged tree: the traversal's visit guard ran out) -> RG_STEP_LIMIT */
+enum {
+    RG_DEVICE_STACK_OVERFLOW = 1u,  /* a ray needed more traversal stack than it may use; its far subtree was dropped */
+    RG_DEVICE_BAD_INDEX = 2u,       /* a node or primitive index out of range, or a node visited twice */
+    RG_DEVICE_QUEUE_OVERFLOW = 4u   /* a path queue ran out of slots; the path was dropped */
+};
 
 /* Invariants of RG_FLAG_VALIDATE (shared/validate.rs:21-197). */
 enum {
@@ -378,8 +390,16 @@ typedef struct rg_tuning {
                                  Either tree gives the same closest hits. */
     uint32_t fetch_budget;    /* wavefront: node visits a lane traverses between refills of idle lanes; 0 = 8
                                  (6 for scenes of spheres only) */
-    uint32_t reserved[4];     /* must be 0 */
+    uint32_t shared_stack;    /* entries of each thread's traversal stack kept in shared memory (the deeper ones
+                                 live in local memory): 0 = library default (8 for scenes of triangles only, else
+                                 none), RG_SHARED_STACK_NONE = all in local memory, else 4, 8 or 16 */
+    uint32_t block;           /* megakernel: threads per block, 64, 128 or 256; 0 = 256 */
+    uint32_t stack_limit;     /* test knob: traversal stack entries a ray may use (1-64); a ray that needs more
+                                 drops the far subtree and the frame reports RG_QUEUE_OVERFLOW; 0 = all 64 */
+    uint32_t reserved[1];     /* must be 0 */
 } rg_tuning;
+
+#define RG_SHARED_STACK_NONE 0xFFFFFFFFu
 
 rg_status rg_set_tuning(rg_handle h, const rg_tuning* t);
 /* The knobs in effect: library defaults appear resolved (never 0). */
@@ -413,6 +433,22 @@ rg_status rg_render_async(rg_handle h, uint64_t seed, float* d_out_rgb, rg_rende
 /* Waits for the handle's stream and fills device timings and counters of the
  * last queued frame. */
 rg_status rg_sync_stats(rg_handle h, rg_render_stats* out_stats);
+
+/* Splits one frame across devices by sample range (no reference counterpart:
+ * the reference folds every sample of a pixel on one machine,
+ * render/renderer.rs:313-336 and accum_buffer.rs:37-42). After this call each
+ * frame of the handle traces only samples [first, first + count) of every
+ * pixel's `samples`, with the random streams those samples have in a whole
+ * frame, and adds their sum divided by `samples` to the accumulation buffer.
+ * Handles that cover disjoint ranges of [0, samples) with the same frame keys
+ * therefore hold accumulation sums whose element-wise sum is the whole
+ * frames' sum (up to float summation order), with the same frame count: the
+ * exchange is one sum-reduce of rg_get_accumulation's sums. count 0 restores
+ * whole frames. Clears the accumulation; rg_set_options restores whole
+ * frames. rg_frame_moments then describes the range's samples, and
+ * rg_backward_frame refuses a sharded frame (RG_NOT_READY). first + count
+ * above `samples` is RG_INVALID_ARG. */
+rg_status rg_set_sample_range(rg_handle h, uint32_t first, uint32_t count);
 
 /* Checkpoint/resume of the AccumulationBuffer (accum_buffer.rs:9-78):
  * `sum` is width*height*3 floats in [x][y][rgb] order, `frames` the count. */
@@ -521,7 +557,7 @@ rg_status rg_backward(rg_handle h, uint64_t seed, const float* adjoint_rgb, cons
 rg_status rg_backward_frame(rg_handle h, uint64_t seed, const float* target_rgb, rg_gradients* out);
 
 /* Path slots of the fixed device array used by rg_render_static_scratch
- * (31 x 4 bytes each: about 8 MB, held by every device that loads the library). */
+ * (108 bytes each: about 7 MB, held by every device that loads the library). */
 #define RG_STATIC_WAVE_PATHS 65536u
 
 /* No counterpart in the reference: the reference renders on the CPU and never
@@ -547,7 +583,10 @@ rg_status rg_backward_frame(rg_handle h, uint64_t seed, const float* target_rgb,
  * call shares the one array and finds it as the last call left it: calls whose
  * kernels overlap on the GPU (other streams, other handles) race. Samples per
  * pixel above RG_STATIC_WAVE_PATHS are rejected with RG_INVALID_ARG. Returns
- * once the kernels are queued on the handle's stream. */
+ * once the kernels are queued on the handle's stream; rg_sync_stats then
+ * reports this frame (device time, samples, launches, counters, error bits and
+ * their status). RG_FLAG_STAGE_TIMES is not honoured here (its events are
+ * created on demand): traverse_ms reads 0. */
 rg_status rg_render_static_scratch(rg_handle h, uint64_t seed, float* d_accum, uint32_t accum_count, float* d_out);
 
 #ifdef __cplusplus

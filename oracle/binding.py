@@ -36,6 +36,11 @@ def lib():
         L.orc_render.argtypes = [C.POINTER(A.rg_scene_desc), C.POINTER(A.rg_camera), C.POINTER(A.rg_render_opts),
                                  C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_int, dp, dp, dp]
         L.orc_render.restype = C.c_int
+        L.orc_render_window.argtypes = [C.POINTER(A.rg_scene_desc), C.POINTER(A.rg_camera),
+                                        C.POINTER(A.rg_render_opts), C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_int,
+                                        C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                        dp, dp, dp]
+        L.orc_render_window.restype = C.c_int
         L.orc_hardware_threads.restype = C.c_int
         L.orc_query_colour.argtypes = [C.POINTER(A.rg_scene_desc), C.c_int, C.c_uint32, fp, fp, fp]
         L.orc_query_colour.restype = C.c_int
@@ -108,6 +113,24 @@ def render(flat, camera, opts, seed=0, frames=1, policy=POLICY_REF_F64, gpu_samp
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     st = lib().orc_render(C.byref(flat.desc), C.byref(camera.to_c()), C.byref(opts.to_c()), int(seed), int(frames),
                           int(policy), 1 if gpu_sampling else 0, int(threads), dp(mean), dp(var), C.byref(secs))
+    return st, mean, var, secs.value
+
+
+def render_window(flat, camera, opts, window, seed=0, frames=1, policy=POLICY_REF_F64, gpu_sampling=False,
+                  threads=0, samples=None):
+    """Renders the pixels window = (x0, y0, w, h) of the full frame (the
+    frame's own pixel coordinates and random streams) and, with `samples` =
+    (first, count), only those samples of each pixel. Returns (status, mean
+    (w,h,3), var (w,h,3), seconds) over the traced samples."""
+    x0, y0, ww, wh = (int(v) for v in window)
+    s0, ns = (0, 0) if samples is None else (int(samples[0]), int(samples[1]))
+    mean = np.zeros((ww, wh, 3))
+    var = np.zeros((ww, wh, 3))
+    secs = C.c_double(0.0)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    st = lib().orc_render_window(C.byref(flat.desc), C.byref(camera.to_c()), C.byref(opts.to_c()), int(seed),
+                                 int(frames), int(policy), 1 if gpu_sampling else 0, int(threads), x0, y0, ww, wh, s0,
+                                 ns, dp(mean), dp(var), C.byref(secs))
     return st, mean, var, secs.value
 
 

@@ -46,17 +46,25 @@ int query_impl(const rg_scene_desc* d, int pretest, uint32_t n, const float* o, 
   return 0;
 }
 
+// Renders the window [x0, x0 + ww) x [y0, y0 + wh) of the W x H frame (the
+// same pixels, samples and random streams as in the whole frame), samples
+// [s0, s0 + ns) of each pixel's opts->samples (ns 0: all), `frames` frames.
+// out_mean / out_var are ww x wh x 3, [x][y][rgb] within the window.
 template <class P>
 int render_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_opts* opts, uint64_t seed, uint32_t frames,
-                int gpu_sampling, int threads, double* out_mean, double* out_var, double* out_seconds) {
+                int gpu_sampling, int threads, uint32_t x0, uint32_t y0, uint32_t ww, uint32_t wh, uint32_t s0,
+                uint32_t ns, double* out_mean, double* out_var, double* out_seconds) {
   Viewport vp;
   if (!calculate_viewport(*cam, vp)) return RG_INVALID_CAMERA;
   if (opts->width == 0 || opts->height == 0 || opts->samples == 0 || opts->ray_branching == 0) return RG_INVALID_ARG;
   if (opts->mode > RG_MODE_SIDE) return RG_UNSUPPORTED_VARIANT;
+  const uint32_t W = opts->width, H = opts->height;
+  if (ww == 0 || wh == 0 || (uint64_t)x0 + ww > W || (uint64_t)y0 + wh > H) return RG_INVALID_ARG;
+  if (ns == 0) { s0 = 0; ns = opts->samples; }
+  if ((uint64_t)s0 + ns > opts->samples) return RG_INVALID_ARG;
   Scene<P> sc;
   sc.load(*d, Options{});
-  const uint32_t W = opts->width, H = opts->height;
-  std::vector<double> sum((size_t)W * H * 3, 0.0), sq((size_t)W * H * 3, 0.0);
+  std::vector<double> sum((size_t)ww * wh * 3, 0.0), sq((size_t)ww * wh * 3, 0.0);
   if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
   auto t0 = std::chrono::steady_clock::now();
   for (uint32_t f = 0; f < frames; ++f) {
@@ -68,12 +76,14 @@ int render_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_op
     std::atomic<uint32_t> next_row{0};
     auto work = [&]() {
       for (;;) {
-        uint32_t y = next_row.fetch_add(1);
-        if (y >= H) break;
-        for (uint32_t x = 0; x < W; ++x) {
+        uint32_t yy = next_row.fetch_add(1);
+        if (yy >= wh) break;
+        const uint32_t y = y0 + yy;
+        for (uint32_t xx = 0; xx < ww; ++xx) {
+          const uint32_t x = x0 + xx;
           SeqRng msaa(fseed, y * W + x, 0xFFFFFFFFu, 0x4d5341u);
-          size_t o = ((size_t)x * H + y) * 3;
-          for (uint32_t s = 0; s < opts->samples; ++s) {
+          size_t o = ((size_t)xx * wh + yy) * 3;
+          for (uint32_t s = s0; s < s0 + ns; ++s) {
             C3 c = R.sample(x, y, s, gpu_sampling != 0, &msaa);
             double v[3] = {c.r, c.g, c.b};
             for (int k = 0; k < 3; ++k) { sum[o + k] += v[k]; sq[o + k] += v[k] * v[k]; }
@@ -88,7 +98,7 @@ int render_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_op
   }
   auto t1 = std::chrono::steady_clock::now();
   if (out_seconds) *out_seconds = std::chrono::duration<double>(t1 - t0).count();
-  const double N = (double)frames * opts->samples;
+  const double N = (double)frames * ns;
   for (size_t i = 0; i < sum.size(); ++i) {
     double m = sum[i] / N;
     if (out_mean) out_mean[i] = m;
@@ -108,7 +118,7 @@ int backward_impl(const rg_scene_desc* d, const rg_camera* cam, const rg_render_
   double l = 0.0;
   if (target) {
     std::vector<double> img(n3);
-    int st = render_impl<P>(d, cam, opts, seed, 1, 1, threads, img.data(), nullptr, nullptr);
+    int st = render_impl<P>(d, cam, opts, seed, 1, 1, threads, 0, 0, W, H, 0, 0, img.data(), nullptr, nullptr);
     if (st != RG_OK) return st;
     for (size_t i = 0; i < n3; ++i) {
       double e = img[i] - (double)target[i];
@@ -219,8 +229,24 @@ int orc_query(const rg_scene_desc* d, int policy, int pretest, uint32_t n, const
 // samplers and counter assignment (gpu_sampling is then forced on).
 int orc_render(const rg_scene_desc* d, const rg_camera* cam, const rg_render_opts* opts, uint64_t seed, uint32_t frames,
                int policy, int gpu_sampling, int threads, double* out_mean, double* out_var, double* out_seconds) {
-  if (policy == 0) return render_impl<RefF64>(d, cam, opts, seed, frames, gpu_sampling, threads, out_mean, out_var, out_seconds);
-  return render_impl<GpuF32>(d, cam, opts, seed, frames, 1, threads, out_mean, out_var, out_seconds);
+  const uint32_t W = opts->width, H = opts->height;
+  if (policy == 0)
+    return render_impl<RefF64>(d, cam, opts, seed, frames, gpu_sampling, threads, 0, 0, W, H, 0, 0, out_mean, out_var,
+                               out_seconds);
+  return render_impl<GpuF32>(d, cam, opts, seed, frames, 1, threads, 0, 0, W, H, 0, 0, out_mean, out_var, out_seconds);
+}
+
+// orc_render over the window [x0, x0 + ww) x [y0, y0 + wh) of the frame and
+// the samples [s0, s0 + ns) of each pixel (ns 0: all); the outputs are
+// ww x wh x 3, the mean and variance over the window's traced samples.
+int orc_render_window(const rg_scene_desc* d, const rg_camera* cam, const rg_render_opts* opts, uint64_t seed,
+                      uint32_t frames, int policy, int gpu_sampling, int threads, uint32_t x0, uint32_t y0, uint32_t ww,
+                      uint32_t wh, uint32_t s0, uint32_t ns, double* out_mean, double* out_var, double* out_seconds) {
+  if (policy == 0)
+    return render_impl<RefF64>(d, cam, opts, seed, frames, gpu_sampling, threads, x0, y0, ww, wh, s0, ns, out_mean, out_var,
+                               out_seconds);
+  return render_impl<GpuF32>(d, cam, opts, seed, frames, 1, threads, x0, y0, ww, wh, s0, ns, out_mean, out_var,
+                             out_seconds);
 }
 
 int orc_query_colour(const rg_scene_desc* d, int policy, uint32_t n, const float* o, const float* dir, float* rgb) {

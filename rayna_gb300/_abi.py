@@ -1,7 +1,10 @@
 """ctypes mirror of include/rayna_gpu.h and the loader of the native library.
 
-The library is built in-tree (``rayna_gb300/_lib/librayna_gpu.so``) by
-``__graft_entry__.build()``. Loading fails loudly when it is missing: there is
+The library is built in-tree by ``__graft_entry__.build()`` in two arithmetic
+builds of one source: ``rayna_gb300/_lib/librayna_gpu.so`` (the performance
+build, loaded by default) and ``librayna_gpu_exact.so`` (fused multiply-adds
+only where the source writes them, loaded with ``exact=True`` or
+RAYNA_GB300_EXACT=1). Loading fails loudly when a library is missing: there is
 no CPU fallback behind this package.
 """
 from __future__ import annotations
@@ -11,6 +14,7 @@ import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "librayna_gpu.so")
+LIB_EXACT_PATH = os.path.join(_HERE, "_lib", "librayna_gpu_exact.so")
 
 RG_OK = 0
 RG_INVALID_ARG = 1
@@ -47,6 +51,9 @@ RG_BATCH_WAVEFRONT = 0
 RG_UV_WRAP, RG_UV_MIRROR, RG_UV_CLAMP_ZERO = 0, 1, 2
 RG_NO_TRANSFORM = 0xFFFFFFFF
 RG_BATCH_TILES = 1
+RG_SHARED_STACK_NONE = 0xFFFFFFFF
+RG_DEVICE_STACK_OVERFLOW, RG_DEVICE_BAD_INDEX, RG_DEVICE_QUEUE_OVERFLOW = 1, 2, 4
+RG_ABI_VERSION = 7
 
 
 class rg_material(C.Structure):
@@ -132,7 +139,8 @@ class rg_scene_info(C.Structure):
 
 class rg_tuning(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("sort_materials", C.c_uint32), ("bvh_width", C.c_uint32),
-                ("fetch_budget", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+                ("fetch_budget", C.c_uint32), ("shared_stack", C.c_uint32), ("block", C.c_uint32),
+                ("stack_limit", C.c_uint32), ("reserved", C.c_uint32 * 1)]
 
 
 class rg_gradients(C.Structure):
@@ -190,9 +198,15 @@ SIGNATURES = {
     "rg_batch_item_seed": (C.c_uint64, [C.c_uint64, C.c_uint32]),
     "rg_backward": (C.c_int, [_P, C.c_uint64, _F, _F, C.POINTER(rg_gradients)]),
     "rg_backward_frame": (C.c_int, [_P, C.c_uint64, _F, C.POINTER(rg_gradients)]),
+    "rg_set_sample_range": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
 }
 
-_lib = None
+_libs = {}
+
+
+def default_exact() -> bool:
+    """Whether the arithmetic-contract build is the default (RAYNA_GB300_EXACT=1)."""
+    return os.environ.get("RAYNA_GB300_EXACT", "0") not in ("", "0")
 
 
 class RaynaError(RuntimeError):
@@ -203,22 +217,26 @@ class RaynaError(RuntimeError):
         self.status = status
 
 
-def load_library(path: str | None = None) -> C.CDLL:
-    """Loads librayna_gpu.so and binds every declared signature."""
-    global _lib
-    if _lib is not None and path is None:
-        return _lib
-    p = path or LIB_PATH
-    if not os.path.exists(p):
+def load_library(path: str | None = None, exact: bool | None = None) -> C.CDLL:
+    """Loads the native library and binds every declared signature: the
+    performance build, or the arithmetic-contract build with `exact` (default:
+    RAYNA_GB300_EXACT), or the library at `path`."""
+    if path is None:
+        if exact is None:
+            exact = default_exact()
+        path = LIB_EXACT_PATH if exact else LIB_PATH
+    lib = _libs.get(path)
+    if lib is not None:
+        return lib
+    if not os.path.exists(path):
         raise RuntimeError(
-            f"native library {p} is missing; build it with `python -c 'import __graft_entry__ as g; g.build()'`")
-    lib = C.CDLL(p)
+            f"native library {path} is missing; build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if path is None:
-        _lib = lib
+    _libs[path] = lib
     return lib
 
 

@@ -18,9 +18,10 @@ from .scene import flatten
 
 
 class BatchRenderer:
-    def __init__(self, items, *, device: int = 0, stream: int | None = None, seed: int = 0):
-        """`items`: list of (scene, camera, opts)."""
-        self._lib = A.load_library()
+    def __init__(self, items, *, device: int = 0, stream: int | None = None, seed: int = 0,
+                 exact: bool | None = None):
+        """`items`: list of (scene, camera, opts). `exact`: the arithmetic-contract build."""
+        self._lib = A.load_library(exact=exact)
         self.items = list(items)
         self._flats = [flatten(s) for s, _, _ in self.items]
         n = len(self.items)

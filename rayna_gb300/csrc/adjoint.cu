@@ -252,6 +252,8 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
     return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward differentiates solid albedos: no textures or image sky");
   if (h->host.vol_transformed)
     return set_error(h, RG_UNSUPPORTED_VARIANT, "rg_backward's density scores need untransformed media");
+  if (h->range_count)
+    return set_error(h, RG_NOT_READY, "rg_backward differentiates whole frames: reset the sample range first");
   cudaStream_t st = h->stream;
   // Device scratch of the adjoint: image, target/adjoint image, gradients, loss.
   size_t need = (2 * npx3 + 2 * (size_t)n_mat * 3 + n_vol + 4) * sizeof(float) + sizeof(double) + 512;
@@ -273,6 +275,7 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
   cudaError_t e;
   auto cuda_err = [&](cudaError_t err) { cudaGetLastError(); return set_error(h, RG_CUDA_ERROR, cudaGetErrorString(err)); };
   if ((e = cudaMemsetAsync(h->d_adj, 0, need, st)) != cudaSuccess) return cuda_err(e);
+  if ((e = cudaMemsetAsync(h->d_err, 0, sizeof(uint32_t), st)) != cudaSuccess) return cuda_err(e);
   FrameParams fp;
   fill_frame_params(h, seed, fp);
   if (target && last_frame) {
@@ -290,7 +293,7 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
     ff.frame_var = nullptr;
     ff.accum_count = 1;
     // the handle's kernel form renders it (both forms give the same image)
-    e = h->form == RG_FORM_WAVEFRONT ? launch_wavefront(h, ff) : launch_megakernel(h->gs, ff, false, st);
+    e = h->form == RG_FORM_WAVEFRONT ? launch_wavefront(h, ff) : launch_megakernel(h->gs, ff, false, st, h->mega_block);
     if (e != cudaSuccess) return cuda_err(e);
     if ((e = cudaMemcpyAsync(d_adjoint, target, npx3 * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return cuda_err(e);
@@ -313,8 +316,12 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
   if (out->density && n_vol && (e = cudaMemcpyAsync(out->density, d_gden, n_vol * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     return cuda_err(e);
   if ((e = cudaMemcpyAsync(&loss, d_loss, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return cuda_err(e);
+  uint32_t err = 0;
+  if ((e = cudaMemcpyAsync(&err, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return cuda_err(e);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e);
   out->loss = loss;
+  const rg_status dst = device_status(err);
+  if (dst != RG_OK) return set_error(h, dst, "rg_backward: device error bits set (traversal stack, queue or tree index)");
   return RG_OK;
 }
 

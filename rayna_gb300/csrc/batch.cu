@@ -66,6 +66,8 @@ __global__ void k_batch(const BatchItemDev* __restrict__ items, const uint32_t* 
   const uint32_t lane = threadIdx.x & 31;
   Counters cnt;
   uint32_t segments = 0;
+  uint2 stack_entries[kTravStack];
+  LocalStack stack{stack_entries};
   for (;;) {
     uint32_t w = 0;
     if (lane == 0) w = atomicAdd(counter, 1u);
@@ -85,7 +87,7 @@ __global__ void k_batch(const BatchItemDev* __restrict__ items, const uint32_t* 
     for (uint32_t r = 0; r < rounds_per_item; ++r) {
       uint32_t first = (round0 + r) * ppr;
       if (first >= n_pix) break;
-      mega_round<F, false>(sc, fp, first, n_pix, cnt, segments);
+      mega_round<F, false, kSamplePbr>(sc, fp, first, n_pix, cnt, segments, stack);
     }
   }
   FrameParams f0;
@@ -422,6 +424,14 @@ uint32_t batch_features(const rg_batch* b) {
   return b->features | (wide ? F_WIDE : 0u);
 }
 
+// Clears the error bits of the batch and of every render: each frame reports its own.
+cudaError_t clear_errors(rg_batch* b) {
+  cudaError_t e = cudaMemsetAsync(b->d_err, 0, sizeof(uint32_t), b->stream);
+  for (size_t i = 0; e == cudaSuccess && i < b->items.size(); ++i)
+    e = cudaMemsetAsync(b->items[i]->d_err, 0, sizeof(uint32_t), b->stream);
+  return e;
+}
+
 cudaError_t enqueue_frame(rg_batch* b) {
   cudaError_t e;
   if ((e = cudaMemcpyAsync(b->d_items, b->h_items, b->items.size() * sizeof(BatchItemDev), cudaMemcpyHostToDevice,
@@ -429,6 +439,7 @@ cudaError_t enqueue_frame(rg_batch* b) {
     return e;
   if ((e = cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), b->stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(b->d_counters, 0, CNT_N * sizeof(unsigned long long), b->stream)) != cudaSuccess) return e;
+  if ((e = clear_errors(b)) != cudaSuccess) return e;
   if (b->tuning.form == RG_BATCH_WAVEFRONT)
     return dispatch_features(batch_features(b), [&](auto f) { return launch_batch_wavefront<decltype(f)::value>(b); });
   b->launches = 1;
@@ -475,6 +486,8 @@ rg_status finish_stats(rg_batch* b, rg_render_stats* stats, std::chrono::steady_
   stats->error_flags = err;
   stats->kernel_launches = b->launches;
   stats->duration_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  const rg_status dst = device_status(err);
+  if (dst != RG_OK) return bfail(b, dst, "device error bits 0x%x this frame", err);
   return RG_OK;
 }
 
@@ -636,6 +649,7 @@ rg_status rg_batch_render_sequential(rg_batch_handle b, uint64_t seed, rg_render
   rg_status st = prepare_frame(b, seed);
   if (st != RG_OK) return st;
   BCUDA(b, cudaMemsetAsync(b->d_counters, 0, CNT_N * sizeof(unsigned long long), b->stream), "batch counters");
+  BCUDA(b, clear_errors(b), "batch error bits");
   BCUDA(b, cudaEventRecord(b->ev0, b->stream), "event");
   for (size_t i = 0; i < b->items.size(); ++i) {
     cudaError_t e = launch_megakernel(b->h_items[i].sc, b->h_items[i].fp, false, b->stream);

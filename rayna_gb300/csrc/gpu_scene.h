@@ -199,13 +199,15 @@ struct GpuScene {
   const float4* texels;       // every image's texels, RGB + pad, [x][y]
   const uint8_t* perm;        // noise: per Perlin source, 512 permutation entries
   uint32_t sky_image;         // RG_SKY_IMAGE: index into images
+  uint32_t stack_limit;       // traversal stack entries a ray may use (rg_tuning.stack_limit; kStackSize by default)
+  uint32_t shared_stack;      // traversal stack entries per thread in shared memory (0: all in local memory)
 };
 
-// Device error bits (rg_render_stats::error_flags).
+// Device error bits (rg_render_stats::error_flags, RG_DEVICE_* in the C ABI).
 enum : uint32_t {
-  ERR_STACK_OVERFLOW = 1u,
-  ERR_BAD_INDEX = 2u,
-  ERR_QUEUE_OVERFLOW = 4u,
+  ERR_STACK_OVERFLOW = RG_DEVICE_STACK_OVERFLOW,
+  ERR_BAD_INDEX = RG_DEVICE_BAD_INDEX,
+  ERR_QUEUE_OVERFLOW = RG_DEVICE_QUEUE_OVERFLOW,
 };
 
 // Counters (RG_FLAG_COUNTERS): indices into the u64 counter array.
@@ -216,8 +218,13 @@ enum : uint32_t {
 };
 
 // Per-frame launch parameters (all f32 values rounded from the f64 host viewport).
+// `spp` is the number of samples per pixel traced by this frame: samples
+// sample_base .. sample_base + spp - 1 of the pixel's spp_total (the whole
+// frame unless rg_set_sample_range split it). The stratification and the
+// divisor of the per-pixel sum follow spp_total.
 struct FrameParams {
   uint32_t width, height, spp, ray_depth;
+  uint32_t sample_base, spp_total;
   uint32_t mode;          // RG_MODE_*: PBR, or a single-intersection visualisation
   uint32_t branching;     // RenderOpts::ray_branching: scattered rays per bounce
   uint32_t strat_d;

@@ -19,7 +19,7 @@ __device__ __forceinline__ void write_pixel(const FrameParams& fp, uint32_t pix,
                                             uint32_t n) {
   uint32_t x = pix % fp.width, y = pix / fp.width;
   size_t idx = ((size_t)x * fp.height + y) * 3 + c;
-  float mean = sum / (float)n;
+  float mean = sum / (float)fp.spp_total;  // n = spp_total unless the frame is one sample range of it
   float acc = fp.accum[idx] + mean;
   fp.accum[idx] = acc;
   if (fp.out) fp.out[idx] = (float)((double)acc / (double)fp.accum_count);
@@ -34,9 +34,9 @@ __device__ __forceinline__ void write_pixel(const FrameParams& fp, uint32_t pix,
 __host__ __device__ __forceinline__ uint32_t pixels_per_round(uint32_t spp) { return spp <= 32 ? 32 / spp : 1u; }
 
 // One warp round starting at pixel `first` (all 32 lanes must call it).
-template <uint32_t F, bool COUNT, uint32_t KIND = kSamplePbr>
+template <uint32_t F, bool COUNT, uint32_t KIND, class Stack>
 __device__ __forceinline__ void mega_round(const GpuScene& sc, const FrameParams& fp, uint32_t first, uint32_t n_pix,
-                                           Counters& cnt, uint32_t& segments) {
+                                           Counters& cnt, uint32_t& segments, Stack& stack) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t spp = fp.spp;
   if (spp <= 32) {
@@ -45,7 +45,8 @@ __device__ __forceinline__ void mega_round(const GpuScene& sc, const FrameParams
     const uint32_t pix = first + lp;
     const bool active = lp < ppw && pix < n_pix;
     C3f col{0.0f, 0.0f, 0.0f};
-    if (active) col = trace_path<F, COUNT, KIND>(sc, fp, pix % fp.width, pix / fp.width, s, cnt, segments);
+    if (active)
+      col = trace_path<F, COUNT, KIND>(sc, fp, pix % fp.width, pix / fp.width, fp.sample_base + s, cnt, segments, stack);
     // The lane holding sample 0 of a pixel adds samples 1..spp-1 in order.
     const uint32_t base = lp * spp;
     float v[3] = {col.r, col.g, col.b};
@@ -71,7 +72,8 @@ __device__ __forceinline__ void mega_round(const GpuScene& sc, const FrameParams
     double psq[3] = {0.0, 0.0, 0.0};
     if (active) {
       for (uint32_t s = lane; s < spp; s += 32) {
-        C3f col = trace_path<F, COUNT, KIND>(sc, fp, pix % fp.width, pix / fp.width, s, cnt, segments);
+        C3f col = trace_path<F, COUNT, KIND>(sc, fp, pix % fp.width, pix / fp.width, fp.sample_base + s, cnt, segments,
+                                             stack);
         part[0] = part[0] + col.r; part[1] = part[1] + col.g; part[2] = part[2] + col.b;
         psq[0] += (double)col.r * col.r; psq[1] += (double)col.g * col.g; psq[2] += (double)col.b * col.b;
       }

@@ -8,46 +8,59 @@
 
 namespace rg {
 
+// Threads per block: rg_tuning.block (64, 128 or 256; 256 by default). The
+// launch bounds admit the largest.
 constexpr int kMegaBlock = 256;
-constexpr int kWarpsPerBlock = kMegaBlock / 32;
 
+// The top sc.shared_stack entries of each thread's traversal stack live in
+// the block's dynamic shared memory (shared_stack x blockDim x 8 bytes), the
+// deeper ones in local memory; the current node and the postponed leaf stay
+// in registers.
 template <uint32_t F, bool COUNT, uint32_t KIND = kSamplePbr>
 __global__ void __launch_bounds__(kMegaBlock) k_megakernel(GpuScene sc, FrameParams fp, uint32_t n_pix) {
-  const uint32_t warp = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  extern __shared__ uint2 mega_stack_sh[];
+  const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  uint2 stack_loc[kTravStack];
+  DynStack stack{mega_stack_sh + threadIdx.x, stack_loc, (int)sc.shared_stack, (int)blockDim.x};
   Counters cnt;
   uint32_t segments = 0;
-  mega_round<F, COUNT, KIND>(sc, fp, warp * pixels_per_round(fp.spp), n_pix, cnt, segments);
+  mega_round<F, COUNT, KIND>(sc, fp, warp * pixels_per_round(fp.spp), n_pix, cnt, segments, stack);
   flush_counters<COUNT>(fp, cnt, segments);
 }
 
 template <uint32_t F>
-static void launch_mega(const GpuScene& sc, const FrameParams& fp, bool counters, uint32_t blocks, uint32_t n_pix,
-                        cudaStream_t stream) {
-  if (counters) k_megakernel<F, true><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
-  else k_megakernel<F, false><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+static void launch_mega(const GpuScene& sc, const FrameParams& fp, bool counters, uint32_t blocks, uint32_t block,
+                        size_t smem, uint32_t n_pix, cudaStream_t stream) {
+  if (counters) k_megakernel<F, true><<<blocks, block, smem, stream>>>(sc, fp, n_pix);
+  else k_megakernel<F, false><<<blocks, block, smem, stream>>>(sc, fp, n_pix);
 }
 
-cudaError_t launch_megakernel(const GpuScene& sc, const FrameParams& fp, bool counters, cudaStream_t stream) {
+cudaError_t launch_megakernel(const GpuScene& sc, const FrameParams& fp, bool counters, cudaStream_t stream,
+                              uint32_t block) {
+  if (block == 0) block = kMegaBlock;
+  if (block % 32 || block > (uint32_t)kMegaBlock) return cudaErrorInvalidValue;
+  const uint32_t warps_per_block = block / 32;
+  const size_t smem = (size_t)sc.shared_stack * block * sizeof(uint2);
   const uint32_t n_pix = fp.width * fp.height;
   const uint32_t ppw = pixels_per_round(fp.spp);
   const uint32_t warps = (n_pix + ppw - 1) / ppw;
-  const uint32_t blocks = (warps + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const uint32_t blocks = (warps + warps_per_block - 1) / warps_per_block;
   if (fp.mode != RG_MODE_PBR || fp.branching > 1) {
     // Debug render modes and ray_branching > 1: one variant over every
     // primitive kind (these are not throughput paths); work counters off.
     const uint32_t kind = fp.mode != RG_MODE_PBR ? kSampleMode : kSampleBranch;
     const bool wide = (sc.features & F_WIDE) != 0;
     if (kind == kSampleMode) {
-      if (wide) k_megakernel<F_ANY | F_WIDE, false, kSampleMode><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
-      else k_megakernel<F_ANY, false, kSampleMode><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+      if (wide) k_megakernel<F_ANY | F_WIDE, false, kSampleMode><<<blocks, block, smem, stream>>>(sc, fp, n_pix);
+      else k_megakernel<F_ANY, false, kSampleMode><<<blocks, block, smem, stream>>>(sc, fp, n_pix);
     } else {
-      if (wide) k_megakernel<F_ANY | F_WIDE, false, kSampleBranch><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
-      else k_megakernel<F_ANY, false, kSampleBranch><<<blocks, kMegaBlock, 0, stream>>>(sc, fp, n_pix);
+      if (wide) k_megakernel<F_ANY | F_WIDE, false, kSampleBranch><<<blocks, block, smem, stream>>>(sc, fp, n_pix);
+      else k_megakernel<F_ANY, false, kSampleBranch><<<blocks, block, smem, stream>>>(sc, fp, n_pix);
     }
     return cudaGetLastError();
   }
   dispatch_features(sc.features, [&](auto f) {
-    launch_mega<decltype(f)::value>(sc, fp, counters, blocks, n_pix, stream);
+    launch_mega<decltype(f)::value>(sc, fp, counters, blocks, block, smem, n_pix, stream);
     return 0;
   });
   return cudaGetLastError();

@@ -11,7 +11,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -343,6 +345,7 @@ template <class T>
 rg_status upload(rg_renderer* h, T*& dst, const T* src, size_t n, const char* what) {
   dfree(dst);
   if (n == 0) return RG_OK;
+  if (alloc_fault()) return fail(h, RG_OOM, "%s: allocation failed (RAYNA_GPU_FAIL_ALLOC)", what);
   RG_CUDA(h, cudaMalloc((void**)&dst, n * sizeof(T)), what);
   RG_CUDA(h, cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, h->stream), what);
   return RG_OK;
@@ -358,6 +361,7 @@ namespace rg {
 rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs) {
   rg_status st = validate_scene(h, d);
   if (st != RG_OK) return st;
+  if (alloc_fault()) throw std::bad_alloc();  // RAYNA_GPU_FAIL_ALLOC: as if the host arrays could not be allocated
   hs = HostScene{};
   hs.ns = d.n_spheres; hs.nt = d.n_triangles; hs.nb = d.n_boxes; hs.nv = d.n_volumes; hs.nsdf = d.n_sdfs;
   hs.nq = d.n_quads; hs.nc = d.n_cylinders; hs.npl = d.n_planes;
@@ -685,6 +689,24 @@ uint32_t effective_bvh_width(uint32_t requested, const GpuScene& g, uint32_t for
   return (w == 8 && g.n_wnodes > 0) ? 8u : 2u;
 }
 
+bool alloc_fault() {
+  static std::mutex mu;
+  static long countdown = -1;  // -1: not read yet; 0: off or spent
+  std::lock_guard<std::mutex> lock(mu);
+  if (countdown < 0) {
+    const char* v = std::getenv("RAYNA_GPU_FAIL_ALLOC");
+    countdown = v ? std::max(0L, std::strtol(v, nullptr, 10)) : 0;
+  }
+  if (countdown == 0) return false;
+  return --countdown == 0;
+}
+
+rg_status device_status(uint32_t err) {
+  if (err & (ERR_STACK_OVERFLOW | ERR_QUEUE_OVERFLOW)) return RG_QUEUE_OVERFLOW;
+  if (err & ERR_BAD_INDEX) return RG_STEP_LIMIT;
+  return RG_OK;
+}
+
 cudaError_t stage_mark(rg_renderer* h) {
   if (h->stage_used == h->stage_ev.size()) {
     cudaEvent_t ev;
@@ -708,6 +730,9 @@ uint32_t effective_budget(const rg_renderer* h) {
 
 void apply_features(rg_renderer* h) {
   h->gs.features = h->kinds | (effective_bvh_width(h->bvh_width, h->gs, h->form) == 8 ? F_WIDE : 0u);
+  h->gs.stack_limit = h->stack_limit ? h->stack_limit : (uint32_t)kStackSize;
+  h->gs.shared_stack = h->shared_stack == 0 ? (h->kinds == F_TRI ? kDefaultSharedStackTriangles : 0u)
+                     : (h->shared_stack == RG_SHARED_STACK_NONE ? 0u : h->shared_stack);
 }
 
 void free_scene(DeviceScene& ds) {
@@ -722,7 +747,9 @@ rg_status ensure_frame_buffers(rg_renderer* h) {
   const uint32_t w = h->opts.width, hh = h->opts.height;
   if (h->acc_w == w && h->acc_h == hh && h->d_accum) return RG_OK;
   dfree(h->d_accum); dfree(h->d_out); dfree(h->d_fmean); dfree(h->d_fvar);
+  h->acc_w = h->acc_h = 0;
   size_t n = (size_t)w * hh * 3;
+  if (alloc_fault()) return fail(h, RG_OOM, "frame buffers: allocation failed (RAYNA_GPU_FAIL_ALLOC)");
   RG_CUDA(h, cudaMalloc((void**)&h->d_accum, n * sizeof(float)), "alloc accumulation");
   RG_CUDA(h, cudaMalloc((void**)&h->d_out, n * sizeof(float)), "alloc output");
   RG_CUDA(h, cudaMalloc((void**)&h->d_fmean, n * sizeof(float)), "alloc frame mean");
@@ -738,13 +765,16 @@ void fill_frame_params(rg_renderer* h, uint64_t seed, FrameParams& fp) {
   std::memset(&fp, 0, sizeof(fp));
   fp.width = h->opts.width;
   fp.height = h->opts.height;
-  fp.spp = h->opts.samples;
+  fp.spp_total = h->opts.samples;
+  fp.spp = h->range_count ? h->range_count : h->opts.samples;
+  fp.sample_base = h->range_count ? h->range_first : 0u;
   fp.ray_depth = h->opts.ray_depth;
   fp.mode = h->opts.mode;
   fp.branching = h->opts.ray_branching;
-  uint32_t d = (uint32_t)std::sqrt((double)fp.spp);
-  while ((uint64_t)(d + 1) * (d + 1) <= fp.spp) ++d;
-  while ((uint64_t)d * d > fp.spp) --d;
+  // render_px_msaa's strata (renderer.rs:370-389): d = floor(sqrt(samples)) of the whole pixel
+  uint32_t d = (uint32_t)std::sqrt((double)fp.spp_total);
+  while ((uint64_t)(d + 1) * (d + 1) <= fp.spp_total) ++d;
+  while ((uint64_t)d * d > fp.spp_total) --d;
   fp.strat_d = d;
   fp.strat_inv = 1.0f / (float)d;
   fp.seed_lo = (uint32_t)seed;
@@ -864,9 +894,14 @@ rg_status rg_clear_accumulation(rg_handle h) {
 
 rg_status rg_inspect_scene(const rg_scene_desc* scene, rg_scene_info* out) {
   if (!scene || !out) return fail(nullptr, RG_INVALID_ARG, "rg_inspect_scene: NULL argument");
-  HostScene hs;
-  rg_status st = build_scene_host(nullptr, *scene, hs);
   std::memset(out, 0, sizeof(*out));
+  HostScene hs;
+  rg_status st;
+  try {
+    st = build_scene_host(nullptr, *scene, hs);
+  } catch (const std::bad_alloc&) {
+    return fail(nullptr, RG_OOM, "rg_inspect_scene: out of host memory");
+  }
   if (st != RG_OK) return st;
   out->n_prims = (uint32_t)hs.prims.size();
   out->n_unbounded = (uint32_t)hs.sdfs.size();
@@ -906,7 +941,12 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene) {
   if (!h || !scene) return fail(h, RG_INVALID_ARG, "rg_set_scene: NULL argument");
   cudaSetDevice(h->device);
   HostScene hs;
-  rg_status st = build_scene_host(h, *scene, hs);
+  rg_status st;
+  try {
+    st = build_scene_host(h, *scene, hs);
+  } catch (const std::bad_alloc&) {
+    return fail(h, RG_OOM, "rg_set_scene: out of host memory");
+  }
   if (st != RG_OK) return st;
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "rg_set_scene");
   if ((st = upload_scene(h, hs)) != RG_OK) return st;
@@ -963,8 +1003,8 @@ rg_status rg_backward_frame(rg_handle h, uint64_t seed, const float* target_rgb,
   cudaSetDevice(h->device);
   if (!h->cam_ok) return fail(h, RG_INVALID_CAMERA, "camera viewport could not be calculated");
   if (!h->frame_current)
-    return fail(h, RG_NOT_READY, "rg_backward_frame: no PBR frame rendered since the scene, camera, options, "
-                                 "parameters or accumulation last changed");
+    return fail(h, RG_NOT_READY, "rg_backward_frame: no whole PBR frame rendered since the scene, camera, options, "
+                                 "parameters, sample range or accumulation last changed");
   return backward_device(h, seed, nullptr, target_rgb, out, true);
 }
 
@@ -972,6 +1012,12 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   if (!h || !t) return fail(h, RG_INVALID_ARG, "rg_set_tuning: NULL argument");
   for (uint32_t r : t->reserved)
     if (r != 0) return fail(h, RG_INVALID_ARG, "rg_tuning: reserved fields must be 0");
+  if (t->shared_stack != 0 && t->shared_stack != RG_SHARED_STACK_NONE && t->shared_stack != 4 && t->shared_stack != 8 &&
+      t->shared_stack != 16)
+    return fail(h, RG_INVALID_ARG, "rg_tuning: shared_stack must be 0, RG_SHARED_STACK_NONE, 4, 8 or 16");
+  if (t->block != 0 && t->block != 64 && t->block != 128 && t->block != 256)
+    return fail(h, RG_INVALID_ARG, "rg_tuning: block must be 0, 64, 128 or 256");
+  if (t->stack_limit > (uint32_t)kStackSize) return fail(h, RG_INVALID_ARG, "rg_tuning: stack_limit must be at most 64");
   if (t->sort_materials > 2) return fail(h, RG_INVALID_ARG, "rg_tuning: sort_materials must be 0, 1 or 2");
   if (t->fetch_budget > 4096) return fail(h, RG_INVALID_ARG, "rg_tuning: fetch_budget must be at most 4096");
   if (t->bvh_width != 0 && t->bvh_width != 2 && t->bvh_width != 8)
@@ -981,6 +1027,9 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   h->wf_sort = t->sort_materials;
   h->wf_budget = t->fetch_budget;
   h->bvh_width = t->bvh_width;
+  h->shared_stack = t->shared_stack;
+  h->mega_block = t->block;
+  h->stack_limit = t->stack_limit;
   apply_features(h);
   return RG_OK;
 }
@@ -992,6 +1041,9 @@ rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
   out->sort_materials = effective_sort(h) ? 1u : 2u;
   out->fetch_budget = effective_budget(h);
   out->bvh_width = effective_bvh_width(h->bvh_width, h->gs, h->form);
+  out->shared_stack = h->gs.shared_stack ? h->gs.shared_stack : RG_SHARED_STACK_NONE;
+  out->block = h->mega_block ? h->mega_block : 256u;
+  out->stack_limit = h->gs.stack_limit;
   return RG_OK;
 }
 
@@ -1020,6 +1072,18 @@ rg_status rg_set_options(rg_handle h, const rg_render_opts* opts) {
   }
   if (opts->ray_depth > 4096) return fail(h, RG_INVALID_ARG, "ray_depth too large");
   h->opts = *opts;
+  h->range_first = h->range_count = 0;  // whole frames again
+  return rg_clear_accumulation(h);
+}
+
+rg_status rg_set_sample_range(rg_handle h, uint32_t first, uint32_t count) {
+  if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
+  if (count > 0 && ((uint64_t)first + count > h->opts.samples))
+    return fail(h, RG_INVALID_ARG, "sample range [%u, %u) exceeds the %u samples per pixel", first, first + count,
+                h->opts.samples);
+  const bool whole = count == 0 || (first == 0 && count == h->opts.samples);
+  h->range_first = whole ? 0u : first;
+  h->range_count = whole ? 0u : count;
   return rg_clear_accumulation(h);
 }
 
@@ -1033,6 +1097,7 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
   fp.accum_count = h->pixel_accum;
   if (d_out_override) fp.out = d_out_override;
   RG_CUDA(h, cudaMemsetAsync(h->d_counters, 0, CNT_N * sizeof(unsigned long long), h->stream), "reset counters");
+  RG_CUDA(h, cudaMemsetAsync(h->d_err, 0, sizeof(uint32_t), h->stream), "reset error bits");
   RG_CUDA(h, cudaEventRecord(h->ev0, h->stream), "event");
   cudaError_t e;
   h->last_launches = 1;
@@ -1043,12 +1108,12 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
     e = launch_wavefront(h, fp);
   } else {
     if ((h->flags & RG_FLAG_STAGE_TIMES) && (e = stage_mark(h)) != cudaSuccess) return cuda_fail(h, e, "stage event");
-    e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream);
+    e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream, h->mega_block);
     if (e == cudaSuccess && (h->flags & RG_FLAG_STAGE_TIMES)) e = stage_mark(h);
   }
   if (e != cudaSuccess) { h->frame_current = false; return cuda_fail(h, e, "render launch"); }
   RG_CUDA(h, cudaEventRecord(h->ev1, h->stream), "event");
-  h->frame_current = fp.mode == RG_MODE_PBR && fp.branching == 1 && fp.frame_mean != nullptr;
+  h->frame_current = fp.mode == RG_MODE_PBR && fp.branching == 1 && fp.frame_mean != nullptr && fp.spp == fp.spp_total;
   h->last_samples = (uint64_t)fp.width * fp.height * fp.spp;
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
@@ -1065,7 +1130,8 @@ rg_status rg_sync_stats(rg_handle h, rg_render_stats* stats) {
   if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
   cudaSetDevice(h->device);
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "rg_sync_stats");
-  if (!stats) return RG_OK;
+  rg_render_stats local;
+  if (!stats) stats = &local;  // the error bits decide the status either way
   float ms = 0.0f;
   if (cudaEventElapsedTime(&ms, h->ev0, h->ev1) != cudaSuccess) { cudaGetLastError(); ms = 0.0f; }
   unsigned long long c[CNT_N];
@@ -1092,6 +1158,10 @@ rg_status rg_sync_stats(rg_handle h, rg_render_stats* stats) {
     if (cudaEventElapsedTime(&t, h->stage_ev[i], h->stage_ev[i + 1]) != cudaSuccess) { cudaGetLastError(); t = 0.0f; }
     stats->traverse_ms += t;
   }
+  const rg_status dst = device_status(err);
+  if (dst != RG_OK)
+    return fail(h, dst, "device error bits 0x%x this frame (%s%s%s)", err, (err & ERR_STACK_OVERFLOW) ? "traversal stack " : "",
+                (err & ERR_QUEUE_OVERFLOW) ? "path queue " : "", (err & ERR_BAD_INDEX) ? "bad node index" : "");
   return RG_OK;
 }
 
@@ -1189,6 +1259,7 @@ rg_status rg_query_rays(rg_handle h, uint32_t n, const float* origins, const flo
   rg_hit* d_out = nullptr;
   rg_status st = RG_OK;
   cudaError_t e = cudaSuccess;
+  uint32_t qerr = 0;
   do {
     if ((e = cudaMalloc((void**)&d_o, 3ull * n * sizeof(float))) != cudaSuccess) break;
     if ((e = cudaMalloc((void**)&d_d, 3ull * n * sizeof(float))) != cudaSuccess) break;
@@ -1201,11 +1272,14 @@ rg_status rg_query_rays(rg_handle h, uint32_t n, const float* origins, const flo
     if ((e = cudaMemcpyAsync(d_t0, tmin, n * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
     if ((e = cudaMemcpyAsync(d_t1, tmax, n * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
     if (d_u && (e = cudaMemcpyAsync(d_u, volume_u, n * nv * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(h->d_err, 0, sizeof(uint32_t), h->stream)) != cudaSuccess) break;
     if ((e = launch_query(h->gs, n, d_o, d_d, d_t0, d_t1, d_u, d_out, h->d_err, h->stream)) != cudaSuccess) break;
     if ((e = cudaMemcpyAsync(out, d_out, n * sizeof(rg_hit), cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(&qerr, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess) break;
     e = cudaStreamSynchronize(h->stream);
   } while (0);
   if (e != cudaSuccess) st = cuda_fail(h, e, "rg_query_rays");
+  else if ((st = device_status(qerr)) != RG_OK) fail(h, st, "rg_query_rays: device error bits 0x%x", qerr);
   dfree(d_o); dfree(d_d); dfree(d_t0); dfree(d_t1); dfree(d_u); dfree(d_out);
   return st;
 }

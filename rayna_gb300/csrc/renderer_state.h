@@ -111,6 +111,11 @@ struct rg_renderer {
   uint32_t wf_sort = 0;       // wavefront: 1 sorted extend/shade stages, 2 fused bounce kernel, 0 by scene
   uint32_t wf_budget = 0;     // wavefront: node visits between refills (0: library default)
   uint32_t bvh_width = 0;     // requested traversal: 2, 8, or 0 for the library default
+  uint32_t shared_stack = 0;  // requested shared traversal-stack entries: 0 default, RG_SHARED_STACK_NONE, 4, 8, 16
+  uint32_t mega_block = 0;    // megakernel threads per block (0: 256)
+  uint32_t stack_limit = 0;   // traversal stack entries a ray may use (0: kStackSize)
+  uint32_t range_first = 0;   // rg_set_sample_range: the frame's first sample
+  uint32_t range_count = 0;   //   and its number of samples (0: whole frames)
   uint32_t kinds = 0;         // F_* primitive-kind bits of the scene's kernel variant
 
   void* d_adj = nullptr;      // adjoint scratch (image, adjoint image, gradients)
@@ -149,9 +154,20 @@ bool effective_sort(const rg_renderer* h);
 // Node visits between refills of the persistent kernels: as requested, else
 // the default for the scene's kinds.
 uint32_t effective_budget(const rg_renderer* h);
-// Kernel variant bits: the scene's primitive kinds, plus F_WIDE when the
-// handle traverses the 8-wide tree.
+// Shared traversal-stack entries per thread when the tuning leaves them at 0:
+// 8 for scenes of triangles only (the 1.3M-triangle mesh measured 1.07x with
+// the split in the persistent kernels), none elsewhere (0.98x on spheres,
+// 1.00x on the SDF scene).
+constexpr uint32_t kDefaultSharedStackTriangles = 8;
+// Kernel variant bits (the scene's primitive kinds, plus F_WIDE when the
+// handle traverses the 8-wide tree) and the stack knobs of the handle's scene.
 void apply_features(rg_renderer* h);
+// Status of a frame's device error bits (RG_DEVICE_*): RG_OK when none.
+rg_status device_status(uint32_t err);
+// RAYNA_GPU_FAIL_ALLOC=n: the n-th allocation the library counts (host scene
+// build or device buffer, from 1) fails as if memory ran out. A test hook for
+// the RG_OOM paths; every allocation site asks before allocating.
+bool alloc_fault();
 rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs);
 void fill_frame_params(rg_renderer* h, uint64_t seed, FrameParams& fp);
 rg_status ensure_frame_buffers(rg_renderer* h);

@@ -561,6 +561,19 @@ struct LocalStack {
   __device__ __forceinline__ uint2 get(int i) const { return s[i]; }
   __device__ __forceinline__ void set(int i, uint2 v) { s[i] = v; }
 };
+// DynStack: the same split with the shared entries per thread and the
+// stride chosen at launch (rg_tuning.shared_stack, the block size); `loc`
+// has kTravStack entries, of which the first n_sh stay unused.
+struct DynStack {
+  uint2* sh;   // this thread's column of the block's dynamic shared array
+  uint2* loc;
+  int n_sh, stride;
+  __device__ __forceinline__ uint2 get(int i) const { return i < n_sh ? sh[i * stride] : loc[i]; }
+  __device__ __forceinline__ void set(int i, uint2 v) {
+    if (i < n_sh) sh[i * stride] = v;
+    else loc[i] = v;
+  }
+};
 template <int SH, int STRIDE>
 struct SplitStack {
   uint2* sh;   // this thread's column of the block's shared array (unused when SH is 0)
@@ -659,7 +672,7 @@ __device__ __forceinline__ bool run_binary(Traversal& t, Stack& stack, const Gpu
       if (h0 && h1) {
         bool swap = tn1 < tn0;
         t.ref = swap ? r1 : r0;
-        if (t.sp < kStackSize) {
+        if (t.sp < (int)sc.stack_limit) {
           stack.set(t.sp, make_uint2((uint32_t)(swap ? r0 : r1), __float_as_uint(swap ? tn0 : tn1)));
           ++t.sp;
         } else {
@@ -734,7 +747,7 @@ __device__ __forceinline__ bool run_wide(Traversal& t, Stack& stack, const GpuSc
       const uint32_t slot = k ^ oct;
       const uint32_t idx = t.ng.x + __popc(t.ng.y & ((1u << slot) - 1u) & 0xFFu);
       if (t.ng.y > 0x00FFFFFFu) {
-        if (t.sp < kTravStack) {
+        if (t.sp < (int)sc.stack_limit) {
           stack.set(t.sp, t.ng);
           ++t.sp;
         } else {
@@ -1254,13 +1267,13 @@ enum : uint32_t { kSamplePbr = 0, kSampleMode = 1, kSampleBranch = 2 };
 
 // Render::render_px_once for the debug modes (renderer.rs:427-490): one
 // intersection of the camera ray, coloured by mode; the sky on a miss.
-template <uint32_t F, bool COUNT>
+template <uint32_t F, bool COUNT, class Stack>
 __device__ C3f mode_sample(const GpuScene& sc, const FrameParams& fp, const Ray& ray, RngCtx& ctx, Counters& cnt,
-                           uint32_t& segments) {
+                           uint32_t& segments, Stack& stack) {
   ctx.depth = 0;
   HitRec h;
   ++segments;
-  if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) return sky_of<F>(sc, ray.d);
+  if (!closest_hit_with<F, COUNT>(stack, sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) return sky_of<F>(sc, ray.d);
   Surface s;
   finalize_hit<F, true>(sc, ray, h, ctx, s, 1e-3f);
   // The reference's visualisation colours (renderer.rs:439-453)
@@ -1305,9 +1318,9 @@ __device__ C3f mode_sample(const GpuScene& sc, const FrameParams& fp, const Ray&
 // (emission or sky). Random streams are keyed by node: node n's children are
 // n b + 1 + i, its free-flight draws use key n and the scatter of branch i key
 // n b + i (for b = 1 these reduce to the depth keys of the PBR path).
-template <uint32_t F, bool COUNT>
+template <uint32_t F, bool COUNT, class Stack>
 __device__ C3f branch_sample(const GpuScene& sc, const FrameParams& fp, Ray ray, RngCtx& ctx, Counters& cnt,
-                             uint32_t& segments) {
+                             uint32_t& segments, Stack& stack) {
   struct Level {
     Surface surf;
     Ray in;
@@ -1324,7 +1337,7 @@ __device__ C3f branch_sample(const GpuScene& sc, const FrameParams& fp, Ray ray,
     ctx.depth = node;
     HitRec h;
     ++segments;
-    if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
+    if (!closest_hit_with<F, COUNT>(stack, sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
       const C3f sk = sky_of<F>(sc, ray.d);
       L = C3f{L.r + w.r * sk.r, L.g + w.g * sk.g, L.b + w.b * sk.b};
     } else {
@@ -1365,21 +1378,22 @@ __device__ C3f branch_sample(const GpuScene& sc, const FrameParams& fp, Ray ray,
   return L;
 }
 
-// One sample of pixel (x, y). PBR: ray_colour_recursive (renderer.rs:508-572)
+// One sample of pixel (x, y); `s` is the sample's index among the pixel's
+// spp_total samples. PBR: ray_colour_recursive (renderer.rs:508-572)
 // evaluated front to back, L = sum_k beta_k * emitted_k + beta_K * sky.
-template <uint32_t F, bool COUNT, uint32_t KIND = kSamplePbr>
+template <uint32_t F, bool COUNT, uint32_t KIND, class Stack>
 __device__ C3f trace_path(const GpuScene& sc, const FrameParams& fp, uint32_t x, uint32_t y, uint32_t s, Counters& cnt,
-                          uint32_t& segments) {
+                          uint32_t& segments, Stack& stack) {
   RngCtx ctx{fp.seed_lo, fp.seed_hi, y * fp.width + x, s, 0, nullptr};
   Ray ray = camera_ray(fp, x, y, s, ctx);
-  if (KIND == kSampleMode) return mode_sample<F, COUNT>(sc, fp, ray, ctx, cnt, segments);
-  if (KIND == kSampleBranch) return branch_sample<F, COUNT>(sc, fp, ray, ctx, cnt, segments);
+  if (KIND == kSampleMode) return mode_sample<F, COUNT>(sc, fp, ray, ctx, cnt, segments, stack);
+  if (KIND == kSampleBranch) return branch_sample<F, COUNT>(sc, fp, ray, ctx, cnt, segments, stack);
   C3f L{0.0f, 0.0f, 0.0f}, beta{1.0f, 1.0f, 1.0f};
   for (uint32_t depth = 0; depth <= fp.ray_depth; ++depth) {
     ctx.depth = depth;
     HitRec h;
     ++segments;
-    if (!closest_hit<F, COUNT>(sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
+    if (!closest_hit_with<F, COUNT>(stack, sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err)) {
       C3f sk = sky_of<F>(sc, ray.d);
       L = C3f{L.r + beta.r * sk.r, L.g + beta.g * sk.g, L.b + beta.b * sk.b};
       break;

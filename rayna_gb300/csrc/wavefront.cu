@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(kWfBlock) k_generate(FrameParams fp, PathState
     s.counts[1] = 0;
   }
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.n_paths; p += gridDim.x * blockDim.x) {
-    uint32_t pix = wp.first_pixel + p / fp.spp, smp = p % fp.spp;
+    uint32_t pix = wp.first_pixel + p / fp.spp, smp = fp.sample_base + p % fp.spp;
     uint32_t x = pix % fp.width, y = pix / fp.width;
     RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, 0, nullptr};
     Ray r = camera_ray(fp, x, y, smp, ctx);
@@ -67,9 +67,9 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
   Ray r;
   C3f beta;
   Traversal t;
-  __shared__ uint2 stack_sh[kSharedStackOf<F> > 0 ? kSharedStackOf<F> * kWfBlock : 1];
-  uint2 stack_loc[kTravStack - kSharedStackOf<F>];
-  SplitStack<kSharedStackOf<F>, kWfBlock> stack{stack_sh + threadIdx.x, stack_loc};
+  extern __shared__ uint2 wf_stack_sh[];  // sc.shared_stack entries per thread
+  uint2 stack_loc[kTravStack];
+  DynStack stack{wf_stack_sh + threadIdx.x, stack_loc, (int)sc.shared_stack, kWfBlock};
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !has);
     if (idle && !drained) {
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
         if (i < n) {
           p = s.active[cur][i];
           pix = wp.first_pixel + p / fp.spp;
-          smp = p % fp.spp;
+          smp = fp.sample_base + p % fp.spp;
           const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1], r2 = s.rec[3 * (size_t)p + 2];
           depth = __float_as_uint(r0.w);
           r.o = v3(r0.x, r0.y, r0.z);
@@ -166,9 +166,9 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
   uint32_t p = 0, pix = 0, smp = 0, depth = 0;
   Ray r;
   Traversal t;
-  __shared__ uint2 stack_sh[kSharedStackOf<F> > 0 ? kSharedStackOf<F> * kWfBlock : 1];
-  uint2 stack_loc[kTravStack - kSharedStackOf<F>];
-  SplitStack<kSharedStackOf<F>, kWfBlock> stack{stack_sh + threadIdx.x, stack_loc};
+  extern __shared__ uint2 wf_stack_sh[];  // sc.shared_stack entries per thread
+  uint2 stack_loc[kTravStack];
+  DynStack stack{wf_stack_sh + threadIdx.x, stack_loc, (int)sc.shared_stack, kWfBlock};
   for (;;) {
     const unsigned idle = __ballot_sync(0xffffffffu, !has);
     if (idle && !drained) {
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
         if (i < n) {
           p = s.active[cur][i];
           pix = wp.first_pixel + p / fp.spp;
-          smp = p % fp.spp;
+          smp = fp.sample_base + p % fp.spp;
           const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1];
           depth = __float_as_uint(r0.w);
           r.o = v3(r0.x, r0.y, r0.z);
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kWfBlock) k_shade(GpuScene sc, FrameParams fp,
 #pragma unroll
     for (int j = 1; j < kKinds; ++j) k += i >= off[j] ? 1u : 0u;
     const uint32_t p = s.kindq[(size_t)k * wp.capacity + (i - off[k])];
-    const uint32_t pix = wp.first_pixel + p / fp.spp, smp = p % fp.spp;
+    const uint32_t pix = wp.first_pixel + p / fp.spp, smp = fp.sample_base + p % fp.spp;
     const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1], r2 = s.rec[3 * (size_t)p + 2];
     Ray r;
     r.o = v3(r0.x, r0.y, r0.z);
@@ -269,23 +269,26 @@ __global__ void __launch_bounds__(kWfBlock) k_accumulate(FrameParams fp, PathSta
 }
 
 // Runs every wave of one frame on the path arrays `s` (capacity `cap` slots).
+// `timed`: bracket the traversal launches with the handle's stage events.
 template <uint32_t F>
-cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s, size_t cap, size_t pix_per_wave) {
+cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s, size_t cap, size_t pix_per_wave,
+                      bool timed) {
   const size_t spp = fp.spp;
   const size_t n_pix = (size_t)fp.width * fp.height;
   const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
   const bool sorted = effective_sort(h);
-  const bool timed = (h->flags & RG_FLAG_STAGE_TIMES) != 0;
   const int budget = (int)effective_budget(h);
   const int grid = sm_count(h->device) * 8;
-  // The persistent traversal kernels run as many blocks as are resident at once.
+  // The persistent traversal kernels run as many blocks as are resident at
+  // once, each with its threads' shared stack entries.
+  const size_t smem = (size_t)h->gs.shared_stack * kWfBlock * sizeof(uint2);
   int ext_per_sm = 0;
-  if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_extend<F, true>, kWfBlock, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_extend<F, false>, kWfBlock, 0);
+  if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_extend<F, true>, kWfBlock, smem);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_extend<F, false>, kWfBlock, smem);
   const int ext_grid = sm_count(h->device) * std::max(ext_per_sm, 1);
   int bounce_per_sm = 0;
-  if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bounce_per_sm, k_bounce<F, true>, kWfBlock, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bounce_per_sm, k_bounce<F, false>, kWfBlock, 0);
+  if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bounce_per_sm, k_bounce<F, true>, kWfBlock, smem);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bounce_per_sm, k_bounce<F, false>, kWfBlock, smem);
   const int bounce_grid = sm_count(h->device) * std::max(bounce_per_sm, 1);
   cudaStream_t st = h->stream;
   cudaError_t e;
@@ -306,14 +309,14 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
       if (sorted) {
         if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
-        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
-        else k_extend<F, false><<<ext_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
+        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget);
+        else k_extend<F, false><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget);
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
         k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
       } else {
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
-        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
-        else k_bounce<F, false><<<bounce_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, budget);
+        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget);
+        else k_bounce<F, false><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget);
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
       }
       cur ^= 1;
@@ -326,9 +329,10 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   return cudaSuccess;
 }
 
-cudaError_t run_frame(rg_renderer* h, const FrameParams& fp, const PathState& s, size_t cap, size_t pix_per_wave) {
+cudaError_t run_frame(rg_renderer* h, const FrameParams& fp, const PathState& s, size_t cap, size_t pix_per_wave,
+                      bool timed) {
   return dispatch_features(h->gs.features,
-                           [&](auto f) { return run_waves<decltype(f)::value>(h, fp, s, cap, pix_per_wave); });
+                           [&](auto f) { return run_waves<decltype(f)::value>(h, fp, s, cap, pix_per_wave, timed); });
 }
 
 }  // namespace
@@ -352,14 +356,15 @@ cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp) {
   }
   PathState s;
   carve((char*)h->wf.arena, h->wf.capacity, s);
-  return run_frame(h, fp, s, h->wf.capacity, pix_per_wave);
+  return run_frame(h, fp, s, h->wf.capacity, pix_per_wave, (h->flags & RG_FLAG_STAGE_TIMES) != 0);
 }
 
 // ---------------------------------------------------------------------------
 // Allocation-free variant: the path state of one wave lives in a fixed
 // file-scope device array instead of a cudaMalloc'ed arena.
 // ---------------------------------------------------------------------------
-constexpr size_t kStaticArenaBytes = 31ull * 4ull * RG_STATIC_WAVE_PATHS + 256ull;
+constexpr size_t kStaticArenaBytes = arena_bytes(RG_STATIC_WAVE_PATHS);
+static_assert(kStaticArenaBytes <= 108ull * RG_STATIC_WAVE_PATHS + 256ull, "static scratch larger than documented");
 static __device__ __align__(256) unsigned char g_wave_scratch[kStaticArenaBytes];
 
 namespace {
@@ -394,7 +399,8 @@ cudaError_t launch_wavefront_static(rg_renderer* h, const FrameParams& fp) {
   if (e != cudaSuccess) return e;
   PathState s;
   carve((char*)arena, cap, s);
-  return run_frame(h, fp, s, cap, std::min(cap / spp, n_pix));
+  // No stage timing here: its events are created on demand, and this entry allocates nothing.
+  return run_frame(h, fp, s, cap, std::min(cap / spp, n_pix), false);
 }
 
 }  // namespace rg
@@ -423,9 +429,16 @@ extern "C" rg_status rg_render_static_scratch(rg_handle h, uint64_t seed, float*
   fp.frame_mean = nullptr;
   fp.frame_var = nullptr;
   fp.accum_count = accum_count;
-  if ((e = cudaMemsetAsync(h->d_counters, 0, CNT_N * sizeof(unsigned long long), h->stream)) != cudaSuccess)
+  // The frame's bookkeeping, as rg_render keeps it, so rg_sync_stats reports
+  // this frame: counters and error bits cleared, events around the launches.
+  h->stage_used = 0;
+  h->last_launches = 0;
+  h->last_samples = (uint64_t)fp.width * fp.height * fp.spp;
+  if ((e = cudaMemsetAsync(h->d_counters, 0, CNT_N * sizeof(unsigned long long), h->stream)) != cudaSuccess ||
+      (e = cudaMemsetAsync(h->d_err, 0, sizeof(uint32_t), h->stream)) != cudaSuccess ||
+      (e = cudaEventRecord(h->ev0, h->stream)) != cudaSuccess)
     return set_error(h, RG_CUDA_ERROR, cudaGetErrorString(e));
-  if ((e = launch_wavefront_static(h, fp)) != cudaSuccess) {
+  if ((e = launch_wavefront_static(h, fp)) != cudaSuccess || (e = cudaEventRecord(h->ev1, h->stream)) != cudaSuccess) {
     cudaGetLastError();
     return set_error(h, RG_CUDA_ERROR, cudaGetErrorString(e));
   }

@@ -17,11 +17,12 @@ namespace rg {
 
 constexpr int kWfBlock = 256;
 // Traversal stack entries per thread kept in shared memory by the persistent
-// kernels (16 KB per block of 256); deeper entries live in local memory. The
-// split measured 1.07x on the 1.3M-triangle mesh (8 and 16 entries alike),
-// 0.98x on scenes of spheres only (shallow trees) and 1.00x on the SDF scene;
-// it is used where it was measured to pay, the triangle-only variants, and
-// every other variant keeps the whole stack in local memory.
+// batched kernel (16 KB per block of 256); deeper entries live in local
+// memory. The split measured 1.07x on the 1.3M-triangle mesh (8 and 16
+// entries alike), 0.98x on scenes of spheres only (shallow trees) and 1.00x
+// on the SDF scene; it is used where it was measured to pay, the
+// triangle-only variants. (Single renders take the count from the handle's
+// tuning, rg_tuning.shared_stack, with the same default.)
 constexpr int kSharedStack = 8;
 template <uint32_t F> constexpr int kSharedStackOf = kinds_of(F) == F_TRI ? kSharedStack : 0;
 constexpr int kKinds = 6;  // miss, lambertian, metal, dielectric, isotropic, light
@@ -166,7 +167,7 @@ __device__ __forceinline__ void accumulate_pixel(const FrameParams& fp, const Pa
   }
   uint32_t x = pix % fp.width, y = pix / fp.width;
   size_t idx = ((size_t)x * fp.height + y) * 3 + c;
-  float mean = sum / (float)spp;
+  float mean = sum / (float)fp.spp_total;  // spp_total = spp unless the frame is one sample range of it
   float acc = fp.accum[idx] + mean;
   fp.accum[idx] = acc;
   if (fp.out) fp.out[idx] = (float)((double)acc / (double)fp.accum_count);
@@ -177,31 +178,40 @@ __device__ __forceinline__ void accumulate_pixel(const FrameParams& fp, const Pa
   }
 }
 
-// Lays the path arrays out from `arena` (256-byte aligned each) and returns
-// the number of bytes used (108 per slot plus the counts); with a null arena
-// it only measures.
-inline size_t carve(char* arena, size_t cap, PathState& s) {
+// Bytes per path slot of each path array, in the order carve lays them out:
+// the records, the side record, the sample radiance r, g, b, the two active
+// queues and the material-kind queues; then the counts.
+constexpr size_t kSlotArrayBytes[] = {48, 16, 4, 4, 4, 4, 4, 4 * kKinds};
+constexpr size_t kCountsBytes = 64 * 4;
+constexpr size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Bytes carve uses for `cap` slots (108 per slot, each array 256-byte aligned, plus the counts).
+constexpr size_t arena_bytes(size_t cap) {
   size_t used = 0;
-  auto take = [&](size_t bytes) {
-    char* r = arena ? arena + used : nullptr;
-    used += (bytes + 255) & ~size_t(255);
-    return r;
-  };
-  s.rec = (float4*)take(cap * 48);
-  s.aux = (float4*)take(cap * 16);
-  s.sr = (float*)take(cap * 4);
-  s.sg = (float*)take(cap * 4);
-  s.sb = (float*)take(cap * 4);
-  s.active[0] = (uint32_t*)take(cap * 4);
-  s.active[1] = (uint32_t*)take(cap * 4);
-  s.kindq = (uint32_t*)take(cap * 4 * kKinds);
-  s.counts = (uint32_t*)take(64 * 4);
-  return used;
+  for (size_t b : kSlotArrayBytes) used += round256(cap * b);
+  return used + round256(kCountsBytes);
 }
 
-inline size_t arena_bytes(size_t cap) {
-  PathState s;
-  return carve(nullptr, cap, s);
+// Lays the path arrays out from `arena` (256-byte aligned each) and returns
+// the number of bytes used, arena_bytes(cap).
+inline size_t carve(char* arena, size_t cap, PathState& s) {
+  size_t used = 0;
+  int k = 0;
+  auto take = [&](size_t bytes) {
+    char* r = arena + used;
+    used += round256(bytes);
+    return r;
+  };
+  s.rec = (float4*)take(cap * kSlotArrayBytes[k++]);
+  s.aux = (float4*)take(cap * kSlotArrayBytes[k++]);
+  s.sr = (float*)take(cap * kSlotArrayBytes[k++]);
+  s.sg = (float*)take(cap * kSlotArrayBytes[k++]);
+  s.sb = (float*)take(cap * kSlotArrayBytes[k++]);
+  s.active[0] = (uint32_t*)take(cap * kSlotArrayBytes[k++]);
+  s.active[1] = (uint32_t*)take(cap * kSlotArrayBytes[k++]);
+  s.kindq = (uint32_t*)take(cap * kSlotArrayBytes[k++]);
+  s.counts = (uint32_t*)take(kCountsBytes);
+  return used;
 }
 
 inline int sm_count(int device) {

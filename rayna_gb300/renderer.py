@@ -60,14 +60,17 @@ class Renderer:
 
     def __init__(self, scene: Scene, camera: Camera, options: RenderOpts, *, device: int = 0,
                  form: str = "wavefront", seed: int = 0, stream: int | None = None, counters: bool = False,
-                 stage_times: bool = False, validate: bool = False):
+                 stage_times: bool = False, validate: bool = False, exact: bool | None = None):
         """`form`: "wavefront" (the default: persistent extend/bounce kernels
         over waves of path slots, 1.5-2.5x the plain form on the workloads) or
         "megakernel" (one thread per pixel-sample). Both render identical
         images; debug render modes and ray_branching > 1 always run the
         megakernel. `counters`, `stage_times`, `validate`: RG_FLAG_* (work
-        counters, traversal timing, the reference's debug invariants)."""
-        self._lib = A.load_library()
+        counters, traversal timing, the reference's debug invariants).
+        `exact`: render with the arithmetic-contract build (fused
+        multiply-adds only where the source writes them; bit-exact with the
+        oracle's f32 policy) instead of the performance build."""
+        self._lib = A.load_library(exact=exact)
         dopts = A.rg_device_opts()
         dopts.device = device
         dopts.stream = stream
@@ -78,6 +81,7 @@ class Renderer:
         st = self._lib.rg_create(C.byref(dopts), C.byref(h))
         A.check(self._lib, None, st)
         self._h = h
+        self._stack_knobs = (0, 0, 0)  # requested shared_stack, block, stack_limit (0: library defaults)
         self.form = form
         self.seed = int(seed)
         self._frame = 0
@@ -226,15 +230,22 @@ class Renderer:
         return m
 
     def set_tuning(self, wave_paths: int | None = None, sort_materials: bool | None = None,
-                   bvh_width: int | None = None, fetch_budget: int | None = None):
+                   bvh_width: int | None = None, fetch_budget: int | None = None, shared_stack: int | None = None,
+                   block: int | None = None, stack_limit: int | None = None):
         """Launch knobs (rg_tuning); None leaves a knob as it is. wave_paths:
         wavefront path slots per wave (0 = library default); sort_materials:
         wavefront shading in material-kind order (True) or one fused bounce
         kernel (False); bvh_width: 2 (binary node pairs) or 8 (compressed
         8-wide nodes), 0 = library default; fetch_budget: node visits a
-        wavefront lane traverses between refills (0 = library default)."""
+        wavefront lane traverses between refills (0 = library default);
+        shared_stack: traversal stack entries per thread in shared memory
+        (0 = library default, -1 = none, else 4, 8 or 16); block: megakernel
+        threads per block (0 = 256, else 64 or 128); stack_limit: a test knob
+        capping the traversal stack a ray may use (0 = all 64)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
+        # the resolved defaults come back from rg_get_tuning; hand the requested knobs back
+        t.shared_stack, t.block, t.stack_limit = self._stack_knobs
         if wave_paths is not None:
             t.wave_paths = int(wave_paths)
         if sort_materials is not None:
@@ -243,14 +254,30 @@ class Renderer:
             t.bvh_width = int(bvh_width)
         if fetch_budget is not None:
             t.fetch_budget = int(fetch_budget)
+        if shared_stack is not None:
+            t.shared_stack = A.RG_SHARED_STACK_NONE if shared_stack < 0 else int(shared_stack)
+        if block is not None:
+            t.block = int(block)
+        if stack_limit is not None:
+            t.stack_limit = int(stack_limit)
         self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
+        self._stack_knobs = (t.shared_stack, t.block, t.stack_limit)
 
     def tuning(self) -> dict:
-        """The knobs in effect (library defaults resolved)."""
+        """The knobs in effect (library defaults resolved; shared_stack -1 = none)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
         return {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials == 1, "bvh_width": t.bvh_width,
-                "fetch_budget": t.fetch_budget}
+                "fetch_budget": t.fetch_budget,
+                "shared_stack": -1 if t.shared_stack == A.RG_SHARED_STACK_NONE else t.shared_stack,
+                "block": t.block, "stack_limit": t.stack_limit}
+
+    def set_sample_range(self, first: int, count: int):
+        """Frames trace samples [first, first + count) of each pixel's
+        `samples` and add their sum / samples to the accumulation
+        (rg_set_sample_range): disjoint ranges on several devices sum to whole
+        frames. count 0 restores whole frames; clears the accumulation."""
+        self._check(self._lib.rg_set_sample_range(self._h, int(first), int(count)))
 
     def set_wave_paths(self, n: int, sort_materials: bool | None = None):
         """Wavefront path slots per wave (0: library default) and, optionally,

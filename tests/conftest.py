@@ -29,7 +29,8 @@ def native_libs():
     from oracle import build as ob
     ob.build()
     from rayna_gb300 import build as rb
-    if _stale(rb.LIB, os.path.join(ROOT, "rayna_gb300", "csrc")) or _stale(rb.LIB, os.path.join(ROOT, "include")):
+    if any(_stale(lib, os.path.join(ROOT, d)) for lib in (rb.LIB, rb.LIB_EXACT)
+           for d in (os.path.join("rayna_gb300", "csrc"), "include")):
         rb.build()
     yield
 

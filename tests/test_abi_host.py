@@ -34,7 +34,55 @@ def test_library_exports_every_declared_symbol():
     for s in syms:
         assert hasattr(lib, s), s
     assert set(syms) == set(A.SIGNATURES), "ctypes signatures must cover the header exactly"
-    assert lib.rg_abi_version() == 6
+    assert lib.rg_abi_version() == A.RG_ABI_VERSION == 7
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_both_arithmetic_builds_load_and_export_the_same_symbols(exact):
+    lib = A.load_library(exact=exact)
+    for s in declared_symbols():
+        assert hasattr(lib, s), s
+    assert lib.rg_abi_version() == 7
+    assert A.load_library(exact=exact) is lib
+
+
+def test_header_constants_match_the_ctypes_mirror():
+    text = open(HEADER).read()
+    assert re.search(r"#define RG_SHARED_STACK_NONE 0xFFFFFFFFu", text)
+    for name in ("RG_DEVICE_STACK_OVERFLOW", "RG_DEVICE_BAD_INDEX", "RG_DEVICE_QUEUE_OVERFLOW"):
+        m = re.search(name + r" = (\d+)u", text)
+        assert m and int(m.group(1)) == getattr(A, name), name
+
+
+def _run_child(code, env_extra):
+    import subprocess
+    import sys
+    env = dict(os.environ, **env_extra)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return r.stdout.strip().splitlines()[-1]
+
+
+@pytest.mark.parametrize("exact", ["0", "1"])
+def test_forced_host_allocation_failure_reports_oom(exact):
+    """RAYNA_GPU_FAIL_ALLOC=1 fails the first allocation the library counts
+    (here the host arrays of the scene build): rg_inspect_scene returns
+    RG_OOM with a message instead of unwinding through the C ABI, and the
+    next call, with the injection spent, builds the scene."""
+    code = (
+        "import ctypes as C\n"
+        "from rayna_gb300 import _abi as A, presets\n"
+        "from rayna_gb300.scene import flatten\n"
+        "lib = A.load_library()\n"
+        "flat = flatten(presets.random_spheres(seed=0)[0])\n"
+        "info = A.rg_scene_info()\n"
+        "a = lib.rg_inspect_scene(C.byref(flat.desc), C.byref(info))\n"
+        "msg = A.last_error(lib, None)\n"
+        "b = lib.rg_inspect_scene(C.byref(flat.desc), C.byref(info))\n"
+        "print(a, b, info.n_prims, 'memory' in msg)\n")
+    out = _run_child(code, {"RAYNA_GPU_FAIL_ALLOC": "1", "RAYNA_GB300_EXACT": exact})
+    assert out == f"{A.RG_OOM} {A.RG_OK} 488 True", out
 
 
 def test_struct_sizes_match_header_layout():
