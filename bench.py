@@ -1,18 +1,26 @@
 """Benchmark of the per-sample path-tracing hot path on one GB300.
 
 A step is one progressive frame (Renderer::render, render/renderer.rs:224)
-of the workload at its full resolution and samples per pixel. Default
-workload: the triangle-mesh scene (displaced icosphere of 1,310,720
-triangles in a 12-triangle Cornell box, 1024x1024, 64 spp, depth 8).
+of a workload at its full resolution and samples per pixel. The headline
+workload is the triangle mesh (displaced icosphere of 1,310,720 triangles in
+a 12-triangle Cornell box, 1024x1024, 64 spp, depth 8); by default the run
+also times the random-spheres workload (400x225, 32 spp, depth 50) and the
+SDF + media workload (1280x720, 128 spp, depth 16), reported under
+`workloads` with their own roofline and CPU baseline.
+
+Every workload times the plain megakernel and the wavefront form (fused for
+the mesh and the spheres, material-sorted for the SDF scene, the library's
+defaults), so the wavefront / megakernel ratio is in the same line.
 
 Prints one JSON line:
-  value   Msamples/s over K frames, inputs resident in HBM, device time
-          (CUDA events around each frame on the renderer's stream; the L2 is
-          flushed with a 512 MB write between frames, outside the events)
-  e2e     the same metric through the public API (Renderer.render -> C ABI
-          rg_render) with the image copied back to host memory every frame
-  roofline, cpu_baseline, clocks, gpu_launches as described in the README of
-          the JSON keys below.
+  value    Msamples/s of the headline workload's fastest form, over K frames,
+           inputs resident in HBM, device time (CUDA events around each frame
+           on the renderer's stream; the L2 is flushed with a 512 MB write
+           between frames, outside the events)
+  e2e      the same metric through the public API (Renderer.render -> C ABI
+           rg_render) with the image copied back to host memory every frame
+  roofline of the dominant kernels (the traversal launches), see roofline()
+  cpu_baseline, clocks, gpu_launches, workloads, adjoint, batch
 
 --impl reference times the CPU restatement of the reference renderer (the
 reference crate cannot be built: no Rust toolchain) on the host cores.
@@ -139,23 +147,30 @@ class ClockSampler:
 
 def cpu_baseline(name: str, threads: int, target_s: float = 15.0):
     """Times the f64 CPU restatement of the reference renderer on a bounded
-    sample of the workload (same scene, camera, depth and spp; reduced
-    resolution), scaled to about `target_s` seconds of work."""
+    sample of the workload: a centred window of the full-resolution frame
+    (same scene, camera, pixels, depth and spp), sized to about `target_s`
+    seconds of work."""
     from oracle import binding as ob
-    from rayna_gb300.scene import RenderOpts, flatten
+    from rayna_gb300.scene import flatten
     scene, cam, opts = load_workload(name)
     flat = flatten(scene)
-    probe = RenderOpts(width=16, height=16, samples=opts.samples, ray_depth=opts.ray_depth)
-    st, _, _, secs = ob.render(flat, cam, probe, seed=1, frames=1, policy=ob.POLICY_REF_F64, threads=threads)
+
+    def centred(w, h):
+        return ((opts.width - w) // 2, (opts.height - h) // 2, w, h)
+
+    st, _, _, secs = ob.render_window(flat, cam, opts, centred(16, 16), seed=1, policy=ob.POLICY_REF_F64,
+                                      threads=threads)
+    assert st == 0
     per_px = max(secs, 1e-3) / (16 * 16)
     npx = int(max(256, min(opts.width * opts.height, target_s / per_px)))
-    side_w = max(16, int(round((npx * opts.width / opts.height) ** 0.5)))
-    side_h = max(16, int(round(npx / side_w)))
-    sample = RenderOpts(width=side_w, height=side_h, samples=opts.samples, ray_depth=opts.ray_depth)
-    st, _, _, secs = ob.render(flat, cam, sample, seed=2, frames=1, policy=ob.POLICY_REF_F64, threads=threads)
-    ns = side_w * side_h * opts.samples
+    w = min(opts.width, max(16, int(round((npx * opts.width / opts.height) ** 0.5))))
+    h = min(opts.height, max(16, int(round(npx / w))))
+    st, _, _, secs = ob.render_window(flat, cam, opts, centred(w, h), seed=2, policy=ob.POLICY_REF_F64,
+                                      threads=threads)
+    assert st == 0
+    ns = w * h * opts.samples
     return {"value": ns / secs / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
-            "sample": f"{side_w}x{side_h} px x {opts.samples} spp of the same scene and camera "
+            "sample": f"centred {w}x{h} window of the {opts.width}x{opts.height} frame x {opts.samples} spp "
                       f"({ns / 1e6:.2f} M samples, {secs:.1f} s), f64 oracle, {threads} threads"}, secs
 
 
@@ -270,8 +285,9 @@ def run_reference(args, rank, world):
 
 
 # DRAM bytes (read + write) per ray segment of the traversal kernels, from an
-# ncu capture of every traversal launch of one frame (profiles/), by
-# (workload, timed form); scaled to a frame by its ray segments.
+# ncu capture of the traversal launches of one frame (the profile summaries
+# beside this file), by (workload, timed form); scaled to a frame by its ray
+# segments.
 DRAM_BYTES_PER_SEGMENT = {
     # 18 k_extend launches of one 512x512x64 frame: 20.76 GB over 86.67 M segments
     ("mesh", "wavefront_sorted"): 239.5,
@@ -279,9 +295,8 @@ DRAM_BYTES_PER_SEGMENT = {
     ("mesh", "wavefront"): 242.3,
 }
 
-# Kernel configurations timed per workload: (form, material-sorted shading,
-# BVH width). "megakernel" is the plain form: one thread per pixel-sample over
-# binary node pairs.
+# Kernel configurations: (form, material-sorted shading, BVH width). The
+# megakernel is the plain form: one thread per pixel-sample.
 FORMS = {
     "megakernel": ("megakernel", False, 2),
     "megakernel_wide": ("megakernel", False, 8),
@@ -290,15 +305,180 @@ FORMS = {
     "wavefront_wide": ("wavefront", False, 8),
     "wavefront_sorted_wide": ("wavefront", True, 8),
 }
+# Forms timed by default: the plain megakernel and the wavefront form the
+# library picks for the scene (fused, or material-sorted for SDFs and media).
+DEFAULT_FORMS = {"mesh": ["megakernel", "wavefront"], "spheres": ["megakernel", "wavefront"],
+                 "sdf": ["megakernel", "wavefront_sorted"]}
+
+# Algorithmic work per unit (one node visit, one primitive test, one SDF
+# evaluation, one Mandelbulb escape iteration, one hit), fixed by formula:
+#   bytes: 64 per binary node pair (80 per 8-wide node), 48 per triangle test
+#          (v0, e1, e2), 16 per sphere test (centre, radius), 36 per normal
+#          fetch and 32 per material fetch at a hit, 12 per output pixel;
+#   FP32:  48 per binary node pair (two slab tests of 12 sub/mul + 12
+#          min/max), 184 per 8-wide node, 27 per Moller-Trumbore test, 17 per
+#          sphere test, 12 per SDF evaluation outside the escape loop, 55 per
+#          Mandelbulb iteration (the z^8 step by three complex squarings);
+#   SFU:   1 per triangle test (reciprocal), 1 per sphere test (square root),
+#          2 per SDF evaluation (square root, logarithm), 6 per Mandelbulb
+#          iteration (two square roots, four divisions).
+PRIM_COST = {"mesh": (48, 27, 1), "spheres": (16, 17, 1), "sdf": (16, 17, 1)}  # bytes, FP32, SFU per test
 
 
-def run_gpu(args, rank, world):
+def roofline(workload: str, r: dict, hbm_gbs: float, sm_count: int, sm_mhz: float) -> dict:
+    """Roofline of the dominant kernels of one frame (the traversal launches:
+    the megakernel, or the wavefront's bounce / extend kernels, timed live with
+    their own CUDA events): achieved = the largest of algorithmic bytes / time
+    against the measured HBM copy bandwidth, FP32 operations / time against
+    SMs x 128 lanes x 2 (FMA) x the sampled SM clock, and SFU operations / time
+    against SMs x 16 x the sampled clock."""
+    t = r["traverse_ms_per_step"] / 1e3
+    wide = r["bvh_width"] == 8
+    pb, pf, ps = PRIM_COST[workload]
+    npx = r["pixels"]
+    alg_bytes = (80 if wide else 64) * r["node_visits"] + pb * r["prim_tests"] + (36 + 32) * r["hits"] + 12 * npx
+    flops = (184 if wide else 48) * r["node_visits"] + pf * r["prim_tests"] + 12 * r["sdf_steps"] + 55 * r["sdf_iterations"]
+    sfu = ps * r["prim_tests"] + 2 * r["sdf_steps"] + 6 * r["sdf_iterations"]
+    fp32_peak = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s
+    sfu_peak = sm_count * 16 * sm_mhz * 1e6 / 1e12         # Tops/s
+    terms = {
+        "hbm": {"achieved": alg_bytes / t / 1e9, "peak": hbm_gbs, "unit": "GB/s"},
+        "fp32": {"achieved": flops / t / 1e12, "peak": fp32_peak, "unit": "TFLOP/s"},
+        "sfu": {"achieved": sfu / t / 1e12, "peak": sfu_peak, "unit": "Tops/s"},
+    }
+    for v in terms.values():
+        v["frac"] = v["achieved"] / v["peak"]
+    bound = max(terms, key=lambda k: terms[k]["frac"])
+    dram = DRAM_BYTES_PER_SEGMENT.get((workload, r["form"]))
+    traffic = dram * r["rays_per_frame"] if dram else None
+    b = terms[bound]
+    return {"bound": bound, "achieved": b["achieved"], "peak": b["peak"], "unit": b["unit"], "frac": b["frac"],
+            "traffic": traffic, "dram_frac": traffic / t / 1e9 / hbm_gbs if traffic else None,
+            "terms": terms, "per": "frame (all traversal launches of one frame)",
+            "algorithmic_bytes": alg_bytes, "fp32_ops": flops, "sfu_ops": sfu, "kernel_ms": t * 1e3,
+            "kernel_share": r["traverse_ms_per_step"] / r["ms_per_step"],
+            "peak_kind": "hbm: measured; fp32, sfu: SM count x lanes x sampled SM clock"}
+
+
+def time_form(name, scene, cam, opts, form, steps, warmup, stream, flush, rank, world, dist, dev, args, e2e=True):
+    """Times `steps` frames of one kernel configuration (after `warmup`) and
+    a counting frame for the work per frame."""
     import ctypes as C
 
     import torch
 
     from rayna_gb300 import Renderer
     from rayna_gb300 import _abi as A
+    kind, sort, width = FORMS[form]
+    r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank,
+                          stage_times=True)
+    r.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
+    # counting frame: algorithmic work per frame (node visits, primitive tests, SDF steps, hits)
+    rc = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=99, counters=True)
+    rc.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
+    cst = rc.render().stats
+    rc.close()
+    lib, h = r._lib, r.handle
+    st = A.rg_render_stats()
+    for _ in range(warmup):
+        A.check(lib, h, lib.rg_render_async(h, r.next_seed(), None, C.byref(st)))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    traverse_ms = 0.0
+    launches = 0
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        w0 = time.perf_counter()
+        for k in range(steps):
+            flush.fill_(float(k))
+            starts[k].record(stream)
+            A.check(lib, h, lib.rg_render_async(h, r.next_seed(), None, C.byref(st)))
+            ends[k].record(stream)
+            # the traversal kernels' own event pairs, read back after each frame
+            A.check(lib, h, lib.rg_sync_stats(h, C.byref(st)))
+            traverse_ms += st.traverse_ms
+            launches += st.kernel_launches
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    if dist:
+        dist.barrier()
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    dev_s = rank_max(sum(ms) / 1e3, dist, "cuda")
+    samples = opts.width * opts.height * opts.samples
+    e2e_s = float("nan")
+    if e2e:
+        # end to end: the public call with the image read back to host memory every frame
+        r.clear_accumulation()
+        for _ in range(2):
+            r.render()
+        e0 = time.perf_counter()
+        for _ in range(steps):
+            out = r.render()
+        e2e_s = time.perf_counter() - e0
+        assert out.stats.error_flags == 0, out.stats.error_flags
+    e2e_s = rank_max(e2e_s, dist, "cuda")
+    r.close()
+    return {
+        "form": form, "msamples_s": samples * steps * world / dev_s / 1e6, "ms_per_step": dev_s * 1e3 / steps,
+        "e2e_msamples_s": samples * steps * world / e2e_s / 1e6 if e2e else None,
+        "mrays_s": cst.rays * steps * world / dev_s / 1e6, "rays_per_frame": cst.rays,
+        "node_visits": cst.node_visits, "prim_tests": cst.prim_tests, "sdf_steps": cst.sdf_steps,
+        "sdf_iterations": cst.sdf_iterations, "hits": cst.hits, "pixels": opts.width * opts.height,
+        "wall_s": wall, "clocks": clk.summary(), "launches_per_frame": launches // max(steps, 1),
+        "bvh_width": width, "traverse_ms_per_step": traverse_ms / steps, "steps": steps,
+    }
+
+
+def run_workload(name, forms, steps, warmup, stream, flush, rank, world, dist, dev, args, e2e_best=True):
+    """Every form of one workload; returns (results by form, best form)."""
+    scene, cam, opts = load_workload(name)
+    if name == args.workload:
+        if args.width:
+            opts.width = args.width
+        if args.height:
+            opts.height = args.height
+        if args.spp:
+            opts.samples = args.spp
+    res = {}
+    for form in forms:
+        from rayna_gb300 import _abi as A
+        try:
+            res[form] = time_form(name, scene, cam, opts, form, steps, warmup, stream, flush, rank, world, dist,
+                                  dev, args, e2e=False)
+        except A.RaynaError as e:
+            res[form] = {"error": str(e)}
+    ok = {f: v for f, v in res.items() if "error" not in v}
+    best = max(ok, key=lambda f: ok[f]["msamples_s"])
+    if e2e_best and not args.no_e2e:
+        # the best form again, end to end through Renderer.render
+        res[best] = time_form(name, scene, cam, opts, best, steps, warmup, stream, flush, rank, world, dist, dev,
+                              args, e2e=True)
+    return res, best
+
+
+def summarise(name, res, best, hbm, sm_count):
+    """The per-workload JSON object: forms, ratio, roofline of the best form."""
+    keys = ("msamples_s", "mrays_s", "e2e_msamples_s", "ms_per_step", "rays_per_frame", "node_visits", "prim_tests",
+            "sdf_steps", "sdf_iterations", "hits", "wall_s", "launches_per_frame", "bvh_width", "steps",
+            "traverse_ms_per_step")
+    b = res[best]
+    clk = b["clocks"].get("sm_mhz") or 2070.0
+    out = {"workload": WORKLOADS[name], "best_form": best, "msamples_s": b["msamples_s"],
+           "forms": {f: ({k: v[k] for k in keys} if "error" not in v else v) for f, v in res.items()},
+           "roofline": roofline(name, b, hbm, sm_count, clk), "clocks": b["clocks"]}
+    if "megakernel" in res and "error" not in res["megakernel"]:
+        wf = [f for f in res if f.startswith("wavefront") and "error" not in res[f]]
+        if wf:
+            w = max(wf, key=lambda f: res[f]["msamples_s"])
+            out["wavefront_over_megakernel"] = res[w]["msamples_s"] / res["megakernel"]["msamples_s"]
+    return out
+
+
+def run_gpu(args, rank, world):
+    import torch
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
@@ -306,132 +486,59 @@ def run_gpu(args, rank, world):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    scene, cam, opts = load_workload(args.workload)
-    if args.width:
-        opts.width = args.width
-    if args.height:
-        opts.height = args.height
-    if args.spp:
-        opts.samples = args.spp
     # a dedicated stream: the library launches on it, so events on it time its kernels
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    forms = list(FORMS) if args.form == "best" else [args.form]
-    results = {}
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    t_setup = time.perf_counter()
-    for form in forms:
-        kind, sort, width = FORMS[form]
-        try:
-            r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank,
-                                  stage_times=True)
-            r.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
-        except A.RaynaError as e:
-            results[form] = {"error": str(e)}
-            continue
-        # counting frame: algorithmic work per frame (node visits, primitive tests)
-        rc = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=99, counters=True)
-        rc.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
-        cst = rc.render().stats
-        rc.close()
-        lib, h = r._lib, r.handle
-        st = A.rg_render_stats()
-        for i in range(args.warmup):
-            A.check(lib, h, lib.rg_render_async(h, r.next_seed(), None, C.byref(st)))
-        torch.cuda.synchronize()
+    hbm, _ = measured_peaks()
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    forms = (list(FORMS) if args.form == "all" else
+             DEFAULT_FORMS[args.workload] if args.form == "default" else args.form.split(","))
+    res, best = run_workload(args.workload, forms, args.steps, args.warmup, stream, flush, rank, world, dist, dev, args)
+    if rank != 0 and not (world == 1):
         if dist:
-            dist.barrier()
-        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        rays = 0
-        torch.cuda.synchronize()
-        traverse_ms = 0.0
-        with ClockSampler(dev) as clk:
-            w0 = time.perf_counter()
-            for k in range(args.steps):
-                flush.fill_(float(k))
-                starts[k].record(stream)
-                A.check(lib, h, lib.rg_render_async(h, r.next_seed(), None, C.byref(st)))
-                ends[k].record(stream)
-                # the traversal kernels' own event pairs, read back after each frame
-                A.check(lib, h, lib.rg_sync_stats(h, C.byref(st)))
-                traverse_ms += st.traverse_ms
-            torch.cuda.synchronize()
-            wall = time.perf_counter() - w0
-        if dist:
-            dist.barrier()
-        ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-        dev_s = rank_max(sum(ms) / 1e3, dist, "cuda")
-        samples = opts.width * opts.height * opts.samples
-        assert st.error_flags == 0, st.error_flags
-        # end-to-end: the public call with the image read back to host memory every frame
-        e2e_s = float("nan")
-        if not args.no_e2e:
-            r.clear_accumulation()
-            for _ in range(2):
-                r.render()
-            e0 = time.perf_counter()
-            for _ in range(args.steps):
-                out = r.render()
-            e2e_s = time.perf_counter() - e0
-            assert out.stats.error_flags == 0, out.stats.error_flags
-        e2e_s = rank_max(e2e_s, dist, "cuda")
-        results[form] = {
-            "msamples_s": samples * args.steps * world / dev_s / 1e6,
-            "ms_per_step": dev_s * 1e3 / args.steps,
-            "e2e_msamples_s": samples * args.steps * world / e2e_s / 1e6,
-            "mrays_s": cst.rays * args.steps * world / dev_s / 1e6,
-            "rays_per_frame": cst.rays, "node_visits": cst.node_visits, "prim_tests": cst.prim_tests,
-            "sdf_steps": cst.sdf_steps, "wall_s": wall, "clocks": clk.summary(), "device_ms": ms,
-            "launches_per_frame": st.kernel_launches, "bvh_width": width,
-            "traverse_ms_per_step": traverse_ms / args.steps,
-        }
-        r.close()
-    if rank != 0:
+            dist.destroy_process_group()
         return
-    ok = {f: v for f, v in results.items() if "error" not in v}
-    best = max(ok, key=lambda f: ok[f]["msamples_s"])
-    b = ok[best]
-    hbm, peak_kind = measured_peaks()
-    npx = opts.width * opts.height
-    # Roofline of the dominant kernels, the traversal launches of a frame (the
-    # megakernel, or the wavefront's extend / bounce kernels), timed live with
-    # their own CUDA events: algorithmic bytes = one node fetch per node visit
-    # (64 B pair, 80 B wide node) + 48 B per primitive test + the 48-byte path
-    # record per ray segment.
-    node_bytes = 80 if b["bvh_width"] == 8 else 64
-    alg_bytes = node_bytes * b["node_visits"] + 48 * b["prim_tests"] + 48 * b["rays_per_frame"]
-    achieved = alg_bytes / (b["traverse_ms_per_step"] / 1e3) / 1e9
-    dram_per_segment = DRAM_BYTES_PER_SEGMENT.get((args.workload, best))
-    traffic = dram_per_segment * b["rays_per_frame"] if dram_per_segment else None
+    head = summarise(args.workload, res, best, hbm, sm_count)
+    b = res[best]
+    opts_px = b["pixels"]
+    gpu_launches = sum(v["launches_per_frame"] * v["steps"] for v in res.values() if "error" not in v)
     line = {
         "metric": "Msamples/s", "value": b["msamples_s"], "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "form": best, "l2": "flushed (512 MB write) between frames",
-                   "parallelism": f"replicas{world}"},
+                   "parallelism": f"replicas{world}", "build": "performance (-fmad=true)"},
         "e2e": {"value": b["e2e_msamples_s"], "unit": "Msamples/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": npx * 12},
+                "d2h_bytes_per_step": opts_px * 12},
         "mrays_s": b["mrays_s"],
-        "forms": {f: {k: v[k] for k in ("msamples_s", "mrays_s", "e2e_msamples_s", "ms_per_step", "rays_per_frame",
-                                         "node_visits", "prim_tests", "sdf_steps", "wall_s", "launches_per_frame",
-                                         "bvh_width")} if "error" not in v
-                  else v for f, v in results.items()},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_kind": peak_kind, "traffic": traffic, "per": "frame (all traversal launches of one frame)",
-                     "algorithmic_bytes": alg_bytes, "kernel_ms": b["traverse_ms_per_step"],
-                     "kernel_share": b["traverse_ms_per_step"] / b["ms_per_step"]},
-        "gpu_launches": b["launches_per_frame"] * args.steps,
+        "forms": head["forms"],
+        "wavefront_over_megakernel": head.get("wavefront_over_megakernel"),
+        "roofline": head["roofline"],
+        "gpu_launches": gpu_launches,
         "clocks": b["clocks"],
     }
+    if world == 1 and args.all_workloads:
+        line["workloads"] = {}
+        for name in WORKLOADS:
+            if name == args.workload:
+                continue
+            sub_steps = min(args.steps, args.sub_steps)
+            r2, b2 = run_workload(name, DEFAULT_FORMS[name], sub_steps, min(args.warmup, 3), stream, flush, rank,
+                                  world, dist, dev, args)
+            line["workloads"][name] = summarise(name, r2, b2, hbm, sm_count)
+            line["gpu_launches"] += sum(v["launches_per_frame"] * v["steps"] for v in r2.values() if "error" not in v)
     if world == 1 and not args.no_adjoint:
         line["adjoint"] = run_adjoint(stream=stream)
     if world == 1 and args.batch_scale > 0:
         line["batch"] = run_batch(args.batch_scale, max(2, args.steps), stream=stream)
     if world == 1 and not args.no_cpu_baseline:
         from oracle import binding as ob
-        cb, _ = cpu_baseline(args.workload, ob.hardware_threads(), target_s=args.ref_seconds)
+        threads = ob.hardware_threads()
+        cb, _ = cpu_baseline(args.workload, threads, target_s=args.ref_seconds)
         line["cpu_baseline"] = cb
+        for name, w in line.get("workloads", {}).items():
+            w["cpu_baseline"], _ = cpu_baseline(name, threads, target_s=args.ref_seconds / 2)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -444,19 +551,28 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="mesh")
-    ap.add_argument("--form", choices=["best"] + list(FORMS), default="best")
+    ap.add_argument("--form", default="default",
+                    help="'default' (megakernel and the library's wavefront form), 'all', or a comma list of " +
+                         ", ".join(FORMS))
     ap.add_argument("--fetch-budget", type=int, default=0,
                     help="node visits between refills in the persistent wavefront kernels (0: library default)")
-    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=0, help="override the workload resolution (profiling)")
     ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--only", action="store_true", help="time the --workload alone (no `workloads` sub-results)")
+    ap.add_argument("--sub-steps", type=int, default=5, help="timed frames of the other workloads")
     ap.add_argument("--batch-scale", type=float, default=1.0,
                     help="resolution scale of the batched workload (1: the configured resolutions; 0: skip)")
     args = ap.parse_args()
+    args.all_workloads = not args.only
+    if args.form not in ("default", "all"):
+        for f in args.form.split(","):
+            if f not in FORMS:
+                ap.error(f"unknown form {f}")
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
     if args.impl == "reference":

@@ -289,7 +289,7 @@ typedef struct rg_render_stats {
     uint64_t rays;            /* extend queries (ray segments) this frame */
     uint64_t node_visits;     /* BVH node pairs fetched (RG_FLAG_COUNTERS only, else 0) */
     uint64_t prim_tests;      /* primitive tests (RG_FLAG_COUNTERS only, else 0) */
-    uint64_t sdf_steps;       /* SDF evaluations (RG_FLAG_COUNTERS only, else 0) */
+    uint64_t sdf_steps;       /* SDF evaluations, the normals' central differences included (RG_FLAG_COUNTERS only) */
     uint32_t accum_frames;    /* AccumulationBuffer::frame_count */
     uint32_t img_width;       /* dimensions of the image written to out_rgb */
     uint32_t img_height;
@@ -301,6 +301,8 @@ typedef struct rg_render_stats {
     uint64_t invalid_hits;    /* RG_FLAG_VALIDATE: hits or path colours that broke an invariant this frame */
     uint32_t invalid_mask;    /* RG_FLAG_VALIDATE: RG_INVALID_* bits of the invariants broken */
     uint32_t reserved0;
+    uint64_t hits;            /* closest-hit queries that found a surface (RG_FLAG_COUNTERS only, else 0) */
+    uint64_t sdf_iterations;  /* Mandelbulb escape-loop iterations in the SDF evaluations (RG_FLAG_COUNTERS only) */
 } rg_render_stats;
 
 /* Device error bits (rg_render_stats.error_flags). They are cleared at the start
@@ -375,7 +377,9 @@ rg_status rg_last_error(rg_handle h, char* buf, size_t len);
 rg_status rg_inspect_scene(const rg_scene_desc* scene, rg_scene_info* out);
 
 /* Renderer::set_scene (renderer.rs:165-168): copies the scene to the device,
- * builds the BVH and clears the accumulation buffer. */
+ * builds the BVH and clears the accumulation buffer. A scene rejected by
+ * validation leaves the previous one in place; a failed device upload
+ * (RG_OOM, RG_CUDA_ERROR) leaves the empty scene. */
 rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene);
 
 /* Launch-shape knobs of the kernel forms (no reference counterpart: the

@@ -127,7 +127,8 @@ class rg_render_stats(C.Structure):
                 ("sdf_steps", C.c_uint64), ("accum_frames", C.c_uint32), ("img_width", C.c_uint32),
                 ("img_height", C.c_uint32), ("num_threads", C.c_uint32), ("error_flags", C.c_uint32),
                 ("kernel_launches", C.c_uint32), ("traverse_ms", C.c_double), ("invalid_hits", C.c_uint64),
-                ("invalid_mask", C.c_uint32), ("reserved0", C.c_uint32)]
+                ("invalid_mask", C.c_uint32), ("reserved0", C.c_uint32), ("hits", C.c_uint64),
+                ("sdf_iterations", C.c_uint64)]
 
 
 class rg_scene_info(C.Structure):

@@ -214,7 +214,9 @@ enum : uint32_t {
 enum : uint32_t {
   CNT_RAYS = 0, CNT_NODES = 1, CNT_PRIMS = 2, CNT_SDF = 3, CNT_SAMPLES = 4,
   CNT_INVALID = 5, CNT_INVALID_MASK = 6,  // RG_FLAG_VALIDATE: broken invariants, and which (RG_INVALID_*)
-  CNT_N = 8
+  CNT_SDF_ITERS = 7,  // Mandelbulb escape-loop iterations inside the SDF evaluations
+  CNT_HITS = 8,       // closest-hit queries that found a surface
+  CNT_N = 16
 };
 
 // Per-frame launch parameters (all f32 values rounded from the f64 host viewport).

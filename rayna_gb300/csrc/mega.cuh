@@ -104,16 +104,20 @@ __device__ __forceinline__ void flush_counters(const FrameParams& fp, const Coun
   for (int o = 16; o > 0; o >>= 1) seg += __shfl_down_sync(0xffffffffu, seg, o);
   if (lane == 0 && seg) atomicAdd(fp.counters + CNT_RAYS, seg);
   if (COUNT) {
-    unsigned long long a = cnt.nodes, b = cnt.prims, c = cnt.sdf_steps;
+    unsigned long long a = cnt.nodes, b = cnt.prims, c = cnt.sdf_steps, d = cnt.sdf_iters, e = cnt.hits;
     for (int o = 16; o > 0; o >>= 1) {
       a += __shfl_down_sync(0xffffffffu, a, o);
       b += __shfl_down_sync(0xffffffffu, b, o);
       c += __shfl_down_sync(0xffffffffu, c, o);
+      d += __shfl_down_sync(0xffffffffu, d, o);
+      e += __shfl_down_sync(0xffffffffu, e, o);
     }
     if (lane == 0) {
       atomicAdd(fp.counters + CNT_NODES, a);
       atomicAdd(fp.counters + CNT_PRIMS, b);
       atomicAdd(fp.counters + CNT_SDF, c);
+      atomicAdd(fp.counters + CNT_SDF_ITERS, d);
+      atomicAdd(fp.counters + CNT_HITS, e);
     }
   }
 }

@@ -949,7 +949,22 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene) {
   }
   if (st != RG_OK) return st;
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "rg_set_scene");
-  if ((st = upload_scene(h, hs)) != RG_OK) return st;
+  if ((st = upload_scene(h, hs)) != RG_OK) {
+    // The device arrays are partly replaced: drop them all and hold the empty
+    // scene (what Renderer::new_default starts from), so nothing points at
+    // freed memory.
+    cudaStreamSynchronize(h->stream);
+    free_scene(h->dev);
+    const uint32_t sky = h->gs.sky;
+    h->gs = GpuScene{};
+    h->gs.sky = sky;
+    h->host = HostScene{};
+    h->have_scene = false;
+    h->kinds = F_ALL;
+    apply_features(h);
+    h->frame_current = false;
+    return st;
+  }
   h->host = std::move(hs);
   h->have_scene = true;
   on_scene_changed(h);
@@ -1144,6 +1159,8 @@ rg_status rg_sync_stats(rg_handle h, rg_render_stats* stats) {
   stats->node_visits = c[CNT_NODES];
   stats->prim_tests = c[CNT_PRIMS];
   stats->sdf_steps = c[CNT_SDF];
+  stats->hits = c[CNT_HITS];
+  stats->sdf_iterations = c[CNT_SDF_ITERS];
   stats->accum_frames = h->frame_count;
   stats->img_width = h->opts.width;
   stats->img_height = h->opts.height;

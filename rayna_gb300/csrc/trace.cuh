@@ -245,7 +245,8 @@ __device__ __forceinline__ bool volume_t(const GpuPrim& p, uint32_t kind, uint32
 // ---------------------------------------------------------------------------
 constexpr float kBulbInner = 1.2f, kBulbOuter = 1.5f;
 
-__device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x) {
+// `iter_count`, when given, counts the Mandelbulb's escape-loop iterations (work counters).
+__device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long long* iter_count = nullptr) {
   V3 q = x - v3(s.cx, s.cy, s.cz);
   if (s.kind == RG_SDF_SPHERE) return length3(q) - s.p0;
   if (s.kind == RG_SDF_TORUS) {
@@ -255,6 +256,7 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x) {
   // Mandelbulb distance estimator: z -> z^power + c in spherical coordinates
   // with the running derivative dr; outside kBulbOuter the distance to the
   // enclosing sphere of radius kBulbInner is used (a lower bound).
+  unsigned long long* counted = iter_count;
   float sc = s.p2;
   V3 z0 = v3(q.x / sc, q.y / sc, q.z / sc);
   float rq = length3(z0);
@@ -267,6 +269,7 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x) {
     // z^8 without transcendentals: with cos t = z/r, sin t = rho/r and
     // cos p + i sin p = (x + i y)/rho, three complex squarings give 8t and 8p.
     for (int i = 0; i < iters; ++i) {
+      if (counted) ++*counted;
       float rho2 = z.x * z.x + z.y * z.y;
       float r2 = rho2 + z.z * z.z;
       rr = __fsqrt_rn(r2);
@@ -391,43 +394,96 @@ __device__ __forceinline__ bool cylinder_t(const GpuPrim& p, const Ray& r, float
 struct SdfHit { float t; V3 n; bool front; uint32_t side; bool flip; };
 
 // RaymarchedIsosurfaceMesh::intersect (mesh/isosurface/raymarched.rs:73-122)
-// with two exact early exits that cannot change the result:
+// as a resumable march: sdf_march_begin, then sdf_march_step until it returns
+// a hit or a miss, then sdf_march_hit for the hit record. Two exact early
+// exits cannot change the result:
 //  - total distance is non-decreasing, so once it passes the distance that
 //    must be beaten (`beat`, inclusive when nothing has been hit yet) no later
 //    step can produce the closest hit;
 //  - outside the function's bound radius and moving away, every later step
 //    evaluates to more than epsilon, so no later step can hit.
+struct SdfMarch {
+  float total;  // distance marched from the ray's origin
+  V3 point;     // ray.at(total)
+  uint32_t i;   // steps taken (the hit's Intersection::side)
+  float d;      // the last evaluation (its sign is the hit's front face)
+};
+enum : int { kMarchOn = 0, kMarchHit = 1, kMarchMiss = 2 };
+
+__device__ __forceinline__ void sdf_march_begin(const Ray& r, float start, SdfMarch& m) {
+  m.total = start;
+  m.point = at3(r.o, r.d, start);
+  m.i = 0;
+  m.d = 0.0f;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ int sdf_march_step(const GpuSdf& s, const Ray& r, float start, float end, float beat,
+                                              bool beat_inclusive, SdfMarch& m, unsigned long long& steps,
+                                              unsigned long long& iters) {
+  const float d = sdf_eval(s, m.point, COUNT ? &iters : nullptr);
+  if (COUNT) ++steps;
+  m.total = m.total + fabsf(d);
+  m.point = at3(r.o, r.d, m.total);
+  m.d = d;
+  const bool beaten = beat_inclusive ? m.total <= beat : m.total < beat;
+  if (fabsf(d) < s.eps && start <= m.total && m.total <= end) return beaten ? kMarchHit : kMarchMiss;
+  if (m.i > s.max_iter) return kMarchMiss;
+  if (!beaten) return kMarchMiss;
+  const V3 q = m.point - v3(s.cx, s.cy, s.cz);
+  if (dot3(q, q) > s.bound_radius * s.bound_radius && dot3(q, r.d) > 0.0f) return kMarchMiss;
+  ++m.i;
+  return kMarchOn;
+}
+
+// The hit record at a step that returned kMarchHit: the normal by central
+// differences with step epsilon (raymarched.rs:107-111), not flipped.
+template <bool COUNT>
+__device__ __forceinline__ void sdf_march_hit(const GpuSdf& s, const SdfMarch& m, SdfHit& h, unsigned long long& steps) {
+  const float eps = s.eps;
+  const V3 pp = m.point;
+  if (COUNT) steps += 6;
+  V3 g = v3(sdf_eval(s, v3(pp.x + eps, pp.y, pp.z)) - sdf_eval(s, v3(pp.x - eps, pp.y, pp.z)),
+            sdf_eval(s, v3(pp.x, pp.y + eps, pp.z)) - sdf_eval(s, v3(pp.x, pp.y - eps, pp.z)),
+            sdf_eval(s, v3(pp.x, pp.y, pp.z + eps)) - sdf_eval(s, v3(pp.x, pp.y, pp.z - eps)));
+  h.t = m.total;
+  h.n = normalize3(g);
+  h.front = !signbit(m.d);
+  h.side = m.i;
+  h.flip = false;
+}
+
+// The whole march in one call.
 template <bool COUNT>
 __device__ bool sdf_march(const GpuSdf& s, const Ray& r, float start, float end, float beat, bool beat_inclusive, SdfHit& h,
-                          unsigned long long& steps) {
-  float eps = s.eps;
-  float total = start;
-  V3 c = v3(s.cx, s.cy, s.cz);
-  V3 point = at3(r.o, r.d, total);
-  float br2 = s.bound_radius * s.bound_radius;
-  for (uint32_t i = 0;; ++i) {
-    float d = sdf_eval(s, point);
-    if (COUNT) ++steps;
-    total = total + fabsf(d);
-    point = at3(r.o, r.d, total);
-    if (fabsf(d) < eps && start <= total && total <= end) {
-      if (!(beat_inclusive ? total <= beat : total < beat)) return false;
-      V3 pp = point;
-      V3 g = v3(sdf_eval(s, v3(pp.x + eps, pp.y, pp.z)) - sdf_eval(s, v3(pp.x - eps, pp.y, pp.z)),
-                sdf_eval(s, v3(pp.x, pp.y + eps, pp.z)) - sdf_eval(s, v3(pp.x, pp.y - eps, pp.z)),
-                sdf_eval(s, v3(pp.x, pp.y, pp.z + eps)) - sdf_eval(s, v3(pp.x, pp.y, pp.z - eps)));
-      h.t = total;
-      h.n = normalize3(g);
-      h.front = !signbit(d);
-      h.side = i;
-      h.flip = false;
+                          unsigned long long& steps, unsigned long long& iters) {
+  SdfMarch m;
+  sdf_march_begin(r, start, m);
+  for (;;) {
+    const int st = sdf_march_step<COUNT>(s, r, start, end, beat, beat_inclusive, m, steps, iters);
+    if (st == kMarchMiss) return false;
+    if (st == kMarchHit) {
+      sdf_march_hit<COUNT>(s, m, h, steps);
       return true;
     }
-    if (i > s.max_iter) return false;
-    if (!(beat_inclusive ? total <= beat : total < beat)) return false;
-    V3 q = point - c;
-    if (dot3(q, q) > br2 && dot3(q, r.d) > 0.0f) return false;
   }
+}
+
+// Whether the segment [start, lim] of the ray can reach the SDF's bound
+// sphere (radius widened by 1e-3 relative for the test's own rounding): when
+// it cannot, the march above returns no hit, since a hit needs a point within
+// epsilon of the surface and every such point lies inside the bound.
+__device__ __forceinline__ bool sdf_bound_reachable(const GpuSdf& s, const Ray& r, float start, float lim) {
+  const V3 oc = r.o - v3(s.cx, s.cy, s.cz);
+  const float R = s.bound_radius * 1.001f;
+  const float b = dot3(oc, r.d);
+  // r^2 - |l|^2 with l the centre-to-line vector: no cancellation for distant origins
+  const V3 l = v3(__fmaf_rn(-b, r.d.x, oc.x), __fmaf_rn(-b, r.d.y, oc.y), __fmaf_rn(-b, r.d.z, oc.z));
+  const float disc = R * R - dot3(l, l);
+  if (disc < 0.0f) return false;
+  const float sq = __fsqrt_rn(disc);
+  const float slack = 1e-3f * (fabsf(b) + R);
+  return -b + sq + slack >= start && -b - sq - slack <= lim;
 }
 
 // ---------------------------------------------------------------------------
@@ -442,7 +498,7 @@ struct HitRec {
 };
 
 struct Counters {
-  unsigned long long nodes = 0, prims = 0, sdf_steps = 0;
+  unsigned long long nodes = 0, prims = 0, sdf_steps = 0, sdf_iters = 0, hits = 0;
 };
 
 
@@ -854,7 +910,7 @@ __device__ __forceinline__ bool finish_hit(const GpuScene& sc, const Ray& r, flo
         if (!plane_t(v3(f.cx, f.cy, f.cz), f.p0, r, start, end, pt, denom) || (any && !(pt < h.t))) continue;
         sh = SdfHit{pt, v3(f.cx, f.cy, f.cz), (bool)signbit(denom), 0u, !signbit(denom)};
       } else if (F & F_SDF) {
-        if (!sdf_march<COUNT>(f, r, start, end, any ? h.t : end, !any, sh, cnt.sdf_steps)) continue;
+        if (!sdf_march<COUNT>(f, r, start, end, any ? h.t : end, !any, sh, cnt.sdf_steps, cnt.sdf_iters)) continue;
       } else {
         continue;
       }
@@ -864,6 +920,7 @@ __device__ __forceinline__ bool finish_hit(const GpuScene& sc, const Ray& r, flo
       any = true;
     }
   }
+  if (COUNT && any) ++cnt.hits;
   return any;
 }
 

@@ -154,9 +154,52 @@ __device__ __forceinline__ void record_hit(const GpuScene& sc, const FrameParams
   }
 }
 
+// `defer`: the scene's raymarched SDFs (and infinite planes) are left to the
+// k_march stages; this kernel stores the tree's closest hit in the path
+// record (distance, primitive, mesh-space distance of a transformed hit) and
+// appends nothing to the kind queues.
+// After the last SDF's march: the infinite planes (tested after the SDFs, in
+// list order, replacing the hit only when strictly closer) and the path's
+// material-kind queue.
+template <uint32_t F, bool COUNT>
+__device__ __forceinline__ void finish_march(const GpuScene& sc, const FrameParams& fp, const PathState& s,
+                                             const WaveParams& wp, uint32_t p, const Ray& r, Counters& cnt) {
+  HitRec h;
+  const float4 r1 = s.rec[3 * (size_t)p + 1];
+  const int code = __float_as_int(s.rec[3 * (size_t)p + 2].w);
+  bool any = code != kPrimMiss;
+  h.t = r1.w;
+  h.prim = code >= 0 ? code : -1;
+  h.sdf = code <= -2 ? -2 - code : -1;
+  h.tl = 0.0f;
+  if (h.sdf >= 0) {
+    const float4 a = s.aux[p];
+    const uint32_t fl = __float_as_uint(a.w);
+    h.sh = SdfHit{h.t, v3(a.x, a.y, a.z), (fl >> 31) != 0, fl & 0x3FFFFFFFu, false};
+  } else if ((F & F_EXT) && sc.prim_xform && h.prim >= 0) {
+    h.tl = s.aux[p].x;
+  }
+  if (F & F_PLANE) {
+    for (uint32_t k = 0; k < sc.n_sdfs; ++k) {
+      const GpuSdf& f = sc.sdfs[k];
+      if (f.kind != kUnboundedPlane) continue;
+      // InfinitePlaneMesh::intersect (mesh/planar/infinite_plane.rs:87-92)
+      float pt, denom;
+      if (!plane_t(v3(f.cx, f.cy, f.cz), f.p0, r, 1e-3f, 3.402823466e38f, pt, denom) || (any && !(pt < h.t))) continue;
+      h.t = pt;
+      h.sdf = (int)k;
+      h.prim = -1;
+      h.sh = SdfHit{pt, v3(f.cx, f.cy, f.cz), (bool)signbit(denom), 0u, !signbit(denom)};
+      any = true;
+    }
+  }
+  if (COUNT && any) ++cnt.hits;
+  record_hit<F, COUNT>(sc, fp, s, wp, p, any, h);
+}
+
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
-                                                     int budget) {
+                                                     int budget, int defer) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
@@ -198,13 +241,92 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
       const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
       if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget)) {
         HitRec h;
-        const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
-        record_hit<F, COUNT>(sc, fp, s, wp, p, hit, h);
+        if ((F & F_SDF) && defer) {
+          if (finish_hit<F & ~(F_SDF | F_PLANE), false>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt)) {
+            s.rec[3 * (size_t)p + 1].w = h.t;
+            s.rec[3 * (size_t)p + 2].w = __int_as_float(h.prim);
+            if ((F & F_EXT) && sc.prim_xform) s.aux[p].x = h.tl;
+          }
+        } else {
+          const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
+          record_hit<F, COUNT>(sc, fp, s, wp, p, hit, h);
+        }
         has = false;
       }
     }
   }
   flush_wave_counters<COUNT>(fp, cnt, queries);
+}
+
+// Material-sorted variant with raymarched SDFs, stage 1b: the march of SDF k
+// (the unbounded list's k-th object) for every path of the bounce, after the
+// tree (k_extend with `defer`) and the SDFs before k. It replaces the path's
+// hit when strictly closer (or when nothing was hit), as ObjectList's loop
+// over unbounded objects does (object/list.rs:112-129). Persistent with
+// dynamic fetch: every lane marches the same function, `budget` evaluations
+// at a time, and lanes whose march has ended take the next path (one atomic
+// per warp), so a long march does not hold idle lanes. Paths whose segment
+// cannot reach the function's bound sphere end at once. The last stage also
+// tests the infinite planes and appends each path to its material kind's
+// queue.
+template <uint32_t F, bool COUNT>
+__global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
+                                                    uint32_t k, int last, int budget) {
+  const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
+  uint32_t* next = s.counts + kFetchCounter;
+  const uint32_t lane = threadIdx.x & 31u;
+  const GpuSdf f = sc.sdfs[k];
+  const float start = 1e-3f, end = 3.402823466e38f;
+  Counters cnt;
+  bool has = false, drained = false;
+  uint32_t p = 0;
+  Ray r;
+  float best = 0.0f;
+  bool any = false;
+  SdfMarch m;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !has);
+    if (idle && !drained) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(next, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= n) drained = true;
+      if (!has) {
+        const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (i < n) {
+          p = s.active[cur][i];
+          const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1];
+          r.o = v3(r0.x, r0.y, r0.z);
+          r.d = v3(r1.x, r1.y, r1.z);
+          any = __float_as_int(s.rec[3 * (size_t)p + 2].w) != kPrimMiss;
+          best = r1.w;
+          has = true;
+          sdf_march_begin(r, start, m);
+          if (!sdf_bound_reachable(f, r, start, any ? best : end)) has = false;
+          if (!has && last) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, has)) break;
+    if (has) {
+      int st = kMarchOn;
+      for (int e = 0; e < budget && st == kMarchOn; ++e)
+        st = sdf_march_step<COUNT>(f, r, start, end, any ? best : end, !any, m, cnt.sdf_steps, cnt.sdf_iters);
+      if (st != kMarchOn) {
+        if (st == kMarchHit) {
+          SdfHit sh;
+          sdf_march_hit<COUNT>(f, m, sh, cnt.sdf_steps);
+          s.rec[3 * (size_t)p + 1].w = sh.t;
+          s.rec[3 * (size_t)p + 2].w = __int_as_float(-2 - (int)k);
+          s.aux[p] = make_float4(sh.n.x, sh.n.y, sh.n.z,
+                                 __uint_as_float((sh.front ? 0x80000000u : 0u) | (sh.side & 0x3FFFFFFFu)));
+        }
+        if (last) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
+        has = false;
+      }
+    }
+  }
+  flush_wave_counters<COUNT>(fp, cnt, 0);
 }
 
 // Material-sorted variant, stage 2: shading over the kind queues end to end.
@@ -290,6 +412,16 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bounce_per_sm, k_bounce<F, true>, kWfBlock, smem);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bounce_per_sm, k_bounce<F, false>, kWfBlock, smem);
   const int bounce_grid = sm_count(h->device) * std::max(bounce_per_sm, 1);
+  // Raymarched SDFs in the material-sorted form: one k_march stage per SDF
+  // after the tree (h->host.nsdf SDFs lead the unbounded list).
+  const uint32_t n_march = (F & F_SDF) && sorted ? h->host.nsdf : 0u;
+  const int march_budget = (int)kMarchBudget;
+  int march_per_sm = 0;
+  if (n_march) {
+    if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&march_per_sm, k_march<F, true>, kWfBlock, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&march_per_sm, k_march<F, false>, kWfBlock, 0);
+  }
+  const int march_grid = sm_count(h->device) * std::max(march_per_sm, 1);
   cudaStream_t st = h->stream;
   cudaError_t e;
   uint32_t launches = 0;
@@ -301,7 +433,8 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
     wp.capacity = (uint32_t)cap;
     uint32_t gen_blocks = (uint32_t)std::min<size_t>((wp.n_paths + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
     k_generate<<<gen_blocks, kWfBlock, 0, st>>>(fp, s, wp);
-    launches += 2 + fp.ray_depth + 1 + (sorted ? fp.ray_depth + 1 : 0);  // generate, accumulate, bounce stages
+    // generate, accumulate, and per bounce the bounce kernel or extend + march stages + shade
+    launches += 2 + (fp.ray_depth + 1) * (sorted ? 2 + n_march : 1);
     int cur = 0;
     for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
       if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
@@ -309,8 +442,15 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
       if (sorted) {
         if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
-        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget);
-        else k_extend<F, false><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget);
+        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, n_march > 0);
+        else k_extend<F, false><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, n_march > 0);
+        // the SDFs in list order, each over every path of the bounce
+        for (uint32_t k = 0; k < n_march; ++k) {
+          if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+          const int last = k + 1 == n_march;
+          if (counters) k_march<F, true><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, last, march_budget);
+          else k_march<F, false><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, last, march_budget);
+        }
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
         k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
       } else {

@@ -25,6 +25,8 @@ constexpr int kWfBlock = 256;
 // tuning, rg_tuning.shared_stack, with the same default.)
 constexpr int kSharedStack = 8;
 template <uint32_t F> constexpr int kSharedStackOf = kinds_of(F) == F_TRI ? kSharedStack : 0;
+// SDF evaluations a k_march lane performs between refills of idle lanes.
+constexpr uint32_t kMarchBudget = 8;
 constexpr int kKinds = 6;  // miss, lambertian, metal, dielectric, isotropic, light
 enum : uint32_t { KQ_MISS = 0 };
 constexpr int kPrimMiss = -1;  // rec[2].w: >= 0 BVH primitive, -1 miss, -2 - k SDF k
@@ -120,16 +122,20 @@ __device__ __forceinline__ void flush_wave_counters(const FrameParams& fp, const
   for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(0xffffffffu, q, o);
   if ((threadIdx.x & 31) == 0 && q) atomicAdd(fp.counters + CNT_RAYS, q);
   if (COUNT) {
-    unsigned long long a = cnt.nodes, b = cnt.prims, c = cnt.sdf_steps;
+    unsigned long long a = cnt.nodes, b = cnt.prims, c = cnt.sdf_steps, d = cnt.sdf_iters, e = cnt.hits;
     for (int o = 16; o > 0; o >>= 1) {
       a += __shfl_down_sync(0xffffffffu, a, o);
       b += __shfl_down_sync(0xffffffffu, b, o);
       c += __shfl_down_sync(0xffffffffu, c, o);
+      d += __shfl_down_sync(0xffffffffu, d, o);
+      e += __shfl_down_sync(0xffffffffu, e, o);
     }
     if ((threadIdx.x & 31) == 0) {
       atomicAdd(fp.counters + CNT_NODES, a);
       atomicAdd(fp.counters + CNT_PRIMS, b);
       atomicAdd(fp.counters + CNT_SDF, c);
+      atomicAdd(fp.counters + CNT_SDF_ITERS, d);
+      atomicAdd(fp.counters + CNT_HITS, e);
     }
   }
 }

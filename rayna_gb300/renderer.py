@@ -39,6 +39,8 @@ class RenderStats:
     traverse_ms: float = 0.0
     invalid_hits: int = 0          # validate=True: hits / colours breaking shared/validate.rs's invariants
     invalid_mask: int = 0          # which invariants (RG_INVALID_* bits)
+    hits: int = 0                  # counters=True: closest-hit queries that found a surface
+    sdf_iterations: int = 0        # counters=True: Mandelbulb escape-loop iterations
 
 
 @dataclass
@@ -313,7 +315,8 @@ class Renderer:
                          kernel_ms=stats.kernel_ms, samples=stats.samples, rays=stats.rays,
                          node_visits=stats.node_visits, prim_tests=stats.prim_tests,
                          sdf_steps=stats.sdf_steps, error_flags=stats.error_flags, traverse_ms=stats.traverse_ms,
-                         invalid_hits=stats.invalid_hits, invalid_mask=stats.invalid_mask)
+                         invalid_hits=stats.invalid_hits, invalid_mask=stats.invalid_mask, hits=stats.hits,
+                         sdf_iterations=stats.sdf_iterations)
         return Render(img=img, stats=rs)
 
     def frame_moments(self):

@@ -87,7 +87,7 @@ def test_colour_fixture():
 def test_device_meets_fixture(name):
     from rayna_gb300 import Renderer
     from rayna_gb300.scene import Camera, RenderOpts
-    with Renderer.new_from(SCENES[name], Camera(), RenderOpts(width=8, height=8)) as r:
+    with Renderer.new_from(SCENES[name], Camera(), RenderOpts(width=8, height=8), exact=True) as r:
         g = r.query_rays(FIX[f"{name}_o"], FIX[f"{name}_d"])
     agree, frac = check_against_fixture(name, g["hit"], g["prim"], g["t"])
     print(f"{name}: hit/miss agree on {agree:.4f} of rays, distances within 1e-4 on {frac:.4f} of hits")

@@ -15,23 +15,24 @@ def small_batch():
     return presets.batch_scenes(n=7, seed=3, scale=0.08, max_tris=20_000)
 
 
-def test_batch_equals_sequential_and_standalone():
+@pytest.mark.parametrize("exact", [True, False])
+def test_batch_equals_sequential_and_standalone(exact):
     items = small_batch()
     seeds = [11, 12]
-    with BatchRenderer(items) as b:
+    with BatchRenderer(items, exact=exact) as b:
         for s in seeds:
             st = b.render(seed=s)
             assert st.error_flags == 0
             assert st.samples == b.n_samples
         graph_imgs = [b.image(i) for i in range(len(items))]
         keys = [[b.item_seed(s, i) for s in seeds] for i in range(len(items))]
-    with BatchRenderer(items) as b:
+    with BatchRenderer(items, exact=exact) as b:
         for s in seeds:
             b.render_sequential(seed=s)
         seq_imgs = [b.image(i) for i in range(len(items))]
     for i, (scene, cam, opts) in enumerate(items):
         np.testing.assert_array_equal(graph_imgs[i], seq_imgs[i])
-        with Renderer.new_from(scene, cam, opts, 0) as r:
+        with Renderer.new_from(scene, cam, opts, 0, exact=exact) as r:
             for k in keys[i]:
                 img = r.render(seed=k).img
         np.testing.assert_array_equal(graph_imgs[i], img)

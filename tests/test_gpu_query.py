@@ -1,16 +1,32 @@
 """Ray-query parity on the GPU, through the C ABI (rg_query_rays).
 
 For closed-form primitives (sphere, triangle, box, torus and sphere SDFs) the
-device must be bit-exact against the f32 oracle that follows the kernels'
-operation order, evaluated by brute force over every primitive (no bounding
-volumes): same hit/miss, same primitive (up to exact-distance ties), same
-distance and normal bits. The device's slab test is conservative, so its BVH
-never changes which primitive is closest. Against the faithful f64 oracle the distance
-must agree within 1e-5 relative, or within the f32 error bound of the
-primitive's formula where that bound is larger (ill-conditioned hits:
-counted and reported). Media (free-flight logarithm) and the Mandelbulb
-(transcendental distance estimator) use library transcendentals on both
-sides and are held to tolerances stated in each test.
+arithmetic-contract build must be bit-exact against the f32 oracle that
+follows the kernels' operation order, evaluated by brute force over every
+primitive (no bounding volumes): same hit/miss, same primitive (up to
+exact-distance ties), same distance and normal bits. The device's slab test
+is conservative, so its BVH never changes which primitive is closest.
+
+Against the faithful f64 oracle, on every suite and in both builds (the
+performance build fuses multiply-adds where the compiler finds them):
+
+* hit/miss agrees on at least 99.9% of rays (99.8% on the planar suite);
+* where the two pick different primitives, the disagreements are counted,
+  bounded per suite, and must be near-ties: the f32 distance still within
+  tolerance of the f64 closest distance;
+* the distance agrees within 1e-5 relative, or within the first-order f32
+  error bound of the primitive's formula where that bound is larger
+  (ill-conditioned hits: counted and reported);
+* the outward normal agrees within 1e-5 (normals are unit vectors, so
+  absolute = relative), or within the first-order f32 error bound of the
+  normal's formula (the f32 distance error divided by the radius for
+  spheres, the barycentric error times the vertex-normal spread for
+  triangles, the central difference's rounding divided by its step for
+  raymarched surfaces); the fraction beyond 1e-5 is reported.
+
+Media (free-flight logarithm) and the Mandelbulb (transcendental distance
+estimator) use library transcendentals on both sides and are held to
+tolerances stated in each test.
 """
 import numpy as np
 import pytest
@@ -27,8 +43,8 @@ pytestmark = pytest.mark.gpu
 EPS32 = np.finfo(np.float32).eps
 
 
-def renderer_for(scene, bvh_width=2):
-    r = Renderer.new_from(scene, Camera(), RenderOpts(width=8, height=8))
+def renderer_for(scene, bvh_width=2, exact=True):
+    r = Renderer.new_from(scene, Camera(), RenderOpts(width=8, height=8), exact=exact)
     r.set_tuning(bvh_width=bvh_width)
     assert r.tuning()["bvh_width"] == bvh_width
     return r
@@ -118,17 +134,90 @@ def f64_error_bound(flat, o, d, prim, t64):
     return bound
 
 
-def compare_f64(flat, o, d, g, label, min_agree=0.999):
-    h, t64, _ = ob.query(flat, o, d, policy=ob.POLICY_REF_F64, pretest=True)
+def normal_error_bound(flat, o, d, prim, t64, dt):
+    """First-order f32 error bound of the outward normal of each hit (on top
+    of a few ulps of the normalisation)."""
+    o = o.astype(np.float64)
+    d = d.astype(np.float64) / np.linalg.norm(d, axis=1, keepdims=True)
+    ns, nt = flat.desc.n_spheres, flat.desc.n_triangles
+    bound = np.full(len(prim), 8 * EPS32)
+    s = prim < ns
+    if s.any():  # (p - c) / r with p = o + t d
+        sp = flat.a_spheres[prim[s]].astype(np.float64)
+        scale = np.abs(o[s]).max(axis=1) + t64[s] + np.abs(sp[:, :3]).max(axis=1) + sp[:, 3]
+        bound[s] += (np.abs(dt[s]) + 8 * EPS32 * scale) / sp[:, 3]
+    tr = (prim >= ns) & (prim < ns + nt)
+    if tr.any():  # sum_i b_i n_i with the barycentric errors of Moller-Trumbore
+        v = flat.a_tri_v[prim[tr] - ns].astype(np.float64)
+        n = flat.a_tri_n[prim[tr] - ns].astype(np.float64)
+        e1, e2 = v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]
+        det = np.maximum(np.abs(np.einsum("ij,ij->i", e1, np.cross(d[tr], e2))), 1e-300)
+        dist = np.linalg.norm(o[tr] - v[:, 0], axis=1) + t64[tr]
+        du = 16 * EPS32 * dist * np.linalg.norm(e2, axis=1) / det
+        dv = 16 * EPS32 * dist * np.linalg.norm(e1, axis=1) / det
+        bound[tr] += du * np.linalg.norm(n[:, 1] - n[:, 0], axis=1) + dv * np.linalg.norm(n[:, 2] - n[:, 0], axis=1)
+    D = flat.desc
+    s0 = ns + nt + D.n_boxes + D.n_volumes
+    sd = (prim >= s0) & (prim < s0 + D.n_sdfs)
+    if sd.any():  # central differences of the SDF with step eps: rounding of each evaluation / (2 eps)
+        for k in np.unique(prim[sd] - s0):
+            f = flat.c_sdfs[int(k)]
+            sel = sd & (prim - s0 == k)
+            p = o[sel] + d[sel] * t64[sel, None]
+            mag = np.abs(p).max(axis=1) + max(abs(f.centre[0]), abs(f.centre[1]), abs(f.centre[2])) + abs(f.params[0])
+            bound[sel] += 16 * EPS32 * mag / f.epsilon + np.abs(dt[sel]) / max(f.params[1], f.params[0], 1e-3)
+    return bound
+
+
+def sdf_distance_bound(flat, prim, d, n64):
+    """Sphere tracing stops within epsilon of the surface in either
+    precision: the distance can differ by about epsilon over the cosine of
+    the incidence."""
+    D = flat.desc
+    s0 = flat.desc.n_spheres + flat.desc.n_triangles + D.n_boxes + D.n_volumes
+    out = np.zeros(len(prim))
+    sd = (prim >= s0) & (prim < s0 + D.n_sdfs)
+    if sd.any():
+        dn = d[sd].astype(np.float64) / np.linalg.norm(d[sd], axis=1, keepdims=True)
+        cos = np.abs(np.einsum("ij,ij->i", dn, n64[sd]))
+        eps = np.array([flat.c_sdfs[int(k)].epsilon for k in prim[sd] - s0])
+        out[sd] = 4 * eps / np.maximum(cos, 0.05)
+    return out
+
+
+def compare_f64(flat, o, d, g, label, min_agree=0.999, max_prim_diff=0.002):
+    """Device hits g against the faithful f64 oracle; returns a dict of the
+    agreement figures (asserting the bars in the module docstring)."""
+    h, t64, n64 = ob.query(flat, o, d, policy=ob.POLICY_REF_F64, pretest=True)
     agree = np.mean(g["hit"] == h["hit"])
     assert agree >= min_agree, f"{label}: hit agreement with f64 {agree:.5f}"
-    m = (g["hit"] == 1) & (h["hit"] == 1) & (g["prim"] == h["prim"])
-    rel = np.abs(g["t"][m].astype(np.float64) - t64[m]) / np.maximum(t64[m], 1e-30)
-    bnd = f64_error_bound(flat, o[m], d[m], g["prim"][m], t64[m])
-    ok = (rel <= 1e-5) | (np.abs(g["t"][m] - t64[m]) <= bnd)
-    assert ok.all(), f"{label}: {np.sum(~ok)} distances outside tolerance; worst rel {rel[~ok].max()}"
-    ill = np.mean(rel > 1e-5)
-    return float(agree), float(ill), float(np.median(rel)) if rel.size else 0.0
+    both = (g["hit"] == 1) & (h["hit"] == 1)
+    t32 = g["t"].astype(np.float64)
+    bnd_t = np.zeros(len(o))
+    bnd_t[both] = f64_error_bound(flat, o[both], d[both], g["prim"][both], t64[both])
+    bnd_t[both] += sdf_distance_bound(flat, g["prim"][both], d[both], n64[both])
+    rel = np.abs(t32 - t64) / np.maximum(np.abs(t64), 1e-30)
+    t_ok = (rel <= 1e-5) | (np.abs(t32 - t64) <= bnd_t)
+    # a different primitive: counted, and only at a near-tie of distance
+    pdiff = both & (g["prim"] != h["prim"])
+    frac_pdiff = pdiff.sum() / max(both.sum(), 1)
+    assert frac_pdiff <= max_prim_diff, f"{label}: {pdiff.sum()} primitive disagreements ({frac_pdiff:.5f})"
+    assert t_ok[pdiff].all(), f"{label}: a primitive disagreement that is not a near-tie of distance"
+    m = both & ~pdiff
+    assert t_ok[m].all(), f"{label}: {np.sum(~t_ok[m])} distances outside tolerance; worst rel {rel[m][~t_ok[m]].max()}"
+    ill = float(np.mean(rel[m] > 1e-5)) if m.any() else 0.0
+    # outward normals
+    n32 = g["normal"].astype(np.float64)
+    nerr = np.abs(n32 - n64).max(axis=1)
+    nb = np.zeros(len(o))
+    nb[m] = normal_error_bound(flat, o[m], d[m], g["prim"][m], t64[m], (t32 - t64)[m])
+    n_ok = (nerr <= 1e-5) | (nerr <= nb)
+    assert n_ok[m].all(), (f"{label}: {np.sum(~n_ok[m])} normals outside tolerance; worst {nerr[m][~n_ok[m]].max():.3e}"
+                           f" (bound {nb[m][~n_ok[m]].max():.3e})")
+    n_beyond = float(np.mean(nerr[m] > 1e-5)) if m.any() else 0.0
+    return {"agree": float(agree), "prim_diff": float(frac_pdiff), "t_ill": ill,
+            "t_median_rel": float(np.median(rel[m])) if m.any() else 0.0, "normal_beyond_1e-5": n_beyond,
+            "normal_median": float(np.median(nerr[m])) if m.any() else 0.0, "hits": int(m.sum())}
 
 
 def axis_aligned_rays(rng, n, lo, hi):
@@ -144,10 +233,11 @@ def axis_aligned_rays(rng, n, lo, hi):
     return o, d
 
 
-@pytest.mark.parametrize("bvh_width", [2, 8])
-@pytest.mark.parametrize("suite", ["spheres", "triangles", "mesh", "boxes", "sdf_analytic", "axis_aligned", "planar",
-                                   "transformed", "transformed_scaled", "cornell"])
-def test_query_bit_exact_vs_f32_oracle(suite, bvh_width):
+SUITES = ["spheres", "triangles", "mesh", "boxes", "sdf_analytic", "axis_aligned", "planar", "transformed",
+          "transformed_scaled", "cornell"]
+
+
+def suite_rays(suite):
     seeds = {"spheres": 1, "triangles": 2, "mesh": 7, "boxes": 3, "sdf_analytic": 4, "axis_aligned": 8, "planar": 9,
              "transformed": 10, "transformed_scaled": 11, "cornell": 12}
     rng = np.random.Generator(np.random.PCG64(seeds[suite]))
@@ -180,6 +270,13 @@ def test_query_bit_exact_vs_f32_oracle(suite, bvh_width):
         s = sdf_scene()
         scene = Scene(objects=[s.objects[0], s.objects[1], s.objects[3]])
         o, d = rays_at(rng, 4000, (-1.5, -1, -1.5), (3.2, 2, 1.5))
+    return scene, o, d
+
+
+@pytest.mark.parametrize("bvh_width", [2, 8])
+@pytest.mark.parametrize("suite", SUITES)
+def test_query_bit_exact_vs_f32_oracle(suite, bvh_width):
+    scene, o, d = suite_rays(suite)
     flat = flatten(scene)
     with renderer_for(scene, bvh_width) as r:
         g = r.query_rays(o, d)
@@ -187,9 +284,57 @@ def test_query_bit_exact_vs_f32_oracle(suite, bvh_width):
     nhit, nties = compare_bit_exact(g, h, suite)
     assert nhit > 0.2 * len(o)
     print(f"{suite} (bvh width {bvh_width}): {nhit} hits bit-exact, {nties} exact-distance ties")
-    if suite in ("spheres", "triangles", "planar"):
-        agree, ill, med = compare_f64(flat, o, d, g, suite, min_agree=0.998 if suite == "planar" else 0.999)
-        print(f"{suite}: f64 agreement {agree:.5f}, ill-conditioned {ill:.4f}, median rel err {med:.2e}")
+
+
+# Suites compared with the faithful f64 oracle. transformed_scaled is left
+# out on purpose: under scaling the reference bounds a mesh-space distance by
+# the world-space interval end, so its closest hit depends on the order of
+# its traversal (about one ray in six on this suite); the device returns the
+# closest world-space hit, which the rigid `transformed` suite and the f32
+# oracle pin instead.
+F64_SUITES = [s for s in SUITES if s != "transformed_scaled"]
+# Primitive disagreements allowed per suite (fraction of hits both sides
+# report): shared edges and vertices of meshes, coplanar box faces, and the
+# reference's order-dependent cylinder rule give near-ties whose winner f32
+# rounding decides.
+MAX_PRIM_DIFF = {"planar": 0.004, "mesh": 0.004, "triangles": 0.004, "axis_aligned": 0.004, "cornell": 0.004}
+
+
+@pytest.mark.parametrize("exact", [True, False])
+@pytest.mark.parametrize("suite", F64_SUITES)
+def test_query_vs_f64_oracle(suite, exact):
+    scene, o, d = suite_rays(suite)
+    flat = flatten(scene)
+    with renderer_for(scene, 2, exact=exact) as r:
+        g = r.query_rays(o, d)
+    st = compare_f64(flat, o, d, g, suite, min_agree=0.998 if suite == "planar" else 0.999,
+                     max_prim_diff=MAX_PRIM_DIFF.get(suite, 0.002))
+    build = "exact" if exact else "performance"
+    print(f"{suite} ({build} build) vs f64: {st}")
+
+
+@pytest.mark.parametrize("level", [8])
+def test_query_full_mesh_vs_oracles(level):
+    """The benchmarked triangle-mesh workload itself (1,310,732 triangles):
+    bit-exact against the f32 oracle's BVH walk and within the f64 bars."""
+    scene = presets.cornell_mesh(level=level)[0]
+    flat = flatten(scene)
+    rng = np.random.Generator(np.random.PCG64(80 + level))
+    o, d = rays_at(rng, 20000, (0.02, 0.02, 0.02), (0.98, 0.98, 0.98))
+    # half of the rays aimed at the displaced sphere's surface
+    c = np.array([0.5, 0.3, 0.5])
+    dirs = rng.normal(size=(10000, 3))
+    tgt = c + 0.25 * dirs / np.linalg.norm(dirs, axis=1, keepdims=True)
+    d[:10000] = (tgt - o[:10000]).astype(np.float32)
+    with renderer_for(scene, 2) as r:
+        g = r.query_rays(o, d)
+    with renderer_for(scene, 8) as r:
+        g8 = r.query_rays(o, d)
+    h, _, _ = ob.query(flat, o, d, policy=ob.POLICY_GPU_F32, pretest=False)
+    nhit, nties = compare_bit_exact(g, h, "mesh level 8")
+    compare_bit_exact(g8, h, "mesh level 8, 8-wide")
+    st = compare_f64(flat, o, d, g, "mesh level 8", max_prim_diff=0.004)
+    print(f"mesh level {level}: {nhit} hits bit-exact, {nties} ties; vs f64: {st}")
 
 
 @pytest.mark.parametrize("bvh_width", [2, 8])

@@ -1,12 +1,13 @@
 """Image parity and Renderer semantics on the GPU, through the C ABI.
 
 * The reference's known answers (simple_renders.rs:22-142) on the device.
-* Path-by-path parity: with the same frame seed, the device and the f32
-  oracle that mirrors its samplers trace the same paths; per-pixel means agree
-  to float rounding except where a transcendental's last ulp flips a discrete
-  decision (counted).
-* Statistical parity with the faithful f64 oracle (the reference's rejection
-  samplers): per-pixel means within 3 standard errors, relRMSE reported.
+* Path-by-path parity: with the same frame seed, the device's
+  arithmetic-contract build and the f32 oracle that mirrors its samplers
+  trace the same paths; per-pixel means agree to float rounding except where
+  a transcendental's last ulp flips a discrete decision (counted).
+* Statistical parity of the performance build (the default) with the
+  faithful f64 oracle (the reference's rejection samplers): per-pixel means
+  within 3 standard errors, relRMSE reported.
 * Accumulation, checkpoint/resume, invalid camera, unsupported variants.
 """
 import math
@@ -55,7 +56,7 @@ def test_path_by_path_parity_with_f32_oracle(case):
     scene, cam, opts = CASES[case]()
     flat = flatten(scene)
     seed = 0x1234567 + len(case)
-    with Renderer.new_from(scene, cam, opts, 0) as r:
+    with Renderer.new_from(scene, cam, opts, 0, exact=True) as r:
         r.render(seed=seed)
         gm, gv = r.frame_moments()
     st, om, ov, _ = ob.render(flat, cam, opts, seed=seed, frames=1, policy=ob.POLICY_GPU_F32)
@@ -176,7 +177,7 @@ def test_debug_modes_path_by_path(case, mode):
     scene, cam, opts = MODE_CASES[case]()
     opts.mode = mode
     flat = flatten(scene)
-    with Renderer.new_from(scene, cam, opts, 0, form="wavefront") as r:  # routes to the megakernel
+    with Renderer.new_from(scene, cam, opts, 0, form="wavefront", exact=True) as r:  # routes to the megakernel
         r.render(seed=41)
         gm, _ = r.frame_moments()
     st, om, _, _ = ob.render(flat, cam, opts, seed=41, frames=1, policy=ob.POLICY_GPU_F32)
@@ -193,7 +194,7 @@ def test_branching_path_by_path_and_statistics():
     scene, cam, opts = small(presets.cornell_quads, 24, 24, 4, 4)
     flat = flatten(scene)
     opts.ray_branching = 2
-    with Renderer.new_from(scene, cam, opts, 0) as r:
+    with Renderer.new_from(scene, cam, opts, 0, exact=True) as r:
         r.render(seed=5)
         gm, _ = r.frame_moments()
     st, om, _, _ = ob.render(flat, cam, opts, seed=5, frames=1, policy=ob.POLICY_GPU_F32)
@@ -223,7 +224,7 @@ def test_large_spp_path_and_counters():
     cam = Camera(pos=(0, 0, -2.7), v_fov=Angle.from_degrees(45), fwd=(0, 0, 1), focus_dist=1.0)
     opts = RenderOpts(width=8, height=8, samples=300, ray_depth=5)
     flat = flatten(scene)
-    with Renderer.new_from(scene, cam, opts, 0, counters=True) as r:
+    with Renderer.new_from(scene, cam, opts, 0, counters=True, exact=True) as r:
         out = r.render(seed=9)
         gm, _ = r.frame_moments()
         assert out.stats.samples == 8 * 8 * 300
@@ -233,10 +234,12 @@ def test_large_spp_path_and_counters():
     np.testing.assert_allclose(gm, om, rtol=1e-4, atol=1e-5)
 
 
+@pytest.mark.parametrize("exact", [True, False])
 @pytest.mark.parametrize("case", list(CASES) + ["large_spp"])
-def test_wavefront_equals_megakernel(case):
+def test_wavefront_equals_megakernel(case, exact):
     """Both kernel forms run the same per-path code with the same random
-    streams and sum samples in the same order: identical images."""
+    streams and sum samples in the same order: identical images, in either
+    arithmetic build."""
     if case == "large_spp":
         scene = presets.single_sphere((0.3, 0.6, 0.9))
         cam = Camera(pos=(0, 0, -2.7), v_fov=Angle.from_degrees(45), fwd=(0, 0, 1), focus_dist=1.0)
@@ -246,7 +249,7 @@ def test_wavefront_equals_megakernel(case):
     imgs = {}
     for width in (2, 8):
         for form, sort in (("megakernel", None), ("wavefront", False), ("wavefront", True)):
-            with Renderer.new_from(scene, cam, opts, 0, form=form, counters=True) as r:
+            with Renderer.new_from(scene, cam, opts, 0, form=form, counters=True, exact=exact) as r:
                 r.set_tuning(bvh_width=width, sort_materials=sort)
                 assert r.tuning()["bvh_width"] == width
                 for k in range(2):

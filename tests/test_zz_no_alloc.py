@@ -41,8 +41,35 @@ def test_static_scratch_matches_rg_render_on_two_calls():
             stats = A.rg_render_stats()
             A.check(lib, h, lib.rg_sync_stats(h, C.byref(stats)))
             assert stats.error_flags == 0
+            # the stats describe this frame, not an earlier rg_render's
+            assert stats.samples == opts.width * opts.height * opts.samples
+            assert stats.kernel_ms > 0.0 and stats.kernel_launches > 0
             got = out.cpu().numpy().reshape(opts.width, opts.height, 3)
             np.testing.assert_array_equal(got, expected[k])
+
+
+def test_static_scratch_frame_stats_with_stage_times():
+    """With RG_FLAG_STAGE_TIMES the regular entry times its traversal
+    launches; the allocation-free entry does not (its events would be created
+    on demand), so after it rg_sync_stats reports traverse_ms 0 and this
+    frame's samples, call after call, instead of the earlier frame's figures."""
+    torch = pytest.importorskip("torch")
+    scene, cam, _ = presets.random_spheres(seed=0)
+    opts = RenderOpts(width=64, height=36, samples=8, ray_depth=8)
+    with Renderer.new_from(scene, cam, opts, 0, stage_times=True) as r:
+        first = r.render(seed=3).stats
+        assert first.traverse_ms > 0.0
+        lib, h = r._lib, r.handle
+        n = opts.width * opts.height * 3
+        accum = torch.zeros(n, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        for k in range(4):
+            A.check(lib, h, lib.rg_render_static_scratch(h, 100 + k, C.c_void_p(accum.data_ptr()), k + 1, None))
+            stats = A.rg_render_stats()
+            A.check(lib, h, lib.rg_sync_stats(h, C.byref(stats)))
+            assert stats.traverse_ms == 0.0
+            assert stats.samples == opts.width * opts.height * opts.samples
+            assert stats.error_flags == 0
 
 
 def test_static_scratch_rejects_sizes_beyond_its_array():
