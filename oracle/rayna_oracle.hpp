@@ -474,7 +474,8 @@ template <class P> struct Parallelogram {
 };
 
 // CylinderMesh (mesh/primitive/cylinder.rs:24-183). The f32 policy follows the
-// device's operation order (explicit fused multiply-adds) and, like the
+// device's operation order (explicit fused multiply-adds; the body roots
+// evaluated without the discriminant's cancellation) and, like the
 // device, evaluates the test against [start, inf) before clipping to the
 // interval's end: the reference's test is not monotone in the end (a cap
 // nearer than the body roots is dropped when both roots lie beyond it), so
@@ -514,23 +515,40 @@ template <class P> struct Cylinder {
     using M = Math<P>;
     V3<T> rd = ray.dir, oc = ray.pos - origin;
     T bard = M::dot(along, rd), baoc = M::dot(along, oc);
-    T a, b, c, disc;
+    T a, b, c, disc, sq, dist;
     if constexpr (P::gpu) {
+      // the device's evaluation of the same roots without the discriminant's
+      // cancellation (trace.cuh, cylinder_t): components normal to the axis,
+      // the closest approach to the axis, roots q / a and c / q
       a = std::fma(-bard, bard, lsq);
-      b = std::fma(lsq, M::dot(oc, rd), -(baoc * bard));
-      c = std::fma(lsq, M::dot(oc, oc), -(baoc * baoc)) - (radius * radius) * lsq;
-      disc = std::fma(b, b, -(c * a));
+      if (a == T(0)) return false;
+      V3<T> dp{std::fma(lsq, rd.x, -(bard * along.x)), std::fma(lsq, rd.y, -(bard * along.y)),
+               std::fma(lsq, rd.z, -(bard * along.z))};
+      V3<T> op{std::fma(lsq, oc.x, -(baoc * along.x)), std::fma(lsq, oc.y, -(baoc * along.y)),
+               std::fma(lsq, oc.z, -(baoc * along.z))};
+      b = M::dot(op, rd);
+      c = std::fma(-(radius * radius), lsq, M::dot(op, op) / lsq);
+      T k = b / a;
+      V3<T> w{std::fma(-k, dp.x, op.x), std::fma(-k, dp.y, op.y), std::fma(-k, dp.z, op.z)};
+      disc = a * std::fma(radius * radius, lsq, -(M::dot(w, w) / lsq));
+      if (disc < T(0)) return false;
+      sq = std::sqrt(disc);
+      T q = b > T(0) ? -b - sq : -b + sq;
+      T r1 = q / a, r2 = q != T(0) ? c / q : q;
+      dist = std::fmin(r1, r2);
+      if (!iv.contains(dist)) dist = std::fmax(r1, r2);
+      if (!iv.contains(dist)) return false;
     } else {
       a = lsq - bard * bard;
       b = lsq * M::dot(oc, rd) - baoc * bard;
       c = lsq * M::dot(oc, oc) - baoc * baoc - radius * radius * lsq;
       disc = b * b - c * a;
+      if (disc < T(0)) return false;
+      sq = std::sqrt(disc);
+      dist = (-b - sq) / a;
+      if (!iv.contains(dist)) dist = (-b + sq) / a;
+      if (!iv.contains(dist)) return false;
     }
-    if (disc < T(0)) return false;
-    T sq = std::sqrt(disc);
-    T dist = (-b - sq) / a;
-    if (!iv.contains(dist)) dist = (-b + sq) / a;
-    if (!iv.contains(dist)) return false;
     T dan;
     if constexpr (P::gpu) dan = std::fma(dist, bard, baoc) / lsq;
     else dan = (baoc + dist * bard) / lsq;
@@ -615,6 +633,10 @@ template <class P> struct Sdf {
     V3<T> q = x - c;
     if (kind == RG_SDF_SPHERE) return Math<P>::length(q) - p[0];
     if (kind == RG_SDF_TORUS) {
+      if constexpr (P::gpu) {  // the device's explicit fused multiply-adds
+        T a = std::sqrt(std::fma(q.x, q.x, q.z * q.z)) - p[0];
+        return std::sqrt(std::fma(a, a, q.y * q.y)) - p[1];
+      }
       T a = std::sqrt(q.x * q.x + q.z * q.z) - p[0];
       return std::sqrt(a * a + q.y * q.y) - p[1];
     }
@@ -632,8 +654,14 @@ template <class P> struct Sdf {
       // z^8 without transcendentals: with cos t = z/r, sin t = rho/r and
       // cos p + i sin p = (x + i y)/rho, three complex squarings give 8t, 8p.
       for (int i = 0; i < iters; ++i) {
-        T rho2 = z.x * z.x + z.y * z.y;
-        T r2 = rho2 + z.z * z.z;
+        T rho2, r2;
+        if constexpr (P::gpu) {  // the device's explicit fused multiply-adds
+          rho2 = std::fma(z.x, z.x, z.y * z.y);
+          r2 = std::fma(z.z, z.z, rho2);
+        } else {
+          rho2 = z.x * z.x + z.y * z.y;
+          r2 = rho2 + z.z * z.z;
+        }
         r = std::sqrt(r2);
         if (r > T(2)) break;
         T rho = std::sqrt(rho2);
@@ -641,17 +669,25 @@ template <class P> struct Sdf {
         if (r > T(0)) { ct = z.z / r; st = rho / r; }
         if (rho > T(0)) { cp = z.x / rho; sp = z.y / rho; }
         for (int k = 0; k < 3; ++k) {
-          T c2 = ct * ct - st * st;
+          T c2, d2;
+          if constexpr (P::gpu) c2 = std::fma(ct, ct, -(st * st));
+          else c2 = ct * ct - st * st;
           st = T(2) * ct * st;
           ct = c2;
-          T d2 = cp * cp - sp * sp;
+          if constexpr (P::gpu) d2 = std::fma(cp, cp, -(sp * sp));
+          else d2 = cp * cp - sp * sp;
           sp = T(2) * cp * sp;
           cp = d2;
         }
         T r4 = r2 * r2;
         T zr = r4 * r4;
-        dr = (r4 * r2 * r) * T(8) * dr + T(1);
-        z = V3<T>{zr * (st * cp), zr * (sp * st), zr * ct} + z0;
+        if constexpr (P::gpu) {
+          dr = std::fma((r4 * r2 * r) * T(8), dr, T(1));
+          z = V3<T>{std::fma(zr, st * cp, z0.x), std::fma(zr, sp * st, z0.y), std::fma(zr, ct, z0.z)};
+        } else {
+          dr = (r4 * r2 * r) * T(8) * dr + T(1);
+          z = V3<T>{zr * (st * cp), zr * (sp * st), zr * ct} + z0;
+        }
       }
       return (T(0.5) * std::log(r) * r / dr) * s;
     }
@@ -660,12 +696,22 @@ template <class P> struct Sdf {
       if (r > T(2)) break;
       T theta = std::acos(z.z / r);
       T phi = std::atan2(z.y, z.x);
-      dr = std::pow(r, power - T(1)) * power * dr + T(1);
       T zr = std::pow(r, power);
-      theta = theta * power;
-      phi = phi * power;
-      T st = std::sin(theta);
-      z = V3<T>{zr * (st * std::cos(phi)), zr * (std::sin(phi) * st), zr * std::cos(theta)} + z0;
+      T st;
+      if constexpr (P::gpu) {
+        dr = std::fma(std::pow(r, power - T(1)) * power, dr, T(1));
+        theta = theta * power;
+        phi = phi * power;
+        st = std::sin(theta);
+        z = V3<T>{std::fma(zr, st * std::cos(phi), z0.x), std::fma(zr, std::sin(phi) * st, z0.y),
+                  std::fma(zr, std::cos(theta), z0.z)};
+      } else {
+        dr = std::pow(r, power - T(1)) * power * dr + T(1);
+        theta = theta * power;
+        phi = phi * power;
+        st = std::sin(theta);
+        z = V3<T>{zr * (st * std::cos(phi)), zr * (std::sin(phi) * st), zr * std::cos(theta)} + z0;
+      }
     }
     return (T(0.5) * std::log(r) * r / dr) * s;
   }

@@ -7,14 +7,18 @@ bits); only the time does. A key is
 
 and its entry records the best configuration found and the timings of every
 candidate. Single renders choose between the megakernel and the wavefront
-form, the tree (binary or 8-wide) and, for the wavefront, the path budget
-per wave (queue capacity), fused or material-sorted shading and the node
-visits between refills of the persistent traversal kernels; batches
-choose the batched form (wavefront with its path slots per wave, or tiles with
-the persistent kernel's block size, blocks per SM and the work-item
-granularity of the global queue). Entries live in a JSON file
-(RAYNA_GB300_TUNE_CACHE, default rayna_gb300/tuning_cache.json) and are
-measured with CUDA events on the device the first time a key is seen.
+form; for the megakernel the tree (binary or 8-wide), the traversal stack's
+placement (entries per thread in shared memory) and the block size; for the
+wavefront the tree, fused or material-sorted shading, the node visits between
+refills of the persistent traversal kernels, the path budget per wave (queue
+capacity) and the stack placement. Each form is searched by coordinate
+descent: from the library defaults, one knob at a time over its candidates,
+keeping the best, in a fixed order. Batches choose the batched form (wavefront
+with its path slots per wave, or tiles with the persistent kernel's block
+size, blocks per SM and the work-item granularity of the global queue).
+Entries live in a JSON file (RAYNA_GB300_TUNE_CACHE, default
+~/.cache/rayna_gb300/tuning_cache.json) and are measured with CUDA events on
+the device the first time a key is seen.
 """
 from __future__ import annotations
 
@@ -25,11 +29,17 @@ import time
 
 from . import _abi as A
 
-DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_cache.json")
+DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "rayna_gb300", "tuning_cache.json")
 
 WAVE_PATHS = [1 << 23, 1 << 24, 1 << 25]
 FETCH_BUDGETS = [4, 8, 16]
 BVH_WIDTHS = [2, 8]
+SHARED_STACKS = [-1, 8, 16]  # -1: the whole traversal stack in local memory
+MEGA_BLOCKS = [64, 128, 256]
+# Coordinate-descent axes per form, searched in this order.
+MEGA_AXES = [("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS), ("block", MEGA_BLOCKS)]
+WAVE_AXES = [("sort_materials", [False, True]), ("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS),
+             ("fetch_budget", FETCH_BUDGETS), ("wave_paths", WAVE_PATHS)]
 BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 23, 1 << 24, 1 << 25)] +
                 [dict(form="tiles", block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)])
 
@@ -63,6 +73,7 @@ class Tuner:
 
     def store(self, key: str, best: dict, timings: list):
         self.table[key] = {"best": best, "timings": timings, "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
+        os.makedirs(os.path.dirname(os.path.abspath(self.path)), exist_ok=True)
         tmp = self.path + ".tmp"
         with open(tmp, "w") as f:
             json.dump(self.table, f, indent=1, sort_keys=True)
@@ -81,6 +92,26 @@ class Tuner:
                 ms.append(st.kernel_ms)
         return sorted(ms)[len(ms) // 2]
 
+    @classmethod
+    def _descend(cls, r, form: str, axes, start: dict, frames: int, seed0: int, timings: list, opts) -> dict:
+        """Coordinate descent over `axes` from `start`; returns the best knobs."""
+        best = dict(start)
+        r.set_tuning(**best)
+        best_ms = cls._frame_ms(r, frames, seed0)
+        timings.append(dict(best, form=form, ms=best_ms))
+        for name, values in axes:
+            for v in values:
+                if v == best.get(name) or (name == "wave_paths" and v < opts.samples):
+                    continue
+                cand = dict(best, **{name: v})
+                r.set_tuning(**cand)
+                ms = cls._frame_ms(r, frames, seed0)
+                timings.append(dict(cand, form=form, ms=ms))
+                if ms < best_ms:
+                    best, best_ms = cand, ms
+        r.set_tuning(**best)
+        return dict(best, form=form, ms=best_ms)
+
     def tune_render(self, scene, camera, opts, frames: int = 2, force: bool = False, **renderer_kw) -> dict:
         """Best launch configuration for this scene size; measured once per key."""
         from .renderer import Renderer
@@ -90,22 +121,16 @@ class Tuner:
         if not force and self.lookup(key):
             return self.lookup(key)
         timings = []
+        results = []
         with Renderer.new_from(scene, camera, opts, 0, form="megakernel", **renderer_kw) as r:
-            for width in BVH_WIDTHS:
-                r.set_tuning(bvh_width=width)
-                timings.append({"form": "megakernel", "bvh_width": width, "ms": self._frame_ms(r, frames, 1000)})
+            d = r.tuning()
+            start = {"bvh_width": d["bvh_width"], "shared_stack": d["shared_stack"], "block": d["block"]}
+            results.append(self._descend(r, "megakernel", MEGA_AXES, start, frames, 1000, timings, opts))
         with Renderer.new_from(scene, camera, opts, 0, form="wavefront", **renderer_kw) as r:
-            for sort in (False, True):
-                for width in BVH_WIDTHS:
-                    for budget in FETCH_BUDGETS:
-                        for wp in WAVE_PATHS:
-                            if wp < opts.samples:
-                                continue
-                            r.set_tuning(wave_paths=wp, sort_materials=sort, bvh_width=width, fetch_budget=budget)
-                            timings.append({"form": "wavefront", "wave_paths": wp, "sort_materials": sort,
-                                            "bvh_width": width, "fetch_budget": budget,
-                                            "ms": self._frame_ms(r, frames, 2000)})
-        best = min(timings, key=lambda t: t["ms"])
+            d = r.tuning()
+            start = {k: d[k] for k in ("sort_materials", "bvh_width", "shared_stack", "fetch_budget", "wave_paths")}
+            results.append(self._descend(r, "wavefront", WAVE_AXES, start, frames, 2000, timings, opts))
+        best = min(results, key=lambda t: t["ms"])
         cfg = {k: v for k, v in best.items() if k != "ms"}
         self.store(key, cfg, timings)
         return cfg

@@ -19,10 +19,13 @@
 // gradients of a sample are exact; density gradients are the score-function
 // estimator of the derivative of the expectation. Geometric edges are out of
 // scope. Gradients are summed with warp-aggregated atomics
-// (__match_any_sync on the material or medium index).
+// (__match_any_sync on the material or medium index). The replay kernel is
+// persistent with dynamic fetch of (pixel, sample) work items.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -98,119 +101,176 @@ __device__ __forceinline__ void medium_scores(const GpuScene& sc, const Ray& r, 
 constexpr int kAdjSharedStack = 8;
 using AdjStack = SplitStack<kAdjSharedStack, kAdjBlock>;
 
-template <uint32_t F>
-__device__ void replay_sample(AdjStack& stack, const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, uint32_t x,
-                              uint32_t y, uint32_t s, float d0, float d1, float d2) {
-  RngCtx ctx{fp.seed_lo, fp.seed_hi, y * fp.width + x, s, 0, nullptr};
-  Ray ray = camera_ray(fp, x, y, s, ctx);
+// One replayed path's vertices (thread-local): material, light and
+// albedo-dependence flags, the non-albedo factor g_j (Beer term), the
+// throughput before each vertex and the media's free-flight scores of each
+// segment.
+struct ReplayPath {
   int mat[kAdjMaxVertices];
-  bool light[kAdjMaxVertices], albdep[kAdjMaxVertices];
-  float g[kAdjMaxVertices][3], beta[kAdjMaxVertices + 1][3], score[kAdjMaxVertices + 1][kAdjMaxVolumes];
-  float b0 = 1.0f, b1 = 1.0f, b2 = 1.0f;
-  int K = 0;
-  bool escaped = false;
-  C3f sky{0.0f, 0.0f, 0.0f};
-  Counters cnt;
-  const uint32_t n_vol = ap.n_vol;
-  for (uint32_t depth = 0; depth <= fp.ray_depth; ++depth) {
-    ctx.depth = depth;
-    HitRec h;
-    bool hit = closest_hit_with<F, false>(stack, sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
-    int winner = -1;
-    if (hit && h.sdf < 0 && (F & F_VOL)) {
-      uint32_t kind = prim_kind(sc.prims[h.prim]);
-      if (kind == PK_VOL_SPHERE || kind == PK_VOL_BOX) winner = (int)(prim_id(sc.prims[h.prim]) - sc.vol_base);
-    }
-    beta[K][0] = b0; beta[K][1] = b1; beta[K][2] = b2;
-    if (F & F_VOL) medium_scores(sc, ray, 1e-3f, hit ? h.t : CUDART_INF_F, winner, n_vol, score[K]);
-    if (!hit) {
-      escaped = true;
-      sky = sky_colour(sc.sky, ray.d);
-      break;
-    }
-    Surface surf;
-    finalize_hit<F>(sc, ray, h, ctx, surf, 1e-3f);
-    const rg_material m = sc.materials[surf.material];
-    mat[K] = (int)surf.material;
-    light[K] = m.kind == RG_MAT_LIGHT;
-    albdep[K] = false;
-    g[K][0] = g[K][1] = g[K][2] = 1.0f;
-    ++K;
-    if (m.kind == RG_MAT_LIGHT || depth == fp.ray_depth) break;
-    V3 dir;
-    if (!scatter(m, ray, surf, ctx, dir)) break;
-    C3f a = attenuation<F>(sc, m, ray, surf);
-    if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) {
-      albdep[K - 1] = true;
-    } else if (!(m.kind == RG_MAT_DIELECTRIC && surf.front)) {
-      float e = expf(-m.density * length3(surf.pos - ray.o));
-      albdep[K - 1] = true;
-      g[K - 1][0] = g[K - 1][1] = g[K - 1][2] = e;
-    }
-    b0 = b0 * a.r; b1 = b1 * a.g; b2 = b2 * a.b;
-    ray = make_ray(surf.pos, dir);
+  uint32_t light, albdep;  // bit j: vertex j
+  float g[kAdjMaxVertices];
+  float beta[kAdjMaxVertices + 1][3];
+  float score[kAdjMaxVertices + 1][kAdjMaxVolumes];
+  float b0, b1, b2;
+  int K;
+  bool escaped;
+  C3f sky;
+};
+
+__device__ __forceinline__ void replay_begin(ReplayPath& P) {
+  P.b0 = P.b1 = P.b2 = 1.0f;
+  P.K = 0;
+  P.light = P.albdep = 0u;
+  P.escaped = false;
+  P.sky = C3f{0.0f, 0.0f, 0.0f};
+}
+
+// The segment of the path that just ended at its closest hit (or escaped):
+// records the vertex and, when the path goes on, replaces `ray` with the
+// scattered ray and returns true (the forward path's decisions, trace.cuh's
+// trace_path, with the same random streams).
+template <uint32_t F>
+__device__ __forceinline__ bool replay_segment(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap,
+                                               ReplayPath& P, Ray& ray, const RngCtx& ctx, uint32_t depth, bool hit,
+                                               const HitRec& h) {
+  const int K = P.K;
+  int winner = -1;
+  if (hit && h.sdf < 0 && (F & F_VOL)) {
+    uint32_t kind = prim_kind(sc.prims[h.prim]);
+    if (kind == PK_VOL_SPHERE || kind == PK_VOL_BOX) winner = (int)(prim_id(sc.prims[h.prim]) - sc.vol_base);
   }
-  // Backward over the vertices.
+  P.beta[K][0] = P.b0; P.beta[K][1] = P.b1; P.beta[K][2] = P.b2;
+  if (F & F_VOL) medium_scores(sc, ray, 1e-3f, hit ? h.t : CUDART_INF_F, winner, ap.n_vol, P.score[K]);
+  if (!hit) {
+    P.escaped = true;
+    P.sky = sky_colour(sc.sky, ray.d);
+    return false;
+  }
+  Surface surf;
+  finalize_hit<F>(sc, ray, h, ctx, surf, 1e-3f);
+  const rg_material m = sc.materials[surf.material];
+  P.mat[K] = (int)surf.material;
+  if (m.kind == RG_MAT_LIGHT) P.light |= 1u << K;
+  P.g[K] = 1.0f;
+  P.K = K + 1;
+  if (m.kind == RG_MAT_LIGHT || depth == fp.ray_depth) return false;
+  V3 dir;
+  if (!scatter(m, ray, surf, ctx, dir)) return false;
+  const C3f a = attenuation<F>(sc, m, ray, surf);
+  if (m.kind == RG_MAT_LAMBERTIAN || m.kind == RG_MAT_METAL) {
+    P.albdep |= 1u << K;
+  } else if (!(m.kind == RG_MAT_DIELECTRIC && surf.front)) {
+    P.albdep |= 1u << K;
+    P.g[K] = expf(-m.density * length3(surf.pos - ray.o));
+  }
+  P.b0 = P.b0 * a.r; P.b1 = P.b1 * a.g; P.b2 = P.b2 * a.b;
+  ray = make_ray(surf.pos, dir);
+  return true;
+}
+
+// Backward over a finished path's vertices, gradients to global memory with
+// warp-aggregated atomics among the lanes finishing together. (d0, d1, d2)
+// is the pixel's dLoss/dI divided by its samples.
+template <uint32_t F>
+__device__ __forceinline__ void replay_backward(const GpuScene& sc, const AdjParams& ap, const ReplayPath& P, float d0,
+                                                float d1, float d2) {
+  const int K = P.K;
+  const uint32_t n_vol = ap.n_vol;
   float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
-  if (escaped) {
-    c0 = sky.r; c1 = sky.g; c2 = sky.b;
+  if (P.escaped) {
+    c0 = P.sky.r; c1 = P.sky.g; c2 = P.sky.b;
     if (F & F_VOL)
       for (uint32_t v = 0; v < n_vol; ++v) {
-        float sv = score[K][v];
-        float gv = sv * (d0 * beta[K][0] * c0 + d1 * beta[K][1] * c1 + d2 * beta[K][2] * c2);
+        float sv = P.score[K][v];
+        float gv = sv * (d0 * P.beta[K][0] * c0 + d1 * P.beta[K][1] * c1 + d2 * P.beta[K][2] * c2);
         if (gv != 0.0f) warp_add1(ap.g_density, (int)v, gv);
       }
   }
   for (int j = K - 1; j >= 0; --j) {
-    const int m = mat[j];
+    const int m = P.mat[j];
     const rg_material mm = sc.materials[m];
-    if (light[j]) {
-      warp_add3(ap.g_emission, m, d0 * beta[j][0], d1 * beta[j][1], d2 * beta[j][2]);
+    if ((P.light >> j) & 1u) {
+      warp_add3(ap.g_emission, m, d0 * P.beta[j][0], d1 * P.beta[j][1], d2 * P.beta[j][2]);
       c0 = mm.albedo[0]; c1 = mm.albedo[1]; c2 = mm.albedo[2];
-    } else {
-      if (albdep[j]) {
-        warp_add3(ap.g_albedo, m, d0 * beta[j][0] * g[j][0] * c0, d1 * beta[j][1] * g[j][1] * c1,
-                  d2 * beta[j][2] * g[j][2] * c2);
-        c0 = c0 * (mm.albedo[0] * g[j][0]);
-        c1 = c1 * (mm.albedo[1] * g[j][1]);
-        c2 = c2 * (mm.albedo[2] * g[j][2]);
-      }
-      // a vertex that does not depend on the albedo (dielectric entry) passes c on unchanged
+    } else if ((P.albdep >> j) & 1u) {
+      const float gj = P.g[j];
+      warp_add3(ap.g_albedo, m, d0 * P.beta[j][0] * gj * c0, d1 * P.beta[j][1] * gj * c1, d2 * P.beta[j][2] * gj * c2);
+      c0 = c0 * (mm.albedo[0] * gj);
+      c1 = c1 * (mm.albedo[1] * gj);
+      c2 = c2 * (mm.albedo[2] * gj);
     }
+    // a vertex that does not depend on the albedo (dielectric entry) passes c on unchanged
     if (F & F_VOL)
       for (uint32_t v = 0; v < n_vol; ++v) {
-        float sv = score[j][v];
-        float gv = sv * (d0 * beta[j][0] * c0 + d1 * beta[j][1] * c1 + d2 * beta[j][2] * c2);
+        float sv = P.score[j][v];
+        float gv = sv * (d0 * P.beta[j][0] * c0 + d1 * P.beta[j][1] * c1 + d2 * P.beta[j][2] * c2);
         if (gv != 0.0f) warp_add1(ap.g_density, (int)v, gv);
       }
   }
 }
 
+// The replay, persistent with dynamic fetch: a warp keeps 32 paths in flight
+// (work item i = pixel i / spp, sample i % spp), traverses for `budget` node
+// visits at a time, and a lane whose path has ended (and been differentiated)
+// takes the next item from a global counter (one atomic per warp and
+// refill), so short paths do not leave lanes idle while a warp's longest path
+// finishes, as in the persistent wavefront kernels.
 template <uint32_t F>
-__global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_pix) {
+__global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_items,
+                                                      uint32_t* counter, int budget) {
   __shared__ uint2 stack_sh[kAdjSharedStack * kAdjBlock];
   uint2 stack_loc[kTravStack - kAdjSharedStack];
   AdjStack stack{stack_sh + threadIdx.x, stack_loc};
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t warp = blockIdx.x * (kAdjBlock / 32) + (threadIdx.x >> 5);
   const uint32_t spp = fp.spp;
   const float inv = 1.0f / (float)spp;
-  if (spp <= 32) {
-    const uint32_t ppw = 32 / spp;
-    const uint32_t lp = lane / spp, s = lane % spp;
-    const uint32_t pix = warp * ppw + lp;
-    if (lp < ppw && pix < n_pix) {
-      uint32_t x = pix % fp.width, y = pix / fp.width;
-      size_t idx = ((size_t)x * fp.height + y) * 3;
-      replay_sample<F>(stack, sc, fp, ap, x, y, s, ap.adjoint[idx] * inv, ap.adjoint[idx + 1] * inv, ap.adjoint[idx + 2] * inv);
+  bool has = false, drained = false;
+  uint32_t pix = 0, smp = 0, depth = 0;
+  float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f;
+  Ray ray;
+  Traversal t;
+  ReplayPath P;
+  Counters cnt;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !has);
+    if (idle && !drained) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(counter, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= n_items) drained = true;
+      if (!has) {
+        const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (i < n_items) {
+          pix = i / spp;
+          smp = i % spp;
+          const uint32_t x = pix % fp.width, y = pix / fp.width;
+          const size_t idx = ((size_t)x * fp.height + y) * 3;
+          d0 = ap.adjoint[idx] * inv;
+          d1 = ap.adjoint[idx + 1] * inv;
+          d2 = ap.adjoint[idx + 2] * inv;
+          const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, 0, nullptr};
+          ray = camera_ray(fp, x, y, smp, ctx);
+          replay_begin(P);
+          depth = 0;
+          trav_init<F>(t, sc, ray, 3.402823466e38f);
+          has = true;
+        }
+      }
     }
-  } else {
-    const uint32_t pix = warp;
-    if (pix < n_pix) {
-      uint32_t x = pix % fp.width, y = pix / fp.width;
-      size_t idx = ((size_t)x * fp.height + y) * 3;
-      float d0 = ap.adjoint[idx] * inv, d1 = ap.adjoint[idx + 1] * inv, d2 = ap.adjoint[idx + 2] * inv;
-      for (uint32_t s = lane; s < spp; s += 32) replay_sample<F>(stack, sc, fp, ap, x, y, s, d0, d1, d2);
+    if (!__any_sync(0xffffffffu, has)) break;
+    if (has) {
+      const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
+      if (trav_run<F, false, true>(t, stack, sc, ray, 1e-3f, ctx, cnt, fp.err, budget)) {
+        HitRec h;
+        const bool hit = finish_hit<F, false>(sc, ray, 1e-3f, 3.402823466e38f, t, h, cnt);
+        if (replay_segment<F>(sc, fp, ap, P, ray, ctx, depth, hit, h)) {
+          ++depth;
+          trav_init<F>(t, sc, ray, 3.402823466e38f);
+        } else {
+          replay_backward<F>(sc, ap, P, d0, d1, d2);
+          has = false;
+        }
+      }
     }
   }
 }
@@ -228,12 +288,14 @@ __global__ void k_l2_adjoint(const float* image, const float* target, float* adj
 }
 
 template <uint32_t F>
-void launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, cudaStream_t st) {
-  const uint32_t n_pix = fp.width * fp.height;
-  const uint32_t ppw = fp.spp <= 32 ? 32 / fp.spp : 1u;
-  const uint32_t warps = (n_pix + ppw - 1) / ppw;
-  const uint32_t blocks = (warps + kAdjBlock / 32 - 1) / (kAdjBlock / 32);
-  k_replay<F><<<blocks, kAdjBlock, 0, st>>>(sc, fp, ap, n_pix);
+void launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, uint32_t* counter, int device,
+                   int budget, cudaStream_t st) {
+  const uint32_t n_items = fp.width * fp.height * fp.spp;
+  int per_sm = 0, sms = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_replay<F>, kAdjBlock, 0);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  const uint32_t blocks = (uint32_t)(sms * std::max(per_sm, 1));
+  k_replay<F><<<blocks, kAdjBlock, 0, st>>>(sc, fp, ap, n_items, counter, budget);
 }
 
 }  // namespace
@@ -256,7 +318,7 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
     return set_error(h, RG_NOT_READY, "rg_backward differentiates whole frames: reset the sample range first");
   cudaStream_t st = h->stream;
   // Device scratch of the adjoint: image, target/adjoint image, gradients, loss.
-  size_t need = (2 * npx3 + 2 * (size_t)n_mat * 3 + n_vol + 4) * sizeof(float) + sizeof(double) + 512;
+  size_t need = (2 * npx3 + 2 * (size_t)n_mat * 3 + n_vol + 4) * sizeof(float) + sizeof(double) + 512 + 64;
   if (h->adj_bytes < need) {
     if (h->d_adj) cudaFree(h->d_adj);
     h->d_adj = nullptr;
@@ -303,8 +365,10 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
       return cuda_err(e);
   }
   AdjParams ap{d_adjoint, d_galb, d_gem, d_gden, n_vol};
+  // the replay's work counter (zeroed with the scratch), 16-byte aligned after the density gradients
+  uint32_t* d_counter = (uint32_t*)(((uintptr_t)(d_gden + n_vol) + 15) & ~(uintptr_t)15);
   dispatch_features(h->gs.features, [&](auto f) {
-    launch_replay<decltype(f)::value>(h->gs, fp, ap, st);
+    launch_replay<decltype(f)::value>(h->gs, fp, ap, d_counter, h->device, (int)effective_budget(h), st);
     return 0;
   });
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e);

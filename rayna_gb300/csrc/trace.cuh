@@ -245,13 +245,18 @@ __device__ __forceinline__ bool volume_t(const GpuPrim& p, uint32_t kind, uint32
 // ---------------------------------------------------------------------------
 constexpr float kBulbInner = 1.2f, kBulbOuter = 1.5f;
 
-// `iter_count`, when given, counts the Mandelbulb's escape-loop iterations (work counters).
+// `iter_count`, when given, counts the Mandelbulb's escape-loop iterations
+// (work counters). Every multiply-add here is written out (explicit fma, and
+// __fmul_rn where a product must not fuse into the caller's subtraction, as in
+// the normal's central differences), so the performance build evaluates the
+// function exactly as the arithmetic-contract build does, whichever kernel
+// inlines it.
 __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long long* iter_count = nullptr) {
   V3 q = x - v3(s.cx, s.cy, s.cz);
   if (s.kind == RG_SDF_SPHERE) return length3(q) - s.p0;
   if (s.kind == RG_SDF_TORUS) {
-    float a = __fsqrt_rn(q.x * q.x + q.z * q.z) - s.p0;
-    return __fsqrt_rn(a * a + q.y * q.y) - s.p1;
+    float a = __fsqrt_rn(__fmaf_rn(q.x, q.x, __fmul_rn(q.z, q.z))) - s.p0;
+    return __fsqrt_rn(__fmaf_rn(a, a, __fmul_rn(q.y, q.y))) - s.p1;
   }
   // Mandelbulb distance estimator: z -> z^power + c in spherical coordinates
   // with the running derivative dr; outside kBulbOuter the distance to the
@@ -260,7 +265,7 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long l
   float sc = s.p2;
   V3 z0 = v3(q.x / sc, q.y / sc, q.z / sc);
   float rq = length3(z0);
-  if (rq > kBulbOuter) return (rq - kBulbInner) * sc;
+  if (rq > kBulbOuter) return __fmul_rn(rq - kBulbInner, sc);
   float power = s.p0;
   int iters = (int)s.p1;
   V3 z = z0;
@@ -270,27 +275,27 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long l
     // cos p + i sin p = (x + i y)/rho, three complex squarings give 8t and 8p.
     for (int i = 0; i < iters; ++i) {
       if (counted) ++*counted;
-      float rho2 = z.x * z.x + z.y * z.y;
-      float r2 = rho2 + z.z * z.z;
+      float rho2 = __fmaf_rn(z.x, z.x, __fmul_rn(z.y, z.y));
+      float r2 = __fmaf_rn(z.z, z.z, rho2);
       rr = __fsqrt_rn(r2);
       if (rr > 2.0f) break;
       float rho = __fsqrt_rn(rho2);
       float ct = 1.0f, st = 0.0f, cp = 1.0f, sp = 0.0f;
-      if (rr > 0.0f) { ct = z.z / rr; st = rho / rr; }
-      if (rho > 0.0f) { cp = z.x / rho; sp = z.y / rho; }
+      if (rr > 0.0f) { ct = __fdiv_rn(z.z, rr); st = __fdiv_rn(rho, rr); }
+      if (rho > 0.0f) { cp = __fdiv_rn(z.x, rho); sp = __fdiv_rn(z.y, rho); }
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        float c2 = ct * ct - st * st;
-        st = 2.0f * ct * st;
+        float c2 = __fmaf_rn(ct, ct, -__fmul_rn(st, st));
+        st = __fmul_rn(2.0f * ct, st);
         ct = c2;
-        float d2 = cp * cp - sp * sp;
-        sp = 2.0f * cp * sp;
+        float d2 = __fmaf_rn(cp, cp, -__fmul_rn(sp, sp));
+        sp = __fmul_rn(2.0f * cp, sp);
         cp = d2;
       }
-      float r4 = r2 * r2;
-      float zr = r4 * r4;
-      dr = (r4 * r2 * rr) * 8.0f * dr + 1.0f;
-      z = v3(zr * (st * cp), zr * (sp * st), zr * ct) + z0;
+      float r4 = __fmul_rn(r2, r2);
+      float zr = __fmul_rn(r4, r4);
+      dr = __fmaf_rn(__fmul_rn(__fmul_rn(__fmul_rn(r4, r2), rr), 8.0f), dr, 1.0f);
+      z = v3(__fmaf_rn(zr, __fmul_rn(st, cp), z0.x), __fmaf_rn(zr, __fmul_rn(sp, st), z0.y), __fmaf_rn(zr, ct, z0.z));
     }
   } else {
     for (int i = 0; i < iters; ++i) {
@@ -298,15 +303,16 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long l
       if (rr > 2.0f) break;
       float theta = acosf(z.z / rr);
       float phi = atan2f(z.y, z.x);
-      dr = powf(rr, power - 1.0f) * power * dr + 1.0f;
+      dr = __fmaf_rn(__fmul_rn(powf(rr, power - 1.0f), power), dr, 1.0f);
       float zr = powf(rr, power);
       theta = theta * power;
       phi = phi * power;
       float st = sinf(theta);
-      z = v3(zr * (st * cosf(phi)), zr * (sinf(phi) * st), zr * cosf(theta)) + z0;
+      z = v3(__fmaf_rn(zr, __fmul_rn(st, cosf(phi)), z0.x), __fmaf_rn(zr, __fmul_rn(sinf(phi), st), z0.y),
+             __fmaf_rn(zr, cosf(theta), z0.z));
     }
   }
-  return (0.5f * logf(rr) * rr / dr) * sc;
+  return __fmul_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, logf(rr)), rr), dr), sc);
 }
 
 // Planar::intersect_bounded (mesh/planar/mod.rs:161-194): the distance to
@@ -349,6 +355,18 @@ __device__ __forceinline__ bool quad_t(const GpuPrim& p, const float* quad_ext, 
 // objects are tested in; callers evaluate it against [start, inf) and clip
 // the result to their end, which is order-independent and equals the
 // reference's answer for the first object tested.
+//
+// The body quadratic a t^2 + 2 b t + c (a = L^2 - (ba.d)^2, b = L^2 oc.d -
+// (ba.oc)(ba.d), c = L^2 |oc|^2 - (ba.oc)^2 - r^2 L^2 with ba = p2 - p1 of
+// length L) is the reference's; in f32 its discriminant b^2 - a c cancels
+// for grazing rays (normals off by up to 2e-3). It is evaluated here without
+// that cancellation, as the sphere's is: with dp = L^2 d - (ba.d) ba and
+// op = L^2 oc - (ba.oc) ba (the components normal to the axis, scaled),
+// b = op.d, c = |op|^2 / L^2 - r^2 L^2 and b^2 - a c = a (r^2 L^2 -
+// |op - (b/a) dp|^2 / L^2), the vector being the ray's closest approach to
+// the axis; the roots are q / a and c / q with q = -(b + sign(b) sqrt(disc)).
+// A ray parallel to the axis (a = 0) misses, as in the reference (its body
+// roots are infinite and its cap test |a t + b| < |b| fails).
 struct CylHit { float t, dan; uint32_t face; };
 __device__ __forceinline__ bool cylinder_t(const GpuPrim& p, const Ray& r, float start, float end, CylHit& ch) {
   const V3 o1 = xyz(p.a), along = xyz(p.b);
@@ -356,13 +374,22 @@ __device__ __forceinline__ bool cylinder_t(const GpuPrim& p, const Ray& r, float
   const V3 oc = v3(r.o.x - o1.x, r.o.y - o1.y, r.o.z - o1.z);
   const float bard = dot3(along, r.d), baoc = dot3(along, oc);
   const float a = __fmaf_rn(-bard, bard, lsq);
-  const float b = __fmaf_rn(lsq, dot3(oc, r.d), -(baoc * bard));
-  const float c = __fmaf_rn(lsq, dot3(oc, oc), -(baoc * baoc)) - (rad * rad) * lsq;
-  const float disc = __fmaf_rn(b, b, -(c * a));
+  if (a == 0.0f) return false;
+  const V3 dp = v3(__fmaf_rn(lsq, r.d.x, -(bard * along.x)), __fmaf_rn(lsq, r.d.y, -(bard * along.y)),
+                   __fmaf_rn(lsq, r.d.z, -(bard * along.z)));
+  const V3 op = v3(__fmaf_rn(lsq, oc.x, -(baoc * along.x)), __fmaf_rn(lsq, oc.y, -(baoc * along.y)),
+                   __fmaf_rn(lsq, oc.z, -(baoc * along.z)));
+  const float b = dot3(op, r.d);
+  const float c = __fmaf_rn(-(rad * rad), lsq, __fdiv_rn(dot3(op, op), lsq));
+  const float k = __fdiv_rn(b, a);
+  const V3 w = v3(__fmaf_rn(-k, dp.x, op.x), __fmaf_rn(-k, dp.y, op.y), __fmaf_rn(-k, dp.z, op.z));
+  const float disc = a * __fmaf_rn(rad * rad, lsq, -__fdiv_rn(dot3(w, w), lsq));
   if (disc < 0.0f) return false;
   const float sq = __fsqrt_rn(disc);
-  float dist = __fdiv_rn(-b - sq, a);
-  if (!(start <= dist && dist <= end)) dist = __fdiv_rn(-b + sq, a);
+  const float q = b > 0.0f ? -b - sq : -b + sq;
+  const float r1 = __fdiv_rn(q, a), r2 = q != 0.0f ? __fdiv_rn(c, q) : q;
+  float dist = fminf(r1, r2);
+  if (!(start <= dist && dist <= end)) dist = fmaxf(r1, r2);
   if (!(start <= dist && dist <= end)) return false;
   const float dan = __fdiv_rn(__fmaf_rn(dist, bard, baoc), lsq);
   ch.dan = dan;

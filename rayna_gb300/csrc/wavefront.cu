@@ -307,7 +307,13 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
         }
       }
     }
-    if (!__any_sync(0xffffffffu, has)) break;
+    // A lane can end its path at fetch (out of reach of the bound sphere):
+    // the warp stops only once the queue is drained, not when a refill
+    // happens to leave every lane idle.
+    if (!__any_sync(0xffffffffu, has)) {
+      if (drained) break;
+      continue;
+    }
     if (has) {
       int st = kMarchOn;
       for (int e = 0; e < budget && st == kMarchOn; ++e)

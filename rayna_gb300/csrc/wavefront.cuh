@@ -173,8 +173,10 @@ __device__ __forceinline__ void accumulate_pixel(const FrameParams& fp, const Pa
   }
   uint32_t x = pix % fp.width, y = pix / fp.width;
   size_t idx = ((size_t)x * fp.height + y) * 3 + c;
-  float mean = sum / (float)fp.spp_total;  // spp_total = spp unless the frame is one sample range of it
-  float acc = fp.accum[idx] + mean;
+  float mean = sum / (float)spp;
+  // the accumulation adds sum / spp_total: the mean itself for a whole frame,
+  // this range's share of it for one sample range of the frame
+  float acc = fp.accum[idx] + (spp == fp.spp_total ? mean : sum / (float)fp.spp_total);
   fp.accum[idx] = acc;
   if (fp.out) fp.out[idx] = (float)((double)acc / (double)fp.accum_count);
   if (fp.frame_mean) fp.frame_mean[idx] = mean;

@@ -108,10 +108,7 @@ class Renderer:
         from .autotune import Tuner
         cfg = (tuner or Tuner()).tune_render(scene, camera, options, **kw)
         r = cls(scene, camera, options, form=cfg["form"], **kw)
-        r.set_tuning(bvh_width=cfg.get("bvh_width", 0))
-        if cfg["form"] == "wavefront":
-            r.set_tuning(wave_paths=cfg["wave_paths"], sort_materials=cfg.get("sort_materials", False),
-                         fetch_budget=cfg.get("fetch_budget", 0))
+        r.set_tuning(**{k: v for k, v in cfg.items() if k != "form"})
         return r
 
     @classmethod

@@ -13,6 +13,12 @@ def test_keys_bucket_by_size():
     assert autotune.batch_key(64, 2_700_000, 52_000_000, 2_000_000_000).startswith("batch:n6:")
 
 
+def test_default_cache_is_outside_the_package():
+    import os
+    pkg = os.path.dirname(os.path.abspath(autotune.__file__))
+    assert not os.path.abspath(autotune.DEFAULT_CACHE).startswith(pkg)
+
+
 def test_cache_round_trip(tmp_path):
     path = tmp_path / "tune.json"
     t = autotune.Tuner(str(path))
@@ -34,6 +40,10 @@ def test_tuning_pass_picks_a_measured_candidate(tmp_path):
     assert cfg["form"] in ("megakernel", "wavefront")
     entry = t.table[autotune.render_key(488, 64, 36, 8)]
     assert len(entry["timings"]) >= 2 and all(x["ms"] > 0 for x in entry["timings"])
+    # the stack placement and the megakernel's block size were searched
+    mega = [x for x in entry["timings"] if x["form"] == "megakernel"]
+    assert {x["block"] for x in mega} == set(autotune.MEGA_BLOCKS)
+    assert {x["shared_stack"] for x in mega} == set(autotune.SHARED_STACKS)
     with Renderer.tuned(scene, cam, opts, tuner=t) as r:
         assert r.form == cfg["form"]
         r.render()
