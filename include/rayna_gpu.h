@@ -400,7 +400,8 @@ typedef struct rg_tuning {
     uint32_t block;           /* megakernel: threads per block, 64, 128 or 256; 0 = 256 */
     uint32_t stack_limit;     /* test knob: traversal stack entries a ray may use (1-64); a ray that needs more
                                  drops the far subtree and the frame reports RG_QUEUE_OVERFLOW; 0 = all 64 */
-    uint32_t reserved[1];     /* must be 0 */
+    uint32_t march_budget;    /* material-sorted wavefront with raymarched SDFs: distance evaluations a lane of a
+                                 march stage performs between refills of idle lanes (1-4096); 0 = 8 */
 } rg_tuning;
 
 #define RG_SHARED_STACK_NONE 0xFFFFFFFFu

@@ -134,6 +134,20 @@ def render_window(flat, camera, opts, window, seed=0, frames=1, policy=POLICY_RE
     return st, mean, var, secs.value
 
 
+def ln_f32(x) -> np.ndarray:
+    """The f32 natural logarithm the f32 policy and the device share."""
+    L = lib()
+    if not hasattr(L, "_ln_bound"):
+        L.orc_ln_f32.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]
+        L.orc_ln_f32.restype = None
+        L._ln_bound = True
+    a = np.ascontiguousarray(x, np.float32).ravel()
+    out = np.empty_like(a)
+    fp = lambda v: v.ctypes.data_as(C.POINTER(C.c_float))
+    L.orc_ln_f32(fp(a), fp(out), a.size)
+    return out
+
+
 def hardware_threads() -> int:
     return int(lib().orc_hardware_threads())
 

@@ -256,4 +256,9 @@ int orc_query_colour(const rg_scene_desc* d, int policy, uint32_t n, const float
 
 int orc_hardware_threads(void) { return (int)std::thread::hardware_concurrency(); }
 
+// The f32 policy's (and the device's) natural logarithm over an array.
+void orc_ln_f32(const float* x, float* out, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) out[i] = ln_f32(x[i]);
+}
+
 }  // extern "C"

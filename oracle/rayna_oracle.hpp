@@ -39,6 +39,7 @@
 #include <limits>
 #include <memory>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "../include/rayna_gpu.h"
@@ -113,6 +114,38 @@ template <class T> inline V3<T> operator*(V3<T> a, T s) { return {a.x * s, a.y *
 template <class T> inline V3<T> operator/(V3<T> a, T s) { return {a.x / s, a.y / s, a.z / s}; }
 template <class T> inline V3<T> operator-(V3<T> a) { return {-a.x, -a.y, -a.z}; }
 template <class T> inline T comp(V3<T> v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+
+// The device's natural logarithm (trace.cuh, ln_f32), operation for
+// operation: x = m 2^e with m in [sqrt(1/2), sqrt(2)), ln m = 2 atanh(s) by
+// the series of Abramowitz & Stegun 4.1.27 to s^9, e ln 2 in two parts. The
+// f32 policy uses it for the free-flight distance and the Mandelbulb; the f64
+// policy uses std::log.
+inline float ln_f32(float x) {
+  if (!(x > 0.0f)) return x == 0.0f ? -std::numeric_limits<float>::infinity() : std::numeric_limits<float>::quiet_NaN();
+  if (std::isinf(x)) return x;
+  int e = 0;
+  if (x < 1.17549435e-38f) { x = x * 8388608.0f; e = -23; }
+  uint32_t bits;
+  std::memcpy(&bits, &x, 4);
+  e += (int)((bits >> 23) & 0xFFu) - 127;
+  const uint32_t mb = (bits & 0x7FFFFFu) | 0x3F800000u;
+  float m;
+  std::memcpy(&m, &mb, 4);
+  if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+  const float s = (m - 1.0f) / (m + 1.0f);
+  const float s2 = s * s;
+  float p = std::fma(s2, 0.111111111f, 0.142857143f);
+  p = std::fma(s2, p, 0.2f);
+  p = std::fma(s2, p, 0.333333333f);
+  p = std::fma(s2, p, 1.0f);
+  const float lm = (2.0f * s) * p;
+  const float fe = (float)e;
+  return std::fma(fe, 0.693145751953125f, std::fma(fe, 1.42860676533018e-06f, lm));
+}
+template <class T> inline T policy_log(T x) {
+  if constexpr (std::is_same_v<T, float>) return ln_f32(x);
+  else return std::log(x);
+}
 
 template <class P> struct Math {
   using T = typename P::T;
@@ -689,7 +722,7 @@ template <class P> struct Sdf {
           z = V3<T>{zr * (st * cp), zr * (sp * st), zr * ct} + z0;
         }
       }
-      return (T(0.5) * std::log(r) * r / dr) * s;
+      return (T(0.5) * policy_log(r) * r / dr) * s;
     }
     for (int i = 0; i < iters; ++i) {
       r = Math<P>::length(z);
@@ -713,7 +746,7 @@ template <class P> struct Sdf {
         z = V3<T>{zr * (st * std::cos(phi)), zr * (std::sin(phi) * st), zr * std::cos(theta)} + z0;
       }
     }
-    return (T(0.5) * std::log(r) * r / dr) * s;
+    return (T(0.5) * policy_log(r) * r / dr) * s;
   }
   // RaymarchedIsosurfaceMesh::intersect (raymarched.rs:73-122)
   bool intersect(const Ray<P>& ray, const Interval<T>& iv, Hit<T>& h) const {
@@ -1400,7 +1433,7 @@ template <class P> struct Scene {
     if (rng.injected_volume_u) u = (T)rng.injected_volume_u[vi];
     else if (rng.gpu) { blk = rng.block(depth, kPurposeVolume0 + vi); u = (T)u01f_open0(blk.v[0]); }
     else u = (T)rng.seq.gen();
-    T hit_dist = v.neg_inv_density * std::log(u);
+    T hit_dist = v.neg_inv_density * policy_log(u);
     T dist = enter + hit_dist;
     if (hit_dist > inside) return false;
     h.dist = dist;

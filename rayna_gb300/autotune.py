@@ -11,7 +11,8 @@ form; for the megakernel the tree (binary or 8-wide), the traversal stack's
 placement (entries per thread in shared memory) and the block size; for the
 wavefront the tree, fused or material-sorted shading, the node visits between
 refills of the persistent traversal kernels, the path budget per wave (queue
-capacity) and the stack placement. Each form is searched by coordinate
+capacity), the stack placement and, for scenes with raymarched SDFs, the
+evaluations per lane between refills of the march stages. Each form is searched by coordinate
 descent: from the library defaults, one knob at a time over its candidates,
 keeping the best, in a fixed order. Batches choose the batched form (wavefront
 with its path slots per wave, or tiles with the persistent kernel's block
@@ -38,8 +39,10 @@ SHARED_STACKS = [-1, 8, 16]  # -1: the whole traversal stack in local memory
 MEGA_BLOCKS = [64, 128, 256]
 # Coordinate-descent axes per form, searched in this order.
 MEGA_AXES = [("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS), ("block", MEGA_BLOCKS)]
+MARCH_BUDGETS = [4, 8, 16, 32]
 WAVE_AXES = [("sort_materials", [False, True]), ("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS),
              ("fetch_budget", FETCH_BUDGETS), ("wave_paths", WAVE_PATHS)]
+WAVE_SDF_AXES = WAVE_AXES + [("march_budget", MARCH_BUDGETS)]
 BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 23, 1 << 24, 1 << 25)] +
                 [dict(form="tiles", block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)])
 
@@ -129,7 +132,11 @@ class Tuner:
         with Renderer.new_from(scene, camera, opts, 0, form="wavefront", **renderer_kw) as r:
             d = r.tuning()
             start = {k: d[k] for k in ("sort_materials", "bvh_width", "shared_stack", "fetch_budget", "wave_paths")}
-            results.append(self._descend(r, "wavefront", WAVE_AXES, start, frames, 2000, timings, opts))
+            axes = WAVE_AXES
+            if flat.desc.n_sdfs:  # the march stages' refill budget
+                start["march_budget"] = d["march_budget"]
+                axes = WAVE_SDF_AXES
+            results.append(self._descend(r, "wavefront", axes, start, frames, 2000, timings, opts))
         best = min(results, key=lambda t: t["ms"])
         cfg = {k: v for k, v in best.items() if k != "ms"}
         self.store(key, cfg, timings)

@@ -47,7 +47,13 @@ struct AdjParams {
   float* g_emission;     // n_mat x 3
   float* g_density;      // n_vol
   uint32_t n_vol;
+  uint32_t n_mat;
+  int block_sums;        // accumulate per block in shared memory, flush to g_* at the end
 };
+
+// Gradient entries a block can sum in shared memory (48 KB less the 16 KB
+// of traversal stacks): scenes with up to 2730 materials.
+constexpr uint32_t kAdjSharedGrads = 8192;
 
 // Adds (v0, v1, v2) to base[3*key .. 3*key+2], one atomic per distinct key in the warp.
 __device__ __forceinline__ void warp_add3(float* base, int key, float v0, float v1, float v2) {
@@ -117,6 +123,13 @@ struct ReplayPath {
   C3f sky;
 };
 
+// Where a path's gradients go: the block's shared-memory sums, or global memory.
+struct GradSink {
+  float* albedo;
+  float* emission;
+  float* density;
+};
+
 __device__ __forceinline__ void replay_begin(ReplayPath& P) {
   P.b0 = P.b1 = P.b2 = 1.0f;
   P.K = 0;
@@ -172,8 +185,8 @@ __device__ __forceinline__ bool replay_segment(const GpuScene& sc, const FramePa
 // warp-aggregated atomics among the lanes finishing together. (d0, d1, d2)
 // is the pixel's dLoss/dI divided by its samples.
 template <uint32_t F>
-__device__ __forceinline__ void replay_backward(const GpuScene& sc, const AdjParams& ap, const ReplayPath& P, float d0,
-                                                float d1, float d2) {
+__device__ __forceinline__ void replay_backward(const GpuScene& sc, const AdjParams& ap, const GradSink& gs,
+                                                const ReplayPath& P, float d0, float d1, float d2) {
   const int K = P.K;
   const uint32_t n_vol = ap.n_vol;
   float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
@@ -183,18 +196,18 @@ __device__ __forceinline__ void replay_backward(const GpuScene& sc, const AdjPar
       for (uint32_t v = 0; v < n_vol; ++v) {
         float sv = P.score[K][v];
         float gv = sv * (d0 * P.beta[K][0] * c0 + d1 * P.beta[K][1] * c1 + d2 * P.beta[K][2] * c2);
-        if (gv != 0.0f) warp_add1(ap.g_density, (int)v, gv);
+        if (gv != 0.0f) warp_add1(gs.density, (int)v, gv);
       }
   }
   for (int j = K - 1; j >= 0; --j) {
     const int m = P.mat[j];
     const rg_material mm = sc.materials[m];
     if ((P.light >> j) & 1u) {
-      warp_add3(ap.g_emission, m, d0 * P.beta[j][0], d1 * P.beta[j][1], d2 * P.beta[j][2]);
+      warp_add3(gs.emission, m, d0 * P.beta[j][0], d1 * P.beta[j][1], d2 * P.beta[j][2]);
       c0 = mm.albedo[0]; c1 = mm.albedo[1]; c2 = mm.albedo[2];
     } else if ((P.albdep >> j) & 1u) {
       const float gj = P.g[j];
-      warp_add3(ap.g_albedo, m, d0 * P.beta[j][0] * gj * c0, d1 * P.beta[j][1] * gj * c1, d2 * P.beta[j][2] * gj * c2);
+      warp_add3(gs.albedo, m, d0 * P.beta[j][0] * gj * c0, d1 * P.beta[j][1] * gj * c1, d2 * P.beta[j][2] * gj * c2);
       c0 = c0 * (mm.albedo[0] * gj);
       c1 = c1 * (mm.albedo[1] * gj);
       c2 = c2 * (mm.albedo[2] * gj);
@@ -204,7 +217,7 @@ __device__ __forceinline__ void replay_backward(const GpuScene& sc, const AdjPar
       for (uint32_t v = 0; v < n_vol; ++v) {
         float sv = P.score[j][v];
         float gv = sv * (d0 * P.beta[j][0] * c0 + d1 * P.beta[j][1] * c1 + d2 * P.beta[j][2] * c2);
-        if (gv != 0.0f) warp_add1(ap.g_density, (int)v, gv);
+        if (gv != 0.0f) warp_add1(gs.density, (int)v, gv);
       }
   }
 }
@@ -214,10 +227,22 @@ __device__ __forceinline__ void replay_backward(const GpuScene& sc, const AdjPar
 // visits at a time, and a lane whose path has ended (and been differentiated)
 // takes the next item from a global counter (one atomic per warp and
 // refill), so short paths do not leave lanes idle while a warp's longest path
-// finishes, as in the persistent wavefront kernels.
+// finishes, as in the persistent wavefront kernels. Lanes that finish
+// together are few and of unrelated pixels, so gradient atomics aggregate
+// little within a warp; with `block_sums` they go to the block's shared
+// memory (the popular materials' addresses no longer serialise in L2) and
+// each block adds its sums to global memory once, at the end.
 template <uint32_t F>
 __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_items,
                                                       uint32_t* counter, int budget) {
+  extern __shared__ float grad_sh[];  // albedo, emission (n_mat x 3 each), density (n_vol), with block_sums
+  const uint32_t n_grad = 6 * ap.n_mat + ap.n_vol;
+  GradSink gs{ap.g_albedo, ap.g_emission, ap.g_density};
+  if (ap.block_sums) {
+    for (uint32_t i = threadIdx.x; i < n_grad; i += blockDim.x) grad_sh[i] = 0.0f;
+    gs = GradSink{grad_sh, grad_sh + 3 * ap.n_mat, grad_sh + 6 * ap.n_mat};
+    __syncthreads();
+  }
   __shared__ uint2 stack_sh[kAdjSharedStack * kAdjBlock];
   uint2 stack_loc[kTravStack - kAdjSharedStack];
   AdjStack stack{stack_sh + threadIdx.x, stack_loc};
@@ -267,9 +292,20 @@ __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams f
           ++depth;
           trav_init<F>(t, sc, ray, 3.402823466e38f);
         } else {
-          replay_backward<F>(sc, ap, P, d0, d1, d2);
+          replay_backward<F>(sc, ap, gs, P, d0, d1, d2);
           has = false;
         }
+      }
+    }
+  }
+  if (ap.block_sums) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n_grad; i += blockDim.x) {
+      const float v = grad_sh[i];
+      if (v != 0.0f) {
+        float* dst = i < 3 * ap.n_mat ? ap.g_albedo + i
+                   : (i < 6 * ap.n_mat ? ap.g_emission + (i - 3 * ap.n_mat) : ap.g_density + (i - 6 * ap.n_mat));
+        atomicAdd(dst, v);
       }
     }
   }
@@ -291,11 +327,12 @@ template <uint32_t F>
 void launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, uint32_t* counter, int device,
                    int budget, cudaStream_t st) {
   const uint32_t n_items = fp.width * fp.height * fp.spp;
+  const size_t smem = ap.block_sums ? (6 * (size_t)ap.n_mat + ap.n_vol) * sizeof(float) : 0;
   int per_sm = 0, sms = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_replay<F>, kAdjBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_replay<F>, kAdjBlock, smem);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   const uint32_t blocks = (uint32_t)(sms * std::max(per_sm, 1));
-  k_replay<F><<<blocks, kAdjBlock, 0, st>>>(sc, fp, ap, n_items, counter, budget);
+  k_replay<F><<<blocks, kAdjBlock, smem, st>>>(sc, fp, ap, n_items, counter, budget);
 }
 
 }  // namespace
@@ -364,7 +401,7 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
     if ((e = cudaMemcpyAsync(d_adjoint, adjoint, npx3 * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return cuda_err(e);
   }
-  AdjParams ap{d_adjoint, d_galb, d_gem, d_gden, n_vol};
+  AdjParams ap{d_adjoint, d_galb, d_gem, d_gden, n_vol, n_mat, 6 * n_mat + n_vol <= kAdjSharedGrads ? 1 : 0};
   // the replay's work counter (zeroed with the scratch), 16-byte aligned after the density gradients
   uint32_t* d_counter = (uint32_t*)(((uintptr_t)(d_gden + n_vol) + 15) & ~(uintptr_t)15);
   dispatch_features(h->gs.features, [&](auto f) {

@@ -1025,8 +1025,7 @@ rg_status rg_backward_frame(rg_handle h, uint64_t seed, const float* target_rgb,
 
 rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   if (!h || !t) return fail(h, RG_INVALID_ARG, "rg_set_tuning: NULL argument");
-  for (uint32_t r : t->reserved)
-    if (r != 0) return fail(h, RG_INVALID_ARG, "rg_tuning: reserved fields must be 0");
+  if (t->march_budget > 4096) return fail(h, RG_INVALID_ARG, "rg_tuning: march_budget must be at most 4096");
   if (t->shared_stack != 0 && t->shared_stack != RG_SHARED_STACK_NONE && t->shared_stack != 4 && t->shared_stack != 8 &&
       t->shared_stack != 16)
     return fail(h, RG_INVALID_ARG, "rg_tuning: shared_stack must be 0, RG_SHARED_STACK_NONE, 4, 8 or 16");
@@ -1045,6 +1044,7 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   h->shared_stack = t->shared_stack;
   h->mega_block = t->block;
   h->stack_limit = t->stack_limit;
+  h->march_budget = t->march_budget;
   apply_features(h);
   return RG_OK;
 }
@@ -1059,6 +1059,7 @@ rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
   out->shared_stack = h->gs.shared_stack ? h->gs.shared_stack : RG_SHARED_STACK_NONE;
   out->block = h->mega_block ? h->mega_block : 256u;
   out->stack_limit = h->gs.stack_limit;
+  out->march_budget = h->march_budget ? h->march_budget : 8u;
   return RG_OK;
 }
 

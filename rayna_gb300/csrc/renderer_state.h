@@ -114,6 +114,7 @@ struct rg_renderer {
   uint32_t shared_stack = 0;  // requested shared traversal-stack entries: 0 default, RG_SHARED_STACK_NONE, 4, 8, 16
   uint32_t mega_block = 0;    // megakernel threads per block (0: 256)
   uint32_t stack_limit = 0;   // traversal stack entries a ray may use (0: kStackSize)
+  uint32_t march_budget = 0;  // SDF evaluations per lane between refills in the march stages (0: kMarchBudget)
   uint32_t range_first = 0;   // rg_set_sample_range: the frame's first sample
   uint32_t range_count = 0;   //   and its number of samples (0: whole frames)
   uint32_t kinds = 0;         // F_* primitive-kind bits of the scene's kernel variant

@@ -46,6 +46,35 @@ __device__ __forceinline__ bool try_normalize3(V3 v, V3& out) {
 }
 __device__ __forceinline__ float signumf(float x) { return isnan(x) ? x : copysignf(1.0f, x); }
 
+// Natural logarithm, written out so that the oracle's f32 policy evaluates
+// the same operations (its own ln_f32) and the free-flight distances and the
+// Mandelbulb's distance bit for bit alike: x = m 2^e with m in [sqrt(1/2),
+// sqrt(2)), ln m = 2 atanh(s) = 2 (s + s^3/3 + ... + s^9/9) with s = (m - 1) /
+// (m + 1), |s| < 0.172 (the series of Abramowitz & Stegun 4.1.27; the
+// truncation is below 1e-9), and e ln 2 in two parts. Error within 3 ulp of
+// the exact logarithm over the normal and subnormal range (the roundings of s
+// and of the series); 0 gives -inf,
+// negative values NaN, +inf itself.
+__device__ __forceinline__ float ln_f32(float x) {
+  if (!(x > 0.0f)) return x == 0.0f ? -CUDART_INF_F : CUDART_NAN_F;
+  if (isinf(x)) return x;
+  int e = 0;
+  if (x < 1.17549435e-38f) { x = __fmul_rn(x, 8388608.0f); e = -23; }  // subnormal: scale by 2^23
+  const uint32_t bits = __float_as_uint(x);
+  e += (int)((bits >> 23) & 0xFFu) - 127;
+  float m = __uint_as_float((bits & 0x7FFFFFu) | 0x3F800000u);
+  if (m > 1.41421356f) { m = __fmul_rn(m, 0.5f); e += 1; }
+  const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+  const float s2 = __fmul_rn(s, s);
+  float p = __fmaf_rn(s2, 0.111111111f, 0.142857143f);
+  p = __fmaf_rn(s2, p, 0.2f);
+  p = __fmaf_rn(s2, p, 0.333333333f);
+  p = __fmaf_rn(s2, p, 1.0f);
+  const float lm = __fmul_rn(__fmul_rn(2.0f, s), p);
+  const float fe = (float)e;
+  return __fmaf_rn(fe, 0.693145751953125f, __fmaf_rn(fe, 1.42860676533018e-06f, lm));
+}
+
 // ---------------------------------------------------------------------------
 // Philox4x32-10 counter-based random numbers (Salmon et al., SC'11).
 // Block (pixel, sample, depth, purpose) keyed by the frame seed.
@@ -234,7 +263,7 @@ __device__ __forceinline__ bool volume_t(const GpuPrim& p, uint32_t kind, uint32
   float inside = exitd - enter;
   float u = ctx.vol_u ? ctx.vol_u[vol_index] : u01_open0(ctx.block(kPurposeVolume0 + vol_index).x);
   float neg_inv_density = kind == PK_VOL_SPHERE ? p.b.z : p.c.w;
-  float hit_dist = neg_inv_density * logf(u);
+  float hit_dist = __fmul_rn(neg_inv_density, ln_f32(u));
   if (hit_dist > inside) return false;
   t = enter + hit_dist;
   return true;
@@ -312,7 +341,7 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long l
              __fmaf_rn(zr, cosf(theta), z0.z));
     }
   }
-  return __fmul_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, logf(rr)), rr), dr), sc);
+  return __fmul_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, ln_f32(rr)), rr), dr), sc);
 }
 
 // Planar::intersect_bounded (mesh/planar/mod.rs:161-194): the distance to

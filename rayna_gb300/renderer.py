@@ -230,7 +230,7 @@ class Renderer:
 
     def set_tuning(self, wave_paths: int | None = None, sort_materials: bool | None = None,
                    bvh_width: int | None = None, fetch_budget: int | None = None, shared_stack: int | None = None,
-                   block: int | None = None, stack_limit: int | None = None):
+                   block: int | None = None, stack_limit: int | None = None, march_budget: int | None = None):
         """Launch knobs (rg_tuning); None leaves a knob as it is. wave_paths:
         wavefront path slots per wave (0 = library default); sort_materials:
         wavefront shading in material-kind order (True) or one fused bounce
@@ -240,7 +240,9 @@ class Renderer:
         shared_stack: traversal stack entries per thread in shared memory
         (0 = library default, -1 = none, else 4, 8 or 16); block: megakernel
         threads per block (0 = 256, else 64 or 128); stack_limit: a test knob
-        capping the traversal stack a ray may use (0 = all 64)."""
+        capping the traversal stack a ray may use (0 = all 64); march_budget:
+        SDF evaluations per lane between refills in the material-sorted
+        wavefront's march stages (0 = 8)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
         # the resolved defaults come back from rg_get_tuning; hand the requested knobs back
@@ -259,6 +261,8 @@ class Renderer:
             t.block = int(block)
         if stack_limit is not None:
             t.stack_limit = int(stack_limit)
+        if march_budget is not None:
+            t.march_budget = int(march_budget)
         self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
         self._stack_knobs = (t.shared_stack, t.block, t.stack_limit)
 
@@ -269,7 +273,7 @@ class Renderer:
         return {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials == 1, "bvh_width": t.bvh_width,
                 "fetch_budget": t.fetch_budget,
                 "shared_stack": -1 if t.shared_stack == A.RG_SHARED_STACK_NONE else t.shared_stack,
-                "block": t.block, "stack_limit": t.stack_limit}
+                "block": t.block, "stack_limit": t.stack_limit, "march_budget": t.march_budget}
 
     def set_sample_range(self, first: int, count: int):
         """Frames trace samples [first, first + count) of each pixel's

@@ -276,7 +276,7 @@ pub struct rg_tuning {
     pub shared_stack: u32,
     pub block: u32,
     pub stack_limit: u32,
-    pub reserved: [u32; 1],
+    pub march_budget: u32,
 }
 
 #[repr(C)]

@@ -168,3 +168,23 @@ def test_sample_range_matches_the_oracle_path_by_path(form):
     frac = np.all(np.abs(gm - om) <= 1e-4 * (1 + np.abs(om)), axis=2).mean()
     print(f"sample range [{first}, {first + count}) ({form}): {frac:.4f} of pixels match the f32 oracle path for path")
     assert frac >= 0.97
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_march_stages_render_the_megakernel_image(exact):
+    """The material-sorted wavefront marches each SDF in its own persistent
+    stage, `march_budget` evaluations per lane between refills; every budget,
+    and the megakernel's one-call march, give the same image bits."""
+    scene, cam, opts = small(presets.sdf_volumes, 64, 36, 8, 12, n_spheres=20)
+    with Renderer.new_from(scene, cam, opts, 0, form="megakernel", exact=exact) as r:
+        ref = r.render(seed=23).img
+    for budget in (1, 4, 8, 64):
+        with Renderer.new_from(scene, cam, opts, 0, form="wavefront", exact=exact) as r:
+            r.set_tuning(sort_materials=True, march_budget=budget)
+            assert r.tuning()["march_budget"] == budget
+            out = r.render(seed=23)
+            assert out.stats.error_flags == 0
+            np.testing.assert_array_equal(out.img, ref, err_msg=f"march budget {budget}")
+    with Renderer.new_from(scene, cam, opts, 0) as r:
+        with pytest.raises(RaynaError):
+            r.set_tuning(march_budget=5000)

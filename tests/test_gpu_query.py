@@ -191,7 +191,7 @@ def sdf_distance_bound(flat, prim, d, n64):
     return out
 
 
-def compare_f64(flat, o, d, g, label, min_agree=0.999, max_prim_diff=0.002):
+def compare_f64(flat, o, d, g, label, min_agree=0.999, max_prim_diff=0.002, max_leak=0.0):
     """Device hits g against the faithful f64 oracle; returns a dict of the
     agreement figures (asserting the bars in the module docstring)."""
     h, t64, n64 = ob.query(flat, o, d, policy=ob.POLICY_REF_F64, pretest=True)
@@ -214,7 +214,13 @@ def compare_f64(flat, o, d, g, label, min_agree=0.999, max_prim_diff=0.002):
     c0 = D.n_spheres + D.n_triangles + D.n_boxes + D.n_volumes + D.n_sdfs + D.n_quads
     is_cyl = lambda pr: (pr >= c0) & (pr < c0 + D.n_cylinders)
     cyl_rule = pdiff & (is_cyl(g["prim"]) | is_cyl(h["prim"])) & (t32 < t64)
-    assert (t_ok | cyl_rule)[pdiff].all(), f"{label}: a primitive disagreement that is not a near-tie of distance"
+    # Moller-Trumbore is not watertight (triangle.rs:53-109 rejects u, v
+    # outside [0, 1] with rounding either side of a shared edge): a ray aimed
+    # exactly at a shared vertex can pass between the triangles in one
+    # precision and hit one of them in the other, then hit something behind
+    leak = pdiff & ~t_ok & ~cyl_rule
+    frac_leak = leak.sum() / max(both.sum(), 1)
+    assert frac_leak <= max_leak, f"{label}: {leak.sum()} primitive disagreements that are not near-ties ({frac_leak:.5f})"
     m = both & ~pdiff
     assert t_ok[m].all(), f"{label}: {np.sum(~t_ok[m])} distances outside tolerance; worst rel {rel[m][~t_ok[m]].max()}"
     ill = float(np.mean(rel[m] > 1e-5)) if m.any() else 0.0
@@ -227,7 +233,8 @@ def compare_f64(flat, o, d, g, label, min_agree=0.999, max_prim_diff=0.002):
     assert n_ok[m].all(), (f"{label}: {np.sum(~n_ok[m])} normals outside tolerance; worst {nerr[m][~n_ok[m]].max():.3e}"
                            f" (bound {nb[m][~n_ok[m]].max():.3e})")
     n_beyond = float(np.mean(nerr[m] > 1e-5)) if m.any() else 0.0
-    return {"agree": float(agree), "prim_diff": float(frac_pdiff), "cylinder_rule": int(cyl_rule.sum()), "t_ill": ill,
+    return {"agree": float(agree), "prim_diff": float(frac_pdiff), "cylinder_rule": int(cyl_rule.sum()),
+            "edge_leaks": int(leak.sum()), "t_ill": ill,
             "t_median_rel": float(np.median(rel[m])) if m.any() else 0.0, "normal_beyond_1e-5": n_beyond,
             "normal_median": float(np.median(nerr[m])) if m.any() else 0.0, "hits": int(m.sum())}
 
@@ -324,7 +331,7 @@ def test_query_vs_f64_oracle(suite, exact):
     with renderer_for(scene, 2, exact=exact) as r:
         g = r.query_rays(o, d)
     st = compare_f64(flat, o, d, g, suite, min_agree=0.998 if suite == "planar" else 0.999,
-                     max_prim_diff=MAX_PRIM_DIFF.get(suite, 0.002))
+                     max_prim_diff=MAX_PRIM_DIFF.get(suite, 0.002), max_leak=0.01 if suite == "triangles" else 0.0)
     build = "exact" if exact else "performance"
     print(f"{suite} ({build} build) vs f64: {st}")
 
@@ -376,14 +383,15 @@ def test_query_volumes_injected_uniforms(bvh_width, transformed):
     assert agree64 >= 0.999, agree64
 
 
-def test_query_mandelbulb_tolerance():
+@pytest.mark.parametrize("exact", [True, False])
+def test_query_mandelbulb_tolerance(exact):
     rng = np.random.Generator(np.random.PCG64(6))
     from rayna_gb300.scene import Scene
     s = sdf_scene()
     scene = Scene(objects=[s.objects[2]])
     flat = flatten(scene)
     o, d = rays_at(rng, 3000, (-3.7, -1.2, -1.2), (-1.3, 1.2, 1.2), inside_frac=0.0)
-    with renderer_for(scene) as r:
+    with renderer_for(scene, exact=exact) as r:
         g = r.query_rays(o, d)
     h, _, _ = ob.query(flat, o, d, policy=ob.POLICY_GPU_F32, pretest=False)
     agree = np.mean(g["hit"] == h["hit"])
@@ -392,3 +400,8 @@ def test_query_mandelbulb_tolerance():
     assert m.sum() > 300
     err = np.abs(g["t"][m] - h["t"][m])
     assert np.mean(err <= 1e-3) >= 0.99, np.quantile(err, 0.99)
+    # the distance estimator is the same sequence of IEEE operations on both
+    # sides (its logarithm included), so the marches agree bit for bit
+    same = np.mean(bits(g["t"][m]) == bits(h["t"][m]))
+    print(f"mandelbulb: {same:.5f} of hits bit-exact")
+    assert same >= 0.999, same

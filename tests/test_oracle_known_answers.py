@@ -42,3 +42,26 @@ def test_triangle_known_answers(policy, rtol):
         K.check_triangle(hits, t, n_int, front, ray_n, rtol, t_hits=t64, n_hits=n64)
     else:
         K.check_triangle(hits, t, n_int, front, ray_n, rtol)
+
+
+def test_ln_f32_within_three_ulp():
+    """The logarithm the f32 policy and the device share (the atanh series of
+    Abramowitz & Stegun 4.1.27): within 3 ulp of the exact value over normal
+    and subnormal arguments, and the IEEE special cases."""
+    rng = np.random.Generator(np.random.PCG64(1))
+    x = np.concatenate([
+        rng.uniform(0, 1, 200000).astype(np.float32),
+        np.exp(rng.uniform(-87, 88, 200000)).astype(np.float32),
+        np.float32(2.0) ** np.arange(-149, 128, dtype=np.float64).astype(np.float32),
+        np.nextafter(np.float32(1.0), np.float32(2.0)) + np.zeros(1, np.float32),
+        np.array([1.0, 0.5, 2.0, 1.4142135, 1.4142137, 0.70710677], np.float32),
+    ])
+    x = x[x > 0]
+    got = ob.ln_f32(x).astype(np.float64)
+    exact = np.log(x.astype(np.float64))
+    ulp = np.spacing(np.abs(exact).astype(np.float32)).astype(np.float64)
+    err = np.abs(got - exact) / np.maximum(ulp, np.finfo(np.float32).tiny)
+    assert err.max() <= 3.0, (err.max(), x[np.argmax(err)])
+    assert ob.ln_f32([1.0])[0] == 0.0
+    sp = ob.ln_f32([0.0, -1.0, np.inf, np.nan])
+    assert sp[0] == -np.inf and np.isnan(sp[1]) and sp[2] == np.inf and np.isnan(sp[3])
