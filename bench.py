@@ -174,18 +174,19 @@ def cpu_baseline(name: str, threads: int, target_s: float = 15.0):
                       f"({ns / 1e6:.2f} M samples, {secs:.1f} s), f64 oracle, {threads} threads"}, secs
 
 
-def run_adjoint(iters: int = 5, stream=None):
+def run_adjoint(iters: int = 5, stream=None, width: int = 512, height: int = 512):
     """Differentiable-rendering workload: 1000 Lambertian spheres (3000 albedo
     parameters) + one medium (3 albedo + 1 density), 512x512, forward and
     backward at 16 spp, depth 8, L2 loss against a 1024-spp target of the
     ground-truth parameters; Adam steps on the host. Each iteration renders the
     forward frame, then takes the adjoint of that frame (rg_backward_frame: its
-    image, the paths of an independent frame key replayed). Returns timings."""
+    image, the paths of an independent frame key replayed). Returns timings.
+    `width`, `height`: a smaller image of the same scene (profiling)."""
     import torch
 
     from rayna_gb300 import Renderer, presets
-    scene, cam, opts = presets.adjoint_scene(n_spheres=1000, ground_truth=False)
-    gt, _, _ = presets.adjoint_scene(n_spheres=1000, ground_truth=True)
+    scene, cam, opts = presets.adjoint_scene(n_spheres=1000, ground_truth=False, width=width, height=height)
+    gt, _, _ = presets.adjoint_scene(n_spheres=1000, ground_truth=True, width=width, height=height)
     s = stream.cuda_stream if stream is not None else None
     topts = type(opts)(width=opts.width, height=opts.height, samples=1024, ray_depth=opts.ray_depth)
     with Renderer.new_from(gt, cam, topts, 0, stream=s) as r:
@@ -482,6 +483,12 @@ def run_gpu(args, rank, world):
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
+    if args.adjoint_only:  # the adjoint workload alone (profiling), at --width x --height when given
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        res = run_adjoint(iters=args.steps, stream=stream, width=args.width or 512, height=args.height or 512)
+        print(json.dumps({"adjoint": res}), flush=True)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -564,6 +571,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--only", action="store_true", help="time the --workload alone (no `workloads` sub-results)")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run the adjoint workload alone (iterations = --steps; --width/--height shrink it)")
     ap.add_argument("--sub-steps", type=int, default=5, help="timed frames of the other workloads")
     ap.add_argument("--batch-scale", type=float, default=1.0,
                     help="resolution scale of the batched workload (1: the configured resolutions; 0: skip)")
