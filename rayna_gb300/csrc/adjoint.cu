@@ -19,8 +19,8 @@
 // gradients of a sample are exact; density gradients are the score-function
 // estimator of the derivative of the expectation. Geometric edges are out of
 // scope. Gradients are summed with warp-aggregated atomics
-// (__match_any_sync on the material or medium index). The replay kernel is
-// persistent with dynamic fetch of (pixel, sample) work items.
+// (__match_any_sync on the material or medium index), per block in shared
+// memory when the scene's gradients fit there.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,8 +52,12 @@ struct AdjParams {
 };
 
 // Gradient entries a block can sum in shared memory (48 KB less the 16 KB
-// of traversal stacks): scenes with up to 2730 materials.
+// of traversal stacks): scenes with up to 1365 materials. RG_ADJ_BLOCK_SUMS=0
+// at build time sends every gradient atomic to global memory instead.
 constexpr uint32_t kAdjSharedGrads = 8192;
+#ifndef RG_ADJ_BLOCK_SUMS
+#define RG_ADJ_BLOCK_SUMS 1
+#endif
 
 // Adds (v0, v1, v2) to base[3*key .. 3*key+2], one atomic per distinct key in the warp.
 __device__ __forceinline__ void warp_add3(float* base, int key, float v0, float v1, float v2) {
@@ -222,19 +226,36 @@ __device__ __forceinline__ void replay_backward(const GpuScene& sc, const AdjPar
   }
 }
 
-// The replay, persistent with dynamic fetch: a warp keeps 32 paths in flight
-// (work item i = pixel i / spp, sample i % spp), traverses for `budget` node
-// visits at a time, and a lane whose path has ended (and been differentiated)
-// takes the next item from a global counter (one atomic per warp and
-// refill), so short paths do not leave lanes idle while a warp's longest path
-// finishes, as in the persistent wavefront kernels. Lanes that finish
-// together are few and of unrelated pixels, so gradient atomics aggregate
-// little within a warp; with `block_sums` they go to the block's shared
-// memory (the popular materials' addresses no longer serialise in L2) and
-// each block adds its sums to global memory once, at the end.
+// One path of pixel (x, y), sample s: traced again with its random streams,
+// then differentiated; (d0, d1, d2) is the pixel's dLoss/dI over its samples.
 template <uint32_t F>
-__global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_items,
-                                                      uint32_t* counter, int budget) {
+__device__ __forceinline__ void replay_path(AdjStack& stack, const GpuScene& sc, const FrameParams& fp,
+                                            const AdjParams& ap, const GradSink& gs, uint32_t x, uint32_t y, uint32_t s,
+                                            float d0, float d1, float d2) {
+  const uint32_t pix = y * fp.width + x;
+  Ray ray = camera_ray(fp, x, y, s, RngCtx{fp.seed_lo, fp.seed_hi, pix, s, 0, nullptr});
+  ReplayPath P;
+  replay_begin(P);
+  Counters cnt;
+  for (uint32_t depth = 0;; ++depth) {
+    const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, s, depth, nullptr};
+    HitRec h;
+    const bool hit = closest_hit_with<F, false>(stack, sc, ray, 1e-3f, 3.402823466e38f, ctx, h, cnt, fp.err);
+    if (!replay_segment<F>(sc, fp, ap, P, ray, ctx, depth, hit, h)) break;
+  }
+  replay_backward<F>(sc, ap, gs, P, d0, d1, d2);
+}
+
+// The replay: one thread per pixel-sample, a warp taking whole pixels as the
+// megakernel does (its lanes then end their backward passes together, so
+// the warp-aggregated atomics group every lane with the same material).
+// With `block_sums` the gradients go to the block's shared memory and each
+// block adds its sums to global memory once, at the end. (A persistent
+// dynamic-fetch form of this kernel measured slower: 7.4 against 5.9 ms per
+// iteration on the adjoint workload, since lanes finishing at different times
+// aggregate their atomics far less.)
+template <uint32_t F>
+__global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_pix) {
   extern __shared__ float grad_sh[];  // albedo, emission (n_mat x 3 each), density (n_vol), with block_sums
   const uint32_t n_grad = 6 * ap.n_mat + ap.n_vol;
   GradSink gs{ap.g_albedo, ap.g_emission, ap.g_density};
@@ -247,55 +268,26 @@ __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams f
   uint2 stack_loc[kTravStack - kAdjSharedStack];
   AdjStack stack{stack_sh + threadIdx.x, stack_loc};
   const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = blockIdx.x * (kAdjBlock / 32) + (threadIdx.x >> 5);
   const uint32_t spp = fp.spp;
   const float inv = 1.0f / (float)spp;
-  bool has = false, drained = false;
-  uint32_t pix = 0, smp = 0, depth = 0;
-  float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f;
-  Ray ray;
-  Traversal t;
-  ReplayPath P;
-  Counters cnt;
-  for (;;) {
-    const unsigned idle = __ballot_sync(0xffffffffu, !has);
-    if (idle && !drained) {
-      uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(counter, (uint32_t)__popc(idle));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (base + (uint32_t)__popc(idle) >= n_items) drained = true;
-      if (!has) {
-        const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-        if (i < n_items) {
-          pix = i / spp;
-          smp = i % spp;
-          const uint32_t x = pix % fp.width, y = pix / fp.width;
-          const size_t idx = ((size_t)x * fp.height + y) * 3;
-          d0 = ap.adjoint[idx] * inv;
-          d1 = ap.adjoint[idx + 1] * inv;
-          d2 = ap.adjoint[idx + 2] * inv;
-          const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, 0, nullptr};
-          ray = camera_ray(fp, x, y, smp, ctx);
-          replay_begin(P);
-          depth = 0;
-          trav_init<F>(t, sc, ray, 3.402823466e38f);
-          has = true;
-        }
-      }
+  if (spp <= 32) {
+    const uint32_t ppw = 32 / spp;
+    const uint32_t lp = lane / spp, s = lane % spp;
+    const uint32_t pix = warp * ppw + lp;
+    if (lp < ppw && pix < n_pix) {
+      const uint32_t x = pix % fp.width, y = pix / fp.width;
+      const size_t idx = ((size_t)x * fp.height + y) * 3;
+      replay_path<F>(stack, sc, fp, ap, gs, x, y, s, ap.adjoint[idx] * inv, ap.adjoint[idx + 1] * inv,
+                     ap.adjoint[idx + 2] * inv);
     }
-    if (!__any_sync(0xffffffffu, has)) break;
-    if (has) {
-      const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
-      if (trav_run<F, false, true>(t, stack, sc, ray, 1e-3f, ctx, cnt, fp.err, budget)) {
-        HitRec h;
-        const bool hit = finish_hit<F, false>(sc, ray, 1e-3f, 3.402823466e38f, t, h, cnt);
-        if (replay_segment<F>(sc, fp, ap, P, ray, ctx, depth, hit, h)) {
-          ++depth;
-          trav_init<F>(t, sc, ray, 3.402823466e38f);
-        } else {
-          replay_backward<F>(sc, ap, gs, P, d0, d1, d2);
-          has = false;
-        }
-      }
+  } else {
+    const uint32_t pix = warp;
+    if (pix < n_pix) {
+      const uint32_t x = pix % fp.width, y = pix / fp.width;
+      const size_t idx = ((size_t)x * fp.height + y) * 3;
+      const float d0 = ap.adjoint[idx] * inv, d1 = ap.adjoint[idx + 1] * inv, d2 = ap.adjoint[idx + 2] * inv;
+      for (uint32_t s = lane; s < spp; s += 32) replay_path<F>(stack, sc, fp, ap, gs, x, y, s, d0, d1, d2);
     }
   }
   if (ap.block_sums) {
@@ -324,15 +316,13 @@ __global__ void k_l2_adjoint(const float* image, const float* target, float* adj
 }
 
 template <uint32_t F>
-void launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, uint32_t* counter, int device,
-                   int budget, cudaStream_t st) {
-  const uint32_t n_items = fp.width * fp.height * fp.spp;
+void launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, cudaStream_t st) {
+  const uint32_t n_pix = fp.width * fp.height;
+  const uint32_t ppw = fp.spp <= 32 ? 32 / fp.spp : 1u;
+  const uint32_t warps = (n_pix + ppw - 1) / ppw;
+  const uint32_t blocks = (warps + kAdjBlock / 32 - 1) / (kAdjBlock / 32);
   const size_t smem = ap.block_sums ? (6 * (size_t)ap.n_mat + ap.n_vol) * sizeof(float) : 0;
-  int per_sm = 0, sms = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_replay<F>, kAdjBlock, smem);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  const uint32_t blocks = (uint32_t)(sms * std::max(per_sm, 1));
-  k_replay<F><<<blocks, kAdjBlock, smem, st>>>(sc, fp, ap, n_items, counter, budget);
+  k_replay<F><<<blocks, kAdjBlock, smem, st>>>(sc, fp, ap, n_pix);
 }
 
 }  // namespace
@@ -401,11 +391,10 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
     if ((e = cudaMemcpyAsync(d_adjoint, adjoint, npx3 * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return cuda_err(e);
   }
-  AdjParams ap{d_adjoint, d_galb, d_gem, d_gden, n_vol, n_mat, 6 * n_mat + n_vol <= kAdjSharedGrads ? 1 : 0};
-  // the replay's work counter (zeroed with the scratch), 16-byte aligned after the density gradients
-  uint32_t* d_counter = (uint32_t*)(((uintptr_t)(d_gden + n_vol) + 15) & ~(uintptr_t)15);
+  AdjParams ap{d_adjoint, d_galb, d_gem, d_gden, n_vol, n_mat,
+               RG_ADJ_BLOCK_SUMS && 6 * n_mat + n_vol <= kAdjSharedGrads ? 1 : 0};
   dispatch_features(h->gs.features, [&](auto f) {
-    launch_replay<decltype(f)::value>(h->gs, fp, ap, d_counter, h->device, (int)effective_budget(h), st);
+    launch_replay<decltype(f)::value>(h->gs, fp, ap, st);
     return 0;
   });
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e);

@@ -285,8 +285,13 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
   bool any = false;
   SdfMarch m;
   for (;;) {
-    const unsigned idle = __ballot_sync(0xffffffffu, !has);
-    if (idle && !drained) {
+    // Refill idle lanes until every lane has a march or the queue is drained:
+    // most paths end at fetch (out of reach of the bound sphere), and a lane
+    // that took one must not wait out the marching lanes' budget before its
+    // next fetch.
+    while (!drained) {
+      const unsigned idle = __ballot_sync(0xffffffffu, !has);
+      if (!idle) break;
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(next, (uint32_t)__popc(idle));
       base = __shfl_sync(0xffffffffu, base, 0);
@@ -307,13 +312,7 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
         }
       }
     }
-    // A lane can end its path at fetch (out of reach of the bound sphere):
-    // the warp stops only once the queue is drained, not when a refill
-    // happens to leave every lane idle.
-    if (!__any_sync(0xffffffffu, has)) {
-      if (drained) break;
-      continue;
-    }
+    if (!__any_sync(0xffffffffu, has)) break;  // drained, and nothing left to march
     if (has) {
       int st = kMarchOn;
       for (int e = 0; e < budget && st == kMarchOn; ++e)

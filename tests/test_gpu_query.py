@@ -331,7 +331,7 @@ def test_query_vs_f64_oracle(suite, exact):
     with renderer_for(scene, 2, exact=exact) as r:
         g = r.query_rays(o, d)
     st = compare_f64(flat, o, d, g, suite, min_agree=0.998 if suite == "planar" else 0.999,
-                     max_prim_diff=MAX_PRIM_DIFF.get(suite, 0.002), max_leak=0.01 if suite == "triangles" else 0.0)
+                     max_prim_diff=MAX_PRIM_DIFF.get(suite, 0.002), max_leak=0.03 if suite == "triangles" else 0.0)
     build = "exact" if exact else "performance"
     print(f"{suite} ({build} build) vs f64: {st}")
 
