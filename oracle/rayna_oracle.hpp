@@ -684,8 +684,9 @@ template <class P> struct Sdf {
     V3<T> z = z0;
     T dr = T(1), r = T(0);
     if (power == T(8)) {
-      // z^8 without transcendentals: with cos t = z/r, sin t = rho/r and
-      // cos p + i sin p = (x + i y)/rho, three complex squarings give 8t, 8p.
+      // z^8 without transcendentals: w = z + i rho (|w| = r, arg w = t) squared
+      // three times is r^8 (cos 8t + i sin 8t); the azimuth's unit complex
+      // number (x + i y) / rho squared three times is cos 8p + i sin 8p.
       for (int i = 0; i < iters; ++i) {
         T rho2, r2;
         if constexpr (P::gpu) {  // the device's explicit fused multiply-adds
@@ -698,28 +699,30 @@ template <class P> struct Sdf {
         r = std::sqrt(r2);
         if (r > T(2)) break;
         T rho = std::sqrt(rho2);
-        T ct = T(1), st = T(0), cp = T(1), sp = T(0);
-        if (r > T(0)) { ct = z.z / r; st = rho / r; }
-        if (rho > T(0)) { cp = z.x / rho; sp = z.y / rho; }
+        T wa = z.z, wb = rho, cp = T(1), sp = T(0);
+        if (rho > T(0)) {
+          T inv = T(1) / rho;
+          cp = z.x * inv;
+          sp = z.y * inv;
+        }
         for (int k = 0; k < 3; ++k) {
-          T c2, d2;
-          if constexpr (P::gpu) c2 = std::fma(ct, ct, -(st * st));
-          else c2 = ct * ct - st * st;
-          st = T(2) * ct * st;
-          ct = c2;
+          T a2, d2;
+          if constexpr (P::gpu) a2 = std::fma(wa, wa, -(wb * wb));
+          else a2 = wa * wa - wb * wb;
+          wb = T(2) * wa * wb;
+          wa = a2;
           if constexpr (P::gpu) d2 = std::fma(cp, cp, -(sp * sp));
           else d2 = cp * cp - sp * sp;
           sp = T(2) * cp * sp;
           cp = d2;
         }
         T r4 = r2 * r2;
-        T zr = r4 * r4;
         if constexpr (P::gpu) {
           dr = std::fma((r4 * r2 * r) * T(8), dr, T(1));
-          z = V3<T>{std::fma(zr, st * cp, z0.x), std::fma(zr, sp * st, z0.y), std::fma(zr, ct, z0.z)};
+          z = V3<T>{std::fma(wb, cp, z0.x), std::fma(wb, sp, z0.y), wa + z0.z};
         } else {
           dr = (r4 * r2 * r) * T(8) * dr + T(1);
-          z = V3<T>{zr * (st * cp), zr * (sp * st), zr * ct} + z0;
+          z = V3<T>{wb * cp + z0.x, wb * sp + z0.y, wa + z0.z};
         }
       }
       return (T(0.5) * policy_log(r) * r / dr) * s;

@@ -300,8 +300,11 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long l
   V3 z = z0;
   float dr = 1.0f, rr = 0.0f;
   if (power == 8.0f) {
-    // z^8 without transcendentals: with cos t = z/r, sin t = rho/r and
-    // cos p + i sin p = (x + i y)/rho, three complex squarings give 8t and 8p.
+    // z^8 without transcendentals or per-iteration normalisation of the polar
+    // angle: with w = z + i rho (|w| = r, arg w = t) three complex squarings
+    // give w^8 = r^8 (cos 8t + i sin 8t); the azimuth's unit complex number
+    // (x + i y) / rho, squared three times, gives cos 8p + i sin 8p. One
+    // division and two square roots per iteration.
     for (int i = 0; i < iters; ++i) {
       if (counted) ++*counted;
       float rho2 = __fmaf_rn(z.x, z.x, __fmul_rn(z.y, z.y));
@@ -309,22 +312,24 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long l
       rr = __fsqrt_rn(r2);
       if (rr > 2.0f) break;
       float rho = __fsqrt_rn(rho2);
-      float ct = 1.0f, st = 0.0f, cp = 1.0f, sp = 0.0f;
-      if (rr > 0.0f) { ct = __fdiv_rn(z.z, rr); st = __fdiv_rn(rho, rr); }
-      if (rho > 0.0f) { cp = __fdiv_rn(z.x, rho); sp = __fdiv_rn(z.y, rho); }
+      float wa = z.z, wb = rho, cp = 1.0f, sp = 0.0f;
+      if (rho > 0.0f) {
+        const float inv = __fdiv_rn(1.0f, rho);
+        cp = __fmul_rn(z.x, inv);
+        sp = __fmul_rn(z.y, inv);
+      }
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        float c2 = __fmaf_rn(ct, ct, -__fmul_rn(st, st));
-        st = __fmul_rn(2.0f * ct, st);
-        ct = c2;
+        float a2 = __fmaf_rn(wa, wa, -__fmul_rn(wb, wb));
+        wb = __fmul_rn(2.0f * wa, wb);
+        wa = a2;
         float d2 = __fmaf_rn(cp, cp, -__fmul_rn(sp, sp));
         sp = __fmul_rn(2.0f * cp, sp);
         cp = d2;
       }
       float r4 = __fmul_rn(r2, r2);
-      float zr = __fmul_rn(r4, r4);
       dr = __fmaf_rn(__fmul_rn(__fmul_rn(__fmul_rn(r4, r2), rr), 8.0f), dr, 1.0f);
-      z = v3(__fmaf_rn(zr, __fmul_rn(st, cp), z0.x), __fmaf_rn(zr, __fmul_rn(sp, st), z0.y), __fmaf_rn(zr, ct, z0.z));
+      z = v3(__fmaf_rn(wb, cp, z0.x), __fmaf_rn(wb, sp, z0.y), __fadd_rn(wa, z0.z));
     }
   } else {
     for (int i = 0; i < iters; ++i) {
