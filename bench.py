@@ -328,8 +328,9 @@ PRIM_COST = {"mesh": (48, 27, 1), "spheres": (16, 17, 1), "sdf": (16, 17, 1)}  #
 
 def roofline(workload: str, r: dict, hbm_gbs: float, sm_count: int, sm_mhz: float) -> dict:
     """Roofline of the dominant kernels of one frame (the traversal launches:
-    the megakernel, or the wavefront's bounce / extend kernels, timed live with
-    their own CUDA events): achieved = the largest of algorithmic bytes / time
+    the megakernel, or the wavefront's bounce / extend / march kernels; their
+    time is the timed frames' device time times their share of a frame,
+    measured with their own CUDA events on separate frames): achieved = the largest of algorithmic bytes / time
     against the measured HBM copy bandwidth, FP32 operations / time against
     SMs x 128 lanes x 2 (FMA) x the sampled SM clock, and SFU operations / time
     against SMs x 16 x the sampled clock."""
@@ -371,8 +372,7 @@ def time_form(name, scene, cam, opts, form, steps, warmup, stream, flush, rank, 
     from rayna_gb300 import Renderer
     from rayna_gb300 import _abi as A
     kind, sort, width = FORMS[form]
-    r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank,
-                          stage_times=True)
+    r = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=1000 + rank)
     r.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
     # counting frame: algorithmic work per frame (node visits, primitive tests, SDF steps, hits)
     rc = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=99, counters=True)
@@ -388,7 +388,6 @@ def time_form(name, scene, cam, opts, form, steps, warmup, stream, flush, rank, 
         dist.barrier()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    traverse_ms = 0.0
     launches = 0
     torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
@@ -398,12 +397,25 @@ def time_form(name, scene, cam, opts, form, steps, warmup, stream, flush, rank, 
             starts[k].record(stream)
             A.check(lib, h, lib.rg_render_async(h, r.next_seed(), None, C.byref(st)))
             ends[k].record(stream)
-            # the traversal kernels' own event pairs, read back after each frame
-            A.check(lib, h, lib.rg_sync_stats(h, C.byref(st)))
-            traverse_ms += st.traverse_ms
             launches += st.kernel_launches
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
+    # The traversal kernels' share of a frame, from their own event pairs
+    # (RG_FLAG_STAGE_TIMES) on separate frames: recording those events between
+    # launches costs time, so the timed frames above carry none.
+    rs = Renderer.new_from(scene, cam, opts, 0, form=kind, stream=stream.cuda_stream, seed=2000 + rank,
+                           stage_times=True)
+    rs.set_tuning(sort_materials=sort, bvh_width=width, fetch_budget=args.fetch_budget)
+    trav, frame = [], []
+    for k in range(4):
+        flush.fill_(float(k))
+        A.check(rs._lib, rs.handle, rs._lib.rg_render_async(rs.handle, rs.next_seed(), None, C.byref(st)))
+        A.check(rs._lib, rs.handle, rs._lib.rg_sync_stats(rs.handle, C.byref(st)))
+        if k:
+            trav.append(st.traverse_ms)
+            frame.append(st.kernel_ms)
+    rs.close()
+    share = sum(trav) / max(sum(frame), 1e-9)
     if dist:
         dist.barrier()
     ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
@@ -429,7 +441,8 @@ def time_form(name, scene, cam, opts, form, steps, warmup, stream, flush, rank, 
         "node_visits": cst.node_visits, "prim_tests": cst.prim_tests, "sdf_steps": cst.sdf_steps,
         "sdf_iterations": cst.sdf_iterations, "hits": cst.hits, "pixels": opts.width * opts.height,
         "wall_s": wall, "clocks": clk.summary(), "launches_per_frame": launches // max(steps, 1),
-        "bvh_width": width, "traverse_ms_per_step": traverse_ms / steps, "steps": steps,
+        "bvh_width": width, "traverse_ms_per_step": dev_s * 1e3 / steps * share, "traverse_share": share,
+        "steps": steps,
     }
 
 

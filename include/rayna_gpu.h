@@ -392,16 +392,15 @@ typedef struct rg_tuning {
                                  only, sorted otherwise) */
     uint32_t bvh_width;       /* 2 = binary node pairs, 8 = compressed 8-wide nodes; 0 = library default (2).
                                  Either tree gives the same closest hits. */
-    uint32_t fetch_budget;    /* wavefront: node visits a lane traverses between refills of idle lanes; 0 = 8
-                                 (6 for scenes of spheres only) */
+    uint32_t fetch_budget;    /* wavefront: node visits a lane traverses between refills of idle lanes; 0 = 6 */
     uint32_t shared_stack;    /* entries of each thread's traversal stack kept in shared memory (the deeper ones
                                  live in local memory): 0 = library default (8 for scenes of triangles only, else
                                  none), RG_SHARED_STACK_NONE = all in local memory, else 4, 8 or 16 */
-    uint32_t block;           /* megakernel: threads per block, 64, 128 or 256; 0 = 256 */
+    uint32_t block;           /* megakernel: threads per block, 64, 128 or 256; 0 = 128 */
     uint32_t stack_limit;     /* test knob: traversal stack entries a ray may use (1-64); a ray that needs more
                                  drops the far subtree and the frame reports RG_QUEUE_OVERFLOW; 0 = all 64 */
     uint32_t march_budget;    /* material-sorted wavefront with raymarched SDFs: distance evaluations a lane of a
-                                 march stage performs between refills of idle lanes (1-4096); 0 = 8 */
+                                 march stage performs between refills of idle lanes (1-4096); 0 = 32 */
 } rg_tuning;
 
 #define RG_SHARED_STACK_NONE 0xFFFFFFFFu

@@ -382,7 +382,7 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
     ff.frame_var = nullptr;
     ff.accum_count = 1;
     // the handle's kernel form renders it (both forms give the same image)
-    e = h->form == RG_FORM_WAVEFRONT ? launch_wavefront(h, ff) : launch_megakernel(h->gs, ff, false, st, h->mega_block);
+    e = h->form == RG_FORM_WAVEFRONT ? launch_wavefront(h, ff) : launch_megakernel(h->gs, ff, false, st, h->mega_block ? h->mega_block : kDefaultMegaBlock);
     if (e != cudaSuccess) return cuda_err(e);
     if ((e = cudaMemcpyAsync(d_adjoint, target, npx3 * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return cuda_err(e);

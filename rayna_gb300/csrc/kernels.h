@@ -7,7 +7,7 @@
 
 namespace rg {
 
-// `block`: threads per block (a multiple of 32, at most 256; 0 = 256). The
+// `block`: threads per block (a multiple of 32, at most 256; 0 = 256, the launch bound). The
 // launch takes sc.shared_stack x block x 8 bytes of dynamic shared memory.
 cudaError_t launch_megakernel(const GpuScene& sc, const FrameParams& fp, bool counters, cudaStream_t stream,
                               uint32_t block = 0);

@@ -725,7 +725,7 @@ bool effective_sort(const rg_renderer* h) {
 
 uint32_t effective_budget(const rg_renderer* h) {
   if (h->wf_budget) return h->wf_budget;
-  return h->kinds == F_SPHERE ? kDefaultFetchBudgetSpheres : kDefaultFetchBudget;
+  return kDefaultFetchBudget;
 }
 
 void apply_features(rg_renderer* h) {
@@ -1057,9 +1057,9 @@ rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
   out->fetch_budget = effective_budget(h);
   out->bvh_width = effective_bvh_width(h->bvh_width, h->gs, h->form);
   out->shared_stack = h->gs.shared_stack ? h->gs.shared_stack : RG_SHARED_STACK_NONE;
-  out->block = h->mega_block ? h->mega_block : 256u;
+  out->block = h->mega_block ? h->mega_block : kDefaultMegaBlock;
   out->stack_limit = h->gs.stack_limit;
-  out->march_budget = h->march_budget ? h->march_budget : 8u;
+  out->march_budget = h->march_budget ? h->march_budget : kMarchBudgetDefault;
   return RG_OK;
 }
 
@@ -1124,7 +1124,8 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
     e = launch_wavefront(h, fp);
   } else {
     if ((h->flags & RG_FLAG_STAGE_TIMES) && (e = stage_mark(h)) != cudaSuccess) return cuda_fail(h, e, "stage event");
-    e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream, h->mega_block);
+    e = launch_megakernel(h->gs, fp, (h->flags & RG_FLAG_COUNTERS) != 0, h->stream,
+                          h->mega_block ? h->mega_block : kDefaultMegaBlock);
     if (e == cudaSuccess && (h->flags & RG_FLAG_STAGE_TIMES)) e = stage_mark(h);
   }
   if (e != cudaSuccess) { h->frame_current = false; return cuda_fail(h, e, "render launch"); }

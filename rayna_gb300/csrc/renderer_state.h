@@ -114,7 +114,7 @@ struct rg_renderer {
   uint32_t shared_stack = 0;  // requested shared traversal-stack entries: 0 default, RG_SHARED_STACK_NONE, 4, 8, 16
   uint32_t mega_block = 0;    // megakernel threads per block (0: 256)
   uint32_t stack_limit = 0;   // traversal stack entries a ray may use (0: kStackSize)
-  uint32_t march_budget = 0;  // SDF evaluations per lane between refills in the march stages (0: kMarchBudget)
+  uint32_t march_budget = 0;  // SDF evaluations per lane between refills in the march stages (0: kMarchBudgetDefault)
   uint32_t range_first = 0;   // rg_set_sample_range: the frame's first sample
   uint32_t range_count = 0;   //   and its number of samples (0: whole frames)
   uint32_t kinds = 0;         // F_* primitive-kind bits of the scene's kernel variant
@@ -130,11 +130,20 @@ namespace rg {
 // every form measured faster on the binary tree.
 constexpr uint32_t kDefaultBvhWidthWavefront = 2;
 constexpr uint32_t kDefaultBvhWidthMegakernel = 2;
-// Node visits between refills of the persistent traversal kernels: 8, or 6
-// for scenes of spheres only (measured best of 4-16 on the mesh, SDF and
-// sphere workloads).
-constexpr uint32_t kDefaultFetchBudget = 8;
-constexpr uint32_t kDefaultFetchBudgetSpheres = 6;
+// Node visits between refills of the persistent traversal kernels: 6
+// (measured on the fused mesh workload 614 Msamples/s at 6 against 598 at 8
+// and 565 at 12; on the random-spheres workload 1195 at 6, 1100 at 8, 1096 at
+// 4).
+constexpr uint32_t kDefaultFetchBudget = 6;
+// Megakernel threads per block when the tuning leaves it at 0: 128 (the three
+// workloads measured within 1 % of their best at 128: mesh 350 Msamples/s
+// against 353 at 64 and 345 at 256, random spheres 820 / 823 / 798, SDF 177
+// against 173 at 256).
+constexpr uint32_t kDefaultMegaBlock = 128;
+// Distance evaluations per lane between refills in the SDF march stages when
+// the tuning leaves it at 0 (the SDF workload measured 431, 554, 684, 778 and
+// 814 Msamples/s at 2, 4, 8, 16 and 32).
+constexpr uint32_t kMarchBudgetDefault = 32;
 // Default path slots per wave (about 3.6 GB of path state; clamped to the
 // frame). Larger waves keep more rays in flight at the tail of each bounce:
 // 2^25 measured 1.18x 2^23 on the SDF workload and 1.03x on the mesh.

@@ -420,7 +420,7 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   // Raymarched SDFs in the material-sorted form: one k_march stage per SDF
   // after the tree (h->host.nsdf SDFs lead the unbounded list).
   const uint32_t n_march = (F & F_SDF) && sorted ? h->host.nsdf : 0u;
-  const int march_budget = (int)(h->march_budget ? h->march_budget : kMarchBudget);
+  const int march_budget = (int)(h->march_budget ? h->march_budget : kMarchBudgetDefault);
   int march_per_sm = 0;
   if (n_march) {
     if (counters) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&march_per_sm, k_march<F, true>, kWfBlock, 0);

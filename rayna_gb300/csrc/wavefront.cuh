@@ -25,8 +25,6 @@ constexpr int kWfBlock = 256;
 // tuning, rg_tuning.shared_stack, with the same default.)
 constexpr int kSharedStack = 8;
 template <uint32_t F> constexpr int kSharedStackOf = kinds_of(F) == F_TRI ? kSharedStack : 0;
-// SDF evaluations a k_march lane performs between refills of idle lanes.
-constexpr uint32_t kMarchBudget = 8;
 constexpr int kKinds = 6;  // miss, lambertian, metal, dielectric, isotropic, light
 enum : uint32_t { KQ_MISS = 0 };
 constexpr int kPrimMiss = -1;  // rec[2].w: >= 0 BVH primitive, -1 miss, -2 - k SDF k

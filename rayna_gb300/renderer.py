@@ -239,10 +239,10 @@ class Renderer:
         wavefront lane traverses between refills (0 = library default);
         shared_stack: traversal stack entries per thread in shared memory
         (0 = library default, -1 = none, else 4, 8 or 16); block: megakernel
-        threads per block (0 = 256, else 64 or 128); stack_limit: a test knob
+        threads per block (0 = 128, else 64 or 256); stack_limit: a test knob
         capping the traversal stack a ray may use (0 = all 64); march_budget:
         SDF evaluations per lane between refills in the material-sorted
-        wavefront's march stages (0 = 8)."""
+        wavefront's march stages (0 = 32)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
         # the resolved defaults come back from rg_get_tuning; hand the requested knobs back

@@ -66,7 +66,7 @@ def test_tuning_rejects_unknown_stack_and_block_values():
                 r.set_tuning(**bad)
             assert e.value.status == A.RG_INVALID_ARG
         # defaults resolve: 8 shared entries for triangle-only scenes, none otherwise
-        assert r.tuning()["shared_stack"] == -1 and r.tuning()["block"] == 256 and r.tuning()["stack_limit"] == 64
+        assert r.tuning()["shared_stack"] == -1 and r.tuning()["block"] == 128 and r.tuning()["stack_limit"] == 64
 
 
 @pytest.mark.parametrize("form,width", [("megakernel", 2), ("megakernel", 8), ("wavefront", 2), ("wavefront", 8)])
