@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 7u
+#define RG_ABI_VERSION 8u
 
 /* Status codes. 0 is success. */
 typedef enum rg_status {
@@ -401,6 +401,10 @@ typedef struct rg_tuning {
                                  drops the far subtree and the frame reports RG_QUEUE_OVERFLOW; 0 = all 64 */
     uint32_t march_budget;    /* material-sorted wavefront with raymarched SDFs: distance evaluations a lane of a
                                  march stage performs between refills of idle lanes (1-4096); 0 = 32 */
+    uint32_t shade_lanes;     /* wavefront: a warp of a persistent kernel finishes its ready paths (shading in the
+                                 fused bounce kernel, the hit record in the extend stage, the hit normal in a march
+                                 stage) together, once at least this many of its lanes are ready or all of its live
+                                 lanes are (1-32; 1 = each path as soon as it is ready); 0 = 16 */
 } rg_tuning;
 
 #define RG_SHARED_STACK_NONE 0xFFFFFFFFu
@@ -493,7 +497,8 @@ typedef struct rg_batch_tuning {
     uint32_t bvh_width;        /* 2 or 8 as in rg_tuning; 0 = library default (2) */
     uint32_t form;             /* RG_BATCH_WAVEFRONT or RG_BATCH_TILES */
     uint32_t wave_paths;       /* RG_BATCH_WAVEFRONT: path slots per wave; 0 = min(2^25, all paths of a frame) */
-    uint32_t reserved[2];      /* must be 0 */
+    uint32_t shade_lanes;      /* RG_BATCH_WAVEFRONT: as rg_tuning.shade_lanes (1-32); 0 = 16 */
+    uint32_t reserved;         /* must be 0 */
 } rg_batch_tuning;
 
 /* Creates a batch of `n` independent renders (scene, camera, options each,

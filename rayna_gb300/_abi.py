@@ -53,7 +53,7 @@ RG_NO_TRANSFORM = 0xFFFFFFFF
 RG_BATCH_TILES = 1
 RG_SHARED_STACK_NONE = 0xFFFFFFFF
 RG_DEVICE_STACK_OVERFLOW, RG_DEVICE_BAD_INDEX, RG_DEVICE_QUEUE_OVERFLOW = 1, 2, 4
-RG_ABI_VERSION = 7
+RG_ABI_VERSION = 8
 
 
 class rg_material(C.Structure):
@@ -141,7 +141,7 @@ class rg_scene_info(C.Structure):
 class rg_tuning(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("sort_materials", C.c_uint32), ("bvh_width", C.c_uint32),
                 ("fetch_budget", C.c_uint32), ("shared_stack", C.c_uint32), ("block", C.c_uint32),
-                ("stack_limit", C.c_uint32), ("march_budget", C.c_uint32)]
+                ("stack_limit", C.c_uint32), ("march_budget", C.c_uint32), ("shade_lanes", C.c_uint32)]
 
 
 class rg_gradients(C.Structure):
@@ -152,7 +152,7 @@ class rg_gradients(C.Structure):
 class rg_batch_tuning(C.Structure):
     _fields_ = [("block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("rounds_per_item", C.c_uint32),
                 ("bvh_width", C.c_uint32), ("form", C.c_uint32), ("wave_paths", C.c_uint32),
-                ("reserved", C.c_uint32 * 2)]
+                ("shade_lanes", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class rg_hit(C.Structure):

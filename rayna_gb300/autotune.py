@@ -33,15 +33,16 @@ from . import _abi as A
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "rayna_gb300", "tuning_cache.json")
 
 WAVE_PATHS = [1 << 23, 1 << 24, 1 << 25]
-FETCH_BUDGETS = [4, 8, 16]
+FETCH_BUDGETS = [4, 6, 8, 16]
 BVH_WIDTHS = [2, 8]
 SHARED_STACKS = [-1, 8, 16]  # -1: the whole traversal stack in local memory
 MEGA_BLOCKS = [64, 128, 256]
 # Coordinate-descent axes per form, searched in this order.
 MEGA_AXES = [("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS), ("block", MEGA_BLOCKS)]
-MARCH_BUDGETS = [4, 8, 16, 32]
+MARCH_BUDGETS = [8, 16, 32, 64]
+SHADE_LANES = [1, 8, 16, 24]
 WAVE_AXES = [("sort_materials", [False, True]), ("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS),
-             ("fetch_budget", FETCH_BUDGETS), ("wave_paths", WAVE_PATHS)]
+             ("fetch_budget", FETCH_BUDGETS), ("shade_lanes", SHADE_LANES), ("wave_paths", WAVE_PATHS)]
 WAVE_SDF_AXES = WAVE_AXES + [("march_budget", MARCH_BUDGETS)]
 BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 23, 1 << 24, 1 << 25)] +
                 [dict(form="tiles", block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)])
@@ -131,7 +132,8 @@ class Tuner:
             results.append(self._descend(r, "megakernel", MEGA_AXES, start, frames, 1000, timings, opts))
         with Renderer.new_from(scene, camera, opts, 0, form="wavefront", **renderer_kw) as r:
             d = r.tuning()
-            start = {k: d[k] for k in ("sort_materials", "bvh_width", "shared_stack", "fetch_budget", "wave_paths")}
+            start = {k: d[k] for k in ("sort_materials", "bvh_width", "shared_stack", "fetch_budget", "shade_lanes",
+                                       "wave_paths")}
             axes = WAVE_AXES
             if flat.desc.n_sdfs:  # the march stages' refill budget
                 start["march_budget"] = d["march_budget"]

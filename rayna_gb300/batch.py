@@ -66,16 +66,19 @@ class BatchRenderer:
         return sum(o.width * o.height * o.samples for _, _, o in self.items)
 
     def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, rounds_per_item: int = 0, bvh_width: int = 0,
-                   form="wavefront", wave_paths: int = 0):
+                   form="wavefront", wave_paths: int = 0, shade_lanes: int = 0):
         """rg_batch_tuning. form: "wavefront" (shared waves of path slots, the
         default) or "tiles" (a persistent megakernel over (render, tile) work
         items); block / blocks_per_sm / rounds_per_item shape the tile form,
-        wave_paths the wavefront's path slots per wave (0 = library default)."""
+        wave_paths the wavefront's path slots per wave and shade_lanes the
+        ready lanes a warp of its bounce kernel shades together (0 = library
+        defaults)."""
         t = A.rg_batch_tuning()
         t.block, t.blocks_per_sm, t.rounds_per_item = int(block), int(blocks_per_sm), int(rounds_per_item)
         t.bvh_width = int(bvh_width)
         t.form = {"wavefront": A.RG_BATCH_WAVEFRONT, "tiles": A.RG_BATCH_TILES}.get(form, form)
         t.wave_paths = int(wave_paths)
+        t.shade_lanes = int(shade_lanes)
         self._check(self._lib.rg_batch_set_tuning(self._h, C.byref(t)))
 
     def next_seed(self) -> int:

@@ -134,20 +134,21 @@ __global__ void __launch_bounds__(kWfBlock) k_bgenerate(const BatchItemDev* __re
 }
 
 // One bounce of the live paths of every render of the wave: closest hit and
-// shading, persistent with dynamic ray fetch as in the single-render form; a
-// lane reads its render's scene and frame parameters through its chunk.
+// shading, persistent with dynamic ray fetch as in the single-render form
+// (finished lanes shade together, finish_now); a lane reads its render's
+// scene and frame parameters through its chunk.
 template <uint32_t F>
 __global__ void __launch_bounds__(kWfBlock) k_bbounce(const BatchItemDev* __restrict__ items,
                                                       const BatchChunk* __restrict__ chunks, WaveParams wp, PathState s,
                                                       const uint32_t* __restrict__ chunk_of, int cur, int budget,
-                                                      uint32_t* err, unsigned long long* counters) {
+                                                      int shade_lanes, uint32_t* err, unsigned long long* counters) {
   const uint32_t n = clamp_count(s.counts[cur], wp, err);
   const int nxt = cur ^ 1;
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
   Counters cnt;
   uint32_t queries = 0;
-  bool has = false, drained = false;
+  bool has = false, done = false, drained = false;
   uint32_t p = 0, pix = 0, smp = 0, depth = 0, item = 0;
   Ray r;
   C3f beta;
@@ -183,21 +184,26 @@ __global__ void __launch_bounds__(kWfBlock) k_bbounce(const BatchItemDev* __rest
         }
       }
     }
-    if (!__any_sync(0xffffffffu, has)) break;
-    if (has) {
+    const unsigned live = __ballot_sync(0xffffffffu, has);
+    if (!live) break;
+    if (has && !done) {
       const GpuScene& sc = items[item].sc;
       const FrameParams& fp = items[item].fp;
       const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
-      if (trav_run<F, false, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget)) {
-        HitRec h;
-        const bool hit = finish_hit<F, false>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
-        if (shade_path<F>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
-          uint32_t slot = warp_append(s.counts + nxt, true);
-          if (slot < wp.n_paths) s.active[nxt][slot] = p;
-          else atomicOr(err, ERR_QUEUE_OVERFLOW);
-        }
-        has = false;
+      done = trav_run<F, false, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget);
+    }
+    if (finish_now(done, live, shade_lanes)) {
+      const GpuScene& sc = items[item].sc;
+      const FrameParams& fp = items[item].fp;
+      HitRec h;
+      const bool hit = finish_hit<F, false>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
+      if (shade_path<F>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
+        uint32_t slot = warp_append(s.counts + nxt, true);
+        if (slot < wp.n_paths) s.active[nxt][slot] = p;
+        else atomicOr(err, ERR_QUEUE_OVERFLOW);
       }
+      has = false;
+      done = false;
     }
   }
   FrameParams f0;
@@ -352,6 +358,7 @@ cudaError_t launch_batch_wavefront(rg_batch* b) {
   const int bounce_grid = sms * std::max(per_sm, 1);
   const int grid = sms * 8;
   const int budget = (int)kDefaultFetchBudget;
+  const int shade_lanes = (int)(b->tuning.shade_lanes ? b->tuning.shade_lanes : kShadeLanesDefault);
   cudaStream_t st = b->stream;
   cudaError_t e;
   b->launches = 0;
@@ -368,8 +375,8 @@ cudaError_t launch_batch_wavefront(rg_batch* b) {
     for (uint32_t d = 0; d <= w.max_depth; ++d) {
       if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
       if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-      k_bbounce<F><<<bounce_grid, kWfBlock, 0, st>>>(b->d_items, b->d_chunks, wp, s, chunk_of, cur, budget, b->d_err,
-                                                     b->d_counters);
+      k_bbounce<F><<<bounce_grid, kWfBlock, 0, st>>>(b->d_items, b->d_chunks, wp, s, chunk_of, cur, budget,
+                                                     shade_lanes, b->d_err, b->d_counters);
       cur ^= 1;
     }
     const uint32_t acc_blocks = (uint32_t)std::min<size_t>((w.n_pixels * 3 + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
@@ -589,8 +596,8 @@ rg_status rg_batch_last_error(rg_batch_handle b, char* buf, size_t len) {
 
 rg_status rg_batch_set_tuning(rg_batch_handle b, const rg_batch_tuning* t) {
   if (!b || !t) return RG_INVALID_ARG;
-  for (uint32_t r : t->reserved)
-    if (r) return bfail(b, RG_INVALID_ARG, "rg_batch_tuning: reserved fields must be 0");
+  if (t->reserved) return bfail(b, RG_INVALID_ARG, "rg_batch_tuning: reserved field must be 0");
+  if (t->shade_lanes > 32) return bfail(b, RG_INVALID_ARG, "rg_batch_tuning: shade_lanes must be at most 32");
   if (t->block && (t->block % 32 || t->block < 64 || t->block > 512))
     return bfail(b, RG_INVALID_ARG, "block must be a multiple of 32 in [64, 512]");
   if (t->rounds_per_item > 4096) return bfail(b, RG_INVALID_ARG, "rounds_per_item too large");

@@ -115,6 +115,7 @@ struct rg_renderer {
   uint32_t mega_block = 0;    // megakernel threads per block (0: 256)
   uint32_t stack_limit = 0;   // traversal stack entries a ray may use (0: kStackSize)
   uint32_t march_budget = 0;  // SDF evaluations per lane between refills in the march stages (0: kMarchBudgetDefault)
+  uint32_t shade_lanes = 0;   // ready lanes before a persistent wavefront warp finishes them (0: kShadeLanesDefault)
   uint32_t range_first = 0;   // rg_set_sample_range: the frame's first sample
   uint32_t range_count = 0;   //   and its number of samples (0: whole frames)
   uint32_t kinds = 0;         // F_* primitive-kind bits of the scene's kernel variant
@@ -141,9 +142,16 @@ constexpr uint32_t kDefaultFetchBudget = 6;
 // against 173 at 256).
 constexpr uint32_t kDefaultMegaBlock = 128;
 // Distance evaluations per lane between refills in the SDF march stages when
-// the tuning leaves it at 0 (the SDF workload measured 431, 554, 684, 778 and
-// 814 Msamples/s at 2, 4, 8, 16 and 32).
+// the tuning leaves it at 0 (the SDF workload measured 431, 554, 684, 778,
+// 819, 779 and 733 Msamples/s at 2, 4, 8, 16, 32, 64 and 128).
 constexpr uint32_t kMarchBudgetDefault = 32;
+// A warp of a persistent wavefront kernel finishes its ready paths (shading,
+// hit records, SDF hit normals: long code that would otherwise run for one or
+// two lanes at a time) together once this many lanes are ready, or all of its
+// live lanes are. The fused mesh workload measured 610 Msamples/s at 1 (each
+// path finished when ready), 676 at 8, 695 at 16, 653 at 24 and 503 at 32;
+// random spheres 1240 at 1, 1308 at 16, 1320 at 24.
+constexpr uint32_t kShadeLanesDefault = 16;
 // Default path slots per wave (about 3.6 GB of path state; clamped to the
 // frame). Larger waves keep more rays in flight at the tail of each bounce:
 // 2^25 measured 1.18x 2^23 on the SDF workload and 1.03x on the mesh.

@@ -50,19 +50,22 @@ __global__ void __launch_bounds__(kWfBlock) k_generate(FrameParams fp, PathState
 // One bounce of every live path: closest hit and shading in one kernel,
 // persistent with dynamic ray fetch (Aila & Laine 2009, "replacing terminated
 // rays"): a warp keeps 32 paths in flight, traverses for `budget` node visits
-// at a time, and a lane whose traversal has finished shades its path and
-// then takes the next one from the queue (one atomic per warp and refill), so
-// lanes do not idle while the warp's longest ray finishes.
+// at a time, and lanes whose traversal has finished shade their paths and
+// then take the next ones from the queue (one atomic per warp and refill), so
+// lanes do not idle while the warp's longest ray finishes. Finished lanes wait
+// until `shade_lanes` of them (or every live lane) are ready and then shade
+// together: shading is long code, and run for the one or two lanes that finish
+// in a given step it cost more than the wait.
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
-                                                     int budget) {
+                                                     int budget, int shade_lanes) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   const int nxt = cur ^ 1;
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
   Counters cnt;
   uint32_t queries = 0;
-  bool has = false, drained = false;
+  bool has = false, done = false, drained = false;
   uint32_t p = 0, pix = 0, smp = 0, depth = 0;
   Ray r;
   C3f beta;
@@ -95,19 +98,22 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
         }
       }
     }
-    if (!__any_sync(0xffffffffu, has)) break;
-    if (has) {
+    const unsigned live = __ballot_sync(0xffffffffu, has);
+    if (!live) break;
+    if (has && !done) {
       const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
-      if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget)) {
-        HitRec h;
-        const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
-        if (shade_path<F, COUNT>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
-          uint32_t slot = warp_append(s.counts + nxt, true);
-          if (slot < wp.n_paths) s.active[nxt][slot] = p;
-          else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
-        }
-        has = false;
+      done = trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget);
+    }
+    if (finish_now(done, live, shade_lanes)) {
+      HitRec h;
+      const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
+      if (shade_path<F, COUNT>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
+        uint32_t slot = warp_append(s.counts + nxt, true);
+        if (slot < wp.n_paths) s.active[nxt][slot] = p;
+        else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
       }
+      has = false;
+      done = false;
     }
   }
   flush_wave_counters<COUNT>(fp, cnt, queries);
@@ -118,7 +124,8 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
 // (Aila & Laine 2009, "replacing terminated rays"): a warp keeps 32 rays in
 // flight, traverses for `budget` node visits at a time, and lanes whose ray
 // has finished take the next rays from the queue (one atomic per warp), so
-// lanes do not idle while the warp's longest ray finishes.
+// lanes do not idle while the warp's longest ray finishes. Finished lanes
+// record their hits together (finish_now), as the fused kernel shades.
 
 template <uint32_t F, bool COUNT>
 __device__ __forceinline__ void record_hit(const GpuScene& sc, const FrameParams& fp, const PathState& s,
@@ -199,13 +206,13 @@ __device__ __forceinline__ void finish_march(const GpuScene& sc, const FramePara
 
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
-                                                     int budget, int defer) {
+                                                     int budget, int defer, int shade_lanes) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
   Counters cnt;
   uint32_t queries = 0;
-  bool has = false, drained = false;
+  bool has = false, done = false, drained = false;
   uint32_t p = 0, pix = 0, smp = 0, depth = 0;
   Ray r;
   Traversal t;
@@ -236,23 +243,26 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
         }
       }
     }
-    if (!__any_sync(0xffffffffu, has)) break;
-    if (has) {
+    const unsigned live = __ballot_sync(0xffffffffu, has);
+    if (!live) break;
+    if (has && !done) {
       const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
-      if (trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget)) {
-        HitRec h;
-        if ((F & F_SDF) && defer) {
-          if (finish_hit<F & ~(F_SDF | F_PLANE), false>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt)) {
-            s.rec[3 * (size_t)p + 1].w = h.t;
-            s.rec[3 * (size_t)p + 2].w = __int_as_float(h.prim);
-            if ((F & F_EXT) && sc.prim_xform) s.aux[p].x = h.tl;
-          }
-        } else {
-          const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
-          record_hit<F, COUNT>(sc, fp, s, wp, p, hit, h);
+      done = trav_run<F, COUNT, true>(t, stack, sc, r, 1e-3f, ctx, cnt, fp.err, budget);
+    }
+    if (finish_now(done, live, shade_lanes)) {
+      HitRec h;
+      if ((F & F_SDF) && defer) {
+        if (finish_hit<F & ~(F_SDF | F_PLANE), false>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt)) {
+          s.rec[3 * (size_t)p + 1].w = h.t;
+          s.rec[3 * (size_t)p + 2].w = __int_as_float(h.prim);
+          if ((F & F_EXT) && sc.prim_xform) s.aux[p].x = h.tl;
         }
-        has = false;
+      } else {
+        const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
+        record_hit<F, COUNT>(sc, fp, s, wp, p, hit, h);
       }
+      has = false;
+      done = false;
     }
   }
   flush_wave_counters<COUNT>(fp, cnt, queries);
@@ -266,23 +276,26 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
 // dynamic fetch: every lane marches the same function, `budget` evaluations
 // at a time, and lanes whose march has ended take the next path (one atomic
 // per warp), so a long march does not hold idle lanes. Paths whose segment
-// cannot reach the function's bound sphere end at once. The last stage also
-// tests the infinite planes and appends each path to its material kind's
-// queue.
+// cannot reach the function's bound sphere end at once. A warp finishes its
+// ended marches together (the hit normal, six distance evaluations; the last
+// stage's planes and queue append) once `shade_lanes` of them, or all of its
+// live lanes, have ended. The last stage also tests the infinite planes and
+// appends each path to its material kind's queue.
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
-                                                    uint32_t k, int last, int budget) {
+                                                    uint32_t k, int last, int budget, int shade_lanes) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
   const GpuSdf f = sc.sdfs[k];
   const float start = 1e-3f, end = 3.402823466e38f;
   Counters cnt;
-  bool has = false, drained = false;
+  bool has = false, done = false, drained = false;
   uint32_t p = 0;
   Ray r;
   float best = 0.0f;
   bool any = false;
+  int st = kMarchOn;  // a finished march's outcome, kept until the warp finishes it
   SdfMarch m;
   for (;;) {
     // Refill idle lanes until every lane has a march or the queue is drained:
@@ -312,23 +325,26 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
         }
       }
     }
-    if (!__any_sync(0xffffffffu, has)) break;  // drained, and nothing left to march
-    if (has) {
-      int st = kMarchOn;
+    const unsigned live = __ballot_sync(0xffffffffu, has);
+    if (!live) break;  // drained, and nothing left to march
+    if (has && !done) {
+      st = kMarchOn;
       for (int e = 0; e < budget && st == kMarchOn; ++e)
         st = sdf_march_step<COUNT>(f, r, start, end, any ? best : end, !any, m, cnt.sdf_steps, cnt.sdf_iters);
-      if (st != kMarchOn) {
-        if (st == kMarchHit) {
-          SdfHit sh;
-          sdf_march_hit<COUNT>(f, m, sh, cnt.sdf_steps);
-          s.rec[3 * (size_t)p + 1].w = sh.t;
-          s.rec[3 * (size_t)p + 2].w = __int_as_float(-2 - (int)k);
-          s.aux[p] = make_float4(sh.n.x, sh.n.y, sh.n.z,
-                                 __uint_as_float((sh.front ? 0x80000000u : 0u) | (sh.side & 0x3FFFFFFFu)));
-        }
-        if (last) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
-        has = false;
+      done = st != kMarchOn;
+    }
+    if (finish_now(done, live, shade_lanes)) {
+      if (st == kMarchHit) {
+        SdfHit sh;
+        sdf_march_hit<COUNT>(f, m, sh, cnt.sdf_steps);
+        s.rec[3 * (size_t)p + 1].w = sh.t;
+        s.rec[3 * (size_t)p + 2].w = __int_as_float(-2 - (int)k);
+        s.aux[p] = make_float4(sh.n.x, sh.n.y, sh.n.z,
+                               __uint_as_float((sh.front ? 0x80000000u : 0u) | (sh.side & 0x3FFFFFFFu)));
       }
+      if (last) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
+      has = false;
+      done = false;
     }
   }
   flush_wave_counters<COUNT>(fp, cnt, 0);
@@ -405,6 +421,7 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   const bool counters = (h->flags & RG_FLAG_COUNTERS) != 0;
   const bool sorted = effective_sort(h);
   const int budget = (int)effective_budget(h);
+  const int shade_lanes = (int)(h->shade_lanes ? h->shade_lanes : kShadeLanesDefault);
   const int grid = sm_count(h->device) * 8;
   // The persistent traversal kernels run as many blocks as are resident at
   // once, each with its threads' shared stack entries.
@@ -447,21 +464,25 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
       if (sorted) {
         if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
-        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, n_march > 0);
-        else k_extend<F, false><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, n_march > 0);
+        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, n_march > 0,
+                                                               shade_lanes);
+        else k_extend<F, false><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, n_march > 0,
+                                                                shade_lanes);
         // the SDFs in list order, each over every path of the bounce
         for (uint32_t k = 0; k < n_march; ++k) {
           if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
           const int last = k + 1 == n_march;
-          if (counters) k_march<F, true><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, last, march_budget);
-          else k_march<F, false><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, last, march_budget);
+          if (counters) k_march<F, true><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, last, march_budget,
+                                                            shade_lanes);
+          else k_march<F, false><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, last, march_budget,
+                                                             shade_lanes);
         }
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
         k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
       } else {
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
-        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget);
-        else k_bounce<F, false><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget);
+        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, shade_lanes);
+        else k_bounce<F, false><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, shade_lanes);
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
       }
       cur ^= 1;

@@ -230,7 +230,8 @@ class Renderer:
 
     def set_tuning(self, wave_paths: int | None = None, sort_materials: bool | None = None,
                    bvh_width: int | None = None, fetch_budget: int | None = None, shared_stack: int | None = None,
-                   block: int | None = None, stack_limit: int | None = None, march_budget: int | None = None):
+                   block: int | None = None, stack_limit: int | None = None, march_budget: int | None = None,
+                   shade_lanes: int | None = None):
         """Launch knobs (rg_tuning); None leaves a knob as it is. wave_paths:
         wavefront path slots per wave (0 = library default); sort_materials:
         wavefront shading in material-kind order (True) or one fused bounce
@@ -242,7 +243,8 @@ class Renderer:
         threads per block (0 = 128, else 64 or 256); stack_limit: a test knob
         capping the traversal stack a ray may use (0 = all 64); march_budget:
         SDF evaluations per lane between refills in the material-sorted
-        wavefront's march stages (0 = 32)."""
+        wavefront's march stages (0 = 32); shade_lanes: ready lanes a warp
+        of a persistent wavefront kernel finishes together (1-32, 0 = 16)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
         # the resolved defaults come back from rg_get_tuning; hand the requested knobs back
@@ -263,6 +265,8 @@ class Renderer:
             t.stack_limit = int(stack_limit)
         if march_budget is not None:
             t.march_budget = int(march_budget)
+        if shade_lanes is not None:
+            t.shade_lanes = int(shade_lanes)
         self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
         self._stack_knobs = (t.shared_stack, t.block, t.stack_limit)
 
@@ -273,7 +277,8 @@ class Renderer:
         return {"wave_paths": t.wave_paths, "sort_materials": t.sort_materials == 1, "bvh_width": t.bvh_width,
                 "fetch_budget": t.fetch_budget,
                 "shared_stack": -1 if t.shared_stack == A.RG_SHARED_STACK_NONE else t.shared_stack,
-                "block": t.block, "stack_limit": t.stack_limit, "march_budget": t.march_budget}
+                "block": t.block, "stack_limit": t.stack_limit, "march_budget": t.march_budget,
+                "shade_lanes": t.shade_lanes}
 
     def set_sample_range(self, first: int, count: int):
         """Frames trace samples [first, first + count) of each pixel's

@@ -5,7 +5,7 @@
 
 use std::os::raw::{c_char, c_void};
 
-pub const RG_ABI_VERSION: u32 = 7;
+pub const RG_ABI_VERSION: u32 = 8;
 
 pub type rg_status = i32;
 pub const RG_OK: rg_status = 0;
@@ -277,6 +277,7 @@ pub struct rg_tuning {
     pub block: u32,
     pub stack_limit: u32,
     pub march_budget: u32,
+    pub shade_lanes: u32,
 }
 
 #[repr(C)]
@@ -288,7 +289,8 @@ pub struct rg_batch_tuning {
     pub bvh_width: u32,
     pub form: u32,
     pub wave_paths: u32,
-    pub reserved: [u32; 2],
+    pub shade_lanes: u32,
+    pub reserved: u32,
 }
 
 #[repr(C)]

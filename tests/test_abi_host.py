@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
     for s in syms:
         assert hasattr(lib, s), s
     assert set(syms) == set(A.SIGNATURES), "ctypes signatures must cover the header exactly"
-    assert lib.rg_abi_version() == A.RG_ABI_VERSION == 7
+    assert lib.rg_abi_version() == A.RG_ABI_VERSION == 8
 
 
 @pytest.mark.parametrize("exact", [False, True])
@@ -42,7 +42,7 @@ def test_both_arithmetic_builds_load_and_export_the_same_symbols(exact):
     lib = A.load_library(exact=exact)
     for s in declared_symbols():
         assert hasattr(lib, s), s
-    assert lib.rg_abi_version() == 7
+    assert lib.rg_abi_version() == 8
     assert A.load_library(exact=exact) is lib
 
 

@@ -44,6 +44,8 @@ def test_tuning_pass_picks_a_measured_candidate(tmp_path):
     mega = [x for x in entry["timings"] if x["form"] == "megakernel"]
     assert {x["block"] for x in mega} == set(autotune.MEGA_BLOCKS)
     assert {x["shared_stack"] for x in mega} == set(autotune.SHARED_STACKS)
+    wave = [x for x in entry["timings"] if x["form"] == "wavefront"]
+    assert {x["shade_lanes"] for x in wave} == set(autotune.SHADE_LANES)
     with Renderer.tuned(scene, cam, opts, tuner=t) as r:
         assert r.form == cfg["form"]
         r.render()

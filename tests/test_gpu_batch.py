@@ -45,7 +45,8 @@ def test_batch_tuning_does_not_change_images():
     # are cut into runs spanning several waves, on either tree
     for tune in [dict(), dict(form="tiles"), dict(form="tiles", block=128, rounds_per_item=1),
                  dict(form="tiles", block=64, blocks_per_sm=1, rounds_per_item=16),
-                 dict(wave_paths=50_000), dict(wave_paths=50_000, bvh_width=8)]:
+                 dict(wave_paths=50_000), dict(wave_paths=50_000, bvh_width=8),
+                 dict(shade_lanes=1), dict(wave_paths=50_000, shade_lanes=32)]:
         with BatchRenderer(items) as b:
             b.set_tuning(**tune)
             b.render(seed=5)
@@ -61,6 +62,9 @@ def test_batch_rejects_launch_shapes_it_cannot_run():
     with BatchRenderer(small_batch()[:2]) as b:
         with pytest.raises(RaynaError) as e:
             b.set_tuning(block=1024)
+        assert e.value.status == 1
+        with pytest.raises(RaynaError) as e:
+            b.set_tuning(shade_lanes=33)
         assert e.value.status == 1
         try:  # 512 threads fit only if the kernel uses <= 128 registers
             b.set_tuning(block=512)

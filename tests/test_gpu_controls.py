@@ -1,8 +1,9 @@
 """Launch knobs, failure statuses and sample-range sharding on the GPU,
 through the C ABI.
 
-* Stack placement (shared entries per thread) and the megakernel's block
-  size change only the time: every setting renders the same image.
+* Stack placement (shared entries per thread), the megakernel's block
+  size and the ready lanes a wavefront warp finishes together change only
+  the time: every setting renders the same image.
 * Device errors are statuses: a traversal stack capped below what a ray
   needs (the rg_tuning.stack_limit test knob) makes the frame return
   RG_QUEUE_OVERFLOW promptly, and the next normal frame returns RG_OK (the
@@ -43,7 +44,9 @@ def test_stack_placement_and_block_do_not_change_images(case):
                         else small(presets.random_spheres, 64, 36, 8, 12))
     imgs = {}
     for form, knobs in [("megakernel", dict(shared_stack=sh, block=b)) for sh in (-1, 4, 8, 16) for b in (64, 128, 256)] + \
-                       [("wavefront", dict(shared_stack=sh, sort_materials=so)) for sh in (-1, 8, 16) for so in (False, True)]:
+                       [("wavefront", dict(shared_stack=sh, sort_materials=so)) for sh in (-1, 8, 16) for so in (False, True)] + \
+                       [("wavefront", dict(shared_stack=8, sort_materials=so, shade_lanes=sl))
+                        for so in (False, True) for sl in (1, 7, 32)]:
         with Renderer.new_from(scene, cam, opts, 0, form=form) as r:
             r.set_tuning(**knobs)
             t = r.tuning()
@@ -61,12 +64,13 @@ def test_stack_placement_and_block_do_not_change_images(case):
 def test_tuning_rejects_unknown_stack_and_block_values():
     scene, cam, opts = small(presets.random_spheres, 8, 8, 1, 2)
     with Renderer.new_from(scene, cam, opts, 0) as r:
-        for bad in (dict(shared_stack=3), dict(block=96), dict(stack_limit=65)):
+        for bad in (dict(shared_stack=3), dict(block=96), dict(stack_limit=65), dict(shade_lanes=33)):
             with pytest.raises(RaynaError) as e:
                 r.set_tuning(**bad)
             assert e.value.status == A.RG_INVALID_ARG
         # defaults resolve: 8 shared entries for triangle-only scenes, none otherwise
         assert r.tuning()["shared_stack"] == -1 and r.tuning()["block"] == 128 and r.tuning()["stack_limit"] == 64
+        assert r.tuning()["shade_lanes"] == 16
 
 
 @pytest.mark.parametrize("form,width", [("megakernel", 2), ("megakernel", 8), ("wavefront", 2), ("wavefront", 8)])
@@ -173,18 +177,19 @@ def test_sample_range_matches_the_oracle_path_by_path(form):
 @pytest.mark.parametrize("exact", [True, False])
 def test_march_stages_render_the_megakernel_image(exact):
     """The material-sorted wavefront marches each SDF in its own persistent
-    stage, `march_budget` evaluations per lane between refills; every budget,
-    and the megakernel's one-call march, give the same image bits."""
+    stage, `march_budget` evaluations per lane between refills, and finishes
+    `shade_lanes` ended marches of a warp together; every setting, and the
+    megakernel's one-call march, give the same image bits."""
     scene, cam, opts = small(presets.sdf_volumes, 64, 36, 8, 12, n_spheres=20)
     with Renderer.new_from(scene, cam, opts, 0, form="megakernel", exact=exact) as r:
         ref = r.render(seed=23).img
-    for budget in (1, 4, 8, 64):
+    for budget, lanes in [(1, 16), (4, 16), (8, 16), (64, 16), (8, 1), (8, 32), (32, 24)]:
         with Renderer.new_from(scene, cam, opts, 0, form="wavefront", exact=exact) as r:
-            r.set_tuning(sort_materials=True, march_budget=budget)
-            assert r.tuning()["march_budget"] == budget
+            r.set_tuning(sort_materials=True, march_budget=budget, shade_lanes=lanes)
+            assert r.tuning()["march_budget"] == budget and r.tuning()["shade_lanes"] == lanes
             out = r.render(seed=23)
             assert out.stats.error_flags == 0
-            np.testing.assert_array_equal(out.img, ref, err_msg=f"march budget {budget}")
+            np.testing.assert_array_equal(out.img, ref, err_msg=f"march budget {budget}, shade lanes {lanes}")
     with Renderer.new_from(scene, cam, opts, 0) as r:
         with pytest.raises(RaynaError):
             r.set_tuning(march_budget=5000)

@@ -26,7 +26,7 @@ def test_rust_sys_declares_every_header_function():
     text = open(SYS).read()
     fns = set(re.findall(r"pub fn (rg_\w+)\(", text))
     assert fns == set(declared_symbols())
-    assert "pub const RG_ABI_VERSION: u32 = 7;" in text
+    assert "pub const RG_ABI_VERSION: u32 = 8;" in text
 
 
 def test_rust_sys_struct_fields_follow_the_ctypes_mirror():
