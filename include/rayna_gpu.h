@@ -497,7 +497,7 @@ typedef struct rg_batch_tuning {
     uint32_t bvh_width;        /* 2 or 8 as in rg_tuning; 0 = library default (2) */
     uint32_t form;             /* RG_BATCH_WAVEFRONT or RG_BATCH_TILES */
     uint32_t wave_paths;       /* RG_BATCH_WAVEFRONT: path slots per wave; 0 = min(2^25, all paths of a frame) */
-    uint32_t shade_lanes;      /* RG_BATCH_WAVEFRONT: as rg_tuning.shade_lanes (1-32); 0 = 16 */
+    uint32_t shade_lanes;      /* RG_BATCH_WAVEFRONT: as rg_tuning.shade_lanes (1-32); 0 = 24 */
     uint32_t reserved;         /* must be 0 */
 } rg_batch_tuning;
 

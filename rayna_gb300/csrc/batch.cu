@@ -358,7 +358,7 @@ cudaError_t launch_batch_wavefront(rg_batch* b) {
   const int bounce_grid = sms * std::max(per_sm, 1);
   const int grid = sms * 8;
   const int budget = (int)kDefaultFetchBudget;
-  const int shade_lanes = (int)(b->tuning.shade_lanes ? b->tuning.shade_lanes : kShadeLanesDefault);
+  const int shade_lanes = (int)(b->tuning.shade_lanes ? b->tuning.shade_lanes : kBatchShadeLanesDefault);
   cudaStream_t st = b->stream;
   cudaError_t e;
   b->launches = 0;

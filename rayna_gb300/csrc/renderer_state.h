@@ -150,8 +150,12 @@ constexpr uint32_t kMarchBudgetDefault = 32;
 // two lanes at a time) together once this many lanes are ready, or all of its
 // live lanes are. The fused mesh workload measured 610 Msamples/s at 1 (each
 // path finished when ready), 676 at 8, 695 at 16, 653 at 24 and 503 at 32;
-// random spheres 1240 at 1, 1308 at 16, 1320 at 24.
+// random spheres 1237 at 1, 1305 at 16, 1313 at 24; the SDF workload (extend
+// and march stages) 822 at 1, 835 at 16, 817 at 24.
 constexpr uint32_t kShadeLanesDefault = 16;
+// The same for the batched wavefront's bounce kernel: the 64-scene batch
+// measured 1917 Msamples/s at 1, 2282 at 16 and 2331 at 24.
+constexpr uint32_t kBatchShadeLanesDefault = 24;
 // Default path slots per wave (about 3.6 GB of path state; clamped to the
 // frame). Larger waves keep more rays in flight at the tail of each bounce:
 // 2^25 measured 1.18x 2^23 on the SDF workload and 1.03x on the mesh.
