@@ -549,7 +549,7 @@ def run_gpu(args, rank, world):
             line["workloads"][name] = summarise(name, r2, b2, hbm, sm_count)
             line["gpu_launches"] += sum(v["launches_per_frame"] * v["steps"] for v in r2.values() if "error" not in v)
     if world == 1 and not args.no_adjoint:
-        line["adjoint"] = run_adjoint(iters=20, stream=stream)  # host-timed: a median over 20 iterations
+        line["adjoint"] = run_adjoint(stream=stream)
     if world == 1 and args.batch_scale > 0:
         line["batch"] = run_batch(args.batch_scale, max(2, args.steps), stream=stream)
     if world == 1 and not args.no_cpu_baseline:

@@ -226,6 +226,34 @@ __device__ __forceinline__ void replay_backward(const GpuScene& sc, const AdjPar
   }
 }
 
+// The block's gradient sink: shared-memory sums (zeroed here; the whole
+// block calls this) when `block_sums`, else global memory.
+__device__ __forceinline__ GradSink block_sink(const AdjParams& ap, float* grad_sh) {
+  GradSink gs{ap.g_albedo, ap.g_emission, ap.g_density};
+  if (ap.block_sums) {
+    const uint32_t n_grad = 6 * ap.n_mat + ap.n_vol;
+    for (uint32_t i = threadIdx.x; i < n_grad; i += blockDim.x) grad_sh[i] = 0.0f;
+    gs = GradSink{grad_sh, grad_sh + 3 * ap.n_mat, grad_sh + 6 * ap.n_mat};
+    __syncthreads();
+  }
+  return gs;
+}
+
+// Adds the block's shared-memory sums to global memory (the whole block calls this).
+__device__ __forceinline__ void flush_block_sums(const AdjParams& ap, const float* grad_sh) {
+  if (!ap.block_sums) return;
+  __syncthreads();
+  const uint32_t n_grad = 6 * ap.n_mat + ap.n_vol;
+  for (uint32_t i = threadIdx.x; i < n_grad; i += blockDim.x) {
+    const float v = grad_sh[i];
+    if (v != 0.0f) {
+      float* dst = i < 3 * ap.n_mat ? ap.g_albedo + i
+                 : (i < 6 * ap.n_mat ? ap.g_emission + (i - 3 * ap.n_mat) : ap.g_density + (i - 6 * ap.n_mat));
+      atomicAdd(dst, v);
+    }
+  }
+}
+
 // One path of pixel (x, y), sample s: traced again with its random streams,
 // then differentiated; (d0, d1, d2) is the pixel's dLoss/dI over its samples.
 template <uint32_t F>
@@ -246,24 +274,17 @@ __device__ __forceinline__ void replay_path(AdjStack& stack, const GpuScene& sc,
   replay_backward<F>(sc, ap, gs, P, d0, d1, d2);
 }
 
-// The replay: one thread per pixel-sample, a warp taking whole pixels as the
-// megakernel does (its lanes then end their backward passes together, so
-// the warp-aggregated atomics group every lane with the same material).
-// With `block_sums` the gradients go to the block's shared memory and each
-// block adds its sums to global memory once, at the end. (A persistent
-// dynamic-fetch form of this kernel measured slower: 7.4 against 5.9 ms per
-// iteration on the adjoint workload, since lanes finishing at different times
-// aggregate their atomics far less.)
+// The replay's grid form (RG_ADJ_PERSISTENT=0): one thread per pixel-sample,
+// a warp taking whole pixels as the megakernel does (its lanes then end their
+// backward passes together, so the warp-aggregated atomics group every lane
+// with the same material). With `block_sums` the gradients go to the block's
+// shared memory and each block adds its sums to global memory once, at the
+// end. It measured 6.06 ms per iteration of the adjoint workload against the
+// persistent form's 4.29.
 template <uint32_t F>
 __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_pix) {
   extern __shared__ float grad_sh[];  // albedo, emission (n_mat x 3 each), density (n_vol), with block_sums
-  const uint32_t n_grad = 6 * ap.n_mat + ap.n_vol;
-  GradSink gs{ap.g_albedo, ap.g_emission, ap.g_density};
-  if (ap.block_sums) {
-    for (uint32_t i = threadIdx.x; i < n_grad; i += blockDim.x) grad_sh[i] = 0.0f;
-    gs = GradSink{grad_sh, grad_sh + 3 * ap.n_mat, grad_sh + 6 * ap.n_mat};
-    __syncthreads();
-  }
+  const GradSink gs = block_sink(ap, grad_sh);
   __shared__ uint2 stack_sh[kAdjSharedStack * kAdjBlock];
   uint2 stack_loc[kTravStack - kAdjSharedStack];
   AdjStack stack{stack_sh + threadIdx.x, stack_loc};
@@ -290,17 +311,80 @@ __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams f
       for (uint32_t s = lane; s < spp; s += 32) replay_path<F>(stack, sc, fp, ap, gs, x, y, s, d0, d1, d2);
     }
   }
-  if (ap.block_sums) {
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n_grad; i += blockDim.x) {
-      const float v = grad_sh[i];
-      if (v != 0.0f) {
-        float* dst = i < 3 * ap.n_mat ? ap.g_albedo + i
-                   : (i < 6 * ap.n_mat ? ap.g_emission + (i - 3 * ap.n_mat) : ap.g_density + (i - 6 * ap.n_mat));
-        atomicAdd(dst, v);
+  flush_block_sums(ap, grad_sh);
+}
+
+// The replay (default form) as a persistent kernel with dynamic fetch, as the forward's
+// wavefront traversal kernels run: each lane holds one path (samples taken
+// in pixel order from one counter, one atomic per warp and refill), traverses
+// `budget` node visits at a time, and the lanes whose segment has ended are
+// finished together once `shade_lanes` of them (or all of the warp's live
+// lanes) are ready: the vertex is recorded and the path scattered, or, at
+// its end, differentiated, so the backward passes and their warp-aggregated
+// atomics run on many lanes at once. Gradients are summed per block in
+// shared memory when they fit.
+template <uint32_t F>
+__global__ void __launch_bounds__(kAdjBlock) k_replay_persistent(GpuScene sc, FrameParams fp, AdjParams ap,
+                                                                 uint32_t n_items, uint32_t* counter, int budget,
+                                                                 int shade_lanes) {
+  extern __shared__ float grad_sh[];
+  const GradSink gs = block_sink(ap, grad_sh);
+  __shared__ uint2 stack_sh[kAdjSharedStack * kAdjBlock];
+  uint2 stack_loc[kTravStack - kAdjSharedStack];
+  AdjStack stack{stack_sh + threadIdx.x, stack_loc};
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t spp = fp.spp;
+  const float inv = 1.0f / (float)spp;
+  bool has = false, done = false, drained = false;
+  uint32_t pix = 0, smp = 0, depth = 0;
+  float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f;
+  Ray ray;
+  Traversal t;
+  ReplayPath P;
+  Counters cnt;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !has);
+    if (idle && !drained) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(counter, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= n_items) drained = true;
+      if (!has) {
+        const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (i < n_items) {
+          pix = i / spp;
+          smp = i % spp;
+          const uint32_t x = pix % fp.width, y = pix / fp.width;
+          const size_t idx = ((size_t)x * fp.height + y) * 3;
+          d0 = ap.adjoint[idx] * inv;
+          d1 = ap.adjoint[idx + 1] * inv;
+          d2 = ap.adjoint[idx + 2] * inv;
+          ray = camera_ray(fp, x, y, smp, RngCtx{fp.seed_lo, fp.seed_hi, pix, smp, 0, nullptr});
+          replay_begin(P);
+          depth = 0;
+          trav_init<F>(t, sc, ray, 3.402823466e38f);
+          has = true;
+        }
       }
     }
+    const unsigned live = __ballot_sync(0xffffffffu, has);
+    if (!live) break;
+    const RngCtx ctx{fp.seed_lo, fp.seed_hi, pix, smp, depth, nullptr};
+    if (has && !done) done = trav_run<F, false, true>(t, stack, sc, ray, 1e-3f, ctx, cnt, fp.err, budget);
+    if (finish_now(done, live, shade_lanes)) {
+      HitRec h;
+      const bool hit = finish_hit<F, false>(sc, ray, 1e-3f, 3.402823466e38f, t, h, cnt);
+      if (replay_segment<F>(sc, fp, ap, P, ray, ctx, depth, hit, h)) {
+        ++depth;
+        trav_init<F>(t, sc, ray, 3.402823466e38f);
+      } else {
+        replay_backward<F>(sc, ap, gs, P, d0, d1, d2);
+        has = false;
+      }
+      done = false;
+    }
   }
+  flush_block_sums(ap, grad_sh);
 }
 
 // L2 loss against a target: adjoint = 2 (I - T), loss = sum (I - T)^2.
@@ -315,14 +399,32 @@ __global__ void k_l2_adjoint(const float* image, const float* target, float* adj
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc);
 }
 
+// RG_ADJ_PERSISTENT=0 at build time selects the one-thread-per-sample grid
+// form of the replay instead of the persistent one.
+#ifndef RG_ADJ_PERSISTENT
+#define RG_ADJ_PERSISTENT 1
+#endif
+
+// `counter`: a zeroed device word (the persistent form's fetch counter).
 template <uint32_t F>
-void launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, cudaStream_t st) {
+cudaError_t launch_replay(const GpuScene& sc, const FrameParams& fp, const AdjParams& ap, uint32_t* counter,
+                          int budget, int shade_lanes, int device, cudaStream_t st) {
   const uint32_t n_pix = fp.width * fp.height;
-  const uint32_t ppw = fp.spp <= 32 ? 32 / fp.spp : 1u;
-  const uint32_t warps = (n_pix + ppw - 1) / ppw;
-  const uint32_t blocks = (warps + kAdjBlock / 32 - 1) / (kAdjBlock / 32);
   const size_t smem = ap.block_sums ? (6 * (size_t)ap.n_mat + ap.n_vol) * sizeof(float) : 0;
-  k_replay<F><<<blocks, kAdjBlock, smem, st>>>(sc, fp, ap, n_pix);
+  if (RG_ADJ_PERSISTENT) {
+    int per_sm = 0, sms = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_replay_persistent<F>, kAdjBlock, smem);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return e;
+    const uint32_t blocks = (uint32_t)std::max(sms, 1) * (uint32_t)std::max(per_sm, 1);
+    k_replay_persistent<F><<<blocks, kAdjBlock, smem, st>>>(sc, fp, ap, n_pix * fp.spp, counter, budget, shade_lanes);
+  } else {
+    const uint32_t ppw = fp.spp <= 32 ? 32 / fp.spp : 1u;
+    const uint32_t warps = (n_pix + ppw - 1) / ppw;
+    const uint32_t blocks = (warps + kAdjBlock / 32 - 1) / (kAdjBlock / 32);
+    k_replay<F><<<blocks, kAdjBlock, smem, st>>>(sc, fp, ap, n_pix);
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace
@@ -393,11 +495,13 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
   }
   AdjParams ap{d_adjoint, d_galb, d_gem, d_gden, n_vol, n_mat,
                RG_ADJ_BLOCK_SUMS && 6 * n_mat + n_vol <= kAdjSharedGrads ? 1 : 0};
-  dispatch_features(h->gs.features, [&](auto f) {
-    launch_replay<decltype(f)::value>(h->gs, fp, ap, st);
-    return 0;
+  uint32_t* d_counter = (uint32_t*)((char*)d_loss + 64);  // zeroed with the scratch above
+  const int budget = (int)effective_budget(h);
+  const int shade_lanes = (int)(h->shade_lanes ? h->shade_lanes : kShadeLanesDefault);
+  e = dispatch_features(h->gs.features, [&](auto f) {
+    return launch_replay<decltype(f)::value>(h->gs, fp, ap, d_counter, budget, shade_lanes, h->device, st);
   });
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e);
+  if (e != cudaSuccess) return cuda_err(e);
   double loss = 0.0;
   if (out->albedo && (e = cudaMemcpyAsync(out->albedo, d_galb, (size_t)n_mat * 3 * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     return cuda_err(e);

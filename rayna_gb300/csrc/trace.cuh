@@ -941,6 +941,16 @@ __device__ __forceinline__ bool run_wide(Traversal& t, Stack& stack, const GpuSc
   }
 }
 
+// Whether this lane finishes its ready path now: a warp of a persistent
+// kernel finishes its ready lanes together once at least `min_ready` of them
+// are ready or all of its live lanes (`live`, a subset of which is ready)
+// are, so the finishing code runs on many lanes at once. Called by the whole
+// warp.
+__device__ __forceinline__ bool finish_now(bool ready, unsigned live, int min_ready) {
+  const unsigned r = __ballot_sync(0xffffffffu, ready);
+  return ready && ((int)__popc(r) >= min_ready || r == live);
+}
+
 // Runs a traversal to completion (BOUNDED false) or for at most `budget`
 // node visits (BOUNDED true); returns true once it is complete.
 template <uint32_t F, bool COUNT, bool BOUNDED, class Stack>

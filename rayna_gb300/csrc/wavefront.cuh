@@ -54,16 +54,6 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
   return base + __popc(ballot & ((1u << lane) - 1u));
 }
 
-// Whether this lane finishes its ready path now: a warp of a persistent
-// kernel finishes its ready lanes together once at least `min_ready` of them
-// are ready or all of its live lanes (`live`, a subset of which is ready)
-// are, so the finishing code runs on many lanes at once. Called by the whole
-// warp.
-__device__ __forceinline__ bool finish_now(bool ready, unsigned live, int min_ready) {
-  const unsigned r = __ballot_sync(0xffffffffu, ready);
-  return ready && ((int)__popc(r) >= min_ready || r == live);
-}
-
 __device__ __forceinline__ void store_path(const PathState& s, uint32_t p, V3 o, uint32_t depth, V3 d, C3f beta) {
   s.rec[3 * (size_t)p] = make_float4(o.x, o.y, o.z, __uint_as_float(depth));
   s.rec[3 * (size_t)p + 1] = make_float4(d.x, d.y, d.z, 0.0f);
