@@ -124,7 +124,9 @@ struct GpuSdf {
   uint32_t material;
   uint32_t prim_id;
   float bound_radius;  // outside this radius (and moving away) no hit is possible
-  float pad[3];
+  float inv_scale;     // Mandelbulb: 1 / scale when the scale is a power of two (the division is then an exact
+                       // product), else 0
+  float pad[2];
 };
 
 // Kernel variant bits (GpuScene::features): the primitive kinds a kernel is

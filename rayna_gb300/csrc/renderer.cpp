@@ -495,6 +495,12 @@ rg_status build_scene_host(rg_renderer* h, const rg_scene_desc& d, HostScene& hs
     else r0 = 1.5 * s.params[2];
     double margin = std::max(1e-3 * std::max(r0, 1.0), 16.0 * (double)s.epsilon);
     g.bound_radius = (float)((r0 + margin) * (1.0 + 1e-4));
+    if (s.kind == RG_SDF_MANDELBULB) {
+      int ex = 0;
+      const float m = std::frexp(s.params[2], &ex);
+      // scale = 2^(ex-1) with both it and its reciprocal normal
+      if (m == 0.5f && ex - 1 >= -125 && ex - 1 <= 125) g.inv_scale = std::ldexp(1.0f, 1 - ex);
+    }
     hs.sdfs.push_back(g);
   }
   // Parallelograms and cylinders: bounded, stored after the volumes in the

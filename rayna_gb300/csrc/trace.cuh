@@ -292,7 +292,10 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long l
   // enclosing sphere of radius kBulbInner is used (a lower bound).
   unsigned long long* counted = iter_count;
   float sc = s.p2;
-  V3 z0 = v3(q.x / sc, q.y / sc, q.z / sc);
+  // q / scale; for a power-of-two scale the product with its reciprocal is
+  // the same correctly rounded quotient, without three divisions
+  V3 z0 = s.inv_scale != 0.0f ? v3(__fmul_rn(q.x, s.inv_scale), __fmul_rn(q.y, s.inv_scale), __fmul_rn(q.z, s.inv_scale))
+                              : v3(q.x / sc, q.y / sc, q.z / sc);
   float rq = length3(z0);
   if (rq > kBulbOuter) return __fmul_rn(rq - kBulbInner, sc);
   float power = s.p0;

@@ -161,10 +161,6 @@ __device__ __forceinline__ void record_hit(const GpuScene& sc, const FrameParams
   }
 }
 
-// `defer`: the scene's raymarched SDFs (and infinite planes) are left to the
-// k_march stages; this kernel stores the tree's closest hit in the path
-// record (distance, primitive, mesh-space distance of a transformed hit) and
-// appends nothing to the kind queues.
 // After the last SDF's march: the infinite planes (tested after the SDFs, in
 // list order, replacing the hit only when strictly closer) and the path's
 // material-kind queue.
@@ -204,9 +200,16 @@ __device__ __forceinline__ void finish_march(const GpuScene& sc, const FramePara
   record_hit<F, COUNT>(sc, fp, s, wp, p, any, h);
 }
 
+// With `n_march` > 0 the scene's first n_march unbounded objects are
+// raymarched SDFs, left to the k_march stages: this kernel stores the tree's
+// closest hit in the path record (distance, primitive, mesh-space distance of
+// a transformed hit); a path whose segment up to that hit can reach one of
+// the SDFs' bound spheres goes to the march queue (the next bounce's active
+// array, free until shading), and any other path is finished here as the last
+// march stage would finish it (finish_march): no SDF can replace its hit.
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
-                                                     int budget, int defer, int shade_lanes) {
+                                                     int budget, int n_march, int shade_lanes) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
@@ -251,11 +254,24 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
     }
     if (finish_now(done, live, shade_lanes)) {
       HitRec h;
-      if ((F & F_SDF) && defer) {
-        if (finish_hit<F & ~(F_SDF | F_PLANE), false>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt)) {
+      if ((F & F_SDF) && n_march > 0) {
+        const bool tree_hit = finish_hit<F & ~(F_SDF | F_PLANE), false>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
+        if (tree_hit) {
           s.rec[3 * (size_t)p + 1].w = h.t;
           s.rec[3 * (size_t)p + 2].w = __int_as_float(h.prim);
           if ((F & F_EXT) && sc.prim_xform) s.aux[p].x = h.tl;
+        }
+        // The march stages only shorten the segment, so one that cannot reach
+        // an SDF's bound sphere now never can.
+        bool reach = false;
+        for (int k = 0; k < n_march && !reach; ++k)
+          reach = sdf_bound_reachable(sc.sdfs[k], r, 1e-3f, tree_hit ? h.t : 3.402823466e38f);
+        if (reach) {
+          const uint32_t slot = warp_append(s.counts + kMarchCounter, true);
+          if (slot < wp.n_paths) s.active[cur ^ 1][slot] = p;
+          else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+        } else {
+          finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
         }
       } else {
         const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
@@ -269,8 +285,9 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
 }
 
 // Material-sorted variant with raymarched SDFs, stage 1b: the march of SDF k
-// (the unbounded list's k-th object) for every path of the bounce, after the
-// tree (k_extend with `defer`) and the SDFs before k. It replaces the path's
+// (the unbounded list's k-th object) for every path of the march queue (the
+// paths of the bounce that k_extend found able to reach some SDF), after the
+// tree and the SDFs before k. It replaces the path's
 // hit when strictly closer (or when nothing was hit), as ObjectList's loop
 // over unbounded objects does (object/list.rs:112-129). Persistent with
 // dynamic fetch: every lane marches the same function, `budget` evaluations
@@ -284,7 +301,8 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
                                                     uint32_t k, int last, int budget, int shade_lanes) {
-  const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
+  const uint32_t n = clamp_count(s.counts[kMarchCounter], wp, fp.err);
+  const uint32_t* queue = s.active[cur ^ 1];
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
   const GpuSdf f = sc.sdfs[k];
@@ -312,7 +330,7 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
       if (!has) {
         const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
         if (i < n) {
-          p = s.active[cur][i];
+          p = queue[i];
           const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1];
           r.o = v3(r0.x, r0.y, r0.z);
           r.d = v3(r1.x, r1.y, r1.z);
@@ -462,11 +480,12 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
       if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
       if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
       if (sorted) {
-        if ((e = cudaMemsetAsync(s.counts + 2, 0, kKinds * sizeof(uint32_t), st)) != cudaSuccess) return e;
+        // the kind counts, the fetch counter and the march queue's count
+        if ((e = cudaMemsetAsync(s.counts + 2, 0, (kKinds + 2) * sizeof(uint32_t), st)) != cudaSuccess) return e;
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
-        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, n_march > 0,
+        if (counters) k_extend<F, true><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, (int)n_march,
                                                                shade_lanes);
-        else k_extend<F, false><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, n_march > 0,
+        else k_extend<F, false><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, (int)n_march,
                                                                 shade_lanes);
         // the SDFs in list order, each over every path of the bounce
         for (uint32_t k = 0; k < n_march; ++k) {

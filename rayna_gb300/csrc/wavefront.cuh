@@ -35,9 +35,11 @@ struct PathState {
   float *sr, *sg, *sb;  // per-slot sample radiance
   uint32_t* active[2];
   uint32_t* kindq;      // kKinds x capacity
-  uint32_t* counts;     // [0], [1]: active counts; [2 .. 2+kKinds): kind counts; [kFetchCounter]: the traversal kernels' fetch counter
+  uint32_t* counts;     // [0], [1]: active counts; [2 .. 2+kKinds): kind counts; [kFetchCounter]: the traversal kernels'
+                        // fetch counter; [kMarchCounter]: the march queue's count
 };
 constexpr int kFetchCounter = 2 + kKinds;
+constexpr int kMarchCounter = kFetchCounter + 1;
 
 struct WaveParams {
   uint32_t first_pixel, n_pixels, n_paths, capacity;
