@@ -386,7 +386,8 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene);
  * reference has no device; these are what the autotuner sets). Zero fields
  * select the library defaults. Changing them does not change the image. */
 typedef struct rg_tuning {
-    uint32_t wave_paths;      /* wavefront: path slots per wave (whole pixels per wave); 0 = 2^25 */
+    uint32_t wave_paths;      /* wavefront: path slots per wave (whole pixels per wave; 108 bytes of device memory
+                                 each); 0 = 2^27, clamped to the frame */
     uint32_t sort_materials;  /* wavefront: 1 = separate extend and shade stages, shading in material-kind order;
                                  2 = one fused bounce kernel; 0 = library default (fused for scenes of spheres
                                  only, sorted otherwise) */
@@ -496,7 +497,7 @@ typedef struct rg_batch_tuning {
     uint32_t rounds_per_item;  /* RG_BATCH_TILES: warp rounds of pixels per work item; 0 = 4 */
     uint32_t bvh_width;        /* 2 or 8 as in rg_tuning; 0 = library default (2) */
     uint32_t form;             /* RG_BATCH_WAVEFRONT or RG_BATCH_TILES */
-    uint32_t wave_paths;       /* RG_BATCH_WAVEFRONT: path slots per wave; 0 = min(2^25, all paths of a frame) */
+    uint32_t wave_paths;       /* RG_BATCH_WAVEFRONT: path slots per wave; 0 = min(2^27, all paths of a frame) */
     uint32_t shade_lanes;      /* RG_BATCH_WAVEFRONT: as rg_tuning.shade_lanes (1-32); 0 = 24 */
     uint32_t reserved;         /* must be 0 */
 } rg_batch_tuning;

@@ -32,7 +32,7 @@ from . import _abi as A
 
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "rayna_gb300", "tuning_cache.json")
 
-WAVE_PATHS = [1 << 23, 1 << 24, 1 << 25]
+WAVE_PATHS = [1 << 24, 1 << 25, 1 << 26, 1 << 27]
 FETCH_BUDGETS = [4, 6, 8, 16]
 BVH_WIDTHS = [2, 8]
 SHARED_STACKS = [-1, 8, 16]  # -1: the whole traversal stack in local memory
@@ -44,7 +44,7 @@ SHADE_LANES = [1, 8, 16, 24]
 WAVE_AXES = [("sort_materials", [False, True]), ("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS),
              ("fetch_budget", FETCH_BUDGETS), ("shade_lanes", SHADE_LANES), ("wave_paths", WAVE_PATHS)]
 WAVE_SDF_AXES = WAVE_AXES + [("march_budget", MARCH_BUDGETS)]
-BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 23, 1 << 24, 1 << 25)] +
+BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 25, 1 << 26, 1 << 27)] +
                 [dict(form="tiles", block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)])
 
 

@@ -156,10 +156,14 @@ constexpr uint32_t kShadeLanesDefault = 16;
 // The same for the batched wavefront's bounce kernel: the 64-scene batch
 // measured 1917 Msamples/s at 1, 2282 at 16 and 2331 at 24.
 constexpr uint32_t kBatchShadeLanesDefault = 24;
-// Default path slots per wave (about 3.6 GB of path state; clamped to the
-// frame). Larger waves keep more rays in flight at the tail of each bounce:
-// 2^25 measured 1.18x 2^23 on the SDF workload and 1.03x on the mesh.
-constexpr size_t kDefaultWavePaths = size_t(1) << 25;
+// Default path slots per wave (at most about 14.5 GB of path state at 108
+// bytes per slot; clamped to the frame). Every wave pays each bounce's tail,
+// the few longest paths (a long march, a deep traversal) that hold the stage
+// while most of the GPU idles, so frames run best as few waves as memory
+// allows: the SDF workload (118 M paths) measured 814, 891 and 937
+// Msamples/s at 2^25, 2^26 and 2^27 slots, the mesh (67 M) 699 and 710 at
+// 2^25 and 2^26, the 64-scene batch 2354, 2410 and 2432.
+constexpr size_t kDefaultWavePaths = size_t(1) << 27;
 
 // Defined in renderer.cpp
 // RG_FLAG_STAGE_TIMES: records the next event of the frame's traversal timing

@@ -28,6 +28,12 @@
 #include "renderer_state.h"
 #include "wavefront.cuh"
 
+// RG_MARCH_ROUTE=0 at build time sends every path of a bounce through the
+// march stages (no finishing in the extend stage).
+#ifndef RG_MARCH_ROUTE
+#define RG_MARCH_ROUTE 1
+#endif
+
 namespace rg {
 
 namespace {
@@ -263,7 +269,7 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
         }
         // The march stages only shorten the segment, so one that cannot reach
         // an SDF's bound sphere now never can.
-        bool reach = false;
+        bool reach = !RG_MARCH_ROUTE;
         for (int k = 0; k < n_march && !reach; ++k)
           reach = sdf_bound_reachable(sc.sdfs[k], r, 1e-3f, tree_hit ? h.t : 3.402823466e38f);
         if (reach) {
