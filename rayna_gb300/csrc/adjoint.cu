@@ -279,8 +279,8 @@ __device__ __forceinline__ void replay_path(AdjStack& stack, const GpuScene& sc,
 // backward passes together, so the warp-aggregated atomics group every lane
 // with the same material). With `block_sums` the gradients go to the block's
 // shared memory and each block adds its sums to global memory once, at the
-// end. It measured 6.06 ms per iteration of the adjoint workload against the
-// persistent form's 4.29.
+// end. It measured 4.54 ms per iteration of the adjoint workload against the
+// persistent form's 3.60.
 template <uint32_t F>
 __global__ void __launch_bounds__(kAdjBlock) k_replay(GpuScene sc, FrameParams fp, AdjParams ap, uint32_t n_pix) {
   extern __shared__ float grad_sh[];  // albedo, emission (n_mat x 3 each), density (n_vol), with block_sums
@@ -399,6 +399,12 @@ __global__ void k_l2_adjoint(const float* image, const float* target, float* adj
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc);
 }
 
+// RG_ADJ_KIND_VARIANTS=0 at build time replays spheres with media in the
+// general kernel variant.
+#ifndef RG_ADJ_KIND_VARIANTS
+#define RG_ADJ_KIND_VARIANTS 1
+#endif
+
 // RG_ADJ_PERSISTENT=0 at build time selects the one-thread-per-sample grid
 // form of the replay instead of the persistent one.
 #ifndef RG_ADJ_PERSISTENT
@@ -498,9 +504,15 @@ rg_status backward_device(rg_renderer* h, uint64_t seed, const float* adjoint, c
   uint32_t* d_counter = (uint32_t*)((char*)d_loss + 64);  // zeroed with the scratch above
   const int budget = (int)effective_budget(h);
   const int shade_lanes = (int)(h->shade_lanes ? h->shade_lanes : kShadeLanesDefault);
-  e = dispatch_features(h->gs.features, [&](auto f) {
-    return launch_replay<decltype(f)::value>(h->gs, fp, ap, d_counter, budget, shade_lanes, h->device, st);
-  });
+  // Spheres with media (the differentiable workloads' scenes) have a replay
+  // of their own: the general variant's code for every other kind made the
+  // persistent kernel stall on instruction fetch.
+  if (RG_ADJ_KIND_VARIANTS && h->have == (F_SPHERE | F_VOL) && !(h->gs.features & F_WIDE))
+    e = launch_replay<F_SPHERE | F_VOL>(h->gs, fp, ap, d_counter, budget, shade_lanes, h->device, st);
+  else
+    e = dispatch_features(h->gs.features, [&](auto f) {
+      return launch_replay<decltype(f)::value>(h->gs, fp, ap, d_counter, budget, shade_lanes, h->device, st);
+    });
   if (e != cudaSuccess) return cuda_err(e);
   double loss = 0.0;
   if (out->albedo && (e = cudaMemcpyAsync(out->albedo, d_galb, (size_t)n_mat * 3 * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess)

@@ -686,6 +686,7 @@ rg_status upload_scene(rg_renderer* h, const HostScene& hs) {
                   (hs.nsdf ? F_SDF : 0) | (hs.nq ? F_QUAD : 0) | (hs.nc ? F_CYLINDER : 0) | (hs.npl ? F_PLANE : 0) |
                   ((hs.textured || !hs.prim_xform.empty()) ? F_EXT : 0);
   h->kinds = have == F_TRI ? F_TRI : (have == F_SPHERE ? F_SPHERE : ((have & F_EXT) ? F_ANY : F_ALL));
+  h->have = have;
   apply_features(h);
   return RG_OK;
 }
@@ -967,6 +968,7 @@ rg_status rg_set_scene(rg_handle h, const rg_scene_desc* scene) {
     h->host = HostScene{};
     h->have_scene = false;
     h->kinds = F_ALL;
+    h->have = F_ALL;
     apply_features(h);
     h->frame_current = false;
     return st;

@@ -119,6 +119,7 @@ struct rg_renderer {
   uint32_t range_first = 0;   // rg_set_sample_range: the frame's first sample
   uint32_t range_count = 0;   //   and its number of samples (0: whole frames)
   uint32_t kinds = 0;         // F_* primitive-kind bits of the scene's kernel variant
+  uint32_t have = 255u;       // F_* bits of the kinds the scene holds (F_EXT with transforms or textures); F_ALL
 
   void* d_adj = nullptr;      // adjoint scratch (image, adjoint image, gradients)
   size_t adj_bytes = 0;
