@@ -67,6 +67,8 @@ struct WavefrontState {
   size_t capacity = 0;
   void* arena = nullptr;
   size_t arena_bytes = 0;
+  void* marchq = nullptr;  // per-SDF march queues (SDFs x capacity u32)
+  size_t marchq_bytes = 0;
 };
 
 }  // namespace rg

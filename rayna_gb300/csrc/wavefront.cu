@@ -28,12 +28,6 @@
 #include "renderer_state.h"
 #include "wavefront.cuh"
 
-// RG_MARCH_ROUTE=0 at build time sends every path of a bounce through the
-// march stages (no finishing in the extend stage).
-#ifndef RG_MARCH_ROUTE
-#define RG_MARCH_ROUTE 1
-#endif
-
 namespace rg {
 
 namespace {
@@ -206,12 +200,49 @@ __device__ __forceinline__ void finish_march(const GpuScene& sc, const FramePara
   record_hit<F, COUNT>(sc, fp, s, wp, p, any, h);
 }
 
+// Appends path p to the march queue of SDF `k` (per-SDF queues) or to the
+// one march queue (k >= 0 then only says "some SDF"); k < 0 appends nothing.
+// Called by the lanes that are finishing together; every lane passes its k.
+__device__ __forceinline__ void march_append(const FrameParams& fp, const PathState& s, const WaveParams& wp, int cur,
+                                             int n_march, uint32_t p, int k) {
+  if (!s.marchq) {
+    const bool mine = k >= 0;
+    if (__any_sync(__activemask(), mine)) {
+      const uint32_t slot = warp_append(s.counts + kMarchCounter, mine);
+      if (mine) {
+        if (slot < wp.n_paths) s.active[cur ^ 1][slot] = p;
+        else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+      }
+    }
+    return;
+  }
+  for (int j = 0; j < n_march; ++j) {
+    const bool mine = k == j;
+    if (__any_sync(__activemask(), mine)) {
+      const uint32_t slot = warp_append(s.counts + kMarchQueueCount0 + j, mine);
+      if (mine) {
+        if (slot < wp.n_paths) s.marchq[(size_t)j * wp.capacity + slot] = p;
+        else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+      }
+    }
+  }
+}
+
+// The first SDF from `k0` on whose bound sphere the segment [start, lim] can
+// reach, or -1.
+__device__ __forceinline__ int next_reachable(const GpuScene& sc, int k0, int n_march, const Ray& r, float start,
+                                              float lim) {
+  for (int k = k0; k < n_march; ++k)
+    if (sdf_bound_reachable(sc.sdfs[k], r, start, lim)) return k;
+  return -1;
+}
+
 // With `n_march` > 0 the scene's first n_march unbounded objects are
 // raymarched SDFs, left to the k_march stages: this kernel stores the tree's
 // closest hit in the path record (distance, primitive, mesh-space distance of
 // a transformed hit); a path whose segment up to that hit can reach one of
-// the SDFs' bound spheres goes to the march queue (the next bounce's active
-// array, free until shading), and any other path is finished here as the last
+// the SDFs' bound spheres goes to the march queue of the first such SDF (or
+// to the one march queue), and any other path is finished here as the last
 // march stage would finish it (finish_march): no SDF can replace its hit.
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
@@ -269,16 +300,9 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
         }
         // The march stages only shorten the segment, so one that cannot reach
         // an SDF's bound sphere now never can.
-        bool reach = !RG_MARCH_ROUTE;
-        for (int k = 0; k < n_march && !reach; ++k)
-          reach = sdf_bound_reachable(sc.sdfs[k], r, 1e-3f, tree_hit ? h.t : 3.402823466e38f);
-        if (reach) {
-          const uint32_t slot = warp_append(s.counts + kMarchCounter, true);
-          if (slot < wp.n_paths) s.active[cur ^ 1][slot] = p;
-          else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
-        } else {
-          finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
-        }
+        const int first = next_reachable(sc, 0, n_march, r, 1e-3f, tree_hit ? h.t : 3.402823466e38f);
+        march_append(fp, s, wp, cur, n_march, p, first);
+        if (first < 0) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
       } else {
         const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
         record_hit<F, COUNT>(sc, fp, s, wp, p, hit, h);
@@ -290,10 +314,29 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
   flush_wave_counters<COUNT>(fp, cnt, queries);
 }
 
+// After path p's march of SDF k (or its rejection at fetch): with per-SDF
+// queues, on to the queue of the next SDF its segment [start, lim] can reach,
+// or finished when there is none; with one march queue, finished by the last
+// stage. `lim`: the distance the remaining SDFs must beat.
+template <uint32_t F, bool COUNT>
+__device__ __forceinline__ void pass_on(const GpuScene& sc, const FrameParams& fp, const PathState& s,
+                                        const WaveParams& wp, int cur, int k, int n_march, uint32_t p, const Ray& r,
+                                        float lim, Counters& cnt) {
+  if (!s.marchq) {
+    if (k + 1 == n_march) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
+    return;
+  }
+  const int nk = next_reachable(sc, k + 1, n_march, r, 1e-3f, lim);
+  march_append(fp, s, wp, cur, n_march, p, nk);
+  if (nk < 0) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
+}
+
 // Material-sorted variant with raymarched SDFs, stage 1b: the march of SDF k
-// (the unbounded list's k-th object) for every path of the march queue (the
-// paths of the bounce that k_extend found able to reach some SDF), after the
-// tree and the SDFs before k. It replaces the path's
+// (the unbounded list's k-th object) for every path of its march queue (the
+// paths whose segment, after the tree and the SDFs before k, can reach its
+// bound sphere; with one march queue for every stage, all paths that can
+// reach some SDF). After its march a path goes on to the queue of the next
+// SDF it can reach, or is finished (infinite planes, material-kind queue). It replaces the path's
 // hit when strictly closer (or when nothing was hit), as ObjectList's loop
 // over unbounded objects does (object/list.rs:112-129). Persistent with
 // dynamic fetch: every lane marches the same function, `budget` evaluations
@@ -306,9 +349,9 @@ __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp
 // appends each path to its material kind's queue.
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
-                                                    uint32_t k, int last, int budget, int shade_lanes) {
-  const uint32_t n = clamp_count(s.counts[kMarchCounter], wp, fp.err);
-  const uint32_t* queue = s.active[cur ^ 1];
+                                                    uint32_t k, int n_march, int budget, int shade_lanes) {
+  const uint32_t n = clamp_count(s.counts[s.marchq ? kMarchQueueCount0 + k : kMarchCounter], wp, fp.err);
+  const uint32_t* queue = s.marchq ? s.marchq + (size_t)k * wp.capacity : s.active[cur ^ 1];
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
   const GpuSdf f = sc.sdfs[k];
@@ -344,8 +387,10 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
           best = r1.w;
           has = true;
           sdf_march_begin(r, start, m);
-          if (!sdf_bound_reachable(f, r, start, any ? best : end)) has = false;
-          if (!has && last) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
+          if (!sdf_bound_reachable(f, r, start, any ? best : end)) {
+            has = false;
+            pass_on<F, COUNT>(sc, fp, s, wp, cur, (int)k, n_march, p, r, any ? best : end, cnt);
+          }
         }
       }
     }
@@ -366,7 +411,7 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
         s.aux[p] = make_float4(sh.n.x, sh.n.y, sh.n.z,
                                __uint_as_float((sh.front ? 0x80000000u : 0u) | (sh.side & 0x3FFFFFFFu)));
       }
-      if (last) finish_march<F, COUNT>(sc, fp, s, wp, p, r, cnt);
+      pass_on<F, COUNT>(sc, fp, s, wp, cur, (int)k, n_march, p, r, st == kMarchHit ? m.total : (any ? best : end), cnt);
       has = false;
       done = false;
     }
@@ -488,19 +533,20 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
       if (sorted) {
         // the kind counts, the fetch counter and the march queue's count
         if ((e = cudaMemsetAsync(s.counts + 2, 0, (kKinds + 2) * sizeof(uint32_t), st)) != cudaSuccess) return e;
+        if (s.marchq && (e = cudaMemsetAsync(s.counts + kMarchQueueCount0, 0, n_march * sizeof(uint32_t), st)) != cudaSuccess)
+          return e;
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
         if (counters) k_extend<F, true><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, (int)n_march,
                                                                shade_lanes);
         else k_extend<F, false><<<ext_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, (int)n_march,
                                                                 shade_lanes);
-        // the SDFs in list order, each over every path of the bounce
+        // the SDFs in list order, each over its march queue
         for (uint32_t k = 0; k < n_march; ++k) {
           if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
-          const int last = k + 1 == n_march;
-          if (counters) k_march<F, true><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, last, march_budget,
-                                                            shade_lanes);
-          else k_march<F, false><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, last, march_budget,
-                                                             shade_lanes);
+          if (counters) k_march<F, true><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, (int)n_march,
+                                                                        march_budget, shade_lanes);
+          else k_march<F, false><<<march_grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur, k, (int)n_march,
+                                                                 march_budget, shade_lanes);
         }
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
         k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
@@ -538,8 +584,7 @@ cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp) {
   size_t cap = pix_per_wave * spp;
   if (cap > 0xFFFFFFFFull) return cudaErrorInvalidValue;
   if (h->wf.capacity < cap) {
-    if (h->wf.arena) cudaFree(h->wf.arena);
-    h->wf = WavefrontState{};
+    free_extra(h);
     cudaError_t e = cudaMalloc(&h->wf.arena, arena_bytes(cap));
     if (e != cudaSuccess) return e;
     h->wf.capacity = cap;
@@ -547,6 +592,21 @@ cudaError_t launch_wavefront(rg_renderer* h, const FrameParams& fp) {
   }
   PathState s;
   carve((char*)h->wf.arena, h->wf.capacity, s);
+  // Per-SDF march queues for the material-sorted form of scenes with
+  // raymarched SDFs (without them every stage reads one march queue).
+  const uint32_t n_march = effective_sort(h) ? h->host.nsdf : 0u;
+  if (n_march > 0 && n_march <= (uint32_t)kMaxRoutedSdfs) {
+    const size_t need = (size_t)n_march * h->wf.capacity * sizeof(uint32_t);
+    if (h->wf.marchq_bytes < need) {
+      if (h->wf.marchq) cudaFree(h->wf.marchq);
+      h->wf.marchq = nullptr;
+      h->wf.marchq_bytes = 0;
+      cudaError_t e = cudaMalloc(&h->wf.marchq, need);
+      if (e != cudaSuccess) return e;
+      h->wf.marchq_bytes = need;
+    }
+    s.marchq = (uint32_t*)h->wf.marchq;
+  }
   return run_frame(h, fp, s, h->wf.capacity, pix_per_wave, (h->flags & RG_FLAG_STAGE_TIMES) != 0);
 }
 
@@ -640,6 +700,7 @@ namespace rg {
 
 void free_extra(rg_renderer* h) {
   if (h->wf.arena) cudaFree(h->wf.arena);
+  if (h->wf.marchq) cudaFree(h->wf.marchq);
   h->wf = WavefrontState{};
 }
 

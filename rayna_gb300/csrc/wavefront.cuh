@@ -35,11 +35,15 @@ struct PathState {
   float *sr, *sg, *sb;  // per-slot sample radiance
   uint32_t* active[2];
   uint32_t* kindq;      // kKinds x capacity
+  uint32_t* marchq;     // per-SDF march queues (n_march x capacity, counts at kMarchQueueCount0 + k), or null: one
+                        // march queue (the next bounce's active array) for every stage
   uint32_t* counts;     // [0], [1]: active counts; [2 .. 2+kKinds): kind counts; [kFetchCounter]: the traversal kernels'
                         // fetch counter; [kMarchCounter]: the march queue's count
 };
 constexpr int kFetchCounter = 2 + kKinds;
 constexpr int kMarchCounter = kFetchCounter + 1;
+constexpr int kMarchQueueCount0 = 16;  // counts[16 + k]: SDF k's march queue
+constexpr int kMaxRoutedSdfs = 48;     // SDFs that get queues of their own (the counts array holds 64 words)
 
 struct WaveParams {
   uint32_t first_pixel, n_pixels, n_paths, capacity;
@@ -218,6 +222,7 @@ inline size_t carve(char* arena, size_t cap, PathState& s) {
   s.active[0] = (uint32_t*)take(cap * kSlotArrayBytes[k++]);
   s.active[1] = (uint32_t*)take(cap * kSlotArrayBytes[k++]);
   s.kindq = (uint32_t*)take(cap * kSlotArrayBytes[k++]);
+  s.marchq = nullptr;
   s.counts = (uint32_t*)take(kCountsBytes);
   return used;
 }

@@ -48,6 +48,29 @@ def test_static_scratch_matches_rg_render_on_two_calls():
             np.testing.assert_array_equal(got, expected[k])
 
 
+def test_static_scratch_sdf_scene_matches_rg_render():
+    """Scenes with raymarched SDFs: rg_render gives each SDF's march stage a
+    queue of its own (allocated with the path state); the allocation-free
+    entry, which allocates nothing, sends every path that can reach some SDF
+    through each stage. Both give the same image bits."""
+    torch = pytest.importorskip("torch")
+    scene, cam, _ = presets.sdf_volumes(n_spheres=20)
+    opts = RenderOpts(width=64, height=36, samples=8, ray_depth=12)
+    with Renderer.new_from(scene, cam, opts, 0, form="wavefront") as ref:
+        expected = ref.render(seed=77).img.copy()
+    with Renderer.new_from(scene, cam, opts, 0, form="wavefront") as r:
+        lib, h = r._lib, r.handle
+        n = opts.width * opts.height * 3
+        accum = torch.zeros(n, dtype=torch.float32, device="cuda")
+        out = torch.empty(n, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        A.check(lib, h, lib.rg_render_static_scratch(h, 77, C.c_void_p(accum.data_ptr()), 1, C.c_void_p(out.data_ptr())))
+        stats = A.rg_render_stats()
+        A.check(lib, h, lib.rg_sync_stats(h, C.byref(stats)))
+        assert stats.error_flags == 0
+        np.testing.assert_array_equal(out.cpu().numpy().reshape(opts.width, opts.height, 3), expected)
+
+
 def test_static_scratch_frame_stats_with_stage_times():
     """With RG_FLAG_STAGE_TIMES the regular entry times its traversal
     launches; the allocation-free entry does not (its events would be created
