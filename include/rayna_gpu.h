@@ -401,7 +401,7 @@ typedef struct rg_tuning {
     uint32_t stack_limit;     /* test knob: traversal stack entries a ray may use (1-64); a ray that needs more
                                  drops the far subtree and the frame reports RG_QUEUE_OVERFLOW; 0 = all 64 */
     uint32_t march_budget;    /* material-sorted wavefront with raymarched SDFs: distance evaluations a lane of a
-                                 march stage performs between refills of idle lanes (1-4096); 0 = 32 */
+                                 march stage performs between refills of idle lanes (1-4096); 0 = 16 */
     uint32_t shade_lanes;     /* wavefront: a warp of a persistent kernel finishes its ready paths (shading in the
                                  fused bounce kernel, the hit record in the extend stage, the hit normal in a march
                                  stage) together, once at least this many of its lanes are ready or all of its live

@@ -145,9 +145,11 @@ constexpr uint32_t kDefaultFetchBudget = 6;
 // against 173 at 256).
 constexpr uint32_t kDefaultMegaBlock = 128;
 // Distance evaluations per lane between refills in the SDF march stages when
-// the tuning leaves it at 0 (the SDF workload measured 431, 554, 684, 778,
-// 819, 779 and 733 Msamples/s at 2, 4, 8, 16, 32, 64 and 128).
-constexpr uint32_t kMarchBudgetDefault = 32;
+// the tuning leaves it at 0. With per-SDF march queues (few paths rejected at
+// fetch, so refills are cheap) the SDF workload measured 1005, 1010, 1009,
+// 1009 and 994 Msamples/s at 8, 12, 16, 24 and 32; with one queue for every
+// stage it had peaked at 32 (819, against 778 at 16 and 779 at 64).
+constexpr uint32_t kMarchBudgetDefault = 16;
 // A warp of a persistent wavefront kernel finishes its ready paths (shading,
 // hit records, SDF hit normals: long code that would otherwise run for one or
 // two lanes at a time) together once this many lanes are ready, or all of its

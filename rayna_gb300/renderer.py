@@ -243,7 +243,7 @@ class Renderer:
         threads per block (0 = 128, else 64 or 256); stack_limit: a test knob
         capping the traversal stack a ray may use (0 = all 64); march_budget:
         SDF evaluations per lane between refills in the material-sorted
-        wavefront's march stages (0 = 32); shade_lanes: ready lanes a warp
+        wavefront's march stages (0 = 16); shade_lanes: ready lanes a warp
         of a persistent wavefront kernel finishes together (1-32, 0 = 16)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
