@@ -143,6 +143,7 @@ __global__ void __launch_bounds__(kWfBlock) k_bbounce(const BatchItemDev* __rest
                                                       const uint32_t* __restrict__ chunk_of, int cur, int budget,
                                                       int shade_lanes, uint32_t* err, unsigned long long* counters) {
   const uint32_t n = clamp_count(s.counts[cur], wp, err);
+  if (warp_unneeded(n)) return;
   const int nxt = cur ^ 1;
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;

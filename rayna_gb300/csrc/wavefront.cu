@@ -60,6 +60,7 @@ template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
                                                      int budget, int shade_lanes) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
+  if (warp_unneeded(n)) return;
   const int nxt = cur ^ 1;
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
@@ -248,6 +249,7 @@ template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_extend(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
                                                      int budget, int n_march, int shade_lanes) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
+  if (warp_unneeded(n)) return;
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
   Counters cnt;
@@ -351,6 +353,7 @@ template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
                                                     uint32_t k, int n_march, int budget, int shade_lanes) {
   const uint32_t n = clamp_count(s.counts[s.marchq ? kMarchQueueCount0 + k : kMarchCounter], wp, fp.err);
+  if (warp_unneeded(n)) return;
   const uint32_t* queue = s.marchq ? s.marchq + (size_t)k * wp.capacity : s.active[cur ^ 1];
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;

@@ -70,6 +70,15 @@ __device__ __forceinline__ void finish_path(const PathState& s, uint32_t p, C3f 
   s.sr[p] = L.r; s.sg[p] = L.g; s.sb[p] = L.b;
 }
 
+// Whether this warp of a persistent kernel has nothing to do: only the first
+// ceil(n / 32) warps of the grid take paths from a queue of n, so that a
+// short queue (the tail bounces) is not fetched from by every resident warp
+// (thousands of atomics on one counter) just to find it empty.
+__device__ __forceinline__ bool warp_unneeded(uint32_t n) {
+  const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  return (uint64_t)gwarp * 32u >= n;
+}
+
 __device__ __forceinline__ uint32_t clamp_count(uint32_t n, const WaveParams& wp, uint32_t* err) {
   if (n > wp.n_paths) {  // never expected: record and clamp instead of reading past the queue
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_QUEUE_OVERFLOW);
