@@ -141,7 +141,8 @@ class rg_scene_info(C.Structure):
 class rg_tuning(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("sort_materials", C.c_uint32), ("bvh_width", C.c_uint32),
                 ("fetch_budget", C.c_uint32), ("shared_stack", C.c_uint32), ("block", C.c_uint32),
-                ("stack_limit", C.c_uint32), ("march_budget", C.c_uint32), ("shade_lanes", C.c_uint32)]
+                ("stack_limit", C.c_uint32), ("march_budget", C.c_uint32), ("shade_lanes", C.c_uint32),
+                ("tail_paths", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class rg_gradients(C.Structure):

@@ -1035,6 +1035,7 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   if (!h || !t) return fail(h, RG_INVALID_ARG, "rg_set_tuning: NULL argument");
   if (t->march_budget > 4096) return fail(h, RG_INVALID_ARG, "rg_tuning: march_budget must be at most 4096");
   if (t->shade_lanes > 32) return fail(h, RG_INVALID_ARG, "rg_tuning: shade_lanes must be at most 32");
+  if (t->reserved) return fail(h, RG_INVALID_ARG, "rg_tuning: reserved field must be 0");
   if (t->shared_stack != 0 && t->shared_stack != RG_SHARED_STACK_NONE && t->shared_stack != 4 && t->shared_stack != 8 &&
       t->shared_stack != 16)
     return fail(h, RG_INVALID_ARG, "rg_tuning: shared_stack must be 0, RG_SHARED_STACK_NONE, 4, 8 or 16");
@@ -1055,6 +1056,7 @@ rg_status rg_set_tuning(rg_handle h, const rg_tuning* t) {
   h->stack_limit = t->stack_limit;
   h->march_budget = t->march_budget;
   h->shade_lanes = t->shade_lanes;
+  h->tail_paths = t->tail_paths;
   apply_features(h);
   return RG_OK;
 }
@@ -1071,6 +1073,7 @@ rg_status rg_get_tuning(rg_handle h, rg_tuning* out) {
   out->stack_limit = h->gs.stack_limit;
   out->march_budget = h->march_budget ? h->march_budget : kMarchBudgetDefault;
   out->shade_lanes = h->shade_lanes ? h->shade_lanes : kShadeLanesDefault;
+  out->tail_paths = h->tail_paths ? h->tail_paths : kTailPathsDefault;
   return RG_OK;
 }
 

@@ -118,6 +118,7 @@ struct rg_renderer {
   uint32_t stack_limit = 0;   // traversal stack entries a ray may use (0: kStackSize)
   uint32_t march_budget = 0;  // SDF evaluations per lane between refills in the march stages (0: kMarchBudgetDefault)
   uint32_t shade_lanes = 0;   // ready lanes before a persistent wavefront warp finishes them (0: kShadeLanesDefault)
+  uint32_t tail_paths = 0;    // fused bounce: queues of at most this many paths run to their ends (0: kTailPathsDefault)
   uint32_t range_first = 0;   // rg_set_sample_range: the frame's first sample
   uint32_t range_count = 0;   //   and its number of samples (0: whole frames)
   uint32_t kinds = 0;         // F_* primitive-kind bits of the scene's kernel variant
@@ -161,6 +162,9 @@ constexpr uint32_t kShadeLanesDefault = 16;
 // The same for the batched wavefront's bounce kernel: the 64-scene batch
 // measured 1917 Msamples/s at 1, 2282 at 16 and 2331 at 24.
 constexpr uint32_t kBatchShadeLanesDefault = 24;
+// A fused bounce whose queue holds at most this many paths runs them to their
+// ends in that launch (rg_tuning.tail_paths).
+constexpr uint32_t kTailPathsDefault = 65536;
 // Default path slots per wave (at most about 14.5 GB of path state at 108
 // bytes per slot; clamped to the frame). Every wave pays each bounce's tail,
 // the few longest paths (a long march, a deep traversal) that hold the stage

@@ -56,11 +56,18 @@ __global__ void __launch_bounds__(kWfBlock) k_generate(FrameParams fp, PathState
 // until `shade_lanes` of them (or every live lane) are ready and then shade
 // together: shading is long code, and run for the one or two lanes that finish
 // in a given step it cost more than the wait.
+// A bounce whose queue holds at most `tail_paths` paths (the long tail of deep
+// scenes, where a few paths keep bouncing) runs each of them to its end in
+// this launch instead of queueing it for the next: every bounce launch costs
+// the latency of a path's whole dependent chain through L2, while within one
+// launch the later bounces find the tree in L1. The later launches then find
+// their queues empty.
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
-                                                     int budget, int shade_lanes) {
+                                                     int budget, int shade_lanes, uint32_t tail_paths) {
   const uint32_t n = clamp_count(s.counts[cur], wp, fp.err);
   if (warp_unneeded(n)) return;
+  const bool tail = n <= tail_paths;
   const int nxt = cur ^ 1;
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
@@ -108,12 +115,28 @@ __global__ void __launch_bounds__(kWfBlock) k_bounce(GpuScene sc, FrameParams fp
     if (finish_now(done, live, shade_lanes)) {
       HitRec h;
       const bool hit = finish_hit<F, COUNT>(sc, r, 1e-3f, 3.402823466e38f, t, h, cnt);
+      bool go_on = false;
       if (shade_path<F, COUNT>(sc, fp, s, p, pix, smp, depth, r, beta, hit, h)) {
-        uint32_t slot = warp_append(s.counts + nxt, true);
-        if (slot < wp.n_paths) s.active[nxt][slot] = p;
-        else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+        if (tail) {
+          go_on = true;
+        } else {
+          uint32_t slot = warp_append(s.counts + nxt, true);
+          if (slot < wp.n_paths) s.active[nxt][slot] = p;
+          else atomicOr(fp.err, ERR_QUEUE_OVERFLOW);
+        }
       }
-      has = false;
+      if (go_on) {  // the path's next segment, from the record shade_path just wrote
+        const float4 r0 = s.rec[3 * (size_t)p], r1 = s.rec[3 * (size_t)p + 1], r2 = s.rec[3 * (size_t)p + 2];
+        depth = __float_as_uint(r0.w);
+        r.o = v3(r0.x, r0.y, r0.z);
+        r.d = v3(r1.x, r1.y, r1.z);
+        r.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));
+        beta = C3f{r2.x, r2.y, r2.z};
+        trav_init<F>(t, sc, r, 3.402823466e38f);
+        ++queries;
+      } else {
+        has = false;
+      }
       done = false;
     }
   }
@@ -494,6 +517,7 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
   const bool sorted = effective_sort(h);
   const int budget = (int)effective_budget(h);
   const int shade_lanes = (int)(h->shade_lanes ? h->shade_lanes : kShadeLanesDefault);
+  const uint32_t tail_paths = h->tail_paths ? h->tail_paths : kTailPathsDefault;
   const int grid = sm_count(h->device) * 8;
   // The persistent traversal kernels run as many blocks as are resident at
   // once, each with its threads' shared stack entries.
@@ -555,8 +579,10 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
         k_shade<F><<<grid, kWfBlock, 0, st>>>(h->gs, fp, s, wp, cur);
       } else {
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
-        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, shade_lanes);
-        else k_bounce<F, false><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, shade_lanes);
+        if (counters) k_bounce<F, true><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, shade_lanes,
+                                                                         tail_paths);
+        else k_bounce<F, false><<<bounce_grid, kWfBlock, smem, st>>>(h->gs, fp, s, wp, cur, budget, shade_lanes,
+                                                                     tail_paths);
         if (timed && (e = stage_mark(h)) != cudaSuccess) return e;
       }
       cur ^= 1;

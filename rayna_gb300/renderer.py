@@ -231,7 +231,7 @@ class Renderer:
     def set_tuning(self, wave_paths: int | None = None, sort_materials: bool | None = None,
                    bvh_width: int | None = None, fetch_budget: int | None = None, shared_stack: int | None = None,
                    block: int | None = None, stack_limit: int | None = None, march_budget: int | None = None,
-                   shade_lanes: int | None = None):
+                   shade_lanes: int | None = None, tail_paths: int | None = None):
         """Launch knobs (rg_tuning); None leaves a knob as it is. wave_paths:
         wavefront path slots per wave (0 = library default); sort_materials:
         wavefront shading in material-kind order (True) or one fused bounce
@@ -244,7 +244,9 @@ class Renderer:
         capping the traversal stack a ray may use (0 = all 64); march_budget:
         SDF evaluations per lane between refills in the material-sorted
         wavefront's march stages (0 = 16); shade_lanes: ready lanes a warp
-        of a persistent wavefront kernel finishes together (1-32, 0 = 16)."""
+        of a persistent wavefront kernel finishes together (1-32, 0 = 16);
+        tail_paths: a fused bounce whose queue holds at most this many paths
+        runs them to their ends in that launch (0 = 65536, 1 = off)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
         # the resolved defaults come back from rg_get_tuning; hand the requested knobs back
@@ -267,6 +269,8 @@ class Renderer:
             t.march_budget = int(march_budget)
         if shade_lanes is not None:
             t.shade_lanes = int(shade_lanes)
+        if tail_paths is not None:
+            t.tail_paths = int(tail_paths)
         self._check(self._lib.rg_set_tuning(self._h, C.byref(t)))
         self._stack_knobs = (t.shared_stack, t.block, t.stack_limit)
 
@@ -278,7 +282,7 @@ class Renderer:
                 "fetch_budget": t.fetch_budget,
                 "shared_stack": -1 if t.shared_stack == A.RG_SHARED_STACK_NONE else t.shared_stack,
                 "block": t.block, "stack_limit": t.stack_limit, "march_budget": t.march_budget,
-                "shade_lanes": t.shade_lanes}
+                "shade_lanes": t.shade_lanes, "tail_paths": t.tail_paths}
 
     def set_sample_range(self, first: int, count: int):
         """Frames trace samples [first, first + count) of each pixel's

@@ -278,6 +278,8 @@ pub struct rg_tuning {
     pub stack_limit: u32,
     pub march_budget: u32,
     pub shade_lanes: u32,
+    pub tail_paths: u32,
+    pub reserved: u32,
 }
 
 #[repr(C)]

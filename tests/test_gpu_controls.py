@@ -46,7 +46,8 @@ def test_stack_placement_and_block_do_not_change_images(case):
     for form, knobs in [("megakernel", dict(shared_stack=sh, block=b)) for sh in (-1, 4, 8, 16) for b in (64, 128, 256)] + \
                        [("wavefront", dict(shared_stack=sh, sort_materials=so)) for sh in (-1, 8, 16) for so in (False, True)] + \
                        [("wavefront", dict(shared_stack=8, sort_materials=so, shade_lanes=sl))
-                        for so in (False, True) for sl in (1, 7, 32)]:
+                        for so in (False, True) for sl in (1, 7, 32)] + \
+                       [("wavefront", dict(shared_stack=8, sort_materials=False, tail_paths=tp)) for tp in (1, 100, 1 << 30)]:
         with Renderer.new_from(scene, cam, opts, 0, form=form) as r:
             r.set_tuning(**knobs)
             t = r.tuning()
@@ -70,7 +71,7 @@ def test_tuning_rejects_unknown_stack_and_block_values():
             assert e.value.status == A.RG_INVALID_ARG
         # defaults resolve: 8 shared entries for triangle-only scenes, none otherwise
         assert r.tuning()["shared_stack"] == -1 and r.tuning()["block"] == 128 and r.tuning()["stack_limit"] == 64
-        assert r.tuning()["shade_lanes"] == 16
+        assert r.tuning()["shade_lanes"] == 16 and r.tuning()["tail_paths"] == 65536
 
 
 @pytest.mark.parametrize("form,width", [("megakernel", 2), ("megakernel", 8), ("wavefront", 2), ("wavefront", 8)])
