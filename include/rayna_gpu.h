@@ -407,7 +407,7 @@ typedef struct rg_tuning {
                                  stage) together, once at least this many of its lanes are ready or all of its live
                                  lanes are (1-32; 1 = each path as soon as it is ready); 0 = 16 */
     uint32_t tail_paths;      /* fused wavefront: a bounce whose queue holds at most this many paths runs each of them
-                                 to its end in that launch (the tail of deep scenes); 0 = 65536, 1 = never in effect */
+                                 to its end in that launch (the tail of deep scenes); 0 = 2^22, 1 = never in effect */
     uint32_t reserved;        /* must be 0 */
 } rg_tuning;
 

@@ -41,8 +41,10 @@ MEGA_BLOCKS = [64, 128, 256]
 MEGA_AXES = [("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS), ("block", MEGA_BLOCKS)]
 MARCH_BUDGETS = [8, 16, 32, 64]
 SHADE_LANES = [1, 8, 16, 24]
+TAIL_PATHS = [1, 1 << 16, 1 << 22, 1 << 30]  # 1: no continuation; 2^30: every path runs to its end in its first launch
 WAVE_AXES = [("sort_materials", [False, True]), ("bvh_width", BVH_WIDTHS), ("shared_stack", SHARED_STACKS),
-             ("fetch_budget", FETCH_BUDGETS), ("shade_lanes", SHADE_LANES), ("wave_paths", WAVE_PATHS)]
+             ("fetch_budget", FETCH_BUDGETS), ("shade_lanes", SHADE_LANES), ("tail_paths", TAIL_PATHS),
+             ("wave_paths", WAVE_PATHS)]
 WAVE_SDF_AXES = WAVE_AXES + [("march_budget", MARCH_BUDGETS)]
 BATCH_SHAPES = ([dict(form="wavefront", wave_paths=w) for w in (1 << 25, 1 << 26, 1 << 27)] +
                 [dict(form="tiles", block=b, blocks_per_sm=0, rounds_per_item=r) for b in (64, 128, 256) for r in (1, 4, 16)])
@@ -133,7 +135,7 @@ class Tuner:
         with Renderer.new_from(scene, camera, opts, 0, form="wavefront", **renderer_kw) as r:
             d = r.tuning()
             start = {k: d[k] for k in ("sort_materials", "bvh_width", "shared_stack", "fetch_budget", "shade_lanes",
-                                       "wave_paths")}
+                                       "tail_paths", "wave_paths")}
             axes = WAVE_AXES
             if flat.desc.n_sdfs:  # the march stages' refill budget
                 start["march_budget"] = d["march_budget"]

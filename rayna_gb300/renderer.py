@@ -246,7 +246,7 @@ class Renderer:
         wavefront's march stages (0 = 16); shade_lanes: ready lanes a warp
         of a persistent wavefront kernel finishes together (1-32, 0 = 16);
         tail_paths: a fused bounce whose queue holds at most this many paths
-        runs them to their ends in that launch (0 = 65536, 1 = off)."""
+        runs them to their ends in that launch (0 = 2^22, 1 = off)."""
         t = A.rg_tuning()
         self._check(self._lib.rg_get_tuning(self._h, C.byref(t)))
         # the resolved defaults come back from rg_get_tuning; hand the requested knobs back

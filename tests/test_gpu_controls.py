@@ -71,7 +71,7 @@ def test_tuning_rejects_unknown_stack_and_block_values():
             assert e.value.status == A.RG_INVALID_ARG
         # defaults resolve: 8 shared entries for triangle-only scenes, none otherwise
         assert r.tuning()["shared_stack"] == -1 and r.tuning()["block"] == 128 and r.tuning()["stack_limit"] == 64
-        assert r.tuning()["shade_lanes"] == 16 and r.tuning()["tail_paths"] == 65536
+        assert r.tuning()["shade_lanes"] == 16 and r.tuning()["tail_paths"] == 1 << 22
 
 
 @pytest.mark.parametrize("form,width", [("megakernel", 2), ("megakernel", 8), ("wavefront", 2), ("wavefront", 8)])
