@@ -551,10 +551,14 @@ cudaError_t run_waves(rg_renderer* h, const FrameParams& fp, const PathState& s,
     wp.capacity = (uint32_t)cap;
     uint32_t gen_blocks = (uint32_t)std::min<size_t>((wp.n_paths + kWfBlock - 1) / kWfBlock, (size_t)grid * 4);
     k_generate<<<gen_blocks, kWfBlock, 0, st>>>(fp, s, wp);
+    // A fused wave whose first queue is within the tail threshold runs every
+    // path to its end in the first bounce launch: the later ones would find
+    // empty queues, so they are not launched.
+    const uint32_t last_bounce = !sorted && wp.n_paths <= tail_paths ? 0u : fp.ray_depth;
     // generate, accumulate, and per bounce the bounce kernel or extend + march stages + shade
-    launches += 2 + (fp.ray_depth + 1) * (sorted ? 2 + n_march : 1);
+    launches += 2 + (last_bounce + 1) * (sorted ? 2 + n_march : 1);
     int cur = 0;
-    for (uint32_t d = 0; d <= fp.ray_depth; ++d) {
+    for (uint32_t d = 0; d <= last_bounce; ++d) {
       if ((e = cudaMemsetAsync(s.counts + (cur ^ 1), 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
       if ((e = cudaMemsetAsync(s.counts + kFetchCounter, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
       if (sorted) {
