@@ -844,6 +844,7 @@ rg_status rg_create(const rg_device_opts* opts, rg_handle* out) {
   }
   if ((e = cudaMalloc((void**)&h->d_counters, CNT_N * sizeof(unsigned long long))) != cudaSuccess ||
       (e = cudaMalloc((void**)&h->d_err, sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaMallocHost((void**)&h->h_counters, (CNT_N + 1) * sizeof(unsigned long long))) != cudaSuccess ||
       (e = cudaEventCreate(&h->ev0)) != cudaSuccess || (e = cudaEventCreate(&h->ev1)) != cudaSuccess) {
     rg_destroy(h);
     return cuda_fail(nullptr, e, "rg_create resources");
@@ -870,6 +871,8 @@ rg_status rg_destroy(rg_handle h) {
   if (h->d_adj) cudaFree(h->d_adj);
   dfree(h->d_accum); dfree(h->d_out); dfree(h->d_fmean); dfree(h->d_fvar);
   dfree(h->d_counters); dfree(h->d_err);
+  if (h->h_counters) cudaFreeHost(h->h_counters);
+  if (h->h_image) cudaFreeHost(h->h_image);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (cudaEvent_t ev : h->stage_ev) cudaEventDestroy(ev);
@@ -1160,15 +1163,18 @@ static rg_status render_frame(rg_handle h, uint64_t seed, float* d_out_override,
 rg_status rg_sync_stats(rg_handle h, rg_render_stats* stats) {
   if (!h) return fail(nullptr, RG_INVALID_ARG, "handle is NULL");
   cudaSetDevice(h->device);
+  unsigned long long* c = h->h_counters;
+  RG_CUDA(h, cudaMemcpyAsync(c, h->d_counters, CNT_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream),
+          "read counters");
+  RG_CUDA(h, cudaMemcpyAsync(c + CNT_N, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream),
+          "read error flags");
   RG_CUDA(h, cudaStreamSynchronize(h->stream), "rg_sync_stats");
   rg_render_stats local;
   if (!stats) stats = &local;  // the error bits decide the status either way
   float ms = 0.0f;
   if (cudaEventElapsedTime(&ms, h->ev0, h->ev1) != cudaSuccess) { cudaGetLastError(); ms = 0.0f; }
-  unsigned long long c[CNT_N];
   uint32_t err = 0;
-  RG_CUDA(h, cudaMemcpy(c, h->d_counters, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
-  RG_CUDA(h, cudaMemcpy(&err, h->d_err, sizeof(err), cudaMemcpyDeviceToHost), "read error flags");
+  std::memcpy(&err, c + CNT_N, sizeof(err));
   stats->kernel_ms = ms;
   stats->samples = h->last_samples;
   stats->rays = c[CNT_RAYS];
@@ -1225,11 +1231,18 @@ rg_status rg_render(rg_handle h, uint64_t seed, float* out_rgb, rg_render_stats*
   }
   rg_status st = render_frame(h, seed, nullptr, stats);
   if (st != RG_OK) return st;
-  if (out_rgb)
-    RG_CUDA(h, cudaMemcpyAsync(out_rgb, h->d_out, (size_t)w * hh * 3 * sizeof(float), cudaMemcpyDeviceToHost, h->stream),
-            "copy image");
+  const size_t img_bytes = (size_t)w * hh * 3 * sizeof(float);
+  if (out_rgb && h->h_image_bytes < img_bytes) {
+    if (h->h_image) cudaFreeHost(h->h_image);
+    h->h_image = nullptr;
+    h->h_image_bytes = 0;
+    RG_CUDA(h, cudaMallocHost((void**)&h->h_image, img_bytes), "image staging buffer");
+    h->h_image_bytes = img_bytes;
+  }
+  if (out_rgb) RG_CUDA(h, cudaMemcpyAsync(h->h_image, h->d_out, img_bytes, cudaMemcpyDeviceToHost, h->stream), "copy image");
   rg_render_stats tmp;
-  st = rg_sync_stats(h, stats ? stats : &tmp);
+  st = rg_sync_stats(h, stats ? stats : &tmp);  // synchronises the stream: the image has arrived
+  if (out_rgb) std::memcpy(out_rgb, h->h_image, img_bytes);
   if (st != RG_OK) return st;
   if (stats) stats->duration_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return RG_OK;
