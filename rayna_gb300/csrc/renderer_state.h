@@ -106,13 +106,9 @@ struct rg_renderer {
 
   unsigned long long* d_counters = nullptr;
   uint32_t* d_err = nullptr;
-  // Page-locked host copies: the frame's counters and error word (read back
-  // with one asynchronous copy each and a single stream synchronisation), and
-  // the image rg_render hands back (copied from the device at full rate, then
-  // into the caller's buffer).
+  // Page-locked host copy of the frame's counters and error word, read back
+  // with one asynchronous copy each and a single stream synchronisation.
   unsigned long long* h_counters = nullptr;  // CNT_N counters, then the error word
-  float* h_image = nullptr;
-  size_t h_image_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
   rg::WavefrontState wf;
