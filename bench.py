@@ -427,10 +427,13 @@ def time_form(name, scene, cam, opts, form, steps, warmup, stream, flush, rank, 
         r.clear_accumulation()
         for _ in range(2):
             r.render()
+        # short frames are timed over about a quarter of a second of frames, so
+        # one host hiccup does not decide the mean
+        e2e_frames = max(steps, min(400, int(0.25 / max(dev_s / steps, 1e-6))))
         e0 = time.perf_counter()
-        for _ in range(steps):
+        for _ in range(e2e_frames):
             out = r.render()
-        e2e_s = time.perf_counter() - e0
+        e2e_s = (time.perf_counter() - e0) * steps / e2e_frames
         assert out.stats.error_flags == 0, out.stats.error_flags
     e2e_s = rank_max(e2e_s, dist, "cuda")
     r.close()
