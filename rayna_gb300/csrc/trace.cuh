@@ -274,80 +274,6 @@ __device__ __forceinline__ bool volume_t(const GpuPrim& p, uint32_t kind, uint32
 // ---------------------------------------------------------------------------
 constexpr float kBulbInner = 1.2f, kBulbOuter = 1.5f;
 
-// The power-8 Mandelbulb distance estimate in resumable form: bulb_begin,
-// bulb_step until it returns true, bulb_end. sdf_eval runs it in one call;
-// the wavefront's march stage advances the lanes of a warp through their
-// escape loops independently. z -> z^8 + c in spherical coordinates without
-// transcendentals or per-iteration normalisation of the polar angle: with
-// w = z + i rho (|w| = r, arg w = t) three complex squarings give
-// w^8 = r^8 (cos 8t + i sin 8t); the azimuth's unit complex number
-// (x + i y) / rho, squared three times, gives cos 8p + i sin 8p. One
-// division and two square roots per iteration.
-struct BulbDe {
-  V3 z0, z;
-  float dr, rr;
-  int i;  // iterations done
-};
-
-// Starts the estimate at x. Returns false when x lies outside kBulbOuter;
-// `d` is then the distance (to the enclosing sphere of radius kBulbInner, a
-// lower bound).
-__device__ __forceinline__ bool bulb_begin(const GpuSdf& s, V3 x, BulbDe& b, float& d) {
-  const V3 q = x - v3(s.cx, s.cy, s.cz);
-  const float sc = s.p2;
-  // q / scale; for a power-of-two scale the product with its reciprocal is
-  // the same correctly rounded quotient, without three divisions
-  const V3 z0 = s.inv_scale != 0.0f
-                    ? v3(__fmul_rn(q.x, s.inv_scale), __fmul_rn(q.y, s.inv_scale), __fmul_rn(q.z, s.inv_scale))
-                    : v3(q.x / sc, q.y / sc, q.z / sc);
-  const float rq = length3(z0);
-  if (rq > kBulbOuter) {
-    d = __fmul_rn(rq - kBulbInner, sc);
-    return false;
-  }
-  b.z0 = z0;
-  b.z = z0;
-  b.dr = 1.0f;
-  b.rr = 0.0f;
-  b.i = 0;
-  return true;
-}
-
-// One escape-loop iteration (b.i < iters); returns true once the estimate is
-// complete (|z| > 2, or `iters` iterations done).
-__device__ __forceinline__ bool bulb_step(BulbDe& b, int iters, unsigned long long* counted) {
-  if (counted) ++*counted;
-  const V3 z = b.z;
-  const float rho2 = __fmaf_rn(z.x, z.x, __fmul_rn(z.y, z.y));
-  const float r2 = __fmaf_rn(z.z, z.z, rho2);
-  b.rr = __fsqrt_rn(r2);
-  if (b.rr > 2.0f) return true;
-  const float rho = __fsqrt_rn(rho2);
-  float wa = z.z, wb = rho, cp = 1.0f, sp = 0.0f;
-  if (rho > 0.0f) {
-    const float inv = __fdiv_rn(1.0f, rho);
-    cp = __fmul_rn(z.x, inv);
-    sp = __fmul_rn(z.y, inv);
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    float a2 = __fmaf_rn(wa, wa, -__fmul_rn(wb, wb));
-    wb = __fmul_rn(2.0f * wa, wb);
-    wa = a2;
-    float d2 = __fmaf_rn(cp, cp, -__fmul_rn(sp, sp));
-    sp = __fmul_rn(2.0f * cp, sp);
-    cp = d2;
-  }
-  const float r4 = __fmul_rn(r2, r2);
-  b.dr = __fmaf_rn(__fmul_rn(__fmul_rn(__fmul_rn(r4, r2), b.rr), 8.0f), b.dr, 1.0f);
-  b.z = v3(__fmaf_rn(wb, cp, b.z0.x), __fmaf_rn(wb, sp, b.z0.y), __fadd_rn(wa, b.z0.z));
-  return ++b.i >= iters;
-}
-
-__device__ __forceinline__ float bulb_end(const GpuSdf& s, const BulbDe& b) {
-  return __fmul_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, ln_f32(b.rr)), b.rr), b.dr), s.p2);
-}
-
 // `iter_count`, when given, counts the Mandelbulb's escape-loop iterations
 // (work counters). Every multiply-add here is written out (explicit fma, and
 // __fmul_rn where a product must not fuse into the caller's subtraction, as in
@@ -365,25 +291,50 @@ __device__ __forceinline__ float sdf_eval(const GpuSdf& s, V3 x, unsigned long l
   // with the running derivative dr; outside kBulbOuter the distance to the
   // enclosing sphere of radius kBulbInner is used (a lower bound).
   unsigned long long* counted = iter_count;
-  float power = s.p0;
-  int iters = (int)s.p1;
-  if (power == 8.0f) {
-    BulbDe b;
-    float d;
-    if (!bulb_begin(s, x, b, d)) return d;
-    if (iters > 0)
-      while (!bulb_step(b, iters, counted)) {
-      }
-    return bulb_end(s, b);
-  }
   float sc = s.p2;
+  // q / scale; for a power-of-two scale the product with its reciprocal is
+  // the same correctly rounded quotient, without three divisions
   V3 z0 = s.inv_scale != 0.0f ? v3(__fmul_rn(q.x, s.inv_scale), __fmul_rn(q.y, s.inv_scale), __fmul_rn(q.z, s.inv_scale))
                               : v3(q.x / sc, q.y / sc, q.z / sc);
   float rq = length3(z0);
   if (rq > kBulbOuter) return __fmul_rn(rq - kBulbInner, sc);
+  float power = s.p0;
+  int iters = (int)s.p1;
   V3 z = z0;
   float dr = 1.0f, rr = 0.0f;
-  {
+  if (power == 8.0f) {
+    // z^8 without transcendentals or per-iteration normalisation of the polar
+    // angle: with w = z + i rho (|w| = r, arg w = t) three complex squarings
+    // give w^8 = r^8 (cos 8t + i sin 8t); the azimuth's unit complex number
+    // (x + i y) / rho, squared three times, gives cos 8p + i sin 8p. One
+    // division and two square roots per iteration.
+    for (int i = 0; i < iters; ++i) {
+      if (counted) ++*counted;
+      float rho2 = __fmaf_rn(z.x, z.x, __fmul_rn(z.y, z.y));
+      float r2 = __fmaf_rn(z.z, z.z, rho2);
+      rr = __fsqrt_rn(r2);
+      if (rr > 2.0f) break;
+      float rho = __fsqrt_rn(rho2);
+      float wa = z.z, wb = rho, cp = 1.0f, sp = 0.0f;
+      if (rho > 0.0f) {
+        const float inv = __fdiv_rn(1.0f, rho);
+        cp = __fmul_rn(z.x, inv);
+        sp = __fmul_rn(z.y, inv);
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float a2 = __fmaf_rn(wa, wa, -__fmul_rn(wb, wb));
+        wb = __fmul_rn(2.0f * wa, wb);
+        wa = a2;
+        float d2 = __fmaf_rn(cp, cp, -__fmul_rn(sp, sp));
+        sp = __fmul_rn(2.0f * cp, sp);
+        cp = d2;
+      }
+      float r4 = __fmul_rn(r2, r2);
+      dr = __fmaf_rn(__fmul_rn(__fmul_rn(__fmul_rn(r4, r2), rr), 8.0f), dr, 1.0f);
+      z = v3(__fmaf_rn(wb, cp, z0.x), __fmaf_rn(wb, sp, z0.y), __fadd_rn(wa, z0.z));
+    }
+  } else {
     for (int i = 0; i < iters; ++i) {
       rr = length3(z);
       if (rr > 2.0f) break;
@@ -530,9 +481,12 @@ __device__ __forceinline__ void sdf_march_begin(const Ray& r, float start, SdfMa
   m.d = 0.0f;
 }
 
-// The march step after its distance evaluation `d` at m.point.
-__device__ __forceinline__ int sdf_march_advance(const GpuSdf& s, const Ray& r, float start, float end, float beat,
-                                                 bool beat_inclusive, SdfMarch& m, float d) {
+template <bool COUNT>
+__device__ __forceinline__ int sdf_march_step(const GpuSdf& s, const Ray& r, float start, float end, float beat,
+                                              bool beat_inclusive, SdfMarch& m, unsigned long long& steps,
+                                              unsigned long long& iters) {
+  const float d = sdf_eval(s, m.point, COUNT ? &iters : nullptr);
+  if (COUNT) ++steps;
   m.total = m.total + fabsf(d);
   m.point = at3(r.o, r.d, m.total);
   m.d = d;
@@ -544,15 +498,6 @@ __device__ __forceinline__ int sdf_march_advance(const GpuSdf& s, const Ray& r, 
   if (dot3(q, q) > s.bound_radius * s.bound_radius && dot3(q, r.d) > 0.0f) return kMarchMiss;
   ++m.i;
   return kMarchOn;
-}
-
-template <bool COUNT>
-__device__ __forceinline__ int sdf_march_step(const GpuSdf& s, const Ray& r, float start, float end, float beat,
-                                              bool beat_inclusive, SdfMarch& m, unsigned long long& steps,
-                                              unsigned long long& iters) {
-  const float d = sdf_eval(s, m.point, COUNT ? &iters : nullptr);
-  if (COUNT) ++steps;
-  return sdf_march_advance(s, r, start, end, beat, beat_inclusive, m, d);
 }
 
 // The hit record at a step that returned kMarchHit: the normal by central

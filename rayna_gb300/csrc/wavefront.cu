@@ -28,13 +28,6 @@
 #include "renderer_state.h"
 #include "wavefront.cuh"
 
-// RG_MARCH_TICKS=0 at build time marches the Mandelbulb like the other SDFs
-// (whole distance evaluations per step, the warp waiting for its longest
-// escape loop).
-#ifndef RG_MARCH_TICKS
-#define RG_MARCH_TICKS 1
-#endif
-
 namespace rg {
 
 namespace {
@@ -388,8 +381,6 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
   uint32_t* next = s.counts + kFetchCounter;
   const uint32_t lane = threadIdx.x & 31u;
   const GpuSdf f = sc.sdfs[k];
-  const bool bulb8 = RG_MARCH_TICKS && f.kind == RG_SDF_MANDELBULB && f.p0 == 8.0f;
-  const int bulb_iters = (int)f.p1;
   const float start = 1e-3f, end = 3.402823466e38f;
   Counters cnt;
   bool has = false, done = false, drained = false;
@@ -431,39 +422,7 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
     }
     const unsigned live = __ballot_sync(0xffffffffu, has);
     if (!live) break;  // drained, and nothing left to march
-    if (bulb8) {
-      // The power-8 Mandelbulb: each lane advances through its own escape
-      // loop one iteration at a time, and the lanes whose evaluation is
-      // complete finish their march steps together (once `shade_lanes` of
-      // them, or all the warp's marching lanes, are ready) and start the
-      // next evaluation, so lanes with short escape loops do not idle while
-      // the warp's longest one runs. Each lane's arithmetic is sdf_eval's.
-      const bool marching = has && !done;
-      if (marching) st = kMarchOn;
-      int e = 0;
-      bool fresh = true, ready = false, de_in = false;
-      float de_out = 0.0f;
-      BulbDe de;
-      for (;;) {
-        const bool act = marching && st == kMarchOn && e < budget;
-        const unsigned actm = __ballot_sync(0xffffffffu, act);
-        if (!actm) break;
-        if (act && fresh) {  // sdf_eval's order: outside kBulbOuter the distance is known at once
-          de_in = bulb_begin(f, m.point, de, de_out);
-          ready = !de_in || bulb_iters <= 0;
-          fresh = false;
-        }
-        if (act && !ready) ready = bulb_step(de, bulb_iters, COUNT ? &cnt.sdf_iters : nullptr);
-        if (finish_now(act && ready, actm, shade_lanes)) {
-          if (COUNT) ++cnt.sdf_steps;
-          st = sdf_march_advance(f, r, start, end, any ? best : end, !any, m, de_in ? bulb_end(f, de) : de_out);
-          ++e;
-          fresh = true;
-          ready = false;
-        }
-      }
-      if (marching) done = st != kMarchOn;
-    } else if (has && !done) {
+    if (has && !done) {
       st = kMarchOn;
       for (int e = 0; e < budget && st == kMarchOn; ++e)
         st = sdf_march_step<COUNT>(f, r, start, end, any ? best : end, !any, m, cnt.sdf_steps, cnt.sdf_iters);
