@@ -48,6 +48,31 @@ def test_backward_matches_fp64_cpu_adjoint():
     print(f"albedo rel err {np.linalg.norm(ga - ra) / norm:.2e}, density {gd:.5g} vs {rd:.5g}")
 
 
+def test_backward_general_kernel_variant_matches_fp64_cpu_adjoint():
+    """Scenes of spheres with media replay in a kernel variant of their own;
+    a scene with another primitive kind (here an axis box) takes the general
+    variant, whose gradients must match the FP64 CPU adjoint as well."""
+    from rayna_gb300.scene import AxisBoxMesh, LambertianMaterial, SimpleObject
+    scene, gt, cam, opts = small_case()
+    for s in (scene, gt):
+        s.objects.insert(1, SimpleObject(AxisBoxMesh((-2.5, 0.0, -1.0), (-1.5, 1.2, 0.0)),
+                                         LambertianMaterial((0.6, 0.4, 0.3))))
+    with Renderer.new_from(gt, cam, opts, 0) as r:
+        target = r.frame(seed=71)
+    seed = 515
+    with Renderer.new_from(scene, cam, opts, 0) as r:
+        g = r.backward(seed, target=target)
+    ref = ob.backward(flatten(scene), cam, opts, seed, target=target, policy=ob.POLICY_REF_F64)
+    assert abs(g["loss"] - ref["loss"]) <= 2e-3 * ref["loss"]
+    ga, ra = g["albedo"].astype(np.float64), ref["albedo"]
+    norm = np.linalg.norm(ra)
+    assert norm > 0
+    assert np.linalg.norm(ga - ra) <= 0.01 * norm, np.linalg.norm(ga - ra) / norm
+    gd, rd = float(g["density"][0]), float(ref["density"][0])
+    assert abs(gd - rd) <= 0.02 * abs(rd) + 1e-6, (gd, rd)
+    print(f"general variant: albedo rel err {np.linalg.norm(ga - ra) / norm:.2e}, density {gd:.5g} vs {rd:.5g}")
+
+
 def test_backward_albedo_matches_finite_differences():
     scene, gt, cam, opts = small_case()
     with Renderer.new_from(gt, cam, opts, 0) as r:
