@@ -669,11 +669,6 @@ __device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t sel) {
   return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | sel));
 }
 
-// RG_PREFETCH_FAR=0 at build time leaves the far children unprefetched.
-#ifndef RG_PREFETCH_FAR
-#define RG_PREFETCH_FAR 1
-#endif
-
 constexpr int kTravStack = 64;
 static_assert(kTravStack >= kStackSize && kTravStack >= kWideMaxDepth + 1, "traversal stack too small");
 
@@ -797,14 +792,6 @@ __device__ __forceinline__ bool run_binary(Traversal& t, Stack& stack, const Gpu
       if (h0 && h1) {
         bool swap = tn1 < tn0;
         t.ref = swap ? r1 : r0;
-        if (RG_PREFETCH_FAR) {
-          // The far child waits on the stack while the near subtree is
-          // walked: ask L2 for its node pair (or its leaf's first primitive)
-          // now, so that the pop does not wait on DRAM.
-          const int far = swap ? r0 : r1;
-          const void* fa = far >= 0 ? (const void*)(sc.nodes + far) : (const void*)(sc.prims + ((~far) >> 3));
-          asm volatile("{\n\t.reg .u64 g;\n\tcvta.to.global.u64 g, %0;\n\tprefetch.global.L2 [g];\n\t}" ::"l"(fa));
-        }
         if (t.sp < (int)sc.stack_limit) {
           stack.set(t.sp, make_uint2((uint32_t)(swap ? r0 : r1), __float_as_uint(swap ? tn0 : tn1)));
           ++t.sp;
