@@ -357,21 +357,19 @@ __device__ __forceinline__ void pass_on(const GpuScene& sc, const FrameParams& f
 }
 
 // Material-sorted variant with raymarched SDFs, stage 1b: the march of SDF k
-// (the unbounded list's k-th object) for every path of its march queue (the
+// (the unbounded list's k-th object) for every path of its march queue: the
 // paths whose segment, after the tree and the SDFs before k, can reach its
-// bound sphere; with one march queue for every stage, all paths that can
-// reach some SDF). After its march a path goes on to the queue of the next
-// SDF it can reach, or is finished (infinite planes, material-kind queue). It replaces the path's
-// hit when strictly closer (or when nothing was hit), as ObjectList's loop
-// over unbounded objects does (object/list.rs:112-129). Persistent with
-// dynamic fetch: every lane marches the same function, `budget` evaluations
-// at a time, and lanes whose march has ended take the next path (one atomic
-// per warp), so a long march does not hold idle lanes. Paths whose segment
-// cannot reach the function's bound sphere end at once. A warp finishes its
-// ended marches together (the hit normal, six distance evaluations; the last
-// stage's planes and queue append) once `shade_lanes` of them, or all of its
-// live lanes, have ended. The last stage also tests the infinite planes and
-// appends each path to its material kind's queue.
+// bound sphere (with one march queue for every stage: all paths that can
+// reach some SDF). A hit replaces the path's hit when strictly closer (or
+// when nothing was hit), as ObjectList's loop over unbounded objects does
+// (object/list.rs:112-129); then the path goes on to the queue of the next SDF
+// it can reach, or is finished (infinite planes, material-kind queue).
+// Persistent with dynamic fetch: every lane marches the same function,
+// `budget` evaluations at a time, and lanes whose march has ended take the
+// next path (one atomic per warp), so a long march does not hold idle lanes.
+// A warp finishes its ended marches together (the hit normal, six distance
+// evaluations; passing the path on) once `shade_lanes` of them, or all of its
+// live lanes, have ended.
 template <uint32_t F, bool COUNT>
 __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp, PathState s, WaveParams wp, int cur,
                                                     uint32_t k, int n_march, int budget, int shade_lanes) {
@@ -392,9 +390,9 @@ __global__ void __launch_bounds__(kWfBlock) k_march(GpuScene sc, FrameParams fp,
   SdfMarch m;
   for (;;) {
     // Refill idle lanes until every lane has a march or the queue is drained:
-    // most paths end at fetch (out of reach of the bound sphere), and a lane
-    // that took one must not wait out the marching lanes' budget before its
-    // next fetch.
+    // a path whose segment no longer reaches the bound sphere (an earlier
+    // SDF's hit shortened it) ends at fetch, and its lane must not wait out
+    // the marching lanes' budget before its next fetch.
     while (!drained) {
       const unsigned idle = __ballot_sync(0xffffffffu, !has);
       if (!idle) break;
