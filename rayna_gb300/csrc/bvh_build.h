@@ -16,7 +16,7 @@ struct BvhBuildResult {
   int max_depth = 0;
 };
 
-// Binned SAH (16 bins over centroid bounds on each axis, cost N_L*A_L +
+// Binned SAH (`bins` bins over centroid bounds on each axis, cost N_L*A_L +
 // N_R*A_R), leaves of at most `max_leaf` primitives. Below depth
 // `sah_depth_limit` the split switches to the centroid median of the widest
 // axis, which bounds the depth by sah_depth_limit + log2(n).
