@@ -13,6 +13,14 @@ def test_keys_bucket_by_size():
     assert autotune.batch_key(64, 2_700_000, 52_000_000, 2_000_000_000).startswith("batch:n6:")
 
 
+def test_wavefront_axes_cover_the_launch_knobs():
+    axes = dict(autotune.WAVE_AXES)
+    assert axes["shade_lanes"] == autotune.SHADE_LANES and 16 in autotune.SHADE_LANES
+    assert axes["tail_paths"] == autotune.TAIL_PATHS and 1 in autotune.TAIL_PATHS  # 1: no continuation
+    assert axes["wave_paths"][-1] == 1 << 27
+    assert dict(autotune.WAVE_SDF_AXES)["march_budget"] == autotune.MARCH_BUDGETS
+
+
 def test_default_cache_is_outside_the_package():
     import os
     pkg = os.path.dirname(os.path.abspath(autotune.__file__))
