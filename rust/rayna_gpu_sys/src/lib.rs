@@ -1,4 +1,4 @@
-//! Raw bindings of `include/rayna_gpu.h` (C ABI version 7). Not compiled here:
+//! Raw bindings of `include/rayna_gpu.h` (C ABI version 8). Not compiled here:
 //! this image has no Rust toolchain. Layouts follow the header field for
 //! field; every function returns an `rg_status` (0 = `RG_OK`).
 #![allow(non_camel_case_types)]
